@@ -1,0 +1,338 @@
+#!/usr/bin/env python
+"""Benchmark: FP64 APGD solve of the 200 000-contact friction problem on one GB300 (time to residual).
+
+Workload (one "step"): DualFrictionProblem::solveWith(ProjectedGradient, r) with the reference's defaults
+(APGD, SOC law, line search 8 / 1.25 / 0.5) at tol 1e-6 with at most 500 iterations, from r = 0, on the
+seeded grid problem (50 000 rigid bodies, 200 000 contacts, W assembled on the GPU). The solve stops at
+the tolerance or after 500 iterations, whichever comes first; the GPU and the CPU oracle run bit-identical
+iterations, so both arms do the same work.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Our arm prints `value` (ms per solve, inputs resident in HBM, CUDA events on the library's stream), `e2e`
+(the C-ABI call with host buffers: upload of W/b/mu/r, solve, download of r), the roofline of the
+persistent solver kernel, FP64 pipe use and the CPU baseline (the oracle on the host cores).
+`--impl reference` times the CPU restatement of the reference (the oracle, OpenMP on all host cores) on the
+same workload. With N > 1 (torchrun) every rank solves its own replica (a single problem does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [os.path.join(REPO, "so-bogus_gb300")]
+
+TOL = 1e-6
+MAX_ITERS = 500
+METRIC = "time-to-residual 1e-6 (ms), FP64 APGD, 200k contacts"
+WORKLOAD = "fp64_apgd_200k_contacts"
+
+
+def config_dict(n, nnzb_full, extra=None):
+    d = {"workload": WORKLOAD, "contacts": n, "bodies": 50_000, "w_blocks_full": nnzb_full,
+         "w_blocks_lower": (nnzb_full + n) // 2, "solver": "APGD (reference defaults), SOC law",
+         "tol": TOL, "max_iters": MAX_ITERS, "start": "r = 0", "generator": "grid, seed 1",
+         "l2": "inputs exceed L2 (W both triangles = %.0f MB > 129 MB)" % (nnzb_full * 76 / 1e6),
+         "parallelism": "replicas (one problem per GPU)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traffic_from_profiles(algorithmic_bytes):
+    """DRAM bytes of the solver launch: the ncu capture of the same kernel on the same problem (a solve capped at
+    20 iterations, committed summary) gives DRAM bytes per algorithmic byte; traffic grows with the passes over
+    W, so the launch's traffic is that ratio times its algorithmic bytes. None when the summary is absent."""
+    p = os.path.join(REPO, "profiles", "pg_persistent_apgd_200k.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_algorithmic_byte:"):
+            try:
+                return float(line.split(":", 1)[1].strip()) * algorithmic_bytes
+            except ValueError:
+                return None
+    return None
+
+
+def make_problem():
+    from bogus_gpu import generator
+
+    return generator.make("c2")
+
+
+# --------------------------------------------------------------------------------------------------------
+def cpu_oracle_solve(d, threads=None):
+    """The oracle (CPU restatement of the reference) on all host cores: returns (ms, residual, iterations)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    if threads:
+        pyoracle.set_num_threads(threads)
+    P = pyoracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    rp, cl, vl = P.assemble()
+    O = pyoracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    t0 = time.perf_counter()
+    res, r, it = O.solve_pg(np.zeros(3 * d.n), variant=3, coulomb=False, tol=TOL, max_iters=MAX_ITERS)
+    ms = (time.perf_counter() - t0) * 1e3
+    return ms, res, it, pyoracle.num_threads(), (rp, cl, vl)
+
+
+def run_reference(args, rank, world):
+    if world > 1 and rank != 0:
+        return
+    d = make_problem()
+    times = []
+    res = it = cores = None
+    nnz_full = 0
+    for step in range(args.warmup + args.steps):
+        ms, res, it, cores, lower = cpu_oracle_solve(d)
+        nnz_full = 2 * len(lower[1]) - d.n
+        if step >= args.warmup:
+            times.append(ms)
+    v = statistics.mean(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded grid generator)",
+        "config": config_dict(d.n, nnz_full or 0, {"iterations": it, "final_residual": res}),
+        "cpu_baseline": {"value": v, "unit": "ms", "cores": cores, "kind": "port",
+                         "sample": f"full solve ({it} APGD iterations) of the same problem, per step"},
+        "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import bogus_gpu
+
+    torch.cuda.set_device(local_rank)
+    dev = local_rank
+    d = make_problem()
+    D = bogus_gpu.DualFrictionProblem(dev)
+    D.computeFrom(bogus_gpu.PrimalFrictionProblem.from_generated(d))
+    asm = D.solve_stats()
+    n = d.n
+    nnz_full = D.nnzb()
+    pg = bogus_gpu.ProjectedGradient()
+    pg.setTol(TOL)
+    pg.setMaxIters(MAX_ITERS)
+    r = torch.zeros(3 * n, dtype=torch.float64, device=f"cuda:{dev}")
+    stream = torch.cuda.ExternalStream(D.stream(), device=f"cuda:{dev}")
+
+    def step():
+        with torch.cuda.stream(stream):
+            r.zero_()
+        return D.solve_pg_device(pg, r.data_ptr(), staticProblem=True)
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    kernel_ms, bytes_, fmas, iters, res = [], [], [], [], []
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+    for _ in range(args.steps):
+        rr, it = step()
+        st = D.solve_stats()
+        kernel_ms.append(st["device_ms"])
+        bytes_.append(st["algorithmic_bytes"])
+        fmas.append(st["fp64_fma"])
+        iters.append(it)
+        res.append(rr)
+    with torch.cuda.stream(stream):
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ck = clocks.stop()
+    ms_step = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms_step], dtype=torch.float64, device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+
+    # end to end through the C ABI with host buffers: upload W (lower), b, mu and r, solve, download r
+    rp, cl, vl = D.W_lower()
+    vl = np.ascontiguousarray(vl.reshape(-1))
+    e2e_steps = max(1, min(args.steps, 3))
+    h2d = rp.nbytes + cl.nbytes + vl.nbytes + d.b.nbytes + d.mu.nbytes + 3 * n * 8
+    d2h = 3 * n * 8
+    E = bogus_gpu.DualFrictionProblem(dev)
+    rh = np.zeros(3 * n)
+    E.set(rp, cl, vl, d.b, d.mu)  # warm (allocations)
+    E.solveWith(pg, rh)
+    e2e_ms = []
+    for _ in range(e2e_steps):
+        rh = np.zeros(3 * n)
+        t0 = time.perf_counter()
+        E.set(rp, cl, vl, d.b, d.mu)
+        E.solveWith(pg, rh)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    del E
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    kms = statistics.mean(kernel_ms)
+    achieved = statistics.mean(bytes_) / (kms * 1e-3) / 1e9
+    fp64_peak = bogus_gpu.measure_fp64_peak(dev)
+    fp64_ach = 2.0 * statistics.mean(fmas) / (kms * 1e-3) / 1e12
+    traffic = traffic_from_profiles(statistics.mean(bytes_))
+    line = {
+        "metric": METRIC, "value": ms_step, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded grid generator)",
+        "config": config_dict(n, nnz_full, {"iterations": iters[-1], "final_residual": res[-1],
+                                            "assembly_ms": asm["device_ms"]}),
+        "e2e": {"value": statistics.mean(e2e_ms), "unit": "ms", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind, "kernel": "k_pg_persistent",
+                     "algorithmic_bytes_per_launch": statistics.mean(bytes_), "kernel_ms": kms},
+        "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak,
+                 "note": "FMA work of the W passes only; GB300's FP64 rate bounds the FP64 kernels"},
+        "gpu_launches": args.steps,
+        "clocks": ck,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        cms, cres, cit, cores, _ = cpu_oracle_solve(d)
+        line["cpu_baseline"] = {"value": cms, "unit": "ms", "cores": cores, "kind": "port",
+                                "sample": f"one full solve ({cit} iterations, residual {cres:.3e}) of the same problem"}
+        line["cpu_baseline"]["identical_result"] = bool(cit == iters[-1] and cres == res[-1])
+    print(json.dumps(line), flush=True)
+
+
+def run_profile(iters: int) -> None:
+    """One APGD solve of the benchmark problem capped at `iters` iterations (the solver kernel under ncu)."""
+    import bogus_gpu
+
+    d = make_problem()
+    D = bogus_gpu.DualFrictionProblem(0)
+    D.computeFrom(bogus_gpu.PrimalFrictionProblem.from_generated(d))
+    pg = bogus_gpu.ProjectedGradient()
+    pg.setTol(TOL)
+    pg.setMaxIters(iters)
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r)
+    st = D.solve_stats()
+    print(json.dumps({"profile_iters": iters, "residual": res, "stats": st}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", type=int, default=0,
+                    help="run one solve capped at this many iterations and exit (for ncu captures)")
+    args = ap.parse_args()
+    if args.profile:
+        run_profile(args.profile)
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl", device_id=torch.device(f"cuda:{local_rank}"))
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

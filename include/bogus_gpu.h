@@ -1,0 +1,184 @@
+/*
+ * bogus_gpu — C ABI of the GB300 (sm_103a) friction-solve library.
+ *
+ * A drop-in for So-bogus's friction-solve path: 3x3-block sparse products, Delassus assembly
+ * W = H M^-1 H^T, colored block Gauss-Seidel, projected gradient (APGD / SPG / ...) and the
+ * SOCLaw<3> / Coulomb local solver, run by hand-written CUDA kernels on one GPU.
+ *
+ * Conventions (the reference's, Interfaces/FrictionProblem.hpp:127-214):
+ *  - one handle = one dual problem  u = W r + b  on one device; contacts are 3-vectors in the local
+ *    basis (normal first), arrays are contact-major: r[3*i + k];
+ *  - W is given as 3x3-block BSR (row pointers, column indices, row-major blocks of 9 doubles), either
+ *    the symmetric lower triangle (the reference's SparseBlockMatrix<Matrix3d, SYMMETRIC> storage) or
+ *    both triangles;
+ *  - the caller owns every array; r is in/out (warm start and result) as in solveWith();
+ *  - every call returns a bogus_gpu_status; a solve also writes the reference's return value (the
+ *    error function of ConstrainedSolverBase::eval) to *residual;
+ *  - no CPU fallback: without a usable GPU, calls return BOGUS_GPU_NO_DEVICE or BOGUS_GPU_CUDA_ERROR;
+ *  - a handle is not thread-safe; it owns one CUDA stream.
+ */
+#ifndef BOGUS_GPU_H
+#define BOGUS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bogus_gpu_status {
+  BOGUS_GPU_OK = 0,
+  BOGUS_GPU_NOT_CONVERGED = 1, /* iteration budget exhausted; r holds the best iterate */
+  BOGUS_GPU_BAD_INPUT = 2,     /* malformed sizes, indices or options */
+  BOGUS_GPU_NONFINITE = 3,     /* NaN / Inf in the inputs */
+  BOGUS_GPU_CUDA_ERROR = 4,    /* a CUDA call failed (see bogus_gpu_last_error) */
+  BOGUS_GPU_TIMEOUT = 5,       /* a device-side wait ran out (the kernel stopped itself) */
+  BOGUS_GPU_NO_DEVICE = 6,     /* no CUDA device / wrong architecture */
+  BOGUS_GPU_NO_PROBLEM = 7     /* solve called before the problem was set */
+} bogus_gpu_status;
+
+/* projected_gradient::Variant (Core/BlockSolvers.fwd.hpp) */
+typedef enum bogus_gpu_pg_variant {
+  BOGUS_GPU_PG_STANDARD = 0,
+  BOGUS_GPU_PG_DESCENT = 1,
+  BOGUS_GPU_PG_CONJUGATED = 2,
+  BOGUS_GPU_PG_APGD = 3,
+  BOGUS_GPU_PG_SPG = 4
+} bogus_gpu_pg_variant;
+
+/* local_soc_solver::Strategy (Extra/SecondOrder.fwd.hpp:33-55) */
+typedef enum bogus_gpu_local_strategy {
+  BOGUS_GPU_LOCAL_PURE_NEWTON = 0,
+  BOGUS_GPU_LOCAL_PURE_ENUMERATIVE = 1,
+  BOGUS_GPU_LOCAL_HYBRID = 2,
+  BOGUS_GPU_LOCAL_REV_HYBRID = 3
+} bogus_gpu_local_strategy;
+
+/* Signal<unsigned, double> listener (Core/Utils/Signal.hpp:25-54, BlockSolverBase::callback()).
+ * Fired on the calling thread, in iteration order, when the solve returns. */
+typedef void (*bogus_gpu_callback)(unsigned iteration, double residual, void* user);
+
+/* ProjectedGradient setters and defaults (Core/BlockSolvers/ProjectedGradient.hpp:61-95,
+ * BlockSolverBase.hpp:38-43, ConstrainedSolverBase.hpp:31). */
+typedef struct bogus_gpu_pg_options {
+  double tol;                     /* 1e-6 */
+  unsigned max_iters;             /* 300 */
+  unsigned ls_iters;              /* 8 */
+  double ls_optimistic_factor;    /* 1.25 */
+  double ls_pessimistic_factor;   /* 0.5 */
+  double ls_armijo_coefficient;   /* 0.5 */
+  int variant;                    /* bogus_gpu_pg_variant, APGD */
+  int use_infinity_norm;          /* 0 */
+  int static_problem;             /* 1: SOC law; 0: Coulomb (DualFrictionProblem::solveWith(pg) default 1) */
+} bogus_gpu_pg_options;
+
+/* GaussSeidel setters and defaults (Core/BlockSolvers/GaussSeidelBase.hpp:39-91) plus the coloring switch
+ * of MecheFrictionProblem::Options (Interfaces/MecheInterface.hpp:44-69). */
+typedef struct bogus_gpu_gs_options {
+  double tol;                     /* 1e-6 */
+  unsigned max_iters;             /* 250 */
+  unsigned eval_every;            /* 25 */
+  double skip_tol;                /* 1e-6 */
+  unsigned skip_iters;            /* 10 */
+  double auto_regularization;     /* 0 */
+  int try_zero_as_well;           /* 1 */
+  int use_infinity_norm;          /* 0 */
+  int static_problem;             /* 0: Coulomb law (DualFrictionProblem::solveWith(gs) default) */
+  int local_strategy;             /* bogus_gpu_local_strategy, RevHybrid */
+} bogus_gpu_gs_options;
+
+typedef struct bogus_gpu_problem bogus_gpu_problem;
+
+/* Option defaults, identical to the reference's constructors. */
+void bogus_gpu_pg_options_default(bogus_gpu_pg_options* opts);
+void bogus_gpu_gs_options_default(bogus_gpu_gs_options* opts);
+
+const char* bogus_gpu_status_string(int status);
+/* Last CUDA / validation message recorded on this thread. */
+const char* bogus_gpu_last_error(void);
+
+/* Creates a problem handle on `device` (checks for an sm_103 device). */
+int bogus_gpu_create(int device, bogus_gpu_problem** out);
+int bogus_gpu_destroy(bogus_gpu_problem* h);
+
+/* DualFrictionProblem<3> members W, b, mu (Interfaces/FrictionProblem.hpp:140-150), from host arrays.
+ * symmetric_lower != 0: blocks hold the lower triangle incl. diagonal, rows sorted by column
+ * (SparseBlockMatrix<Matrix3d RowMajor, SYMMETRIC>); 0: both triangles, rows sorted. */
+int bogus_gpu_set_dual(bogus_gpu_problem* h, int n, const int* rowptr, const int* colidx, const double* blocks,
+                       int symmetric_lower, const double* b, const double* mu);
+
+/* Same, from device pointers (full both-triangle BSR already on the device; copied into the handle). */
+int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* d_rowptr, const int* d_colidx,
+                              const double* d_blocks, const double* d_b, const double* d_mu);
+
+/* Number of stored blocks of the both-triangle W held on the device. */
+int bogus_gpu_nnzb(const bogus_gpu_problem* h, int* nnzb);
+
+/* BlockSolverBase::callback() (Core/BlockSolvers/BlockSolverBase.hpp:45-51). */
+int bogus_gpu_set_callback(bogus_gpu_problem* h, bogus_gpu_callback cb, void* user);
+
+/* y = W x (SparseBlockMatrixBase::multiply, Core/Block/SparseMatrixVectorProduct.impl.hpp:423-432); host arrays. */
+int bogus_gpu_spmv(bogus_gpu_problem* h, const double* x, double* y);
+
+/* DualFrictionProblem::evalWith (Interfaces/FrictionProblem.cpp:56-66): error function at r, u = W r + b. */
+int bogus_gpu_eval(bogus_gpu_problem* h, const double* r, int static_problem, int use_infinity_norm,
+                   double* residual);
+
+/* DualFrictionProblem::solveWith(ProjectedGradient&, r, staticProblem) (Interfaces/FrictionProblem.cpp:49-54,
+ * ProjectedGradient.impl.hpp:74-382). r: host array, in/out. iters may be NULL. Variants APGD, Descent, SPG. */
+int bogus_gpu_solve_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* opts, double* r, double* residual,
+                       unsigned* iters);
+
+/* Same with r on the device (no host copies). */
+int bogus_gpu_solve_pg_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* opts, double* d_r, double* residual,
+                              unsigned* iters);
+
+/* DualFrictionProblem::solveWith(GaussSeidel&, r, staticProblem) (Interfaces/FrictionProblem.cpp:42-47,
+ * GaussSeidel.impl.hpp:62-205) with greedy coloring and the contact permutation of
+ * MecheFrictionProblem::solve (Interfaces/MecheInterface.cpp:326-337, Coloring.impl.hpp:20-62): colors are
+ * swept in order, one launch per color. Requires W set from host arrays (the coloring is built on the host). */
+int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* opts, double* r, double* residual,
+                       unsigned* iters);
+
+/* Greedy coloring used by bogus_gpu_solve_gs: perm[n] (contact order, colors contiguous) and colors[ncolors+1]
+ * offsets; colors must hold n + 1 ints. */
+int bogus_gpu_coloring(bogus_gpu_problem* h, int* perm, int* colors, int* ncolors);
+
+/* PrimalFrictionProblem data (Interfaces/FrictionProblem.hpp:55-116) for rigid bodies with a uniform number
+ * of dofs: minv[nbodies][ndof][ndof] (M^-1 blocks), contact i couples body objA[i] and objB[i] (-1: none)
+ * through 3 x ndof Jacobian blocks HA[i], HB[i] (row-major, local contact basis). */
+int bogus_gpu_set_primal(bogus_gpu_problem* h, int nbodies, int ndof, const double* minv, int ncontacts,
+                         const int* objA, const int* objB, const double* HA, const double* HB);
+
+/* DualFrictionProblem::computeFrom (Interfaces/FrictionProblem.cpp:30-40): W = H M^-1 H^T assembled on the
+ * device and b = w - H M^-1 f (w in the local basis, E = I; f may be NULL for f = 0); mu copied. The result
+ * replaces the handle's dual problem. */
+int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double* w, const double* mu);
+
+/* Copies the lower triangle of the device-held W back (rowptr[n+1], colidx/blocks sized by *nnzb_lower;
+ * pass NULL arrays first to get the size). */
+int bogus_gpu_get_dual_lower(bogus_gpu_problem* h, int* rowptr, int* colidx, double* blocks, int* nnzb_lower);
+
+/* Measurements of the last solve, spmv or assembly (no counterpart in the reference, which only offers
+ * MecheFrictionProblem::lastSolveTime, Interfaces/MecheInterface.hpp:173). */
+typedef struct bogus_gpu_solve_stats {
+  double device_ms;          /* device time between CUDA events around the solver kernels */
+  unsigned kernel_launches;  /* kernels launched */
+  unsigned iterations;
+  unsigned w_passes;         /* full passes over W (products) */
+  double algorithmic_bytes;  /* bytes the passes had to move: W (values + indices) + vector streams */
+  double fp64_fma;           /* FP64 fused multiply-adds of the W passes */
+} bogus_gpu_solve_stats;
+int bogus_gpu_get_solve_stats(const bogus_gpu_problem* h, bogus_gpu_solve_stats* out);
+
+/* The CUDA stream (cudaStream_t) the handle launches on, so callers can order and time their own work
+ * with it (no counterpart in the reference). */
+int bogus_gpu_get_stream(const bogus_gpu_problem* h, void** stream);
+
+/* Measures the FP64 fused multiply-add throughput of `device` in TFLOP/s: the ceiling of the FP64 kernels
+ * on GPUs whose FP64 rate is below their memory bandwidth's need (no counterpart in the reference). */
+int bogus_gpu_measure_fp64_peak(int device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BOGUS_GPU_H */

@@ -1,0 +1,253 @@
+"""ctypes binding of the CPU oracle (oracle/src). Test infrastructure only.
+
+Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py import this module, as the
+checker. The oracle restates So-bogus's friction-solve path in plain C++ (see oracle/src/*.hpp for the
+reference files each part follows).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "build", "liboracle.so")
+_lib = None
+
+CALLBACK = C.CFUNCTYPE(None, C.c_uint, C.c_double, C.c_void_p)
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def build() -> str:
+    """Compile liboracle.so with the committed Makefile (g++, OpenMP)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        build()
+    L = C.CDLL(_LIB_PATH)
+    vp = C.c_void_p
+    L.oracle_num_threads.restype = C.c_int
+    L.oracle_set_num_threads.argtypes = [C.c_int]
+    L.oracle_dual_create.restype = vp
+    L.oracle_dual_create.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp]
+    L.oracle_dual_destroy.argtypes = [vp]
+    L.oracle_dual_nnz_full.restype = C.c_int
+    L.oracle_dual_nnz_full.argtypes = [vp]
+    L.oracle_dual_full.argtypes = [vp, _ip, _ip, _dp]
+    L.oracle_dual_spmv.argtypes = [vp, _dp, _dp, C.c_void_p]
+    L.oracle_dual_split_row.argtypes = [vp, C.c_int, _dp, _dp]
+    L.oracle_dual_eval.restype = C.c_double
+    L.oracle_dual_eval.argtypes = [vp, C.c_int, _dp, C.c_int]
+    L.oracle_dual_solve_pg.restype = C.c_double
+    L.oracle_dual_solve_pg.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_double,
+                                       C.c_double, C.c_int, _dp, C.POINTER(C.c_uint), CALLBACK, C.c_void_p]
+    L.oracle_dual_coloring.restype = C.c_int
+    L.oracle_dual_coloring.argtypes = [vp, _ip, _ip]
+    L.oracle_dual_solve_gs.restype = C.c_double
+    L.oracle_dual_solve_gs.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_uint,
+                                       C.c_double, C.c_int, C.c_int, C.c_int, _dp, C.POINTER(C.c_uint), CALLBACK,
+                                       C.c_void_p]
+    L.oracle_local_solve.restype = C.c_double
+    L.oracle_local_solve.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_double, C.c_double, C.c_double]
+    L.oracle_law_solve_local.restype = C.c_int
+    L.oracle_law_solve_local.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_double, C.c_double]
+    L.oracle_real_roots.restype = C.c_int
+    L.oracle_real_roots.argtypes = [_dp, C.c_int, C.c_int, C.c_int, _dp]
+    L.oracle_project.argtypes = [C.c_double, _dp]
+    L.oracle_law_eval.restype = C.c_double
+    L.oracle_law_eval.argtypes = [C.c_int, C.c_double, _dp, _dp]
+    L.oracle_fb_jacobian.argtypes = [C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, _dp, _dp]
+    L.oracle_canonical_sum.restype = C.c_double
+    L.oracle_canonical_sum.argtypes = [_dp, C.c_size_t]
+    L.oracle_primal_create.restype = vp
+    L.oracle_primal_create.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip, _ip, _dp, _dp]
+    L.oracle_primal_destroy.argtypes = [vp]
+    L.oracle_primal_assemble.restype = C.c_int
+    L.oracle_primal_assemble.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.oracle_primal_rhs.argtypes = [vp, _dp, _dp, _dp]
+    L.oracle_primal_solve_admm.restype = C.c_double
+    L.oracle_primal_solve_admm.argtypes = [vp, _dp, C.c_double, _dp, _dp, _dp, C.c_double, C.c_uint, C.c_double,
+                                           C.c_int, C.c_int, _dp, _dp, C.POINTER(C.c_uint), CALLBACK, C.c_void_p]
+    _lib = L
+    return L
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def set_num_threads(t: int) -> None:
+    lib().oracle_set_num_threads(int(t))
+
+
+def num_threads() -> int:
+    return lib().oracle_num_threads()
+
+
+class Trace:
+    """Collects (iteration, residual) pairs from a solver callback."""
+
+    def __init__(self):
+        self.items = []
+        self._cb = CALLBACK(lambda it, r, _u: self.items.append((int(it), float(r))))
+
+
+_NO_CB = CALLBACK(0)
+
+
+class DualProblem:
+    """DualFrictionProblem<3>: W (lower-triangle BSR), b, mu."""
+
+    def __init__(self, rowptr, col, val, b, mu):
+        self.rowptr, self.col, self.val = _i32(rowptr), _i32(col), _f64(val).reshape(-1)
+        self.b, self.mu = _f64(b).reshape(-1), _f64(mu).reshape(-1)
+        self.n = len(self.rowptr) - 1
+        self.h = lib().oracle_dual_create(self.n, self.rowptr, self.col, self.val, self.b, self.mu)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.oracle_dual_destroy(self.h)
+            self.h = None
+
+    def full(self):
+        L = lib()
+        nnz = L.oracle_dual_nnz_full(self.h)
+        rp = np.zeros(self.n + 1, np.int32)
+        cl = np.zeros(nnz, np.int32)
+        vl = np.zeros(9 * nnz, np.float64)
+        L.oracle_dual_full(self.h, rp, cl, vl)
+        return rp, cl, vl
+
+    def spmv(self, x, init=None):
+        y = np.zeros(3 * self.n)
+        xi = _f64(x)
+        ii = None if init is None else _f64(init)
+        lib().oracle_dual_spmv(self.h, xi, y, None if ii is None else ii.ctypes.data_as(C.c_void_p))
+        return y
+
+    def split_row(self, row, x, res):
+        res = _f64(res).copy()
+        lib().oracle_dual_split_row(self.h, int(row), _f64(x), res)
+        return res
+
+    def eval(self, r, coulomb=True, inf_norm=False):
+        return lib().oracle_dual_eval(self.h, int(coulomb), _f64(r), int(inf_norm))
+
+    def coloring(self):
+        perm = np.zeros(self.n, np.int32)
+        colors = np.zeros(self.n + 1, np.int32)
+        nc = lib().oracle_dual_coloring(self.h, perm, colors)
+        return perm, colors[: nc + 1]
+
+    def solve_pg(self, r, variant=3, coulomb=False, tol=1e-6, max_iters=300, ls_iters=8, optimistic=1.25,
+                 pessimistic=0.5, armijo=0.5, inf_norm=False, trace: Trace | None = None):
+        r = _f64(r).copy()
+        it = C.c_uint(0)
+        cb = trace._cb if trace else _NO_CB
+        res = lib().oracle_dual_solve_pg(self.h, variant, int(coulomb), tol, max_iters, ls_iters, optimistic,
+                                         pessimistic, armijo, int(inf_norm), r, C.byref(it), cb, None)
+        return res, r, it.value
+
+    def solve_gs(self, r, coulomb=True, strategy=3, tol=1e-6, max_iters=250, eval_every=25, skip_tol=1e-6,
+                 skip_iters=10, auto_reg=0.0, try_zero=True, inf_norm=False, coloring=True,
+                 trace: Trace | None = None):
+        r = _f64(r).copy()
+        it = C.c_uint(0)
+        cb = trace._cb if trace else _NO_CB
+        res = lib().oracle_dual_solve_gs(self.h, int(coulomb), strategy, tol, max_iters, eval_every, skip_tol,
+                                         skip_iters, auto_reg, int(try_zero), int(inf_norm), int(coloring), r,
+                                         C.byref(it), cb, None)
+        return res, r, it.value
+
+
+def local_solve(A, b, x, mu, coulomb=True, strategy=3, tol=1.8189894035458565e-12, scaling=1.0):
+    x = _f64(x).copy()
+    res = lib().oracle_local_solve(int(coulomb), strategy, _f64(A).reshape(-1), _f64(b), x, mu, tol, scaling)
+    return res, x
+
+
+def law_solve_local(A, b, x, mu, coulomb=True, strategy=3, scaling=1.0):
+    x = _f64(x).copy()
+    ok = lib().oracle_law_solve_local(int(coulomb), strategy, _f64(A).reshape(-1), _f64(b), x, mu, scaling)
+    return bool(ok), x
+
+
+def real_roots(coeffs, degenerate=False, filt=0):
+    c = _f64(coeffs)
+    dim = len(c) - (1 if degenerate else 0)
+    roots = np.zeros(max(dim, 1))
+    n = lib().oracle_real_roots(c, dim, int(degenerate), filt, roots)
+    return roots[:n]
+
+
+def project(mu, x):
+    x = _f64(x).copy()
+    lib().oracle_project(mu, x)
+    return x
+
+
+def law_eval(mu, x, y, coulomb=True):
+    return lib().oracle_law_eval(int(coulomb), mu, _f64(x), _f64(y))
+
+
+def canonical_sum(v):
+    v = _f64(v)
+    return lib().oracle_canonical_sum(v, v.size)
+
+
+class PrimalProblem:
+    """Rigid-body primal data: uniform ndof per body, block-diagonal M^-1, contacts with 1 or 2 bodies."""
+
+    def __init__(self, minv, objA, objB, HA, HB):
+        self.minv = _f64(minv)
+        self.nbodies, self.ndof = self.minv.shape[0], self.minv.shape[1]
+        self.objA, self.objB = _i32(objA), _i32(objB)
+        self.HA, self.HB = _f64(HA), _f64(HB)
+        self.n = len(self.objA)
+        self.h = lib().oracle_primal_create(self.nbodies, self.ndof, self.minv.reshape(-1), self.n, self.objA,
+                                            self.objB, self.HA.reshape(-1), self.HB.reshape(-1))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.oracle_primal_destroy(self.h)
+            self.h = None
+
+    def assemble(self):
+        L = lib()
+        nnz = L.oracle_primal_assemble(self.h, None, None, None)
+        rp = np.zeros(self.n + 1, np.int32)
+        cl = np.zeros(nnz, np.int32)
+        vl = np.zeros(9 * nnz)
+        L.oracle_primal_assemble(self.h, rp.ctypes.data_as(C.c_void_p), cl.ctypes.data_as(C.c_void_p),
+                                 vl.ctypes.data_as(C.c_void_p))
+        return rp, cl, vl
+
+    def rhs(self, f, w):
+        b = np.zeros(3 * self.n)
+        lib().oracle_primal_rhs(self.h, _f64(f).reshape(-1), _f64(w).reshape(-1), b)
+        return b
+
+    def solve_admm(self, prox_inv, lam, mu, f, w, v, r, tol=1e-6, max_iters=300, step=1e-2, accelerated=True,
+                   inf_norm=False, trace: Trace | None = None):
+        v = _f64(v).copy()
+        r = _f64(r).copy()
+        it = C.c_uint(0)
+        cb = trace._cb if trace else _NO_CB
+        res = lib().oracle_primal_solve_admm(self.h, _f64(prox_inv).reshape(-1), lam, _f64(mu), _f64(f).reshape(-1),
+                                             _f64(w).reshape(-1), tol, max_iters, step, int(accelerated),
+                                             int(inf_norm), v, r, C.byref(it), cb, None)
+        return res, v, r, it.value

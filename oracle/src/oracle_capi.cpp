@@ -1,0 +1,261 @@
+// ORACLE — test infrastructure only (see oracle_math.hpp). C entry points for the Python tests and for
+// the CPU-baseline leg of bench.py (ctypes). Mirrors the reference's dual-problem calls:
+// DualFrictionProblem::solveWith / evalWith (Interfaces/FrictionProblem.cpp:42-66), including the
+// coloring + permutation wiring of MecheFrictionProblem::solve (Interfaces/MecheInterface.cpp:326-337).
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "oracle_math.hpp"
+#include "oracle_solvers.hpp"
+#include "oracle_sparse.hpp"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace oracle;
+
+namespace {
+
+struct DualProblem {
+  BSR low;   // stored lower triangle, as given
+  BSR full;  // both triangles
+  std::vector<double> b, mu;
+};
+
+typedef void (*oracle_callback)(unsigned, double, void*);
+
+Callback wrap(oracle_callback cb, void* user) {
+  if (!cb) return Callback();
+  return [cb, user](unsigned it, double r) { cb(it, r, user); };
+}
+
+BSR makeBSR(int n, const int* rowptr, const int* col, const double* val) {
+  BSR m;
+  m.n = n;
+  m.rowptr.assign(rowptr, rowptr + n + 1);
+  const int nnz = rowptr[n];
+  m.col.assign(col, col + nnz);
+  m.val.assign(val, val + 9 * (size_t)nnz);
+  return m;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_num_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void oracle_set_num_threads(int t) {
+#ifdef _OPENMP
+  if (t > 0) omp_set_num_threads(t);
+#else
+  (void)t;
+#endif
+}
+
+void* oracle_dual_create(int n, const int* rowptr, const int* col, const double* val, const double* b,
+                         const double* mu) {
+  auto* p = new DualProblem;
+  p->low = makeBSR(n, rowptr, col, val);
+  p->full = expandSymmetric(p->low);
+  p->b.assign(b, b + 3 * (size_t)n);
+  p->mu.assign(mu, mu + n);
+  return p;
+}
+
+void oracle_dual_destroy(void* h) { delete static_cast<DualProblem*>(h); }
+
+int oracle_dual_nnz_full(void* h) { return static_cast<DualProblem*>(h)->full.nnzb(); }
+
+void oracle_dual_full(void* h, int* rowptr, int* col, double* val) {
+  const BSR& f = static_cast<DualProblem*>(h)->full;
+  std::memcpy(rowptr, f.rowptr.data(), sizeof(int) * (f.n + 1));
+  std::memcpy(col, f.col.data(), sizeof(int) * f.nnzb());
+  std::memcpy(val, f.val.data(), sizeof(double) * 9 * (size_t)f.nnzb());
+}
+
+// y = W x (init null) or y = init + W x
+void oracle_dual_spmv(void* h, const double* x, double* y, const double* init) {
+  spmv(static_cast<DualProblem*>(h)->full, x, y, init);
+}
+
+void oracle_dual_split_row(void* h, int row, const double* x, double* res) {
+  splitRowMultiply(static_cast<DualProblem*>(h)->full, row, x, res);
+}
+
+// evalWith (FrictionProblem.impl.hpp:58-74): u = W r + b, scalings of the solver's matrix
+double oracle_dual_eval(void* h, int desaxce, const double* r, int useInfinityNorm) {
+  auto* p = static_cast<DualProblem*>(h);
+  SolverBase s;
+  s.setMatrix(p->full);
+  s.useInfinityNorm = useInfinityNorm != 0;
+  std::vector<double> u(p->b.size());
+  spmv(p->full, r, u.data());
+  for (size_t k = 0; k < u.size(); ++k) u[k] = u[k] + p->b[k];
+  Law law{desaxce != 0, RevHybrid, p->mu.data()};
+  return s.eval(law, u.data(), r);
+}
+
+double oracle_dual_solve_pg(void* h, int variant, int desaxce, double tol, unsigned maxIters, unsigned lsIters,
+                            double optimistic, double pessimistic, double armijo, int useInfinityNorm, double* r,
+                            unsigned* iters, oracle_callback cb, void* user) {
+  auto* p = static_cast<DualProblem*>(h);
+  ProjectedGradient pg;
+  pg.setMatrix(p->full);
+  pg.variant = variant;
+  pg.tol = tol;
+  pg.maxIters = maxIters;
+  pg.lsIters = lsIters;
+  pg.lsOptimisticFactor = optimistic;
+  pg.lsPessimisticFactor = pessimistic;
+  pg.lsArmijoCoefficient = armijo;
+  pg.useInfinityNorm = useInfinityNorm != 0;
+  pg.callback = wrap(cb, user);
+  Law law{desaxce != 0, RevHybrid, p->mu.data()};
+  return pg.solve(law, p->b.data(), r, iters);
+}
+
+// Greedy coloring of the stored lower triangle; returns the number of colors (perm: n, colors: ncolors+1).
+int oracle_dual_coloring(void* h, int* perm, int* colors) {
+  auto* p = static_cast<DualProblem*>(h);
+  std::vector<int> pm, cl;
+  greedyColoring(p->low, pm, cl);
+  std::memcpy(perm, pm.data(), sizeof(int) * pm.size());
+  std::memcpy(colors, cl.data(), sizeof(int) * cl.size());
+  return (int)cl.size() - 1;
+}
+
+// GaussSeidel through solveWith: with use_coloring the problem is permuted so that colors are contiguous
+// (applyPermutation), solved color by color, and r is permuted back.
+double oracle_dual_solve_gs(void* h, int desaxce, int strat, double tol, unsigned maxIters, unsigned evalEvery,
+                            double skipTol, unsigned skipIters, double autoReg, int tryZero, int useInfinityNorm,
+                            int useColoring, double* r, unsigned* iters, oracle_callback cb, void* user) {
+  auto* p = static_cast<DualProblem*>(h);
+  const int n = p->low.n;
+  GaussSeidel gs;
+  gs.tol = tol;
+  gs.maxIters = maxIters;
+  gs.evalEvery = evalEvery;
+  gs.skipTol = skipTol;
+  gs.skipIters = skipIters;
+  gs.autoRegularization = autoReg;
+  gs.tryZeroAsWell = tryZero != 0;
+  gs.useInfinityNorm = useInfinityNorm != 0;
+  gs.callback = wrap(cb, user);
+  if (!useColoring) {
+    gs.setMatrix(p->full);
+    Law law{desaxce != 0, strat, p->mu.data()};
+    return gs.solve(law, p->b.data(), r, iters);
+  }
+  std::vector<int> perm, colors;
+  greedyColoring(p->low, perm, colors);
+  const BSR plow = permuteSymmetric(p->low, perm);
+  const BSR pfull = expandSymmetric(plow);
+  const std::vector<double> pb = permuteSegments(p->b, perm, 3);
+  const std::vector<double> pmu = permuteSegments(p->mu, perm, 1);
+  std::vector<double> rv(r, r + 3 * (size_t)n);
+  std::vector<double> pr = permuteSegments(rv, perm, 3);
+  gs.perm.resize(n);
+  for (int i = 0; i < n; ++i) gs.perm[i] = i;
+  gs.colors = colors;
+  gs.setMatrix(pfull);
+  Law law{desaxce != 0, strat, pmu.data()};
+  const double res = gs.solve(law, pb.data(), pr.data(), iters);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) r[3 * (size_t)perm[i] + k] = pr[3 * (size_t)i + k];
+  return res;
+}
+
+// ---- per-contact mathematics -------------------------------------------------------------------
+double oracle_local_solve(int desaxce, int strat, const double* A, const double* b, double* x, double mu, double tol,
+                          double scaling) {
+  return localSolve(desaxce != 0, strat, A, b, x, mu, tol, scaling);
+}
+
+int oracle_law_solve_local(int desaxce, int strat, const double* A, const double* b, double* x, double mu,
+                           double scaling) {
+  return lawSolveLocal(desaxce != 0, strat, A, b, x, mu, scaling) ? 1 : 0;
+}
+
+// coeffs: dim entries (monic, degenerate == 0) or dim + 1 entries (degenerate != 0; copied first)
+int oracle_real_roots(const double* coeffs, int dim, int degenerate, int filter, double* roots) {
+  double c[8];
+  for (int k = 0; k < dim + (degenerate ? 1 : 0); ++k) c[k] = coeffs[k];
+  if (degenerate) return realRootsDegenerate(c, dim, roots, (RootsFilter)filter);
+  return realRootsMonic(c, dim, roots, (RootsFilter)filter);
+}
+
+void oracle_project(double mu, double* x) { projectCone(mu, x); }
+
+double oracle_law_eval(int desaxce, double mu, const double* x, const double* y) {
+  return lawEval(desaxce != 0, mu, x, y);
+}
+
+void oracle_fb_jacobian(int desaxce, double mu, double scaling, const double* A, const double* b, const double* x,
+                        double* fb, double* dFdx) {
+  LocalFB f{desaxce != 0, mu, scaling, A, b};
+  f.computeJacobian(x, fb, dFdx);
+}
+
+double oracle_canonical_sum(const double* v, size_t n) { return canonicalSum(v, n); }
+
+// ---- primal problem / Delassus assembly ---------------------------------------------------------
+void* oracle_primal_create(int nbodies, int ndof, const double* minv, int ncontacts, const int* objA, const int* objB,
+                           const double* HA, const double* HB) {
+  auto* P = new Primal;
+  P->nbodies = nbodies;
+  P->ndof = ndof;
+  P->ncontacts = ncontacts;
+  P->minv.assign(minv, minv + (size_t)nbodies * ndof * ndof);
+  P->objA.assign(objA, objA + ncontacts);
+  P->objB.assign(objB, objB + ncontacts);
+  P->HA.assign(HA, HA + (size_t)ncontacts * 3 * ndof);
+  P->HB.assign(HB, HB + (size_t)ncontacts * 3 * ndof);
+  return P;
+}
+
+void oracle_primal_destroy(void* h) { delete static_cast<Primal*>(h); }
+
+// Assembles the lower triangle of W; returns nnzb. Call with null outputs first to size them.
+int oracle_primal_assemble(void* h, int* rowptr, int* col, double* val) {
+  const BSR W = assembleW(*static_cast<Primal*>(h));
+  if (rowptr) std::memcpy(rowptr, W.rowptr.data(), sizeof(int) * (W.n + 1));
+  if (col) std::memcpy(col, W.col.data(), sizeof(int) * W.nnzb());
+  if (val) std::memcpy(val, W.val.data(), sizeof(double) * 9 * (size_t)W.nnzb());
+  return W.nnzb();
+}
+
+void oracle_primal_rhs(void* h, const double* f, const double* w, double* b) {
+  const std::vector<double> bb = assembleB(*static_cast<Primal*>(h), f, w);
+  std::memcpy(b, bb.data(), sizeof(double) * bb.size());
+}
+
+// PrimalFrictionProblem::solveWith(ADMM&, lambda, v, r): proxInv = (M + lambda I)^-1 blocks
+double oracle_primal_solve_admm(void* h, const double* proxInv, double lambda, const double* mu, const double* f,
+                                const double* w, double tol, unsigned maxIters, double stepSize, int accelerated,
+                                int useInfinityNorm, double* v, double* r, unsigned* iters, oracle_callback cb,
+                                void* user) {
+  auto* P = static_cast<Primal*>(h);
+  ADMMSolver s;
+  s.P = P;
+  s.tol = tol;
+  s.maxIters = maxIters;
+  s.stepSize = stepSize;
+  s.accelerated = accelerated != 0;
+  s.useInfinityNorm = useInfinityNorm != 0;
+  s.callback = wrap(cb, user);
+  std::vector<double> invMu(P->ncontacts);
+  for (int i = 0; i < P->ncontacts; ++i) invMu[i] = 1. / mu[i];
+  std::vector<double> pinv(proxInv, proxInv + (size_t)P->nbodies * P->ndof * P->ndof);
+  return s.solve(invMu.data(), pinv, lambda, f, w, v, r, iters);
+}
+
+}  // extern "C"

@@ -1,0 +1,629 @@
+// ORACLE — test infrastructure only (see oracle_math.hpp).
+//
+// CPU restatement of the reference's block solvers on a dual friction problem (W, b, mu):
+//   ConstrainedSolverBase  (Core/BlockSolvers/ConstrainedSolverBase.impl.hpp)
+//   GaussSeidel            (Core/BlockSolvers/GaussSeidel.impl.hpp, GaussSeidelBase.impl.hpp)
+//   ProjectedGradient      (Core/BlockSolvers/ProjectedGradient.impl.hpp), all five variants
+//   ADMM / QuadraticProxOp (Core/BlockSolvers/ADMM.impl.hpp:29-127)
+// Vectors are contact-major: x[3i + k]. Every global dot product or residual is the canonicalSum() of
+// per-contact values; per-contact values use the evaluation order of oracle_math.hpp.
+#pragma once
+
+#include <cfloat>
+#include <functional>
+#include <vector>
+
+#include "oracle_math.hpp"
+#include "oracle_sparse.hpp"
+
+namespace oracle {
+
+using Callback = std::function<void(unsigned, double)>;
+
+struct Law {
+  bool desaxce;        // Coulomb (De Saxce change of variable) or plain SOC
+  int strat;           // local_soc_solver::Strategy
+  const double* mu;
+};
+
+struct SolverBase {
+  const BSR* W = nullptr;  // full view (both triangles)
+  std::vector<double> scaling;
+  bool useInfinityNorm = false;
+  double tol = 1e-6;
+  unsigned maxIters = 300;
+  Callback callback;
+
+  // updateScalings (ConstrainedSolverBase.impl.hpp:78-118): max(1, trace(W_ii)/3), 1 without a diagonal block
+  void setMatrix(const BSR& M) {
+    W = &M;
+    scaling.assign(M.n, 1.0);
+    for (int i = 0; i < M.n; ++i) {
+      const int p = M.diagPtr(i);
+      if (p >= 0) {
+        const double* B = M.block(p);
+        scaling[i] = dmax(1.0, ((B[0] + B[4]) + B[8]) / 3.0);
+      }
+    }
+  }
+  int n() const { return W->n; }
+
+  // eval (ConstrainedSolverBase.impl.hpp:21-74)
+  double eval(const Law& law, const double* y, const double* x) const {
+    const int N = n();
+    std::vector<double> v(N);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; ++i) {
+      const double s = scaling[i];
+      const double lx[3] = {x[3 * i] * s, x[3 * i + 1] * s, x[3 * i + 2] * s};
+      v[i] = lawEval(law.desaxce, law.mu[i], lx, &y[3 * i]);
+    }
+    if (useInfinityNorm) return maxOf(v.data(), N);
+    return canonicalSum(v.data(), N) / (double)(1 + N);
+  }
+  void projectOnConstraints(const Law& law, double* x) const {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n(); ++i) projectCone(law.mu[i], &x[3 * i]);
+  }
+  void dualityCOVAll(const Law& law, const double* y, double* s) const {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n(); ++i) dualityCOV(law.desaxce, law.mu[i], &y[3 * i], &s[3 * i]);
+  }
+  void trigger(unsigned it, double r) const {
+    if (callback) callback(it, r);
+  }
+};
+
+// Per-contact reduction helpers (canonical)
+template <typename F>
+inline double reduceContacts(int n, F f) {
+  std::vector<double> v(n);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; ++i) v[i] = f(i);
+  return canonicalSum(v.data(), n);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Gauss-Seidel (GaussSeidel.impl.hpp:62-205, GaussSeidelBase.impl.hpp:21-77)
+// ---------------------------------------------------------------------------------------------
+struct GaussSeidel : SolverBase {
+  unsigned evalEvery = 25;
+  double skipTol = 1e-6;
+  unsigned skipIters = 10;
+  double autoRegularization = 0.0;
+  bool tryZeroAsWell = true;
+  std::vector<int> perm, colors;   // Coloring: permutation + color offsets
+  std::vector<double> local;       // 9 n, diagonal blocks (+ regularization)
+  std::vector<double> reg;         // n
+
+  GaussSeidel() { tol = 1e-6; maxIters = 250; }
+
+  // setMatrix + updateLocalMatrices + processLocalMatrices; coloring reset to one color (natural order)
+  void setMatrix(const BSR& M) {
+    SolverBase::setMatrix(M);
+    const int N = M.n;
+    if ((int)perm.size() != N) {
+      perm.resize(N);
+      std::iota(perm.begin(), perm.end(), 0);
+      colors = {0, N};
+    }
+    local.assign(9 * (size_t)N, 0.0);
+    reg.assign(N, 0.0);
+    for (int i = 0; i < N; ++i) {
+      const int p = M.diagPtr(i);
+      if (p >= 0) std::copy(M.block(p), M.block(p) + 9, &local[9 * (size_t)i]);
+      const double* D = &local[9 * (size_t)i];
+      scaling[i] = dmax(1.0, ((D[0] + D[4]) + D[8]) / 3.0);
+      if (autoRegularization > 0.) {
+        const double lmin = minEigenSymmetric3(D);
+        reg[i] = dmax(0.0, autoRegularization - lmin);
+        local[9 * (size_t)i + 0] += reg[i];
+        local[9 * (size_t)i + 4] += reg[i];
+        local[9 * (size_t)i + 8] += reg[i];
+      }
+    }
+  }
+
+  // Smallest eigenvalue of a symmetric 3x3 block by cyclic Jacobi rotations (the reference takes the real
+  // parts of Eigen's general eigenvalues; W_ii is symmetric so both agree up to rounding).
+  static double minEigenSymmetric3(const double* D) {
+    double a[9];
+    for (int k = 0; k < 9; ++k) a[k] = D[k];
+    for (int sweep = 0; sweep < 50; ++sweep) {
+      const double off = a[1] * a[1] + a[2] * a[2] + a[5] * a[5];
+      if (off == 0.0) break;
+      for (int p = 0; p < 2; ++p)
+        for (int q = p + 1; q < 3; ++q) {
+          const double apq = a[3 * p + q];
+          if (apq == 0.0) continue;
+          const double theta = (a[3 * q + q] - a[3 * p + p]) / (2.0 * apq);
+          const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+          const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+          for (int k = 0; k < 3; ++k) {  // A <- A J
+            const double akp = a[3 * k + p], akq = a[3 * k + q];
+            a[3 * k + p] = c * akp - s * akq;
+            a[3 * k + q] = s * akp + c * akq;
+          }
+          for (int k = 0; k < 3; ++k) {  // A <- J^T A
+            const double apk = a[3 * p + k], aqk = a[3 * q + k];
+            a[3 * p + k] = c * apk - s * aqk;
+            a[3 * q + k] = s * apk + c * aqk;
+          }
+        }
+    }
+    return dmin(dmin(a[0], a[4]), a[8]);
+  }
+
+  double evalAndKeepBest(const Law& law, const double* x, const double* y, std::vector<double>& x_best,
+                         double& err_best) const {
+    const double err = eval(law, y, x);
+    if (err < err_best) {
+      x_best.assign(x, x + 3 * (size_t)n());
+      err_best = err;
+    }
+    return err;
+  }
+
+  void innerLoop(const Law& law, const double* b, std::vector<unsigned char>& skip, double& ndxRef, double* x) const {
+    const double absSkipTol = dmin(skipTol, tol);
+    const double absSkipIters = dmin((double)skipIters, (double)(unsigned)std::sqrt((double)skip.size()));
+    for (size_t c = 0; c + 1 < colors.size(); ++c) {
+      for (int pi = colors[c]; pi < colors[c + 1]; ++pi) {
+        const int i = perm[pi];
+        if (skip[i]) {
+          --skip[i];
+          continue;
+        }
+        double lx[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+        double lb[3];
+        for (int k = 0; k < 3; ++k) lb[k] = b[3 * i + k] - reg[i] * lx[k];
+        splitRowMultiply(*W, i, x, lb);
+        double ldx[3] = {-lx[0], -lx[1], -lx[2]};
+        const bool ok = lawSolveLocal(law.desaxce, law.strat, &local[9 * (size_t)i], lb, lx, law.mu[i], scaling[i]);
+        for (int k = 0; k < 3; ++k) ldx[k] = ldx[k] + lx[k];
+        if (!ok) {
+          ldx[0] *= .5; ldx[1] *= .5; ldx[2] *= .5;
+        }
+        for (int k = 0; k < 3; ++k) x[3 * i + k] = x[3 * i + k] + ldx[k];
+        const double s2 = scaling[i] * scaling[i];
+        const double nx2 = s2 * sq3(lx);
+        const double ndx2 = s2 * sq3(ldx);
+        if (ndx2 > ndxRef) ndxRef = ndx2;
+        if (dmin(nx2, ndx2) < absSkipTol || ndx2 < skipTol * dmin(nx2, ndxRef))
+          skip[i] = (unsigned char)absSkipIters;
+      }
+    }
+  }
+
+  // solve(law, b, x, tryZeroAsWell) == solveWithLinearConstraints(law, Zero, b, x, tryZero, 0)
+  double solve(const Law& law, const double* b, double* x, unsigned* itersOut = nullptr) const {
+    const int N = n();
+    const size_t n3 = 3 * (size_t)N;
+    std::vector<double> y(n3), x_best;
+    double err_best = DBL_MAX;
+    spmv(*W, x, y.data(), b);
+    evalAndKeepBest(law, x, y.data(), x_best, err_best);
+    if (tryZeroAsWell) {  // tryZero (GaussSeidelBase.impl.hpp:61-77)
+      std::vector<double> zero(n3, 0.0);
+      const double err_zero = eval(law, b, zero.data());
+      if (err_zero < err_best) {
+        err_best = err_zero;
+        x_best.assign(n3, 0.0);
+        std::fill(x, x + n3, 0.0);
+      } else {
+        std::copy(x_best.begin(), x_best.end(), x);
+      }
+    }
+    trigger(0, err_best);
+    std::vector<unsigned char> skip(N, 0);
+    double ndxRef = 0;
+    unsigned GSIter;
+    for (GSIter = 1; GSIter <= maxIters; ++GSIter) {
+      innerLoop(law, b, skip, ndxRef, x);
+      if (0 == (GSIter % evalEvery)) {
+        spmv(*W, x, y.data(), b);
+        const double err = evalAndKeepBest(law, x, y.data(), x_best, err_best);
+        trigger(GSIter, err);
+        if (err < tol) break;
+        ndxRef /= evalEvery;
+      }
+    }
+    if (GSIter > maxIters) std::copy(x_best.begin(), x_best.end(), x);
+    if (itersOut) *itersOut = GSIter > maxIters ? maxIters : GSIter;
+    return err_best;
+  }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Projected gradient (ProjectedGradient.impl.hpp)
+// ---------------------------------------------------------------------------------------------
+enum PGVariant { Standard = 0, Descent = 1, Conjugated = 2, APGD = 3, SPG = 4 };  // projected_gradient::Variant
+
+struct ProjectedGradient : SolverBase {
+  unsigned lsIters = 8;
+  double lsOptimisticFactor = 1.25, lsPessimisticFactor = .5, lsArmijoCoefficient = .5;
+  int variant = APGD;
+
+  ProjectedGradient() { tol = 1e-6; maxIters = 300; }
+
+  bool testResidual(const Law& law, unsigned it, const double* x, const double* y, std::vector<double>& x_best,
+                    double& min_res) const {
+    const double res = eval(law, y, x);
+    trigger(it, res);
+    if (0 == it || res < min_res) {
+      x_best.assign(x, x + 3 * (size_t)n());
+      min_res = res;
+    }
+    return res < tol;
+  }
+
+  // guess_alpha (:21-28)
+  void guessAlpha(const double* x, double& alpha) const {
+    const int N = n();
+    std::vector<double> d(3 * (size_t)N), Md(3 * (size_t)N);
+    for (size_t k = 0; k < d.size(); ++k) d[k] = x[k] - 1.0;
+    spmv(*W, d.data(), Md.data());
+    const double nMx = reduceContacts(N, [&](int i) { return sq3(&Md[3 * i]); });
+    if (nMx > 1.e-16) alpha = dmin(1., reduceContacts(N, [&](int i) { return sq3(&d[3 * i]); }) / nMx);
+  }
+
+  double objective(const double* x, const double* Mx, const double* b, const double* s) const {
+    return reduceContacts(n(), [&](int i) {
+      double t[3];
+      for (int k = 0; k < 3; ++k) t[k] = (0.5 * Mx[3 * i + k] + b[3 * i + k]) + s[3 * i + k];
+      return dot3(&x[3 * i], t);
+    });
+  }
+
+  double solve(const Law& law, const double* b, double* x, unsigned* itersOut = nullptr) const {
+    switch (variant) {
+      case APGD: return solveAPGD(law, b, x, true, itersOut);
+      case Descent: return solveAPGD(law, b, x, false, itersOut);
+      case SPG: return solveSPG(law, b, x, itersOut);
+      case Standard: return solveStandard(law, b, x, itersOut);
+      case Conjugated: return solveConjugated(law, b, x, itersOut);
+    }
+    return -1;
+  }
+
+  // PgMethod<APGD / Descent> (:74-155)
+  double solveAPGD(const Law& law, const double* b, double* x, bool apgd, unsigned* itersOut) const {
+    const int N = n();
+    const size_t n3 = 3 * (size_t)N;
+    std::vector<double> Mx(n3), y(n3), xs(n3), s(n3), prev, x_best;
+    projectOnConstraints(law, x);
+    spmv(*W, x, Mx.data());
+    double theta = 1., q = 0;
+    prev.assign(x, x + n3);
+    double alpha = 1.;
+    guessAlpha(x, alpha);
+    double min_res = -1;
+    unsigned it;
+    for (it = 0; it < maxIters; ++it) {
+      for (size_t k = 0; k < n3; ++k) y[k] = Mx[k] + b[k];
+      if (testResidual(law, it, x, y.data(), x_best, min_res)) break;
+      dualityCOVAll(law, y.data(), s.data());
+      for (size_t k = 0; k < n3; ++k) y[k] = y[k] + s[k];
+      const double J = objective(x, Mx.data(), b, s.data());
+      double Js = J;
+      alpha *= lsOptimisticFactor;
+      for (unsigned ls = 0; ls < lsIters; ++ls, alpha *= lsPessimisticFactor) {
+        for (size_t k = 0; k < n3; ++k) xs[k] = std::fma(-alpha, y[k], x[k]);
+        projectOnConstraints(law, xs.data());
+        spmv(*W, xs.data(), Mx.data());
+        Js = objective(xs.data(), Mx.data(), b, s.data());
+        const double decr = reduceContacts(N, [&](int i) {
+          const double d[3] = {xs[3 * i] - x[3 * i], xs[3 * i + 1] - x[3 * i + 1], xs[3 * i + 2] - x[3 * i + 2]};
+          return dot3(&y[3 * i], d);
+        });
+        const double nrm = reduceContacts(N, [&](int i) {
+          const double d[3] = {xs[3 * i] - x[3 * i], xs[3 * i + 1] - x[3 * i + 1], xs[3 * i + 2] - x[3 * i + 2]};
+          return sq3(d);
+        });
+        if (Js < (J + decr) + (.5 / alpha) * nrm) break;
+      }
+      const double decr2 = reduceContacts(N, [&](int i) {
+        const double d[3] = {xs[3 * i] - prev[3 * i], xs[3 * i + 1] - prev[3 * i + 1], xs[3 * i + 2] - prev[3 * i + 2]};
+        return dot3(d, &y[3 * i]);
+      });
+      if (apgd && decr2 < 0) {
+        const double beta = nesterovInertia(theta, q);
+        for (size_t k = 0; k < n3; ++k) x[k] = std::fma(beta, xs[k] - prev[k], xs[k]);
+        spmv(*W, x, Mx.data());
+      } else {
+        std::copy(xs.begin(), xs.end(), x);
+        theta = 1.;
+      }
+      prev = xs;
+    }
+    std::copy(x_best.begin(), x_best.end(), x);
+    if (itersOut) *itersOut = it;
+    return min_res;
+  }
+
+  // PgMethod<SPG> (:288-351)
+  double solveSPG(const Law& law, const double* b, double* x, unsigned* itersOut) const {
+    const int N = n();
+    const size_t n3 = 3 * (size_t)N;
+    std::vector<double> Mx(n3), y(n3), xs(n3), s(n3), z(n3), w(n3), prev, x_best;
+    projectOnConstraints(law, x);
+    prev.assign(x, x + n3);
+    spmv(*W, x, Mx.data());
+    double theta = 1, q = 0;
+    const double a_min = 1.e-6, a_max = 1.e6;
+    double alpha = 1;
+    guessAlpha(x, alpha);
+    double min_res = -1;
+    unsigned it;
+    for (it = 0; it < maxIters; ++it) {
+      for (size_t k = 0; k < n3; ++k) y[k] = Mx[k] + b[k];
+      if (testResidual(law, it, x, y.data(), x_best, min_res)) break;
+      dualityCOVAll(law, y.data(), s.data());
+      for (size_t k = 0; k < n3; ++k) y[k] = y[k] + s[k];
+      for (size_t k = 0; k < n3; ++k) xs[k] = std::fma(-alpha, y[k], x[k]);
+      projectOnConstraints(law, xs.data());
+      const double decr = reduceContacts(N, [&](int i) {
+        const double d[3] = {xs[3 * i] - prev[3 * i], xs[3 * i + 1] - prev[3 * i + 1], xs[3 * i + 2] - prev[3 * i + 2]};
+        return dot3(d, &y[3 * i]);
+      });
+      if (decr < 0.) {
+        const double beta = nesterovInertia(theta, q);
+        for (size_t k = 0; k < n3; ++k) {
+          w[k] = std::fma(beta, xs[k] - prev[k], xs[k]) - x[k];
+          x[k] = x[k] + w[k];
+        }
+      } else {
+        for (size_t k = 0; k < n3; ++k) {
+          w[k] = xs[k] - x[k];
+          x[k] = xs[k];
+        }
+        theta = 1.;
+      }
+      for (size_t k = 0; k < n3; ++k) z[k] = -Mx[k];
+      spmv(*W, x, Mx.data());
+      prev = xs;
+      for (size_t k = 0; k < n3; ++k) z[k] = z[k] + Mx[k];
+      const double wz = reduceContacts(N, [&](int i) { return dot3(&w[3 * i], &z[3 * i]); });
+      const double zz = reduceContacts(N, [&](int i) { return sq3(&z[3 * i]); });
+      alpha = wz / zz;
+      alpha = dmin(a_max, dmax(a_min, alpha));
+    }
+    std::copy(x_best.begin(), x_best.end(), x);
+    if (itersOut) *itersOut = it;
+    return min_res;
+  }
+
+  // armijo_ls (:54-72) on the objective with linear part bs = b + s
+  void armijoLS(const Law& law, const double* x, const double* bs, const double* dir, const double* grad, double J,
+                double& alpha, double* xs, double& Js, double* Mx) const {
+    const int N = n();
+    const size_t n3 = 3 * (size_t)N;
+    Js = J;
+    std::vector<double> zero(n3, 0.0);
+    for (unsigned ls = 0; ls < lsIters; ++ls, alpha *= lsPessimisticFactor) {
+      for (size_t k = 0; k < n3; ++k) xs[k] = std::fma(alpha, dir[k], x[k]);
+      projectOnConstraints(law, xs);
+      spmv(*W, xs, Mx);
+      Js = objective(xs, Mx, bs, zero.data());
+      const double decr = reduceContacts(N, [&](int i) {
+        const double d[3] = {xs[3 * i] - x[3 * i], xs[3 * i + 1] - x[3 * i + 1], xs[3 * i + 2] - x[3 * i + 2]};
+        return dot3(&grad[3 * i], d);
+      });
+      if (Js < J + lsArmijoCoefficient * decr) break;
+    }
+  }
+
+  // PgMethod<Standard> (:157-209)
+  double solveStandard(const Law& law, const double* b, double* x, unsigned* itersOut) const {
+    const int N = n();
+    const size_t n3 = 3 * (size_t)N;
+    std::vector<double> Mx(n3), y(n3), xs(n3), s(n3), pg(n3), Mpg(n3), bs(n3), x_best;
+    projectOnConstraints(law, x);
+    spmv(*W, x, Mx.data());
+    double alpha = 1;
+    double min_res = -1;
+    unsigned it;
+    for (it = 0; it < maxIters; ++it) {
+      for (size_t k = 0; k < n3; ++k) y[k] = Mx[k] + b[k];
+      if (testResidual(law, it, x, y.data(), x_best, min_res)) break;
+      dualityCOVAll(law, y.data(), s.data());
+      for (size_t k = 0; k < n3; ++k) y[k] = y[k] + s[k];
+      const double J = objective(x, Mx.data(), b, s.data());
+      for (size_t k = 0; k < n3; ++k) xs[k] = x[k] - y[k];
+      projectOnConstraints(law, xs.data());
+      for (size_t k = 0; k < n3; ++k) pg[k] = x[k] - xs[k];
+      spmv(*W, pg.data(), Mpg.data());
+      const double num = reduceContacts(N, [&](int i) { return dot3(&y[3 * i], &pg[3 * i]); });
+      const double den = reduceContacts(N, [&](int i) { return dot3(&pg[3 * i], &Mpg[3 * i]); });
+      const double beta = -num / den;
+      for (size_t k = 0; k < n3; ++k) pg[k] *= beta;
+      double Js;
+      alpha = dmin(1., alpha * lsOptimisticFactor);
+      for (size_t k = 0; k < n3; ++k) bs[k] = b[k] + s[k];
+      armijoLS(law, x, bs.data(), pg.data(), y.data(), J, alpha, xs.data(), Js, Mx.data());
+      std::copy(xs.begin(), xs.end(), x);
+    }
+    std::copy(x_best.begin(), x_best.end(), x);
+    if (itersOut) *itersOut = it;
+    return min_res;
+  }
+
+  // PgMethod<Conjugated> (:211-286)
+  double solveConjugated(const Law& law, const double* b, double* x, unsigned* itersOut) const {
+    const int N = n();
+    const size_t n3 = 3 * (size_t)N;
+    std::vector<double> Mx(n3), y(n3), xs(n3), s(n3), dir(n3), prev_dir(n3), prev_pg, bs(n3), x_best;
+    projectOnConstraints(law, x);
+    spmv(*W, x, Mx.data());
+    prev_pg.assign(x, x + n3);
+    double prev_n2 = 0;
+    double alpha = 1.;
+    double min_res = -1;
+    unsigned it;
+    for (it = 0; it < maxIters; ++it) {
+      for (size_t k = 0; k < n3; ++k) y[k] = Mx[k] + b[k];
+      if (testResidual(law, it, x, y.data(), x_best, min_res)) break;
+      dualityCOVAll(law, y.data(), s.data());
+      for (size_t k = 0; k < n3; ++k) y[k] = y[k] + s[k];
+      const double J = objective(x, Mx.data(), b, s.data());
+      {
+        for (size_t k = 0; k < n3; ++k) xs[k] = x[k] - y[k];
+        projectOnConstraints(law, xs.data());
+        for (size_t k = 0; k < n3; ++k) xs[k] = x[k] - xs[k];
+        const double ng2 = reduceContacts(N, [&](int i) { return sq3(&xs[3 * i]); });
+        if (prev_n2 == 0.) {
+          for (size_t k = 0; k < n3; ++k) dir[k] = -y[k];
+        } else {
+          const double den = reduceContacts(N, [&](int i) {
+            const double d[3] = {xs[3 * i] - prev_pg[3 * i], xs[3 * i + 1] - prev_pg[3 * i + 1],
+                                 xs[3 * i + 2] - prev_pg[3 * i + 2]};
+            return dot3(&prev_dir[3 * i], d);
+          });
+          const double xp = reduceContacts(N, [&](int i) { return dot3(&xs[3 * i], &prev_pg[3 * i]); });
+          const double beta = (den < 1.e-12) ? dmax(0., (ng2 - xp)) / prev_n2 : dmax(0., (ng2 - xp)) / den;
+          for (size_t k = 0; k < n3; ++k) dir[k] = beta * prev_dir[k] - y[k];
+          const double dy = reduceContacts(N, [&](int i) { return dot3(&dir[3 * i], &y[3 * i]); });
+          if (dy >= 0.)
+            for (size_t k = 0; k < n3; ++k) dir[k] = -y[k];
+        }
+        prev_pg = xs;
+        prev_n2 = ng2;
+      }
+      double Js;
+      alpha = alpha * lsOptimisticFactor;
+      for (size_t k = 0; k < n3; ++k) bs[k] = b[k] + s[k];
+      armijoLS(law, x, bs.data(), dir.data(), y.data(), J, alpha, xs.data(), Js, Mx.data());
+      for (size_t k = 0; k < n3; ++k) prev_dir[k] = (xs[k] - x[k]) / alpha;
+      std::copy(xs.begin(), xs.end(), x);
+    }
+    std::copy(x_best.begin(), x_best.end(), x);
+    if (itersOut) *itersOut = it;
+    return min_res;
+  }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Primal ADMM / AMA (ADMM.impl.hpp:54-127) with QuadraticProxOp (:29-38), as called by
+// PrimalFrictionProblem::solveWith(ADMM&, lambda, v, r) (Interfaces/PrimalFrictionProblem.cpp:61-76):
+// law SOCLaw<3, false> on 1/mu, operator H (contacts x bodies, 3 x ndof blocks), prox operator
+// (M + lambda I)^-1 given as block-diagonal dense inverses `proxInv` (M^-1 when lambda == 0).
+// The residual uses the error function of a non-square matrix: all scalings are 1.
+// ---------------------------------------------------------------------------------------------
+struct ADMMSolver {
+  const Primal* P = nullptr;
+  double tol = 1e-6;
+  unsigned maxIters = 300;
+  double stepSize = 1e-2;
+  bool accelerated = true;
+  bool useInfinityNorm = false;
+  Callback callback;
+
+  // ut = w + H v
+  void Hmul(const double* v, const double* w, double* ut) const {
+    const int n = P->ncontacts, d = P->ndof;
+    for (int i = 0; i < n; ++i) {
+      int bodies[2]; const double* H[2]; int nb;
+      contactBodies(*P, i, bodies, H, nb);
+      for (int r = 0; r < 3; ++r) {
+        double a = w ? w[3 * i + r] : 0.0;
+        for (int t = 0; t < nb; ++t)
+          for (int m = 0; m < d; ++m) a = std::fma(H[t][r * d + m], v[(size_t)bodies[t] * d + m], a);
+        ut[3 * i + r] = a;
+      }
+    }
+  }
+  // out = init + H^T r, accumulated body by body over its contacts in increasing contact index
+  void HTmul(const double* r, const double* init, double* out) const {
+    const int n = P->ncontacts, d = P->ndof;
+    const size_t m = (size_t)P->nbodies * d;
+    for (size_t k = 0; k < m; ++k) out[k] = init ? init[k] : 0.0;
+    for (int i = 0; i < n; ++i) {
+      int bodies[2]; const double* H[2]; int nb;
+      contactBodies(*P, i, bodies, H, nb);
+      for (int t = 0; t < nb; ++t)
+        for (int q = 0; q < d; ++q) {
+          double a = out[(size_t)bodies[t] * d + q];
+          for (int rr = 0; rr < 3; ++rr) a = std::fma(H[t][rr * d + q], r[3 * i + rr], a);
+          out[(size_t)bodies[t] * d + q] = a;
+        }
+    }
+  }
+  // res = proxInv (rhs - f), block diagonal
+  void prox(const std::vector<double>& proxInv, const double* rhs, const double* f, double* res) const {
+    const int d = P->ndof;
+    for (int k = 0; k < P->nbodies; ++k) {
+      double t[16];
+      for (int q = 0; q < d; ++q) t[q] = rhs[(size_t)k * d + q] - f[(size_t)k * d + q];
+      for (int m = 0; m < d; ++m) {
+        double a = 0.0;
+        for (int q = 0; q < d; ++q) a = std::fma(proxInv[(size_t)k * d * d + m * d + q], t[q], a);
+        res[(size_t)k * d + m] = a;
+      }
+    }
+  }
+
+  double solve(const double* invMu, const std::vector<double>& proxInv, double lambda, const double* f,
+               const double* w, double* x, double* r, unsigned* itersOut = nullptr) const {
+    const int n = P->ncontacts;
+    const size_t n3 = 3 * (size_t)n, m = (size_t)P->nbodies * P->ndof;
+    const double gamma = stepSize, inv_gamma = 1. / gamma;
+    double res = -1;
+    std::vector<double> ut(n3), prox_arg(m), z(n3), y(n3), y_prev(n3), zacc, z_prev, tmp(n3);
+    Hmul(x, w, ut.data());
+    for (size_t k = 0; k < n3; ++k) z[k] = ut[k] - inv_gamma * r[k];
+    for (int i = 0; i < n; ++i) projectCone(invMu[i], &z[3 * i]);
+    for (size_t k = 0; k < n3; ++k) y_prev[k] = -inv_gamma * r[k];
+    zacc = z;
+    z_prev = z;
+    double theta_prev = 1.;
+    double res_prev = -1;
+    unsigned it;
+    std::vector<double> ev(n);
+    for (it = 0; it < maxIters; ++it) {
+      if (lambda < kEps) {
+        HTmul(r, nullptr, prox_arg.data());
+      } else {
+        for (size_t k = 0; k < n3; ++k) tmp[k] = std::fma(gamma, zacc[k] - ut[k], r[k]);
+        // prox_arg = x / lambda ... multiply<true>(ut, prox_arg, 1, 1/lambda): prox_arg = (1/lambda) x + H^T ut
+        std::vector<double> sx(m);
+        const double il = 1. / lambda;
+        for (size_t k = 0; k < m; ++k) sx[k] = il * x[k];
+        HTmul(tmp.data(), sx.data(), prox_arg.data());
+      }
+      prox(proxInv, prox_arg.data(), f, x);
+      Hmul(x, w, ut.data());
+      // eval(law, r, ut): per contact FB(1/mu, ut_i (scaling 1), r_i) with SOC law
+      for (int i = 0; i < n; ++i) ev[i] = lawEval(false, invMu[i], &ut[3 * i], &r[3 * i]);
+      double e = useInfinityNorm ? maxOf(ev.data(), n) : canonicalSum(ev.data(), n) / (double)(1 + n);
+      std::vector<double> gap(n);
+      for (int i = 0; i < n; ++i) {
+        const double d3[3] = {ut[3 * i] - z[3 * i], ut[3 * i + 1] - z[3 * i + 1], ut[3 * i + 2] - z[3 * i + 2]};
+        gap[i] = useInfinityNorm ? dmax(dmax(std::fabs(d3[0]), std::fabs(d3[1])), std::fabs(d3[2])) : sq3(d3);
+      }
+      res = e + (useInfinityNorm ? maxOf(gap.data(), n) : canonicalSum(gap.data(), n) / (double)(1 + n3));
+      if (callback) callback(it, res);
+      if (res < tol) break;
+      for (size_t k = 0; k < n3; ++k) z[k] = ut[k] - inv_gamma * r[k];
+      for (int i = 0; i < n; ++i) projectCone(invMu[i], &z[3 * i]);
+      if (accelerated && res < res_prev) {
+        for (size_t k = 0; k < n3; ++k) y[k] = (ut[k] - z[k]) - inv_gamma * r[k];
+        const double beta = nesterovInertia(theta_prev, 0.);
+        for (size_t k = 0; k < n3; ++k) r[k] = -gamma * std::fma(beta, y[k] - y_prev[k], y[k]);
+        y_prev = y;
+        for (size_t k = 0; k < n3; ++k) zacc[k] = std::fma(beta, z[k] - z_prev[k], z[k]);
+        z_prev = z;
+      } else {
+        for (size_t k = 0; k < n3; ++k) r[k] = std::fma(gamma, z[k] - ut[k], r[k]);
+        zacc = z;
+        z_prev = z;
+        for (size_t k = 0; k < n3; ++k) y_prev[k] = -inv_gamma * r[k];
+        theta_prev = 1;
+      }
+      res_prev = res;
+    }
+    if (itersOut) *itersOut = it;
+    return res;
+  }
+};
+
+}  // namespace oracle

@@ -1,0 +1,375 @@
+"""bogus_gpu — Python host interface of the GB300 friction-solve library (ctypes over libbogus_gpu.so).
+
+Mirrors So-bogus's friction-solve API (Interfaces/FrictionProblem.hpp, Core/BlockSolvers/*.hpp) with the
+same names, defaults and argument meanings:
+
+    problem = DualFrictionProblem()            # W (3x3-block BSR), b, mu on the GPU
+    problem.computeFrom(primal)                # W = H M^-1 H^T, b = w - H M^-1 f   (on the GPU)
+    pg = ProjectedGradient(); pg.setTol(1e-6)  # APGD by default
+    res = problem.solveWith(pg, r)             # r: warm start in, solution out (staticProblem=True)
+    gs = GaussSeidel()
+    res = problem.solveWith(gs, r)             # colored GS, Coulomb law (staticProblem=False)
+
+Every solve runs the CUDA kernels of libbogus_gpu.so; there is no CPU path. Importing this module on a
+machine without the built library raises ImportError; calls without a usable sm_103 GPU raise BogusGpuError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libbogus_gpu.so")
+
+OK, NOT_CONVERGED, BAD_INPUT, NONFINITE, CUDA_ERROR, TIMEOUT, NO_DEVICE, NO_PROBLEM = range(8)
+STANDARD, DESCENT, CONJUGATED, APGD, SPG = range(5)            # projected_gradient::Variant
+PURE_NEWTON, PURE_ENUMERATIVE, HYBRID, REV_HYBRID = range(4)   # local_soc_solver::Strategy
+
+
+class BogusGpuError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"bogus_gpu status {status}: {message}")
+        self.status = status
+
+
+class PgOptions(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint), ("ls_iters", C.c_uint),
+                ("ls_optimistic_factor", C.c_double), ("ls_pessimistic_factor", C.c_double),
+                ("ls_armijo_coefficient", C.c_double), ("variant", C.c_int), ("use_infinity_norm", C.c_int),
+                ("static_problem", C.c_int)]
+
+
+class GsOptions(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint), ("eval_every", C.c_uint), ("skip_tol", C.c_double),
+                ("skip_iters", C.c_uint), ("auto_regularization", C.c_double), ("try_zero_as_well", C.c_int),
+                ("use_infinity_norm", C.c_int), ("static_problem", C.c_int), ("local_strategy", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("device_ms", C.c_double), ("kernel_launches", C.c_uint), ("iterations", C.c_uint),
+                ("w_passes", C.c_uint), ("algorithmic_bytes", C.c_double), ("fp64_fma", C.c_double)]
+
+
+CALLBACK = C.CFUNCTYPE(None, C.c_uint, C.c_double, C.c_void_p)
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lib = None
+
+EXPORTED = [
+    "bogus_gpu_pg_options_default", "bogus_gpu_gs_options_default", "bogus_gpu_status_string",
+    "bogus_gpu_last_error", "bogus_gpu_create", "bogus_gpu_destroy", "bogus_gpu_set_dual",
+    "bogus_gpu_set_dual_device", "bogus_gpu_nnzb", "bogus_gpu_set_callback", "bogus_gpu_spmv", "bogus_gpu_eval",
+    "bogus_gpu_solve_pg", "bogus_gpu_solve_pg_device", "bogus_gpu_solve_gs", "bogus_gpu_coloring",
+    "bogus_gpu_set_primal", "bogus_gpu_assemble_dual", "bogus_gpu_get_dual_lower", "bogus_gpu_get_solve_stats",
+    "bogus_gpu_get_stream", "bogus_gpu_measure_fp64_peak",
+]
+
+
+def lib():
+    """Loads libbogus_gpu.so (raises ImportError when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libbogus_gpu.so is not built ({LIB_PATH}); run __graft_entry__.build()")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    L.bogus_gpu_pg_options_default.argtypes = [C.POINTER(PgOptions)]
+    L.bogus_gpu_gs_options_default.argtypes = [C.POINTER(GsOptions)]
+    L.bogus_gpu_status_string.restype = C.c_char_p
+    L.bogus_gpu_status_string.argtypes = [C.c_int]
+    L.bogus_gpu_last_error.restype = C.c_char_p
+    L.bogus_gpu_create.argtypes = [C.c_int, C.POINTER(vp)]
+    L.bogus_gpu_destroy.argtypes = [vp]
+    L.bogus_gpu_set_dual.argtypes = [vp, C.c_int, _ip, vp, vp, C.c_int, _dp, _dp]
+    L.bogus_gpu_set_dual_device.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp]
+    L.bogus_gpu_nnzb.argtypes = [vp, C.POINTER(C.c_int)]
+    L.bogus_gpu_set_callback.argtypes = [vp, CALLBACK, vp]
+    L.bogus_gpu_spmv.argtypes = [vp, _dp, _dp]
+    L.bogus_gpu_eval.argtypes = [vp, _dp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.bogus_gpu_solve_pg.argtypes = [vp, C.POINTER(PgOptions), _dp, C.POINTER(C.c_double), C.POINTER(C.c_uint)]
+    L.bogus_gpu_solve_pg_device.argtypes = [vp, C.POINTER(PgOptions), vp, C.POINTER(C.c_double), C.POINTER(C.c_uint)]
+    L.bogus_gpu_solve_gs.argtypes = [vp, C.POINTER(GsOptions), _dp, C.POINTER(C.c_double), C.POINTER(C.c_uint)]
+    L.bogus_gpu_coloring.argtypes = [vp, _ip, _ip, C.POINTER(C.c_int)]
+    L.bogus_gpu_set_primal.argtypes = [vp, C.c_int, C.c_int, _dp, C.c_int, _ip, _ip, _dp, _dp]
+    L.bogus_gpu_assemble_dual.argtypes = [vp, vp, _dp, _dp]
+    L.bogus_gpu_get_dual_lower.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_int)]
+    L.bogus_gpu_get_solve_stats.argtypes = [vp, C.POINTER(SolveStats)]
+    L.bogus_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.bogus_gpu_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    _lib = L
+    return L
+
+
+def _check(status: int, allow_not_converged: bool = True) -> int:
+    if status == OK or (allow_not_converged and status == NOT_CONVERGED):
+        return status
+    L = lib()
+    raise BogusGpuError(status, f"{L.bogus_gpu_status_string(status).decode()}: {L.bogus_gpu_last_error().decode()}")
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Signal:
+    """Signal<unsigned, double> (Core/Utils/Signal.hpp): listeners receive (iteration, residual)."""
+
+    def __init__(self):
+        self._callees = []
+
+    def connect(self, fn) -> None:
+        self._callees.append(fn)
+
+    def disconnectAll(self) -> None:
+        self._callees.clear()
+
+    def trigger(self, it: int, res: float) -> None:
+        for fn in self._callees:
+            fn(it, res)
+
+
+class _SolverBase:
+    def __init__(self, tol: float, max_iters: int):
+        self._tol = tol
+        self._max_iters = max_iters
+        self._inf = False
+        self._callback = Signal()
+
+    def setTol(self, tol: float) -> None: self._tol = float(tol)
+    def tol(self) -> float: return self._tol
+    def setMaxIters(self, n: int) -> None: self._max_iters = int(n)
+    def maxIters(self) -> int: return self._max_iters
+    def useInfinityNorm(self, on: bool) -> None: self._inf = bool(on)
+    def usesInfinityNorm(self) -> bool: return self._inf
+    def callback(self) -> Signal: return self._callback
+
+
+class ProjectedGradient(_SolverBase):
+    """ProjectedGradient<WType> (Core/BlockSolvers/ProjectedGradient.hpp:21-107): tol 1e-6, 300 iterations,
+    8 line-search iterations, factors 1.25 / 0.5 / 0.5, APGD."""
+
+    def __init__(self):
+        super().__init__(1e-6, 300)
+        self._ls = 8
+        self._opt, self._pess, self._armijo = 1.25, 0.5, 0.5
+        self._variant = APGD
+
+    def setLineSearchIterations(self, n: int) -> None: self._ls = int(n)
+    def setLineSearchOptimisticFactor(self, f: float) -> None: self._opt = float(f)
+    def setLineSearchPessimisticFactor(self, f: float) -> None: self._pess = float(f)
+    def setLineSearchArmijoCoefficient(self, f: float) -> None: self._armijo = float(f)
+    def setDefaultVariant(self, v: int) -> None: self._variant = int(v)
+    def lineSearchIterations(self) -> int: return self._ls
+
+    def options(self, static_problem: bool) -> PgOptions:
+        o = PgOptions()
+        lib().bogus_gpu_pg_options_default(C.byref(o))
+        o.tol, o.max_iters, o.ls_iters = self._tol, self._max_iters, self._ls
+        o.ls_optimistic_factor, o.ls_pessimistic_factor, o.ls_armijo_coefficient = self._opt, self._pess, self._armijo
+        o.variant, o.use_infinity_norm, o.static_problem = self._variant, int(self._inf), int(static_problem)
+        return o
+
+
+class GaussSeidel(_SolverBase):
+    """GaussSeidel<WType> (Core/BlockSolvers/GaussSeidel.hpp, GaussSeidelBase.hpp:39-91): tol 1e-6,
+    250 sweeps, evalEvery 25, skipTol 1e-6, skipIters 10, tryZeroAsWell. Always colored."""
+
+    def __init__(self):
+        super().__init__(1e-6, 250)
+        self._eval_every, self._skip_tol, self._skip_iters = 25, 1e-6, 10
+        self._auto_reg, self._try_zero = 0.0, True
+        self._strategy = REV_HYBRID
+
+    def setEvalEvery(self, n: int) -> None: self._eval_every = int(n)
+    def setSkipTol(self, t: float) -> None: self._skip_tol = float(t)
+    def setSkipIters(self, n: int) -> None: self._skip_iters = int(n)
+    def setAutoRegularization(self, r: float) -> None: self._auto_reg = float(r)
+    def doTryZeroAsWell(self, on: bool = True) -> None: self._try_zero = bool(on)
+    def setLocalStrategy(self, s: int) -> None:
+        """SOCLaw's Strat template argument (default RevHybrid)."""
+        self._strategy = int(s)
+
+    def options(self, static_problem: bool) -> GsOptions:
+        o = GsOptions()
+        lib().bogus_gpu_gs_options_default(C.byref(o))
+        o.tol, o.max_iters, o.eval_every = self._tol, self._max_iters, self._eval_every
+        o.skip_tol, o.skip_iters, o.auto_regularization = self._skip_tol, self._skip_iters, self._auto_reg
+        o.try_zero_as_well, o.use_infinity_norm = int(self._try_zero), int(self._inf)
+        o.static_problem, o.local_strategy = int(static_problem), self._strategy
+        return o
+
+
+class PrimalFrictionProblem:
+    """PrimalFrictionProblem<3> for rigid bodies (Interfaces/FrictionProblem.hpp:55-116): M^-1 blocks,
+    per-contact Jacobian blocks for one or two bodies, f, w (local contact basis), mu."""
+
+    def __init__(self, minv, objA, objB, HA, HB, w, mu, f=None):
+        self.minv = _f64(minv)
+        self.objA, self.objB = _i32(objA), _i32(objB)
+        self.HA, self.HB = _f64(HA), _f64(HB)
+        self.w, self.mu = _f64(w).reshape(-1), _f64(mu).reshape(-1)
+        self.f = None if f is None else _f64(f).reshape(-1)
+
+    @classmethod
+    def from_generated(cls, data) -> "PrimalFrictionProblem":
+        """Wraps generator.PrimalData: w = b (free velocity, f = 0)."""
+        return cls(data.minv, data.objA, data.objB, data.HA, data.HB, data.b, data.mu)
+
+    def computeMInv(self, M) -> None:
+        """Sets the inverse mass blocks from mass blocks M[nbodies, ndof, ndof] (PrimalFrictionProblem::computeMInv)."""
+        self.minv = _f64(np.linalg.inv(_f64(M)))
+
+
+class DualFrictionProblem:
+    """DualFrictionProblem<3> (Interfaces/FrictionProblem.hpp:127-214) held on one GPU."""
+
+    def __init__(self, device: int = 0):
+        L = lib()
+        h = C.c_void_p()
+        _check(L.bogus_gpu_create(int(device), C.byref(h)), False)
+        self._h = h
+        self.n = 0
+        self._cb_keep = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.bogus_gpu_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set(self, rowptr, col, blocks, b, mu, symmetric_lower: bool = True) -> None:
+        """Sets W (3x3-block BSR, lower triangle by default), b and mu from host arrays."""
+        rowptr, col, blocks = _i32(rowptr), _i32(col), _f64(blocks).reshape(-1)
+        b, mu = _f64(b).reshape(-1), _f64(mu).reshape(-1)
+        n = len(rowptr) - 1
+        if b.size != 3 * n or mu.size != n or blocks.size != 9 * col.size:
+            raise ValueError("inconsistent W / b / mu sizes")
+        _check(lib().bogus_gpu_set_dual(self._h, n, rowptr, col.ctypes.data_as(C.c_void_p),
+                                        blocks.ctypes.data_as(C.c_void_p), int(symmetric_lower), b, mu), False)
+        self.n = n
+
+    def computeFrom(self, primal: PrimalFrictionProblem) -> None:
+        """W = H M^-1 H^T and b = w - H M^-1 f on the GPU (DualFrictionProblem::computeFrom)."""
+        L = lib()
+        nb, ndof = primal.minv.shape[0], primal.minv.shape[1]
+        n = primal.objA.size
+        _check(L.bogus_gpu_set_primal(self._h, nb, ndof, primal.minv.reshape(-1), n, primal.objA, primal.objB,
+                                      primal.HA.reshape(-1), primal.HB.reshape(-1)), False)
+        fptr = None if primal.f is None else primal.f.ctypes.data_as(C.c_void_p)
+        _check(L.bogus_gpu_assemble_dual(self._h, fptr, primal.w, primal.mu), False)
+        self.n = n
+
+    def W_lower(self):
+        """Lower triangle of W as (rowptr, col, blocks[nnzb, 3, 3])."""
+        L = lib()
+        nnz = C.c_int()
+        _check(L.bogus_gpu_get_dual_lower(self._h, None, None, None, C.byref(nnz)), False)
+        rp = np.zeros(self.n + 1, np.int32)
+        cl = np.zeros(nnz.value, np.int32)
+        vl = np.zeros(9 * nnz.value)
+        _check(L.bogus_gpu_get_dual_lower(self._h, rp.ctypes.data_as(C.c_void_p), cl.ctypes.data_as(C.c_void_p),
+                                          vl.ctypes.data_as(C.c_void_p), C.byref(nnz)), False)
+        return rp, cl, vl.reshape(-1, 3, 3)
+
+    def nnzb(self) -> int:
+        v = C.c_int()
+        _check(lib().bogus_gpu_nnzb(self._h, C.byref(v)), False)
+        return v.value
+
+    def multiply(self, x) -> np.ndarray:
+        """y = W x."""
+        x = _f64(x).reshape(-1)
+        y = np.zeros_like(x)
+        _check(lib().bogus_gpu_spmv(self._h, x, y), False)
+        return y
+
+    def _bind(self, solver) -> None:
+        sig = solver.callback()
+        if sig._callees:
+            cb = CALLBACK(lambda it, res, _u: sig.trigger(int(it), float(res)))
+            self._cb_keep = cb
+            lib().bogus_gpu_set_callback(self._h, cb, None)
+        else:
+            self._cb_keep = None
+            lib().bogus_gpu_set_callback(self._h, CALLBACK(0), None)
+
+    def solveWith(self, solver, r, staticProblem: bool | None = None) -> float:
+        """Solves in place (r: float64 array of 3n entries, warm start and result); returns the residual.
+        staticProblem defaults as in the reference: False for GaussSeidel, True for ProjectedGradient."""
+        if not (isinstance(r, np.ndarray) and r.dtype == np.float64 and r.flags.c_contiguous):
+            raise TypeError("r must be a C-contiguous float64 numpy array (solved in place)")
+        res = C.c_double()
+        it = C.c_uint()
+        self._bind(solver)
+        if isinstance(solver, GaussSeidel):
+            sp = False if staticProblem is None else staticProblem
+            o = solver.options(sp)
+            st = lib().bogus_gpu_solve_gs(self._h, C.byref(o), r.reshape(-1), C.byref(res), C.byref(it))
+        elif isinstance(solver, ProjectedGradient):
+            sp = True if staticProblem is None else staticProblem
+            o = solver.options(sp)
+            st = lib().bogus_gpu_solve_pg(self._h, C.byref(o), r.reshape(-1), C.byref(res), C.byref(it))
+        else:
+            raise TypeError("solver must be GaussSeidel or ProjectedGradient")
+        _check(st)
+        self.last_status, self.last_iterations = st, it.value
+        return res.value
+
+    def evalWith(self, solver, r, staticProblem: bool | None = None) -> float:
+        """Error function at r with the solver's norm (DualFrictionProblem::evalWith)."""
+        sp = staticProblem
+        if sp is None:
+            sp = isinstance(solver, ProjectedGradient)
+        res = C.c_double()
+        _check(lib().bogus_gpu_eval(self._h, _f64(r).reshape(-1), int(sp), int(solver.usesInfinityNorm()),
+                                    C.byref(res)), False)
+        return res.value
+
+    def coloring(self):
+        perm = np.zeros(self.n, np.int32)
+        colors = np.zeros(self.n + 1, np.int32)
+        nc = C.c_int()
+        _check(lib().bogus_gpu_coloring(self._h, perm, colors, C.byref(nc)), False)
+        return perm, colors[: nc.value + 1]
+
+    def solve_stats(self) -> dict:
+        """Device time, launches, W passes, algorithmic bytes and FP64 FMAs of the last solve."""
+        st = SolveStats()
+        _check(lib().bogus_gpu_get_solve_stats(self._h, C.byref(st)), False)
+        return {k: getattr(st, k) for k, _ in SolveStats._fields_}
+
+    def stream(self) -> int:
+        """The cudaStream_t (as an integer) this problem's kernels run on."""
+        v = C.c_void_p()
+        _check(lib().bogus_gpu_get_stream(self._h, C.byref(v)), False)
+        return v.value or 0
+
+    def solve_pg_device(self, solver: "ProjectedGradient", d_r_ptr: int, staticProblem: bool = True):
+        """APGD / SPG with r already in device memory (pointer to 3n doubles); returns (residual, iterations)."""
+        res = C.c_double()
+        it = C.c_uint()
+        self._bind(solver)
+        o = solver.options(staticProblem)
+        st = lib().bogus_gpu_solve_pg_device(self._h, C.byref(o), C.c_void_p(d_r_ptr), C.byref(res), C.byref(it))
+        _check(st)
+        self.last_status, self.last_iterations = st, it.value
+        return res.value, it.value
+
+
+def measure_fp64_peak(device: int = 0) -> float:
+    """FP64 FMA throughput of the device in TFLOP/s (the ceiling of the FP64 kernels)."""
+    v = C.c_double()
+    _check(lib().bogus_gpu_measure_fp64_peak(int(device), C.byref(v)), False)
+    return v.value

@@ -1,0 +1,1004 @@
+// Host side of the C ABI declared in include/bogus_gpu.h: problem upload and validation, the solve drivers
+// (persistent projected gradient, colored Gauss-Seidel), the error function and the Delassus assembly.
+// Host work is limited to one-off structure preparation (symmetric expansion, coloring, permutation,
+// assembly pattern); every iteration runs on the GPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bogus_gpu.h"
+#include "host_sparse.h"
+#include "internal.h"
+#include "soc_device.cuh"
+
+namespace bogus_gpu {
+
+// assembly kernels (kernels_assembly.cu)
+struct AssemblyPlan {
+  int n = 0, nbodies = 0, ndof = 0;
+  int nlow = 0;  // lower blocks to compute
+};
+cudaError_t launch_assembly_T(int n, int ndof, const double* minv, const int* cb, const double* H, double* T,
+                              cudaStream_t s);
+cudaError_t launch_assembly_W(int nlow, int ndof, const int* li, const int* lj, const int* pair_off,
+                              const int* pair_ti, const int* pair_tj, const double* H, const double* T,
+                              const int* pos_ij, const int* pos_ji, double* val, cudaStream_t s);
+cudaError_t launch_assembly_b(int n, int nbodies, int ndof, const double* minv, const double* f, const int* cb,
+                              const double* H, const double* w, double* mf, double* b, cudaStream_t s);
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const std::string& msg) {
+  g_last_error = msg;
+  return status;
+}
+
+#define BG_CUDA(call)                                                                          \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
+      return fail(BOGUS_GPU_CUDA_ERROR, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, (count ? count : 1) * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct GSCache {
+  bool valid = false;
+  std::vector<int> perm, colors;
+  DevBuf<int> rowptr, col;
+  DevBuf<double> val, local, reg, scaling, b, mu;
+  DevBuf<double> x, nx2, ndx2, y, chunk, scalar, xbest;
+  DevBuf<unsigned char> skip, processed;
+  DevBuf<unsigned long long> tile_max;
+  DevBuf<double> ndx_ref;
+  double auto_reg = -1.0;
+  void release() {
+    rowptr.release(); col.release(); val.release(); local.release(); reg.release(); scaling.release();
+    b.release(); mu.release(); x.release(); nx2.release(); ndx2.release(); y.release(); chunk.release();
+    scalar.release(); xbest.release(); skip.release(); processed.release(); tile_max.release(); ndx_ref.release();
+    valid = false;
+  }
+};
+
+}  // namespace
+
+}  // namespace bogus_gpu
+
+using namespace bogus_gpu;
+
+struct bogus_gpu_problem {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // dual problem (both triangles on the device)
+  DevBSR W;
+  DevBuf<int> rowptr, col, diag;
+  DevBuf<double> val, b, mu, scaling;
+  bool has_dual = false;
+  bool host_lower_valid = false;
+  HostBSR host_lower;  // lower triangle (for the coloring); kept when W came from host arrays or assembly
+  std::vector<double> host_b, host_mu;
+  // projected-gradient work
+  DevBuf<double> X, MX, Y, S0, XB, Wv, csum, scal, trace;
+  DevBuf<PGOut> pgout;
+  DevBuf<unsigned> barrier;
+  DevBuf<int> status;
+  // misc work
+  DevBuf<double> vx, vy, chunk, scalar;
+  GSCache gs;
+  // primal data for the assembly
+  int nbodies = 0, ndof = 0, ncontacts = 0;
+  DevBuf<double> minv, H, T, mf;
+  DevBuf<int> cb;  // per contact: body of slot 0, body of slot 1 (-1), slot order by body index
+  std::vector<int> h_cb;
+  bogus_gpu_callback callback = nullptr;
+  void* callback_user = nullptr;
+  float last_ms = 0.f;
+  unsigned last_launches = 0;
+  bogus_gpu_solve_stats last_stats{};
+};
+
+namespace {
+
+int check_handle(const bogus_gpu_problem* h) {
+  if (!h) return fail(BOGUS_GPU_BAD_INPUT, "null handle");
+  return BOGUS_GPU_OK;
+}
+
+int set_device(const bogus_gpu_problem* h) {
+  const cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return fail(BOGUS_GPU_CUDA_ERROR, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  return BOGUS_GPU_OK;
+}
+
+// Uploads a both-triangle host BSR and b, mu; computes diagonal positions and scalings on the device.
+int upload_full(bogus_gpu_problem* h, const HostBSR& f, const double* b, const double* mu) {
+  const int n = f.n;
+  const int nnz = f.nnzb();
+  BG_CUDA(h->rowptr.ensure(n + 1));
+  BG_CUDA(h->col.ensure(nnz));
+  BG_CUDA(h->val.ensure(9 * (size_t)nnz));
+  BG_CUDA(h->diag.ensure(n));
+  BG_CUDA(h->b.ensure(3 * (size_t)n));
+  BG_CUDA(h->mu.ensure(n));
+  BG_CUDA(h->scaling.ensure(n));
+  BG_CUDA(cudaMemcpyAsync(h->rowptr.p, f.rowptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, h->stream));
+  if (nnz) {
+    BG_CUDA(cudaMemcpyAsync(h->col.p, f.col.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, h->stream));
+    BG_CUDA(cudaMemcpyAsync(h->val.p, f.val.data(), sizeof(double) * 9 * (size_t)nnz, cudaMemcpyHostToDevice, h->stream));
+  }
+  if (n) {
+    BG_CUDA(cudaMemcpyAsync(h->b.p, b, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, h->stream));
+    BG_CUDA(cudaMemcpyAsync(h->mu.p, mu, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  }
+  h->W.n = n;
+  h->W.nnzb = nnz;
+  h->W.rowptr = h->rowptr.p;
+  h->W.col = h->col.p;
+  h->W.val = h->val.p;
+  h->W.diag = h->diag.p;
+  BG_CUDA(launch_diag_and_scaling(h->W, h->scaling.p, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  h->has_dual = true;
+  h->gs.valid = false;
+  return BOGUS_GPU_OK;
+}
+
+int check_finite(const double* v, size_t m, const char* what) {
+  for (size_t k = 0; k < m; ++k)
+    if (!std::isfinite(v[k])) return fail(BOGUS_GPU_NONFINITE, std::string("non-finite value in ") + what);
+  return BOGUS_GPU_OK;
+}
+
+int ensure_pg_work(bogus_gpu_problem* h, unsigned max_iters) {
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  const int C = (n + 31) / 32;
+  BG_CUDA(h->X.ensure(3 * n3));
+  BG_CUDA(h->MX.ensure(2 * n3));
+  BG_CUDA(h->Y.ensure(n3));
+  BG_CUDA(h->S0.ensure(n));
+  BG_CUDA(h->XB.ensure(n3));
+  BG_CUDA(h->Wv.ensure(n3));
+  BG_CUDA(h->csum.ensure(4 * (size_t)C));
+  BG_CUDA(h->scal.ensure(8));
+  BG_CUDA(h->trace.ensure((size_t)max_iters + 1));
+  BG_CUDA(h->pgout.ensure(1));
+  BG_CUDA(h->barrier.ensure(2));
+  BG_CUDA(h->status.ensure(1));
+  return BOGUS_GPU_OK;
+}
+
+// Runs the persistent solver with r already in X[0]; returns the buffer holding the result.
+int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual, unsigned* iters, const double** best) {
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  PGArgs a{};
+  a.n = n;
+  a.nchunks = (n + 31) / 32;
+  a.rowptr = h->W.rowptr;
+  a.col = h->W.col;
+  a.val = h->W.val;
+  a.b = h->b.p;
+  a.mu = h->mu.p;
+  a.scaling = h->scaling.p;
+  a.X0 = h->X.p;
+  a.X1 = h->X.p + n3;
+  a.X2 = h->X.p + 2 * n3;
+  a.MX0 = h->MX.p;
+  a.MX1 = h->MX.p + n3;
+  a.Y = h->Y.p;
+  a.S0 = h->S0.p;
+  a.XB = h->XB.p;
+  a.Wv = h->Wv.p;
+  a.csum = h->csum.p;
+  a.scal = h->scal.p;
+  a.trace = h->trace.p;
+  a.out = h->pgout.p;
+  a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.desaxce = o->static_problem ? 0 : 1;
+  a.variant = o->variant;
+  a.use_inf = o->use_infinity_norm ? 1 : 0;
+  a.tol = o->tol;
+  a.opt = o->ls_optimistic_factor;
+  a.pess = o->ls_pessimistic_factor;
+  a.max_iters = o->max_iters;
+  a.ls_iters = o->ls_iters;
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 2 * sizeof(unsigned), h->stream));
+  BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
+  int grid = pg_max_grid(h->device);
+  if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
+  const int want = (a.nchunks + 7) / 8;
+  if (want < grid) grid = want < 1 ? 1 : want;
+  BG_CUDA(cudaEventRecord(h->ev0, h->stream));
+  BG_CUDA(launch_pg_persistent(a, grid, h->stream));
+  BG_CUDA(cudaEventRecord(h->ev1, h->stream));
+  PGOut out{};
+  int st = 0;
+  BG_CUDA(cudaMemcpyAsync(&out, h->pgout.p, sizeof(PGOut), cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaMemcpyAsync(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  h->last_launches = 1;
+  if (st != 0) return fail(st, "device-side wait timed out in the projected-gradient kernel");
+  {
+    // algorithmic bytes per pass kind (FP64): W pass = nnzb (72 + 4) + 4 (n + 1); per-contact vector bytes
+    // of each pass as listed in PGOut::phases (3-vectors 24 B, scalars 8 B)
+    const double wpass = (double)h->W.nnzb * 76.0 + 4.0 * (n + 1);
+    const bool spg = o->variant == BOGUS_GPU_PG_SPG;
+    const double per_contact[9] = {56, 48, spg ? 168.0 : 144.0, 152, 80, 72, 144, 120, 96};
+    const bool has_w[9] = {false, true, false, true, false, false, true, false, true};
+    double bytes = 0, fma = 0;
+    unsigned passes = 0;
+    for (int k = 0; k < 9; ++k) {
+      bytes += out.phases[k] * (per_contact[k] * n + (has_w[k] ? wpass : 0.0));
+      if (has_w[k]) {
+        passes += out.phases[k];
+        fma += out.phases[k] * 9.0 * h->W.nnzb * (k == 1 ? 2.0 : 1.0);
+      }
+    }
+    h->last_stats.iterations = out.iters;
+    h->last_stats.w_passes = passes;
+    h->last_stats.algorithmic_bytes = bytes;
+    h->last_stats.fp64_fma = fma;
+  }
+  if (residual) *residual = out.min_res;
+  if (iters) *iters = out.iters;
+  *best = out.best_buf == 3 ? h->XB.p : h->X.p + (size_t)out.best_buf * n3;
+  if (h->callback) {
+    const unsigned count = out.converged ? out.iters + 1 : out.iters;
+    std::vector<double> tr(count);
+    if (count) {
+      BG_CUDA(cudaMemcpy(tr.data(), h->trace.p, sizeof(double) * count, cudaMemcpyDeviceToHost));
+    }
+    for (unsigned k = 0; k < count; ++k) h->callback(k, tr[k], h->callback_user);
+  }
+  return out.converged ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
+}
+
+int check_pg_options(const bogus_gpu_pg_options* o) {
+  if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
+  if (o->variant != BOGUS_GPU_PG_APGD && o->variant != BOGUS_GPU_PG_DESCENT && o->variant != BOGUS_GPU_PG_SPG)
+    return fail(BOGUS_GPU_BAD_INPUT, "projected-gradient variant not available on the GPU (APGD, Descent, SPG)");
+  if (o->ls_iters == 0 && o->variant != BOGUS_GPU_PG_SPG)
+    return fail(BOGUS_GPU_BAD_INPUT, "ls_iters must be >= 1 (the reference reuses an undefined step otherwise)");
+  if (!(o->tol >= 0) || !(o->ls_optimistic_factor > 0) || !(o->ls_pessimistic_factor > 0))
+    return fail(BOGUS_GPU_BAD_INPUT, "invalid projected-gradient factors");
+  return BOGUS_GPU_OK;
+}
+
+// ---- Gauss-Seidel ---------------------------------------------------------------------------------
+int prepare_gs(bogus_gpu_problem* h, double auto_reg) {
+  GSCache& g = h->gs;
+  if (g.valid && g.auto_reg == auto_reg) return BOGUS_GPU_OK;
+  if (!h->host_lower_valid) return fail(BOGUS_GPU_BAD_INPUT, "Gauss-Seidel needs W set from host arrays");
+  const HostBSR& low = h->host_lower;
+  const int n = low.n;
+  greedy_coloring(low, g.perm, g.colors);
+  const HostBSR plow = permute_lower(low, g.perm);
+  const HostBSR pf = expand_lower(n, plow.rowptr.data(), plow.col.data(), plow.val.data());
+  std::vector<double> pb(3 * (size_t)n), pmu(n), local(9 * (size_t)n, 0.0), reg(n, 0.0), sc(n, 1.0);
+  for (int i = 0; i < n; ++i) {
+    const int o = g.perm[i];
+    for (int k = 0; k < 3; ++k) pb[3 * (size_t)i + k] = h->host_b[3 * (size_t)o + k];
+    pmu[i] = h->host_mu[o];
+    for (int k = pf.rowptr[i]; k < pf.rowptr[i + 1]; ++k)
+      if (pf.col[k] == i) std::copy(&pf.val[9 * (size_t)k], &pf.val[9 * (size_t)k] + 9, &local[9 * (size_t)i]);
+    double* D = &local[9 * (size_t)i];
+    sc[i] = dmax(1.0, ((D[0] + D[4]) + D[8]) / 3.0);
+    if (auto_reg > 0.) {
+      reg[i] = dmax(0.0, auto_reg - min_eigen_symmetric3(D));
+      D[0] += reg[i];
+      D[4] += reg[i];
+      D[8] += reg[i];
+    }
+  }
+  const int nnz = pf.nnzb();
+  const int ntiles = (n + kGSTile - 1) / kGSTile;
+  BG_CUDA(g.rowptr.ensure(n + 1));
+  BG_CUDA(g.col.ensure(nnz));
+  BG_CUDA(g.val.ensure(9 * (size_t)nnz));
+  BG_CUDA(g.local.ensure(9 * (size_t)n));
+  BG_CUDA(g.reg.ensure(n));
+  BG_CUDA(g.scaling.ensure(n));
+  BG_CUDA(g.b.ensure(3 * (size_t)n));
+  BG_CUDA(g.mu.ensure(n));
+  BG_CUDA(g.x.ensure(3 * (size_t)n));
+  BG_CUDA(g.xbest.ensure(3 * (size_t)n));
+  BG_CUDA(g.y.ensure(3 * (size_t)n));
+  BG_CUDA(g.nx2.ensure(n));
+  BG_CUDA(g.ndx2.ensure(n));
+  BG_CUDA(g.skip.ensure(n));
+  BG_CUDA(g.processed.ensure(n));
+  BG_CUDA(g.tile_max.ensure(2 * (size_t)(ntiles > 0 ? ntiles : 1)));
+  BG_CUDA(g.ndx_ref.ensure(2));
+  BG_CUDA(g.chunk.ensure((n + 31) / 32 + 1));
+  BG_CUDA(g.scalar.ensure(2));
+  cudaStream_t s = h->stream;
+  BG_CUDA(cudaMemcpyAsync(g.rowptr.p, pf.rowptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+  if (nnz) {
+    BG_CUDA(cudaMemcpyAsync(g.col.p, pf.col.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(g.val.p, pf.val.data(), sizeof(double) * 9 * (size_t)nnz, cudaMemcpyHostToDevice, s));
+  }
+  if (n) {
+    BG_CUDA(cudaMemcpyAsync(g.local.p, local.data(), sizeof(double) * 9 * (size_t)n, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(g.reg.p, reg.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(g.scaling.p, sc.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(g.b.p, pb.data(), sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(g.mu.p, pmu.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  }
+  BG_CUDA(cudaStreamSynchronize(s));
+  g.auto_reg = auto_reg;
+  g.valid = true;
+  return BOGUS_GPU_OK;
+}
+
+// error function of the permuted GS problem at g.x: u = init + W x (init = b) as in solveWithLinearConstraints
+int gs_eval(bogus_gpu_problem* h, const GSArgs& a, const double* xdev, const double* u_init, bool desaxce, bool use_inf,
+            double* err) {
+  GSCache& g = h->gs;
+  const int n = a.n;
+  DevBSR Wp;
+  Wp.n = n;
+  Wp.rowptr = g.rowptr.p;
+  Wp.col = g.col.p;
+  Wp.val = g.val.p;
+  const double* u = u_init;
+  if (xdev) {
+    BG_CUDA(launch_spmv(Wp, xdev, u_init, g.y.p, h->stream));
+    u = g.y.p;
+  }
+  const double* xe = xdev ? xdev : g.y.p;  // x = 0 path handled by caller passing a zero vector
+  BG_CUDA(launch_eval_chunks(n, xe, u, g.mu.p, g.scaling.p, desaxce, use_inf, g.chunk.p, h->stream));
+  BG_CUDA(launch_combine(g.chunk.p, (n + 31) / 32, use_inf, use_inf ? 0.0 : (double)(1 + n), g.scalar.p, h->stream));
+  BG_CUDA(cudaMemcpyAsync(err, g.scalar.p, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  h->last_launches += xdev ? 3 : 2;
+  return BOGUS_GPU_OK;
+}
+
+}  // namespace
+
+// =================================================================================================
+extern "C" {
+
+void bogus_gpu_pg_options_default(bogus_gpu_pg_options* o) {
+  if (!o) return;
+  o->tol = 1.e-6;
+  o->max_iters = 300;
+  o->ls_iters = 8;
+  o->ls_optimistic_factor = 1.25;
+  o->ls_pessimistic_factor = .5;
+  o->ls_armijo_coefficient = .5;
+  o->variant = BOGUS_GPU_PG_APGD;
+  o->use_infinity_norm = 0;
+  o->static_problem = 1;
+}
+
+void bogus_gpu_gs_options_default(bogus_gpu_gs_options* o) {
+  if (!o) return;
+  o->tol = 1.e-6;
+  o->max_iters = 250;
+  o->eval_every = 25;
+  o->skip_tol = 1.e-6;
+  o->skip_iters = 10;
+  o->auto_regularization = 0.;
+  o->try_zero_as_well = 1;
+  o->use_infinity_norm = 0;
+  o->static_problem = 0;
+  o->local_strategy = BOGUS_GPU_LOCAL_REV_HYBRID;
+}
+
+const char* bogus_gpu_status_string(int s) {
+  switch (s) {
+    case BOGUS_GPU_OK: return "ok";
+    case BOGUS_GPU_NOT_CONVERGED: return "not converged";
+    case BOGUS_GPU_BAD_INPUT: return "bad input";
+    case BOGUS_GPU_NONFINITE: return "non-finite input";
+    case BOGUS_GPU_CUDA_ERROR: return "CUDA error";
+    case BOGUS_GPU_TIMEOUT: return "device wait timed out";
+    case BOGUS_GPU_NO_DEVICE: return "no suitable CUDA device";
+    case BOGUS_GPU_NO_PROBLEM: return "no problem set";
+  }
+  return "unknown status";
+}
+
+const char* bogus_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int bogus_gpu_create(int device, bogus_gpu_problem** out) {
+  if (!out) return fail(BOGUS_GPU_BAD_INPUT, "null output pointer");
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return fail(BOGUS_GPU_NO_DEVICE, "no CUDA device");
+  if (device < 0 || device >= count) return fail(BOGUS_GPU_NO_DEVICE, "device index out of range");
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return fail(BOGUS_GPU_NO_DEVICE, "device query failed");
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(BOGUS_GPU_NO_DEVICE, std::string("this library is built for sm_103 (GB300); found ") + prop.name);
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  if (!coop) return fail(BOGUS_GPU_NO_DEVICE, "device lacks cooperative launch");
+  auto* h = new bogus_gpu_problem;
+  h->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
+    delete h;
+    return fail(BOGUS_GPU_CUDA_ERROR, "stream/event creation failed");
+  }
+  *out = h;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_destroy(bogus_gpu_problem* h) {
+  if (!h) return BOGUS_GPU_OK;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  for (auto* b : {&h->val, &h->b, &h->mu, &h->scaling, &h->X, &h->MX, &h->Y, &h->S0, &h->XB, &h->Wv, &h->csum,
+                  &h->scal, &h->trace, &h->vx, &h->vy, &h->chunk, &h->scalar, &h->minv, &h->H, &h->T, &h->mf})
+    b->release();
+  h->rowptr.release();
+  h->col.release();
+  h->diag.release();
+  h->cb.release();
+  h->pgout.release();
+  h->barrier.release();
+  h->status.release();
+  h->gs.release();
+  cudaEventDestroy(h->ev0);
+  cudaEventDestroy(h->ev1);
+  cudaStreamDestroy(h->stream);
+  delete h;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_set_dual(bogus_gpu_problem* h, int n, const int* rowptr, const int* colidx, const double* blocks,
+                       int symmetric_lower, const double* b, const double* mu) {
+  if (int e = check_handle(h)) return e;
+  if (n < 0 || (n > 0 && (!rowptr || !b || !mu))) return fail(BOGUS_GPU_BAD_INPUT, "null input array");
+  if (n > 0 && rowptr[n] > 0 && (!colidx || !blocks)) return fail(BOGUS_GPU_BAD_INPUT, "null block arrays");
+  const std::string err = validate_bsr(n, rowptr, colidx, blocks, symmetric_lower != 0);
+  if (!err.empty()) return fail(err.find("non-finite") != std::string::npos ? BOGUS_GPU_NONFINITE : BOGUS_GPU_BAD_INPUT, err);
+  if (int e = check_finite(b, 3 * (size_t)n, "b")) return e;
+  if (int e = check_finite(mu, n, "mu")) return e;
+  if (int e = set_device(h)) return e;
+  HostBSR full;
+  if (symmetric_lower) {
+    full = expand_lower(n, rowptr, colidx, blocks);
+    h->host_lower.n = n;
+    h->host_lower.rowptr.assign(rowptr, rowptr + n + 1);
+    h->host_lower.col.assign(colidx, colidx + rowptr[n]);
+    h->host_lower.val.assign(blocks, blocks + 9 * (size_t)rowptr[n]);
+  } else {
+    full.n = n;
+    full.rowptr.assign(rowptr, rowptr + n + 1);
+    full.col.assign(colidx, colidx + rowptr[n]);
+    full.val.assign(blocks, blocks + 9 * (size_t)rowptr[n]);
+    h->host_lower = lower_of(full);
+  }
+  h->host_lower_valid = true;
+  h->host_b.assign(b, b + 3 * (size_t)n);
+  h->host_mu.assign(mu, mu + n);
+  return upload_full(h, full, b, mu);
+}
+
+int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* d_rowptr, const int* d_colidx,
+                              const double* d_blocks, const double* d_b, const double* d_mu) {
+  if (int e = check_handle(h)) return e;
+  if (n < 0 || nnzb < 0) return fail(BOGUS_GPU_BAD_INPUT, "negative size");
+  if (int e = set_device(h)) return e;
+  BG_CUDA(h->rowptr.ensure(n + 1));
+  BG_CUDA(h->col.ensure(nnzb));
+  BG_CUDA(h->val.ensure(9 * (size_t)nnzb));
+  BG_CUDA(h->diag.ensure(n));
+  BG_CUDA(h->b.ensure(3 * (size_t)n));
+  BG_CUDA(h->mu.ensure(n));
+  BG_CUDA(h->scaling.ensure(n));
+  cudaStream_t s = h->stream;
+  BG_CUDA(cudaMemcpyAsync(h->rowptr.p, d_rowptr, sizeof(int) * (n + 1), cudaMemcpyDeviceToDevice, s));
+  if (nnzb) {
+    BG_CUDA(cudaMemcpyAsync(h->col.p, d_colidx, sizeof(int) * nnzb, cudaMemcpyDeviceToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->val.p, d_blocks, sizeof(double) * 9 * (size_t)nnzb, cudaMemcpyDeviceToDevice, s));
+  }
+  if (n) {
+    BG_CUDA(cudaMemcpyAsync(h->b.p, d_b, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->mu.p, d_mu, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  }
+  h->W.n = n;
+  h->W.nnzb = nnzb;
+  h->W.rowptr = h->rowptr.p;
+  h->W.col = h->col.p;
+  h->W.val = h->val.p;
+  h->W.diag = h->diag.p;
+  BG_CUDA(launch_diag_and_scaling(h->W, h->scaling.p, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  h->has_dual = true;
+  h->host_lower_valid = false;
+  h->gs.valid = false;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_nnzb(const bogus_gpu_problem* h, int* nnzb) {
+  if (int e = check_handle(h)) return e;
+  if (nnzb) *nnzb = h->W.nnzb;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_set_callback(bogus_gpu_problem* h, bogus_gpu_callback cb, void* user) {
+  if (int e = check_handle(h)) return e;
+  h->callback = cb;
+  h->callback_user = user;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_spmv(bogus_gpu_problem* h, const double* x, double* y) {
+  if (int e = check_handle(h)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (int e = set_device(h)) return e;
+  const size_t n3 = 3 * (size_t)h->W.n;
+  if (n3 == 0) return BOGUS_GPU_OK;
+  BG_CUDA(h->vx.ensure(n3));
+  BG_CUDA(h->vy.ensure(n3));
+  BG_CUDA(cudaMemcpyAsync(h->vx.p, x, sizeof(double) * n3, cudaMemcpyHostToDevice, h->stream));
+  BG_CUDA(launch_spmv(h->W, h->vx.p, nullptr, h->vy.p, h->stream));
+  BG_CUDA(cudaMemcpyAsync(y, h->vy.p, sizeof(double) * n3, cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_eval(bogus_gpu_problem* h, const double* r, int static_problem, int use_inf, double* residual) {
+  if (int e = check_handle(h)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (int e = set_device(h)) return e;
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  if (n == 0) {
+    if (residual) *residual = 0.0;
+    return BOGUS_GPU_OK;
+  }
+  BG_CUDA(h->vx.ensure(n3));
+  BG_CUDA(h->vy.ensure(n3));
+  BG_CUDA(h->chunk.ensure((n + 31) / 32));
+  BG_CUDA(h->scalar.ensure(2));
+  BG_CUDA(cudaMemcpyAsync(h->vx.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, h->stream));
+  BG_CUDA(launch_spmv(h->W, h->vx.p, nullptr, h->vy.p, h->stream));
+  BG_CUDA(launch_add((int)n3, h->vy.p, h->b.p, h->vy.p, h->stream));
+  BG_CUDA(launch_eval_chunks(n, h->vx.p, h->vy.p, h->mu.p, h->scaling.p, !static_problem, use_inf != 0, h->chunk.p,
+                             h->stream));
+  BG_CUDA(launch_combine(h->chunk.p, (n + 31) / 32, use_inf != 0, use_inf ? 0.0 : (double)(1 + n), h->scalar.p,
+                         h->stream));
+  double v = 0;
+  BG_CUDA(cudaMemcpyAsync(&v, h->scalar.p, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  if (residual) *residual = v;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_solve_pg_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* d_r, double* residual,
+                              unsigned* iters) {
+  if (int e = check_handle(h)) return e;
+  if (int e = check_pg_options(o)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (int e = set_device(h)) return e;
+  const size_t n3 = 3 * (size_t)h->W.n;
+  if (n3 == 0) {
+    if (residual) *residual = 0.0;
+    if (iters) *iters = 0;
+    return BOGUS_GPU_OK;
+  }
+  if (int e = ensure_pg_work(h, o->max_iters)) return e;
+  BG_CUDA(cudaMemcpyAsync(h->X.p, d_r, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+  const double* best = nullptr;
+  const int st = run_pg(h, o, residual, iters, &best);
+  if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+  BG_CUDA(cudaMemcpyAsync(d_r, best, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  return st;
+}
+
+int bogus_gpu_solve_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, double* residual,
+                       unsigned* iters) {
+  if (int e = check_handle(h)) return e;
+  if (int e = check_pg_options(o)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (int e = set_device(h)) return e;
+  const size_t n3 = 3 * (size_t)h->W.n;
+  if (n3 == 0) {
+    if (residual) *residual = 0.0;
+    if (iters) *iters = 0;
+    return BOGUS_GPU_OK;
+  }
+  if (int e = check_finite(r, n3, "r")) return e;
+  if (int e = ensure_pg_work(h, o->max_iters)) return e;
+  BG_CUDA(cudaMemcpyAsync(h->X.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, h->stream));
+  const double* best = nullptr;
+  const int st = run_pg(h, o, residual, iters, &best);
+  if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+  BG_CUDA(cudaMemcpyAsync(r, best, sizeof(double) * n3, cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  return st;
+}
+
+int bogus_gpu_coloring(bogus_gpu_problem* h, int* perm, int* colors, int* ncolors) {
+  if (int e = check_handle(h)) return e;
+  if (!h->host_lower_valid) return fail(BOGUS_GPU_BAD_INPUT, "coloring needs W set from host arrays");
+  std::vector<int> p, c;
+  greedy_coloring(h->host_lower, p, c);
+  if (perm) std::memcpy(perm, p.data(), sizeof(int) * p.size());
+  if (colors) std::memcpy(colors, c.data(), sizeof(int) * c.size());
+  if (ncolors) *ncolors = (int)c.size() - 1;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* r, double* residual,
+                       unsigned* iters) {
+  if (int e = check_handle(h)) return e;
+  if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (o->eval_every == 0) return fail(BOGUS_GPU_BAD_INPUT, "eval_every must be >= 1");
+  if (o->local_strategy < 0 || o->local_strategy > 3) return fail(BOGUS_GPU_BAD_INPUT, "unknown local strategy");
+  if (int e = set_device(h)) return e;
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  if (n == 0) {
+    if (residual) *residual = 0.0;
+    if (iters) *iters = 0;
+    return BOGUS_GPU_OK;
+  }
+  if (int e = check_finite(r, n3, "r")) return e;
+  if (int e = prepare_gs(h, o->auto_regularization)) return e;
+  GSCache& g = h->gs;
+  cudaStream_t s = h->stream;
+  h->last_launches = 0;
+  // r in the permuted (color-contiguous) order
+  std::vector<double> pr(n3);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) pr[3 * (size_t)i + k] = r[3 * (size_t)g.perm[i] + k];
+  BG_CUDA(cudaMemcpyAsync(g.x.p, pr.data(), sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  const int ntiles = (n + kGSTile - 1) / kGSTile;
+  BG_CUDA(cudaMemsetAsync(g.tile_max.p, 0, sizeof(unsigned long long) * 2 * ntiles, s));
+  BG_CUDA(cudaMemsetAsync(g.ndx_ref.p, 0, sizeof(double) * 2, s));
+  BG_CUDA(cudaMemsetAsync(g.skip.p, 0, n, s));
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  GSArgs a{};
+  a.n = n;
+  a.rowptr = g.rowptr.p;
+  a.col = g.col.p;
+  a.val = g.val.p;
+  a.local = g.local.p;
+  a.reg = g.reg.p;
+  a.scaling = g.scaling.p;
+  a.b = g.b.p;
+  a.mu = g.mu.p;
+  a.x = g.x.p;
+  a.nx2 = g.nx2.p;
+  a.ndx2 = g.ndx2.p;
+  a.skip = g.skip.p;
+  a.processed = g.processed.p;
+  a.tile_max = g.tile_max.p;
+  a.ndx_ref = g.ndx_ref.p;
+  a.desaxce = o->static_problem ? 0 : 1;
+  a.strat = o->local_strategy;
+  const bool desaxce = !o->static_problem;
+  const bool use_inf = o->use_infinity_norm != 0;
+  // initial evaluation and tryZero (GaussSeidel.impl.hpp:152-167)
+  double err_best = DBL_MAX;
+  bool has_best = false;
+  double err = 0;
+  if (int e = gs_eval(h, a, g.x.p, g.b.p, desaxce, use_inf, &err)) return e;
+  if (err < err_best) {
+    BG_CUDA(cudaMemcpyAsync(g.xbest.p, g.x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+    err_best = err;
+    has_best = true;
+  }
+  if (o->try_zero_as_well) {
+    // eval(law, b, 0): u = b, x = 0
+    BG_CUDA(cudaMemsetAsync(g.y.p, 0, sizeof(double) * n3, s));
+    BG_CUDA(launch_eval_chunks(n, g.y.p, g.b.p, g.mu.p, g.scaling.p, desaxce, use_inf, g.chunk.p, s));
+    BG_CUDA(launch_combine(g.chunk.p, (n + 31) / 32, use_inf, use_inf ? 0.0 : (double)(1 + n), g.scalar.p, s));
+    double err_zero = 0;
+    BG_CUDA(cudaMemcpyAsync(&err_zero, g.scalar.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+    h->last_launches += 2;
+    if (err_zero < err_best) {
+      err_best = err_zero;
+      BG_CUDA(cudaMemsetAsync(g.xbest.p, 0, sizeof(double) * n3, s));
+      BG_CUDA(cudaMemsetAsync(g.x.p, 0, sizeof(double) * n3, s));
+      has_best = true;
+    } else if (has_best) {
+      BG_CUDA(cudaMemcpyAsync(g.x.p, g.xbest.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  std::vector<std::pair<unsigned, double>> trace;
+  trace.push_back({0u, err_best});
+  const double abs_skip_tol = dmin(o->skip_tol, o->tol);
+  const int abs_skip_iters = (int)dmin((double)o->skip_iters, (double)(unsigned)std::sqrt((double)n));
+  const int ncolors = (int)g.colors.size() - 1;
+  unsigned it;
+  int parity = 0;
+  bool converged = false;
+  for (it = 1; it <= o->max_iters; ++it) {
+    for (int c = 0; c < ncolors; ++c) BG_CUDA(launch_gs_color(a, g.colors[c], g.colors[c + 1], parity, s));
+    BG_CUDA(launch_gs_skip(a, parity, abs_skip_tol, o->skip_tol, abs_skip_iters, s));
+    h->last_launches += ncolors + 1;
+    parity ^= 1;
+    if (0 == (it % o->eval_every)) {
+      if (int e = gs_eval(h, a, g.x.p, g.b.p, desaxce, use_inf, &err)) return e;
+      if (err < err_best) {
+        BG_CUDA(cudaMemcpyAsync(g.xbest.p, g.x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+        err_best = err;
+        has_best = true;
+      }
+      trace.push_back({it, err});
+      if (err < o->tol) {
+        converged = true;
+        break;
+      }
+      BG_CUDA(launch_scale_scalar(g.ndx_ref.p + parity, (double)o->eval_every, s));
+      h->last_launches += 1;
+    }
+  }
+  const double* result = g.x.p;
+  if (it > o->max_iters && has_best) result = g.xbest.p;
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  BG_CUDA(cudaMemcpyAsync(pr.data(), result, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) r[3 * (size_t)g.perm[i] + k] = pr[3 * (size_t)i + k];
+  if (residual) *residual = err_best;
+  if (iters) *iters = it > o->max_iters ? o->max_iters : it;
+  if (h->callback)
+    for (auto& t : trace) h->callback(t.first, t.second, h->callback_user);
+  return converged ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
+}
+
+// ---- primal data and Delassus assembly ---------------------------------------------------------------
+int bogus_gpu_set_primal(bogus_gpu_problem* h, int nbodies, int ndof, const double* minv, int ncontacts, const int* objA,
+                         const int* objB, const double* HA, const double* HB) {
+  if (int e = check_handle(h)) return e;
+  if (nbodies <= 0 || ndof <= 0 || ndof > 12 || ncontacts < 0) return fail(BOGUS_GPU_BAD_INPUT, "invalid primal sizes");
+  if (!minv || (ncontacts > 0 && (!objA || !objB || !HA || !HB))) return fail(BOGUS_GPU_BAD_INPUT, "null primal array");
+  if (int e = check_finite(minv, (size_t)nbodies * ndof * ndof, "minv")) return e;
+  if (int e = check_finite(HA, (size_t)ncontacts * 3 * ndof, "HA")) return e;
+  if (int e = check_finite(HB, (size_t)ncontacts * 3 * ndof, "HB")) return e;
+  std::vector<int> cbh(2 * (size_t)ncontacts);
+  std::vector<double> Hh(2 * (size_t)ncontacts * 3 * ndof, 0.0);
+  const size_t hs = 3 * (size_t)ndof;
+  for (int i = 0; i < ncontacts; ++i) {
+    const int a = objA[i], b = objB[i];
+    if (a < 0 || a >= nbodies || b < -1 || b >= nbodies) return fail(BOGUS_GPU_BAD_INPUT, "body index out of range");
+    // slots ordered by body index; a repeated body counts once (slot A)
+    int s0 = a, s1 = -1;
+    const double* h0 = HA + i * hs;
+    const double* h1 = nullptr;
+    if (b >= 0 && b != a) {
+      if (b < a) {
+        s0 = b; s1 = a; h0 = HB + i * hs; h1 = HA + i * hs;
+      } else {
+        s1 = b; h1 = HB + i * hs;
+      }
+    }
+    cbh[2 * (size_t)i] = s0;
+    cbh[2 * (size_t)i + 1] = s1;
+    std::copy(h0, h0 + hs, &Hh[(2 * (size_t)i) * hs]);
+    if (h1) std::copy(h1, h1 + hs, &Hh[(2 * (size_t)i + 1) * hs]);
+  }
+  if (int e = set_device(h)) return e;
+  BG_CUDA(h->minv.ensure((size_t)nbodies * ndof * ndof));
+  BG_CUDA(h->H.ensure(Hh.size()));
+  BG_CUDA(h->cb.ensure(cbh.size()));
+  BG_CUDA(cudaMemcpyAsync(h->minv.p, minv, sizeof(double) * nbodies * ndof * ndof, cudaMemcpyHostToDevice, h->stream));
+  if (ncontacts) {
+    BG_CUDA(cudaMemcpyAsync(h->H.p, Hh.data(), sizeof(double) * Hh.size(), cudaMemcpyHostToDevice, h->stream));
+    BG_CUDA(cudaMemcpyAsync(h->cb.p, cbh.data(), sizeof(int) * cbh.size(), cudaMemcpyHostToDevice, h->stream));
+  }
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  h->nbodies = nbodies;
+  h->ndof = ndof;
+  h->ncontacts = ncontacts;
+  h->h_cb = std::move(cbh);
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double* w, const double* mu) {
+  if (int e = check_handle(h)) return e;
+  if (h->ncontacts == 0 && h->nbodies == 0) return fail(BOGUS_GPU_NO_PROBLEM, "no primal problem set");
+  if (!w || !mu) return fail(BOGUS_GPU_BAD_INPUT, "null w or mu");
+  if (int e = set_device(h)) return e;
+  const int n = h->ncontacts, nb = h->nbodies, d = h->ndof;
+  if (int e = check_finite(w, 3 * (size_t)n, "w")) return e;
+  if (int e = check_finite(mu, n, "mu")) return e;
+  if (f)
+    if (int e = check_finite(f, (size_t)nb * d, "f")) return e;
+  // symbolic part: lower blocks (i, j <= i) of contacts sharing a body, shared (slot_i, slot_j) pairs
+  std::vector<std::vector<int>> by_body(nb);
+  for (int i = 0; i < n; ++i)
+    for (int t = 0; t < 2; ++t)
+      if (h->h_cb[2 * (size_t)i + t] >= 0) by_body[h->h_cb[2 * (size_t)i + t]].push_back(i);
+  HostBSR low;
+  low.n = n;
+  low.rowptr.assign(n + 1, 0);
+  std::vector<int> li, lj, pair_off(1, 0), pair_ti, pair_tj, cols;
+  for (int i = 0; i < n; ++i) {
+    cols.clear();
+    for (int t = 0; t < 2; ++t) {
+      const int k = h->h_cb[2 * (size_t)i + t];
+      if (k < 0) continue;
+      for (int j : by_body[k])
+        if (j <= i) cols.push_back(j);
+    }
+    std::sort(cols.begin(), cols.end());
+    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+    for (int j : cols) {
+      li.push_back(i);
+      lj.push_back(j);
+      for (int ti = 0; ti < 2; ++ti)
+        for (int tj = 0; tj < 2; ++tj) {
+          const int bi = h->h_cb[2 * (size_t)i + ti], bj = h->h_cb[2 * (size_t)j + tj];
+          if (bi >= 0 && bi == bj) {
+            pair_ti.push_back(ti);
+            pair_tj.push_back(tj);
+          }
+        }
+      pair_off.push_back((int)pair_ti.size());
+      low.col.push_back(j);
+    }
+    low.rowptr[i + 1] = (int)low.col.size();
+  }
+  const int nlow = (int)li.size();
+  // full-structure positions of every lower block and of its transpose
+  HostBSR fullpat;
+  fullpat.n = n;
+  {
+    std::vector<int> cnt(n + 1, 0);
+    for (int k = 0; k < nlow; ++k) {
+      ++cnt[li[k] + 1];
+      if (lj[k] != li[k]) ++cnt[lj[k] + 1];
+    }
+    fullpat.rowptr.assign(n + 1, 0);
+    for (int i = 0; i < n; ++i) fullpat.rowptr[i + 1] = fullpat.rowptr[i] + cnt[i + 1];
+  }
+  std::vector<int> pos_ij(nlow), pos_ji(nlow, -1);
+  fullpat.col.assign(fullpat.rowptr[n], 0);
+  {
+    std::vector<int> pos(fullpat.rowptr.begin(), fullpat.rowptr.end() - 1);
+    for (int k = 0; k < nlow; ++k) {  // lower blocks come row by row, columns increasing
+      pos_ij[k] = pos[li[k]]++;
+      fullpat.col[pos_ij[k]] = lj[k];
+      if (lj[k] != li[k]) {
+        pos_ji[k] = pos[lj[k]]++;
+        fullpat.col[pos_ji[k]] = li[k];
+      }
+    }
+  }
+  const int nnz = fullpat.rowptr[n];
+  DevBuf<int> d_li, d_lj, d_off, d_ti, d_tj, d_pij, d_pji;
+  BG_CUDA(d_li.ensure(nlow)); BG_CUDA(d_lj.ensure(nlow)); BG_CUDA(d_off.ensure(nlow + 1));
+  BG_CUDA(d_ti.ensure(pair_ti.size())); BG_CUDA(d_tj.ensure(pair_tj.size()));
+  BG_CUDA(d_pij.ensure(nlow)); BG_CUDA(d_pji.ensure(nlow));
+  cudaStream_t s = h->stream;
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
+  };
+  BG_CUDA(up(d_li.p, li.data(), sizeof(int) * nlow));
+  BG_CUDA(up(d_lj.p, lj.data(), sizeof(int) * nlow));
+  BG_CUDA(up(d_off.p, pair_off.data(), sizeof(int) * (nlow + 1)));
+  BG_CUDA(up(d_ti.p, pair_ti.data(), sizeof(int) * pair_ti.size()));
+  BG_CUDA(up(d_tj.p, pair_tj.data(), sizeof(int) * pair_tj.size()));
+  BG_CUDA(up(d_pij.p, pos_ij.data(), sizeof(int) * nlow));
+  BG_CUDA(up(d_pji.p, pos_ji.data(), sizeof(int) * nlow));
+  BG_CUDA(h->rowptr.ensure(n + 1));
+  BG_CUDA(h->col.ensure(nnz));
+  BG_CUDA(h->val.ensure(9 * (size_t)nnz));
+  BG_CUDA(h->diag.ensure(n));
+  BG_CUDA(h->b.ensure(3 * (size_t)n));
+  BG_CUDA(h->mu.ensure(n));
+  BG_CUDA(h->scaling.ensure(n));
+  BG_CUDA(h->T.ensure(2 * (size_t)n * d * 3));
+  BG_CUDA(h->mf.ensure((size_t)nb * d));
+  BG_CUDA(up(h->rowptr.p, fullpat.rowptr.data(), sizeof(int) * (n + 1)));
+  BG_CUDA(up(h->col.p, fullpat.col.data(), sizeof(int) * nnz));
+  BG_CUDA(up(h->mu.p, mu, sizeof(double) * n));
+  DevBuf<double> d_w, d_f;
+  BG_CUDA(d_w.ensure(3 * (size_t)n));
+  BG_CUDA(up(d_w.p, w, sizeof(double) * 3 * n));
+  if (f) {
+    BG_CUDA(d_f.ensure((size_t)nb * d));
+    BG_CUDA(up(d_f.p, f, sizeof(double) * nb * d));
+  }
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  BG_CUDA(launch_assembly_T(n, d, h->minv.p, h->cb.p, h->H.p, h->T.p, s));
+  BG_CUDA(launch_assembly_W(nlow, d, d_li.p, d_lj.p, d_off.p, d_ti.p, d_tj.p, h->H.p, h->T.p, d_pij.p, d_pji.p,
+                            h->val.p, s));
+  BG_CUDA(launch_assembly_b(n, nb, d, h->minv.p, f ? d_f.p : nullptr, h->cb.p, h->H.p, d_w.p, h->mf.p, h->b.p, s));
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  h->W.n = n;
+  h->W.nnzb = nnz;
+  h->W.rowptr = h->rowptr.p;
+  h->W.col = h->col.p;
+  h->W.val = h->val.p;
+  h->W.diag = h->diag.p;
+  BG_CUDA(launch_diag_and_scaling(h->W, h->scaling.p, s));
+  // host copies for the Gauss-Seidel coloring / permutation
+  low.val.resize(9 * (size_t)nlow);
+  std::vector<double> fullval(9 * (size_t)nnz);
+  if (nnz) BG_CUDA(cudaMemcpyAsync(fullval.data(), h->val.p, sizeof(double) * 9 * (size_t)nnz, cudaMemcpyDeviceToHost, s));
+  h->host_b.resize(3 * (size_t)n);
+  if (n) BG_CUDA(cudaMemcpyAsync(h->host_b.data(), h->b.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  h->last_launches = 3;
+  for (int k = 0; k < nlow; ++k) std::copy(&fullval[9 * (size_t)pos_ij[k]], &fullval[9 * (size_t)pos_ij[k]] + 9, &low.val[9 * (size_t)k]);
+  h->host_lower = std::move(low);
+  h->host_lower_valid = true;
+  h->host_mu.assign(mu, mu + n);
+  d_li.release(); d_lj.release(); d_off.release(); d_ti.release(); d_tj.release(); d_pij.release(); d_pji.release();
+  d_w.release(); d_f.release();
+  h->has_dual = true;
+  h->gs.valid = false;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_get_dual_lower(bogus_gpu_problem* h, int* rowptr, int* colidx, double* blocks, int* nnzb_lower) {
+  if (int e = check_handle(h)) return e;
+  if (!h->host_lower_valid) return fail(BOGUS_GPU_NO_PROBLEM, "no host copy of W");
+  const HostBSR& l = h->host_lower;
+  if (nnzb_lower) *nnzb_lower = l.nnzb();
+  if (rowptr) std::memcpy(rowptr, l.rowptr.data(), sizeof(int) * (l.n + 1));
+  if (colidx) std::memcpy(colidx, l.col.data(), sizeof(int) * l.nnzb());
+  if (blocks) std::memcpy(blocks, l.val.data(), sizeof(double) * 9 * (size_t)l.nnzb());
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_get_solve_stats(const bogus_gpu_problem* h, bogus_gpu_solve_stats* out) {
+  if (int e = check_handle(h)) return e;
+  if (!out) return fail(BOGUS_GPU_BAD_INPUT, "null output");
+  *out = h->last_stats;
+  out->device_ms = h->last_ms;
+  out->kernel_launches = h->last_launches;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_get_stream(const bogus_gpu_problem* h, void** stream) {
+  if (int e = check_handle(h)) return e;
+  if (!stream) return fail(BOGUS_GPU_BAD_INPUT, "null output");
+  *stream = (void*)h->stream;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_measure_fp64_peak(int device, double* tflops) {
+  if (!tflops) return fail(BOGUS_GPU_BAD_INPUT, "null output");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
+    return fail(BOGUS_GPU_NO_DEVICE, "no such CUDA device");
+  BG_CUDA(measure_fp64_peak(device, tflops));
+  return BOGUS_GPU_OK;
+}
+
+}  // extern "C"

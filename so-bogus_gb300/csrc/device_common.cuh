@@ -1,0 +1,147 @@
+// Device building blocks shared by the solver kernels: cache-hinted loads, the canonical reduction of
+// per-contact values, and a bounded grid barrier for the persistent (cooperative) solver kernels.
+#pragma once
+
+#include <cstdint>
+
+#include "bogus_gpu.h"
+
+namespace bogus_gpu {
+
+constexpr int kWarp = 32;
+
+// Loads of data written earlier in the same kernel by other CTAs must bypass L1 (it is not coherent).
+__device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+// W streams through once per pass; keep it from evicting the L2-resident vectors.
+__device__ __forceinline__ double ldcs(const double* p) { return __ldcs(p); }
+__device__ __forceinline__ int ldcs(const int* p) { return __ldcs(p); }
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_relaxed_i32(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ unsigned long long global_timer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Canonical chunk reduction: lane l of a warp holds value l of a 32-contact chunk; xor butterfly.
+__device__ __forceinline__ double warp_sum_butterfly(double v) {
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+__device__ __forceinline__ double warp_max_butterfly(double v) {
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    const double o = __shfl_xor_sync(0xffffffffu, v, off);
+    v = (v < o) ? o : v;
+  }
+  return v;
+}
+
+// Second stage of the canonical reduction, executed by one CTA of exactly 8 warps: chunk sums are
+// split into 8 stripes of ceil(C/8) chunks; warp k reduces stripe k (lane l sums chunks start+l,
+// start+l+32, ... sequentially, then a butterfly), and the 8 stripe sums are added left to right.
+// is_max selects the max-combination (infinity norm). Every thread returns the total.
+__device__ __forceinline__ double block8_combine(const double* s, int C, bool is_max, double* smem8) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int per = (C + 7) / 8;
+  const int b = warp * per;
+  const int e = min(C, b + per);
+  double p = 0.0;
+  if (is_max) {
+    for (int c = b + lane; c < e; c += 32) {
+      const double v = ldcg(s + c);
+      p = (v < p) ? p : v;
+    }
+    p = warp_max_butterfly(p);
+  } else {
+    for (int c = b + lane; c < e; c += 32) p = p + ldcg(s + c);
+    p = warp_sum_butterfly(p);
+  }
+  if (lane == 0) smem8[warp] = p;
+  __syncthreads();
+  double total = smem8[0];
+  for (int k = 1; k < 8; ++k) {
+    const double q = smem8[k];
+    total = is_max ? ((q < total) ? total : q) : total + q;
+  }
+  __syncthreads();
+  return total;
+}
+
+// Bounded grid barrier for cooperative launches. The last CTA to arrive runs `last_fn` (with all its
+// threads) before releasing the others, so final reductions cost one CTA's work, not a second barrier.
+// Every wait is bounded: after kBarrierTimeoutNs the waiting CTA records BOGUS_GPU_TIMEOUT in *status and
+// returns false; a CTA that sees a non-zero status also returns false. All threads of a CTA get the
+// same return value.
+constexpr unsigned long long kBarrierTimeoutNs = 4000000000ull;
+
+struct GridBarrier {
+  unsigned* count;
+  unsigned* gen;
+  int* status;
+};
+
+template <class LastFn>
+__device__ __forceinline__ bool grid_barrier(const GridBarrier& gb, LastFn&& last_fn) {
+  __shared__ int s_last, s_ok;
+  __shared__ unsigned s_gen;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned my_gen = ld_acquire_u32(gb.gen);
+    s_gen = my_gen;
+    const unsigned prev = atom_add_acq_rel_u32(gb.count, 1u);
+    s_last = (prev == gridDim.x - 1) ? 1 : 0;
+    s_ok = 1;
+    if (!s_last) {
+      const unsigned long long t0 = global_timer_ns();
+      unsigned spins = 0;
+      while (ld_acquire_u32(gb.gen) == my_gen) {
+        if (ld_relaxed_i32(gb.status) != 0) { s_ok = 0; break; }
+        if ((++spins & 255u) == 0 && global_timer_ns() - t0 > kBarrierTimeoutNs) {
+          atomicCAS(gb.status, 0, (int)BOGUS_GPU_TIMEOUT);
+          s_ok = 0;
+          break;
+        }
+        __nanosleep(40);
+      }
+    }
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    last_fn();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      *gb.count = 0u;
+      __threadfence();
+      st_release_u32(gb.gen, s_gen + 1u);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_ok = (s_ok != 0 && ld_relaxed_i32(gb.status) == 0) ? 1 : 0;
+  __syncthreads();
+  const bool ok = s_ok != 0;
+  __syncthreads();
+  return ok;
+}
+
+}  // namespace bogus_gpu

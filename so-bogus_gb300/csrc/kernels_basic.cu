@@ -1,0 +1,179 @@
+// Stand-alone kernels: 3x3-block SpMV, error function, reductions and small vector helpers.
+//
+// SpMV order (canonical, shared by every kernel and by the CPU oracle): row i accumulates its blocks in
+// increasing column order; for each block, component r runs the chain
+//   acc_r = fma(B[r][0], x0, acc_r); acc_r = fma(B[r][1], x1, acc_r); acc_r = fma(B[r][2], x2, acc_r)
+// starting from 0 (y = W x) or from init_i (y = init + W x). Run sequentially, the reference's symmetric
+// product (Core/Block/SparseMatrixVectorProduct.impl.hpp:89-175) visits row i's columns in this order.
+#include "internal.h"
+#include "soc_device.cuh"
+
+namespace bogus_gpu {
+
+__device__ __forceinline__ void block_accumulate(const double* __restrict__ B, double x0, double x1, double x2,
+                                                 double* acc) {
+  double b[9];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) b[e] = ldcs(B + e);
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    double a = acc[r];
+    a = fma(b[3 * r + 0], x0, a);
+    a = fma(b[3 * r + 1], x1, a);
+    a = fma(b[3 * r + 2], x2, a);
+    acc[r] = a;
+  }
+}
+
+__global__ void k_spmv(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                       const double* __restrict__ val, const double* __restrict__ x, const double* __restrict__ init,
+                       double* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double acc[3] = {0.0, 0.0, 0.0};
+  if (init) {
+    acc[0] = init[3 * i];
+    acc[1] = init[3 * i + 1];
+    acc[2] = init[3 * i + 2];
+  }
+  const int k1 = __ldg(rowptr + i + 1);
+  for (int k = __ldg(rowptr + i); k < k1; ++k) {
+    const int j = ldcs(col + k);
+    block_accumulate(val + 9 * (size_t)k, __ldg(x + 3 * j), __ldg(x + 3 * j + 1), __ldg(x + 3 * j + 2), acc);
+  }
+  y[3 * i] = acc[0];
+  y[3 * i + 1] = acc[1];
+  y[3 * i + 2] = acc[2];
+}
+
+cudaError_t launch_spmv(const DevBSR& W, const double* x, const double* init, double* y, cudaStream_t s) {
+  if (W.n == 0) return cudaSuccess;
+  k_spmv<<<(W.n + 255) / 256, 256, 0, s>>>(W.n, W.rowptr, W.col, W.val, x, init, y);
+  return cudaGetLastError();
+}
+
+// First stage of the error function (ConstrainedSolverBase::eval): per-contact law residual at
+// (scaling_i x_i, u_i), reduced per 32-contact chunk by the canonical butterfly (or max).
+__global__ void k_eval_chunks(int n, const double* __restrict__ x, const double* __restrict__ u,
+                              const double* __restrict__ mu, const double* __restrict__ scaling, int desaxce,
+                              int use_inf, double* __restrict__ chunk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (i < n) {
+    const double s = scaling[i];
+    const double lx[3] = {x[3 * i] * s, x[3 * i + 1] * s, x[3 * i + 2] * s};
+    const double lu[3] = {u[3 * i], u[3 * i + 1], u[3 * i + 2]};
+    v = law_eval(desaxce != 0, mu[i], lx, lu);
+  }
+  v = use_inf ? warp_max_butterfly(v) : warp_sum_butterfly(v);
+  if ((threadIdx.x & 31) == 0 && i - (int)(threadIdx.x & 31) < n) chunk[i >> 5] = v;
+}
+
+cudaError_t launch_eval_chunks(int n, const double* x, const double* u, const double* mu, const double* scaling,
+                               bool desaxce, bool use_inf, double* chunk, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int nt = ((n + 31) / 32) * 32;
+  k_eval_chunks<<<(nt + 255) / 256, 256, 0, s>>>(n, x, u, mu, scaling, desaxce ? 1 : 0, use_inf ? 1 : 0, chunk);
+  return cudaGetLastError();
+}
+
+// Second stage: one CTA of 8 warps; out = total (or total / scale_div when scale_div > 0).
+__global__ void __launch_bounds__(256) k_combine(const double* chunk, int nchunks, int is_max, double scale_div,
+                                                 double* out) {
+  __shared__ double smem8[8];
+  const double t = block8_combine(chunk, nchunks, is_max != 0, smem8);
+  if (threadIdx.x == 0) *out = scale_div > 0.0 ? t / scale_div : t;
+}
+
+cudaError_t launch_combine(const double* chunk, int nchunks, bool is_max, double scale_div, double* out,
+                           cudaStream_t s) {
+  k_combine<<<1, 256, 0, s>>>(chunk, nchunks, is_max ? 1 : 0, scale_div, out);
+  return cudaGetLastError();
+}
+
+// Diagonal block positions and the solver scalings max(1, trace(W_ii)/3)
+// (ConstrainedSolverBase.impl.hpp:78-118; 1 when the diagonal block is absent).
+__global__ void k_diag_scaling(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                               const double* __restrict__ val, int* __restrict__ diag, double* __restrict__ scaling) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int p = -1;
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
+    if (col[k] == i) { p = k; break; }
+  diag[i] = p;
+  double s = 1.0;
+  if (p >= 0) {
+    const double* B = val + 9 * (size_t)p;
+    s = dmax(1.0, ((B[0] + B[4]) + B[8]) / 3.0);
+  }
+  scaling[i] = s;
+}
+
+cudaError_t launch_diag_and_scaling(const DevBSR& W, double* scaling, cudaStream_t s) {
+  if (W.n == 0) return cudaSuccess;
+  k_diag_scaling<<<(W.n + 255) / 256, 256, 0, s>>>(W.n, W.rowptr, W.col, W.val, W.diag, scaling);
+  return cudaGetLastError();
+}
+
+__global__ void k_add(int m, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ y) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < m) y[k] = a[k] + b[k];
+}
+
+cudaError_t launch_add(int m, const double* a, const double* b, double* y, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  k_add<<<(m + 255) / 256, 256, 0, s>>>(m, a, b, y);
+  return cudaGetLastError();
+}
+
+__global__ void k_scale_scalar(double* p, double divisor) { *p = *p / divisor; }
+
+cudaError_t launch_scale_scalar(double* p, double divisor, cudaStream_t s) {
+  k_scale_scalar<<<1, 1, 0, s>>>(p, divisor);
+  return cudaGetLastError();
+}
+
+// FP64 FMA throughput: eight independent chains per thread, enough warps to fill every SM.
+__global__ void k_fp64_peak(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3 + k;
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+cudaError_t measure_fp64_peak(int device, double* tflops) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return e;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  const int nb = sms * 8, nt = 256, iters = 2048;
+  double* out = nullptr;
+  if ((e = cudaMalloc(&out, sizeof(double) * nb * nt)) != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(e0);
+    k_fp64_peak<<<nb, nt>>>(out, iters, 0.999, 1e-3);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *tflops = 2.0 * 8.0 * iters * (double)nb * nt / (best * 1e-3) / 1e12;
+  return e;
+}
+
+}  // namespace bogus_gpu

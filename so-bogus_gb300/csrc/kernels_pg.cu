@@ -1,0 +1,445 @@
+// Persistent projected-gradient solvers: the whole solve of PgMethod<APGD / Descent / SPG>
+// (Core/BlockSolvers/ProjectedGradient.impl.hpp:74-155, 288-351) runs in one cooperative launch.
+//
+// Work split: warp w of the grid owns the 32-contact chunks w, w + W, w + 2W, ... in every phase, lane l
+// contact 32c + l. A phase is one pass over the contacts (row-local vector work) or over W (SpMV with the
+// row-local work fused into its epilogue). Global dot products are reduced in the canonical order: a
+// butterfly per chunk inside the warp, then the 8-stripe combination run by the last CTA to reach the
+// grid barrier, which publishes the scalars; every CTA then takes the same line-search / momentum
+// decisions on identical values. Waits are bounded (grid_barrier), so a fault elsewhere ends the kernel
+// with BOGUS_GPU_TIMEOUT instead of a hang.
+//
+// Phases of one APGD iteration (reference line numbers in ProjectedGradient.impl.hpp):
+//   A   y = Mx + b, residual (:110-111), s = COV(y), y += s, J (:113-115), xs = P(x - a y) (:123-125)
+//   C   Mxs = W xs; Js, y.(xs-x), |xs-x|^2 (:127-132), (xs-prev).y (:135) ............ barrier+reduce
+//   B   line-search retry: xs = P(x - a y) ............................................ barrier
+//   D   momentum x = xs + beta (xs - prev) (:137-139) .................................. barrier
+//   E+A Mx = W x (:141) fused with A of the next iteration ............................. barrier+reduce
+// Without momentum x = xs and Mx = Mxs are buffer swaps and A runs as its own pass.
+#include "internal.h"
+#include "soc_device.cuh"
+
+namespace bogus_gpu {
+
+namespace {
+
+__device__ __forceinline__ void load3cg(const double* p, int i, double* v) {
+  v[0] = ldcg(p + 3 * i);
+  v[1] = ldcg(p + 3 * i + 1);
+  v[2] = ldcg(p + 3 * i + 2);
+}
+__device__ __forceinline__ void store3(double* p, int i, const double* v) {
+  p[3 * i] = v[0];
+  p[3 * i + 1] = v[1];
+  p[3 * i + 2] = v[2];
+}
+
+__device__ __forceinline__ void spmv_row(const PGArgs& a, int i, const double* __restrict__ x, double* acc) {
+  const int k1 = __ldg(a.rowptr + i + 1);
+  for (int k = __ldg(a.rowptr + i); k < k1; ++k) {
+    const int j = ldcs(a.col + k);
+    const double x0 = ldcg(x + 3 * j), x1 = ldcg(x + 3 * j + 1), x2 = ldcg(x + 3 * j + 2);
+    const double* B = a.val + 9 * (size_t)k;
+    double b[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) b[e] = ldcs(B + e);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      double s = acc[r];
+      s = fma(b[3 * r + 0], x0, s);
+      s = fma(b[3 * r + 1], x1, s);
+      s = fma(b[3 * r + 2], x2, s);
+      acc[r] = s;
+    }
+  }
+}
+
+// guess_alpha's product: acc = W x and accd = W (x - 1) in one pass over W
+__device__ __forceinline__ void spmv_row_guess(const PGArgs& a, int i, const double* __restrict__ x, double* acc,
+                                               double* accd) {
+  const int k1 = __ldg(a.rowptr + i + 1);
+  for (int k = __ldg(a.rowptr + i); k < k1; ++k) {
+    const int j = ldcs(a.col + k);
+    const double x0 = ldcg(x + 3 * j), x1 = ldcg(x + 3 * j + 1), x2 = ldcg(x + 3 * j + 2);
+    const double d0 = x0 - 1.0, d1 = x1 - 1.0, d2 = x2 - 1.0;
+    const double* B = a.val + 9 * (size_t)k;
+    double b[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) b[e] = ldcs(B + e);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      double s = acc[r], t = accd[r];
+      s = fma(b[3 * r + 0], x0, s);
+      s = fma(b[3 * r + 1], x1, s);
+      s = fma(b[3 * r + 2], x2, s);
+      t = fma(b[3 * r + 0], d0, t);
+      t = fma(b[3 * r + 1], d1, t);
+      t = fma(b[3 * r + 2], d2, t);
+      acc[r] = s;
+      accd[r] = t;
+    }
+  }
+}
+
+struct Bufs {
+  const PGArgs& a;
+  __device__ double* X(int k) const { return k == 0 ? a.X0 : (k == 1 ? a.X1 : a.X2); }
+  __device__ double* MX(int k) const { return k == 0 ? a.MX0 : a.MX1; }
+};
+
+__device__ __forceinline__ int third(int p, int q) {
+  for (int k = 0; k < 3; ++k)
+    if (k != p && k != q) return k;
+  return 0;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
+  __shared__ double smem8[8];
+  const Bufs B{a};
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int nw = gridDim.x * 8;
+  const bool desaxce = a.desaxce != 0;
+  const bool spg = a.variant == 4;
+  const bool apgd = a.variant == 3;
+  const int C = a.nchunks;
+  const unsigned res_mask = a.use_inf ? 1u : 0u;
+
+  auto put = [&](int q, int c, double v, bool is_max) {
+    v = is_max ? warp_max_butterfly(v) : warp_sum_butterfly(v);
+    if (lane == 0) a.csum[q * C + c] = v;
+  };
+  auto publish = [&](int K, unsigned maxmask) {
+    for (int q = 0; q < K; ++q) {
+      const double v = block8_combine(a.csum + q * C, C, (maxmask >> q) & 1u, smem8);
+      if (threadIdx.x == 0) a.scal[q] = v;
+    }
+  };
+  auto sync = [&]() -> bool { return grid_barrier(a.gb, [] {}); };
+  auto sync_reduce = [&](int K, unsigned maxmask) -> bool {
+    return grid_barrier(a.gb, [&] { publish(K, maxmask); });
+  };
+  auto scal = [&](int q) { return ldcg(a.scal + q); };
+  // ConstrainedSolverBase::eval: sum / (1 + n), or the maximum with the infinity norm
+  auto residual_of = [&](double reduced) { return a.use_inf ? reduced : reduced / (double)(1 + a.n); };
+  unsigned ph[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  auto finish = [&](double min_res, unsigned iters, int best_buf, int converged) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.out->min_res = min_res;
+      a.out->iters = iters;
+      a.out->best_buf = best_buf;
+      a.out->converged = converged;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a.out->phases[k] = ph[k];
+    }
+  };
+
+  int ix = 0, iprev = 0, ixs = 1, imx = 0;
+
+  // projectOnConstraints(x) (:90)
+  ph[0]++;
+  for (int c = gw; c < C; c += nw) {
+    const int i = 32 * c + lane;
+    if (i < a.n) {
+      double x[3];
+      load3cg(a.X0, i, x);
+      project_cone(__ldg(a.mu + i), x);
+      store3(a.X0, i, x);
+    }
+  }
+  if (!sync()) return;
+
+  // Mx = W x (:93) and guess_alpha (:21-28): |W (x - 1)|^2, |x - 1|^2
+  ph[1]++;
+  for (int c = gw; c < C; c += nw) {
+    const int i = 32 * c + lane;
+    double v0 = 0.0, v1 = 0.0;
+    if (i < a.n) {
+      double acc[3] = {0.0, 0.0, 0.0}, accd[3] = {0.0, 0.0, 0.0};
+      spmv_row_guess(a, i, a.X0, acc, accd);
+      store3(a.MX0, i, acc);
+      v0 = sq3(accd);
+      double x[3];
+      load3cg(a.X0, i, x);
+      const double d[3] = {x[0] - 1.0, x[1] - 1.0, x[2] - 1.0};
+      v1 = sq3(d);
+    }
+    put(0, c, v0, false);
+    put(1, c, v1, false);
+  }
+  if (!sync_reduce(2, 0u)) return;
+  double alpha = 1.0;
+  {
+    const double nMx = scal(0);
+    if (nMx > 1.e-16) alpha = dmin(1., scal(1) / nMx);
+  }
+  if (a.max_iters == 0) {
+    finish(-1.0, 0, 0, 0);
+    return;
+  }
+
+  // Row-local part A, given Mx_i: writes y, s0 and xs = P(x - alpha_t y) (APGD) and returns the residual
+  // and objective terms; SPG additionally needs (xs - prev).y.
+  auto phaseA = [&](int i, const double* Mx, double alpha_t, double& res_i, double& second_i) {
+    double x[3], bb[3];
+    load3cg(B.X(ix), i, x);
+    bb[0] = __ldg(a.b + 3 * i);
+    bb[1] = __ldg(a.b + 3 * i + 1);
+    bb[2] = __ldg(a.b + 3 * i + 2);
+    const double mu = __ldg(a.mu + i), sc = __ldg(a.scaling + i);
+    double y[3] = {Mx[0] + bb[0], Mx[1] + bb[1], Mx[2] + bb[2]};
+    const double lx[3] = {x[0] * sc, x[1] * sc, x[2] * sc};
+    res_i = law_eval(desaxce, mu, lx, y);
+    const double s0 = duality_cov(desaxce, mu, y);
+    y[0] = y[0] + s0;
+    y[1] = y[1] + 0.0;
+    y[2] = y[2] + 0.0;
+    double xs[3] = {fma(-alpha_t, y[0], x[0]), fma(-alpha_t, y[1], x[1]), fma(-alpha_t, y[2], x[2])};
+    project_cone(mu, xs);
+    store3(a.Y, i, y);
+    a.S0[i] = s0;
+    store3(B.X(ixs), i, xs);
+    if (spg) {
+      double pv[3];
+      load3cg(B.X(iprev), i, pv);
+      const double d[3] = {xs[0] - pv[0], xs[1] - pv[1], xs[2] - pv[2]};
+      second_i = dot3(d, y);
+    } else {
+      const double t[3] = {(0.5 * Mx[0] + bb[0]) + s0, (0.5 * Mx[1] + bb[1]) + 0.0, (0.5 * Mx[2] + bb[2]) + 0.0};
+      second_i = dot3(x, t);
+    }
+  };
+
+  auto runA = [&](double alpha_t) -> bool {  // A as its own pass (Mx already in MX(imx))
+    ph[2]++;
+    for (int c = gw; c < C; c += nw) {
+      const int i = 32 * c + lane;
+      double r = 0.0, q = 0.0;
+      if (i < a.n) {
+        double Mx[3];
+        load3cg(B.MX(imx), i, Mx);
+        phaseA(i, Mx, alpha_t, r, q);
+      }
+      put(0, c, r, res_mask != 0);
+      put(1, c, q, false);
+    }
+    return sync_reduce(2, res_mask);
+  };
+
+  double min_res = -1.0, theta = 1.0;
+  bool best_pending = false;
+  unsigned it = 0;
+
+  if (!spg) {
+    // ---------------------------------------------------------------- APGD / Descent
+    double alpha_t = alpha * a.opt;
+    if (!runA(alpha_t)) return;
+    for (;;) {
+      const double res = residual_of(scal(0)), J = scal(1);
+      if (blockIdx.x == 0 && threadIdx.x == 0) a.trace[it] = res;
+      if (it == 0 || res < min_res) {
+        min_res = res;
+        best_pending = true;
+      }
+      if (res < a.tol) {
+        finish(min_res, it, best_pending ? ix : 3, 1);
+        return;
+      }
+      alpha = alpha_t;
+      unsigned ls = 0;
+      double decr2 = 0.0;
+      for (;;) {
+        // C: Mxs = W xs and the line-search terms
+        ph[3]++;
+        for (int c = gw; c < C; c += nw) {
+          const int i = 32 * c + lane;
+          double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+          if (i < a.n) {
+            double acc[3] = {0.0, 0.0, 0.0};
+            spmv_row(a, i, B.X(ixs), acc);
+            store3(B.MX(1 - imx), i, acc);
+            double x[3], xs[3], pv[3], y[3];
+            load3cg(B.X(ix), i, x);
+            load3cg(B.X(ixs), i, xs);
+            load3cg(B.X(iprev), i, pv);
+            load3cg(a.Y, i, y);
+            const double s0 = ldcg(a.S0 + i);
+            const double t[3] = {(0.5 * acc[0] + __ldg(a.b + 3 * i)) + s0, (0.5 * acc[1] + __ldg(a.b + 3 * i + 1)) + 0.0,
+                                 (0.5 * acc[2] + __ldg(a.b + 3 * i + 2)) + 0.0};
+            v0 = dot3(xs, t);
+            const double d[3] = {xs[0] - x[0], xs[1] - x[1], xs[2] - x[2]};
+            v1 = dot3(y, d);
+            v2 = sq3(d);
+            const double d2[3] = {xs[0] - pv[0], xs[1] - pv[1], xs[2] - pv[2]};
+            v3 = dot3(d2, y);
+            if (best_pending) store3(a.XB, i, x);
+          }
+          put(0, c, v0, false);
+          put(1, c, v1, false);
+          put(2, c, v2, false);
+          put(3, c, v3, false);
+        }
+        best_pending = false;
+        if (!sync_reduce(4, 0u)) return;
+        const double Js = scal(0), decr = scal(1), nrm = scal(2);
+        decr2 = scal(3);
+        if (Js < (J + decr) + (.5 / alpha) * nrm) break;
+        ++ls;
+        alpha *= a.pess;
+        if (ls >= a.ls_iters) break;
+        // B: retry with a smaller step
+        ph[4]++;
+        for (int c = gw; c < C; c += nw) {
+          const int i = 32 * c + lane;
+          if (i < a.n) {
+            double x[3], y[3];
+            load3cg(B.X(ix), i, x);
+            load3cg(a.Y, i, y);
+            double xs[3] = {fma(-alpha, y[0], x[0]), fma(-alpha, y[1], x[1]), fma(-alpha, y[2], x[2])};
+            project_cone(__ldg(a.mu + i), xs);
+            store3(B.X(ixs), i, xs);
+          }
+        }
+        if (!sync()) return;
+      }
+      ++it;
+      const bool more = it < a.max_iters;
+      if (apgd && decr2 < 0) {
+        const double beta = nesterov_inertia(theta, 0.0);
+        // D: x = xs + beta (xs - prev), written over the old x
+        ph[5]++;
+        for (int c = gw; c < C; c += nw) {
+          const int i = 32 * c + lane;
+          if (i < a.n) {
+            double xs[3], pv[3];
+            load3cg(B.X(ixs), i, xs);
+            load3cg(B.X(iprev), i, pv);
+            const double xn[3] = {fma(beta, xs[0] - pv[0], xs[0]), fma(beta, xs[1] - pv[1], xs[1]),
+                                  fma(beta, xs[2] - pv[2], xs[2])};
+            store3(B.X(ix), i, xn);
+          }
+        }
+        if (!sync()) return;
+        iprev = ixs;
+        ixs = third(ix, iprev);
+        if (!more) break;
+        alpha_t = alpha * a.opt;
+        // E + A: Mx = W x, then A of the next iteration on the same rows
+        ph[6]++;
+        for (int c = gw; c < C; c += nw) {
+          const int i = 32 * c + lane;
+          double r = 0.0, q = 0.0;
+          if (i < a.n) {
+            double acc[3] = {0.0, 0.0, 0.0};
+            spmv_row(a, i, B.X(ix), acc);
+            store3(B.MX(imx), i, acc);
+            phaseA(i, acc, alpha_t, r, q);
+          }
+          put(0, c, r, res_mask != 0);
+          put(1, c, q, false);
+        }
+        if (!sync_reduce(2, res_mask)) return;
+      } else {
+        theta = 1.;
+        ix = ixs;
+        iprev = ixs;
+        imx = 1 - imx;
+        ixs = (ix + 1) % 3;
+        if (!more) break;
+        alpha_t = alpha * a.opt;
+        if (!runA(alpha_t)) return;
+      }
+    }
+    finish(min_res, it, 3, 0);
+    return;
+  }
+
+  // ------------------------------------------------------------------ SPG (:288-351)
+  const double a_min = 1.e-6, a_max = 1.e6;
+  for (;;) {
+    if (!runA(alpha)) return;  // y, residual, s, xs = P(x - alpha y), (xs - prev).y
+    const double res = residual_of(scal(0)), decr = scal(1);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.trace[it] = res;
+    if (it == 0 || res < min_res) {
+      min_res = res;
+      best_pending = true;
+    }
+    if (res < a.tol) {
+      finish(min_res, it, best_pending ? ix : 3, 1);
+      return;
+    }
+    const bool mom = decr < 0.;
+    const double beta = mom ? nesterov_inertia(theta, 0.0) : 0.0;
+    if (!mom) theta = 1.;
+    // D: w and the new x (over the old x); keep the best iterate first
+    ph[7]++;
+    for (int c = gw; c < C; c += nw) {
+      const int i = 32 * c + lane;
+      if (i < a.n) {
+        double x[3], xs[3], pv[3], w[3], xn[3];
+        load3cg(B.X(ix), i, x);
+        load3cg(B.X(ixs), i, xs);
+        load3cg(B.X(iprev), i, pv);
+        if (best_pending) store3(a.XB, i, x);
+        for (int k = 0; k < 3; ++k) {
+          if (mom) {
+            w[k] = fma(beta, xs[k] - pv[k], xs[k]) - x[k];
+            xn[k] = x[k] + w[k];
+          } else {
+            w[k] = xs[k] - x[k];
+            xn[k] = xs[k];
+          }
+        }
+        store3(a.Wv, i, w);
+        store3(B.X(ix), i, xn);
+      }
+    }
+    best_pending = false;
+    if (!sync()) return;
+    // E: Mx_new = W x; z = -Mx_old + Mx_new; w.z, |z|^2
+    ph[8]++;
+    for (int c = gw; c < C; c += nw) {
+      const int i = 32 * c + lane;
+      double v0 = 0.0, v1 = 0.0;
+      if (i < a.n) {
+        double acc[3] = {0.0, 0.0, 0.0}, mo[3], w[3];
+        spmv_row(a, i, B.X(ix), acc);
+        store3(B.MX(1 - imx), i, acc);
+        load3cg(B.MX(imx), i, mo);
+        load3cg(a.Wv, i, w);
+        const double z[3] = {-mo[0] + acc[0], -mo[1] + acc[1], -mo[2] + acc[2]};
+        v0 = dot3(w, z);
+        v1 = sq3(z);
+      }
+      put(0, c, v0, false);
+      put(1, c, v1, false);
+    }
+    if (!sync_reduce(2, 0u)) return;
+    imx = 1 - imx;
+    iprev = ixs;
+    ixs = third(ix, iprev);
+    alpha = scal(0) / scal(1);
+    alpha = dmin(a_max, dmax(a_min, alpha));
+    ++it;
+    if (it >= a.max_iters) break;
+  }
+  finish(min_res, it, 3, 0);
+}
+
+cudaError_t launch_pg_persistent(const PGArgs& a, int grid, cudaStream_t s) {
+  PGArgs copy = a;
+  void* args[] = {&copy};
+  return cudaLaunchCooperativeKernel((const void*)k_pg_persistent, dim3(grid), dim3(256), args, 0, s);
+}
+
+int pg_max_grid(int device) {
+  int sms = 0, per = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_persistent, 256, 0) != cudaSuccess) return 0;
+  if (per > 2) per = 2;
+  return per * sms;
+}
+
+}  // namespace bogus_gpu

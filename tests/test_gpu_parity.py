@@ -1,0 +1,287 @@
+"""GPU kernels (through the C ABI) against the CPU oracle on identical inputs.
+
+The kernels follow the oracle's evaluation order, so products, residuals, iterates, iteration counts and
+callback traces must be bit-identical (exact equality; +0.0 and -0.0 compare equal). At the full
+200 000-contact size, where running the whole oracle solve would take minutes, the checks are
+size-independent: bit-identical assembly and products, the returned residual equal to the oracle's
+error function at the returned iterate, and the first iterations of the solve bit-identical.
+"""
+import numpy as np
+import pytest
+
+from conftest import small_friction_dual
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def bg():
+    import bogus_gpu
+
+    bogus_gpu.lib()
+    return bogus_gpu
+
+
+@pytest.fixture(scope="module")
+def c1(oracle):
+    from bogus_gpu import generator
+
+    d = generator.make("c1")
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    rp, cl, vl = P.assemble()
+    return d, rp, cl, vl
+
+
+def _gpu_dual(bg, rp, cl, vl, b, mu):
+    D = bg.DualFrictionProblem()
+    D.set(rp, cl, vl, b, mu)
+    return D
+
+
+def test_spmv_bitwise(bg, oracle, c1):
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    rng = np.random.default_rng(0)
+    for _ in range(3):
+        x = rng.standard_normal(3 * d.n)
+        assert np.array_equal(D.multiply(x), O.spmv(x))
+
+
+def test_assembly_bitwise(bg, oracle, c1):
+    d, rp, cl, vl = c1
+    D = bg.DualFrictionProblem()
+    D.computeFrom(bg.PrimalFrictionProblem.from_generated(d))
+    grp, gcl, gvl = D.W_lower()
+    assert np.array_equal(grp, rp) and np.array_equal(gcl, cl)
+    assert np.array_equal(gvl.reshape(-1), vl)
+    # b = w - H M^-1 f with f given
+    f = np.random.default_rng(5).standard_normal(6 * d.nbodies)
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    b_oracle = P.rhs(f, d.b)
+    pr = bg.PrimalFrictionProblem(d.minv, d.objA, d.objB, d.HA, d.HB, d.b, d.mu, f=f)
+    D2 = bg.DualFrictionProblem()
+    D2.computeFrom(pr)
+    r = np.zeros(3 * d.n)
+    # W r + b at r = 0 is b: read it through the error function's input path via a product
+    O = oracle.DualProblem(rp, cl, vl, b_oracle, d.mu)
+    for coulomb in (True, False):
+        assert D2.evalWith(bg.GaussSeidel(), r, staticProblem=not coulomb) == O.eval(r, coulomb=coulomb)
+
+
+@pytest.mark.parametrize("inf_norm", [False, True])
+def test_eval_bitwise(bg, oracle, c1, inf_norm):
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    r = np.random.default_rng(1).standard_normal(3 * d.n)
+    pg = bg.ProjectedGradient()
+    pg.useInfinityNorm(inf_norm)
+    for static in (True, False):
+        assert D.evalWith(pg, r, staticProblem=static) == O.eval(r, coulomb=not static, inf_norm=inf_norm)
+
+
+@pytest.mark.parametrize("variant", [3, 1, 4])  # APGD, Descent, SPG
+@pytest.mark.parametrize("static", [True, False])
+def test_projected_gradient_bitwise(bg, oracle, c1, variant, static):
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    pg = bg.ProjectedGradient()
+    pg.setDefaultVariant(variant)
+    pg.setTol(1e-8)
+    pg.setMaxIters(400)
+    trace_gpu = []
+    pg.callback().connect(lambda it, res: trace_gpu.append((it, res)))
+    r0 = np.random.default_rng(2).standard_normal(3 * d.n) * 0.1
+    r = r0.copy()
+    res = D.solveWith(pg, r, staticProblem=static)
+    tr = oracle.Trace()
+    res_o, r_o, it_o = O.solve_pg(r0, variant=variant, coulomb=not static, tol=1e-8, max_iters=400, trace=tr)
+    assert res == res_o
+    assert D.last_iterations == it_o
+    assert np.array_equal(r, r_o)
+    assert trace_gpu == tr.items
+
+
+@pytest.mark.parametrize("strategy", [3, 0, 2])
+@pytest.mark.parametrize("static", [False, True])
+def test_gauss_seidel_bitwise(bg, oracle, c1, strategy, static):
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    gs = bg.GaussSeidel()
+    gs.setLocalStrategy(strategy)
+    gs.setTol(1e-8)
+    gs.setMaxIters(150)
+    trace_gpu = []
+    gs.callback().connect(lambda it, res: trace_gpu.append((it, res)))
+    r0 = np.zeros(3 * d.n)
+    r = r0.copy()
+    res = D.solveWith(gs, r, staticProblem=static)
+    tr = oracle.Trace()
+    res_o, r_o, it_o = O.solve_gs(r0, coulomb=not static, strategy=strategy, tol=1e-8, max_iters=150,
+                                  coloring=True, trace=tr)
+    assert res == res_o
+    assert D.last_iterations == it_o
+    assert np.array_equal(r, r_o)
+    assert trace_gpu == tr.items
+
+
+def test_gauss_seidel_options_bitwise(bg, oracle, c1):
+    """Skip heuristic off, auto-regularization on, infinity norm, no tryZero."""
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    gs = bg.GaussSeidel()
+    gs.setSkipTol(0.0)
+    gs.setAutoRegularization(1e-3)
+    gs.useInfinityNorm(True)
+    gs.doTryZeroAsWell(False)
+    gs.setEvalEvery(10)
+    gs.setMaxIters(60)
+    r = np.ones(3 * d.n)
+    res = D.solveWith(gs, r)
+    res_o, r_o, it_o = O.solve_gs(np.ones(3 * d.n), coulomb=True, skip_tol=0.0, auto_reg=1e-3, inf_norm=True,
+                                  try_zero=False, eval_every=10, max_iters=60, coloring=True)
+    assert res == res_o and D.last_iterations == it_o and np.array_equal(r, r_o)
+
+
+def test_coloring_matches_oracle(bg, oracle, c1):
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    perm, colors = D.coloring()
+    perm_o, colors_o = oracle.DualProblem(rp, cl, vl, d.b, d.mu).coloring()
+    assert np.array_equal(perm, perm_o) and np.array_equal(colors, colors_o)
+
+
+# ---- the reference's SmallFrictionPb known answers, solved on the GPU ----------------------------------
+def test_small_friction_known_answers(bg, oracle, golden):
+    s = golden["small_friction_pb"]
+    rp, cl, vl, b, mu = small_friction_dual(golden, oracle)
+    D = _gpu_dual(bg, rp, cl, vl, b, mu)
+    for strategy in range(4):
+        gs = bg.GaussSeidel()
+        gs.setLocalStrategy(strategy)
+        r = np.ones(6)
+        res = D.solveWith(gs, r)
+        assert res < s["res_tol"]
+        sol = np.array(s["sol"])
+        assert np.linalg.norm(sol - r) <= s["sol_rel_tol"] * min(np.linalg.norm(sol), np.linalg.norm(r))
+    for variant in (3, 1, 4):
+        pg = bg.ProjectedGradient()
+        pg.setTol(1e-8)
+        pg.setDefaultVariant(variant)
+        r = np.ones(6)
+        assert D.solveWith(pg, r) < 1e-8
+
+
+# ---- edge cases ------------------------------------------------------------------------------------------
+def test_empty_problem(bg):
+    D = bg.DualFrictionProblem()
+    D.set(np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0), np.zeros(0), np.zeros(0))
+    r = np.zeros(0)
+    assert D.solveWith(bg.ProjectedGradient(), r) == 0.0
+    assert D.solveWith(bg.GaussSeidel(), r) == 0.0
+
+
+def test_missing_diagonal_negative_mu_and_zero_iterations(bg, oracle):
+    # 3 contacts; contact 1 has no diagonal block; contact 2 has mu < 0
+    rng = np.random.default_rng(9)
+    G = rng.standard_normal((3, 3))
+    A = G @ G.T + np.eye(3)
+    rp = np.array([0, 1, 1, 3], np.int32)
+    cl = np.array([0, 0, 2], np.int32)
+    vl = np.concatenate([A.reshape(-1), 0.1 * G.reshape(-1), A.reshape(-1)])
+    b = rng.standard_normal(9)
+    mu = np.array([0.5, 0.3, -1.0])
+    D = _gpu_dual(bg, rp, cl, vl, b, mu)
+    O = oracle.DualProblem(rp, cl, vl, b, mu)
+    for variant in (3, 4):
+        pg = bg.ProjectedGradient()
+        pg.setDefaultVariant(variant)
+        pg.setMaxIters(50)
+        r = np.ones(9)
+        res = D.solveWith(pg, r, staticProblem=False)
+        res_o, r_o, it_o = O.solve_pg(np.ones(9), variant=variant, coulomb=True, max_iters=50)
+        assert res == res_o and np.array_equal(r, r_o)
+    gs = bg.GaussSeidel()
+    gs.setMaxIters(50)
+    r = np.ones(9)
+    res = D.solveWith(gs, r)
+    res_o, r_o, _ = O.solve_gs(np.ones(9), max_iters=50, coloring=True)
+    assert res == res_o and np.array_equal(r, r_o)
+    # maxIters = 0: the iterate is only projected and the residual is -1, as in the reference
+    pg = bg.ProjectedGradient()
+    pg.setMaxIters(0)
+    r = np.ones(9)
+    res = D.solveWith(pg, r)
+    res_o, r_o, _ = O.solve_pg(np.ones(9), max_iters=0)
+    assert res == res_o == -1.0 and np.array_equal(r, r_o)
+
+
+def test_bad_inputs_raise(bg):
+    D = bg.DualFrictionProblem()
+    with pytest.raises(bg.BogusGpuError) as e:  # block above the diagonal in lower storage
+        D.set([0, 1, 1], [1], np.eye(3).reshape(-1), np.zeros(6), np.ones(2))
+    assert e.value.status == bg.BAD_INPUT
+    with pytest.raises(bg.BogusGpuError) as e:
+        D.set([0, 1], [0], np.eye(3).reshape(-1), np.array([np.nan, 0, 0]), np.ones(1))
+    assert e.value.status == bg.NONFINITE
+    D.set([0, 1], [0], np.eye(3).reshape(-1), np.zeros(3), np.ones(1))
+    pg = bg.ProjectedGradient()
+    pg.setLineSearchIterations(0)
+    with pytest.raises(bg.BogusGpuError):
+        D.solveWith(pg, np.zeros(3))
+
+
+def test_repeatable(bg, c1):
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    outs = []
+    for _ in range(2):
+        r = np.zeros(3 * d.n)
+        outs.append((D.solveWith(bg.ProjectedGradient(), r, staticProblem=False), r.copy()))
+    assert outs[0][0] == outs[1][0] and np.array_equal(outs[0][1], outs[1][1])
+
+
+# ---- full size (200 000 contacts): size-independent checks -----------------------------------------------
+@pytest.fixture(scope="module")
+def c2(bg, oracle):
+    from bogus_gpu import generator
+
+    d = generator.make("c2")
+    D = bg.DualFrictionProblem()
+    D.computeFrom(bg.PrimalFrictionProblem.from_generated(d))
+    return d, D
+
+
+def test_full_size_assembly_and_product(bg, oracle, c2):
+    d, D = c2
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    rp, cl, vl = P.assemble()
+    grp, gcl, gvl = D.W_lower()
+    assert np.array_equal(grp, rp) and np.array_equal(gcl, cl) and np.array_equal(gvl.reshape(-1), vl)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    x = np.random.default_rng(4).standard_normal(3 * d.n)
+    assert np.array_equal(D.multiply(x), O.spmv(x))
+
+
+def test_full_size_apgd(bg, oracle, c2):
+    d, D = c2
+    pg = bg.ProjectedGradient()
+    pg.setMaxIters(500)
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r, staticProblem=False)
+    # the returned residual is the error function at the returned iterate (oracle, canonical order)
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    O = oracle.DualProblem(*P.assemble(), d.b, d.mu)
+    assert res == O.eval(r, coulomb=True)
+    assert np.all(np.isfinite(r))
+    # the first iterations bit-identical to the oracle's
+    pg5 = bg.ProjectedGradient()
+    pg5.setMaxIters(5)
+    r5 = np.zeros(3 * d.n)
+    res5 = D.solveWith(pg5, r5, staticProblem=False)
+    res5_o, r5_o, _ = O.solve_pg(np.zeros(3 * d.n), variant=3, coulomb=True, max_iters=5)
+    assert res5 == res5_o and np.array_equal(r5, r5_o)

@@ -1,0 +1,215 @@
+"""Pins the CPU oracle against So-bogus's own unit tests (values in tests/golden/reference_fixtures.json).
+
+Each test names the reference test it restates; thresholds are the reference's.
+"""
+import numpy as np
+import pytest
+
+from conftest import small_friction_dual
+
+
+def isApprox(a, b, prec):
+    """Eigen's isApprox: |a - b| <= prec * min(|a|, |b|)."""
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.linalg.norm(a - b) <= prec * min(np.linalg.norm(a), np.linalg.norm(b))
+
+
+# ---- tests/ProjectedGradient.cpp:85-108 ----------------------------------------------------------
+def test_projection_cases(oracle, golden):
+    for case in golden["projection"]["cases"]:
+        out = oracle.project(case["mu"], case["x"])
+        exp = np.array(case["expected"], float)
+        if case["exact"]:
+            assert np.array_equal(out, exp)
+        elif np.all(exp == 0):
+            assert np.all(np.abs(out) < 1e-12)  # x.isZero()
+        else:
+            assert isApprox(out, exp, 1e-12)
+
+
+# ---- tests/Polynomial.cpp:17-38 -------------------------------------------------------------------
+def test_quadratic_roots(oracle, golden):
+    for case in golden["polynomial"]["quadratic"]:
+        roots = oracle.real_roots(case["coeffs"], degenerate=False, filt=case["filter"])
+        assert len(roots) == len(case["roots"])
+        # EXPECT_DOUBLE_EQ: within 4 ulps
+        for got, exp in zip(sorted(roots), sorted(case["roots"])):
+            assert abs(got - exp) <= 4 * np.spacing(abs(exp))
+
+
+# ---- tests/Polynomial.cpp:40-94: 3D SOC local problem by the enumerative solver ------------------
+def test_soc_quartic_pure_enumerative(oracle, golden):
+    chk = golden["polynomial"]["soc_quartic_checks"]
+    for case in golden["polynomial"]["soc_quartic"]:
+        W = np.array(case["W"], float).reshape(3, 3)
+        b = np.array(case["b"], float)
+        res, r = oracle.local_solve(W, b, np.zeros(3), case["mu"], coulomb=False, strategy=1, tol=1e-12)
+        u = W @ r + b
+        assert res < chk["res_below"]
+        assert r[0] > 0
+        assert u[0] > 0
+        assert np.float32(u[0]) == pytest.approx(np.float32(np.linalg.norm(u[1:]) * case["mu"]), rel=4 * 2 ** -23)
+        assert u @ r < chk["complementarity_below"]
+
+
+# ---- tests/BlockMV.cpp:193-296: symmetric 3x3-block products ---------------------------------------
+def test_block_mv_symmetric(oracle, golden):
+    g = golden["block_mv_symmetric"]
+    D = oracle.DualProblem(g["rowptr"], g["col"], g["val"], np.zeros(9), np.ones(3))
+    rhs = np.array(g["rhs"], float)
+    assert np.array_equal(D.spmv(rhs), np.array(g["expected_product"], float))
+    res = np.zeros(9)
+    for k in range(3):
+        res[3 * k:3 * k + 3] = D.split_row(k, rhs, res[3 * k:3 * k + 3])
+    assert np.array_equal(res, np.array(g["expected_split_row"], float))
+    # accumulating into the previous result doubles it (the "ussbm" case of the same test)
+    res2 = res.copy()
+    for k in range(3):
+        res2[3 * k:3 * k + 3] = D.split_row(k, rhs, res2[3 * k:3 * k + 3])
+    assert np.array_equal(res2, 2 * np.array(g["expected_split_row"], float))
+
+
+# ---- tests/SparseBlock.cpp:464-498: permutation of a symmetric matrix ---------------------------------
+def test_symmetric_permutation(oracle, golden):
+    perm = np.array(golden["permutation"]["perm"])
+    n = len(perm)
+    # symmetric matrix whose block (i, j) is diag(i + j, j + i): the test's sbm += sbm^T, lower part stored
+    rowptr = np.arange(0, (n + 1) * (n + 2) // 2, 1)
+    rp, cl, vl = [0], [], []
+    for i in range(n):
+        for j in range(i + 1):
+            cl.append(j)
+            vl.extend([i + j, 0, 0, 0, j + i, 0, 0, 0, 0])
+        rp.append(len(cl))
+    del rowptr
+    D = oracle.DualProblem(rp, cl, vl, np.zeros(3 * n), np.ones(n))
+    # new (i, j) = old (perm[i], perm[j]): check through products with unit vectors on the full view
+    frp, fcl, fvl = D.full()
+    dense = np.zeros((3 * n, 3 * n))
+    for i in range(n):
+        for k in range(frp[i], frp[i + 1]):
+            dense[3 * i:3 * i + 3, 3 * fcl[k]:3 * fcl[k] + 3] = fvl[9 * k:9 * k + 9].reshape(3, 3)
+    P = np.zeros((3 * n, 3 * n))
+    for i in range(n):
+        P[3 * i:3 * i + 3, 3 * perm[i]:3 * perm[i] + 3] = np.eye(3)
+    permuted = P @ dense @ P.T
+    for i in range(n):
+        for j in range(i + 1):
+            blk = permuted[3 * i:3 * i + 3, 3 * j:3 * j + 3]
+            assert blk[0, 0] == perm[i] + perm[j]
+            assert blk[1, 1] == perm[j] + perm[i]
+
+
+# ---- tests/SparseBlock.cpp:16-60: H H^T ----------------------------------------------------------------
+def test_sparse_product_hht(oracle, golden):
+    g = golden["sparse_product"]["blocks"]
+    ones = np.ones((3, 4))
+    # block rows 0..2 as "contacts"; block cols 0..1 as 4-dof "bodies"; M^-1 = I
+    minv = np.stack([np.eye(4), np.eye(4)])
+    objA = [1, 0, 0]
+    objB = [-1, -1, 1]
+    HA = np.stack([np.array(g["0,1"]), np.array(g["1,0"]), np.array(g["2,0"])])
+    HB = np.stack([np.zeros((3, 4)), np.zeros((3, 4)), np.array(g["2,1"])])
+    P = oracle.PrimalProblem(minv, objA, objB, HA, HB)
+    rp, cl, vl = P.assemble()
+    blocks = {(i, cl[k]): vl[9 * k:9 * k + 9].reshape(3, 3) for i in range(3) for k in range(rp[i], rp[i + 1])}
+    assert np.array_equal(blocks[(2, 2)], np.full((3, 3), golden["sparse_product"]["diag2_value"]))
+    H = np.zeros((9, 8))
+    H[0:3, 4:8] = ones
+    H[3:6, 0:4] = np.array(g["1,0"])
+    H[6:9, 0:4] = 3 * ones
+    H[6:9, 4:8] = 5 * ones
+    dense = H @ H.T
+    for (i, j), blk in blocks.items():
+        assert np.array_equal(blk, dense[3 * i:3 * i + 3, 3 * j:3 * j + 3])
+    assert (1, 0) not in blocks or np.array_equal(blocks[(1, 0)], dense[3:6, 0:3])
+
+
+# ---- tests/SmallFrictionPb.hpp + tests/GaussSeidel.cpp:19-65 -------------------------------------------
+def test_small_friction_assembly(oracle, golden):
+    s = golden["small_friction_pb"]
+    rp, cl, vl, b, mu = small_friction_dual(golden, oracle)
+    Wd = np.array(s["W_dense"])
+    for i in range(2):
+        for k in range(rp[i], rp[i + 1]):
+            j = cl[k]
+            assert np.allclose(vl[9 * k:9 * k + 9].reshape(3, 3), Wd[3 * i:3 * i + 3, 3 * j:3 * j + 3], rtol=0,
+                               atol=1e-12)
+    assert np.allclose(b, s["b"], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("strategy", [0, 1, 2, 3])
+def test_small_friction_gauss_seidel(oracle, golden, strategy):
+    s = golden["small_friction_pb"]
+    D = oracle.DualProblem(*small_friction_dual(golden, oracle))
+    res, r, _ = D.solve_gs(np.ones(6), coulomb=True, strategy=strategy, coloring=False)
+    assert res < s["res_tol"]
+    assert isApprox(s["sol"], r, s["sol_rel_tol"])
+
+
+def test_small_friction_gauss_seidel_soc(oracle, golden):
+    D = oracle.DualProblem(*small_friction_dual(golden, oracle))
+    res, r, _ = D.solve_gs(np.ones(6), coulomb=False, tol=1e-8, coloring=False)
+    assert res < 1e-8
+
+
+# ---- tests/ProjectedGradient.cpp:16-61 ---------------------------------------------------------------
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+def test_small_friction_projected_gradient(oracle, golden, variant):
+    D = oracle.DualProblem(*small_friction_dual(golden, oracle))
+    res, r, _ = D.solve_pg(np.ones(6), variant=variant, coulomb=False, tol=1e-8)
+    assert res < 1e-8
+
+
+def test_coloring_is_valid_and_follows_reference_rule(oracle):
+    from bogus_gpu import generator
+
+    d = generator.make("c1")
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    rp, cl, vl = P.assemble()
+    D = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    perm, colors = D.coloring()
+    assert sorted(perm.tolist()) == list(range(d.n))
+    color_of = np.empty(d.n, int)
+    for c in range(len(colors) - 1):
+        members = perm[colors[c]:colors[c + 1]]
+        assert np.all(np.diff(members) > 0)
+        color_of[members] = c
+    for i in range(d.n):
+        for k in range(rp[i], rp[i + 1]):
+            j = cl[k]
+            if j < i:
+                assert color_of[i] != color_of[j]
+                # the reference's lower_bound test: no member of i's color lies in [j, i)
+                members = perm[colors[color_of[i]]:colors[color_of[i] + 1]]
+                assert not np.any((members >= j) & (members < i))
+
+
+def test_canonical_sum_matches_its_definition(oracle):
+    rng = np.random.default_rng(3)
+    for n in [0, 1, 31, 32, 33, 1000, 5000]:
+        v = rng.standard_normal(n)
+        C = (n + 31) // 32
+        pad = np.zeros(C * 32)
+        pad[:n] = v
+        sums = []
+        for c in range(C):
+            w = list(pad[32 * c:32 * c + 32])
+            for off in (16, 8, 4, 2, 1):
+                w = [w[l] + w[l ^ off] for l in range(32)]
+            sums.append(w[0])
+        per = (C + 7) // 8
+        total = 0.0
+        for k in range(8):
+            lanes = []
+            for l in range(32):
+                p = 0.0
+                for c in range(k * per + l, min(C, (k + 1) * per), 32):
+                    p = p + sums[c]
+                lanes.append(p)
+            for off in (16, 8, 4, 2, 1):
+                lanes = [lanes[l] + lanes[l ^ off] for l in range(32)]
+            total = lanes[0] if k == 0 else total + lanes[0]
+        got = oracle.canonical_sum(v)
+        assert got == total
+        assert got == pytest.approx(float(np.sum(v)), abs=1e-9 * max(1, n))
