@@ -177,6 +177,28 @@ int bogus_gpu_get_stream(const bogus_gpu_problem* h, void** stream);
  * on GPUs whose FP64 rate is below their memory bandwidth's need (no counterpart in the reference). */
 int bogus_gpu_measure_fp64_peak(int device, double* tflops);
 
+/* ---- Allocation-free projected-gradient solve (no counterpart in the reference) --------------------------
+ * For callers that must not allocate GPU memory while solving: simulation steps run under a fixed device-memory
+ * budget, real-time loops where cudaMalloc's implicit synchronisation would stall the frame, or hosts that hand
+ * the library only buffers they own. Same solve as bogus_gpu_solve_pg_device (APGD, Descent or SPG; the same
+ * iterates and residual), but W (both triangles, as in bogus_gpu_set_dual_device), b, mu and r are caller-owned
+ * device arrays, no handle is needed, and every temporary lives in one fixed array inside the library
+ * (about 14.2 MB of device memory, held on every GPU that loads the library until the process exits).
+ *  - Limits: at most BOGUS_GPU_NOALLOC_MAX_CONTACTS contacts and BOGUS_GPU_NOALLOC_MAX_ITERS iterations;
+ *    larger requests return BOGUS_GPU_BAD_INPUT without launching anything.
+ *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress) with that device
+ *    current; make that first call before any stream capture.
+ *  - Calls on one device share the array and it keeps the last call's contents (each call clears what must
+ *    start at zero): calls whose GPU work overlaps race and must not be issued.
+ *  - No callback. stream: a cudaStream_t, or NULL for the default stream; the call returns when the solve is
+ *    done and r holds the result. */
+#define BOGUS_GPU_NOALLOC_MAX_CONTACTS 65536
+#define BOGUS_GPU_NOALLOC_MAX_ITERS 65536
+int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int* d_rowptr, const int* d_colidx,
+                               const double* d_blocks, const double* d_b, const double* d_mu,
+                               const bogus_gpu_pg_options* opts, double* d_r, double* residual, unsigned* iters,
+                               void* stream);
+
 #ifdef __cplusplus
 }
 #endif

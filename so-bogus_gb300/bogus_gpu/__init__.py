@@ -64,7 +64,7 @@ EXPORTED = [
     "bogus_gpu_set_dual_device", "bogus_gpu_nnzb", "bogus_gpu_set_callback", "bogus_gpu_spmv", "bogus_gpu_eval",
     "bogus_gpu_solve_pg", "bogus_gpu_solve_pg_device", "bogus_gpu_solve_gs", "bogus_gpu_coloring",
     "bogus_gpu_set_primal", "bogus_gpu_assemble_dual", "bogus_gpu_get_dual_lower", "bogus_gpu_get_solve_stats",
-    "bogus_gpu_get_stream", "bogus_gpu_measure_fp64_peak",
+    "bogus_gpu_get_stream", "bogus_gpu_measure_fp64_peak", "bogus_gpu_solve_pg_noalloc",
 ]
 
 
@@ -100,6 +100,8 @@ def lib():
     L.bogus_gpu_get_solve_stats.argtypes = [vp, C.POINTER(SolveStats)]
     L.bogus_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.bogus_gpu_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.bogus_gpu_solve_pg_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, C.POINTER(PgOptions), vp,
+                                             C.POINTER(C.c_double), C.POINTER(C.c_uint), vp]
     _lib = L
     return L
 

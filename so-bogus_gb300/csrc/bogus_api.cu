@@ -88,6 +88,8 @@ struct GSCache {
 
 }  // namespace
 
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
 }  // namespace bogus_gpu
 
 using namespace bogus_gpu;

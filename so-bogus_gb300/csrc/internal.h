@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <string>
 
 #include "device_common.cuh"
 
@@ -99,5 +100,8 @@ cudaError_t launch_gs_skip(const GSArgs& a, int parity, double abs_skip_tol, dou
                            cudaStream_t s);
 cudaError_t launch_scale_scalar(double* p, double divisor, cudaStream_t s);
 cudaError_t measure_fp64_peak(int device, double* tflops);
+
+// Records the message returned by bogus_gpu_last_error() on this thread.
+void set_last_error(const std::string& msg);
 
 }  // namespace bogus_gpu
