@@ -302,6 +302,106 @@ def run_profile(iters: int) -> None:
     print(json.dumps({"profile_iters": iters, "residual": res, "stats": st}))
 
 
+def run_batch(args) -> None:
+    """4096 independent problems (16..4096 contacts, log-uniform) in one persistent launch, against a loop of the
+    single-problem GPU path and the CPU oracle on a stratified sample of the problems."""
+    import torch
+
+    import bogus_gpu
+    from bogus_gpu import generator
+
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    d, cptr = generator.batch(4096)
+    D = bogus_gpu.DualFrictionProblem(0)
+    D.computeFrom(bogus_gpu.PrimalFrictionProblem.from_generated(d))
+    D.setBatch(cptr)
+    pg = bogus_gpu.ProjectedGradient()
+    pg.setTol(TOL)
+    pg.setMaxIters(MAX_ITERS)
+    n = d.n
+    r = torch.zeros(3 * n, dtype=torch.float64, device="cuda:0")
+    stream = torch.cuda.ExternalStream(D.stream(), device="cuda:0")
+
+    def step():
+        with torch.cuda.stream(stream):
+            r.zero_()
+        return D.solveBatch_device(pg, r.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res, its = step()
+    torch.cuda.synchronize()
+    batched_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    st = D.solve_stats()
+    # the single-problem path, problem by problem, on every 16th problem by size (stratified), scaled by 16
+    rp, cl, vl = D.W_lower()
+    vl = vl.reshape(-1, 9)
+    order = np.argsort(np.diff(cptr), kind="stable")
+    sample = order[::16]
+    single = bogus_gpu.DualFrictionProblem(0)
+    import pyoracle
+    t_single = 0.0
+    t_cpu = 0.0
+    same = True
+    for p in sample:
+        c0, c1 = int(cptr[p]), int(cptr[p + 1])
+        prp, pcl, pvl = rp[c0:c1 + 1] - rp[c0], cl[rp[c0]:rp[c1]] - c0, vl[rp[c0]:rp[c1]].reshape(-1)
+        single.set(prp, pcl, pvl, d.b[c0:c1], d.mu[c0:c1])
+        rr = np.zeros(3 * (c1 - c0))
+        t0 = time.perf_counter()
+        res_s = single.solveWith(pg, rr)
+        t_single += time.perf_counter() - t0
+        O = pyoracle.DualProblem(prp, pcl, pvl, d.b[c0:c1], d.mu[c0:c1])
+        t0 = time.perf_counter()
+        res_o, r_o, it_o = O.solve_pg(np.zeros(3 * (c1 - c0)), variant=3, coulomb=False, tol=TOL, max_iters=MAX_ITERS)
+        t_cpu += time.perf_counter() - t0
+        same = same and res_s == res_o == res[p] and it_o == its[p]
+    scale = len(cptr) - 1
+    scale = scale / len(sample)
+    print(json.dumps({
+        "workload": "batched_apgd_4096_problems", "problems": len(cptr) - 1, "contacts": n,
+        "batched_ms": batched_ms, "kernel_ms": st["device_ms"], "iterations_max": int(its.max()),
+        "iterations_mean": float(its.mean()), "converged_fraction": float(np.mean(res < TOL)),
+        "loop_single_gpu_ms_est": t_single * 1e3 * scale, "cpu_oracle_ms_est": t_cpu * 1e3 * scale,
+        "cpu_threads": pyoracle.num_threads(), "sample": f"{len(sample)} problems (every 16th by size), scaled",
+        "speedup_vs_loop": t_single * 1e3 * scale / batched_ms, "identical_on_sample": bool(same),
+        "algorithmic_gbs": st["algorithmic_bytes"] / (st["device_ms"] * 1e-3) / 1e9}), flush=True)
+
+
+def run_gs(args) -> None:
+    """Gauss-Seidel on the 200 000-contact problem, both sweep orders: GPU time per sweep against the oracle."""
+    import bogus_gpu
+
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+
+    d = make_problem()
+    D = bogus_gpu.DualFrictionProblem(0)
+    D.computeFrom(bogus_gpu.PrimalFrictionProblem.from_generated(d))
+    rp, cl, vl = D.W_lower()
+    O = pyoracle.DualProblem(rp, cl, vl.reshape(-1), d.b, d.mu)
+    out = {"workload": "gauss_seidel_200k_contacts", "law": "Coulomb (GaussSeidel default)"}
+    for coloring in (False, True):
+        gs = bogus_gpu.GaussSeidel()
+        gs.coloring().update(coloring)
+        gs.setMaxIters(25)
+        r = np.zeros(3 * d.n)
+        D.solveWith(gs, r)
+        r = np.zeros(3 * d.n)
+        res = D.solveWith(gs, r)
+        gpu_ms = D.solve_stats()["device_ms"]
+        t0 = time.perf_counter()
+        res_o, r_o, _ = O.solve_gs(np.zeros(3 * d.n), max_iters=25, coloring=coloring)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        out["colored" if coloring else "natural_order"] = {
+            "sweeps": 25, "gpu_ms_per_sweep": gpu_ms / 25, "cpu_oracle_ms_per_sweep": cpu_ms / 25,
+            "residual": res, "identical": bool(res == res_o and np.array_equal(r, r_o))}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -311,7 +411,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", type=int, default=0,
                     help="run one solve capped at this many iterations and exit (for ncu captures)")
+    ap.add_argument("--workload", default="apgd", choices=["apgd", "batch", "gs"],
+                    help="apgd: the benchmark line; batch / gs: secondary measurements")
     args = ap.parse_args()
+    if args.workload == "batch":
+        run_batch(args)
+        return
+    if args.workload == "gs":
+        run_gs(args)
+        return
     if args.profile:
         run_profile(args.profile)
         return

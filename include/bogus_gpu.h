@@ -83,6 +83,9 @@ typedef struct bogus_gpu_gs_options {
   int use_infinity_norm;          /* 0 */
   int static_problem;             /* 0: Coulomb law (DualFrictionProblem::solveWith(gs) default) */
   int local_strategy;             /* bogus_gpu_local_strategy, RevHybrid */
+  int use_coloring;               /* 0: contacts swept in their own order, as DualFrictionProblem::solveWith(gs)
+                                     does single-threaded; 1: Coloring::compute + contact permutation, as
+                                     MecheFrictionProblem::solve does with maxThreads != 1 */
 } bogus_gpu_gs_options;
 
 typedef struct bogus_gpu_problem bogus_gpu_problem;
@@ -132,11 +135,31 @@ int bogus_gpu_solve_pg_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* 
                               unsigned* iters);
 
 /* DualFrictionProblem::solveWith(GaussSeidel&, r, staticProblem) (Interfaces/FrictionProblem.cpp:42-47,
- * GaussSeidel.impl.hpp:62-205) with greedy coloring and the contact permutation of
- * MecheFrictionProblem::solve (Interfaces/MecheInterface.cpp:326-337, Coloring.impl.hpp:20-62): colors are
- * swept in order, one launch per color. Requires W set from host arrays (the coloring is built on the host). */
+ * GaussSeidel.impl.hpp:62-205): the reference's sequential sweep, in the contacts' own order or (use_coloring)
+ * in the order of Coloring::compute with the contact permutation of MecheFrictionProblem::solve
+ * (Interfaces/MecheInterface.cpp:326-337, Coloring.impl.hpp:20-62). Contacts are processed level by level:
+ * a contact's level is one more than the highest level among its neighbours that precede it in the sweep, so
+ * each launch solves contacts that share no block of W and every contact sees exactly the values the
+ * sequential sweep would give it. Requires W set from host arrays or assembled (the schedule is built on the
+ * host). */
 int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* opts, double* r, double* residual,
                        unsigned* iters);
+
+/* ---- Batched solves (no counterpart in the reference, which solves one problem per call) ------------------
+ * Marks the handle's W as block diagonal: problem p owns contacts [contact_ptr[p], contact_ptr[p+1]) and its
+ * rows reference only columns of that range (for example a primal problem whose contact groups share no body,
+ * assembled with bogus_gpu_assemble_dual). contact_ptr has nproblems + 1 entries, from 0 to n. */
+int bogus_gpu_set_batch(bogus_gpu_problem* h, int nproblems, const int* contact_ptr);
+
+/* Solves every problem of the batch in one persistent launch (one CTA per problem, largest first). Each
+ * problem gets exactly the result DualFrictionProblem::solveWith(ProjectedGradient&, r) gives for it alone
+ * (same iterates, residual and iteration count). r: all problems, contact-major, in/out; residuals and iters
+ * hold one entry per problem (NULL allowed). Returns BOGUS_GPU_NOT_CONVERGED if any problem did not converge. */
+int bogus_gpu_solve_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* opts, double* r, double* residuals,
+                             unsigned* iters);
+/* Same with r on the device. */
+int bogus_gpu_solve_pg_batch_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* opts, double* d_r,
+                                    double* residuals, unsigned* iters);
 
 /* Greedy coloring used by bogus_gpu_solve_gs: perm[n] (contact order, colors contiguous) and colors[ncolors+1]
  * offsets; colors must hold n + 1 ints. */

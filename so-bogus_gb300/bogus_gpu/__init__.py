@@ -44,7 +44,8 @@ class PgOptions(C.Structure):
 class GsOptions(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint), ("eval_every", C.c_uint), ("skip_tol", C.c_double),
                 ("skip_iters", C.c_uint), ("auto_regularization", C.c_double), ("try_zero_as_well", C.c_int),
-                ("use_infinity_norm", C.c_int), ("static_problem", C.c_int), ("local_strategy", C.c_int)]
+                ("use_infinity_norm", C.c_int), ("static_problem", C.c_int), ("local_strategy", C.c_int),
+                ("use_coloring", C.c_int)]
 
 
 class SolveStats(C.Structure):
@@ -65,6 +66,7 @@ EXPORTED = [
     "bogus_gpu_solve_pg", "bogus_gpu_solve_pg_device", "bogus_gpu_solve_gs", "bogus_gpu_coloring",
     "bogus_gpu_set_primal", "bogus_gpu_assemble_dual", "bogus_gpu_get_dual_lower", "bogus_gpu_get_solve_stats",
     "bogus_gpu_get_stream", "bogus_gpu_measure_fp64_peak", "bogus_gpu_solve_pg_noalloc",
+    "bogus_gpu_set_batch", "bogus_gpu_solve_pg_batch", "bogus_gpu_solve_pg_batch_device",
 ]
 
 
@@ -100,6 +102,10 @@ def lib():
     L.bogus_gpu_get_solve_stats.argtypes = [vp, C.POINTER(SolveStats)]
     L.bogus_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.bogus_gpu_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.bogus_gpu_set_batch.argtypes = [vp, C.c_int, _ip]
+    L.bogus_gpu_solve_pg_batch.argtypes = [vp, C.POINTER(PgOptions), _dp, _dp, np.ctypeslib.ndpointer(dtype=np.uint32)]
+    L.bogus_gpu_solve_pg_batch_device.argtypes = [vp, C.POINTER(PgOptions), vp, _dp,
+                                                  np.ctypeslib.ndpointer(dtype=np.uint32)]
     L.bogus_gpu_solve_pg_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, C.POINTER(PgOptions), vp,
                                              C.POINTER(C.c_double), C.POINTER(C.c_uint), vp]
     _lib = L
@@ -180,15 +186,32 @@ class ProjectedGradient(_SolverBase):
         return o
 
 
+class Coloring:
+    """GaussSeidel::coloring() (Core/BlockSolvers/Coloring.hpp): update(True) selects the order of
+    Coloring::compute with the contact permutation (as MecheFrictionProblem::solve does with several threads);
+    update(False) — the default — sweeps the contacts in their own order."""
+
+    def __init__(self):
+        self.enabled = False
+
+    def update(self, enable: bool, matrix=None) -> None:
+        self.enabled = bool(enable)
+
+
 class GaussSeidel(_SolverBase):
     """GaussSeidel<WType> (Core/BlockSolvers/GaussSeidel.hpp, GaussSeidelBase.hpp:39-91): tol 1e-6,
-    250 sweeps, evalEvery 25, skipTol 1e-6, skipIters 10, tryZeroAsWell. Always colored."""
+    250 sweeps, evalEvery 25, skipTol 1e-6, skipIters 10, tryZeroAsWell; the sequential sweep of the reference,
+    run level by level on the GPU."""
 
     def __init__(self):
         super().__init__(1e-6, 250)
         self._eval_every, self._skip_tol, self._skip_iters = 25, 1e-6, 10
         self._auto_reg, self._try_zero = 0.0, True
         self._strategy = REV_HYBRID
+        self._coloring = Coloring()
+
+    def coloring(self) -> Coloring:
+        return self._coloring
 
     def setEvalEvery(self, n: int) -> None: self._eval_every = int(n)
     def setSkipTol(self, t: float) -> None: self._skip_tol = float(t)
@@ -206,6 +229,7 @@ class GaussSeidel(_SolverBase):
         o.skip_tol, o.skip_iters, o.auto_regularization = self._skip_tol, self._skip_iters, self._auto_reg
         o.try_zero_as_well, o.use_infinity_norm = int(self._try_zero), int(self._inf)
         o.static_problem, o.local_strategy = int(static_problem), self._strategy
+        o.use_coloring = int(self._coloring.enabled)
         return o
 
 
@@ -368,6 +392,35 @@ class DualFrictionProblem:
         _check(st)
         self.last_status, self.last_iterations = st, it.value
         return res.value, it.value
+
+
+    # ---- batches of independent problems -------------------------------------------------------------
+    def setBatch(self, contact_ptr) -> None:
+        """Marks W as block diagonal: problem p owns contacts [contact_ptr[p], contact_ptr[p+1])."""
+        cp = _i32(contact_ptr)
+        _check(lib().bogus_gpu_set_batch(self._h, cp.size - 1, cp), False)
+        self.nproblems = cp.size - 1
+
+    def solveBatchWith(self, solver: "ProjectedGradient", r, staticProblem: bool = True):
+        """Solves every problem of the batch in one launch (r in place); returns (residuals, iterations)."""
+        if not (isinstance(r, np.ndarray) and r.dtype == np.float64 and r.flags.c_contiguous):
+            raise TypeError("r must be a C-contiguous float64 numpy array (solved in place)")
+        res = np.zeros(self.nproblems)
+        its = np.zeros(self.nproblems, np.uint32)
+        o = solver.options(staticProblem)
+        st = lib().bogus_gpu_solve_pg_batch(self._h, C.byref(o), r.reshape(-1), res, its)
+        _check(st)
+        self.last_status = st
+        return res, its
+
+    def solveBatch_device(self, solver: "ProjectedGradient", d_r_ptr: int, staticProblem: bool = True):
+        res = np.zeros(self.nproblems)
+        its = np.zeros(self.nproblems, np.uint32)
+        o = solver.options(staticProblem)
+        st = lib().bogus_gpu_solve_pg_batch_device(self._h, C.byref(o), C.c_void_p(d_r_ptr), res, its)
+        _check(st)
+        self.last_status = st
+        return res, its
 
 
 def measure_fp64_peak(device: int = 0) -> float:

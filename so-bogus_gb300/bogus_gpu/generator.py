@@ -149,6 +149,30 @@ def grid(nbodies: int = 50_000, ncontacts: int = 200_000, seed: int = 1, ground_
     return PrimalData(minv, objA.astype(np.int32), objB.astype(np.int32), HA, HB, b, mu, seed, "grid")
 
 
+def batch(nproblems: int = 4096, nmin: int = 16, nmax: int = 4096, seed: int = 4, ground_fraction: float = 0.1):
+    """Independent problems with contact counts log-uniform in [nmin, nmax] and bodies = contacts / 3
+    (random pairs), concatenated into one primal problem whose contact groups share no body. Returns
+    (PrimalData, contact_ptr)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.floor(np.exp(rng.uniform(np.log(nmin), np.log(nmax + 1), nproblems))).astype(int)
+    sizes = np.clip(sizes, nmin, nmax)
+    parts, body_off = [], 0
+    for p, n in enumerate(sizes):
+        d = random_pairs(nbodies=max(2, int(n) // 3), ncontacts=int(n), seed=seed * 100003 + p,
+                         ground_fraction=ground_fraction)
+        parts.append((d, body_off))
+        body_off += d.nbodies
+    minv = np.concatenate([d.minv for d, _ in parts])
+    objA = np.concatenate([d.objA + off for d, off in parts]).astype(np.int32)
+    objB = np.concatenate([np.where(d.objB >= 0, d.objB + off, -1) for d, off in parts]).astype(np.int32)
+    HA = np.concatenate([d.HA for d, _ in parts])
+    HB = np.concatenate([d.HB for d, _ in parts])
+    b = np.concatenate([d.b for d, _ in parts])
+    mu = np.concatenate([d.mu for d, _ in parts])
+    contact_ptr = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32)
+    return PrimalData(minv, objA, objB, HA, HB, b, mu, seed, "batch"), contact_ptr
+
+
 CONFIGS = {
     "c1": dict(fn=random_pairs, kw=dict(nbodies=200, ncontacts=500, seed=0)),
     "c2": dict(fn=grid, kw=dict(nbodies=50_000, ncontacts=200_000, seed=1)),

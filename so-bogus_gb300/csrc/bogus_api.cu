@@ -71,6 +71,8 @@ struct DevBuf {
 struct GSCache {
   bool valid = false;
   std::vector<int> perm, colors;
+  std::vector<int> level_off;  // contacts of level L: order[level_off[L] .. level_off[L+1])
+  DevBuf<int> order;
   DevBuf<int> rowptr, col;
   DevBuf<double> val, local, reg, scaling, b, mu;
   DevBuf<double> x, nx2, ndx2, y, chunk, scalar, xbest;
@@ -78,7 +80,21 @@ struct GSCache {
   DevBuf<unsigned long long> tile_max;
   DevBuf<double> ndx_ref;
   double auto_reg = -1.0;
+  int use_coloring = -1;
+  // one captured sweep per ndxRef parity, keyed by the law / strategy / skip settings baked into it
+  cudaGraphExec_t sweep[2] = {nullptr, nullptr};
+  long long sweep_key = -1;
+  void drop_graphs() {
+    for (auto& g : sweep)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+    sweep_key = -1;
+  }
   void release() {
+    drop_graphs();
+    order.release();
     rowptr.release(); col.release(); val.release(); local.release(); reg.release(); scaling.release();
     b.release(); mu.release(); x.release(); nx2.release(); ndx2.release(); y.release(); chunk.release();
     scalar.release(); xbest.release(); skip.release(); processed.release(); tile_max.release(); ndx_ref.release();
@@ -119,6 +135,11 @@ struct bogus_gpu_problem {
   DevBuf<double> minv, H, T, mf;
   DevBuf<int> cb;  // per contact: body of slot 0, body of slot 1 (-1), slot order by body index
   std::vector<int> h_cb;
+  // batch partition (block-diagonal W)
+  int nproblems = 0;
+  std::vector<int> h_contact_ptr, h_problem_nnz;
+  DevBuf<int> contact_ptr, chunk_ptr, queue, col_local, next;
+  DevBuf<PGOut> batch_out;
   bogus_gpu_callback callback = nullptr;
   void* callback_user = nullptr;
   float last_ms = 0.f;
@@ -169,6 +190,7 @@ int upload_full(bogus_gpu_problem* h, const HostBSR& f, const double* b, const d
   BG_CUDA(cudaStreamSynchronize(h->stream));
   h->has_dual = true;
   h->gs.valid = false;
+  h->nproblems = 0;
   return BOGUS_GPU_OK;
 }
 
@@ -296,13 +318,20 @@ int check_pg_options(const bogus_gpu_pg_options* o) {
 }
 
 // ---- Gauss-Seidel ---------------------------------------------------------------------------------
-int prepare_gs(bogus_gpu_problem* h, double auto_reg) {
+int prepare_gs(bogus_gpu_problem* h, double auto_reg, int use_coloring) {
   GSCache& g = h->gs;
-  if (g.valid && g.auto_reg == auto_reg) return BOGUS_GPU_OK;
+  if (g.valid && g.auto_reg == auto_reg && g.use_coloring == use_coloring) return BOGUS_GPU_OK;
   if (!h->host_lower_valid) return fail(BOGUS_GPU_BAD_INPUT, "Gauss-Seidel needs W set from host arrays");
+  g.drop_graphs();
   const HostBSR& low = h->host_lower;
   const int n = low.n;
-  greedy_coloring(low, g.perm, g.colors);
+  if (use_coloring) {
+    greedy_coloring(low, g.perm, g.colors);
+  } else {
+    g.perm.resize(n);
+    for (int i = 0; i < n; ++i) g.perm[i] = i;
+    g.colors = {0, n};
+  }
   const HostBSR plow = permute_lower(low, g.perm);
   const HostBSR pf = expand_lower(n, plow.rowptr.data(), plow.col.data(), plow.val.data());
   std::vector<double> pb(3 * (size_t)n), pmu(n), local(9 * (size_t)n, 0.0), reg(n, 0.0), sc(n, 1.0);
@@ -321,8 +350,27 @@ int prepare_gs(bogus_gpu_problem* h, double auto_reg) {
       D[8] += reg[i];
     }
   }
+  // levels of the sweep (renumbered so that the sweep visits 0, 1, 2, ...): one more than the highest level
+  // among the earlier neighbours, i.e. the lower-triangle neighbours of the permuted matrix
+  std::vector<int> level(n, 0);
+  int nlevels = n > 0 ? 1 : 0;
+  for (int i = 0; i < n; ++i) {
+    int lv = 0;
+    for (int k = plow.rowptr[i]; k < plow.rowptr[i + 1]; ++k) {
+      const int j = plow.col[k];
+      if (j < i && level[j] + 1 > lv) lv = level[j] + 1;
+    }
+    level[i] = lv;
+    if (lv + 1 > nlevels) nlevels = lv + 1;
+  }
+  g.level_off.assign(nlevels + 1, 0);
+  for (int i = 0; i < n; ++i) ++g.level_off[level[i] + 1];
+  for (int L = 0; L < nlevels; ++L) g.level_off[L + 1] += g.level_off[L];
+  std::vector<int> order(n), fill(g.level_off.begin(), g.level_off.end() - 1);
+  for (int i = 0; i < n; ++i) order[fill[level[i]]++] = i;
   const int nnz = pf.nnzb();
   const int ntiles = (n + kGSTile - 1) / kGSTile;
+  BG_CUDA(g.order.ensure(n));
   BG_CUDA(g.rowptr.ensure(n + 1));
   BG_CUDA(g.col.ensure(nnz));
   BG_CUDA(g.val.ensure(9 * (size_t)nnz));
@@ -349,6 +397,7 @@ int prepare_gs(bogus_gpu_problem* h, double auto_reg) {
     BG_CUDA(cudaMemcpyAsync(g.val.p, pf.val.data(), sizeof(double) * 9 * (size_t)nnz, cudaMemcpyHostToDevice, s));
   }
   if (n) {
+    BG_CUDA(cudaMemcpyAsync(g.order.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
     BG_CUDA(cudaMemcpyAsync(g.local.p, local.data(), sizeof(double) * 9 * (size_t)n, cudaMemcpyHostToDevice, s));
     BG_CUDA(cudaMemcpyAsync(g.reg.p, reg.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
     BG_CUDA(cudaMemcpyAsync(g.scaling.p, sc.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
@@ -357,7 +406,37 @@ int prepare_gs(bogus_gpu_problem* h, double auto_reg) {
   }
   BG_CUDA(cudaStreamSynchronize(s));
   g.auto_reg = auto_reg;
+  g.use_coloring = use_coloring;
   g.valid = true;
+  return BOGUS_GPU_OK;
+}
+
+// One sweep: every level in order, then the skip update. Captured once per parity into a CUDA graph and
+// replayed (the arguments never change between sweeps of the same settings).
+int launch_sweep(bogus_gpu_problem* h, const GSArgs& a, int parity, double abs_skip_tol, double skip_tol,
+                 int abs_skip_iters, long long key) {
+  GSCache& g = h->gs;
+  cudaStream_t s = h->stream;
+  const int nlevels = (int)g.level_off.size() - 1;
+  if (g.sweep_key != key) g.drop_graphs();
+  if (!g.sweep[parity]) {
+    cudaGraph_t graph = nullptr;
+    BG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int L = 0; L < nlevels && e == cudaSuccess; ++L) e = launch_gs_level(a, g.level_off[L], g.level_off[L + 1], parity, s);
+    if (e == cudaSuccess) e = launch_gs_skip(a, parity, abs_skip_tol, skip_tol, abs_skip_iters, s);
+    const cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return fail(BOGUS_GPU_CUDA_ERROR, std::string("sweep capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    const cudaError_t e3 = cudaGraphInstantiate(&g.sweep[parity], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e3 != cudaSuccess) return fail(BOGUS_GPU_CUDA_ERROR, std::string("sweep instantiate: ") + cudaGetErrorString(e3));
+    g.sweep_key = key;
+  }
+  BG_CUDA(cudaGraphLaunch(g.sweep[parity], s));
+  h->last_launches += nlevels + 1;
   return BOGUS_GPU_OK;
 }
 
@@ -415,6 +494,7 @@ void bogus_gpu_gs_options_default(bogus_gpu_gs_options* o) {
   o->use_infinity_norm = 0;
   o->static_problem = 0;
   o->local_strategy = BOGUS_GPU_LOCAL_REV_HYBRID;
+  o->use_coloring = 0;
 }
 
 const char* bogus_gpu_status_string(int s) {
@@ -467,6 +547,12 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   h->rowptr.release();
   h->col.release();
   h->diag.release();
+  h->contact_ptr.release();
+  h->chunk_ptr.release();
+  h->queue.release();
+  h->col_local.release();
+  h->next.release();
+  h->batch_out.release();
   h->cb.release();
   h->pgout.release();
   h->barrier.release();
@@ -542,6 +628,7 @@ int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* 
   h->has_dual = true;
   h->host_lower_valid = false;
   h->gs.valid = false;
+  h->nproblems = 0;
   return BOGUS_GPU_OK;
 }
 
@@ -673,7 +760,7 @@ int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, doub
     return BOGUS_GPU_OK;
   }
   if (int e = check_finite(r, n3, "r")) return e;
-  if (int e = prepare_gs(h, o->auto_regularization)) return e;
+  if (int e = prepare_gs(h, o->auto_regularization, o->use_coloring ? 1 : 0)) return e;
   GSCache& g = h->gs;
   cudaStream_t s = h->stream;
   h->last_launches = 0;
@@ -704,6 +791,7 @@ int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, doub
   a.processed = g.processed.p;
   a.tile_max = g.tile_max.p;
   a.ndx_ref = g.ndx_ref.p;
+  a.order = g.order.p;
   a.desaxce = o->static_problem ? 0 : 1;
   a.strat = o->local_strategy;
   const bool desaxce = !o->static_problem;
@@ -740,14 +828,22 @@ int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, doub
   trace.push_back({0u, err_best});
   const double abs_skip_tol = dmin(o->skip_tol, o->tol);
   const int abs_skip_iters = (int)dmin((double)o->skip_iters, (double)(unsigned)std::sqrt((double)n));
-  const int ncolors = (int)g.colors.size() - 1;
+  // settings baked into the captured sweeps
+  long long key = 0;
+  {
+    double st = o->skip_tol, ast = abs_skip_tol;
+    unsigned long long b1, b2;
+    std::memcpy(&b1, &st, 8);
+    std::memcpy(&b2, &ast, 8);
+    key = (long long)((b1 * 1000003ull) ^ (b2 * 10007ull) ^ ((unsigned long long)abs_skip_iters << 8) ^
+                      ((unsigned long long)a.desaxce << 4) ^ (unsigned long long)a.strat);
+    if (key < 0) key = -key - 1;
+  }
   unsigned it;
   int parity = 0;
   bool converged = false;
   for (it = 1; it <= o->max_iters; ++it) {
-    for (int c = 0; c < ncolors; ++c) BG_CUDA(launch_gs_color(a, g.colors[c], g.colors[c + 1], parity, s));
-    BG_CUDA(launch_gs_skip(a, parity, abs_skip_tol, o->skip_tol, abs_skip_iters, s));
-    h->last_launches += ncolors + 1;
+    if (int e = launch_sweep(h, a, parity, abs_skip_tol, o->skip_tol, abs_skip_iters, key)) return e;
     parity ^= 1;
     if (0 == (it % o->eval_every)) {
       if (int e = gs_eval(h, a, g.x.p, g.b.p, desaxce, use_inf, &err)) return e;
@@ -964,7 +1060,184 @@ int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double*
   d_w.release(); d_f.release();
   h->has_dual = true;
   h->gs.valid = false;
+  h->nproblems = 0;
   return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_set_batch(bogus_gpu_problem* h, int nproblems, const int* cptr) {
+  if (int e = check_handle(h)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (nproblems < 0 || (nproblems > 0 && !cptr)) return fail(BOGUS_GPU_BAD_INPUT, "invalid batch partition");
+  const int n = h->W.n;
+  if (nproblems == 0 ? n != 0 : (cptr[0] != 0 || cptr[nproblems] != n))
+    return fail(BOGUS_GPU_BAD_INPUT, "contact_ptr must run from 0 to the number of contacts");
+  for (int p = 0; p < nproblems; ++p)
+    if (cptr[p + 1] < cptr[p]) return fail(BOGUS_GPU_BAD_INPUT, "contact_ptr not monotone");
+  if (int e = set_device(h)) return e;
+  // structure of the both-triangle W, to check block-diagonality and localise the column indices
+  std::vector<int> rp(n + 1), cl(h->W.nnzb);
+  BG_CUDA(cudaMemcpyAsync(rp.data(), h->W.rowptr, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, h->stream));
+  if (h->W.nnzb) BG_CUDA(cudaMemcpyAsync(cl.data(), h->W.col, sizeof(int) * h->W.nnzb, cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  std::vector<int> chunk(nproblems + 1, 0), nnz(nproblems, 0);
+  for (int p = 0; p < nproblems; ++p) {
+    const int c0 = cptr[p], c1 = cptr[p + 1];
+    for (int i = c0; i < c1; ++i)
+      for (int k = rp[i]; k < rp[i + 1]; ++k) {
+        if (cl[k] < c0 || cl[k] >= c1)
+          return fail(BOGUS_GPU_BAD_INPUT, "W is not block diagonal for this partition (row " + std::to_string(i) + ")");
+        cl[k] -= c0;
+      }
+    nnz[p] = rp[c1] - rp[c0];
+    chunk[p + 1] = chunk[p] + (c1 - c0 + 31) / 32;
+  }
+  std::vector<int> queue(nproblems);
+  for (int p = 0; p < nproblems; ++p) queue[p] = p;
+  std::stable_sort(queue.begin(), queue.end(),
+                   [&](int a, int b) { return cptr[a + 1] - cptr[a] > cptr[b + 1] - cptr[b]; });
+  BG_CUDA(h->contact_ptr.ensure(nproblems + 1));
+  BG_CUDA(h->chunk_ptr.ensure(nproblems + 1));
+  BG_CUDA(h->queue.ensure(nproblems > 0 ? nproblems : 1));
+  BG_CUDA(h->col_local.ensure(h->W.nnzb));
+  BG_CUDA(h->next.ensure(1));
+  BG_CUDA(h->batch_out.ensure(nproblems > 0 ? nproblems : 1));
+  cudaStream_t s = h->stream;
+  BG_CUDA(cudaMemcpyAsync(h->contact_ptr.p, cptr, sizeof(int) * (nproblems + 1), cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(h->chunk_ptr.p, chunk.data(), sizeof(int) * (nproblems + 1), cudaMemcpyHostToDevice, s));
+  if (nproblems) BG_CUDA(cudaMemcpyAsync(h->queue.p, queue.data(), sizeof(int) * nproblems, cudaMemcpyHostToDevice, s));
+  if (h->W.nnzb) BG_CUDA(cudaMemcpyAsync(h->col_local.p, cl.data(), sizeof(int) * h->W.nnzb, cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  h->nproblems = nproblems;
+  h->h_contact_ptr.assign(cptr, cptr + nproblems + 1);
+  h->h_problem_nnz = nnz;
+  return BOGUS_GPU_OK;
+}
+
+namespace {
+
+int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residuals, unsigned* iters) {
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  const int np = h->nproblems;
+  PGBatchArgs ba{};
+  PGArgs& a = ba.base;
+  a.rowptr = h->W.rowptr;
+  a.col = h->col_local.p;
+  a.val = h->W.val;
+  a.b = h->b.p;
+  a.mu = h->mu.p;
+  a.scaling = h->scaling.p;
+  a.X0 = h->X.p;
+  a.X1 = h->X.p + n3;
+  a.X2 = h->X.p + 2 * n3;
+  a.MX0 = h->MX.p;
+  a.MX1 = h->MX.p + n3;
+  a.Y = h->Y.p;
+  a.S0 = h->S0.p;
+  a.XB = h->XB.p;
+  a.Wv = h->Wv.p;
+  a.csum = h->csum.p;
+  a.out = h->batch_out.p;
+  a.desaxce = o->static_problem ? 0 : 1;
+  a.variant = o->variant;
+  a.use_inf = o->use_infinity_norm ? 1 : 0;
+  a.tol = o->tol;
+  a.opt = o->ls_optimistic_factor;
+  a.pess = o->ls_pessimistic_factor;
+  a.max_iters = o->max_iters;
+  a.ls_iters = o->ls_iters;
+  ba.nproblems = np;
+  ba.contact_ptr = h->contact_ptr.p;
+  ba.chunk_ptr = h->chunk_ptr.p;
+  ba.queue = h->queue.p;
+  ba.next = h->next.p;
+  ba.r = h->X.p;  // each problem's best iterate is copied over its initial iterate
+  int grid = pg_batched_grid(h->device);
+  if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "occupancy query failed");
+  if (np < grid) grid = np > 0 ? np : 1;
+  BG_CUDA(cudaMemsetAsync(h->next.p, 0, sizeof(int), h->stream));
+  BG_CUDA(cudaEventRecord(h->ev0, h->stream));
+  BG_CUDA(launch_pg_batched(ba, grid, h->stream));
+  BG_CUDA(cudaEventRecord(h->ev1, h->stream));
+  std::vector<PGOut> out(np);
+  if (np) BG_CUDA(cudaMemcpyAsync(out.data(), h->batch_out.p, sizeof(PGOut) * np, cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  h->last_launches = 1;
+  bool all = true;
+  double bytes = 0, fma = 0;
+  unsigned passes = 0, maxit = 0;
+  const bool spg = o->variant == BOGUS_GPU_PG_SPG;
+  const double per_contact[9] = {56, 48, spg ? 168.0 : 144.0, 152, 80, 72, 144, 120, 96};
+  const bool has_w[9] = {false, true, false, true, false, false, true, false, true};
+  for (int p = 0; p < np; ++p) {
+    if (residuals) residuals[p] = out[p].min_res;
+    if (iters) iters[p] = out[p].iters;
+    all = all && (out[p].converged || h->h_contact_ptr[p + 1] == h->h_contact_ptr[p]);
+    const int np_c = h->h_contact_ptr[p + 1] - h->h_contact_ptr[p];
+    const double wpass = (double)h->h_problem_nnz[p] * 76.0 + 4.0 * (np_c + 1);
+    for (int k = 0; k < 9; ++k) {
+      bytes += out[p].phases[k] * (per_contact[k] * np_c + (has_w[k] ? wpass : 0.0));
+      if (has_w[k]) {
+        passes += out[p].phases[k];
+        fma += out[p].phases[k] * 9.0 * h->h_problem_nnz[p] * (k == 1 ? 2.0 : 1.0);
+      }
+    }
+    if (out[p].iters > maxit) maxit = out[p].iters;
+  }
+  h->last_stats.iterations = maxit;
+  h->last_stats.w_passes = passes;
+  h->last_stats.algorithmic_bytes = bytes;
+  h->last_stats.fp64_fma = fma;
+  return all ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
+}
+
+int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
+  if (int e = check_handle(h)) return e;
+  if (int e = check_pg_options(o)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (h->nproblems == 0 && h->W.n > 0) return fail(BOGUS_GPU_NO_PROBLEM, "no batch partition set (bogus_gpu_set_batch)");
+  if (int e = set_device(h)) return e;
+  const int n = h->W.n;
+  BG_CUDA(h->X.ensure(3 * 3 * (size_t)n));
+  BG_CUDA(h->MX.ensure(2 * 3 * (size_t)n));
+  BG_CUDA(h->Y.ensure(3 * (size_t)n));
+  BG_CUDA(h->S0.ensure(n));
+  BG_CUDA(h->XB.ensure(3 * (size_t)n));
+  BG_CUDA(h->Wv.ensure(3 * (size_t)n));
+  size_t tot_chunks = 0;
+  for (int p = 0; p < h->nproblems; ++p) tot_chunks += (h->h_contact_ptr[p + 1] - h->h_contact_ptr[p] + 31) / 32;
+  BG_CUDA(h->csum.ensure(4 * tot_chunks + 4));
+  return BOGUS_GPU_OK;
+}
+
+}  // namespace
+
+int bogus_gpu_solve_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, double* residuals,
+                             unsigned* iters) {
+  if (int e = batch_checks(h, o)) return e;
+  const size_t n3 = 3 * (size_t)h->W.n;
+  if (n3 == 0) return BOGUS_GPU_OK;
+  if (int e = check_finite(r, n3, "r")) return e;
+  BG_CUDA(cudaMemcpyAsync(h->X.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, h->stream));
+  const int st = run_pg_batch(h, o, residuals, iters);
+  if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+  BG_CUDA(cudaMemcpyAsync(r, h->X.p, sizeof(double) * n3, cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  return st;
+}
+
+int bogus_gpu_solve_pg_batch_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* d_r, double* residuals,
+                                    unsigned* iters) {
+  if (int e = batch_checks(h, o)) return e;
+  const size_t n3 = 3 * (size_t)h->W.n;
+  if (n3 == 0) return BOGUS_GPU_OK;
+  BG_CUDA(cudaMemcpyAsync(h->X.p, d_r, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+  const int st = run_pg_batch(h, o, residuals, iters);
+  if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+  BG_CUDA(cudaMemcpyAsync(d_r, h->X.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  return st;
 }
 
 int bogus_gpu_get_dual_lower(bogus_gpu_problem* h, int* rowptr, int* colidx, double* blocks, int* nnzb_lower) {

@@ -61,6 +61,18 @@ struct PGArgs {
   unsigned max_iters, ls_iters;
 };
 
+// Batched solves: problem p owns contacts [contact_ptr[p], contact_ptr[p+1]) of every per-contact array of
+// `base` and chunk sums from 4 * chunk_ptr[p]; W rows are global, column indices local to the problem.
+struct PGBatchArgs {
+  PGArgs base;
+  int nproblems;
+  const int* contact_ptr;
+  const int* chunk_ptr;
+  const int* queue;  // problem order (largest first)
+  int* next;         // queue position counter (zeroed before the launch)
+  double* r;         // results, contact-major over all problems
+};
+
 // Launchers (kernels_basic.cu)
 cudaError_t launch_spmv(const DevBSR& W, const double* x, const double* init, double* y, cudaStream_t s);
 cudaError_t launch_eval_chunks(int n, const double* x, const double* u, const double* mu, const double* scaling,
@@ -73,6 +85,8 @@ cudaError_t launch_add(int m, const double* a, const double* b, double* y, cudaS
 // Persistent solvers (kernels_pg.cu)
 cudaError_t launch_pg_persistent(const PGArgs& a, int grid, cudaStream_t s);
 int pg_max_grid(int device);
+cudaError_t launch_pg_batched(const PGBatchArgs& b, int grid, cudaStream_t s);
+int pg_batched_grid(int device);
 
 // Gauss-Seidel (kernels_gs.cu)
 struct GSArgs {
@@ -92,10 +106,11 @@ struct GSArgs {
   unsigned char* processed;
   unsigned long long* tile_max;  // 2 * ntiles (sweep parity)
   double* ndx_ref;               // 2 (sweep parity)
+  const int* order;              // contacts grouped by level (sweep positions)
   int desaxce, strat;
 };
 constexpr int kGSTile = 1024;
-cudaError_t launch_gs_color(const GSArgs& a, int c0, int c1, int parity, cudaStream_t s);
+cudaError_t launch_gs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s);
 cudaError_t launch_gs_skip(const GSArgs& a, int parity, double abs_skip_tol, double skip_tol, int abs_skip_iters,
                            cudaStream_t s);
 cudaError_t launch_scale_scalar(double* p, double divisor, cudaStream_t s);

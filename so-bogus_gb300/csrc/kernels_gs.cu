@@ -1,13 +1,17 @@
-// Colored projected Gauss-Seidel (Core/BlockSolvers/GaussSeidel.impl.hpp:62-124).
+// Projected Gauss-Seidel sweep (Core/BlockSolvers/GaussSeidel.impl.hpp:62-124), level by level.
 //
-// The problem is permuted so that every color is a contiguous range of contacts (MecheInterface.cpp:330-337).
-// Contacts of one color share no block of W, so one launch per color solves them all at once with the
-// same result as the reference's sequential sweep: thread i gathers its split row
+// The sweep order is the contacts' own order or, with coloring, the order of Coloring::compute after the
+// contact permutation (MecheInterface.cpp:330-337); the problem is renumbered so that the sweep visits
+// contacts 0, 1, 2, ... In the sequential sweep, contact i reads the new value of every neighbour visited
+// before it and the old value of every neighbour visited after it. Give each contact the level
+// 1 + max(level of its earlier neighbours): contacts of one level share no block of W, and processing the
+// levels in increasing order gives every contact exactly the values the sequential sweep gives it. So one
+// launch per level reproduces the sequential result bit for bit: thread i gathers its split row
 // b_i - reg_i x_i + sum_{j != i} W_ij x_j (columns in increasing order, canonical chain), runs the local
 // Coulomb / SOC solver and applies the (possibly halved) update.
 //
 // The skip heuristic (:107-117) depends on ndxRef, a running maximum over the contacts already visited in
-// the sweep. It is reproduced exactly after each sweep: the color kernels record every solved contact's
+// the sweep. It is reproduced exactly after each sweep: the level kernels record every solved contact's
 // step norm and a per-tile maximum (max is order-independent), and k_gs_skip turns them into the
 // sequential prefix maximum and the skip counters.
 #include "internal.h"
@@ -17,9 +21,12 @@ namespace bogus_gpu {
 
 __device__ __forceinline__ unsigned long long dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
 
-__global__ void __launch_bounds__(128) k_gs_color(GSArgs a, int c0, int c1, int parity) {
-  const int i = c0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c1) return;
+// One warp per CTA: a level is latency bound (long dependent FP64 chains per contact), so its contacts are
+// spread over as many SMs as possible.
+__global__ void __launch_bounds__(32) k_gs_level(GSArgs a, int l0, int l1, int parity) {
+  const int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= l1) return;
+  const int i = a.order[t];
   if (a.skip[i]) {
     a.skip[i] = (unsigned char)(a.skip[i] - 1);
     a.processed[i] = 0;
@@ -73,9 +80,9 @@ __global__ void __launch_bounds__(128) k_gs_color(GSArgs a, int c0, int c1, int 
   }
 }
 
-cudaError_t launch_gs_color(const GSArgs& a, int c0, int c1, int parity, cudaStream_t s) {
-  if (c1 <= c0) return cudaSuccess;
-  k_gs_color<<<(c1 - c0 + 127) / 128, 128, 0, s>>>(a, c0, c1, parity);
+cudaError_t launch_gs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s) {
+  if (l1 <= l0) return cudaSuccess;
+  k_gs_level<<<(l1 - l0 + 31) / 32, 32, 0, s>>>(a, l0, l1, parity);
   return cudaGetLastError();
 }
 

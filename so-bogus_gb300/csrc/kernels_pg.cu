@@ -95,12 +95,12 @@ __device__ __forceinline__ int third(int p, int q) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
-  __shared__ double smem8[8];
+template <class Ctx>
+__device__ int pg_body(const PGArgs& a, Ctx& ctx) {
   const Bufs B{a};
   const int lane = threadIdx.x & 31;
-  const int gw = blockIdx.x * 8 + (threadIdx.x >> 5);
-  const int nw = gridDim.x * 8;
+  const int gw = ctx.first_warp();
+  const int nw = ctx.num_warps();
   const bool desaxce = a.desaxce != 0;
   const bool spg = a.variant == 4;
   const bool apgd = a.variant == 3;
@@ -111,22 +111,14 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
     v = is_max ? warp_max_butterfly(v) : warp_sum_butterfly(v);
     if (lane == 0) a.csum[q * C + c] = v;
   };
-  auto publish = [&](int K, unsigned maxmask) {
-    for (int q = 0; q < K; ++q) {
-      const double v = block8_combine(a.csum + q * C, C, (maxmask >> q) & 1u, smem8);
-      if (threadIdx.x == 0) a.scal[q] = v;
-    }
-  };
-  auto sync = [&]() -> bool { return grid_barrier(a.gb, [] {}); };
-  auto sync_reduce = [&](int K, unsigned maxmask) -> bool {
-    return grid_barrier(a.gb, [&] { publish(K, maxmask); });
-  };
-  auto scal = [&](int q) { return ldcg(a.scal + q); };
+  auto sync = [&]() -> bool { return ctx.sync(); };
+  auto sync_reduce = [&](int K, unsigned maxmask) -> bool { return ctx.sync_reduce(K, maxmask); };
+  auto scal = [&](int q) { return ctx.scal(q); };
   // ConstrainedSolverBase::eval: sum / (1 + n), or the maximum with the infinity norm
   auto residual_of = [&](double reduced) { return a.use_inf ? reduced : reduced / (double)(1 + a.n); };
   unsigned ph[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  auto finish = [&](double min_res, unsigned iters, int best_buf, int converged) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+  auto finish = [&](double min_res, unsigned iters, int best_buf, int converged) -> int {
+    if (ctx.writer()) {
       a.out->min_res = min_res;
       a.out->iters = iters;
       a.out->best_buf = best_buf;
@@ -134,6 +126,7 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
 #pragma unroll
       for (int k = 0; k < 9; ++k) a.out->phases[k] = ph[k];
     }
+    return best_buf;
   };
 
   int ix = 0, iprev = 0, ixs = 1, imx = 0;
@@ -149,7 +142,7 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
       store3(a.X0, i, x);
     }
   }
-  if (!sync()) return;
+  if (!sync()) return -1;
 
   // Mx = W x (:93) and guess_alpha (:21-28): |W (x - 1)|^2, |x - 1|^2
   ph[1]++;
@@ -169,15 +162,14 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
     put(0, c, v0, false);
     put(1, c, v1, false);
   }
-  if (!sync_reduce(2, 0u)) return;
+  if (!sync_reduce(2, 0u)) return -1;
   double alpha = 1.0;
   {
     const double nMx = scal(0);
     if (nMx > 1.e-16) alpha = dmin(1., scal(1) / nMx);
   }
   if (a.max_iters == 0) {
-    finish(-1.0, 0, 0, 0);
-    return;
+    return finish(-1.0, 0, 0, 0);
   }
 
   // Row-local part A, given Mx_i: writes y, s0 and xs = P(x - alpha_t y) (APGD) and returns the residual
@@ -235,17 +227,16 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
   if (!spg) {
     // ---------------------------------------------------------------- APGD / Descent
     double alpha_t = alpha * a.opt;
-    if (!runA(alpha_t)) return;
+    if (!runA(alpha_t)) return -1;
     for (;;) {
       const double res = residual_of(scal(0)), J = scal(1);
-      if (blockIdx.x == 0 && threadIdx.x == 0) a.trace[it] = res;
+      if (a.trace && ctx.writer()) a.trace[it] = res;
       if (it == 0 || res < min_res) {
         min_res = res;
         best_pending = true;
       }
       if (res < a.tol) {
-        finish(min_res, it, best_pending ? ix : 3, 1);
-        return;
+        return finish(min_res, it, best_pending ? ix : 3, 1);
       }
       alpha = alpha_t;
       unsigned ls = 0;
@@ -282,7 +273,7 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
           put(3, c, v3, false);
         }
         best_pending = false;
-        if (!sync_reduce(4, 0u)) return;
+        if (!sync_reduce(4, 0u)) return -1;
         const double Js = scal(0), decr = scal(1), nrm = scal(2);
         decr2 = scal(3);
         if (Js < (J + decr) + (.5 / alpha) * nrm) break;
@@ -302,7 +293,7 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
             store3(B.X(ixs), i, xs);
           }
         }
-        if (!sync()) return;
+        if (!sync()) return -1;
       }
       ++it;
       const bool more = it < a.max_iters;
@@ -321,7 +312,7 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
             store3(B.X(ix), i, xn);
           }
         }
-        if (!sync()) return;
+        if (!sync()) return -1;
         iprev = ixs;
         ixs = third(ix, iprev);
         if (!more) break;
@@ -340,7 +331,7 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
           put(0, c, r, res_mask != 0);
           put(1, c, q, false);
         }
-        if (!sync_reduce(2, res_mask)) return;
+        if (!sync_reduce(2, res_mask)) return -1;
       } else {
         theta = 1.;
         ix = ixs;
@@ -349,26 +340,24 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
         ixs = (ix + 1) % 3;
         if (!more) break;
         alpha_t = alpha * a.opt;
-        if (!runA(alpha_t)) return;
+        if (!runA(alpha_t)) return -1;
       }
     }
-    finish(min_res, it, 3, 0);
-    return;
+    return finish(min_res, it, 3, 0);
   }
 
   // ------------------------------------------------------------------ SPG (:288-351)
   const double a_min = 1.e-6, a_max = 1.e6;
   for (;;) {
-    if (!runA(alpha)) return;  // y, residual, s, xs = P(x - alpha y), (xs - prev).y
+    if (!runA(alpha)) return -1;  // y, residual, s, xs = P(x - alpha y), (xs - prev).y
     const double res = residual_of(scal(0)), decr = scal(1);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.trace[it] = res;
+    if (a.trace && ctx.writer()) a.trace[it] = res;
     if (it == 0 || res < min_res) {
       min_res = res;
       best_pending = true;
     }
     if (res < a.tol) {
-      finish(min_res, it, best_pending ? ix : 3, 1);
-      return;
+      return finish(min_res, it, best_pending ? ix : 3, 1);
     }
     const bool mom = decr < 0.;
     const double beta = mom ? nesterov_inertia(theta, 0.0) : 0.0;
@@ -397,7 +386,7 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
       }
     }
     best_pending = false;
-    if (!sync()) return;
+    if (!sync()) return -1;
     // E: Mx_new = W x; z = -Mx_old + Mx_new; w.z, |z|^2
     ph[8]++;
     for (int c = gw; c < C; c += nw) {
@@ -416,7 +405,7 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
       put(0, c, v0, false);
       put(1, c, v1, false);
     }
-    if (!sync_reduce(2, 0u)) return;
+    if (!sync_reduce(2, 0u)) return -1;
     imx = 1 - imx;
     iprev = ixs;
     ixs = third(ix, iprev);
@@ -425,7 +414,113 @@ __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
     ++it;
     if (it >= a.max_iters) break;
   }
-  finish(min_res, it, 3, 0);
+  return finish(min_res, it, 3, 0);
+}
+
+
+// Single problem: the whole GPU, phases separated by the bounded grid barrier; the last CTA to arrive
+// publishes the reduced scalars in global memory.
+struct GridCtx {
+  const PGArgs& a;
+  double* smem8;
+  __device__ int first_warp() const { return blockIdx.x * 8 + (threadIdx.x >> 5); }
+  __device__ int num_warps() const { return gridDim.x * 8; }
+  __device__ bool writer() const { return blockIdx.x == 0 && threadIdx.x == 0; }
+  __device__ void publish(int K, unsigned maxmask) {
+    for (int q = 0; q < K; ++q) {
+      const double v = block8_combine(a.csum + q * a.nchunks, a.nchunks, (maxmask >> q) & 1u, smem8);
+      if (threadIdx.x == 0) a.scal[q] = v;
+    }
+  }
+  __device__ bool sync() { return grid_barrier(a.gb, [] {}); }
+  __device__ bool sync_reduce(int K, unsigned maxmask) { return grid_barrier(a.gb, [&] { publish(K, maxmask); }); }
+  __device__ double scal(int q) const { return ldcg(a.scal + q); }
+};
+
+__global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
+  __shared__ double smem8[8];
+  GridCtx ctx{a, smem8};
+  pg_body(a, ctx);
+}
+
+// One problem per CTA (batched solves): phases separated by __syncthreads, scalars reduced by the CTA's
+// 8 warps (the same 8-stripe combination) and kept in shared memory.
+struct BlockCtx {
+  const PGArgs& a;
+  double* smem8;
+  double* sscal;
+  __device__ int first_warp() const { return threadIdx.x >> 5; }
+  __device__ int num_warps() const { return 8; }
+  __device__ bool writer() const { return threadIdx.x == 0; }
+  __device__ bool sync() {
+    __syncthreads();
+    return true;
+  }
+  __device__ bool sync_reduce(int K, unsigned maxmask) {
+    __syncthreads();
+    for (int q = 0; q < K; ++q) {
+      const double v = block8_combine(a.csum + q * a.nchunks, a.nchunks, (maxmask >> q) & 1u, smem8);
+      if (threadIdx.x == 0) sscal[q] = v;
+    }
+    __syncthreads();
+    return true;
+  }
+  __device__ double scal(int q) const { return sscal[q]; }
+};
+
+// Batched solves: CTAs take problems from a queue (largest first); each runs the complete solve of its
+// problem with the same arithmetic as the single-problem kernel, then writes the best iterate to r.
+__global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgs ba) {
+  __shared__ double smem8[8], sscal[8];
+  __shared__ int s_job;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_job = atomicAdd(ba.next, 1);
+    __syncthreads();
+    const int job = s_job;
+    if (job >= ba.nproblems) return;
+    const int p = ba.queue[job];
+    const int c0 = ba.contact_ptr[p];
+    const int n = ba.contact_ptr[p + 1] - c0;
+    PGArgs a = ba.base;
+    a.n = n;
+    a.nchunks = (n + 31) / 32;
+    a.rowptr = ba.base.rowptr + c0;
+    a.b = ba.base.b + 3 * (size_t)c0;
+    a.mu = ba.base.mu + c0;
+    a.scaling = ba.base.scaling + c0;
+    a.X0 = ba.base.X0 + 3 * (size_t)c0;
+    a.X1 = ba.base.X1 + 3 * (size_t)c0;
+    a.X2 = ba.base.X2 + 3 * (size_t)c0;
+    a.MX0 = ba.base.MX0 + 3 * (size_t)c0;
+    a.MX1 = ba.base.MX1 + 3 * (size_t)c0;
+    a.Y = ba.base.Y + 3 * (size_t)c0;
+    a.S0 = ba.base.S0 + c0;
+    a.XB = ba.base.XB + 3 * (size_t)c0;
+    a.Wv = ba.base.Wv + 3 * (size_t)c0;
+    a.csum = ba.base.csum + 4 * (size_t)ba.chunk_ptr[p];
+    a.trace = nullptr;
+    a.out = ba.base.out + p;
+    BlockCtx ctx{a, smem8, sscal};
+    const int best = pg_body(a, ctx);
+    __syncthreads();
+    if (n == 0) continue;
+    const double* src = best == 3 ? a.XB : (best == 0 ? a.X0 : (best == 1 ? a.X1 : a.X2));
+    double* dst = ba.r + 3 * (size_t)c0;
+    for (int k = threadIdx.x; k < 3 * n; k += blockDim.x) dst[k] = ldcg(src + k);
+  }
+}
+
+cudaError_t launch_pg_batched(const PGBatchArgs& b, int grid, cudaStream_t s) {
+  k_pg_batched<<<grid, 256, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+int pg_batched_grid(int device) {
+  int sms = 0, per = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_batched, 256, 0) != cudaSuccess) return 0;
+  return per * sms;
 }
 
 cudaError_t launch_pg_persistent(const PGArgs& a, int grid, cudaStream_t s) {

@@ -106,11 +106,13 @@ def test_projected_gradient_bitwise(bg, oracle, c1, variant, static):
 
 @pytest.mark.parametrize("strategy", [3, 0, 2])
 @pytest.mark.parametrize("static", [False, True])
-def test_gauss_seidel_bitwise(bg, oracle, c1, strategy, static):
+@pytest.mark.parametrize("coloring", [False, True])
+def test_gauss_seidel_bitwise(bg, oracle, c1, strategy, static, coloring):
     d, rp, cl, vl = c1
     D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
     O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
     gs = bg.GaussSeidel()
+    gs.coloring().update(coloring)
     gs.setLocalStrategy(strategy)
     gs.setTol(1e-8)
     gs.setMaxIters(150)
@@ -121,7 +123,7 @@ def test_gauss_seidel_bitwise(bg, oracle, c1, strategy, static):
     res = D.solveWith(gs, r, staticProblem=static)
     tr = oracle.Trace()
     res_o, r_o, it_o = O.solve_gs(r0, coulomb=not static, strategy=strategy, tol=1e-8, max_iters=150,
-                                  coloring=True, trace=tr)
+                                  coloring=coloring, trace=tr)
     assert res == res_o
     assert D.last_iterations == it_o
     assert np.array_equal(r, r_o)
@@ -140,6 +142,7 @@ def test_gauss_seidel_options_bitwise(bg, oracle, c1):
     gs.doTryZeroAsWell(False)
     gs.setEvalEvery(10)
     gs.setMaxIters(60)
+    gs.coloring().update(True)
     r = np.ones(3 * d.n)
     res = D.solveWith(gs, r)
     res_o, r_o, it_o = O.solve_gs(np.ones(3 * d.n), coulomb=True, skip_tol=0.0, auto_reg=1e-3, inf_norm=True,
@@ -205,12 +208,14 @@ def test_missing_diagonal_negative_mu_and_zero_iterations(bg, oracle):
         res = D.solveWith(pg, r, staticProblem=False)
         res_o, r_o, it_o = O.solve_pg(np.ones(9), variant=variant, coulomb=True, max_iters=50)
         assert res == res_o and np.array_equal(r, r_o)
-    gs = bg.GaussSeidel()
-    gs.setMaxIters(50)
-    r = np.ones(9)
-    res = D.solveWith(gs, r)
-    res_o, r_o, _ = O.solve_gs(np.ones(9), max_iters=50, coloring=True)
-    assert res == res_o and np.array_equal(r, r_o)
+    for coloring in (False, True):
+        gs = bg.GaussSeidel()
+        gs.setMaxIters(50)
+        gs.coloring().update(coloring)
+        r = np.ones(9)
+        res = D.solveWith(gs, r)
+        res_o, r_o, _ = O.solve_gs(np.ones(9), max_iters=50, coloring=coloring)
+        assert res == res_o and np.array_equal(r, r_o)
     # maxIters = 0: the iterate is only projected and the residual is -1, as in the reference
     pg = bg.ProjectedGradient()
     pg.setMaxIters(0)
@@ -285,3 +290,58 @@ def test_full_size_apgd(bg, oracle, c2):
     res5 = D.solveWith(pg5, r5, staticProblem=False)
     res5_o, r5_o, _ = O.solve_pg(np.zeros(3 * d.n), variant=3, coulomb=True, max_iters=5)
     assert res5 == res5_o and np.array_equal(r5, r5_o)
+
+
+def test_full_size_gauss_seidel_first_sweeps(bg, oracle, c2):
+    d, D = c2
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    O = oracle.DualProblem(*P.assemble(), d.b, d.mu)
+    for coloring in (False, True):
+        gs = bg.GaussSeidel()
+        gs.coloring().update(coloring)
+        gs.setMaxIters(2)
+        gs.setEvalEvery(1)
+        r = np.zeros(3 * d.n)
+        res = D.solveWith(gs, r)
+        res_o, r_o, _ = O.solve_gs(np.zeros(3 * d.n), max_iters=2, eval_every=1, coloring=coloring)
+        assert res == res_o and np.array_equal(r, r_o)
+
+
+# ---- batched solves: one launch, each problem bit-identical to its own solve --------------------------
+@pytest.mark.parametrize("variant", [3, 4])
+def test_batched_matches_single_problem_solves(bg, oracle, variant):
+    from bogus_gpu import generator
+
+    d, cptr = generator.batch(nproblems=24, nmin=16, nmax=400, seed=7)
+    D = bg.DualFrictionProblem()
+    D.computeFrom(bg.PrimalFrictionProblem.from_generated(d))
+    D.setBatch(cptr)
+    pg = bg.ProjectedGradient()
+    pg.setDefaultVariant(variant)
+    pg.setTol(1e-8)
+    pg.setMaxIters(300)
+    r = np.zeros(3 * d.n)
+    res, its = D.solveBatchWith(pg, r, staticProblem=False)
+    rp, cl, vl = D.W_lower()
+    vl = vl.reshape(-1, 9)
+    for p in range(len(cptr) - 1):
+        c0, c1 = cptr[p], cptr[p + 1]
+        prp = rp[c0:c1 + 1] - rp[c0]
+        pcl = cl[rp[c0]:rp[c1]] - c0
+        pvl = vl[rp[c0]:rp[c1]].reshape(-1)
+        O = oracle.DualProblem(prp, pcl, pvl, d.b[c0:c1], d.mu[c0:c1])
+        res_o, r_o, it_o = O.solve_pg(np.zeros(3 * (c1 - c0)), variant=variant, coulomb=True, tol=1e-8,
+                                      max_iters=300)
+        assert res[p] == res_o and its[p] == it_o, p
+        assert np.array_equal(r[3 * c0:3 * c1], r_o), p
+
+
+def test_batch_rejects_coupled_partition(bg):
+    from bogus_gpu import generator
+
+    d = generator.make("c1")
+    D = bg.DualFrictionProblem()
+    D.computeFrom(bg.PrimalFrictionProblem.from_generated(d))
+    with pytest.raises(bg.BogusGpuError) as e:
+        D.setBatch([0, 250, d.n])  # random pairs couple the two halves
+    assert e.value.status == bg.BAD_INPUT
