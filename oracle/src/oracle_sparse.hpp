@@ -5,8 +5,9 @@
 //    triangle (col <= row) stored (Core/Block/Constants.hpp:60-65, SparseBlockMatrix.hpp:55-135);
 //  * symmetric products y = W x: for row i the stored blocks W_ij (j <= i) act directly and every stored
 //    W_ji (j > i) acts transposed (Core/Block/SparseMatrixVectorProduct.impl.hpp:89-175); run
-//    sequentially this visits row i's columns in increasing order, which is the canonical order used here
-//    (the "full" view holds both triangles, each row sorted by column);
+//    sequentially this visits row i's columns in increasing order; the "full" view holds both triangles,
+//    each row sorted by column, and spmv() sums each row in that column order, cut into the pieces
+//    described at spmv();
 //  * splitRowMultiply: the same row sum without the diagonal block (:298-320);
 //  * the error function and dot products reduce per-contact values with a fixed tree, canonicalSum().
 #pragma once
@@ -91,16 +92,37 @@ inline void blockAccumulate(const double* B, const double* x, double* acc) {
   }
 }
 
-// y = W x (init == nullptr) or y = init + W x, canonical row order; full view.
+// y = W x (init == nullptr) or y = init + W x; full view. Canonical chunk-segmented order (the order the GPU
+// kernels use to keep their lanes evenly loaded): the blocks [B0, B1) of each 32-row chunk are cut into 32
+// consecutive segments of S = ceil((B1 - B0) / 32) blocks; for row i, each segment meeting its blocks gives a
+// piece p (the blockAccumulate chain over the blocks of row i inside the segment, from 0), and
+// y_i = (((init_i + p_first) + p_next) + ...) in segment order. Columns are still visited in increasing order.
 inline void spmv(const BSR& W, const double* x, double* y, const double* init = nullptr) {
+  const int C = (W.n + 31) / 32;
 #pragma omp parallel for schedule(static)
-  for (int i = 0; i < W.n; ++i) {
-    double acc[3] = {0.0, 0.0, 0.0};
-    if (init) { acc[0] = init[3 * i]; acc[1] = init[3 * i + 1]; acc[2] = init[3 * i + 2]; }
-    for (int k = W.rowptr[i]; k < W.rowptr[i + 1]; ++k) blockAccumulate(W.block(k), &x[3 * (size_t)W.col[k]], acc);
-    y[3 * i] = acc[0];
-    y[3 * i + 1] = acc[1];
-    y[3 * i + 2] = acc[2];
+  for (int c = 0; c < C; ++c) {
+    const int r0 = 32 * c, r1 = std::min(W.n, r0 + 32);
+    const int B0 = W.rowptr[r0], B1 = W.rowptr[r1];
+    const int T = B1 - B0;
+    const int S = T > 0 ? (T + 31) / 32 : 1;
+    for (int i = r0; i < r1; ++i) {
+      double acc[3] = {0.0, 0.0, 0.0};
+      if (init) { acc[0] = init[3 * i]; acc[1] = init[3 * i + 1]; acc[2] = init[3 * i + 2]; }
+      int k = W.rowptr[i];
+      const int hi = W.rowptr[i + 1];
+      while (k < hi) {
+        const int l = (k - B0) / S;
+        const int e = std::min(hi, std::min(B0 + (l + 1) * S, B1));
+        double p[3] = {0.0, 0.0, 0.0};
+        for (; k < e; ++k) blockAccumulate(W.block(k), &x[3 * (size_t)W.col[k]], p);
+        acc[0] = acc[0] + p[0];
+        acc[1] = acc[1] + p[1];
+        acc[2] = acc[2] + p[2];
+      }
+      y[3 * i] = acc[0];
+      y[3 * i + 1] = acc[1];
+      y[3 * i + 2] = acc[2];
+    }
   }
 }
 

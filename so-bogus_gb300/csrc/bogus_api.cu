@@ -214,7 +214,7 @@ int ensure_pg_work(bogus_gpu_problem* h, unsigned max_iters) {
   BG_CUDA(h->scal.ensure(8));
   BG_CUDA(h->trace.ensure((size_t)max_iters + 1));
   BG_CUDA(h->pgout.ensure(1));
-  BG_CUDA(h->barrier.ensure(2));
+  BG_CUDA(h->barrier.ensure(4));
   BG_CUDA(h->status.ensure(1));
   return BOGUS_GPU_OK;
 }
@@ -246,6 +246,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.trace = h->trace.p;
   a.out = h->pgout.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.tickets = h->barrier.p + 2;
   a.desaxce = o->static_problem ? 0 : 1;
   a.variant = o->variant;
   a.use_inf = o->use_infinity_norm ? 1 : 0;
@@ -254,7 +255,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.pess = o->ls_pessimistic_factor;
   a.max_iters = o->max_iters;
   a.ls_iters = o->ls_iters;
-  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 2 * sizeof(unsigned), h->stream));
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), h->stream));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
   int grid = pg_max_grid(h->device);
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");

@@ -56,6 +56,7 @@ struct PGArgs {
   double* trace;  // residual per iteration
   PGOut* out;
   GridBarrier gb;
+  unsigned* tickets;  // 2 chunk counters (phase parity) for dynamic work distribution; zero at launch
   int desaxce, variant, use_inf;
   double tol, opt, pess;
   unsigned max_iters, ls_iters;

@@ -1,54 +1,48 @@
 // Stand-alone kernels: 3x3-block SpMV, error function, reductions and small vector helpers.
 //
-// SpMV order (canonical, shared by every kernel and by the CPU oracle): row i accumulates its blocks in
-// increasing column order; for each block, component r runs the chain
-//   acc_r = fma(B[r][0], x0, acc_r); acc_r = fma(B[r][1], x1, acc_r); acc_r = fma(B[r][2], x2, acc_r)
-// starting from 0 (y = W x) or from init_i (y = init + W x). Run sequentially, the reference's symmetric
-// product (Core/Block/SparseMatrixVectorProduct.impl.hpp:89-175) visits row i's columns in this order.
+// SpMV order: row i accumulates its blocks in increasing column order, as the reference's symmetric product
+// (Core/Block/SparseMatrixVectorProduct.impl.hpp:89-175) does when run sequentially, cut into the
+// per-lane pieces of the canonical chunk-segmented order (spmv_chunk.cuh), starting from 0 (y = W x) or from
+// init_i (y = init + W x).
 #include "internal.h"
 #include "soc_device.cuh"
+#include "spmv_chunk.cuh"
 
 namespace bogus_gpu {
 
-__device__ __forceinline__ void block_accumulate(const double* __restrict__ B, double x0, double x1, double x2,
-                                                 double* acc) {
-  double b[9];
-#pragma unroll
-  for (int e = 0; e < 9; ++e) b[e] = ldcs(B + e);
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    double a = acc[r];
-    a = fma(b[3 * r + 0], x0, a);
-    a = fma(b[3 * r + 1], x1, a);
-    a = fma(b[3 * r + 2], x2, a);
-    acc[r] = a;
-  }
-}
-
-__global__ void k_spmv(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
-                       const double* __restrict__ val, const double* __restrict__ x, const double* __restrict__ init,
-                       double* __restrict__ y) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+// One warp per 32-row chunk (canonical chunk-segmented order, spmv_chunk.cuh).
+__global__ void __launch_bounds__(256) k_spmv(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                              const double* __restrict__ val, const double* __restrict__ x,
+                                              const double* __restrict__ init, double* __restrict__ y) {
+  __shared__ ChunkScratch cs[8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * 8 + warp;
+  if (32 * c >= n) return;
+  const int i = 32 * c + lane;
   double acc[3] = {0.0, 0.0, 0.0};
-  if (init) {
+  if (init && i < n) {
     acc[0] = init[3 * i];
     acc[1] = init[3 * i + 1];
     acc[2] = init[3 * i + 2];
   }
-  const int k1 = __ldg(rowptr + i + 1);
-  for (int k = __ldg(rowptr + i); k < k1; ++k) {
-    const int j = ldcs(col + k);
-    block_accumulate(val + 9 * (size_t)k, __ldg(x + 3 * j), __ldg(x + 3 * j + 1), __ldg(x + 3 * j + 2), acc);
+  spmv_chunk<1>(rowptr, col, val, n, c, cs[warp],
+                [&](int j, double* v) {
+                  v[0] = __ldg(x + 3 * j);
+                  v[1] = __ldg(x + 3 * j + 1);
+                  v[2] = __ldg(x + 3 * j + 2);
+                },
+                acc);
+  if (i < n) {
+    y[3 * i] = acc[0];
+    y[3 * i + 1] = acc[1];
+    y[3 * i + 2] = acc[2];
   }
-  y[3 * i] = acc[0];
-  y[3 * i + 1] = acc[1];
-  y[3 * i + 2] = acc[2];
 }
 
 cudaError_t launch_spmv(const DevBSR& W, const double* x, const double* init, double* y, cudaStream_t s) {
   if (W.n == 0) return cudaSuccess;
-  k_spmv<<<(W.n + 255) / 256, 256, 0, s>>>(W.n, W.rowptr, W.col, W.val, x, init, y);
+  const int chunks = (W.n + 31) / 32;
+  k_spmv<<<(chunks + 7) / 8, 256, 0, s>>>(W.n, W.rowptr, W.col, W.val, x, init, y);
   return cudaGetLastError();
 }
 

@@ -18,6 +18,7 @@
 // Without momentum x = xs and Mx = Mxs are buffer swaps and A runs as its own pass.
 #include "internal.h"
 #include "soc_device.cuh"
+#include "spmv_chunk.cuh"
 
 namespace bogus_gpu {
 
@@ -32,53 +33,6 @@ __device__ __forceinline__ void store3(double* p, int i, const double* v) {
   p[3 * i] = v[0];
   p[3 * i + 1] = v[1];
   p[3 * i + 2] = v[2];
-}
-
-__device__ __forceinline__ void spmv_row(const PGArgs& a, int i, const double* __restrict__ x, double* acc) {
-  const int k1 = __ldg(a.rowptr + i + 1);
-  for (int k = __ldg(a.rowptr + i); k < k1; ++k) {
-    const int j = ldcs(a.col + k);
-    const double x0 = ldcg(x + 3 * j), x1 = ldcg(x + 3 * j + 1), x2 = ldcg(x + 3 * j + 2);
-    const double* B = a.val + 9 * (size_t)k;
-    double b[9];
-#pragma unroll
-    for (int e = 0; e < 9; ++e) b[e] = ldcs(B + e);
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      double s = acc[r];
-      s = fma(b[3 * r + 0], x0, s);
-      s = fma(b[3 * r + 1], x1, s);
-      s = fma(b[3 * r + 2], x2, s);
-      acc[r] = s;
-    }
-  }
-}
-
-// guess_alpha's product: acc = W x and accd = W (x - 1) in one pass over W
-__device__ __forceinline__ void spmv_row_guess(const PGArgs& a, int i, const double* __restrict__ x, double* acc,
-                                               double* accd) {
-  const int k1 = __ldg(a.rowptr + i + 1);
-  for (int k = __ldg(a.rowptr + i); k < k1; ++k) {
-    const int j = ldcs(a.col + k);
-    const double x0 = ldcg(x + 3 * j), x1 = ldcg(x + 3 * j + 1), x2 = ldcg(x + 3 * j + 2);
-    const double d0 = x0 - 1.0, d1 = x1 - 1.0, d2 = x2 - 1.0;
-    const double* B = a.val + 9 * (size_t)k;
-    double b[9];
-#pragma unroll
-    for (int e = 0; e < 9; ++e) b[e] = ldcs(B + e);
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      double s = acc[r], t = accd[r];
-      s = fma(b[3 * r + 0], x0, s);
-      s = fma(b[3 * r + 1], x1, s);
-      s = fma(b[3 * r + 2], x2, s);
-      t = fma(b[3 * r + 0], d0, t);
-      t = fma(b[3 * r + 1], d1, t);
-      t = fma(b[3 * r + 2], d2, t);
-      acc[r] = s;
-      accd[r] = t;
-    }
-  }
 }
 
 struct Bufs {
@@ -98,9 +52,12 @@ __device__ __forceinline__ int third(int p, int q) {
 template <class Ctx>
 __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
   const Bufs B{a};
+  ChunkScratch& sh = ctx.cs[threadIdx.x >> 5];
+  // y = W x of chunk c for every lane (row 32c + lane), x gathered from a buffer written earlier in the kernel
+  auto product = [&](int c, const double* __restrict__ xsrc, double* acc) {
+    spmv_chunk<1>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, double* x) { load3cg(xsrc, j, x); }, acc);
+  };
   const int lane = threadIdx.x & 31;
-  const int gw = ctx.first_warp();
-  const int nw = ctx.num_warps();
   const bool desaxce = a.desaxce != 0;
   const bool spg = a.variant == 4;
   const bool apgd = a.variant == 3;
@@ -133,7 +90,7 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
 
   // projectOnConstraints(x) (:90)
   ph[0]++;
-  for (int c = gw; c < C; c += nw) {
+  for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
     const int i = 32 * c + lane;
     if (i < a.n) {
       double x[3];
@@ -146,12 +103,12 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
 
   // Mx = W x (:93) and guess_alpha (:21-28): |W (x - 1)|^2, |x - 1|^2
   ph[1]++;
-  for (int c = gw; c < C; c += nw) {
+  for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
     const int i = 32 * c + lane;
     double v0 = 0.0, v1 = 0.0;
+    double acc[3] = {0.0, 0.0, 0.0}, accd[3] = {0.0, 0.0, 0.0};
+    spmv_chunk<2>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, double* x) { load3cg(a.X0, j, x); }, acc, accd);
     if (i < a.n) {
-      double acc[3] = {0.0, 0.0, 0.0}, accd[3] = {0.0, 0.0, 0.0};
-      spmv_row_guess(a, i, a.X0, acc, accd);
       store3(a.MX0, i, acc);
       v0 = sq3(accd);
       double x[3];
@@ -206,7 +163,7 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
 
   auto runA = [&](double alpha_t) -> bool {  // A as its own pass (Mx already in MX(imx))
     ph[2]++;
-    for (int c = gw; c < C; c += nw) {
+    for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
       const int i = 32 * c + lane;
       double r = 0.0, q = 0.0;
       if (i < a.n) {
@@ -244,12 +201,12 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
       for (;;) {
         // C: Mxs = W xs and the line-search terms
         ph[3]++;
-        for (int c = gw; c < C; c += nw) {
+        for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+          double acc[3] = {0.0, 0.0, 0.0};
+          product(c, B.X(ixs), acc);
           if (i < a.n) {
-            double acc[3] = {0.0, 0.0, 0.0};
-            spmv_row(a, i, B.X(ixs), acc);
             store3(B.MX(1 - imx), i, acc);
             double x[3], xs[3], pv[3], y[3];
             load3cg(B.X(ix), i, x);
@@ -282,7 +239,7 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
         if (ls >= a.ls_iters) break;
         // B: retry with a smaller step
         ph[4]++;
-        for (int c = gw; c < C; c += nw) {
+        for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           if (i < a.n) {
             double x[3], y[3];
@@ -301,7 +258,7 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
         const double beta = nesterov_inertia(theta, 0.0);
         // D: x = xs + beta (xs - prev), written over the old x
         ph[5]++;
-        for (int c = gw; c < C; c += nw) {
+        for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           if (i < a.n) {
             double xs[3], pv[3];
@@ -319,12 +276,12 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
         alpha_t = alpha * a.opt;
         // E + A: Mx = W x, then A of the next iteration on the same rows
         ph[6]++;
-        for (int c = gw; c < C; c += nw) {
+        for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           double r = 0.0, q = 0.0;
+          double acc[3] = {0.0, 0.0, 0.0};
+          product(c, B.X(ix), acc);
           if (i < a.n) {
-            double acc[3] = {0.0, 0.0, 0.0};
-            spmv_row(a, i, B.X(ix), acc);
             store3(B.MX(imx), i, acc);
             phaseA(i, acc, alpha_t, r, q);
           }
@@ -364,7 +321,7 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
     if (!mom) theta = 1.;
     // D: w and the new x (over the old x); keep the best iterate first
     ph[7]++;
-    for (int c = gw; c < C; c += nw) {
+    for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
       const int i = 32 * c + lane;
       if (i < a.n) {
         double x[3], xs[3], pv[3], w[3], xn[3];
@@ -389,12 +346,13 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
     if (!sync()) return -1;
     // E: Mx_new = W x; z = -Mx_old + Mx_new; w.z, |z|^2
     ph[8]++;
-    for (int c = gw; c < C; c += nw) {
+    for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
       const int i = 32 * c + lane;
       double v0 = 0.0, v1 = 0.0;
+      double acc[3] = {0.0, 0.0, 0.0};
+      product(c, B.X(ix), acc);
       if (i < a.n) {
-        double acc[3] = {0.0, 0.0, 0.0}, mo[3], w[3];
-        spmv_row(a, i, B.X(ix), acc);
+        double mo[3], w[3];
         store3(B.MX(1 - imx), i, acc);
         load3cg(B.MX(imx), i, mo);
         load3cg(a.Wv, i, w);
@@ -419,27 +377,52 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
 
 
 // Single problem: the whole GPU, phases separated by the bounded grid barrier; the last CTA to arrive
-// publishes the reduced scalars in global memory.
+// publishes the reduced scalars in global memory. Warps take 32-contact chunks from a ticket counter (one
+// per phase parity, cleared by the last CTA of the barrier that ends the phase), so SMs that finish early
+// take more chunks; every cross-phase dependency goes through a barrier, and the reduction order does not
+// depend on which warp handles a chunk.
 struct GridCtx {
   const PGArgs& a;
   double* smem8;
-  __device__ int first_warp() const { return blockIdx.x * 8 + (threadIdx.x >> 5); }
-  __device__ int num_warps() const { return gridDim.x * 8; }
+  ChunkScratch* cs;
+  unsigned phase = 0;  // barriers passed (identical in every CTA)
+  __device__ int ticket() {
+    int c = 0;
+    if ((threadIdx.x & 31) == 0) c = (int)atomicAdd(a.tickets + (phase & 1u), 1u);
+    return __shfl_sync(0xffffffffu, c, 0);
+  }
+  __device__ int first_chunk() { return ticket(); }
+  __device__ int next_chunk(int) { return ticket(); }
   __device__ bool writer() const { return blockIdx.x == 0 && threadIdx.x == 0; }
+  __device__ void clear_tickets() {
+    if (threadIdx.x == 0) a.tickets[phase & 1u] = 0u;
+  }
   __device__ void publish(int K, unsigned maxmask) {
     for (int q = 0; q < K; ++q) {
       const double v = block8_combine(a.csum + q * a.nchunks, a.nchunks, (maxmask >> q) & 1u, smem8);
       if (threadIdx.x == 0) a.scal[q] = v;
     }
   }
-  __device__ bool sync() { return grid_barrier(a.gb, [] {}); }
-  __device__ bool sync_reduce(int K, unsigned maxmask) { return grid_barrier(a.gb, [&] { publish(K, maxmask); }); }
+  __device__ bool sync() {
+    const bool ok = grid_barrier(a.gb, [&] { clear_tickets(); });
+    ++phase;
+    return ok;
+  }
+  __device__ bool sync_reduce(int K, unsigned maxmask) {
+    const bool ok = grid_barrier(a.gb, [&] {
+      publish(K, maxmask);
+      clear_tickets();
+    });
+    ++phase;
+    return ok;
+  }
   __device__ double scal(int q) const { return ldcg(a.scal + q); }
 };
 
 __global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
   __shared__ double smem8[8];
-  GridCtx ctx{a, smem8};
+  __shared__ ChunkScratch cs[8];
+  GridCtx ctx{a, smem8, cs};
   pg_body(a, ctx);
 }
 
@@ -449,8 +432,9 @@ struct BlockCtx {
   const PGArgs& a;
   double* smem8;
   double* sscal;
-  __device__ int first_warp() const { return threadIdx.x >> 5; }
-  __device__ int num_warps() const { return 8; }
+  ChunkScratch* cs;
+  __device__ int first_chunk() const { return threadIdx.x >> 5; }
+  __device__ int next_chunk(int c) const { return c + 8; }
   __device__ bool writer() const { return threadIdx.x == 0; }
   __device__ bool sync() {
     __syncthreads();
@@ -472,6 +456,7 @@ struct BlockCtx {
 // problem with the same arithmetic as the single-problem kernel, then writes the best iterate to r.
 __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgs ba) {
   __shared__ double smem8[8], sscal[8];
+  __shared__ ChunkScratch cs[8];
   __shared__ int s_job;
   for (;;) {
     __syncthreads();
@@ -501,7 +486,7 @@ __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgs ba) {
     a.csum = ba.base.csum + 4 * (size_t)ba.chunk_ptr[p];
     a.trace = nullptr;
     a.out = ba.base.out + p;
-    BlockCtx ctx{a, smem8, sscal};
+    BlockCtx ctx{a, smem8, sscal, cs};
     const int best = pg_body(a, ctx);
     __syncthreads();
     if (n == 0) continue;

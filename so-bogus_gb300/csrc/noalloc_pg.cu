@@ -12,7 +12,7 @@
 // reuse it. Because that first call does this set-up, it should come before any stream capture.
 //
 // Every call on a device shares the same array. Its contents persist from one call to the next, so each
-// call clears the parts that must start at zero (the grid-barrier words and the error status) before
+// call clears the parts that must start at zero (the grid-barrier words, the chunk counters and the error status) before
 // launching; two calls whose work overlaps on the GPU (different streams, or different host threads) race
 // on the array and must not be issued.
 #include <cuda_runtime.h>
@@ -124,7 +124,7 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   }
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   const size_t n3 = 3 * (size_t)n;
-  unsigned* words = reinterpret_cast<unsigned*>(s + kOffWords);  // [0] count, [1] gen, [2] status
+  unsigned* words = reinterpret_cast<unsigned*>(s + kOffWords);  // [0] count, [1] gen, [2] status, [3..4] tickets
   // diagonal positions and scalings into the scratch
   DevBSR W;
   W.n = n;
@@ -135,7 +135,7 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   W.diag = reinterpret_cast<int*>(s + kOffDiag);
   NA_CUDA(launch_diag_and_scaling(W, s + kOffScaling, cs));
   NA_CUDA(cudaMemcpyAsync(s + kOffX, d_r, sizeof(double) * n3, cudaMemcpyDeviceToDevice, cs));
-  NA_CUDA(cudaMemsetAsync(words, 0, 3 * sizeof(unsigned), cs));
+  NA_CUDA(cudaMemsetAsync(words, 0, 5 * sizeof(unsigned), cs));
   PGArgs a{};
   a.n = n;
   a.nchunks = (n + 31) / 32;
@@ -159,6 +159,7 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   a.trace = s + kOffTrace;
   a.out = reinterpret_cast<PGOut*>(s + kOffOut);
   a.gb = GridBarrier{words, words + 1, reinterpret_cast<int*>(words + 2)};
+  a.tickets = words + 3;
   a.desaxce = o->static_problem ? 0 : 1;
   a.variant = o->variant;
   a.use_inf = o->use_infinity_norm ? 1 : 0;
