@@ -286,7 +286,7 @@ def run_ours(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
-def run_profile(iters: int) -> None:
+def run_profile(iters: int, mixed: bool = False) -> None:
     """One APGD solve of the benchmark problem capped at `iters` iterations (the solver kernel under ncu)."""
     import bogus_gpu
 
@@ -296,6 +296,8 @@ def run_profile(iters: int) -> None:
     pg = bogus_gpu.ProjectedGradient()
     pg.setTol(TOL)
     pg.setMaxIters(iters)
+    if mixed:
+        pg.setMixedPrecision(True, 1)
     r = np.zeros(3 * d.n)
     res = D.solveWith(pg, r)
     st = D.solve_stats()
@@ -402,6 +404,56 @@ def run_gs(args) -> None:
     print(json.dumps(out), flush=True)
 
 
+def run_mixed(args) -> None:
+    """FP32-refined APGD on the 200 000-contact problem: 500 FP32 iterations then up to 50 FP64 ones, against
+    the FP64 solve run to the same FP64 residual (time to the same residual, both on the GPU)."""
+    import bogus_gpu
+
+    d = make_problem()
+    D = bogus_gpu.DualFrictionProblem(0)
+    D.computeFrom(bogus_gpu.PrimalFrictionProblem.from_generated(d))
+
+    def timed(pg):
+        best = None
+        for k in range(args.warmup + args.steps):
+            r = np.zeros(3 * d.n)
+            res = D.solveWith(pg, r, staticProblem=True)
+            st = D.solve_stats()
+            if k >= args.warmup and (best is None or st["device_ms"] < best[1]["device_ms"]):
+                best = (res, st)
+        return best
+
+    pgm = bogus_gpu.ProjectedGradient()
+    pgm.setTol(TOL)
+    pgm.setMaxIters(MAX_ITERS)
+    pgm.setMixedPrecision(True, 50)
+    res_m, st_m = timed(pgm)
+    pg64 = bogus_gpu.ProjectedGradient()
+    pg64.setTol(TOL)
+    pg64.setMaxIters(MAX_ITERS)
+    res_p, st_p = timed(pg64)
+    # the FP64 solve to the residual the mixed solve reached
+    pgt = bogus_gpu.ProjectedGradient()
+    pgt.setTol(res_m)
+    pgt.setMaxIters(4 * MAX_ITERS)
+    res_t, st_t = timed(pgt)
+    m32 = st_m["fp32_device_ms"]
+    print(json.dumps({
+        "workload": "fp32_refined_apgd_200k_contacts", "law": "SOC", "contacts": d.n,
+        "mixed": {"device_ms": st_m["device_ms"], "fp32_ms": m32, "fp32_iterations":
+                  st_m["iterations"] - st_m["refine_iterations"], "fp64_refine_iterations": st_m["refine_iterations"],
+                  "fp64_residual": res_m,
+                  "fp32_ms_per_iteration": m32 / max(1, st_m["iterations"] - st_m["refine_iterations"]),
+                  "algorithmic_gbs": st_m["algorithmic_bytes"] / (st_m["device_ms"] * 1e-3) / 1e9},
+        "fp64_same_iterations": {"device_ms": st_p["device_ms"], "iterations": st_p["iterations"],
+                                 "residual": res_p, "ms_per_iteration": st_p["device_ms"] / max(1, st_p["iterations"])},
+        "fp64_to_mixed_residual": {"device_ms": st_t["device_ms"], "iterations": st_t["iterations"],
+                                   "residual": res_t, "reached": bool(res_t <= res_m)},
+        "speedup_time_to_residual": st_t["device_ms"] / st_m["device_ms"],
+        "timing": f"best of {args.steps} after {args.warmup} warm-up solves, CUDA events on the library stream"}),
+        flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -411,9 +463,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", type=int, default=0,
                     help="run one solve capped at this many iterations and exit (for ncu captures)")
-    ap.add_argument("--workload", default="apgd", choices=["apgd", "batch", "gs"],
-                    help="apgd: the benchmark line; batch / gs: secondary measurements")
+    ap.add_argument("--workload", default="apgd", choices=["apgd", "batch", "gs", "mixed"],
+                    help="apgd: the benchmark line; batch / gs / mixed: secondary measurements")
+    ap.add_argument("--profile-mixed", action="store_true",
+                    help="with --profile: the FP32-refined solve (FP32 iterations, then 1 FP64 iteration)")
     args = ap.parse_args()
+    if args.workload == "mixed":
+        run_mixed(args)
+        return
     if args.workload == "batch":
         run_batch(args)
         return
@@ -421,7 +478,7 @@ def main():
         run_gs(args)
         return
     if args.profile:
-        run_profile(args.profile)
+        run_profile(args.profile, args.profile_mixed)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -68,6 +68,11 @@ typedef struct bogus_gpu_pg_options {
   int variant;                    /* bogus_gpu_pg_variant, APGD */
   int use_infinity_norm;          /* 0 */
   int static_problem;             /* 1: SOC law; 0: Coulomb (DualFrictionProblem::solveWith(pg) default 1) */
+  int mixed_precision;            /* 0: FP64 throughout (the drop-in). 1: FP32-refined: W, the iterates and
+                                     the per-contact law in FP32 (reductions and step decisions in FP64) for up
+                                     to max_iters iterations, then up to refine_max_iters FP64 iterations from
+                                     the FP32 result (the returned residual is the FP64 error function) */
+  unsigned refine_max_iters;      /* 50 */
 } bogus_gpu_pg_options;
 
 /* GaussSeidel setters and defaults (Core/BlockSolvers/GaussSeidelBase.hpp:39-91) plus the coloring switch
@@ -189,6 +194,8 @@ typedef struct bogus_gpu_solve_stats {
   unsigned w_passes;         /* full passes over W (products) */
   double algorithmic_bytes;  /* bytes the passes had to move: W (values + indices) + vector streams */
   double fp64_fma;           /* FP64 fused multiply-adds of the W passes */
+  unsigned refine_iterations; /* FP64 iterations after the FP32 ones (mixed precision), else 0 */
+  double fp32_device_ms;      /* device time of the FP32 part (mixed precision), else 0 */
 } bogus_gpu_solve_stats;
 int bogus_gpu_get_solve_stats(const bogus_gpu_problem* h, bogus_gpu_solve_stats* out);
 

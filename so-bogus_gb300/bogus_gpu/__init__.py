@@ -38,7 +38,7 @@ class PgOptions(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint), ("ls_iters", C.c_uint),
                 ("ls_optimistic_factor", C.c_double), ("ls_pessimistic_factor", C.c_double),
                 ("ls_armijo_coefficient", C.c_double), ("variant", C.c_int), ("use_infinity_norm", C.c_int),
-                ("static_problem", C.c_int)]
+                ("static_problem", C.c_int), ("mixed_precision", C.c_int), ("refine_max_iters", C.c_uint)]
 
 
 class GsOptions(C.Structure):
@@ -50,7 +50,8 @@ class GsOptions(C.Structure):
 
 class SolveStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("kernel_launches", C.c_uint), ("iterations", C.c_uint),
-                ("w_passes", C.c_uint), ("algorithmic_bytes", C.c_double), ("fp64_fma", C.c_double)]
+                ("w_passes", C.c_uint), ("algorithmic_bytes", C.c_double), ("fp64_fma", C.c_double),
+                ("refine_iterations", C.c_uint), ("fp32_device_ms", C.c_double)]
 
 
 CALLBACK = C.CFUNCTYPE(None, C.c_uint, C.c_double, C.c_void_p)
@@ -169,6 +170,12 @@ class ProjectedGradient(_SolverBase):
         self._ls = 8
         self._opt, self._pess, self._armijo = 1.25, 0.5, 0.5
         self._variant = APGD
+        self._mixed, self._refine = False, 50
+
+    def setMixedPrecision(self, on: bool = True, refine_max_iters: int = 50) -> None:
+        """FP32-refined solve: FP32 W / iterates / per-contact law (FP64 reductions and decisions), then up to
+        refine_max_iters FP64 iterations from the FP32 result. No counterpart in the reference."""
+        self._mixed, self._refine = bool(on), int(refine_max_iters)
 
     def setLineSearchIterations(self, n: int) -> None: self._ls = int(n)
     def setLineSearchOptimisticFactor(self, f: float) -> None: self._opt = float(f)
@@ -183,6 +190,7 @@ class ProjectedGradient(_SolverBase):
         o.tol, o.max_iters, o.ls_iters = self._tol, self._max_iters, self._ls
         o.ls_optimistic_factor, o.ls_pessimistic_factor, o.ls_armijo_coefficient = self._opt, self._pess, self._armijo
         o.variant, o.use_infinity_norm, o.static_problem = self._variant, int(self._inf), int(static_problem)
+        o.mixed_precision, o.refine_max_iters = int(self._mixed), self._refine
         return o
 
 

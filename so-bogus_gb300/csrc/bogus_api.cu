@@ -124,6 +124,9 @@ struct bogus_gpu_problem {
   std::vector<double> host_b, host_mu;
   // projected-gradient work
   DevBuf<double> X, MX, Y, S0, XB, Wv, csum, scal, trace;
+  // FP32 copies of W, b, mu, scalings and FP32 work (mixed precision), valid while W is unchanged
+  bool fp32_valid = false;
+  DevBuf<float> val32, b32, mu32, sc32, X32, MX32, Y32, S032, XB32, Wv32;
   DevBuf<PGOut> pgout;
   DevBuf<unsigned> barrier;
   DevBuf<int> status;
@@ -191,6 +194,7 @@ int upload_full(bogus_gpu_problem* h, const HostBSR& f, const double* b, const d
   h->has_dual = true;
   h->gs.valid = false;
   h->nproblems = 0;
+  h->fp32_valid = false;
   return BOGUS_GPU_OK;
 }
 
@@ -217,6 +221,28 @@ int ensure_pg_work(bogus_gpu_problem* h, unsigned max_iters) {
   BG_CUDA(h->barrier.ensure(4));
   BG_CUDA(h->status.ensure(1));
   return BOGUS_GPU_OK;
+}
+
+// Algorithmic bytes and W passes of one persistent solve from its phase counters. A W pass reads nnzb blocks
+// (9 values + a column index) and the n + 1 row pointers; the per-contact vector bytes of each pass kind
+// follow PGOut::phases (3-vectors 3 values, scalars 1 value). elem = bytes per value (8 FP64, 4 FP32).
+struct PGTraffic {
+  double bytes = 0, fma = 0;
+  unsigned passes = 0;
+};
+PGTraffic pg_traffic(const PGOut& out, int n, long long nnzb, bool spg, double elem) {
+  const double wpass = (double)nnzb * (9.0 * elem + 4.0) + 4.0 * (n + 1);
+  const double per_contact[9] = {7, 6, spg ? 21.0 : 18.0, 19, 10, 9, 18, 15, 12};  // values per contact
+  const bool has_w[9] = {false, true, false, true, false, false, true, false, true};
+  PGTraffic t;
+  for (int k = 0; k < 9; ++k) {
+    t.bytes += out.phases[k] * (per_contact[k] * elem * n + (has_w[k] ? wpass : 0.0));
+    if (has_w[k]) {
+      t.passes += out.phases[k];
+      t.fma += out.phases[k] * 9.0 * (double)nnzb * (k == 1 ? 2.0 : 1.0);
+    }
+  }
+  return t;
 }
 
 // Runs the persistent solver with r already in X[0]; returns the buffer holding the result.
@@ -273,25 +299,13 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   h->last_launches = 1;
   if (st != 0) return fail(st, "device-side wait timed out in the projected-gradient kernel");
   {
-    // algorithmic bytes per pass kind (FP64): W pass = nnzb (72 + 4) + 4 (n + 1); per-contact vector bytes
-    // of each pass as listed in PGOut::phases (3-vectors 24 B, scalars 8 B)
-    const double wpass = (double)h->W.nnzb * 76.0 + 4.0 * (n + 1);
-    const bool spg = o->variant == BOGUS_GPU_PG_SPG;
-    const double per_contact[9] = {56, 48, spg ? 168.0 : 144.0, 152, 80, 72, 144, 120, 96};
-    const bool has_w[9] = {false, true, false, true, false, false, true, false, true};
-    double bytes = 0, fma = 0;
-    unsigned passes = 0;
-    for (int k = 0; k < 9; ++k) {
-      bytes += out.phases[k] * (per_contact[k] * n + (has_w[k] ? wpass : 0.0));
-      if (has_w[k]) {
-        passes += out.phases[k];
-        fma += out.phases[k] * 9.0 * h->W.nnzb * (k == 1 ? 2.0 : 1.0);
-      }
-    }
+    const PGTraffic t = pg_traffic(out, n, h->W.nnzb, o->variant == BOGUS_GPU_PG_SPG, 8.0);
     h->last_stats.iterations = out.iters;
-    h->last_stats.w_passes = passes;
-    h->last_stats.algorithmic_bytes = bytes;
-    h->last_stats.fp64_fma = fma;
+    h->last_stats.refine_iterations = 0;
+    h->last_stats.fp32_device_ms = 0.0;
+    h->last_stats.w_passes = t.passes;
+    h->last_stats.algorithmic_bytes = t.bytes;
+    h->last_stats.fp64_fma = t.fma;
   }
   if (residual) *residual = out.min_res;
   if (iters) *iters = out.iters;
@@ -307,6 +321,113 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   return out.converged ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
 }
 
+// FP32 copies of the problem and FP32 work buffers for the mixed-precision solve.
+int ensure_fp32(bogus_gpu_problem* h) {
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  cudaStream_t s = h->stream;
+  BG_CUDA(h->X32.ensure(3 * n3));
+  BG_CUDA(h->MX32.ensure(2 * n3));
+  BG_CUDA(h->Y32.ensure(n3));
+  BG_CUDA(h->S032.ensure(n));
+  BG_CUDA(h->XB32.ensure(n3));
+  BG_CUDA(h->Wv32.ensure(n3));
+  if (h->fp32_valid) return BOGUS_GPU_OK;
+  BG_CUDA(h->val32.ensure(9 * (size_t)h->W.nnzb));
+  BG_CUDA(h->b32.ensure(n3));
+  BG_CUDA(h->mu32.ensure(n));
+  BG_CUDA(h->sc32.ensure(n));
+  BG_CUDA(launch_convert(9 * (size_t)h->W.nnzb, h->W.val, h->val32.p, s));
+  BG_CUDA(launch_convert(n3, h->b.p, h->b32.p, s));
+  BG_CUDA(launch_convert((size_t)n, h->mu.p, h->mu32.p, s));
+  BG_CUDA(launch_convert((size_t)n, h->scaling.p, h->sc32.p, s));
+  h->fp32_valid = true;
+  return BOGUS_GPU_OK;
+}
+
+template <class T>
+void fill_args(PGArgsT<T>& a, const bogus_gpu_pg_options* o) {
+  a.desaxce = o->static_problem ? 0 : 1;
+  a.variant = o->variant;
+  a.use_inf = o->use_infinity_norm ? 1 : 0;
+  a.tol = o->tol;
+  a.opt = o->ls_optimistic_factor;
+  a.pess = o->ls_pessimistic_factor;
+  a.max_iters = o->max_iters;
+  a.ls_iters = o->ls_iters;
+}
+
+// Mixed precision: FP32 solve from X[0] (double), its best iterate back into X[0], then the FP64 solve from
+// there for at most refine_max_iters iterations.
+int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual, unsigned* iters,
+                 const double** best) {
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  if (int e = ensure_fp32(h)) return e;
+  if (int e = ensure_pg_work(h, o->max_iters > o->refine_max_iters ? o->max_iters : o->refine_max_iters)) return e;
+  cudaStream_t s = h->stream;
+  PGArgs32 a{};
+  a.n = n;
+  a.nchunks = (n + 31) / 32;
+  a.rowptr = h->W.rowptr;
+  a.col = h->W.col;
+  a.val = h->val32.p;
+  a.b = h->b32.p;
+  a.mu = h->mu32.p;
+  a.scaling = h->sc32.p;
+  a.X0 = h->X32.p;
+  a.X1 = h->X32.p + n3;
+  a.X2 = h->X32.p + 2 * n3;
+  a.MX0 = h->MX32.p;
+  a.MX1 = h->MX32.p + n3;
+  a.Y = h->Y32.p;
+  a.S0 = h->S032.p;
+  a.XB = h->XB32.p;
+  a.Wv = h->Wv32.p;
+  a.csum = h->csum.p;
+  a.scal = h->scal.p;
+  a.trace = nullptr;
+  a.out = h->pgout.p;
+  a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.tickets = h->barrier.p + 2;
+  fill_args(a, o);
+  BG_CUDA(launch_convert(n3, h->X.p, h->X32.p, s));
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), s));
+  BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
+  int grid = pg_max_grid(h->device, true);
+  if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
+  const int want = (a.nchunks + 7) / 8;
+  if (want < grid) grid = want < 1 ? 1 : want;
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  BG_CUDA(launch_pg_persistent(a, grid, s));
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  PGOut out{};
+  int st = 0;
+  BG_CUDA(cudaMemcpyAsync(&out, h->pgout.p, sizeof(PGOut), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaMemcpyAsync(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  float ms32 = 0.f;
+  BG_CUDA(cudaEventElapsedTime(&ms32, h->ev0, h->ev1));
+  if (st != 0) return fail(st, "device-side wait timed out in the FP32 projected-gradient kernel");
+  const float* b32 = out.best_buf == 3 ? h->XB32.p : h->X32.p + (size_t)out.best_buf * n3;
+  BG_CUDA(launch_convert(n3, b32, h->X.p, s));
+  bogus_gpu_pg_options o64 = *o;
+  o64.max_iters = o->refine_max_iters;
+  const unsigned it32 = out.iters;
+  const int rst = run_pg(h, &o64, residual, iters, best);
+  if (rst != BOGUS_GPU_OK && rst != BOGUS_GPU_NOT_CONVERGED) return rst;
+  const PGTraffic t32 = pg_traffic(out, n, h->W.nnzb, o->variant == BOGUS_GPU_PG_SPG, 4.0);
+  h->last_stats.refine_iterations = h->last_stats.iterations;
+  h->last_stats.iterations = it32 + h->last_stats.iterations;
+  h->last_stats.w_passes += t32.passes;
+  h->last_stats.algorithmic_bytes += t32.bytes;
+  h->last_stats.fp32_device_ms = ms32;
+  h->last_ms += ms32;
+  h->last_launches += 1;
+  if (iters) *iters = it32 + *iters;
+  return rst;
+}
+
 int check_pg_options(const bogus_gpu_pg_options* o) {
   if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
   if (o->variant != BOGUS_GPU_PG_APGD && o->variant != BOGUS_GPU_PG_DESCENT && o->variant != BOGUS_GPU_PG_SPG)
@@ -315,6 +436,8 @@ int check_pg_options(const bogus_gpu_pg_options* o) {
     return fail(BOGUS_GPU_BAD_INPUT, "ls_iters must be >= 1 (the reference reuses an undefined step otherwise)");
   if (!(o->tol >= 0) || !(o->ls_optimistic_factor > 0) || !(o->ls_pessimistic_factor > 0))
     return fail(BOGUS_GPU_BAD_INPUT, "invalid projected-gradient factors");
+  if (o->mixed_precision && o->refine_max_iters == 0)
+    return fail(BOGUS_GPU_BAD_INPUT, "mixed precision needs refine_max_iters >= 1 (the FP64 residual)");
   return BOGUS_GPU_OK;
 }
 
@@ -481,6 +604,8 @@ void bogus_gpu_pg_options_default(bogus_gpu_pg_options* o) {
   o->variant = BOGUS_GPU_PG_APGD;
   o->use_infinity_norm = 0;
   o->static_problem = 1;
+  o->mixed_precision = 0;
+  o->refine_max_iters = 50;
 }
 
 void bogus_gpu_gs_options_default(bogus_gpu_gs_options* o) {
@@ -544,6 +669,8 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   cudaStreamSynchronize(h->stream);
   for (auto* b : {&h->val, &h->b, &h->mu, &h->scaling, &h->X, &h->MX, &h->Y, &h->S0, &h->XB, &h->Wv, &h->csum,
                   &h->scal, &h->trace, &h->vx, &h->vy, &h->chunk, &h->scalar, &h->minv, &h->H, &h->T, &h->mf})
+    b->release();
+  for (auto* b : {&h->val32, &h->b32, &h->mu32, &h->sc32, &h->X32, &h->MX32, &h->Y32, &h->S032, &h->XB32, &h->Wv32})
     b->release();
   h->rowptr.release();
   h->col.release();
@@ -630,6 +757,7 @@ int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* 
   h->host_lower_valid = false;
   h->gs.valid = false;
   h->nproblems = 0;
+  h->fp32_valid = false;
   return BOGUS_GPU_OK;
 }
 
@@ -704,7 +832,7 @@ int bogus_gpu_solve_pg_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* 
   if (int e = ensure_pg_work(h, o->max_iters)) return e;
   BG_CUDA(cudaMemcpyAsync(h->X.p, d_r, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
   const double* best = nullptr;
-  const int st = run_pg(h, o, residual, iters, &best);
+  const int st = o->mixed_precision ? run_pg_mixed(h, o, residual, iters, &best) : run_pg(h, o, residual, iters, &best);
   if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
   BG_CUDA(cudaMemcpyAsync(d_r, best, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
   BG_CUDA(cudaStreamSynchronize(h->stream));
@@ -727,7 +855,7 @@ int bogus_gpu_solve_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, doub
   if (int e = ensure_pg_work(h, o->max_iters)) return e;
   BG_CUDA(cudaMemcpyAsync(h->X.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, h->stream));
   const double* best = nullptr;
-  const int st = run_pg(h, o, residual, iters, &best);
+  const int st = o->mixed_precision ? run_pg_mixed(h, o, residual, iters, &best) : run_pg(h, o, residual, iters, &best);
   if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
   BG_CUDA(cudaMemcpyAsync(r, best, sizeof(double) * n3, cudaMemcpyDeviceToHost, h->stream));
   BG_CUDA(cudaStreamSynchronize(h->stream));
@@ -1062,6 +1190,7 @@ int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double*
   h->has_dual = true;
   h->gs.valid = false;
   h->nproblems = 0;
+  h->fp32_valid = false;
   return BOGUS_GPU_OK;
 }
 
@@ -1166,30 +1295,26 @@ int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
   h->last_launches = 1;
   bool all = true;
-  double bytes = 0, fma = 0;
-  unsigned passes = 0, maxit = 0;
+  PGTraffic sum;
+  unsigned maxit = 0;
   const bool spg = o->variant == BOGUS_GPU_PG_SPG;
-  const double per_contact[9] = {56, 48, spg ? 168.0 : 144.0, 152, 80, 72, 144, 120, 96};
-  const bool has_w[9] = {false, true, false, true, false, false, true, false, true};
   for (int p = 0; p < np; ++p) {
     if (residuals) residuals[p] = out[p].min_res;
     if (iters) iters[p] = out[p].iters;
     all = all && (out[p].converged || h->h_contact_ptr[p + 1] == h->h_contact_ptr[p]);
     const int np_c = h->h_contact_ptr[p + 1] - h->h_contact_ptr[p];
-    const double wpass = (double)h->h_problem_nnz[p] * 76.0 + 4.0 * (np_c + 1);
-    for (int k = 0; k < 9; ++k) {
-      bytes += out[p].phases[k] * (per_contact[k] * np_c + (has_w[k] ? wpass : 0.0));
-      if (has_w[k]) {
-        passes += out[p].phases[k];
-        fma += out[p].phases[k] * 9.0 * h->h_problem_nnz[p] * (k == 1 ? 2.0 : 1.0);
-      }
-    }
+    const PGTraffic t = pg_traffic(out[p], np_c, h->h_problem_nnz[p], spg, 8.0);
+    sum.bytes += t.bytes;
+    sum.fma += t.fma;
+    sum.passes += t.passes;
     if (out[p].iters > maxit) maxit = out[p].iters;
   }
   h->last_stats.iterations = maxit;
-  h->last_stats.w_passes = passes;
-  h->last_stats.algorithmic_bytes = bytes;
-  h->last_stats.fp64_fma = fma;
+  h->last_stats.refine_iterations = 0;
+  h->last_stats.fp32_device_ms = 0.0;
+  h->last_stats.w_passes = sum.passes;
+  h->last_stats.algorithmic_bytes = sum.bytes;
+  h->last_stats.fp64_fma = sum.fma;
   return all ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
 }
 
@@ -1198,6 +1323,7 @@ int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
   if (int e = check_pg_options(o)) return e;
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
   if (h->nproblems == 0 && h->W.n > 0) return fail(BOGUS_GPU_NO_PROBLEM, "no batch partition set (bogus_gpu_set_batch)");
+  if (o->mixed_precision) return fail(BOGUS_GPU_BAD_INPUT, "batched solves run in FP64 only");
   if (int e = set_device(h)) return e;
   const int n = h->W.n;
   BG_CUDA(h->X.ensure(3 * 3 * (size_t)n));

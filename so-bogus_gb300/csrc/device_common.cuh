@@ -12,8 +12,10 @@ constexpr int kWarp = 32;
 
 // Loads of data written earlier in the same kernel by other CTAs must bypass L1 (it is not coherent).
 __device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
 // W streams through once per pass; keep it from evicting the L2-resident vectors.
 __device__ __forceinline__ double ldcs(const double* p) { return __ldcs(p); }
+__device__ __forceinline__ float ldcs(const float* p) { return __ldcs(p); }
 __device__ __forceinline__ int ldcs(const int* p) { return __ldcs(p); }
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {

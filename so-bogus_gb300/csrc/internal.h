@@ -22,7 +22,7 @@ struct DevBSR {
   int* diag = nullptr;    // n: position of the diagonal block, -1 when absent
 };
 
-// Arguments of the persistent projected-gradient kernels (APGD / Descent / SPG).
+// Result of a persistent projected-gradient solve (APGD / Descent / SPG).
 struct PGOut {
   double min_res;
   unsigned iters;
@@ -34,26 +34,29 @@ struct PGOut {
   unsigned phases[9];
 };
 
-struct PGArgs {
+// T: storage and per-contact arithmetic type (double: the FP64 drop-in; float: the FP32 part of the
+// mixed-precision solve). Reductions (chunk sums, published scalars, residual trace) are always FP64.
+template <class T>
+struct PGArgsT {
   int n, nchunks;
   const int* rowptr;
   const int* col;
-  const double* val;
-  const double* b;
-  const double* mu;
-  const double* scaling;
-  double* X0;
-  double* X1;
-  double* X2;
-  double* MX0;
-  double* MX1;
-  double* Y;
-  double* S0;
-  double* XB;
-  double* Wv;     // SPG step w
+  const T* val;
+  const T* b;
+  const T* mu;
+  const T* scaling;
+  T* X0;
+  T* X1;
+  T* X2;
+  T* MX0;
+  T* MX1;
+  T* Y;
+  T* S0;
+  T* XB;
+  T* Wv;          // SPG step w
   double* csum;   // 4 * nchunks chunk sums
   double* scal;   // published scalars
-  double* trace;  // residual per iteration
+  double* trace;  // residual per iteration (may be null)
   PGOut* out;
   GridBarrier gb;
   unsigned* tickets;  // 2 chunk counters (phase parity) for dynamic work distribution; zero at launch
@@ -61,18 +64,23 @@ struct PGArgs {
   double tol, opt, pess;
   unsigned max_iters, ls_iters;
 };
+using PGArgs = PGArgsT<double>;
+using PGArgs32 = PGArgsT<float>;
 
 // Batched solves: problem p owns contacts [contact_ptr[p], contact_ptr[p+1]) of every per-contact array of
 // `base` and chunk sums from 4 * chunk_ptr[p]; W rows are global, column indices local to the problem.
-struct PGBatchArgs {
-  PGArgs base;
+template <class T>
+struct PGBatchArgsT {
+  PGArgsT<T> base;
   int nproblems;
   const int* contact_ptr;
   const int* chunk_ptr;
   const int* queue;  // problem order (largest first)
   int* next;         // queue position counter (zeroed before the launch)
-  double* r;         // results, contact-major over all problems
+  T* r;              // results, contact-major over all problems
 };
+using PGBatchArgs = PGBatchArgsT<double>;
+using PGBatchArgs32 = PGBatchArgsT<float>;
 
 // Launchers (kernels_basic.cu)
 cudaError_t launch_spmv(const DevBSR& W, const double* x, const double* init, double* y, cudaStream_t s);
@@ -85,9 +93,13 @@ cudaError_t launch_add(int m, const double* a, const double* b, double* y, cudaS
 
 // Persistent solvers (kernels_pg.cu)
 cudaError_t launch_pg_persistent(const PGArgs& a, int grid, cudaStream_t s);
-int pg_max_grid(int device);
+cudaError_t launch_pg_persistent(const PGArgs32& a, int grid, cudaStream_t s);
+int pg_max_grid(int device, bool fp32 = false);
 cudaError_t launch_pg_batched(const PGBatchArgs& b, int grid, cudaStream_t s);
-int pg_batched_grid(int device);
+cudaError_t launch_pg_batched(const PGBatchArgs32& b, int grid, cudaStream_t s);
+int pg_batched_grid(int device, bool fp32 = false);
+cudaError_t launch_convert(size_t m, const double* src, float* dst, cudaStream_t s);
+cudaError_t launch_convert(size_t m, const float* src, double* dst, cudaStream_t s);
 
 // Gauss-Seidel (kernels_gs.cu)
 struct GSArgs {

@@ -127,6 +127,24 @@ cudaError_t launch_scale_scalar(double* p, double divisor, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+template <class S, class D>
+__global__ void k_convert(size_t m, const S* __restrict__ src, D* __restrict__ dst) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < m) dst[k] = (D)src[k];
+}
+
+cudaError_t launch_convert(size_t m, const double* src, float* dst, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  k_convert<double, float><<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, src, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_convert(size_t m, const float* src, double* dst, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  k_convert<float, double><<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, src, dst);
+  return cudaGetLastError();
+}
+
 // FP64 FMA throughput: eight independent chains per thread, enough warps to fill every SM.
 __global__ void k_fp64_peak(double* out, int iters, double a, double b) {
   double x[8];

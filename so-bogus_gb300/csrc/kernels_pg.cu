@@ -18,27 +18,31 @@
 // Without momentum x = xs and Mx = Mxs are buffer swaps and A runs as its own pass.
 #include "internal.h"
 #include "soc_device.cuh"
+#include "soc_ops.cuh"
 #include "spmv_chunk.cuh"
 
 namespace bogus_gpu {
 
 namespace {
 
-__device__ __forceinline__ void load3cg(const double* p, int i, double* v) {
+template <class T>
+__device__ __forceinline__ void load3cg(const T* p, int i, T* v) {
   v[0] = ldcg(p + 3 * i);
   v[1] = ldcg(p + 3 * i + 1);
   v[2] = ldcg(p + 3 * i + 2);
 }
-__device__ __forceinline__ void store3(double* p, int i, const double* v) {
+template <class T>
+__device__ __forceinline__ void store3(T* p, int i, const T* v) {
   p[3 * i] = v[0];
   p[3 * i + 1] = v[1];
   p[3 * i + 2] = v[2];
 }
 
+template <class T>
 struct Bufs {
-  const PGArgs& a;
-  __device__ double* X(int k) const { return k == 0 ? a.X0 : (k == 1 ? a.X1 : a.X2); }
-  __device__ double* MX(int k) const { return k == 0 ? a.MX0 : a.MX1; }
+  const PGArgsT<T>& a;
+  __device__ T* X(int k) const { return k == 0 ? a.X0 : (k == 1 ? a.X1 : a.X2); }
+  __device__ T* MX(int k) const { return k == 0 ? a.MX0 : a.MX1; }
 };
 
 __device__ __forceinline__ int third(int p, int q) {
@@ -49,13 +53,14 @@ __device__ __forceinline__ int third(int p, int q) {
 
 }  // namespace
 
-template <class Ctx>
-__device__ int pg_body(const PGArgs& a, Ctx& ctx) {
-  const Bufs B{a};
-  ChunkScratch& sh = ctx.cs[threadIdx.x >> 5];
+template <class T, class Ctx>
+__device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
+  using Ops = SocOps<T>;
+  const Bufs<T> B{a};
+  ChunkScratchT<T>& sh = ctx.cs[threadIdx.x >> 5];
   // y = W x of chunk c for every lane (row 32c + lane), x gathered from a buffer written earlier in the kernel
-  auto product = [&](int c, const double* __restrict__ xsrc, double* acc) {
-    spmv_chunk<1>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, double* x) { load3cg(xsrc, j, x); }, acc);
+  auto product = [&](int c, const T* __restrict__ xsrc, T* acc) {
+    spmv_chunk<1>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, T* x) { load3cg(xsrc, j, x); }, acc);
   };
   const int lane = threadIdx.x & 31;
   const bool desaxce = a.desaxce != 0;
@@ -93,9 +98,9 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
   for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
     const int i = 32 * c + lane;
     if (i < a.n) {
-      double x[3];
+      T x[3];
       load3cg(a.X0, i, x);
-      project_cone(__ldg(a.mu + i), x);
+      Ops::project(__ldg(a.mu + i), x);
       store3(a.X0, i, x);
     }
   }
@@ -106,15 +111,15 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
   for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
     const int i = 32 * c + lane;
     double v0 = 0.0, v1 = 0.0;
-    double acc[3] = {0.0, 0.0, 0.0}, accd[3] = {0.0, 0.0, 0.0};
-    spmv_chunk<2>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, double* x) { load3cg(a.X0, j, x); }, acc, accd);
+    T acc[3] = {T(0), T(0), T(0)}, accd[3] = {T(0), T(0), T(0)};
+    spmv_chunk<2>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, T* x) { load3cg(a.X0, j, x); }, acc, accd);
     if (i < a.n) {
       store3(a.MX0, i, acc);
-      v0 = sq3(accd);
-      double x[3];
+      v0 = Ops::sq3(accd);
+      T x[3];
       load3cg(a.X0, i, x);
-      const double d[3] = {x[0] - 1.0, x[1] - 1.0, x[2] - 1.0};
-      v1 = sq3(d);
+      const T d[3] = {x[0] - T(1), x[1] - T(1), x[2] - T(1)};
+      v1 = Ops::sq3(d);
     }
     put(0, c, v0, false);
     put(1, c, v1, false);
@@ -131,33 +136,34 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
 
   // Row-local part A, given Mx_i: writes y, s0 and xs = P(x - alpha_t y) (APGD) and returns the residual
   // and objective terms; SPG additionally needs (xs - prev).y.
-  auto phaseA = [&](int i, const double* Mx, double alpha_t, double& res_i, double& second_i) {
-    double x[3], bb[3];
+  auto phaseA = [&](int i, const T* Mx, double alpha_t, double& res_i, double& second_i) {
+    T x[3], bb[3];
     load3cg(B.X(ix), i, x);
     bb[0] = __ldg(a.b + 3 * i);
     bb[1] = __ldg(a.b + 3 * i + 1);
     bb[2] = __ldg(a.b + 3 * i + 2);
-    const double mu = __ldg(a.mu + i), sc = __ldg(a.scaling + i);
-    double y[3] = {Mx[0] + bb[0], Mx[1] + bb[1], Mx[2] + bb[2]};
-    const double lx[3] = {x[0] * sc, x[1] * sc, x[2] * sc};
-    res_i = law_eval(desaxce, mu, lx, y);
-    const double s0 = duality_cov(desaxce, mu, y);
+    const T mu = __ldg(a.mu + i), sc = __ldg(a.scaling + i);
+    T y[3] = {Mx[0] + bb[0], Mx[1] + bb[1], Mx[2] + bb[2]};
+    const T lx[3] = {x[0] * sc, x[1] * sc, x[2] * sc};
+    res_i = Ops::law_eval(desaxce, mu, lx, y);
+    const T s0 = Ops::cov(desaxce, mu, y);
     y[0] = y[0] + s0;
-    y[1] = y[1] + 0.0;
-    y[2] = y[2] + 0.0;
-    double xs[3] = {fma(-alpha_t, y[0], x[0]), fma(-alpha_t, y[1], x[1]), fma(-alpha_t, y[2], x[2])};
-    project_cone(mu, xs);
+    y[1] = y[1] + T(0);
+    y[2] = y[2] + T(0);
+    const T na = T(-alpha_t);
+    T xs[3] = {fma(na, y[0], x[0]), fma(na, y[1], x[1]), fma(na, y[2], x[2])};
+    Ops::project(mu, xs);
     store3(a.Y, i, y);
     a.S0[i] = s0;
     store3(B.X(ixs), i, xs);
     if (spg) {
-      double pv[3];
+      T pv[3];
       load3cg(B.X(iprev), i, pv);
-      const double d[3] = {xs[0] - pv[0], xs[1] - pv[1], xs[2] - pv[2]};
-      second_i = dot3(d, y);
+      const T d[3] = {xs[0] - pv[0], xs[1] - pv[1], xs[2] - pv[2]};
+      second_i = Ops::dot3(d, y);
     } else {
-      const double t[3] = {(0.5 * Mx[0] + bb[0]) + s0, (0.5 * Mx[1] + bb[1]) + 0.0, (0.5 * Mx[2] + bb[2]) + 0.0};
-      second_i = dot3(x, t);
+      const T t[3] = {(T(0.5) * Mx[0] + bb[0]) + s0, (T(0.5) * Mx[1] + bb[1]) + T(0), (T(0.5) * Mx[2] + bb[2]) + T(0)};
+      second_i = Ops::dot3(x, t);
     }
   };
 
@@ -167,7 +173,7 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
       const int i = 32 * c + lane;
       double r = 0.0, q = 0.0;
       if (i < a.n) {
-        double Mx[3];
+        T Mx[3];
         load3cg(B.MX(imx), i, Mx);
         phaseA(i, Mx, alpha_t, r, q);
       }
@@ -204,24 +210,24 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
         for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
-          double acc[3] = {0.0, 0.0, 0.0};
+          T acc[3] = {T(0), T(0), T(0)};
           product(c, B.X(ixs), acc);
           if (i < a.n) {
             store3(B.MX(1 - imx), i, acc);
-            double x[3], xs[3], pv[3], y[3];
+            T x[3], xs[3], pv[3], y[3];
             load3cg(B.X(ix), i, x);
             load3cg(B.X(ixs), i, xs);
             load3cg(B.X(iprev), i, pv);
             load3cg(a.Y, i, y);
-            const double s0 = ldcg(a.S0 + i);
-            const double t[3] = {(0.5 * acc[0] + __ldg(a.b + 3 * i)) + s0, (0.5 * acc[1] + __ldg(a.b + 3 * i + 1)) + 0.0,
-                                 (0.5 * acc[2] + __ldg(a.b + 3 * i + 2)) + 0.0};
-            v0 = dot3(xs, t);
-            const double d[3] = {xs[0] - x[0], xs[1] - x[1], xs[2] - x[2]};
-            v1 = dot3(y, d);
-            v2 = sq3(d);
-            const double d2[3] = {xs[0] - pv[0], xs[1] - pv[1], xs[2] - pv[2]};
-            v3 = dot3(d2, y);
+            const T s0 = ldcg(a.S0 + i);
+            const T t[3] = {(T(0.5) * acc[0] + __ldg(a.b + 3 * i)) + s0, (T(0.5) * acc[1] + __ldg(a.b + 3 * i + 1)) + T(0),
+                            (T(0.5) * acc[2] + __ldg(a.b + 3 * i + 2)) + T(0)};
+            v0 = Ops::dot3(xs, t);
+            const T d[3] = {xs[0] - x[0], xs[1] - x[1], xs[2] - x[2]};
+            v1 = Ops::dot3(y, d);
+            v2 = Ops::sq3(d);
+            const T d2[3] = {xs[0] - pv[0], xs[1] - pv[1], xs[2] - pv[2]};
+            v3 = Ops::dot3(d2, y);
             if (best_pending) store3(a.XB, i, x);
           }
           put(0, c, v0, false);
@@ -242,11 +248,12 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
         for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           if (i < a.n) {
-            double x[3], y[3];
+            T x[3], y[3];
             load3cg(B.X(ix), i, x);
             load3cg(a.Y, i, y);
-            double xs[3] = {fma(-alpha, y[0], x[0]), fma(-alpha, y[1], x[1]), fma(-alpha, y[2], x[2])};
-            project_cone(__ldg(a.mu + i), xs);
+            const T na = T(-alpha);
+            T xs[3] = {fma(na, y[0], x[0]), fma(na, y[1], x[1]), fma(na, y[2], x[2])};
+            Ops::project(__ldg(a.mu + i), xs);
             store3(B.X(ixs), i, xs);
           }
         }
@@ -261,11 +268,11 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
         for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           if (i < a.n) {
-            double xs[3], pv[3];
+            T xs[3], pv[3];
             load3cg(B.X(ixs), i, xs);
             load3cg(B.X(iprev), i, pv);
-            const double xn[3] = {fma(beta, xs[0] - pv[0], xs[0]), fma(beta, xs[1] - pv[1], xs[1]),
-                                  fma(beta, xs[2] - pv[2], xs[2])};
+            const T bt = T(beta);
+            const T xn[3] = {fma(bt, xs[0] - pv[0], xs[0]), fma(bt, xs[1] - pv[1], xs[1]), fma(bt, xs[2] - pv[2], xs[2])};
             store3(B.X(ix), i, xn);
           }
         }
@@ -279,7 +286,7 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
         for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           double r = 0.0, q = 0.0;
-          double acc[3] = {0.0, 0.0, 0.0};
+          T acc[3] = {T(0), T(0), T(0)};
           product(c, B.X(ix), acc);
           if (i < a.n) {
             store3(B.MX(imx), i, acc);
@@ -324,14 +331,15 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
     for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
       const int i = 32 * c + lane;
       if (i < a.n) {
-        double x[3], xs[3], pv[3], w[3], xn[3];
+        T x[3], xs[3], pv[3], w[3], xn[3];
         load3cg(B.X(ix), i, x);
         load3cg(B.X(ixs), i, xs);
         load3cg(B.X(iprev), i, pv);
         if (best_pending) store3(a.XB, i, x);
+        const T bt = T(beta);
         for (int k = 0; k < 3; ++k) {
           if (mom) {
-            w[k] = fma(beta, xs[k] - pv[k], xs[k]) - x[k];
+            w[k] = fma(bt, xs[k] - pv[k], xs[k]) - x[k];
             xn[k] = x[k] + w[k];
           } else {
             w[k] = xs[k] - x[k];
@@ -349,16 +357,16 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
     for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
       const int i = 32 * c + lane;
       double v0 = 0.0, v1 = 0.0;
-      double acc[3] = {0.0, 0.0, 0.0};
+      T acc[3] = {T(0), T(0), T(0)};
       product(c, B.X(ix), acc);
       if (i < a.n) {
-        double mo[3], w[3];
+        T mo[3], w[3];
         store3(B.MX(1 - imx), i, acc);
         load3cg(B.MX(imx), i, mo);
         load3cg(a.Wv, i, w);
-        const double z[3] = {-mo[0] + acc[0], -mo[1] + acc[1], -mo[2] + acc[2]};
-        v0 = dot3(w, z);
-        v1 = sq3(z);
+        const T z[3] = {-mo[0] + acc[0], -mo[1] + acc[1], -mo[2] + acc[2]};
+        v0 = Ops::dot3(w, z);
+        v1 = Ops::sq3(z);
       }
       put(0, c, v0, false);
       put(1, c, v1, false);
@@ -381,10 +389,11 @@ __device__ int pg_body(const PGArgs& a, Ctx& ctx) {
 // per phase parity, cleared by the last CTA of the barrier that ends the phase), so SMs that finish early
 // take more chunks; every cross-phase dependency goes through a barrier, and the reduction order does not
 // depend on which warp handles a chunk.
+template <class T>
 struct GridCtx {
-  const PGArgs& a;
+  const PGArgsT<T>& a;
   double* smem8;
-  ChunkScratch* cs;
+  ChunkScratchT<T>* cs;
   unsigned phase = 0;  // barriers passed (identical in every CTA)
   __device__ int ticket() {
     int c = 0;
@@ -419,20 +428,22 @@ struct GridCtx {
   __device__ double scal(int q) const { return ldcg(a.scal + q); }
 };
 
-__global__ void __launch_bounds__(256) k_pg_persistent(PGArgs a) {
+template <class T>
+__global__ void __launch_bounds__(256) k_pg_persistent(PGArgsT<T> a) {
   __shared__ double smem8[8];
-  __shared__ ChunkScratch cs[8];
-  GridCtx ctx{a, smem8, cs};
-  pg_body(a, ctx);
+  __shared__ ChunkScratchT<T> cs[8];
+  GridCtx<T> ctx{a, smem8, cs};
+  pg_body<T>(a, ctx);
 }
 
 // One problem per CTA (batched solves): phases separated by __syncthreads, scalars reduced by the CTA's
 // 8 warps (the same 8-stripe combination) and kept in shared memory.
+template <class T>
 struct BlockCtx {
-  const PGArgs& a;
+  const PGArgsT<T>& a;
   double* smem8;
   double* sscal;
-  ChunkScratch* cs;
+  ChunkScratchT<T>* cs;
   __device__ int first_chunk() const { return threadIdx.x >> 5; }
   __device__ int next_chunk(int c) const { return c + 8; }
   __device__ bool writer() const { return threadIdx.x == 0; }
@@ -454,9 +465,10 @@ struct BlockCtx {
 
 // Batched solves: CTAs take problems from a queue (largest first); each runs the complete solve of its
 // problem with the same arithmetic as the single-problem kernel, then writes the best iterate to r.
-__global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgs ba) {
+template <class T>
+__global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgsT<T> ba) {
   __shared__ double smem8[8], sscal[8];
-  __shared__ ChunkScratch cs[8];
+  __shared__ ChunkScratchT<T> cs[8];
   __shared__ int s_job;
   for (;;) {
     __syncthreads();
@@ -467,7 +479,7 @@ __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgs ba) {
     const int p = ba.queue[job];
     const int c0 = ba.contact_ptr[p];
     const int n = ba.contact_ptr[p + 1] - c0;
-    PGArgs a = ba.base;
+    PGArgsT<T> a = ba.base;
     a.n = n;
     a.nchunks = (n + 31) / 32;
     a.rowptr = ba.base.rowptr + c0;
@@ -486,38 +498,53 @@ __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgs ba) {
     a.csum = ba.base.csum + 4 * (size_t)ba.chunk_ptr[p];
     a.trace = nullptr;
     a.out = ba.base.out + p;
-    BlockCtx ctx{a, smem8, sscal, cs};
-    const int best = pg_body(a, ctx);
+    BlockCtx<T> ctx{a, smem8, sscal, cs};
+    const int best = pg_body<T>(a, ctx);
     __syncthreads();
     if (n == 0) continue;
-    const double* src = best == 3 ? a.XB : (best == 0 ? a.X0 : (best == 1 ? a.X1 : a.X2));
-    double* dst = ba.r + 3 * (size_t)c0;
+    const T* src = best == 3 ? a.XB : (best == 0 ? a.X0 : (best == 1 ? a.X1 : a.X2));
+    T* dst = ba.r + 3 * (size_t)c0;
     for (int k = threadIdx.x; k < 3 * n; k += blockDim.x) dst[k] = ldcg(src + k);
   }
 }
 
 cudaError_t launch_pg_batched(const PGBatchArgs& b, int grid, cudaStream_t s) {
-  k_pg_batched<<<grid, 256, 0, s>>>(b);
+  k_pg_batched<double><<<grid, 256, 0, s>>>(b);
   return cudaGetLastError();
 }
 
-int pg_batched_grid(int device) {
+cudaError_t launch_pg_batched(const PGBatchArgs32& b, int grid, cudaStream_t s) {
+  k_pg_batched<float><<<grid, 256, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+int pg_batched_grid(int device, bool fp32) {
   int sms = 0, per = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_batched, 256, 0) != cudaSuccess) return 0;
+  const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_batched<float>, 256, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_batched<double>, 256, 0);
+  if (e != cudaSuccess) return 0;
   return per * sms;
 }
 
 cudaError_t launch_pg_persistent(const PGArgs& a, int grid, cudaStream_t s) {
   PGArgs copy = a;
   void* args[] = {&copy};
-  return cudaLaunchCooperativeKernel((const void*)k_pg_persistent, dim3(grid), dim3(256), args, 0, s);
+  return cudaLaunchCooperativeKernel((const void*)k_pg_persistent<double>, dim3(grid), dim3(256), args, 0, s);
 }
 
-int pg_max_grid(int device) {
+cudaError_t launch_pg_persistent(const PGArgs32& a, int grid, cudaStream_t s) {
+  PGArgs32 copy = a;
+  void* args[] = {&copy};
+  return cudaLaunchCooperativeKernel((const void*)k_pg_persistent<float>, dim3(grid), dim3(256), args, 0, s);
+}
+
+int pg_max_grid(int device, bool fp32) {
   int sms = 0, per = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_persistent, 256, 0) != cudaSuccess) return 0;
+  const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_persistent<float>, 256, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_persistent<double>, 256, 0);
+  if (e != cudaSuccess) return 0;
   if (per > 2) per = 2;
   return per * sms;
 }

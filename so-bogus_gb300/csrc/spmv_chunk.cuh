@@ -16,18 +16,20 @@
 
 namespace bogus_gpu {
 
-struct ChunkScratch {
-  int st[33];            // row starts of the chunk (rows past n start at B1)
-  double part[63][6];    // pieces (up to two products)
+template <class T>
+struct ChunkScratchT {
+  int st[33];       // row starts of the chunk (rows past n start at B1)
+  T part[63][6];    // pieces (up to two products)
 };
+using ChunkScratch = ChunkScratchT<double>;
 
 // NP = 1: y = init + W x. NP = 2: additionally y2 = init2 + W (x - 1) (both from the same pass over W).
 // Every lane of the warp must call it (warp-uniform c). acc (and acc2) hold init on entry, the result on
 // exit, for row 32c + lane (lanes past n get unspecified values).
-template <int NP, class Gather>
+template <int NP, class T, class Gather>
 __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, const int* __restrict__ col,
-                                           const double* __restrict__ val, int n, int c, ChunkScratch& sh,
-                                           Gather&& gather, double* acc, double* acc2 = nullptr) {
+                                           const T* __restrict__ val, int n, int c, ChunkScratchT<T>& sh,
+                                           Gather&& gather, T* acc, T* acc2 = nullptr) {
   const int lane = threadIdx.x & 31;
   const int r0 = 32 * c;
   const int r1 = min(r0 + 32, n);
@@ -35,8 +37,8 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, const
   if (lane == 0) sh.st[32] = __ldg(rowptr + r1);
   __syncwarp();
   const int B0 = sh.st[0], B1 = sh.st[32];
-  const int T = B1 - B0;
-  const int S = T > 0 ? (T + 31) / 32 : 1;
+  const int nblk = B1 - B0;
+  const int S = nblk > 0 ? (nblk + 31) / 32 : 1;
   int k = B0 + lane * S;
   const int e = min(k + S, B1);
   if (k < e) {
@@ -48,41 +50,41 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, const
     }
     int t = lo;
     int next = sh.st[t + 1];
-    double p[3] = {0.0, 0.0, 0.0}, q[3] = {0.0, 0.0, 0.0};
+    T p[3] = {T(0), T(0), T(0)}, q[3] = {T(0), T(0), T(0)};
     bool open = false;
     for (; k < e; ++k) {
       while (k >= next) {
         if (open) {
-          double* s = sh.part[t + lane];
+          T* s = sh.part[t + lane];
           s[0] = p[0]; s[1] = p[1]; s[2] = p[2];
           if (NP == 2) { s[3] = q[0]; s[4] = q[1]; s[5] = q[2]; }
-          p[0] = p[1] = p[2] = 0.0;
-          q[0] = q[1] = q[2] = 0.0;
+          p[0] = p[1] = p[2] = T(0);
+          q[0] = q[1] = q[2] = T(0);
           open = false;
         }
         ++t;
         next = sh.st[t + 1];
       }
       const int j = ldcs(col + k);
-      double x[3];
+      T x[3];
       gather(j, x);
-      const double* Bk = val + 9 * (size_t)k;
-      double b[9];
+      const T* Bk = val + 9 * (size_t)k;
+      T b[9];
 #pragma unroll
       for (int e2 = 0; e2 < 9; ++e2) b[e2] = ldcs(Bk + e2);
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
-        double s = p[r];
+        T s = p[r];
         s = fma(b[3 * r + 0], x[0], s);
         s = fma(b[3 * r + 1], x[1], s);
         s = fma(b[3 * r + 2], x[2], s);
         p[r] = s;
       }
       if (NP == 2) {
-        const double d0 = x[0] - 1.0, d1 = x[1] - 1.0, d2 = x[2] - 1.0;
+        const T d0 = x[0] - T(1), d1 = x[1] - T(1), d2 = x[2] - T(1);
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-          double s = q[r];
+          T s = q[r];
           s = fma(b[3 * r + 0], d0, s);
           s = fma(b[3 * r + 1], d1, s);
           s = fma(b[3 * r + 2], d2, s);
@@ -92,7 +94,7 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, const
       open = true;
     }
     if (open) {
-      double* s = sh.part[t + lane];
+      T* s = sh.part[t + lane];
       s[0] = p[0]; s[1] = p[1]; s[2] = p[2];
       if (NP == 2) { s[3] = q[0]; s[4] = q[1]; s[5] = q[2]; }
     }
@@ -103,7 +105,7 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, const
     if (rs < re) {
       const int lf = (rs - B0) / S, ll = (re - 1 - B0) / S;
       for (int l = lf; l <= ll; ++l) {
-        const double* s = sh.part[lane + l];
+        const T* s = sh.part[lane + l];
         acc[0] = acc[0] + s[0];
         acc[1] = acc[1] + s[1];
         acc[2] = acc[2] + s[2];

@@ -104,6 +104,47 @@ def test_projected_gradient_bitwise(bg, oracle, c1, variant, static):
     assert trace_gpu == tr.items
 
 
+@pytest.mark.parametrize("static", [True, False])
+def test_mixed_precision_converges_to_fp64_residual(bg, oracle, c1, static):
+    """FP32 iterations then FP64 refinement: the returned residual is the FP64 error function of the returned
+    iterate (bit-identical to the oracle's), it meets the tolerance the FP64 solve meets, and the solve is
+    repeatable bit for bit."""
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    pg = bg.ProjectedGradient()
+    pg.setTol(1e-10)
+    pg.setMaxIters(400)
+    pg.setMixedPrecision(True, 200)
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r, staticProblem=static)
+    st = D.solve_stats()
+    assert res == O.eval(r, coulomb=not static)
+    res_o, _, _ = O.solve_pg(np.zeros(3 * d.n), variant=3, coulomb=not static, tol=1e-10, max_iters=600)
+    assert res_o < 1e-10 and res < 1e-10
+    assert 1 <= st["refine_iterations"] <= 201 and st["iterations"] >= st["refine_iterations"]
+    assert st["fp32_device_ms"] > 0 and st["kernel_launches"] >= 2
+    r2 = np.zeros(3 * d.n)
+    assert D.solveWith(pg, r2, staticProblem=static) == res and np.array_equal(r, r2)
+    # the FP64 path is untouched by the FP32 copies: a plain solve afterwards is still the oracle's
+    pg64 = bg.ProjectedGradient()
+    pg64.setTol(1e-8)
+    pg64.setMaxIters(400)
+    r3 = np.zeros(3 * d.n)
+    res3 = D.solveWith(pg64, r3, staticProblem=static)
+    res3_o, r3_o, _ = O.solve_pg(np.zeros(3 * d.n), variant=3, coulomb=not static, tol=1e-8, max_iters=400)
+    assert res3 == res3_o and np.array_equal(r3, r3_o)
+
+
+def test_mixed_precision_rejects_zero_refinement(bg, c1):
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    pg = bg.ProjectedGradient()
+    pg.setMixedPrecision(True, 0)
+    with pytest.raises(bg.BogusGpuError):
+        D.solveWith(pg, np.zeros(3 * d.n))
+
+
 @pytest.mark.parametrize("strategy", [3, 0, 2])
 @pytest.mark.parametrize("static", [False, True])
 @pytest.mark.parametrize("coloring", [False, True])
@@ -290,6 +331,27 @@ def test_full_size_apgd(bg, oracle, c2):
     res5 = D.solveWith(pg5, r5, staticProblem=False)
     res5_o, r5_o, _ = O.solve_pg(np.zeros(3 * d.n), variant=3, coulomb=True, max_iters=5)
     assert res5 == res5_o and np.array_equal(r5, r5_o)
+
+
+def test_full_size_mixed_precision(bg, oracle, c2):
+    """500 FP32 iterations + up to 50 FP64 ones on 200 000 contacts: the returned residual is the oracle's
+    FP64 error function at the returned iterate, and it is no worse than a tenth of the FP64 solve's
+    improvement over the start (the FP32 part does the work of the FP64 one)."""
+    d, D = c2
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    O = oracle.DualProblem(*P.assemble(), d.b, d.mu)
+    pg = bg.ProjectedGradient()
+    pg.setMaxIters(500)
+    pg.setMixedPrecision(True, 50)
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r, staticProblem=True)
+    assert res == O.eval(r, coulomb=False)
+    pg64 = bg.ProjectedGradient()
+    pg64.setMaxIters(500)
+    r64 = np.zeros(3 * d.n)
+    res64 = D.solveWith(pg64, r64, staticProblem=True)
+    res0 = O.eval(np.zeros(3 * d.n), coulomb=False)
+    assert res <= res0 - 0.9 * (res0 - res64)
 
 
 def test_full_size_gauss_seidel_first_sweeps(bg, oracle, c2):
