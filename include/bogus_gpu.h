@@ -93,11 +93,27 @@ typedef struct bogus_gpu_gs_options {
                                      MecheFrictionProblem::solve does with maxThreads != 1 */
 } bogus_gpu_gs_options;
 
+/* admm::Variant (Core/BlockSolvers/ADMM.hpp:21-29) */
+typedef enum bogus_gpu_admm_variant {
+  BOGUS_GPU_ADMM_STANDARD = 0,
+  BOGUS_GPU_ADMM_ACCELERATED = 1
+} bogus_gpu_admm_variant;
+
+/* ADMM setters and defaults (Core/BlockSolvers/ADMM.hpp:81-100, ConstrainedSolverBase.hpp:31). */
+typedef struct bogus_gpu_admm_options {
+  double tol;                     /* 1e-6 */
+  unsigned max_iters;             /* 300 */
+  double step_size;               /* 1e-2 */
+  int variant;                    /* bogus_gpu_admm_variant, Accelerated */
+  int use_infinity_norm;          /* 0 */
+} bogus_gpu_admm_options;
+
 typedef struct bogus_gpu_problem bogus_gpu_problem;
 
 /* Option defaults, identical to the reference's constructors. */
 void bogus_gpu_pg_options_default(bogus_gpu_pg_options* opts);
 void bogus_gpu_gs_options_default(bogus_gpu_gs_options* opts);
+void bogus_gpu_admm_options_default(bogus_gpu_admm_options* opts);
 
 const char* bogus_gpu_status_string(int status);
 /* Last CUDA / validation message recorded on this thread. */
@@ -180,6 +196,19 @@ int bogus_gpu_set_primal(bogus_gpu_problem* h, int nbodies, int ndof, const doub
  * device and b = w - H M^-1 f (w in the local basis, E = I; f may be NULL for f = 0); mu copied. The result
  * replaces the handle's dual problem. */
 int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double* w, const double* mu);
+
+/* PrimalFrictionProblem::solveWith(ADMMType&, lambda, v, r) (Interfaces/PrimalFrictionProblem.cpp:61-73), or
+ * ADMM::solve(law, QuadraticProxOp(prox, lambda, f), w, v, r) (Core/BlockSolvers/ADMM.impl.hpp:54-127) with
+ * an explicit prox operator: primal ADMM on the handle's primal data (bogus_gpu_set_primal), law
+ * SOCLaw<3, false> on 1 / mu, J(v) = v^T M v / 2 + f^T v.
+ *  - prox: nbodies x ndof x ndof blocks of the linear operator of QuadraticProxOp (row-major), or NULL for the
+ *    M^-1 blocks of bogus_gpu_set_primal (what PrimalFrictionProblem::solveWith passes, whatever lambda);
+ *  - f: nbodies x ndof (NULL: 0); w: 3 n (local basis, E = I); mu: n;
+ *  - v (nbodies x ndof) and r (3 n) are in/out (warm start and result);
+ *  - the callback, when set, fires once per iteration. */
+int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* opts, double lambda,
+                         const double* prox, const double* f, const double* w, const double* mu, double* v,
+                         double* r, double* residual, unsigned* iters);
 
 /* Copies the lower triangle of the device-held W back (rowptr[n+1], colidx/blocks sized by *nnzb_lower;
  * pass NULL arrays first to get the size). */

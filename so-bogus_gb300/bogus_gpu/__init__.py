@@ -26,6 +26,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libbogus_gpu.so")
 OK, NOT_CONVERGED, BAD_INPUT, NONFINITE, CUDA_ERROR, TIMEOUT, NO_DEVICE, NO_PROBLEM = range(8)
 STANDARD, DESCENT, CONJUGATED, APGD, SPG = range(5)            # projected_gradient::Variant
 PURE_NEWTON, PURE_ENUMERATIVE, HYBRID, REV_HYBRID = range(4)   # local_soc_solver::Strategy
+ADMM_STANDARD, ADMM_ACCELERATED = range(2)                     # admm::Variant
 
 
 class BogusGpuError(RuntimeError):
@@ -48,6 +49,11 @@ class GsOptions(C.Structure):
                 ("use_coloring", C.c_int)]
 
 
+class AdmmOptions(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint), ("step_size", C.c_double), ("variant", C.c_int),
+                ("use_infinity_norm", C.c_int)]
+
+
 class SolveStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("kernel_launches", C.c_uint), ("iterations", C.c_uint),
                 ("w_passes", C.c_uint), ("algorithmic_bytes", C.c_double), ("fp64_fma", C.c_double),
@@ -68,6 +74,7 @@ EXPORTED = [
     "bogus_gpu_set_primal", "bogus_gpu_assemble_dual", "bogus_gpu_get_dual_lower", "bogus_gpu_get_solve_stats",
     "bogus_gpu_get_stream", "bogus_gpu_measure_fp64_peak", "bogus_gpu_solve_pg_noalloc",
     "bogus_gpu_set_batch", "bogus_gpu_solve_pg_batch", "bogus_gpu_solve_pg_batch_device",
+    "bogus_gpu_admm_options_default", "bogus_gpu_solve_admm",
 ]
 
 
@@ -104,6 +111,10 @@ def lib():
     L.bogus_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.bogus_gpu_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.bogus_gpu_set_batch.argtypes = [vp, C.c_int, _ip]
+    L.bogus_gpu_admm_options_default.argtypes = [C.POINTER(AdmmOptions)]
+    L.bogus_gpu_admm_options_default.restype = None
+    L.bogus_gpu_solve_admm.argtypes = [vp, C.POINTER(AdmmOptions), C.c_double, vp, vp, _dp, _dp, _dp, _dp,
+                                       C.POINTER(C.c_double), C.POINTER(C.c_uint)]
     L.bogus_gpu_solve_pg_batch.argtypes = [vp, C.POINTER(PgOptions), _dp, _dp, np.ctypeslib.ndpointer(dtype=np.uint32)]
     L.bogus_gpu_solve_pg_batch_device.argtypes = [vp, C.POINTER(PgOptions), vp, _dp,
                                                   np.ctypeslib.ndpointer(dtype=np.uint32)]
@@ -241,16 +252,81 @@ class GaussSeidel(_SolverBase):
         return o
 
 
+class ADMM(_SolverBase):
+    """ADMM<HType> (Core/BlockSolvers/ADMM.hpp:41-110): tol 1e-6, 300 iterations, step size 1e-2,
+    Accelerated variant."""
+
+    def __init__(self):
+        super().__init__(1e-6, 300)
+        self._step = 1e-2
+        self._variant = ADMM_ACCELERATED
+
+    def setStepSize(self, s: float) -> None: self._step = float(s)
+    def stepSize(self) -> float: return self._step
+    def setDefaultVariant(self, v: int) -> None: self._variant = int(v)
+
+    def options(self) -> "AdmmOptions":
+        o = AdmmOptions()
+        lib().bogus_gpu_admm_options_default(C.byref(o))
+        o.tol, o.max_iters, o.step_size = self._tol, self._max_iters, self._step
+        o.variant, o.use_infinity_norm = self._variant, int(self._inf)
+        return o
+
+
 class PrimalFrictionProblem:
     """PrimalFrictionProblem<3> for rigid bodies (Interfaces/FrictionProblem.hpp:55-116): M^-1 blocks,
-    per-contact Jacobian blocks for one or two bodies, f, w (local contact basis), mu."""
+    per-contact Jacobian blocks for one or two bodies, f, w (local contact basis), mu. The arrays are uploaded
+    to the GPU on the first solveWith; call invalidate() after changing them."""
 
-    def __init__(self, minv, objA, objB, HA, HB, w, mu, f=None):
+    def __init__(self, minv, objA, objB, HA, HB, w, mu, f=None, device: int = 0):
         self.minv = _f64(minv)
         self.objA, self.objB = _i32(objA), _i32(objB)
         self.HA, self.HB = _f64(HA), _f64(HB)
         self.w, self.mu = _f64(w).reshape(-1), _f64(mu).reshape(-1)
         self.f = None if f is None else _f64(f).reshape(-1)
+        self._device = int(device)
+        self._gpu = None
+        self.last_status = self.last_iterations = None
+
+    def invalidate(self) -> None:
+        self._gpu = None
+
+    def _uploaded(self) -> "DualFrictionProblem":
+        if self._gpu is None:
+            g = DualFrictionProblem(self._device)
+            nb, ndof = self.minv.shape[0], self.minv.shape[1]
+            _check(lib().bogus_gpu_set_primal(g.handle, nb, ndof, self.minv.reshape(-1), self.objA.size, self.objA,
+                                              self.objB, self.HA.reshape(-1), self.HB.reshape(-1)), False)
+            self._gpu = g
+        return self._gpu
+
+    def solveWith(self, admm: "ADMM", lambda_: float, v, r, prox=None) -> float:
+        """PrimalFrictionProblem::solveWith(ADMMType&, lambda, v, r): v (nbodies * ndof) and r (3n) are solved in
+        place (float64, C-contiguous); returns the residual. prox: the QuadraticProxOp operator blocks
+        [nbodies, ndof, ndof] of ADMM::solve(law, op, w, v, r) (default M^-1, as the reference passes)."""
+        for a, name in ((v, "v"), (r, "r")):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+                raise TypeError(f"{name} must be a C-contiguous float64 numpy array (solved in place)")
+        if v.size != self.minv.shape[0] * self.minv.shape[1] or r.size != 3 * self.objA.size:
+            raise ValueError("inconsistent v / r sizes")
+        g = self._uploaded()
+        g._bind(admm)
+        o = admm.options()
+        res = C.c_double()
+        it = C.c_uint()
+        fptr = None if self.f is None else self.f.ctypes.data_as(C.c_void_p)
+        pb = None if prox is None else _f64(prox).reshape(-1)
+        if pb is not None and pb.size != self.minv.size:
+            raise ValueError("prox must hold nbodies x ndof x ndof blocks")
+        pptr = None if pb is None else pb.ctypes.data_as(C.c_void_p)
+        st = lib().bogus_gpu_solve_admm(g.handle, C.byref(o), float(lambda_), pptr, fptr, self.w, self.mu,
+                                         v.reshape(-1), r.reshape(-1), C.byref(res), C.byref(it))
+        _check(st)
+        self.last_status, self.last_iterations = st, it.value
+        return res.value
+
+    def solve_stats(self) -> dict:
+        return self._uploaded().solve_stats()
 
     @classmethod
     def from_generated(cls, data) -> "PrimalFrictionProblem":

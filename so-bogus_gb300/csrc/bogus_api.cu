@@ -138,6 +138,12 @@ struct bogus_gpu_problem {
   DevBuf<double> minv, H, T, mf;
   DevBuf<int> cb;  // per contact: body of slot 0, body of slot 1 (-1), slot order by body index
   std::vector<int> h_cb;
+  // ADMM: body -> (contact, slot) incidences in increasing contact order, per-call data and work
+  bool admm_incidence_valid = false;
+  size_t admm_ninc = 0;
+  DevBuf<int> bptr, bent;
+  DevBuf<double> a_prox, a_f, a_w, a_mu, a_invmu, a_x, a_r, a_ut, a_z, a_zacc, a_zprev, a_yprev;
+  DevBuf<ADMMOut> admm_out;
   // batch partition (block-diagonal W)
   int nproblems = 0;
   std::vector<int> h_contact_ptr, h_problem_nnz;
@@ -672,6 +678,12 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
     b->release();
   for (auto* b : {&h->val32, &h->b32, &h->mu32, &h->sc32, &h->X32, &h->MX32, &h->Y32, &h->S032, &h->XB32, &h->Wv32})
     b->release();
+  for (auto* b : {&h->a_prox, &h->a_f, &h->a_w, &h->a_mu, &h->a_invmu, &h->a_x, &h->a_r, &h->a_ut, &h->a_z, &h->a_zacc,
+                  &h->a_zprev, &h->a_yprev})
+    b->release();
+  h->bptr.release();
+  h->bent.release();
+  h->admm_out.release();
   h->rowptr.release();
   h->col.release();
   h->diag.release();
@@ -1050,7 +1062,161 @@ int bogus_gpu_set_primal(bogus_gpu_problem* h, int nbodies, int ndof, const doub
   h->ndof = ndof;
   h->ncontacts = ncontacts;
   h->h_cb = std::move(cbh);
+  h->admm_incidence_valid = false;
   return BOGUS_GPU_OK;
+}
+
+void bogus_gpu_admm_options_default(bogus_gpu_admm_options* o) {
+  if (!o) return;
+  o->tol = 1e-6;
+  o->max_iters = 300;
+  o->step_size = 1e-2;
+  o->variant = BOGUS_GPU_ADMM_ACCELERATED;
+  o->use_infinity_norm = 0;
+}
+
+int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, double lambda,
+                         const double* prox, const double* f, const double* w, const double* mu, double* v,
+                         double* r, double* residual, unsigned* iters) {
+  if (int e = check_handle(h)) return e;
+  if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
+  if (h->nbodies == 0) return fail(BOGUS_GPU_NO_PROBLEM, "no primal problem set (bogus_gpu_set_primal)");
+  if (o->variant != BOGUS_GPU_ADMM_STANDARD && o->variant != BOGUS_GPU_ADMM_ACCELERATED)
+    return fail(BOGUS_GPU_BAD_INPUT, "unknown ADMM variant");
+  if (!(o->step_size > 0) || !(o->tol >= 0) || !std::isfinite(lambda) || lambda < 0)
+    return fail(BOGUS_GPU_BAD_INPUT, "invalid ADMM step size, tolerance or lambda");
+  const int n = h->ncontacts, nb = h->nbodies, d = h->ndof;
+  const size_t n3 = 3 * (size_t)n, m = (size_t)nb * d;
+  if ((n > 0 && (!w || !mu || !r)) || !v) return fail(BOGUS_GPU_BAD_INPUT, "null w, mu, v or r");
+  if (int e = check_finite(w, n3, "w")) return e;
+  if (int e = check_finite(mu, n, "mu")) return e;
+  if (int e = check_finite(v, m, "v")) return e;
+  if (int e = check_finite(r, n3, "r")) return e;
+  if (f)
+    if (int e = check_finite(f, m, "f")) return e;
+  if (prox)
+    if (int e = check_finite(prox, m * d, "prox")) return e;
+  if (int e = set_device(h)) return e;
+  cudaStream_t s = h->stream;
+  if (!h->admm_incidence_valid) {
+    std::vector<int> bp(nb + 1, 0), be;
+    for (int i = 0; i < n; ++i)
+      for (int t = 0; t < 2; ++t)
+        if (h->h_cb[2 * (size_t)i + t] >= 0) ++bp[h->h_cb[2 * (size_t)i + t] + 1];
+    for (int k = 0; k < nb; ++k) bp[k + 1] += bp[k];
+    be.resize(bp[nb] > 0 ? bp[nb] : 1);
+    std::vector<int> fill(bp.begin(), bp.end() - 1);
+    for (int i = 0; i < n; ++i)  // increasing contact index within each body
+      for (int t = 0; t < 2; ++t) {
+        const int k = h->h_cb[2 * (size_t)i + t];
+        if (k >= 0) be[fill[k]++] = 2 * i + t;
+      }
+    BG_CUDA(h->bptr.ensure(nb + 1));
+    BG_CUDA(h->bent.ensure(be.size()));
+    BG_CUDA(cudaMemcpyAsync(h->bptr.p, bp.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->bent.p, be.data(), sizeof(int) * be.size(), cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+    h->admm_ninc = (size_t)bp[nb];
+    h->admm_incidence_valid = true;
+  }
+  const size_t nv = n3 > 0 ? n3 : 1;
+  for (auto* b : {&h->a_w, &h->a_r, &h->a_ut, &h->a_z, &h->a_zacc, &h->a_zprev, &h->a_yprev}) BG_CUDA(b->ensure(nv));
+  BG_CUDA(h->a_mu.ensure(n > 0 ? n : 1));
+  BG_CUDA(h->a_invmu.ensure(n > 0 ? n : 1));
+  BG_CUDA(h->a_x.ensure(m));
+  if (f) BG_CUDA(h->a_f.ensure(m));
+  if (prox) BG_CUDA(h->a_prox.ensure(m * d));
+  const int C = (n + 31) / 32;
+  BG_CUDA(h->csum.ensure(2 * (size_t)(C > 0 ? C : 1)));
+  BG_CUDA(h->scal.ensure(8));
+  BG_CUDA(h->trace.ensure((size_t)o->max_iters + 1));
+  BG_CUDA(h->admm_out.ensure(1));
+  BG_CUDA(h->barrier.ensure(4));
+  BG_CUDA(h->status.ensure(1));
+  if (n > 0) {
+    BG_CUDA(cudaMemcpyAsync(h->a_w.p, w, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->a_mu.p, mu, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->a_r.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  }
+  BG_CUDA(cudaMemcpyAsync(h->a_x.p, v, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  if (f) BG_CUDA(cudaMemcpyAsync(h->a_f.p, f, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  if (prox) BG_CUDA(cudaMemcpyAsync(h->a_prox.p, prox, sizeof(double) * m * d, cudaMemcpyHostToDevice, s));
+  ADMMArgs a{};
+  a.n = n;
+  a.nbodies = nb;
+  a.d = d;
+  a.cb = h->cb.p;
+  a.H = h->H.p;
+  a.bptr = h->bptr.p;
+  a.bent = h->bent.p;
+  a.prox = prox ? h->a_prox.p : h->minv.p;
+  a.f = f ? h->a_f.p : nullptr;
+  a.w = h->a_w.p;
+  a.mu = h->a_mu.p;
+  a.inv_mu = h->a_invmu.p;
+  a.x = h->a_x.p;
+  a.r = h->a_r.p;
+  a.ut = h->a_ut.p;
+  a.z = h->a_z.p;
+  a.zacc = h->a_zacc.p;
+  a.zprev = h->a_zprev.p;
+  a.yprev = h->a_yprev.p;
+  a.csum = h->csum.p;
+  a.scal = h->scal.p;
+  a.trace = h->trace.p;
+  a.out = h->admm_out.p;
+  a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.lambda = lambda;
+  a.gamma = o->step_size;
+  a.tol = o->tol;
+  a.max_iters = o->max_iters;
+  a.accelerated = o->variant == BOGUS_GPU_ADMM_ACCELERATED;
+  a.use_inf = o->use_infinity_norm ? 1 : 0;
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), s));
+  BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
+  int grid = admm_max_grid(h->device, d);
+  if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
+  const int units = ((n > nb ? n : nb) + 31) / 32;
+  const int want = (units + 7) / 8;
+  if (want < grid) grid = want < 1 ? 1 : want;
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  BG_CUDA(launch_admm(a, grid, s));
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  ADMMOut out{};
+  int st = 0;
+  BG_CUDA(cudaMemcpyAsync(&out, h->admm_out.p, sizeof(ADMMOut), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaMemcpyAsync(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  h->last_launches = 1;
+  if (st != 0) return fail(st, "device-side wait timed out in the ADMM kernel");
+  BG_CUDA(cudaMemcpy(v, h->a_x.p, sizeof(double) * m, cudaMemcpyDeviceToHost));
+  if (n > 0) BG_CUDA(cudaMemcpy(r, h->a_r.p, sizeof(double) * n3, cudaMemcpyDeviceToHost));
+  {
+    // per iteration: P1 reads the incidences, 3 x d H rows, r (and zacc, ut with lambda) per incidence,
+    // the d x d prox block, f and x per body and writes x; P2 reads H, x of the bodies, w, r, z, 1/mu and
+    // writes ut per contact; P3 reads ut, r (y_prev, z_prev) and writes r, z, zacc, z_prev, y_prev
+    const double inc = (double)h->admm_ninc;
+    const double p1 = inc * (4.0 + 24.0 * d + 24.0 + (lambda < 2.220446049250313e-16 ? 0.0 : 48.0)) +
+                      (double)nb * (8.0 * d * d + (f ? 16.0 : 8.0) * d + 4.0);
+    const double p2 = inc * (24.0 * d + 8.0 * d + 4.0) + (double)n * (24.0 * 4 + 8.0);
+    const double p3 = (double)n * (24.0 * 2 + 8.0 + 48.0 + 24.0 * 4);
+    h->last_stats.iterations = out.iters;
+    h->last_stats.refine_iterations = 0;
+    h->last_stats.fp32_device_ms = 0.0;
+    h->last_stats.w_passes = 0;
+    h->last_stats.algorithmic_bytes = out.iters * (p1 + p2 + p3) + (p2 + p3);
+    h->last_stats.fp64_fma = (double)out.iters * inc * 3.0 * d * 2.0;
+  }
+  if (residual) *residual = out.res;
+  if (iters) *iters = out.iters;
+  if (h->callback) {
+    const unsigned count = out.converged ? out.iters + 1 : out.iters;
+    std::vector<double> tr(count);
+    if (count) BG_CUDA(cudaMemcpy(tr.data(), h->trace.p, sizeof(double) * count, cudaMemcpyDeviceToHost));
+    for (unsigned k = 0; k < count; ++k) h->callback(k, tr[k], h->callback_user);
+  }
+  return out.converged ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
 }
 
 int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double* w, const double* mu) {

@@ -129,6 +129,37 @@ cudaError_t launch_gs_skip(const GSArgs& a, int parity, double abs_skip_tol, dou
 cudaError_t launch_scale_scalar(double* p, double divisor, cudaStream_t s);
 cudaError_t measure_fp64_peak(int device, double* tflops);
 
+// Primal ADMM / AMA (kernels_admm.cu): Core/BlockSolvers/ADMM.impl.hpp:54-127 with QuadraticProxOp
+// (:29-38) as PrimalFrictionProblem::solveWith(ADMM&, lambda, v, r) calls it (PrimalFrictionProblem.cpp:61-73).
+struct ADMMOut {
+  double res;
+  unsigned iters;
+  int converged;
+};
+struct ADMMArgs {
+  int n, nbodies, d;
+  const int* cb;       // 2 n: bodies of the contact's two H slots, ordered by body index (-1: none)
+  const double* H;     // 2 n x 3 x d: slot blocks, row-major
+  const int* bptr;     // nbodies + 1
+  const int* bent;     // incidences of each body, increasing contact index: 2 i + slot
+  const double* prox;  // nbodies x d x d: the prox operator's blocks (M^-1)
+  const double* f;     // nbodies x d, or null (f = 0)
+  const double* w;     // 3 n
+  const double* mu;    // n
+  double* inv_mu;      // n (written)
+  double *x, *r, *ut, *z, *zacc, *zprev, *yprev;
+  double* csum;        // 2 x nchunks
+  double* scal;        // published scalars
+  double* trace;       // max_iters entries, or null
+  ADMMOut* out;
+  GridBarrier gb;
+  double lambda, gamma, tol;
+  unsigned max_iters;
+  int accelerated, use_inf;
+};
+cudaError_t launch_admm(const ADMMArgs& a, int grid, cudaStream_t s);
+int admm_max_grid(int device, int d);
+
 // Records the message returned by bogus_gpu_last_error() on this thread.
 void set_last_error(const std::string& msg);
 

@@ -1,0 +1,285 @@
+// Persistent primal ADMM / AMA solver: the whole ADMM::solve (Core/BlockSolvers/ADMM.impl.hpp:54-127) with
+// QuadraticProxOp::eval (:29-38) in one cooperative launch, as PrimalFrictionProblem::solveWith(ADMM&,
+// lambda, v, r) (Interfaces/PrimalFrictionProblem.cpp:61-73) sets it up: law SOCLaw<3, false> on 1 / mu,
+// constraint matrix H (contacts x bodies, 3 x d blocks), prox operator M^-1 (the reference passes MInv
+// whatever lambda), affine part f, offset w.
+//
+// Phases of one iteration (ADMM.impl.hpp line numbers):
+//   P1 bodies    prox_arg = H^T r (lambda = 0, :85) or x / lambda + H^T (r + gamma (zacc - ut)) (:87-89),
+//                x = prox (prox_arg - f) (:91) .............................................. barrier
+//   P2 contacts  ut = w + H x (:93), error terms FB(1/mu; ut_i, r_i) and |ut_i - z_i|^2 (:95-98) .. barrier
+//                + reduce: res (:95-98), tolerance test (:100)
+//   P3 contacts  z = P(ut - r / gamma) (:102-103), r / y / zacc update, accelerated or not (:105-122) . barrier
+// Body b's H^T accumulation runs over its contacts in increasing contact index, rows 0..2, one FMA chain
+// per dof; contact rows accumulate w, then the slots in body order, dofs 0..d-1; the prox product is an FMA
+// chain over the dofs. Sums use the canonical order (32-contact butterflies, 8 stripes), so the GPU's
+// iterates and residuals equal the CPU oracle's bit for bit. Waits are bounded (grid_barrier).
+#include "internal.h"
+#include "soc_device.cuh"
+
+namespace bogus_gpu {
+
+namespace {
+
+constexpr int kMaxDof = 12;
+
+struct AdmmCtx {
+  const ADMMArgs& a;
+  double* smem8;
+  int nchunks;
+  __device__ bool sync() { return grid_barrier(a.gb, [] {}); }
+  __device__ bool sync_reduce2(unsigned maxmask) {
+    return grid_barrier(a.gb, [&] {
+      for (int q = 0; q < 2; ++q) {
+        const double v = block8_combine(a.csum + q * nchunks, nchunks, (maxmask >> q) & 1u, smem8);
+        if (threadIdx.x == 0) a.scal[q] = v;
+      }
+    });
+  }
+};
+
+// D > 0: d fixed at compile time (registers); D == 0: runtime d <= kMaxDof.
+template <int D>
+__device__ __forceinline__ int dofs(const ADMMArgs& a) {
+  return D > 0 ? D : a.d;
+}
+
+// ut_i = w_i + H_i x (ADMM.impl.hpp:93 via the reference's multiply<false>(x, ut, 1, 1) after ut = w)
+template <int D>
+__device__ __forceinline__ void contact_velocity(const ADMMArgs& a, int i, double* ut) {
+  const int d = dofs<D>(a);
+  const size_t hs = 3 * (size_t)d;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) ut[r] = __ldg(a.w + 3 * i + r);
+  for (int t = 0; t < 2; ++t) {
+    const int body = __ldg(a.cb + 2 * i + t);
+    if (body < 0) continue;
+    const double* Hb = a.H + (2 * (size_t)i + t) * hs;
+    const double* xb = a.x + (size_t)body * d;
+    double xv[D > 0 ? D : kMaxDof];
+#pragma unroll
+    for (int m = 0; m < (D > 0 ? D : kMaxDof); ++m)
+      if (m < d) xv[m] = ldcg(xb + m);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      double acc = ut[r];
+#pragma unroll
+      for (int m = 0; m < (D > 0 ? D : kMaxDof); ++m)
+        if (m < d) acc = fma(__ldg(Hb + r * d + m), xv[m], acc);
+      ut[r] = acc;
+    }
+  }
+}
+
+__device__ __forceinline__ void load3(const double* p, int i, double* v) {
+  v[0] = ldcg(p + 3 * i);
+  v[1] = ldcg(p + 3 * i + 1);
+  v[2] = ldcg(p + 3 * i + 2);
+}
+__device__ __forceinline__ void store3(double* p, int i, const double* v) {
+  p[3 * i] = v[0];
+  p[3 * i + 1] = v[1];
+  p[3 * i + 2] = v[2];
+}
+
+template <int D>
+__device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
+  constexpr int DM = D > 0 ? D : kMaxDof;
+  const int d = dofs<D>(a);
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  const int C = ctx.nchunks;
+  const int CB = (a.nbodies + 31) / 32;
+  const double gamma = a.gamma;
+  const double inv_gamma = 1. / gamma;
+  const bool with_lambda = !(a.lambda < kEps);
+  const double il = with_lambda ? 1. / a.lambda : 0.0;
+  const bool writer = blockIdx.x == 0 && threadIdx.x == 0;
+  auto put = [&](int q, int c, double v, bool is_max) {
+    v = is_max ? warp_max_butterfly(v) : warp_sum_butterfly(v);
+    if (lane == 0) a.csum[q * C + c] = v;
+  };
+
+  // Setup (:64-77): ut = w + H x, z = P(ut - r / gamma), y_prev = -r / gamma, zacc = z_prev = z
+  for (int c = gwarp; c < C; c += nwarps) {
+    const int i = 32 * c + lane;
+    if (i < a.n) {
+      const double im = 1. / __ldg(a.mu + i);
+      a.inv_mu[i] = im;
+      double ut[3], r[3], z[3];
+      contact_velocity<D>(a, i, ut);
+      load3(a.r, i, r);
+      for (int k = 0; k < 3; ++k) z[k] = ut[k] - inv_gamma * r[k];
+      project_cone(im, z);
+      const double yp[3] = {-inv_gamma * r[0], -inv_gamma * r[1], -inv_gamma * r[2]};
+      store3(a.ut, i, ut);
+      store3(a.z, i, z);
+      store3(a.zacc, i, z);
+      store3(a.zprev, i, z);
+      store3(a.yprev, i, yp);
+    }
+  }
+  if (!ctx.sync()) return;
+
+  double theta_prev = 1., res_prev = -1., res = -1.;
+  unsigned it = 0;
+  for (it = 0; it < a.max_iters; ++it) {
+    // P1: x = prox(prox_arg) per body
+    for (int c = gwarp; c < CB; c += nwarps) {
+      const int b = 32 * c + lane;
+      if (b < a.nbodies) {
+        double acc[DM];
+        const double* xb = a.x + (size_t)b * d;
+#pragma unroll
+        for (int q = 0; q < DM; ++q)
+          if (q < d) acc[q] = with_lambda ? il * ldcg(xb + q) : 0.0;
+        const int e0 = __ldg(a.bptr + b), e1 = __ldg(a.bptr + b + 1);
+        for (int e = e0; e < e1; ++e) {
+          const int ent = __ldg(a.bent + e);
+          const int i = ent >> 1;
+          const double* Hb = a.H + (size_t)ent * 3 * d;
+          double rv[3];
+          load3(a.r, i, rv);
+          if (with_lambda) {
+            double za[3], ut[3];
+            load3(a.zacc, i, za);
+            load3(a.ut, i, ut);
+            for (int k = 0; k < 3; ++k) rv[k] = fma(gamma, za[k] - ut[k], rv[k]);
+          }
+#pragma unroll
+          for (int q = 0; q < DM; ++q) {
+            if (q < d) {
+              double s = acc[q];
+              for (int rr = 0; rr < 3; ++rr) s = fma(__ldg(Hb + rr * d + q), rv[rr], s);
+              acc[q] = s;
+            }
+          }
+        }
+        // QuadraticProxOp::eval: res = prox (rhs - f)
+        if (a.f) {
+#pragma unroll
+          for (int q = 0; q < DM; ++q)
+            if (q < d) acc[q] = acc[q] - __ldg(a.f + (size_t)b * d + q);
+        }
+        const double* P = a.prox + (size_t)b * d * d;
+        double xn[DM];
+#pragma unroll
+        for (int m = 0; m < DM; ++m) {
+          if (m < d) {
+            double s = 0.0;
+#pragma unroll
+            for (int q = 0; q < DM; ++q)
+              if (q < d) s = fma(__ldg(P + m * d + q), acc[q], s);
+            xn[m] = s;
+          }
+        }
+        double* xw = a.x + (size_t)b * d;
+#pragma unroll
+        for (int m = 0; m < DM; ++m)
+          if (m < d) xw[m] = xn[m];
+      }
+    }
+    if (!ctx.sync()) return;
+
+    // P2: ut = w + H x, error terms
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      double ev = 0.0, gap = 0.0;
+      if (i < a.n) {
+        double ut[3], r[3], z[3];
+        contact_velocity<D>(a, i, ut);
+        store3(a.ut, i, ut);
+        load3(a.r, i, r);
+        load3(a.z, i, z);
+        ev = law_eval(false, ldcg(a.inv_mu + i), ut, r);
+        const double d3[3] = {ut[0] - z[0], ut[1] - z[1], ut[2] - z[2]};
+        gap = a.use_inf ? dmax(dmax(fabs(d3[0]), fabs(d3[1])), fabs(d3[2])) : sq3(d3);
+      }
+      put(0, c, ev, a.use_inf != 0);
+      put(1, c, gap, a.use_inf != 0);
+    }
+    if (!ctx.sync_reduce2(a.use_inf ? 3u : 0u)) return;
+    {
+      const double e0 = ldcg(a.scal), g0 = ldcg(a.scal + 1);
+      res = a.use_inf ? e0 + g0 : e0 / (double)(1 + a.n) + g0 / (double)(1 + 3 * (size_t)a.n);
+    }
+    if (a.trace && writer) a.trace[it] = res;
+    if (res < a.tol) break;
+
+    // P3: z and the dual update
+    const bool acc_branch = a.accelerated && res < res_prev;
+    double beta = 0.0;
+    if (acc_branch) beta = nesterov_inertia(theta_prev, 0.);
+    else theta_prev = 1.;
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      if (i < a.n) {
+        double ut[3], r[3], z[3];
+        load3(a.ut, i, ut);
+        load3(a.r, i, r);
+        for (int k = 0; k < 3; ++k) z[k] = ut[k] - inv_gamma * r[k];
+        project_cone(ldcg(a.inv_mu + i), z);
+        if (acc_branch) {
+          double yp[3], zp[3], y[3], rn[3], za[3];
+          load3(a.yprev, i, yp);
+          load3(a.zprev, i, zp);
+          for (int k = 0; k < 3; ++k) {
+            y[k] = (ut[k] - z[k]) - inv_gamma * r[k];
+            rn[k] = -gamma * fma(beta, y[k] - yp[k], y[k]);
+            za[k] = fma(beta, z[k] - zp[k], z[k]);
+          }
+          store3(a.r, i, rn);
+          store3(a.yprev, i, y);
+          store3(a.zacc, i, za);
+        } else {
+          double rn[3], yp[3];
+          for (int k = 0; k < 3; ++k) {
+            rn[k] = fma(gamma, z[k] - ut[k], r[k]);
+            yp[k] = -inv_gamma * rn[k];
+          }
+          store3(a.r, i, rn);
+          store3(a.zacc, i, z);
+          store3(a.yprev, i, yp);
+        }
+        store3(a.z, i, z);
+        store3(a.zprev, i, z);
+      }
+    }
+    res_prev = res;
+    if (!ctx.sync()) return;
+  }
+  if (writer) {
+    a.out->res = res;
+    a.out->iters = it;
+    a.out->converged = res >= 0 && res < a.tol;
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_admm_persistent(ADMMArgs a) {
+  __shared__ double smem8[8];
+  AdmmCtx ctx{a, smem8, (a.n + 31) / 32};
+  admm_body<D>(a, ctx);
+}
+
+}  // namespace
+
+cudaError_t launch_admm(const ADMMArgs& a, int grid, cudaStream_t s) {
+  ADMMArgs copy = a;
+  void* args[] = {&copy};
+  const void* fn = a.d == 6 ? (const void*)k_admm_persistent<6> : (const void*)k_admm_persistent<0>;
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s);
+}
+
+int admm_max_grid(int device, int d) {
+  int sms = 0, per = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  const cudaError_t e = d == 6 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_admm_persistent<6>, 256, 0)
+                               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_admm_persistent<0>, 256, 0);
+  if (e != cudaSuccess) return 0;
+  if (per > 2) per = 2;
+  return per * sms;
+}
+
+}  // namespace bogus_gpu

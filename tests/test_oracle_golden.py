@@ -161,6 +161,49 @@ def test_small_friction_projected_gradient(oracle, golden, variant):
     assert res < 1e-8
 
 
+# ---- tests/ADMM.cpp:16-60 (primal AMA with lambda = 0, ADMM with lambda = 0.1) ---------------------------
+def _small_primal(oracle, golden):
+    s = golden["small_friction_pb"]
+    minv = np.array(s["minv"])
+    P = oracle.PrimalProblem(minv, s["objA"], s["objB"], np.array(s["HA"]), np.array(s["HB"]))
+    HA, HB = np.array(s["HA"]), np.array(s["HB"])
+    nd = s["ndof_padded"]
+    Hd = np.zeros((6, 2 * nd))  # dense H of the padded layout
+    for i in range(2):
+        Hd[3 * i:3 * i + 3, nd * s["objA"][i]:nd * s["objA"][i] + nd] += HA[i]
+        if s["objB"][i] >= 0:
+            Hd[3 * i:3 * i + 3, nd * s["objB"][i]:nd * s["objB"][i] + nd] += HB[i]
+    return s, P, minv, Hd
+
+
+def admm_inputs(s, minv, Hd, lam):
+    """The reference test's start (r = 1, v = M^-1 (H^T r - f)) and prox operator: M^-1 for lambda = 0, else
+    (M + I / lambda)^-1 per body (inert padded dofs: 0)."""
+    f = np.array(s["f_padded"])
+    nd = s["ndof_padded"]
+    r = np.ones(6)
+    Minv = np.zeros((2 * nd, 2 * nd))
+    for k in range(2):
+        Minv[nd * k:nd * k + nd, nd * k:nd * k + nd] = minv[k]
+    v = Minv @ (Hd.T @ r - f)
+    if lam == 0:
+        return minv.copy(), v, r, f
+    prox = np.zeros_like(minv)
+    for k, dk in enumerate(s["dofs"]):
+        Mk = np.linalg.inv(minv[k, :dk, :dk])
+        prox[k, :dk, :dk] = np.linalg.inv(Mk + np.eye(dk) / lam)
+    return prox, v, r, f
+
+
+@pytest.mark.parametrize("lam", [0.0, 0.1])
+def test_small_friction_admm(oracle, golden, lam):
+    s, P, minv, Hd = _small_primal(oracle, golden)
+    prox, v, r, f = admm_inputs(s, minv, Hd, lam)
+    res, v, r, it = P.solve_admm(prox, lam, np.array(s["mu"]), f, np.array(s["w"]), v, r, tol=1e-8, max_iters=1000,
+                                 step=1e-2, accelerated=True)
+    assert 0 <= res < 1e-8 and it < 1000
+
+
 def test_coloring_is_valid_and_follows_reference_rule(oracle):
     from bogus_gpu import generator
 
