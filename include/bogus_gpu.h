@@ -210,6 +210,36 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* opt
                          const double* prox, const double* f, const double* w, const double* mu, double* v,
                          double* r, double* residual, unsigned* iters);
 
+/* ---- Adjoint of the SOC solve (no counterpart in the reference, which has no differentiation) ------------
+ * r solves min 1/2 r^T W r + b^T r over r_i in K_mu_i = {|x_T| <= mu x_N} (the SOCLaw<3> problem that
+ * bogus_gpu_solve_pg solves with static_problem = 1). Given that solution r and g = dL/dr of a loss L, the
+ * implicit-function gradients dL/db and dL/dmu follow from one linear solve (conjugate gradients on the
+ * device, one pass over W per iteration, to relative residual tol). r should be solved tightly: the
+ * gradients are those of the fixed point at r. W must be positive definite on the contacts' active
+ * directions (add a compliance term, bogus_gpu_add_compliance, where H M^-1 H^T is singular). */
+typedef struct bogus_gpu_adjoint_options {
+  double tol;                     /* 1e-10 */
+  unsigned max_iters;             /* 5000 */
+} bogus_gpu_adjoint_options;
+void bogus_gpu_adjoint_options_default(bogus_gpu_adjoint_options* opts);
+/* dL_db (3 n) and dL_dmu (n) from r and dL_dr (host arrays); residual: final relative CG residual. */
+int bogus_gpu_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* opts, const double* r,
+                      const double* dL_dr, double* dL_db, double* dL_dmu, double* residual, unsigned* iters);
+/* Same with device arrays. */
+int bogus_gpu_adjoint_device(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* opts, const double* d_r,
+                             const double* d_dL_dr, double* d_dL_db, double* d_dL_dmu, double* residual,
+                             unsigned* iters);
+/* After bogus_gpu_adjoint: dL/dW for the stored lower blocks (the order of bogus_gpu_get_dual_lower; block
+ * W_ij, i > j, stands for W_ji = W_ij^T too): s_i r_j^T + r_i s_j^T off the diagonal, s_i r_i^T on it. */
+int bogus_gpu_adjoint_dual_lower(bogus_gpu_problem* h, double* dL_dW_lower);
+/* After bogus_gpu_adjoint on a W assembled from the handle's primal data (W = H M^-1 H^T, plus compliance,
+ * b = w - H M^-1 f): dL/dHA, dL/dHB (n x 3 x ndof, zero where the contact has no body B), dL/dw (3 n) and
+ * dL/df (nbodies x ndof); f: the f of the assembly (NULL: 0). Any output may be NULL. */
+int bogus_gpu_adjoint_primal(bogus_gpu_problem* h, const double* f, double* dL_dHA, double* dL_dHB, double* dL_dw,
+                             double* dL_df);
+/* W_ii += c_i I for every contact (a compliance term); c: n values >= 0. */
+int bogus_gpu_add_compliance(bogus_gpu_problem* h, const double* c);
+
 /* Copies the lower triangle of the device-held W back (rowptr[n+1], colidx/blocks sized by *nnzb_lower;
  * pass NULL arrays first to get the size). */
 int bogus_gpu_get_dual_lower(bogus_gpu_problem* h, int* rowptr, int* colidx, double* blocks, int* nnzb_lower);

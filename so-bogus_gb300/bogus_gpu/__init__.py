@@ -54,6 +54,10 @@ class AdmmOptions(C.Structure):
                 ("use_infinity_norm", C.c_int)]
 
 
+class AdjointOptions(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint)]
+
+
 class SolveStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("kernel_launches", C.c_uint), ("iterations", C.c_uint),
                 ("w_passes", C.c_uint), ("algorithmic_bytes", C.c_double), ("fp64_fma", C.c_double),
@@ -74,7 +78,9 @@ EXPORTED = [
     "bogus_gpu_set_primal", "bogus_gpu_assemble_dual", "bogus_gpu_get_dual_lower", "bogus_gpu_get_solve_stats",
     "bogus_gpu_get_stream", "bogus_gpu_measure_fp64_peak", "bogus_gpu_solve_pg_noalloc",
     "bogus_gpu_set_batch", "bogus_gpu_solve_pg_batch", "bogus_gpu_solve_pg_batch_device",
-    "bogus_gpu_admm_options_default", "bogus_gpu_solve_admm",
+    "bogus_gpu_admm_options_default", "bogus_gpu_solve_admm", "bogus_gpu_adjoint_options_default",
+    "bogus_gpu_adjoint", "bogus_gpu_adjoint_device", "bogus_gpu_adjoint_dual_lower", "bogus_gpu_adjoint_primal",
+    "bogus_gpu_add_compliance",
 ]
 
 
@@ -111,6 +117,15 @@ def lib():
     L.bogus_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.bogus_gpu_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.bogus_gpu_set_batch.argtypes = [vp, C.c_int, _ip]
+    L.bogus_gpu_adjoint_options_default.argtypes = [C.POINTER(AdjointOptions)]
+    L.bogus_gpu_adjoint_options_default.restype = None
+    L.bogus_gpu_adjoint.argtypes = [vp, C.POINTER(AdjointOptions), _dp, _dp, _dp, _dp, C.POINTER(C.c_double),
+                                    C.POINTER(C.c_uint)]
+    L.bogus_gpu_adjoint_device.argtypes = [vp, C.POINTER(AdjointOptions), vp, vp, vp, vp, C.POINTER(C.c_double),
+                                           C.POINTER(C.c_uint)]
+    L.bogus_gpu_adjoint_dual_lower.argtypes = [vp, _dp]
+    L.bogus_gpu_adjoint_primal.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.bogus_gpu_add_compliance.argtypes = [vp, _dp]
     L.bogus_gpu_admm_options_default.argtypes = [C.POINTER(AdmmOptions)]
     L.bogus_gpu_admm_options_default.restype = None
     L.bogus_gpu_solve_admm.argtypes = [vp, C.POINTER(AdmmOptions), C.c_double, vp, vp, _dp, _dp, _dp, _dp,
@@ -446,6 +461,49 @@ class DualFrictionProblem:
         _check(lib().bogus_gpu_eval(self._h, _f64(r).reshape(-1), int(sp), int(solver.usesInfinityNorm()),
                                     C.byref(res)), False)
         return res.value
+
+    # ---- adjoint of the SOC solve (no counterpart in the reference) ----
+    def adjoint(self, r, dL_dr, tol: float = 1e-10, max_iters: int = 5000):
+        """Implicit-function gradients at the SOC solution r: returns (dL/db [3n], dL/dmu [n]); the final relative
+        residual of the linear solve is in self.last_adjoint_residual."""
+        o = AdjointOptions()
+        lib().bogus_gpu_adjoint_options_default(C.byref(o))
+        o.tol, o.max_iters = float(tol), int(max_iters)
+        db = np.zeros(3 * self.n)
+        dmu = np.zeros(self.n)
+        res = C.c_double()
+        it = C.c_uint()
+        st = lib().bogus_gpu_adjoint(self._h, C.byref(o), _f64(r).reshape(-1), _f64(dL_dr).reshape(-1), db, dmu,
+                                     C.byref(res), C.byref(it))
+        _check(st)
+        self.last_adjoint_residual, self.last_adjoint_iterations = res.value, it.value
+        return db, dmu
+
+    def adjoint_dual_lower(self) -> np.ndarray:
+        """dL/dW for the stored lower blocks of the last adjoint, [nnzb_lower, 3, 3]."""
+        nnz = C.c_int()
+        _check(lib().bogus_gpu_get_dual_lower(self._h, None, None, None, C.byref(nnz)), False)
+        out = np.zeros(9 * nnz.value)
+        _check(lib().bogus_gpu_adjoint_dual_lower(self._h, out), False)
+        return out.reshape(-1, 3, 3)
+
+    def adjoint_primal(self, primal: "PrimalFrictionProblem"):
+        """dL/dHA, dL/dHB, dL/dw, dL/df of the last adjoint, for W and b assembled from `primal`."""
+        n, nb, d = primal.objA.size, primal.minv.shape[0], primal.minv.shape[1]
+        dHA = np.zeros((n, 3, d))
+        dHB = np.zeros((n, 3, d))
+        dw = np.zeros(3 * n)
+        df = np.zeros(nb * d)
+        fptr = None if primal.f is None else primal.f.ctypes.data_as(C.c_void_p)
+        _check(lib().bogus_gpu_adjoint_primal(self._h, fptr, dHA.ctypes.data_as(C.c_void_p),
+                                              dHB.ctypes.data_as(C.c_void_p), dw.ctypes.data_as(C.c_void_p),
+                                              df.ctypes.data_as(C.c_void_p)), False)
+        return dHA, dHB, dw, df
+
+    def add_compliance(self, c) -> None:
+        """W_ii += c_i I (c: one value per contact, or a scalar)."""
+        c = np.broadcast_to(_f64(c), (self.n,)).copy()
+        _check(lib().bogus_gpu_add_compliance(self._h, c), False)
 
     def coloring(self):
         perm = np.zeros(self.n, np.int32)

@@ -18,7 +18,7 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "bogus_gpu", "_lib")
 LIB = os.path.join(LIBDIR, "libbogus_gpu.so")
 SOURCES = ["bogus_api.cu", "kernels_basic.cu", "kernels_pg.cu", "kernels_gs.cu", "kernels_assembly.cu",
-           "noalloc_pg.cu", "kernels_admm.cu"]
+           "noalloc_pg.cu", "kernels_admm.cu", "kernels_adjoint.cu", "kernels_grad.cu"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

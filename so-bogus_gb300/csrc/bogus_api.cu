@@ -137,13 +137,18 @@ struct bogus_gpu_problem {
   int nbodies = 0, ndof = 0, ncontacts = 0;
   DevBuf<double> minv, H, T, mf;
   DevBuf<int> cb;  // per contact: body of slot 0, body of slot 1 (-1), slot order by body index
-  std::vector<int> h_cb;
+  std::vector<int> h_cb, h_objA;
   // ADMM: body -> (contact, slot) incidences in increasing contact order, per-call data and work
   bool admm_incidence_valid = false;
   size_t admm_ninc = 0;
   DevBuf<int> bptr, bent;
   DevBuf<double> a_prox, a_f, a_w, a_mu, a_invmu, a_x, a_r, a_ut, a_z, a_zacc, a_zprev, a_yprev;
   DevBuf<ADMMOut> admm_out;
+  // adjoint: per-contact basis, CG vectors, the last solution r and s = dL/db (device and host copies)
+  DevBuf<double> adj_V, adj_D, adj_K, adj_P, adj_R, adj_Dir, adj_Y, adj_Q, adj_S, adj_dmu, adj_r, adj_g;
+  DevBuf<AdjOut> adj_out;
+  bool adj_valid = false;
+  std::vector<double> h_adj_s, h_adj_r;
   // batch partition (block-diagonal W)
   int nproblems = 0;
   std::vector<int> h_contact_ptr, h_problem_nnz;
@@ -201,6 +206,7 @@ int upload_full(bogus_gpu_problem* h, const HostBSR& f, const double* b, const d
   h->gs.valid = false;
   h->nproblems = 0;
   h->fp32_valid = false;
+  h->adj_valid = false;
   return BOGUS_GPU_OK;
 }
 
@@ -684,6 +690,10 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   h->bptr.release();
   h->bent.release();
   h->admm_out.release();
+  for (auto* b : {&h->adj_V, &h->adj_D, &h->adj_K, &h->adj_P, &h->adj_R, &h->adj_Dir, &h->adj_Y, &h->adj_Q,
+                  &h->adj_S, &h->adj_dmu, &h->adj_r, &h->adj_g})
+    b->release();
+  h->adj_out.release();
   h->rowptr.release();
   h->col.release();
   h->diag.release();
@@ -770,6 +780,7 @@ int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* 
   h->gs.valid = false;
   h->nproblems = 0;
   h->fp32_valid = false;
+  h->adj_valid = false;
   return BOGUS_GPU_OK;
 }
 
@@ -1062,7 +1073,301 @@ int bogus_gpu_set_primal(bogus_gpu_problem* h, int nbodies, int ndof, const doub
   h->ndof = ndof;
   h->ncontacts = ncontacts;
   h->h_cb = std::move(cbh);
+  h->h_objA.assign(objA, objA + ncontacts);
   h->admm_incidence_valid = false;
+  return BOGUS_GPU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Body -> (contact, slot) incidences in increasing contact order (ADMM's H^T products, the adjoint's
+// primal gradients), built once per primal problem.
+int ensure_incidence(bogus_gpu_problem* h) {
+  if (h->admm_incidence_valid) return BOGUS_GPU_OK;
+  const int n = h->ncontacts, nb = h->nbodies;
+  cudaStream_t s = h->stream;
+  std::vector<int> bp(nb + 1, 0), be;
+  for (int i = 0; i < n; ++i)
+    for (int t = 0; t < 2; ++t)
+      if (h->h_cb[2 * (size_t)i + t] >= 0) ++bp[h->h_cb[2 * (size_t)i + t] + 1];
+  for (int k = 0; k < nb; ++k) bp[k + 1] += bp[k];
+  be.resize(bp[nb] > 0 ? bp[nb] : 1);
+  std::vector<int> fill(bp.begin(), bp.end() - 1);
+  for (int i = 0; i < n; ++i)  // increasing contact index within each body
+    for (int t = 0; t < 2; ++t) {
+      const int k = h->h_cb[2 * (size_t)i + t];
+      if (k >= 0) be[fill[k]++] = 2 * i + t;
+    }
+  BG_CUDA(h->bptr.ensure(nb + 1));
+  BG_CUDA(h->bent.ensure(be.size()));
+  BG_CUDA(cudaMemcpyAsync(h->bptr.p, bp.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(h->bent.p, be.data(), sizeof(int) * be.size(), cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  h->admm_ninc = (size_t)bp[nb];
+  h->admm_incidence_valid = true;
+  return BOGUS_GPU_OK;
+}
+
+// Runs the adjoint kernel with r and g already in adj_r / adj_g; leaves s and dL/dmu in adj_S / adj_dmu.
+int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double* residual, unsigned* iters) {
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n > 0 ? 3 * (size_t)n : 1;
+  cudaStream_t s = h->stream;
+  BG_CUDA(h->adj_V.ensure(3 * n3));
+  for (auto* b : {&h->adj_D, &h->adj_K, &h->adj_P, &h->adj_R, &h->adj_Dir, &h->adj_Y, &h->adj_Q, &h->adj_S})
+    BG_CUDA(b->ensure(n3));
+  BG_CUDA(h->adj_dmu.ensure(n > 0 ? n : 1));
+  BG_CUDA(h->adj_out.ensure(1));
+  const int C = (n + 31) / 32;
+  BG_CUDA(h->csum.ensure(4 * (size_t)(C > 0 ? C : 1)));
+  BG_CUDA(h->scal.ensure(8));
+  BG_CUDA(h->barrier.ensure(4));
+  BG_CUDA(h->status.ensure(1));
+  AdjArgs a{};
+  a.n = n;
+  a.nchunks = C;
+  a.rowptr = h->W.rowptr;
+  a.col = h->W.col;
+  a.val = h->W.val;
+  a.b = h->b.p;
+  a.mu = h->mu.p;
+  a.scaling = h->scaling.p;
+  a.r = h->adj_r.p;
+  a.g = h->adj_g.p;
+  a.V = h->adj_V.p;
+  a.D = h->adj_D.p;
+  a.K = h->adj_K.p;
+  a.P = h->adj_P.p;
+  a.R = h->adj_R.p;
+  a.Dir = h->adj_Dir.p;
+  a.Y = h->adj_Y.p;
+  a.Q = h->adj_Q.p;
+  a.S = h->adj_S.p;
+  a.dmu = h->adj_dmu.p;
+  a.csum = h->csum.p;
+  a.scal = h->scal.p;
+  a.out = h->adj_out.p;
+  a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.tol = o->tol;
+  a.max_iters = o->max_iters;
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), s));
+  BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
+  int grid = adjoint_max_grid(h->device);
+  if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
+  const int want = (C + 7) / 8;
+  if (want < grid) grid = want < 1 ? 1 : want;
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  BG_CUDA(launch_adjoint(a, grid, s));
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  AdjOut out{};
+  int st = 0;
+  BG_CUDA(cudaMemcpyAsync(&out, h->adj_out.p, sizeof(AdjOut), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaMemcpyAsync(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  h->last_launches = 1;
+  if (st != 0) return fail(st, "device-side wait timed out in the adjoint kernel");
+  // per CG iteration: one W pass, the basis (9 values), D, dir, Q, P, R, Y streams
+  const double wpass = (double)h->W.nnzb * 76.0 + 4.0 * (n + 1);
+  h->last_stats.iterations = out.iters;
+  h->last_stats.refine_iterations = 0;
+  h->last_stats.fp32_device_ms = 0.0;
+  h->last_stats.w_passes = out.iters + 2;
+  h->last_stats.algorithmic_bytes = (out.iters + 2) * wpass + (double)out.iters * n * 8.0 * (9 + 3 * 12);
+  h->last_stats.fp64_fma = (out.iters + 2) * 9.0 * (double)h->W.nnzb;
+  h->adj_valid = true;
+  if (residual) *residual = out.rel_res;
+  if (iters) *iters = out.iters;
+  const bool ok = n == 0 || out.rel_res <= o->tol;
+  return ok ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
+}
+
+int adjoint_checks(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o) {
+  if (int e = check_handle(h)) return e;
+  if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
+  if (!(o->tol >= 0)) return fail(BOGUS_GPU_BAD_INPUT, "invalid tolerance");
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  return set_device(h);
+}
+
+}  // namespace
+
+extern "C" {
+
+void bogus_gpu_adjoint_options_default(bogus_gpu_adjoint_options* o) {
+  if (!o) return;
+  o->tol = 1e-10;
+  o->max_iters = 5000;
+}
+
+int bogus_gpu_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, const double* r,
+                      const double* dL_dr, double* dL_db, double* dL_dmu, double* residual, unsigned* iters) {
+  if (int e = adjoint_checks(h, o)) return e;
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  if (n > 0 && (!r || !dL_dr)) return fail(BOGUS_GPU_BAD_INPUT, "null r or dL_dr");
+  if (int e = check_finite(r, n3, "r")) return e;
+  if (int e = check_finite(dL_dr, n3, "dL_dr")) return e;
+  BG_CUDA(h->adj_r.ensure(n3 > 0 ? n3 : 1));
+  BG_CUDA(h->adj_g.ensure(n3 > 0 ? n3 : 1));
+  if (n > 0) {
+    BG_CUDA(cudaMemcpyAsync(h->adj_r.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, h->stream));
+    BG_CUDA(cudaMemcpyAsync(h->adj_g.p, dL_dr, sizeof(double) * n3, cudaMemcpyHostToDevice, h->stream));
+  }
+  const int st = run_adjoint(h, o, residual, iters);
+  if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+  h->h_adj_s.resize(n3);
+  h->h_adj_r.assign(r, r + n3);
+  if (n > 0) {
+    BG_CUDA(cudaMemcpy(h->h_adj_s.data(), h->adj_S.p, sizeof(double) * n3, cudaMemcpyDeviceToHost));
+    if (dL_dmu) BG_CUDA(cudaMemcpy(dL_dmu, h->adj_dmu.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    if (dL_db) std::memcpy(dL_db, h->h_adj_s.data(), sizeof(double) * n3);
+  }
+  return st;
+}
+
+int bogus_gpu_adjoint_device(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, const double* d_r,
+                             const double* d_g, double* d_dL_db, double* d_dL_dmu, double* residual,
+                             unsigned* iters) {
+  if (int e = adjoint_checks(h, o)) return e;
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  if (n > 0 && (!d_r || !d_g)) return fail(BOGUS_GPU_BAD_INPUT, "null r or dL_dr");
+  BG_CUDA(h->adj_r.ensure(n3 > 0 ? n3 : 1));
+  BG_CUDA(h->adj_g.ensure(n3 > 0 ? n3 : 1));
+  if (n > 0) {
+    BG_CUDA(cudaMemcpyAsync(h->adj_r.p, d_r, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    BG_CUDA(cudaMemcpyAsync(h->adj_g.p, d_g, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  const int st = run_adjoint(h, o, residual, iters);
+  if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+  h->h_adj_s.clear();
+  h->h_adj_r.clear();
+  if (n > 0) {
+    if (d_dL_db)
+      BG_CUDA(cudaMemcpyAsync(d_dL_db, h->adj_S.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    if (d_dL_dmu)
+      BG_CUDA(cudaMemcpyAsync(d_dL_dmu, h->adj_dmu.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+    BG_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  return st;
+}
+
+int bogus_gpu_adjoint_dual_lower(bogus_gpu_problem* h, double* dW) {
+  if (int e = check_handle(h)) return e;
+  if (!h->adj_valid) return fail(BOGUS_GPU_NO_PROBLEM, "no adjoint computed (bogus_gpu_adjoint)");
+  if (!h->host_lower_valid) return fail(BOGUS_GPU_NO_PROBLEM, "no host copy of W");
+  if (!dW) return fail(BOGUS_GPU_BAD_INPUT, "null output");
+  const HostBSR& l = h->host_lower;
+  const size_t n3 = 3 * (size_t)l.n;
+  if (h->h_adj_s.size() != n3 || h->h_adj_r.size() != n3) {
+    if (int e = set_device(h)) return e;
+    h->h_adj_s.resize(n3);
+    h->h_adj_r.resize(n3);
+    if (n3) {
+      BG_CUDA(cudaMemcpy(h->h_adj_s.data(), h->adj_S.p, sizeof(double) * n3, cudaMemcpyDeviceToHost));
+      BG_CUDA(cudaMemcpy(h->h_adj_r.data(), h->adj_r.p, sizeof(double) * n3, cudaMemcpyDeviceToHost));
+    }
+  }
+  const double* sv = h->h_adj_s.data();
+  const double* rv = h->h_adj_r.data();
+  for (int i = 0; i < l.n; ++i)
+    for (int k = l.rowptr[i]; k < l.rowptr[i + 1]; ++k) {
+      const int j = l.col[k];
+      double* G = dW + 9 * (size_t)k;
+      for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c)
+          G[3 * a + c] = sv[3 * i + a] * rv[3 * j + c] + (i != j ? rv[3 * i + a] * sv[3 * j + c] : 0.0);
+    }
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_adjoint_primal(bogus_gpu_problem* h, const double* f, double* dHA, double* dHB, double* dw,
+                             double* df) {
+  if (int e = check_handle(h)) return e;
+  if (!h->adj_valid) return fail(BOGUS_GPU_NO_PROBLEM, "no adjoint computed (bogus_gpu_adjoint)");
+  if (h->nbodies == 0 || h->ncontacts != h->W.n)
+    return fail(BOGUS_GPU_NO_PROBLEM, "the dual problem was not assembled from the handle's primal data");
+  if (int e = set_device(h)) return e;
+  const int n = h->ncontacts, nb = h->nbodies, d = h->ndof;
+  const size_t m = (size_t)nb * d, n3 = 3 * (size_t)n, hs = 3 * (size_t)d;
+  if (f)
+    if (int e = check_finite(f, m, "f")) return e;
+  if (int e = ensure_incidence(h)) return e;
+  cudaStream_t s = h->stream;
+  DevBuf<double> fd, vr, vs, dH;
+  BG_CUDA(vr.ensure(m));
+  BG_CUDA(vs.ensure(m));
+  BG_CUDA(dH.ensure(2 * n3 * d > 0 ? 2 * n3 * d : 1));
+  if (f) {
+    BG_CUDA(fd.ensure(m));
+    BG_CUDA(cudaMemcpyAsync(fd.p, f, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  }
+  BG_CUDA(launch_body_transpose(nb, d, h->bptr.p, h->bent.p, h->H.p, h->minv.p, h->adj_r.p, f ? fd.p : nullptr,
+                                vr.p, s));
+  BG_CUDA(launch_body_transpose(nb, d, h->bptr.p, h->bent.p, h->H.p, h->minv.p, h->adj_S.p, nullptr, vs.p, s));
+  BG_CUDA(launch_h_gradient(n, d, h->cb.p, h->adj_S.p, h->adj_r.p, vr.p, vs.p, dH.p, s));
+  std::vector<double> slots(2 * n3 * d);
+  std::vector<double> vsh(m);
+  if (n) BG_CUDA(cudaMemcpyAsync(slots.data(), dH.p, sizeof(double) * slots.size(), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaMemcpyAsync(vsh.data(), vs.p, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+  std::vector<double> sh(n3);
+  if (n) BG_CUDA(cudaMemcpyAsync(sh.data(), h->adj_S.p, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < n; ++i) {
+    // slots are ordered by body index; map them back to A and B
+    const int s0 = h->h_cb[2 * (size_t)i], s1 = h->h_cb[2 * (size_t)i + 1];
+    const double* g0 = &slots[(2 * (size_t)i) * hs];
+    const double* g1 = &slots[(2 * (size_t)i + 1) * hs];
+    const bool b_first = s1 >= 0 && s0 != h->h_objA[i];
+    double* A = dHA ? dHA + (size_t)i * hs : nullptr;
+    double* B = dHB ? dHB + (size_t)i * hs : nullptr;
+    for (size_t k = 0; k < hs; ++k) {
+      if (A) A[k] = b_first ? g1[k] : g0[k];
+      if (B) B[k] = s1 < 0 ? 0.0 : (b_first ? g0[k] : g1[k]);
+    }
+  }
+  if (dw) std::memcpy(dw, sh.data(), sizeof(double) * n3);
+  if (df)
+    for (size_t k = 0; k < m; ++k) df[k] = -vsh[k];
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_add_compliance(bogus_gpu_problem* h, const double* c) {
+  if (int e = check_handle(h)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  const int n = h->W.n;
+  if (n > 0 && !c) return fail(BOGUS_GPU_BAD_INPUT, "null compliance");
+  for (int i = 0; i < n; ++i)
+    if (!(c[i] >= 0) || !std::isfinite(c[i])) return fail(BOGUS_GPU_BAD_INPUT, "compliance must be finite and >= 0");
+  if (int e = set_device(h)) return e;
+  {
+    std::vector<int> dg(n);
+    if (n) BG_CUDA(cudaMemcpy(dg.data(), h->W.diag, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i)
+      if (dg[i] < 0) return fail(BOGUS_GPU_BAD_INPUT, "W has no diagonal block at some contact");
+  }
+  DevBuf<double> dc;
+  BG_CUDA(dc.ensure(n > 0 ? n : 1));
+  if (n) BG_CUDA(cudaMemcpyAsync(dc.p, c, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  BG_CUDA(launch_add_diagonal(h->W, dc.p, h->stream));
+  BG_CUDA(launch_diag_and_scaling(h->W, h->scaling.p, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->host_lower_valid) {
+    HostBSR& l = h->host_lower;
+    for (int i = 0; i < n; ++i) {
+      const int k = l.rowptr[i + 1] - 1;  // the diagonal block ends a lower row
+      double* B = &l.val[9 * (size_t)k];
+      B[0] = B[0] + c[i];
+      B[4] = B[4] + c[i];
+      B[8] = B[8] + c[i];
+    }
+  }
+  h->gs.valid = false;
+  h->fp32_valid = false;
+  h->adj_valid = false;
   return BOGUS_GPU_OK;
 }
 
@@ -1098,26 +1403,8 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
     if (int e = check_finite(prox, m * d, "prox")) return e;
   if (int e = set_device(h)) return e;
   cudaStream_t s = h->stream;
-  if (!h->admm_incidence_valid) {
-    std::vector<int> bp(nb + 1, 0), be;
-    for (int i = 0; i < n; ++i)
-      for (int t = 0; t < 2; ++t)
-        if (h->h_cb[2 * (size_t)i + t] >= 0) ++bp[h->h_cb[2 * (size_t)i + t] + 1];
-    for (int k = 0; k < nb; ++k) bp[k + 1] += bp[k];
-    be.resize(bp[nb] > 0 ? bp[nb] : 1);
-    std::vector<int> fill(bp.begin(), bp.end() - 1);
-    for (int i = 0; i < n; ++i)  // increasing contact index within each body
-      for (int t = 0; t < 2; ++t) {
-        const int k = h->h_cb[2 * (size_t)i + t];
-        if (k >= 0) be[fill[k]++] = 2 * i + t;
-      }
-    BG_CUDA(h->bptr.ensure(nb + 1));
-    BG_CUDA(h->bent.ensure(be.size()));
-    BG_CUDA(cudaMemcpyAsync(h->bptr.p, bp.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, s));
-    BG_CUDA(cudaMemcpyAsync(h->bent.p, be.data(), sizeof(int) * be.size(), cudaMemcpyHostToDevice, s));
-    BG_CUDA(cudaStreamSynchronize(s));
-    h->admm_ninc = (size_t)bp[nb];
-    h->admm_incidence_valid = true;
+  if (int e = ensure_incidence(h)) return e;
+  {
   }
   const size_t nv = n3 > 0 ? n3 : 1;
   for (auto* b : {&h->a_w, &h->a_r, &h->a_ut, &h->a_z, &h->a_zacc, &h->a_zprev, &h->a_yprev}) BG_CUDA(b->ensure(nv));
@@ -1357,6 +1644,7 @@ int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double*
   h->gs.valid = false;
   h->nproblems = 0;
   h->fp32_valid = false;
+  h->adj_valid = false;
   return BOGUS_GPU_OK;
 }
 

@@ -160,6 +160,42 @@ struct ADMMArgs {
 cudaError_t launch_admm(const ADMMArgs& a, int grid, cudaStream_t s);
 int admm_max_grid(int device, int d);
 
+// Adjoint of the SOC solve (kernels_adjoint.cu).
+struct AdjOut {
+  unsigned iters;
+  double rel_res;
+};
+struct AdjArgs {
+  int n, nchunks;
+  const int* rowptr;
+  const int* col;
+  const double* val;   // W, both triangles
+  const double* b;
+  const double* mu;
+  const double* scaling;  // per-contact fixed-point step 1 / scaling_i
+  const double* r;     // the solution
+  const double* g;     // dL/dr
+  double *V, *D, *K;   // per contact basis (9), diagonal term (3, negative: masked), dP/dmu (3)
+  double *P, *R, *Dir, *Y, *Q;  // conjugate-gradient vectors (3 per contact)
+  double* S;           // out: dL/db
+  double* dmu;         // out: dL/dmu
+  double* csum;
+  double* scal;
+  AdjOut* out;
+  GridBarrier gb;
+  double tol;
+  unsigned max_iters;
+};
+cudaError_t launch_adjoint(const AdjArgs& a, int grid, cudaStream_t s);
+int adjoint_max_grid(int device);
+// Helpers of the primal gradients and of the compliance term (kernels_grad.cu)
+cudaError_t launch_body_transpose(int nbodies, int d, const int* bptr, const int* bent, const double* H,
+                                  const double* minv, const double* vec, const double* f, double* out,
+                                  cudaStream_t s);
+cudaError_t launch_h_gradient(int n, int d, const int* cb, const double* s, const double* r, const double* vr,
+                              const double* vs, double* dH, cudaStream_t st);
+cudaError_t launch_add_diagonal(const DevBSR& W, const double* c, cudaStream_t s);
+
 // Records the message returned by bogus_gpu_last_error() on this thread.
 void set_last_error(const std::string& msg);
 

@@ -1,0 +1,278 @@
+// Adjoint of the SOC friction solve (no counterpart in the reference, which has no differentiation).
+//
+// r solves min 1/2 r^T W r + b^T r over r_i in K_mu_i (SOCLaw<3>, the problem ProjectedGradient solves with
+// staticProblem), i.e. the fixed point r = P(x), x = r - A (W r + b) for any positive diagonal step A (here
+// alpha_i = 1 / scaling_i, the diagonal scalings of ConstrainedSolverBase; the gradient does not depend on the
+// choice). With J = dP/dx(x) (block diagonal, symmetric) the adjoint system is (I - J + W A J) lam = g
+// (g = dL/dr). Per contact
+// J = V diag(theta) V^T in closed form:
+//   interior (|x_T| <= mu x_N):      V = I, theta = (1, 1, 1)
+//   polar (mu |x_T| <= -x_N, mu < 0): theta = (0, 0, 0)
+//   boundary, c = 1 / (1 + mu^2), u = x_T / |x_T|, p_N = c (x_N + mu |x_T|):
+//     v1 = sqrt(c) (1, mu u), theta 1;  v2 = (0, u_perp), theta = mu p_N / |x_T|;  v3 = sqrt(c) (-mu, u), theta 0.
+// Writing lam in the V basis, the components with theta = 0 ("masked") decouple and the others, scaled as
+// p = alpha theta lam_hat, solve the symmetric positive definite system
+//   S p = D p + M V^T W V M p = M V^T g,   D = (1 / theta - 1) / alpha,  M = the unmasked components,
+// by conjugate gradients (one pass over W per iteration). Then
+//   dL/db = s = -V M p,   lam_hat (masked) = v_k^T (g + W s),   lam_hat (unmasked) = p_k / (alpha theta_k),
+//   dL/dmu_i = K_i^T V_i lam_hat_i with K = dP/dmu(x).
+// A persistent cooperative kernel runs the setup, the CG iterations and the final pass; reductions use the
+// canonical order of the solver kernels, waits are bounded (grid_barrier).
+#include "internal.h"
+#include "soc_device.cuh"
+#include "spmv_chunk.cuh"
+
+namespace bogus_gpu {
+
+namespace {
+
+__device__ __forceinline__ void ld3(const double* p, int i, double* v) {
+  v[0] = ldcg(p + 3 * i);
+  v[1] = ldcg(p + 3 * i + 1);
+  v[2] = ldcg(p + 3 * i + 2);
+}
+__device__ __forceinline__ void st3(double* p, int i, const double* v) {
+  p[3 * i] = v[0];
+  p[3 * i + 1] = v[1];
+  p[3 * i + 2] = v[2];
+}
+
+// Closed-form eigenbasis of the projection Jacobian at x: V (row-major 3x3, columns v1 v2 v3), D (negative
+// for a masked component) and K = dP/dmu.
+__device__ void projection_basis(double mu, const double* x, double alpha, double* V, double* D, double* K) {
+  const double xn = x[0];
+  const double t = sqrt(x[1] * x[1] + x[2] * x[2]);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) V[k] = (k % 4 == 0) ? 1.0 : 0.0;
+  K[0] = K[1] = K[2] = 0.0;
+  if (mu < 0.0 || mu * t <= -xn) {  // polar cone: J = 0
+    D[0] = D[1] = D[2] = -1.0;
+    return;
+  }
+  if (t <= mu * xn) {  // interior: J = I
+    D[0] = D[1] = D[2] = 0.0;
+    return;
+  }
+  const double c = 1.0 / (1.0 + mu * mu);
+  const double sc = sqrt(c);
+  const double u1 = x[1] / t, u2 = x[2] / t;
+  const double pn = (xn + mu * t) * c;
+  // columns: v1 = sc (1, mu u), v2 = (0, -u2, u1), v3 = sc (-mu, u)
+  V[0] = sc;          V[1] = 0.0;  V[2] = -mu * sc;
+  V[3] = sc * mu * u1; V[4] = -u2; V[5] = sc * u1;
+  V[6] = sc * mu * u2; V[7] = u1;  V[8] = sc * u2;
+  const double rho = mu * pn / t;
+  D[0] = 0.0;
+  D[1] = rho > 0.0 ? (1.0 / rho - 1.0) / alpha : -1.0;
+  D[2] = -1.0;
+  const double dpn = t * c - 2.0 * mu * (xn + mu * t) * c * c;
+  const double kt = pn + mu * dpn;
+  K[0] = dpn;
+  K[1] = kt * u1;
+  K[2] = kt * u2;
+}
+
+// y = V (m o p)
+__device__ __forceinline__ void basis_apply(const double* V, const double* D, const double* p, double* y) {
+  double q[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) q[k] = D[k] < 0.0 ? 0.0 : p[k];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) y[r] = V[3 * r] * q[0] + V[3 * r + 1] * q[1] + V[3 * r + 2] * q[2];
+}
+// p = m o (V^T y)
+__device__ __forceinline__ void basis_apply_t(const double* V, const double* D, const double* y, double* p) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double v = V[k] * y[0] + V[3 + k] * y[1] + V[6 + k] * y[2];
+    p[k] = D[k] < 0.0 ? 0.0 : v;
+  }
+}
+
+struct AdjCtx {
+  const AdjArgs& a;
+  double* smem8;
+  __device__ bool sync() { return grid_barrier(a.gb, [] {}); }
+  __device__ bool sync_reduce(int K) {
+    return grid_barrier(a.gb, [&] {
+      for (int q = 0; q < K; ++q) {
+        const double v = block8_combine(a.csum + q * a.nchunks, a.nchunks, false, smem8);
+        if (threadIdx.x == 0) a.scal[q] = v;
+      }
+    });
+  }
+};
+
+__global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
+  __shared__ double smem8[8];
+  __shared__ ChunkScratch cs[8];
+  AdjCtx ctx{a, smem8};
+  ChunkScratch& sh = cs[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  const int C = a.nchunks;
+  const bool writer = blockIdx.x == 0 && threadIdx.x == 0;
+  auto put = [&](int q, int c, double v) {
+    v = warp_sum_butterfly(v);
+    if (lane == 0) a.csum[q * C + c] = v;
+  };
+  auto product = [&](int c, const double* src, double* acc) {
+    spmv_chunk<1>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, double* x) { ld3(src, j, x); }, acc);
+  };
+
+  // setup: x = r - alpha (W r + b), the basis, rhs c = m o V^T g; p = 0, res = dir = c, Y = V (m o c)
+  for (int c = gwarp; c < C; c += nwarps) {
+    const int i = 32 * c + lane;
+    double acc[3] = {0.0, 0.0, 0.0};
+    product(c, a.r, acc);
+    double rr = 0.0;
+    if (i < a.n) {
+      double r[3], x[3], V[9], D[3], K[3], g[3], cv[3], y[3];
+      ld3(a.r, i, r);
+      const double al = 1.0 / __ldg(a.scaling + i);
+      for (int k = 0; k < 3; ++k) x[k] = r[k] - al * (acc[k] + __ldg(a.b + 3 * i + k));
+      projection_basis(__ldg(a.mu + i), x, al, V, D, K);
+      for (int k = 0; k < 9; ++k) a.V[9 * (size_t)i + k] = V[k];
+      st3(a.D, i, D);
+      st3(a.K, i, K);
+      ld3(a.g, i, g);
+      basis_apply_t(V, D, g, cv);
+      const double z[3] = {0.0, 0.0, 0.0};
+      st3(a.P, i, z);
+      st3(a.R, i, cv);
+      st3(a.Dir, i, cv);
+      basis_apply(V, D, cv, y);
+      st3(a.Y, i, y);
+      rr = cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2];
+    }
+    put(0, c, rr);
+  }
+  if (!ctx.sync_reduce(1)) return;
+  const double rr0 = ldcg(a.scal);
+  double rr = rr0;
+  unsigned it = 0;
+  const double stop = a.tol * a.tol * rr0;
+  for (; it < a.max_iters; ++it) {
+    if (!(rr > stop)) break;
+    // q = D o dir + m o V^T W Y, dir . q
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      double acc[3] = {0.0, 0.0, 0.0};
+      product(c, a.Y, acc);
+      double dq = 0.0;
+      if (i < a.n) {
+        double V[9], D[3], d[3], t[3], q[3];
+        for (int k = 0; k < 9; ++k) V[k] = ldcg(a.V + 9 * (size_t)i + k);
+        ld3(a.D, i, D);
+        ld3(a.Dir, i, d);
+        basis_apply_t(V, D, acc, t);
+        for (int k = 0; k < 3; ++k) q[k] = (D[k] < 0.0 ? 0.0 : D[k] * d[k]) + t[k];
+        st3(a.Q, i, q);
+        dq = d[0] * q[0] + d[1] * q[1] + d[2] * q[2];
+      }
+      put(0, c, dq);
+    }
+    if (!ctx.sync_reduce(1)) return;
+    const double dq = ldcg(a.scal);
+    if (!(dq > 0.0)) break;  // S is positive definite on the unmasked components; guards exact convergence
+    const double step = rr / dq;
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      double v = 0.0;
+      if (i < a.n) {
+        double p[3], res[3], d[3], q[3];
+        ld3(a.P, i, p);
+        ld3(a.R, i, res);
+        ld3(a.Dir, i, d);
+        ld3(a.Q, i, q);
+        for (int k = 0; k < 3; ++k) {
+          p[k] = fma(step, d[k], p[k]);
+          res[k] = fma(-step, q[k], res[k]);
+        }
+        st3(a.P, i, p);
+        st3(a.R, i, res);
+        v = res[0] * res[0] + res[1] * res[1] + res[2] * res[2];
+      }
+      put(0, c, v);
+    }
+    if (!ctx.sync_reduce(1)) return;
+    const double rr_new = ldcg(a.scal);
+    const double beta = rr_new / rr;
+    rr = rr_new;
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      if (i < a.n) {
+        double V[9], D[3], res[3], d[3], y[3];
+        for (int k = 0; k < 9; ++k) V[k] = ldcg(a.V + 9 * (size_t)i + k);
+        ld3(a.D, i, D);
+        ld3(a.R, i, res);
+        ld3(a.Dir, i, d);
+        for (int k = 0; k < 3; ++k) d[k] = fma(beta, d[k], res[k]);
+        st3(a.Dir, i, d);
+        basis_apply(V, D, d, y);
+        st3(a.Y, i, y);
+      }
+    }
+    if (!ctx.sync()) return;
+  }
+  // s = dL/db = -V (m o p)
+  for (int c = gwarp; c < C; c += nwarps) {
+    const int i = 32 * c + lane;
+    if (i < a.n) {
+      double V[9], D[3], p[3], y[3];
+      for (int k = 0; k < 9; ++k) V[k] = ldcg(a.V + 9 * (size_t)i + k);
+      ld3(a.D, i, D);
+      ld3(a.P, i, p);
+      basis_apply(V, D, p, y);
+      const double s[3] = {-y[0], -y[1], -y[2]};
+      st3(a.S, i, s);
+    }
+  }
+  if (!ctx.sync()) return;
+  // lam_hat and dL/dmu = K^T V lam_hat
+  for (int c = gwarp; c < C; c += nwarps) {
+    const int i = 32 * c + lane;
+    double acc[3] = {0.0, 0.0, 0.0};
+    product(c, a.S, acc);
+    if (i < a.n) {
+      double V[9], D[3], p[3], g[3], K[3], e[3], lh[3];
+      for (int k = 0; k < 9; ++k) V[k] = ldcg(a.V + 9 * (size_t)i + k);
+      ld3(a.D, i, D);
+      ld3(a.P, i, p);
+      ld3(a.g, i, g);
+      ld3(a.K, i, K);
+      const double al = 1.0 / __ldg(a.scaling + i);
+      for (int k = 0; k < 3; ++k) e[k] = g[k] + acc[k];
+      for (int k = 0; k < 3; ++k) {
+        if (D[k] < 0.0) lh[k] = V[k] * e[0] + V[3 + k] * e[1] + V[6 + k] * e[2];
+        else lh[k] = p[k] * (1.0 + al * D[k]) / al;  // p / (alpha theta), theta = 1 / (1 + alpha D)
+      }
+      double dm = 0.0;
+      for (int r2 = 0; r2 < 3; ++r2) dm += K[r2] * (V[3 * r2] * lh[0] + V[3 * r2 + 1] * lh[1] + V[3 * r2 + 2] * lh[2]);
+      a.dmu[i] = dm;
+    }
+  }
+  if (writer) {
+    a.out->iters = it;
+    a.out->rel_res = rr0 > 0.0 ? sqrt(rr / rr0) : 0.0;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_adjoint(const AdjArgs& a, int grid, cudaStream_t s) {
+  AdjArgs copy = a;
+  void* args[] = {&copy};
+  return cudaLaunchCooperativeKernel((const void*)k_adjoint, dim3(grid), dim3(256), args, 0, s);
+}
+
+int adjoint_max_grid(int device) {
+  int sms = 0, per = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_adjoint, 256, 0) != cudaSuccess) return 0;
+  if (per > 2) per = 2;
+  return per * sms;
+}
+
+}  // namespace bogus_gpu
