@@ -33,6 +33,7 @@ sys.path[:0] = [os.path.join(REPO, "so-bogus_gb300")]
 
 TOL = 1e-6
 MAX_ITERS = 500
+MAX_ADJ_FWD_ITERS = 20000
 METRIC = "time-to-residual 1e-6 (ms), FP64 APGD, 200k contacts"
 WORKLOAD = "fp64_apgd_200k_contacts"
 
@@ -489,6 +490,49 @@ def run_admm(args) -> None:
         flush=True)
 
 
+def run_adjoint(args) -> None:
+    """Gradient workload: 64 problems x 20 000 contacts (bodies = contacts / 3, compliance 0.05 I), forward =
+    batched APGD with the SOC law to 1e-10 per problem, loss L = g . r with g ~ N(0, 1); backward = the adjoint
+    (dL/db, dL/dmu) over the whole batch, then dL/dH, dL/dw, dL/df. Reports t_adjoint / t_forward."""
+    import bogus_gpu
+    from bogus_gpu import generator
+
+    d, cptr = generator.adjoint_batch()
+    P = bogus_gpu.PrimalFrictionProblem(d.minv, d.objA, d.objB, d.HA, d.HB, d.b.reshape(-1), d.mu)
+    D = bogus_gpu.DualFrictionProblem(0)
+    D.computeFrom(P)
+    D.add_compliance(generator.ADJOINT_COMPLIANCE)
+    D.setBatch(cptr)
+    pg = bogus_gpu.ProjectedGradient()
+    pg.setTol(1e-10)
+    pg.setMaxIters(MAX_ADJ_FWD_ITERS)
+    g = np.random.default_rng(6).standard_normal(3 * d.n)
+    fwd, adj, prim = [], [], []
+    for k in range(args.warmup + args.steps):
+        r = np.zeros(3 * d.n)
+        res, its = D.solveBatchWith(pg, r)
+        tf = D.solve_stats()["device_ms"]
+        t0 = time.perf_counter()
+        db, dmu = D.adjoint(r, g, tol=1e-10)
+        ta = D.solve_stats()["device_ms"]
+        t1 = time.perf_counter()
+        D.adjoint_primal(P)
+        t2 = time.perf_counter()
+        if k >= args.warmup:
+            fwd.append(tf)
+            adj.append(ta)
+            prim.append((t2 - t1) * 1e3)
+    tf, ta = statistics.median(fwd), statistics.median(adj)
+    print(json.dumps({
+        "workload": "adjoint_64x20000_contacts", "problems": len(cptr) - 1, "contacts": d.n,
+        "compliance": generator.ADJOINT_COMPLIANCE, "forward_ms": tf, "forward_iterations_max": int(its.max()),
+        "forward_converged_fraction": float(np.mean(res < 1e-10)), "adjoint_ms": ta,
+        "adjoint_cg_iterations": D.last_adjoint_iterations, "adjoint_rel_residual": D.last_adjoint_residual,
+        "primal_gradients_wall_ms": statistics.median(prim), "t_adjoint_over_t_forward": ta / tf,
+        "timing": f"median of {args.steps} after {args.warmup} warm-up; device times (CUDA events) of the batched "
+                  "solve kernel and of the adjoint kernel"}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -498,8 +542,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", type=int, default=0,
                     help="run one solve capped at this many iterations and exit (for ncu captures)")
-    ap.add_argument("--workload", default="apgd", choices=["apgd", "batch", "gs", "mixed", "admm"],
-                    help="apgd: the benchmark line; batch / gs / mixed / admm: secondary measurements")
+    ap.add_argument("--workload", default="apgd", choices=["apgd", "batch", "gs", "mixed", "admm", "adjoint"],
+                    help="apgd: the benchmark line; batch / gs / mixed / admm / adjoint: secondary measurements")
     ap.add_argument("--profile-mixed", action="store_true",
                     help="with --profile: the FP32-refined solve (FP32 iterations, then 1 FP64 iteration)")
     args = ap.parse_args()
@@ -508,6 +552,9 @@ def main():
         return
     if args.workload == "admm":
         run_admm(args)
+        return
+    if args.workload == "adjoint":
+        run_adjoint(args)
         return
     if args.workload == "batch":
         run_batch(args)

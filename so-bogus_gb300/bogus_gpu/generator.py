@@ -173,6 +173,30 @@ def batch(nproblems: int = 4096, nmin: int = 16, nmax: int = 4096, seed: int = 4
     return PrimalData(minv, objA, objB, HA, HB, b, mu, seed, "batch"), contact_ptr
 
 
+def adjoint_batch(nproblems: int = 64, ncontacts: int = 20_000, seed: int = 5, ground_fraction: float = 0.1):
+    """Independent random-pairs problems of `ncontacts` contacts each with bodies = contacts / 3 (each body in
+    about 6 contacts), concatenated like batch(). With 3 n constraint rows on 2 n body dofs, H M^-1 H^T is
+    singular; the gradient workload adds a compliance term (ADJOINT_COMPLIANCE I) so that each solution is
+    unique and differentiable. Returns (PrimalData, contact_ptr)."""
+    parts, body_off = [], 0
+    for p in range(nproblems):
+        d = random_pairs(nbodies=max(2, ncontacts // 3), ncontacts=ncontacts, seed=seed * 100003 + p,
+                         ground_fraction=ground_fraction)
+        parts.append((d, body_off))
+        body_off += d.nbodies
+    minv = np.concatenate([d.minv for d, _ in parts])
+    objA = np.concatenate([d.objA + off for d, off in parts]).astype(np.int32)
+    objB = np.concatenate([np.where(d.objB >= 0, d.objB + off, -1) for d, off in parts]).astype(np.int32)
+    HA = np.concatenate([d.HA for d, _ in parts])
+    HB = np.concatenate([d.HB for d, _ in parts])
+    b = np.concatenate([d.b for d, _ in parts])
+    mu = np.concatenate([d.mu for d, _ in parts])
+    contact_ptr = (np.arange(nproblems + 1) * ncontacts).astype(np.int32)
+    return PrimalData(minv, objA, objB, HA, HB, b, mu, seed, "adjoint_batch"), contact_ptr
+
+
+ADJOINT_COMPLIANCE = 0.05
+
 CONFIGS = {
     "c1": dict(fn=random_pairs, kw=dict(nbodies=200, ncontacts=500, seed=0)),
     "c2": dict(fn=grid, kw=dict(nbodies=50_000, ncontacts=200_000, seed=1)),

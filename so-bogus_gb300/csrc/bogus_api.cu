@@ -145,7 +145,7 @@ struct bogus_gpu_problem {
   DevBuf<double> a_prox, a_f, a_w, a_mu, a_invmu, a_x, a_r, a_ut, a_z, a_zacc, a_zprev, a_yprev;
   DevBuf<ADMMOut> admm_out;
   // adjoint: per-contact basis, CG vectors, the last solution r and s = dL/db (device and host copies)
-  DevBuf<double> adj_V, adj_D, adj_K, adj_P, adj_R, adj_Dir, adj_Y, adj_Q, adj_S, adj_dmu, adj_r, adj_g;
+  DevBuf<double> adj_V, adj_Pc, adj_D, adj_K, adj_P, adj_R, adj_Z, adj_Dir, adj_Y, adj_Q, adj_S, adj_dmu, adj_r, adj_g;
   DevBuf<AdjOut> adj_out;
   bool adj_valid = false;
   std::vector<double> h_adj_s, h_adj_r;
@@ -690,8 +690,8 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   h->bptr.release();
   h->bent.release();
   h->admm_out.release();
-  for (auto* b : {&h->adj_V, &h->adj_D, &h->adj_K, &h->adj_P, &h->adj_R, &h->adj_Dir, &h->adj_Y, &h->adj_Q,
-                  &h->adj_S, &h->adj_dmu, &h->adj_r, &h->adj_g})
+  for (auto* b : {&h->adj_V, &h->adj_Pc, &h->adj_D, &h->adj_K, &h->adj_P, &h->adj_R, &h->adj_Z, &h->adj_Dir,
+                  &h->adj_Y, &h->adj_Q, &h->adj_S, &h->adj_dmu, &h->adj_r, &h->adj_g})
     b->release();
   h->adj_out.release();
   h->rowptr.release();
@@ -1116,7 +1116,9 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   const size_t n3 = 3 * (size_t)n > 0 ? 3 * (size_t)n : 1;
   cudaStream_t s = h->stream;
   BG_CUDA(h->adj_V.ensure(3 * n3));
-  for (auto* b : {&h->adj_D, &h->adj_K, &h->adj_P, &h->adj_R, &h->adj_Dir, &h->adj_Y, &h->adj_Q, &h->adj_S})
+  BG_CUDA(h->adj_Pc.ensure(3 * n3));
+  for (auto* b : {&h->adj_D, &h->adj_K, &h->adj_P, &h->adj_R, &h->adj_Z, &h->adj_Dir, &h->adj_Y, &h->adj_Q,
+                  &h->adj_S})
     BG_CUDA(b->ensure(n3));
   BG_CUDA(h->adj_dmu.ensure(n > 0 ? n : 1));
   BG_CUDA(h->adj_out.ensure(1));
@@ -1136,7 +1138,10 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   a.scaling = h->scaling.p;
   a.r = h->adj_r.p;
   a.g = h->adj_g.p;
+  a.diag = h->W.diag;
   a.V = h->adj_V.p;
+  a.Pc = h->adj_Pc.p;
+  a.Z = h->adj_Z.p;
   a.D = h->adj_D.p;
   a.K = h->adj_K.p;
   a.P = h->adj_P.p;
@@ -1175,7 +1180,9 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   h->last_stats.refine_iterations = 0;
   h->last_stats.fp32_device_ms = 0.0;
   h->last_stats.w_passes = out.iters + 2;
-  h->last_stats.algorithmic_bytes = (out.iters + 2) * wpass + (double)out.iters * n * 8.0 * (9 + 3 * 12);
+  // per iteration per contact: basis 9 x 2, preconditioner 9, D 3 x 2, vectors (dir, Y, Q, P, R, Z) 3 each,
+  // read and written as the phases need them (about 16 streams)
+  h->last_stats.algorithmic_bytes = (out.iters + 2) * wpass + (double)out.iters * n * 8.0 * (18 + 9 + 6 + 3 * 16);
   h->last_stats.fp64_fma = (out.iters + 2) * 9.0 * (double)h->W.nnzb;
   h->adj_valid = true;
   if (residual) *residual = out.rel_res;

@@ -175,8 +175,10 @@ struct AdjArgs {
   const double* scaling;  // per-contact fixed-point step 1 / scaling_i
   const double* r;     // the solution
   const double* g;     // dL/dr
+  const int* diag;     // position of each diagonal block
   double *V, *D, *K;   // per contact basis (9), diagonal term (3, negative: masked), dP/dmu (3)
-  double *P, *R, *Dir, *Y, *Q;  // conjugate-gradient vectors (3 per contact)
+  double* Pc;          // per contact inverse of the preconditioner block (9)
+  double *P, *R, *Z, *Dir, *Y, *Q;  // conjugate-gradient vectors (3 per contact)
   double* S;           // out: dL/db
   double* dmu;         // out: dL/dmu
   double* csum;

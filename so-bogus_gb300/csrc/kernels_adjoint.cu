@@ -13,7 +13,9 @@
 // Writing lam in the V basis, the components with theta = 0 ("masked") decouple and the others, scaled as
 // p = alpha theta lam_hat, solve the symmetric positive definite system
 //   S p = D p + M V^T W V M p = M V^T g,   D = (1 / theta - 1) / alpha,  M = the unmasked components,
-// by conjugate gradients (one pass over W per iteration). Then
+// by conjugate gradients (one pass over W per iteration) preconditioned with the inverse of S's 3 x 3
+// diagonal blocks diag(D_i) + V_i^T W_ii V_i (D grows without bound as theta -> 0 near a regime change, which
+// leaves plain CG unable to converge). Then
 //   dL/db = s = -V M p,   lam_hat (masked) = v_k^T (g + W s),   lam_hat (unmasked) = p_k / (alpha theta_k),
 //   dL/dmu_i = K_i^T V_i lam_hat_i with K = dP/dmu(x).
 // A persistent cooperative kernel runs the setup, the CG iterations and the final pass; reductions use the
@@ -72,6 +74,52 @@ __device__ void projection_basis(double mu, const double* x, double alpha, doubl
   K[2] = kt * u2;
 }
 
+// Inverse of the SPD block diag(D) + V^T Wii V restricted to the unmasked components (identity on the
+// masked ones), by Cholesky factorisation.
+__device__ void precond_block(const double* V, const double* D, const double* Wii, double* Pinv) {
+  double A[9];
+  double T[9];  // Wii V
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) T[3 * r + k] = Wii[3 * r] * V[k] + Wii[3 * r + 1] * V[3 + k] + Wii[3 * r + 2] * V[6 + k];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double v = V[j] * T[k] + V[3 + j] * T[3 + k] + V[6 + j] * T[6 + k];
+      const bool mj = D[j] < 0.0, mk = D[k] < 0.0;
+      A[3 * j + k] = (mj || mk) ? (j == k ? 1.0 : 0.0) : v + (j == k ? D[j] : 0.0);
+    }
+  // symmetrise (V^T Wii V is symmetric up to rounding), then Cholesky A = L L^T
+  const double a10 = 0.5 * (A[3] + A[1]), a20 = 0.5 * (A[6] + A[2]), a21 = 0.5 * (A[7] + A[5]);
+  const double l00 = sqrt(fmax(A[0], 1e-300));
+  const double l10 = a10 / l00, l20 = a20 / l00;
+  const double l11 = sqrt(fmax(A[4] - l10 * l10, 1e-300));
+  const double l21 = (a21 - l20 * l10) / l11;
+  const double l22 = sqrt(fmax(A[8] - l20 * l20 - l21 * l21, 1e-300));
+  // L^-1 (lower triangular)
+  const double i00 = 1.0 / l00, i11 = 1.0 / l11, i22 = 1.0 / l22;
+  const double i10 = -l10 * i00 * i11;
+  const double i21 = -l21 * i11 * i22;
+  const double i20 = -(l20 * i00 + l21 * i10) * i22;
+  // A^-1 = L^-T L^-1
+  Pinv[0] = i00 * i00 + i10 * i10 + i20 * i20;
+  Pinv[1] = i10 * i11 + i20 * i21;
+  Pinv[2] = i20 * i22;
+  Pinv[4] = i11 * i11 + i21 * i21;
+  Pinv[5] = i21 * i22;
+  Pinv[8] = i22 * i22;
+  Pinv[3] = Pinv[1];
+  Pinv[6] = Pinv[2];
+  Pinv[7] = Pinv[5];
+}
+
+__device__ __forceinline__ void mat3_apply(const double* M, const double* x, double* y) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r) y[r] = M[3 * r] * x[0] + M[3 * r + 1] * x[1] + M[3 * r + 2] * x[2];
+}
+
 // y = V (m o p)
 __device__ __forceinline__ void basis_apply(const double* V, const double* D, const double* p, double* y) {
   double q[3];
@@ -121,36 +169,47 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
     spmv_chunk<1>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, double* x) { ld3(src, j, x); }, acc);
   };
 
-  // setup: x = r - alpha (W r + b), the basis, rhs c = m o V^T g; p = 0, res = dir = c, Y = V (m o c)
+  // setup: x = r - alpha (W r + b), the basis, the preconditioner, rhs c = m o V^T g; p = 0, res = c,
+  // z = Pinv c, dir = z, Y = V (m o dir)
   for (int c = gwarp; c < C; c += nwarps) {
     const int i = 32 * c + lane;
     double acc[3] = {0.0, 0.0, 0.0};
     product(c, a.r, acc);
-    double rr = 0.0;
+    double rr = 0.0, rz = 0.0;
     if (i < a.n) {
-      double r[3], x[3], V[9], D[3], K[3], g[3], cv[3], y[3];
+      double r[3], x[3], V[9], D[3], K[3], g[3], cv[3], y[3], Wii[9], Pinv[9], z[3];
       ld3(a.r, i, r);
       const double al = 1.0 / __ldg(a.scaling + i);
       for (int k = 0; k < 3; ++k) x[k] = r[k] - al * (acc[k] + __ldg(a.b + 3 * i + k));
       projection_basis(__ldg(a.mu + i), x, al, V, D, K);
-      for (int k = 0; k < 9; ++k) a.V[9 * (size_t)i + k] = V[k];
+      const int dk = __ldg(a.diag + i);
+      for (int k = 0; k < 9; ++k) Wii[k] = dk >= 0 ? __ldg(a.val + 9 * (size_t)dk + k) : 0.0;
+      precond_block(V, D, Wii, Pinv);
+      for (int k = 0; k < 9; ++k) {
+        a.V[9 * (size_t)i + k] = V[k];
+        a.Pc[9 * (size_t)i + k] = Pinv[k];
+      }
       st3(a.D, i, D);
       st3(a.K, i, K);
       ld3(a.g, i, g);
       basis_apply_t(V, D, g, cv);
-      const double z[3] = {0.0, 0.0, 0.0};
-      st3(a.P, i, z);
+      mat3_apply(Pinv, cv, z);
+      const double zero[3] = {0.0, 0.0, 0.0};
+      st3(a.P, i, zero);
       st3(a.R, i, cv);
-      st3(a.Dir, i, cv);
-      basis_apply(V, D, cv, y);
+      st3(a.Dir, i, z);
+      basis_apply(V, D, z, y);
       st3(a.Y, i, y);
       rr = cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2];
+      rz = cv[0] * z[0] + cv[1] * z[1] + cv[2] * z[2];
     }
     put(0, c, rr);
+    put(1, c, rz);
   }
-  if (!ctx.sync_reduce(1)) return;
+  if (!ctx.sync_reduce(2)) return;
   const double rr0 = ldcg(a.scal);
   double rr = rr0;
+  double rz = ldcg(a.scal + 1);
   unsigned it = 0;
   const double stop = a.tol * a.tol * rr0;
   for (; it < a.max_iters; ++it) {
@@ -176,39 +235,45 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
     if (!ctx.sync_reduce(1)) return;
     const double dq = ldcg(a.scal);
     if (!(dq > 0.0)) break;  // S is positive definite on the unmasked components; guards exact convergence
-    const double step = rr / dq;
+    const double step = rz / dq;
     for (int c = gwarp; c < C; c += nwarps) {
       const int i = 32 * c + lane;
-      double v = 0.0;
+      double v = 0.0, w = 0.0;
       if (i < a.n) {
-        double p[3], res[3], d[3], q[3];
+        double p[3], res[3], d[3], q[3], Pinv[9], z[3];
         ld3(a.P, i, p);
         ld3(a.R, i, res);
         ld3(a.Dir, i, d);
         ld3(a.Q, i, q);
+        for (int k = 0; k < 9; ++k) Pinv[k] = ldcg(a.Pc + 9 * (size_t)i + k);
         for (int k = 0; k < 3; ++k) {
           p[k] = fma(step, d[k], p[k]);
           res[k] = fma(-step, q[k], res[k]);
         }
+        mat3_apply(Pinv, res, z);
         st3(a.P, i, p);
         st3(a.R, i, res);
+        st3(a.Z, i, z);
         v = res[0] * res[0] + res[1] * res[1] + res[2] * res[2];
+        w = res[0] * z[0] + res[1] * z[1] + res[2] * z[2];
       }
       put(0, c, v);
+      put(1, c, w);
     }
-    if (!ctx.sync_reduce(1)) return;
-    const double rr_new = ldcg(a.scal);
-    const double beta = rr_new / rr;
-    rr = rr_new;
+    if (!ctx.sync_reduce(2)) return;
+    rr = ldcg(a.scal);
+    const double rz_new = ldcg(a.scal + 1);
+    const double beta = rz_new / rz;
+    rz = rz_new;
     for (int c = gwarp; c < C; c += nwarps) {
       const int i = 32 * c + lane;
       if (i < a.n) {
-        double V[9], D[3], res[3], d[3], y[3];
+        double V[9], D[3], z[3], d[3], y[3];
         for (int k = 0; k < 9; ++k) V[k] = ldcg(a.V + 9 * (size_t)i + k);
         ld3(a.D, i, D);
-        ld3(a.R, i, res);
+        ld3(a.Z, i, z);
         ld3(a.Dir, i, d);
-        for (int k = 0; k < 3; ++k) d[k] = fma(beta, d[k], res[k]);
+        for (int k = 0; k < 3; ++k) d[k] = fma(beta, d[k], z[k]);
         st3(a.Dir, i, d);
         basis_apply(V, D, d, y);
         st3(a.Y, i, y);
