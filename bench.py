@@ -130,6 +130,18 @@ def traffic_from_profiles(algorithmic_bytes):
     return None
 
 
+def max_over_ranks(value: float, world: int, device: str = "cpu") -> float:
+    """The maximum of a per-rank value over all ranks (every rank gets it); the value itself when world == 1.
+    The tensor lives on `device` (a CUDA device under NCCL, the CPU under gloo)."""
+    if world <= 1:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_problem():
     from bogus_gpu import generator
 
@@ -230,11 +242,7 @@ def run_ours(args, rank, world, local_rank):
     if world > 1:
         torch.distributed.barrier()
     ck = clocks.stop()
-    ms_step = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms_step], dtype=torch.float64, device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, f"cuda:{dev}")
 
     # end to end through the C ABI with host buffers: upload W (lower), b, mu and r, solve, download r
     rp, cl, vl = D.W_lower()
