@@ -1,6 +1,7 @@
 """The multi-rank logic of bench.py (replicas only) on two gloo ranks on the CPU: the step time is the maximum
 over ranks on every rank, only rank 0 runs the reference arm, and the other ranks exit without work."""
 import io
+import json
 import os
 import socket
 import sys
@@ -21,7 +22,7 @@ def _free_port() -> int:
         return s.getsockname()[1]
 
 
-def _rank(rank, world, port, out):
+def _rank(rank, world, port, outdir):
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     sys.path.insert(0, REPO)
@@ -39,18 +40,20 @@ def _rank(rank, world, port, out):
             with redirect_stdout(buf):
                 bench.run_reference(A, rank, world)  # ranks other than 0 return at once
         dist.barrier()
-        out[rank] = (got, buf.getvalue())
+        with open(os.path.join(outdir, f"rank{rank}.json"), "w") as fh:
+            json.dump([got, buf.getvalue()], fh)
     finally:
         dist.destroy_process_group()
 
 
-def test_two_gloo_ranks_take_the_max_and_only_rank0_prints():
+def test_two_gloo_ranks_take_the_max_and_only_rank0_prints(tmp_path):
     world = 2
     port = _free_port()
-    with mp.Manager() as m:
-        out = m.dict()
-        mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
-        res = dict(out)
+    mp.spawn(_rank, args=(world, port, str(tmp_path)), nprocs=world, join=True)  # spawn start method
+    res = {}
+    for r in range(world):
+        with open(tmp_path / f"rank{r}.json") as fh:
+            res[r] = json.load(fh)
     assert res[0][0] == res[1][0] == 15.0
     assert res[1][1] == ""
 
