@@ -124,7 +124,12 @@ struct bogus_gpu_problem {
   std::vector<double> host_b, host_mu;
   // projected-gradient work
   DevBuf<double> X, MX, Y, S0, XB, Wv, csum, scal, trace;
-  // FP32 copies of W, b, mu, scalings and FP32 work (mixed precision), valid while W is unchanged
+  // interleaved copy of W (coalesced chunk layout read by the single-problem solvers), valid while W is unchanged
+  bool il_valid = false;
+  DevBuf<long long> slot0;
+  DevBuf<int> icol;
+  DevBuf<double> ival;
+  // FP32 copies of W (interleaved), b, mu, scalings and FP32 work (mixed precision), valid while W is unchanged
   bool fp32_valid = false;
   DevBuf<float> val32, b32, mu32, sc32, X32, MX32, Y32, S032, XB32, Wv32;
   DevBuf<PGOut> pgout;
@@ -206,6 +211,7 @@ int upload_full(bogus_gpu_problem* h, const HostBSR& f, const double* b, const d
   h->gs.valid = false;
   h->nproblems = 0;
   h->fp32_valid = false;
+  h->il_valid = false;
   h->adj_valid = false;
   return BOGUS_GPU_OK;
 }
@@ -235,6 +241,8 @@ int ensure_pg_work(bogus_gpu_problem* h, unsigned max_iters) {
   return BOGUS_GPU_OK;
 }
 
+int ensure_interleaved(bogus_gpu_problem* h);
+
 // Algorithmic bytes and W passes of one persistent solve from its phase counters. A W pass reads nnzb blocks
 // (9 values + a column index) and the n + 1 row pointers; the per-contact vector bytes of each pass kind
 // follow PGOut::phases (3-vectors 3 values, scalars 1 value). elem = bytes per value (8 FP64, 4 FP32).
@@ -261,12 +269,16 @@ PGTraffic pg_traffic(const PGOut& out, int n, long long nnzb, bool spg, double e
 int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual, unsigned* iters, const double** best) {
   const int n = h->W.n;
   const size_t n3 = 3 * (size_t)n;
+  if (int e = ensure_interleaved(h)) return e;
   PGArgs a{};
   a.n = n;
   a.nchunks = (n + 31) / 32;
   a.rowptr = h->W.rowptr;
   a.col = h->W.col;
   a.val = h->W.val;
+  a.icol = h->icol.p;
+  a.ival = h->ival.p;
+  a.slot0 = h->slot0.p;
   a.b = h->b.p;
   a.mu = h->mu.p;
   a.scaling = h->scaling.p;
@@ -295,7 +307,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.ls_iters = o->ls_iters;
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), h->stream));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
-  int grid = pg_max_grid(h->device);
+  int grid = pg_max_grid(h->device, false, true);
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
   const int want = (a.nchunks + 7) / 8;
   if (want < grid) grid = want < 1 ? 1 : want;
@@ -333,6 +345,33 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   return out.converged ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
 }
 
+// The interleaved copy of W: chunk c (rows 32c .. 32c+31, blocks [B0, B1)) takes 32 S slots, S =
+// ceil((B1 - B0) / 32) (1 for an empty chunk), from slot0[c].
+int ensure_interleaved(bogus_gpu_problem* h) {
+  if (h->il_valid) return BOGUS_GPU_OK;
+  const int n = h->W.n;
+  const int C = (n + 31) / 32;
+  std::vector<int> rp(n + 1);
+  BG_CUDA(cudaMemcpy(rp.data(), h->W.rowptr, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+  std::vector<long long> s0(C + 1, 0);
+  for (int c = 0; c < C; ++c) {
+    const int r1 = std::min(32 * c + 32, n);
+    const int T = rp[r1] - rp[32 * c];
+    const long long S = T > 0 ? (T + 31) / 32 : 1;
+    s0[c + 1] = s0[c] + 32 * S;
+  }
+  const size_t slots = (size_t)s0[C];
+  BG_CUDA(h->slot0.ensure(C + 1));
+  BG_CUDA(h->icol.ensure(slots > 0 ? slots : 1));
+  BG_CUDA(h->ival.ensure(9 * (slots > 0 ? slots : 1)));
+  BG_CUDA(cudaMemcpyAsync(h->slot0.p, s0.data(), sizeof(long long) * (C + 1), cudaMemcpyHostToDevice, h->stream));
+  BG_CUDA(launch_interleave(h->W, h->slot0.p, h->icol.p, h->ival.p, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  h->il_valid = true;
+  h->fp32_valid = false;
+  return BOGUS_GPU_OK;
+}
+
 // FP32 copies of the problem and FP32 work buffers for the mixed-precision solve.
 int ensure_fp32(bogus_gpu_problem* h) {
   const int n = h->W.n;
@@ -344,12 +383,13 @@ int ensure_fp32(bogus_gpu_problem* h) {
   BG_CUDA(h->S032.ensure(n));
   BG_CUDA(h->XB32.ensure(n3));
   BG_CUDA(h->Wv32.ensure(n3));
+  if (int e = ensure_interleaved(h)) return e;
   if (h->fp32_valid) return BOGUS_GPU_OK;
-  BG_CUDA(h->val32.ensure(9 * (size_t)h->W.nnzb));
+  BG_CUDA(h->val32.ensure(h->ival.n));
   BG_CUDA(h->b32.ensure(n3));
   BG_CUDA(h->mu32.ensure(n));
   BG_CUDA(h->sc32.ensure(n));
-  BG_CUDA(launch_convert(9 * (size_t)h->W.nnzb, h->W.val, h->val32.p, s));
+  BG_CUDA(launch_convert(h->ival.n, h->ival.p, h->val32.p, s));
   BG_CUDA(launch_convert(n3, h->b.p, h->b32.p, s));
   BG_CUDA(launch_convert((size_t)n, h->mu.p, h->mu32.p, s));
   BG_CUDA(launch_convert((size_t)n, h->scaling.p, h->sc32.p, s));
@@ -382,8 +422,11 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   a.n = n;
   a.nchunks = (n + 31) / 32;
   a.rowptr = h->W.rowptr;
-  a.col = h->W.col;
-  a.val = h->val32.p;
+  a.col = nullptr;
+  a.val = nullptr;
+  a.icol = h->icol.p;
+  a.ival = h->val32.p;
+  a.slot0 = h->slot0.p;
   a.b = h->b32.p;
   a.mu = h->mu32.p;
   a.scaling = h->sc32.p;
@@ -406,7 +449,7 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   BG_CUDA(launch_convert(n3, h->X.p, h->X32.p, s));
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
-  int grid = pg_max_grid(h->device, true);
+  int grid = pg_max_grid(h->device, true, true);
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
   const int want = (a.nchunks + 7) / 8;
   if (want < grid) grid = want < 1 ? 1 : want;
@@ -684,6 +727,9 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
     b->release();
   for (auto* b : {&h->val32, &h->b32, &h->mu32, &h->sc32, &h->X32, &h->MX32, &h->Y32, &h->S032, &h->XB32, &h->Wv32})
     b->release();
+  h->slot0.release();
+  h->icol.release();
+  h->ival.release();
   for (auto* b : {&h->a_prox, &h->a_f, &h->a_w, &h->a_mu, &h->a_invmu, &h->a_x, &h->a_r, &h->a_ut, &h->a_z, &h->a_zacc,
                   &h->a_zprev, &h->a_yprev})
     b->release();
@@ -780,6 +826,7 @@ int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* 
   h->gs.valid = false;
   h->nproblems = 0;
   h->fp32_valid = false;
+  h->il_valid = false;
   h->adj_valid = false;
   return BOGUS_GPU_OK;
 }
@@ -1127,11 +1174,14 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   BG_CUDA(h->scal.ensure(8));
   BG_CUDA(h->barrier.ensure(4));
   BG_CUDA(h->status.ensure(1));
+  if (int e = ensure_interleaved(h)) return e;
   AdjArgs a{};
   a.n = n;
   a.nchunks = C;
   a.rowptr = h->W.rowptr;
-  a.col = h->W.col;
+  a.icol = h->icol.p;
+  a.ival = h->ival.p;
+  a.slot0 = h->slot0.p;
   a.val = h->W.val;
   a.b = h->b.p;
   a.mu = h->mu.p;
@@ -1374,6 +1424,7 @@ int bogus_gpu_add_compliance(bogus_gpu_problem* h, const double* c) {
   }
   h->gs.valid = false;
   h->fp32_valid = false;
+  h->il_valid = false;
   h->adj_valid = false;
   return BOGUS_GPU_OK;
 }
@@ -1651,6 +1702,7 @@ int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double*
   h->gs.valid = false;
   h->nproblems = 0;
   h->fp32_valid = false;
+  h->il_valid = false;
   h->adj_valid = false;
   return BOGUS_GPU_OK;
 }

@@ -42,6 +42,10 @@ struct PGArgsT {
   const int* rowptr;
   const int* col;
   const T* val;
+  // the interleaved copy of W (InterleavedBlocks, spmv_chunk.cuh); null: the plain BSR arrays are read
+  const int* icol;
+  const T* ival;
+  const long long* slot0;
   const T* b;
   const T* mu;
   const T* scaling;
@@ -94,11 +98,13 @@ cudaError_t launch_add(int m, const double* a, const double* b, double* y, cudaS
 // Persistent solvers (kernels_pg.cu)
 cudaError_t launch_pg_persistent(const PGArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_pg_persistent(const PGArgs32& a, int grid, cudaStream_t s);
-int pg_max_grid(int device, bool fp32 = false);
+int pg_max_grid(int device, bool fp32 = false, bool interleaved = false);
 cudaError_t launch_pg_batched(const PGBatchArgs& b, int grid, cudaStream_t s);
 cudaError_t launch_pg_batched(const PGBatchArgs32& b, int grid, cudaStream_t s);
 int pg_batched_grid(int device, bool fp32 = false);
 cudaError_t launch_convert(size_t m, const double* src, float* dst, cudaStream_t s);
+// Interleaved copy of a both-triangle BSR (InterleavedBlocks): slot0 has nchunks + 1 entries (device).
+cudaError_t launch_interleave(const DevBSR& W, const long long* slot0, int* icol, double* ival, cudaStream_t s);
 cudaError_t launch_convert(size_t m, const float* src, double* dst, cudaStream_t s);
 
 // Gauss-Seidel (kernels_gs.cu)
@@ -168,8 +174,10 @@ struct AdjOut {
 struct AdjArgs {
   int n, nchunks;
   const int* rowptr;
-  const int* col;
-  const double* val;   // W, both triangles
+  const int* icol;     // W, both triangles, interleaved (InterleavedBlocks)
+  const double* ival;
+  const long long* slot0;
+  const double* val;   // W, plain BSR (diagonal blocks)
   const double* b;
   const double* mu;
   const double* scaling;  // per-contact fixed-point step 1 / scaling_i

@@ -166,7 +166,8 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
     if (lane == 0) a.csum[q * C + c] = v;
   };
   auto product = [&](int c, const double* src, double* acc) {
-    spmv_chunk<1>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, double* x) { ld3(src, j, x); }, acc);
+    spmv_chunk<1>(a.rowptr, InterleavedBlocks<double>{a.icol, a.ival, a.slot0}, a.n, c, sh,
+                  [&](int j, double* x) { ld3(src, j, x); }, acc);
   };
 
   // setup: x = r - alpha (W r + b), the basis, the preconditioner, rhs c = m o V^T g; p = 0, res = c,

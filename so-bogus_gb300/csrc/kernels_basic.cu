@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(256) k_spmv(int n, const int* __restrict__ row
     acc[1] = init[3 * i + 1];
     acc[2] = init[3 * i + 2];
   }
-  spmv_chunk<1>(rowptr, col, val, n, c, cs[warp],
+  spmv_chunk<1>(rowptr, PlainBlocks<double>{col, val}, n, c, cs[warp],
                 [&](int j, double* v) {
                   v[0] = __ldg(x + 3 * j);
                   v[1] = __ldg(x + 3 * j + 1);
@@ -37,6 +37,35 @@ __global__ void __launch_bounds__(256) k_spmv(int n, const int* __restrict__ row
     y[3 * i + 1] = acc[1];
     y[3 * i + 2] = acc[2];
   }
+}
+
+// Interleaved copy of W (InterleavedBlocks, spmv_chunk.cuh): one warp per 32-row chunk; slot (s, lane) takes
+// block B0 + lane S + s when it lies in the chunk, else padding (column 0, zero values, never read).
+__global__ void k_interleave(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                             const double* __restrict__ val, const long long* __restrict__ slot0,
+                             int* __restrict__ icol, double* __restrict__ ival) {
+  const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (32 * c >= n) return;
+  const int r1 = min(32 * c + 32, n);
+  const int B0 = rowptr[32 * c], B1 = rowptr[r1];
+  const int T = B1 - B0;
+  const int S = T > 0 ? (T + 31) / 32 : 1;
+  const long long base = slot0[c];
+  for (int st = 0; st < S; ++st) {
+    const int k = B0 + lane * S + st;
+    const bool ok = k < B1;
+    const long long slot = base + 32 * (long long)st + lane;
+    icol[slot] = ok ? col[k] : 0;
+    for (int e = 0; e < 9; ++e) ival[9 * base + 32 * (long long)(9 * st + e) + lane] = ok ? val[9 * (size_t)k + e] : 0.0;
+  }
+}
+
+cudaError_t launch_interleave(const DevBSR& W, const long long* slot0, int* icol, double* ival, cudaStream_t s) {
+  if (W.n == 0) return cudaSuccess;
+  const int chunks = (W.n + 31) / 32;
+  k_interleave<<<(chunks + 7) / 8, 256, 0, s>>>(W.n, W.rowptr, W.col, W.val, slot0, icol, ival);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_spmv(const DevBSR& W, const double* x, const double* init, double* y, cudaStream_t s) {

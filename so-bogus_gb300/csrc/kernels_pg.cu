@@ -53,14 +53,30 @@ __device__ __forceinline__ int third(int p, int q) {
 
 }  // namespace
 
-template <class T, class Ctx>
+template <class T, bool IL>
+struct BlocksOf;
+template <class T>
+struct BlocksOf<T, false> {
+  static __device__ __forceinline__ PlainBlocks<T> make(const PGArgsT<T>& a) { return PlainBlocks<T>{a.col, a.val}; }
+};
+template <class T>
+struct BlocksOf<T, true> {
+  static __device__ __forceinline__ InterleavedBlocks<T> make(const PGArgsT<T>& a) {
+    return InterleavedBlocks<T>{a.icol, a.ival, a.slot0};
+  }
+};
+
+// IL: read W through its interleaved copy (single-problem solves) or the plain BSR arrays (batched and
+// allocation-free solves). The arithmetic is the same.
+template <class T, bool IL, class Ctx>
 __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
   using Ops = SocOps<T>;
   const Bufs<T> B{a};
   ChunkScratchT<T>& sh = ctx.cs[threadIdx.x >> 5];
+  const auto blocks = BlocksOf<T, IL>::make(a);
   // y = W x of chunk c for every lane (row 32c + lane), x gathered from a buffer written earlier in the kernel
   auto product = [&](int c, const T* __restrict__ xsrc, T* acc) {
-    spmv_chunk<1>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, T* x) { load3cg(xsrc, j, x); }, acc);
+    spmv_chunk<1>(a.rowptr, blocks, a.n, c, sh, [&](int j, T* x) { load3cg(xsrc, j, x); }, acc);
   };
   const int lane = threadIdx.x & 31;
   const bool desaxce = a.desaxce != 0;
@@ -112,7 +128,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     const int i = 32 * c + lane;
     double v0 = 0.0, v1 = 0.0;
     T acc[3] = {T(0), T(0), T(0)}, accd[3] = {T(0), T(0), T(0)};
-    spmv_chunk<2>(a.rowptr, a.col, a.val, a.n, c, sh, [&](int j, T* x) { load3cg(a.X0, j, x); }, acc, accd);
+    spmv_chunk<2>(a.rowptr, blocks, a.n, c, sh, [&](int j, T* x) { load3cg(a.X0, j, x); }, acc, accd);
     if (i < a.n) {
       store3(a.MX0, i, acc);
       v0 = Ops::sq3(accd);
@@ -428,12 +444,12 @@ struct GridCtx {
   __device__ double scal(int q) const { return ldcg(a.scal + q); }
 };
 
-template <class T>
+template <class T, bool IL>
 __global__ void __launch_bounds__(256) k_pg_persistent(PGArgsT<T> a) {
   __shared__ double smem8[8];
   __shared__ ChunkScratchT<T> cs[8];
   GridCtx<T> ctx{a, smem8, cs};
-  pg_body<T>(a, ctx);
+  pg_body<T, IL>(a, ctx);
 }
 
 // One problem per CTA (batched solves): phases separated by __syncthreads, scalars reduced by the CTA's
@@ -499,7 +515,7 @@ __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgsT<T> ba) {
     a.trace = nullptr;
     a.out = ba.base.out + p;
     BlockCtx<T> ctx{a, smem8, sscal, cs};
-    const int best = pg_body<T>(a, ctx);
+    const int best = pg_body<T, false>(a, ctx);
     __syncthreads();
     if (n == 0) continue;
     const T* src = best == 3 ? a.XB : (best == 0 ? a.X0 : (best == 1 ? a.X1 : a.X2));
@@ -530,20 +546,24 @@ int pg_batched_grid(int device, bool fp32) {
 cudaError_t launch_pg_persistent(const PGArgs& a, int grid, cudaStream_t s) {
   PGArgs copy = a;
   void* args[] = {&copy};
-  return cudaLaunchCooperativeKernel((const void*)k_pg_persistent<double>, dim3(grid), dim3(256), args, 0, s);
+  const void* fn = a.slot0 ? (const void*)k_pg_persistent<double, true> : (const void*)k_pg_persistent<double, false>;
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s);
 }
 
 cudaError_t launch_pg_persistent(const PGArgs32& a, int grid, cudaStream_t s) {
+  if (!a.slot0) return cudaErrorInvalidValue;  // the FP32 solve reads the interleaved copy only
   PGArgs32 copy = a;
   void* args[] = {&copy};
-  return cudaLaunchCooperativeKernel((const void*)k_pg_persistent<float>, dim3(grid), dim3(256), args, 0, s);
+  return cudaLaunchCooperativeKernel((const void*)k_pg_persistent<float, true>, dim3(grid), dim3(256), args, 0, s);
 }
 
-int pg_max_grid(int device, bool fp32) {
+int pg_max_grid(int device, bool fp32, bool interleaved) {
   int sms = 0, per = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
-  const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_persistent<float>, 256, 0)
-                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_persistent<double>, 256, 0);
+  const void* fn = fp32 ? (const void*)k_pg_persistent<float, true>
+                        : (interleaved ? (const void*)k_pg_persistent<double, true>
+                                       : (const void*)k_pg_persistent<double, false>);
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
   if (e != cudaSuccess) return 0;
   if (per > 2) per = 2;
   return per * sms;

@@ -23,14 +23,48 @@ struct ChunkScratchT {
 };
 using ChunkScratch = ChunkScratchT<double>;
 
+// Where the blocks live. Both sources give block k (original BSR index), met by a lane at step s of its
+// segment (k = B0 + lane S + s).
+//
+// PlainBlocks: the BSR arrays themselves, column col[k], values val[9k .. 9k+8]. A warp's 32 lanes read
+// 32 segments S blocks apart, so each load instruction touches 32 separate sectors.
+template <class T>
+struct PlainBlocks {
+  const int* __restrict__ col;
+  const T* __restrict__ val;
+  __device__ __forceinline__ void chunk(int) {}
+  __device__ __forceinline__ int column(int k, int) const { return ldcs(col + k); }
+  __device__ __forceinline__ T value(int k, int, int e) const { return ldcs(val + 9 * (size_t)k + e); }
+};
+
+// InterleavedBlocks: each chunk stored step-major for coalesced loads. Chunk c owns slots
+// [slot0[c], slot0[c] + 32 S); the block of lane l at step s is slot slot0[c] + 32 s + l, its column is
+// icol[slot] and its value e is ival[9 slot0[c] + 32 (9 s + e) + l]. At a given step the 32 lanes read
+// consecutive words: one 128-byte (int, float) or 256-byte (double) access per load instruction. Slots
+// past the chunk's last block are padding and never read. Built by launch_interleave (kernels_basic.cu).
+template <class T>
+struct InterleavedBlocks {
+  const int* __restrict__ icol;
+  const T* __restrict__ ival;
+  const long long* __restrict__ slot0;
+  long long base = 0;
+  __device__ __forceinline__ void chunk(int c) { base = __ldg(slot0 + c); }
+  __device__ __forceinline__ int column(int, int s) const {
+    return ldcs(icol + base + 32 * (long long)s + (threadIdx.x & 31));
+  }
+  __device__ __forceinline__ T value(int, int s, int e) const {
+    return ldcs(ival + 9 * base + 32 * (long long)(9 * s + e) + (threadIdx.x & 31));
+  }
+};
+
 // NP = 1: y = init + W x. NP = 2: additionally y2 = init2 + W (x - 1) (both from the same pass over W).
 // Every lane of the warp must call it (warp-uniform c). acc (and acc2) hold init on entry, the result on
 // exit, for row 32c + lane (lanes past n get unspecified values).
-template <int NP, class T, class Gather>
-__device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, const int* __restrict__ col,
-                                           const T* __restrict__ val, int n, int c, ChunkScratchT<T>& sh,
-                                           Gather&& gather, T* acc, T* acc2 = nullptr) {
+template <int NP, class T, class Src, class Gather>
+__device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, Src src, int n, int c,
+                                           ChunkScratchT<T>& sh, Gather&& gather, T* acc, T* acc2 = nullptr) {
   const int lane = threadIdx.x & 31;
+  src.chunk(c);
   const int r0 = 32 * c;
   const int r1 = min(r0 + 32, n);
   sh.st[lane] = __ldg(rowptr + min(r0 + lane, r1));
@@ -39,7 +73,8 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, const
   const int B0 = sh.st[0], B1 = sh.st[32];
   const int nblk = B1 - B0;
   const int S = nblk > 0 ? (nblk + 31) / 32 : 1;
-  int k = B0 + lane * S;
+  const int k0 = B0 + lane * S;
+  int k = k0;
   const int e = min(k + S, B1);
   if (k < e) {
     int lo = 0, hi = 31;  // row containing block k: last t with st[t] <= k
@@ -52,7 +87,17 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, const
     int next = sh.st[t + 1];
     T p[3] = {T(0), T(0), T(0)}, q[3] = {T(0), T(0), T(0)};
     bool open = false;
+    // The next block's column index and gathered x are loaded one block ahead, so the dependent col -> x load
+    // chain of block k + 1 overlaps the accumulation of block k (the arithmetic order is unchanged).
+    T xn[3];
+    gather(src.column(k, 0), xn);
     for (; k < e; ++k) {
+      const int step = k - k0;
+      const T x[3] = {xn[0], xn[1], xn[2]};
+      if (k + 1 < e) gather(src.column(k + 1, step + 1), xn);
+      T b[9];
+#pragma unroll
+      for (int e2 = 0; e2 < 9; ++e2) b[e2] = src.value(k, step, e2);
       while (k >= next) {
         if (open) {
           T* s = sh.part[t + lane];
@@ -65,13 +110,6 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, const
         ++t;
         next = sh.st[t + 1];
       }
-      const int j = ldcs(col + k);
-      T x[3];
-      gather(j, x);
-      const T* Bk = val + 9 * (size_t)k;
-      T b[9];
-#pragma unroll
-      for (int e2 = 0; e2 < 9; ++e2) b[e2] = ldcs(Bk + e2);
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
         T s = p[r];
