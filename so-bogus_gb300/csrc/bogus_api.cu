@@ -250,9 +250,11 @@ struct PGTraffic {
   double bytes = 0, fma = 0;
   unsigned passes = 0;
 };
-PGTraffic pg_traffic(const PGOut& out, int n, long long nnzb, bool spg, double elem) {
+PGTraffic pg_traffic(const PGOut& out, int n, long long nnzb, int variant, double elem) {
+  const bool spg = variant == BOGUS_GPU_PG_SPG, apgd = variant == BOGUS_GPU_PG_APGD;
   const double wpass = (double)nnzb * (9.0 * elem + 4.0) + 4.0 * (n + 1);
-  const double per_contact[9] = {7, 6, spg ? 21.0 : 18.0, 19, 10, 9, 18, 15, 12};  // values per contact
+  // values per contact; APGD's trial product also writes the momentum point
+  const double per_contact[9] = {7, 6, spg ? 21.0 : 18.0, apgd ? 22.0 : 19.0, 10, 9, 18, 15, 12};
   const bool has_w[9] = {false, true, false, true, false, false, true, false, true};
   PGTraffic t;
   for (int k = 0; k < 9; ++k) {
@@ -323,7 +325,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   h->last_launches = 1;
   if (st != 0) return fail(st, "device-side wait timed out in the projected-gradient kernel");
   {
-    const PGTraffic t = pg_traffic(out, n, h->W.nnzb, o->variant == BOGUS_GPU_PG_SPG, 8.0);
+    const PGTraffic t = pg_traffic(out, n, h->W.nnzb, o->variant, 8.0);
     h->last_stats.iterations = out.iters;
     h->last_stats.refine_iterations = 0;
     h->last_stats.fp32_device_ms = 0.0;
@@ -333,7 +335,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   }
   if (residual) *residual = out.min_res;
   if (iters) *iters = out.iters;
-  *best = out.best_buf == 3 ? h->XB.p : h->X.p + (size_t)out.best_buf * n3;
+  *best = out.best_buf == 3 ? h->XB.p : (out.best_buf == 4 ? h->Wv.p : h->X.p + (size_t)out.best_buf * n3);
   if (h->callback) {
     const unsigned count = out.converged ? out.iters + 1 : out.iters;
     std::vector<double> tr(count);
@@ -464,14 +466,15 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   float ms32 = 0.f;
   BG_CUDA(cudaEventElapsedTime(&ms32, h->ev0, h->ev1));
   if (st != 0) return fail(st, "device-side wait timed out in the FP32 projected-gradient kernel");
-  const float* b32 = out.best_buf == 3 ? h->XB32.p : h->X32.p + (size_t)out.best_buf * n3;
+  const float* b32 =
+      out.best_buf == 3 ? h->XB32.p : (out.best_buf == 4 ? h->Wv32.p : h->X32.p + (size_t)out.best_buf * n3);
   BG_CUDA(launch_convert(n3, b32, h->X.p, s));
   bogus_gpu_pg_options o64 = *o;
   o64.max_iters = o->refine_max_iters;
   const unsigned it32 = out.iters;
   const int rst = run_pg(h, &o64, residual, iters, best);
   if (rst != BOGUS_GPU_OK && rst != BOGUS_GPU_NOT_CONVERGED) return rst;
-  const PGTraffic t32 = pg_traffic(out, n, h->W.nnzb, o->variant == BOGUS_GPU_PG_SPG, 4.0);
+  const PGTraffic t32 = pg_traffic(out, n, h->W.nnzb, o->variant, 4.0);
   h->last_stats.refine_iterations = h->last_stats.iterations;
   h->last_stats.iterations = it32 + h->last_stats.iterations;
   h->last_stats.w_passes += t32.passes;
@@ -1810,13 +1813,12 @@ int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   bool all = true;
   PGTraffic sum;
   unsigned maxit = 0;
-  const bool spg = o->variant == BOGUS_GPU_PG_SPG;
   for (int p = 0; p < np; ++p) {
     if (residuals) residuals[p] = out[p].min_res;
     if (iters) iters[p] = out[p].iters;
     all = all && (out[p].converged || h->h_contact_ptr[p + 1] == h->h_contact_ptr[p]);
     const int np_c = h->h_contact_ptr[p + 1] - h->h_contact_ptr[p];
-    const PGTraffic t = pg_traffic(out[p], np_c, h->h_problem_nnz[p], spg, 8.0);
+    const PGTraffic t = pg_traffic(out[p], np_c, h->h_problem_nnz[p], o->variant, 8.0);
     sum.bytes += t.bytes;
     sum.fma += t.fma;
     sum.passes += t.passes;

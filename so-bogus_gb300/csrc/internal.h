@@ -26,7 +26,7 @@ struct DevBSR {
 struct PGOut {
   double min_res;
   unsigned iters;
-  int best_buf;   // 0..2: position buffer holding the best iterate; 3: the x_best buffer
+  int best_buf;   // 0..2: position buffer X0..X2 holding the best iterate; 3: the x_best buffer; 4: Wv
   int converged;
   // passes made by the solve, by kind (for the algorithmic-bytes accounting of the roofline):
   // 0 projection, 1 guess product, 2 A, 3 C (trial product), 4 B (retry), 5 D (momentum), 6 E+A,

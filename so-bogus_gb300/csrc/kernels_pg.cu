@@ -11,11 +11,12 @@
 //
 // Phases of one APGD iteration (reference line numbers in ProjectedGradient.impl.hpp):
 //   A   y = Mx + b, residual (:110-111), s = COV(y), y += s, J (:113-115), xs = P(x - a y) (:123-125)
-//   C   Mxs = W xs; Js, y.(xs-x), |xs-x|^2 (:127-132), (xs-prev).y (:135) ............ barrier+reduce
+//   C   Mxs = W xs; Js, y.(xs-x), |xs-x|^2 (:127-132), (xs-prev).y (:135); APGD also writes the
+//       momentum point x = xs + beta (xs - prev) (:137-139) to a spare buffer ........... barrier+reduce
 //   B   line-search retry: xs = P(x - a y) ............................................ barrier
-//   D   momentum x = xs + beta (xs - prev) (:137-139) .................................. barrier
 //   E+A Mx = W x (:141) fused with A of the next iteration ............................. barrier+reduce
-// Without momentum x = xs and Mx = Mxs are buffer swaps and A runs as its own pass.
+// With momentum, the spare buffer becomes x (a buffer swap); without, x = xs and Mx = Mxs are swaps and A
+// runs as its own pass. Phase counter 5 (a separate momentum pass) is no longer used.
 #include "internal.h"
 #include "soc_device.cuh"
 #include "soc_ops.cuh"
@@ -38,10 +39,12 @@ __device__ __forceinline__ void store3(T* p, int i, const T* v) {
   p[3 * i + 2] = v[2];
 }
 
+// Position buffers 0, 1, 2 (X0..X2) and 4 (Wv, free in APGD / Descent: the speculative momentum point);
+// 3 names the x_best buffer in PGOut::best_buf.
 template <class T>
 struct Bufs {
   const PGArgsT<T>& a;
-  __device__ T* X(int k) const { return k == 0 ? a.X0 : (k == 1 ? a.X1 : a.X2); }
+  __device__ T* X(int k) const { return k == 0 ? a.X0 : (k == 1 ? a.X1 : (k == 2 ? a.X2 : a.Wv)); }
   __device__ T* MX(int k) const { return k == 0 ? a.MX0 : a.MX1; }
 };
 
@@ -49,6 +52,19 @@ __device__ __forceinline__ int third(int p, int q) {
   for (int k = 0; k < 3; ++k)
     if (k != p && k != q) return k;
   return 0;
+}
+
+// The first two of the position buffers {0, 1, 2, 4} other than p and q (p == q allowed).
+__device__ __forceinline__ void two_free(int p, int q, int& f0, int& f1) {
+  const int ids[4] = {0, 1, 2, 4};
+  f0 = -1;
+  f1 = -1;
+  for (int k = 0; k < 4; ++k) {
+    const int v = ids[k];
+    if (v == p || v == q) continue;
+    if (f0 < 0) f0 = v;
+    else if (f1 < 0) f1 = v;
+  }
 }
 
 }  // namespace
@@ -205,6 +221,10 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
 
   if (!spg) {
     // ---------------------------------------------------------------- APGD / Descent
+    // APGD's momentum point x = xs + beta (xs - prev) (:137-139) is formed speculatively by every trial
+    // product (C) into the spare buffer ispec, with beta from the Nesterov sequence (it needs no reduction);
+    // when the line search ends with momentum, that buffer becomes x without a pass of its own.
+    int ispec = 4;
     double alpha_t = alpha * a.opt;
     if (!runA(alpha_t)) return -1;
     for (;;) {
@@ -220,8 +240,11 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
       alpha = alpha_t;
       unsigned ls = 0;
       double decr2 = 0.0;
+      double theta_spec = theta;
+      const double beta_spec = apgd ? nesterov_inertia(theta_spec, 0.0) : 0.0;
+      const T bt = T(beta_spec);
       for (;;) {
-        // C: Mxs = W xs and the line-search terms
+        // C: Mxs = W xs, the line-search terms and the speculative momentum point
         ph[3]++;
         for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
@@ -245,6 +268,10 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
             const T d2[3] = {xs[0] - pv[0], xs[1] - pv[1], xs[2] - pv[2]};
             v3 = Ops::dot3(d2, y);
             if (best_pending) store3(a.XB, i, x);
+            if (apgd) {
+              const T xn[3] = {fma(bt, xs[0] - pv[0], xs[0]), fma(bt, xs[1] - pv[1], xs[1]), fma(bt, xs[2] - pv[2], xs[2])};
+              store3(B.X(ispec), i, xn);
+            }
           }
           put(0, c, v0, false);
           put(1, c, v1, false);
@@ -278,23 +305,11 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
       ++it;
       const bool more = it < a.max_iters;
       if (apgd && decr2 < 0) {
-        const double beta = nesterov_inertia(theta, 0.0);
-        // D: x = xs + beta (xs - prev), written over the old x
-        ph[5]++;
-        for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
-          const int i = 32 * c + lane;
-          if (i < a.n) {
-            T xs[3], pv[3];
-            load3cg(B.X(ixs), i, xs);
-            load3cg(B.X(iprev), i, pv);
-            const T bt = T(beta);
-            const T xn[3] = {fma(bt, xs[0] - pv[0], xs[0]), fma(bt, xs[1] - pv[1], xs[1]), fma(bt, xs[2] - pv[2], xs[2])};
-            store3(B.X(ix), i, xn);
-          }
-        }
-        if (!sync()) return -1;
-        iprev = ixs;
-        ixs = third(ix, iprev);
+        theta = theta_spec;  // nesterov_inertia(theta, 0) (:137), whose value beta_spec already holds
+        const int nix = ispec, nprev = ixs;
+        ix = nix;
+        iprev = nprev;
+        two_free(ix, iprev, ixs, ispec);
         if (!more) break;
         alpha_t = alpha * a.opt;
         // E + A: Mx = W x, then A of the next iteration on the same rows
@@ -317,7 +332,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
         ix = ixs;
         iprev = ixs;
         imx = 1 - imx;
-        ixs = (ix + 1) % 3;
+        two_free(ix, iprev, ixs, ispec);
         if (!more) break;
         alpha_t = alpha * a.opt;
         if (!runA(alpha_t)) return -1;
@@ -518,7 +533,7 @@ __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgsT<T> ba) {
     const int best = pg_body<T, false>(a, ctx);
     __syncthreads();
     if (n == 0) continue;
-    const T* src = best == 3 ? a.XB : (best == 0 ? a.X0 : (best == 1 ? a.X1 : a.X2));
+    const T* src = best == 3 ? a.XB : (best == 4 ? a.Wv : (best == 0 ? a.X0 : (best == 1 ? a.X1 : a.X2)));
     T* dst = ba.r + 3 * (size_t)c0;
     for (int k = threadIdx.x; k < 3 * n; k += blockDim.x) dst[k] = ldcg(src + k);
   }

@@ -180,7 +180,9 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   NA_CUDA(cudaMemcpyAsync(&dev_status, words + 2, sizeof(int), cudaMemcpyDeviceToHost, cs));
   NA_CUDA(cudaStreamSynchronize(cs));
   if (dev_status != 0) return fail(dev_status, "device-side wait timed out in the projected-gradient kernel");
-  const double* best = out.best_buf == 3 ? a.XB : (out.best_buf == 0 ? a.X0 : (out.best_buf == 1 ? a.X1 : a.X2));
+  const double* best =
+      out.best_buf == 3 ? a.XB
+                        : (out.best_buf == 4 ? a.Wv : (out.best_buf == 0 ? a.X0 : (out.best_buf == 1 ? a.X1 : a.X2)));
   NA_CUDA(cudaMemcpyAsync(d_r, best, sizeof(double) * n3, cudaMemcpyDeviceToDevice, cs));
   NA_CUDA(cudaStreamSynchronize(cs));
   if (residual) *residual = out.min_res;
