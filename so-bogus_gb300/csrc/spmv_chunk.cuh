@@ -74,30 +74,37 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, Src s
   const int nblk = B1 - B0;
   const int S = nblk > 0 ? (nblk + 31) / 32 : 1;
   const int k0 = B0 + lane * S;
-  int k = k0;
-  const int e = min(k + S, B1);
-  if (k < e) {
-    int lo = 0, hi = 31;  // row containing block k: last t with st[t] <= k
+  const int e = min(k0 + S, B1);
+  // Every lane runs the same S steps (lanes past the end of their segment, or with none, are predicated
+  // off) and the warp reconverges after the per-lane row-boundary flush, so the 9 FMAs of a step issue once
+  // per warp: lanes cross row boundaries at different steps, and a divergent flush left to itself would
+  // split the warp and issue the FMAs once per divergent group.
+  int t = 31;
+  if (k0 < e) {
+    int lo = 0, hi = 31;  // row containing block k0: last t with st[t] <= k0
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (sh.st[mid] <= k) lo = mid;
+      if (sh.st[mid] <= k0) lo = mid;
       else hi = mid - 1;
     }
-    int t = lo;
-    int next = sh.st[t + 1];
-    T p[3] = {T(0), T(0), T(0)}, q[3] = {T(0), T(0), T(0)};
-    bool open = false;
-    // The next block's column index and gathered x are loaded one block ahead, so the dependent col -> x load
-    // chain of block k + 1 overlaps the accumulation of block k (the arithmetic order is unchanged).
-    T xn[3];
-    gather(src.column(k, 0), xn);
-    for (; k < e; ++k) {
-      const int step = k - k0;
-      const T x[3] = {xn[0], xn[1], xn[2]};
-      if (k + 1 < e) gather(src.column(k + 1, step + 1), xn);
-      T b[9];
+    t = lo;
+  }
+  int next = sh.st[t + 1];
+  T p[3] = {T(0), T(0), T(0)}, q[3] = {T(0), T(0), T(0)};
+  bool open = false;
+  // The next block's column index and gathered x are loaded one block ahead, so the dependent col -> x load
+  // chain of block k + 1 overlaps the accumulation of block k (the arithmetic order is unchanged).
+  T xn[3] = {T(0), T(0), T(0)};
+  if (k0 < e) gather(src.column(k0, 0), xn);
+  for (int step = 0; step < S; ++step) {
+    const int k = k0 + step;
+    const bool valid = k < e;
+    const T x[3] = {xn[0], xn[1], xn[2]};
+    if (k + 1 < e) gather(src.column(k + 1, step + 1), xn);
+    T b[9];
 #pragma unroll
-      for (int e2 = 0; e2 < 9; ++e2) b[e2] = src.value(k, step, e2);
+    for (int e2 = 0; e2 < 9; ++e2) b[e2] = valid ? src.value(k, step, e2) : T(0);
+    if (valid) {
       while (k >= next) {
         if (open) {
           T* s = sh.part[t + lane];
@@ -110,6 +117,9 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, Src s
         ++t;
         next = sh.st[t + 1];
       }
+    }
+    __syncwarp();
+    if (valid) {
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
         T s = p[r];
@@ -131,11 +141,11 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, Src s
       }
       open = true;
     }
-    if (open) {
-      T* s = sh.part[t + lane];
-      s[0] = p[0]; s[1] = p[1]; s[2] = p[2];
-      if (NP == 2) { s[3] = q[0]; s[4] = q[1]; s[5] = q[2]; }
-    }
+  }
+  if (open) {
+    T* s = sh.part[t + lane];
+    s[0] = p[0]; s[1] = p[1]; s[2] = p[2];
+    if (NP == 2) { s[3] = q[0]; s[4] = q[1]; s[5] = q[2]; }
   }
   __syncwarp();
   if (r0 + lane < r1) {
