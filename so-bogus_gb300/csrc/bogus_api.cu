@@ -127,6 +127,7 @@ struct bogus_gpu_problem {
   // interleaved copy of W (coalesced chunk layout read by the single-problem solvers), valid while W is unchanged
   bool il_valid = false;
   DevBuf<long long> slot0;
+  DevBuf<int> chunk_order;  // chunks by decreasing segment length (ticket order of the persistent solvers)
   DevBuf<int> icol;
   DevBuf<double> ival;
   // FP32 copies of W (interleaved), b, mu, scalings and FP32 work (mixed precision), valid while W is unchanged
@@ -281,6 +282,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.icol = h->icol.p;
   a.ival = h->ival.p;
   a.slot0 = h->slot0.p;
+  a.chunk_order = h->chunk_order.p;
   a.b = h->b.p;
   a.mu = h->mu.p;
   a.scaling = h->scaling.p;
@@ -356,12 +358,18 @@ int ensure_interleaved(bogus_gpu_problem* h) {
   std::vector<int> rp(n + 1);
   BG_CUDA(cudaMemcpy(rp.data(), h->W.rowptr, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
   std::vector<long long> s0(C + 1, 0);
+  std::vector<int> seg(C), order(C);
   for (int c = 0; c < C; ++c) {
     const int r1 = std::min(32 * c + 32, n);
     const int T = rp[r1] - rp[32 * c];
     const long long S = T > 0 ? (T + 31) / 32 : 1;
     s0[c + 1] = s0[c] + 32 * S;
+    seg[c] = (int)S;
+    order[c] = c;
   }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return seg[x] > seg[y]; });
+  BG_CUDA(h->chunk_order.ensure(C > 0 ? C : 1));
+  if (C) BG_CUDA(cudaMemcpyAsync(h->chunk_order.p, order.data(), sizeof(int) * C, cudaMemcpyHostToDevice, h->stream));
   const size_t slots = (size_t)s0[C];
   BG_CUDA(h->slot0.ensure(C + 1));
   BG_CUDA(h->icol.ensure(slots > 0 ? slots : 1));
@@ -429,6 +437,7 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   a.icol = h->icol.p;
   a.ival = h->val32.p;
   a.slot0 = h->slot0.p;
+  a.chunk_order = h->chunk_order.p;
   a.b = h->b32.p;
   a.mu = h->mu32.p;
   a.scaling = h->sc32.p;
@@ -731,6 +740,7 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   for (auto* b : {&h->val32, &h->b32, &h->mu32, &h->sc32, &h->X32, &h->MX32, &h->Y32, &h->S032, &h->XB32, &h->Wv32})
     b->release();
   h->slot0.release();
+  h->chunk_order.release();
   h->icol.release();
   h->ival.release();
   for (auto* b : {&h->a_prox, &h->a_f, &h->a_w, &h->a_mu, &h->a_invmu, &h->a_x, &h->a_r, &h->a_ut, &h->a_z, &h->a_zacc,

@@ -46,6 +46,7 @@ struct PGArgsT {
   const int* icol;
   const T* ival;
   const long long* slot0;
+  const int* chunk_order;  // chunks in the order the tickets hand them out (largest first); null: natural
   const T* b;
   const T* mu;
   const T* scaling;

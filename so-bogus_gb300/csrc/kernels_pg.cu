@@ -105,6 +105,20 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     v = is_max ? warp_max_butterfly(v) : warp_sum_butterfly(v);
     if (lane == 0) a.csum[q * C + c] = v;
   };
+  // chunk sums of values 0 and 1 (value 0 the maximum when max0)
+  auto put2 = [&](int c, double v0, double v1, bool max0) {
+    if (max0) {
+      put(0, c, v0, true);
+      put(1, c, v1, false);
+      return;
+    }
+    const double v = warp_sum2_butterfly(v0, v1);
+    if ((lane & 15) == 0) a.csum[(lane >> 4) * C + c] = v;
+  };
+  auto put4 = [&](int c, double v0, double v1, double v2, double v3) {
+    const double v = warp_sum4_butterfly(v0, v1, v2, v3);
+    if ((lane & 7) == 0) a.csum[(lane >> 3) * C + c] = v;
+  };
   auto sync = [&]() -> bool { return ctx.sync(); };
   auto sync_reduce = [&](int K, unsigned maxmask) -> bool { return ctx.sync_reduce(K, maxmask); };
   auto scal = [&](int q) { return ctx.scal(q); };
@@ -153,8 +167,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
       const T d[3] = {x[0] - T(1), x[1] - T(1), x[2] - T(1)};
       v1 = Ops::sq3(d);
     }
-    put(0, c, v0, false);
-    put(1, c, v1, false);
+    put2(c, v0, v1, false);
   }
   if (!sync_reduce(2, 0u)) return -1;
   double alpha = 1.0;
@@ -209,8 +222,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
         load3cg(B.MX(imx), i, Mx);
         phaseA(i, Mx, alpha_t, r, q);
       }
-      put(0, c, r, res_mask != 0);
-      put(1, c, q, false);
+      put2(c, r, q, res_mask != 0);
     }
     return sync_reduce(2, res_mask);
   };
@@ -273,10 +285,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
               store3(B.X(ispec), i, xn);
             }
           }
-          put(0, c, v0, false);
-          put(1, c, v1, false);
-          put(2, c, v2, false);
-          put(3, c, v3, false);
+          put4(c, v0, v1, v2, v3);
         }
         best_pending = false;
         if (!sync_reduce(4, 0u)) return -1;
@@ -323,8 +332,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
             store3(B.MX(imx), i, acc);
             phaseA(i, acc, alpha_t, r, q);
           }
-          put(0, c, r, res_mask != 0);
-          put(1, c, q, false);
+          put2(c, r, q, res_mask != 0);
         }
         if (!sync_reduce(2, res_mask)) return -1;
       } else {
@@ -399,8 +407,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
         v0 = Ops::dot3(w, z);
         v1 = Ops::sq3(z);
       }
-      put(0, c, v0, false);
-      put(1, c, v1, false);
+      put2(c, v0, v1, false);
     }
     if (!sync_reduce(2, 0u)) return -1;
     imx = 1 - imx;
@@ -418,7 +425,8 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
 // Single problem: the whole GPU, phases separated by the bounded grid barrier; the last CTA to arrive
 // publishes the reduced scalars in global memory. Warps take 32-contact chunks from a ticket counter (one
 // per phase parity, cleared by the last CTA of the barrier that ends the phase), so SMs that finish early
-// take more chunks; every cross-phase dependency goes through a barrier, and the reduction order does not
+// take more chunks; tickets map to chunks largest first (chunk_order), so the last chunks of a phase are
+// the short ones. Every cross-phase dependency goes through a barrier, and the reduction order does not
 // depend on which warp handles a chunk.
 template <class T>
 struct GridCtx {
@@ -428,7 +436,10 @@ struct GridCtx {
   unsigned phase = 0;  // barriers passed (identical in every CTA)
   __device__ int ticket() {
     int c = 0;
-    if ((threadIdx.x & 31) == 0) c = (int)atomicAdd(a.tickets + (phase & 1u), 1u);
+    if ((threadIdx.x & 31) == 0) {
+      c = (int)atomicAdd(a.tickets + (phase & 1u), 1u);
+      if (a.chunk_order) c = c < a.nchunks ? __ldg(a.chunk_order + c) : a.nchunks;
+    }
     return __shfl_sync(0xffffffffu, c, 0);
   }
   __device__ int first_chunk() { return ticket(); }
@@ -438,10 +449,7 @@ struct GridCtx {
     if (threadIdx.x == 0) a.tickets[phase & 1u] = 0u;
   }
   __device__ void publish(int K, unsigned maxmask) {
-    for (int q = 0; q < K; ++q) {
-      const double v = block8_combine(a.csum + q * a.nchunks, a.nchunks, (maxmask >> q) & 1u, smem8);
-      if (threadIdx.x == 0) a.scal[q] = v;
-    }
+    block8_combine_k(a.csum, a.nchunks, K, maxmask, smem8, a.scal);
   }
   __device__ bool sync() {
     const bool ok = grid_barrier(a.gb, [&] { clear_tickets(); });
@@ -459,9 +467,10 @@ struct GridCtx {
   __device__ double scal(int q) const { return ldcg(a.scal + q); }
 };
 
+// Occupancy targets: 3 resident CTAs per SM for FP64, 4 for FP32 (see pg_max_grid).
 template <class T, bool IL>
-__global__ void __launch_bounds__(256) k_pg_persistent(PGArgsT<T> a) {
-  __shared__ double smem8[8];
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_pg_persistent(PGArgsT<T> a) {
+  __shared__ double smem8[32];
   __shared__ ChunkScratchT<T> cs[8];
   GridCtx<T> ctx{a, smem8, cs};
   pg_body<T, IL>(a, ctx);
@@ -484,11 +493,7 @@ struct BlockCtx {
   }
   __device__ bool sync_reduce(int K, unsigned maxmask) {
     __syncthreads();
-    for (int q = 0; q < K; ++q) {
-      const double v = block8_combine(a.csum + q * a.nchunks, a.nchunks, (maxmask >> q) & 1u, smem8);
-      if (threadIdx.x == 0) sscal[q] = v;
-    }
-    __syncthreads();
+    block8_combine_k(a.csum, a.nchunks, K, maxmask, smem8, sscal);
     return true;
   }
   __device__ double scal(int q) const { return sscal[q]; }
@@ -498,7 +503,7 @@ struct BlockCtx {
 // problem with the same arithmetic as the single-problem kernel, then writes the best iterate to r.
 template <class T>
 __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgsT<T> ba) {
-  __shared__ double smem8[8], sscal[8];
+  __shared__ double smem8[32], sscal[8];
   __shared__ ChunkScratchT<T> cs[8];
   __shared__ int s_job;
   for (;;) {
@@ -581,9 +586,9 @@ int pg_max_grid(int device, bool fp32, bool interleaved) {
   const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
   if (e != cudaSuccess) return 0;
   // Measured on the 200 000-contact problem: 3 resident CTAs per SM for FP64 (0.388 ms per APGD iteration
-  // against 0.411 with 2 and 0.502 with 1) and 5 for FP32 (0.181 ms against 0.232 with 2); more warps hide
-  // the gather latency of the products, and the grid barrier stays cheap at these sizes.
-  const int cap = fp32 ? 5 : 3;
+  // against 0.411 with 2 and 0.502 with 1) and 4 for FP32 at 64 registers (0.132 ms against 0.141 with 5 at
+  // 48 registers and 0.232 with 2); more warps hide the gather latency of the products.
+  const int cap = fp32 ? 4 : 3;
   if (per > cap) per = cap;
   return per * sms;
 }
