@@ -182,6 +182,17 @@ int bogus_gpu_solve_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o
 int bogus_gpu_solve_pg_batch_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* opts, double* d_r,
                                     double* residuals, unsigned* iters);
 
+/* DualFrictionProblem::solveCadoux (Interfaces/FrictionProblem.impl.hpp:76-92, Interfaces/Cadoux.hpp:44-91): the
+ * Coulomb problem solved as up to cadoux_iters SOCQP problems u = W r + (b + COV(u_prev)), each by the
+ * Gauss-Seidel or projected-gradient minimizer with its tolerance tightened to 0.1 max(tol, min(res, 1)). r is
+ * in/out; *residual is the Coulomb error function at the result; *iters the fixed-point iterations run. The
+ * callback fires once per fixed-point iteration (0 = the initial error). The options' static_problem is ignored
+ * (inner problems use the SOC law). */
+int bogus_gpu_solve_cadoux_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* opts, double* r,
+                              unsigned cadoux_iters, double* residual, unsigned* iters);
+int bogus_gpu_solve_cadoux_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* opts, double* r,
+                              unsigned cadoux_iters, double* residual, unsigned* iters);
+
 /* Greedy coloring used by bogus_gpu_solve_gs: perm[n] (contact order, colors contiguous) and colors[ncolors+1]
  * offsets; colors must hold n + 1 ints. */
 int bogus_gpu_coloring(bogus_gpu_problem* h, int* perm, int* colors, int* ncolors);

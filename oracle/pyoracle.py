@@ -53,6 +53,13 @@ def lib():
                                        C.c_double, C.c_int, _dp, C.POINTER(C.c_uint), CALLBACK, C.c_void_p]
     L.oracle_dual_coloring.restype = C.c_int
     L.oracle_dual_coloring.argtypes = [vp, _ip, _ip]
+    L.oracle_dual_solve_cadoux_gs.restype = C.c_double
+    L.oracle_dual_solve_cadoux_gs.argtypes = [vp, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_uint,
+                                              C.c_double, C.c_int, C.c_int, C.c_int, C.c_uint, _dp,
+                                              C.POINTER(C.c_uint), CALLBACK, vp]
+    L.oracle_dual_solve_cadoux_pg.restype = C.c_double
+    L.oracle_dual_solve_cadoux_pg.argtypes = [vp, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_double,
+                                              C.c_double, C.c_int, C.c_uint, _dp, C.POINTER(C.c_uint), CALLBACK, vp]
     L.oracle_dual_solve_gs.restype = C.c_double
     L.oracle_dual_solve_gs.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_uint,
                                        C.c_double, C.c_int, C.c_int, C.c_int, _dp, C.POINTER(C.c_uint), CALLBACK,
@@ -160,6 +167,27 @@ class DualProblem:
         cb = trace._cb if trace else _NO_CB
         res = lib().oracle_dual_solve_pg(self.h, variant, int(coulomb), tol, max_iters, ls_iters, optimistic,
                                          pessimistic, armijo, int(inf_norm), r, C.byref(it), cb, None)
+        return res, r, it.value
+
+    def solve_cadoux_gs(self, r, cadoux_iters, strategy=3, tol=1e-6, max_iters=250, eval_every=25, skip_tol=1e-6,
+                        skip_iters=10, auto_reg=0.0, try_zero=False, inf_norm=False, coloring=False,
+                        trace: Trace | None = None):
+        """DualFrictionProblem::solveCadoux(gs, r, cadoux_iters): returns (residual, r, cadoux iterations run)."""
+        r = _f64(r).copy()
+        it = C.c_uint(0)
+        cb = trace._cb if trace else _NO_CB
+        res = lib().oracle_dual_solve_cadoux_gs(self.h, strategy, tol, max_iters, eval_every, skip_tol, skip_iters,
+                                                auto_reg, int(try_zero), int(inf_norm), int(coloring), cadoux_iters,
+                                                r, C.byref(it), cb, None)
+        return res, r, it.value
+
+    def solve_cadoux_pg(self, r, cadoux_iters, variant=3, tol=1e-6, max_iters=300, ls_iters=8, optimistic=1.25,
+                        pessimistic=0.5, armijo=0.5, inf_norm=False, trace: Trace | None = None):
+        r = _f64(r).copy()
+        it = C.c_uint(0)
+        cb = trace._cb if trace else _NO_CB
+        res = lib().oracle_dual_solve_cadoux_pg(self.h, variant, tol, max_iters, ls_iters, optimistic, pessimistic,
+                                                armijo, int(inf_norm), cadoux_iters, r, C.byref(it), cb, None)
         return res, r, it.value
 
     def solve_gs(self, r, coulomb=True, strategy=3, tol=1e-6, max_iters=250, eval_every=25, skip_tol=1e-6,

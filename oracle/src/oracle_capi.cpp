@@ -174,6 +174,60 @@ double oracle_dual_solve_gs(void* h, int desaxce, int strat, double tol, unsigne
   return res;
 }
 
+// DualFrictionProblem::solveCadoux (Interfaces/FrictionProblem.impl.hpp:76-92) with a GaussSeidel minimizer
+// (the coloring permutation applied around the whole fixed point, as the reference does for a permuted problem).
+double oracle_dual_solve_cadoux_gs(void* h, int strat, double tol, unsigned maxIters, unsigned evalEvery,
+                                   double skipTol, unsigned skipIters, double autoReg, int tryZero,
+                                   int useInfinityNorm, int useColoring, unsigned cadouxIters, double* r,
+                                   unsigned* iters, oracle_callback cb, void* user) {
+  auto* p = static_cast<DualProblem*>(h);
+  const int n = p->low.n;
+  GaussSeidel gs;
+  gs.tol = tol;
+  gs.maxIters = maxIters;
+  gs.evalEvery = evalEvery;
+  gs.skipTol = skipTol;
+  gs.skipIters = skipIters;
+  gs.autoRegularization = autoReg;
+  gs.tryZeroAsWell = tryZero != 0;
+  gs.useInfinityNorm = useInfinityNorm != 0;
+  std::vector<int> perm(n), colors{0, n};
+  for (int i = 0; i < n; ++i) perm[i] = i;
+  if (useColoring) greedyColoring(p->low, perm, colors);
+  const BSR plow = permuteSymmetric(p->low, perm);
+  const BSR pfull = expandSymmetric(plow);
+  const std::vector<double> pb = permuteSegments(p->b, perm, 3);
+  const std::vector<double> pmu = permuteSegments(p->mu, perm, 1);
+  std::vector<double> rv(r, r + 3 * (size_t)n);
+  std::vector<double> pr = permuteSegments(rv, perm, 3);
+  gs.perm.resize(n);
+  for (int i = 0; i < n; ++i) gs.perm[i] = i;
+  gs.colors = colors;
+  gs.setMatrix(pfull);
+  const double res = solveCadoux(gs, pfull, pb.data(), pmu.data(), strat, pr.data(), cadouxIters, wrap(cb, user), iters);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) r[3 * (size_t)perm[i] + k] = pr[3 * (size_t)i + k];
+  return res;
+}
+
+// DualFrictionProblem::solveCadoux with a ProjectedGradient minimizer.
+double oracle_dual_solve_cadoux_pg(void* h, int variant, double tol, unsigned maxIters, unsigned lsIters,
+                                   double optimistic, double pessimistic, double armijo, int useInfinityNorm,
+                                   unsigned cadouxIters, double* r, unsigned* iters, oracle_callback cb, void* user) {
+  auto* p = static_cast<DualProblem*>(h);
+  ProjectedGradient pg;
+  pg.setMatrix(p->full);
+  pg.variant = variant;
+  pg.tol = tol;
+  pg.maxIters = maxIters;
+  pg.lsIters = lsIters;
+  pg.lsOptimisticFactor = optimistic;
+  pg.lsPessimisticFactor = pessimistic;
+  pg.lsArmijoCoefficient = armijo;
+  pg.useInfinityNorm = useInfinityNorm != 0;
+  return solveCadoux(pg, p->full, p->b.data(), p->mu.data(), RevHybrid, r, cadouxIters, wrap(cb, user), iters);
+}
+
 // ---- per-contact mathematics -------------------------------------------------------------------
 double oracle_local_solve(int desaxce, int strat, const double* A, const double* b, double* x, double mu, double tol,
                           double scaling) {

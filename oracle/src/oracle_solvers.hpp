@@ -503,6 +503,53 @@ struct ProjectedGradient : SolverBase {
 };
 
 // ---------------------------------------------------------------------------------------------
+// Cadoux fixed point (Interfaces/Cadoux.hpp:44-91): a Coulomb problem solved as a sequence of SOCQP problems
+// whose right-hand side carries the De Saxce change of variable of the previous velocity:
+//   s = W r + b, res = eval(Coulomb, s, r)
+//   repeat: tol_inner = tolTighten * max(tol, min(res, 1)); s = COV(s) + b; solve SOC with rhs s from r;
+//           s = W r + b; res = eval(Coulomb, s, r); stop when res < tol
+// `m` is the inner minimizer (GaussSeidel or ProjectedGradient) set up on W; its tolerance is restored.
+// W r + b is formed as the product with b as its initial value (spmv with init).
+// ---------------------------------------------------------------------------------------------
+template <class Minimizer>
+double solveCadoux(Minimizer& m, const BSR& W, const double* b, const double* mu, int strat, double* r,
+                   unsigned cadouxIterations, const Callback& callback, unsigned* itersOut = nullptr,
+                   double tolTighten = 1.e-1) {
+  const int n = W.n;
+  const size_t n3 = 3 * (size_t)n;
+  const Law coulomb{true, strat, mu};
+  const Law soc{false, strat, mu};
+  std::vector<double> s(n3);
+  spmv(W, r, s.data(), b);
+  double res = m.eval(coulomb, s.data(), r);
+  if (callback) callback(0, res);
+  const double tol = m.tol;
+  unsigned it = 0;
+  for (; it < cadouxIterations; ++it) {
+    m.tol = tolTighten * dmax(tol, dmin(res, 1.));
+    for (int i = 0; i < n; ++i) {
+      double c[3];
+      dualityCOV(true, mu[i], &s[3 * i], c);
+      s[3 * i] = c[0];
+      s[3 * i + 1] = c[1];
+      s[3 * i + 2] = c[2];
+    }
+    for (size_t k = 0; k < n3; ++k) s[k] = s[k] + b[k];
+    m.solve(soc, s.data(), r);
+    spmv(W, r, s.data(), b);
+    res = m.eval(coulomb, s.data(), r);
+    if (callback) callback(it + 1, res);
+    if (res < tol) {
+      ++it;
+      break;
+    }
+  }
+  m.tol = tol;
+  if (itersOut) *itersOut = it;
+  return res;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Primal ADMM / AMA (ADMM.impl.hpp:54-127) with QuadraticProxOp (:29-38), as called by
 // PrimalFrictionProblem::solveWith(ADMM&, lambda, v, r) (Interfaces/PrimalFrictionProblem.cpp:61-76):
 // law SOCLaw<3, false> on 1/mu, operator H (contacts x bodies, 3 x ndof blocks), prox operator

@@ -80,7 +80,7 @@ EXPORTED = [
     "bogus_gpu_set_batch", "bogus_gpu_solve_pg_batch", "bogus_gpu_solve_pg_batch_device",
     "bogus_gpu_admm_options_default", "bogus_gpu_solve_admm", "bogus_gpu_adjoint_options_default",
     "bogus_gpu_adjoint", "bogus_gpu_adjoint_device", "bogus_gpu_adjoint_dual_lower", "bogus_gpu_adjoint_primal",
-    "bogus_gpu_add_compliance",
+    "bogus_gpu_add_compliance", "bogus_gpu_solve_cadoux_gs", "bogus_gpu_solve_cadoux_pg",
 ]
 
 
@@ -126,6 +126,10 @@ def lib():
     L.bogus_gpu_adjoint_dual_lower.argtypes = [vp, _dp]
     L.bogus_gpu_adjoint_primal.argtypes = [vp, vp, vp, vp, vp, vp]
     L.bogus_gpu_add_compliance.argtypes = [vp, _dp]
+    L.bogus_gpu_solve_cadoux_gs.argtypes = [vp, C.POINTER(GsOptions), _dp, C.c_uint, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_uint)]
+    L.bogus_gpu_solve_cadoux_pg.argtypes = [vp, C.POINTER(PgOptions), _dp, C.c_uint, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_uint)]
     L.bogus_gpu_admm_options_default.argtypes = [C.POINTER(AdmmOptions)]
     L.bogus_gpu_admm_options_default.restype = None
     L.bogus_gpu_solve_admm.argtypes = [vp, C.POINTER(AdmmOptions), C.c_double, vp, vp, _dp, _dp, _dp, _dp,
@@ -446,6 +450,29 @@ class DualFrictionProblem:
             sp = True if staticProblem is None else staticProblem
             o = solver.options(sp)
             st = lib().bogus_gpu_solve_pg(self._h, C.byref(o), r.reshape(-1), C.byref(res), C.byref(it))
+        else:
+            raise TypeError("solver must be GaussSeidel or ProjectedGradient")
+        _check(st)
+        self.last_status, self.last_iterations = st, it.value
+        return res.value
+
+    def solveCadoux(self, solver, r, cadouxIterations: int) -> float:
+        """DualFrictionProblem::solveCadoux (Interfaces/FrictionProblem.impl.hpp:76-92): the Coulomb problem as a
+        sequence of SOCQP solves with the De Saxce change of variable; r in place; returns the Coulomb error.
+        The solver's callback fires once per fixed-point iteration."""
+        if not (isinstance(r, np.ndarray) and r.dtype == np.float64 and r.flags.c_contiguous):
+            raise TypeError("r must be a C-contiguous float64 numpy array (solved in place)")
+        res = C.c_double()
+        it = C.c_uint()
+        self._bind(solver)
+        if isinstance(solver, GaussSeidel):
+            o = solver.options(True)
+            st = lib().bogus_gpu_solve_cadoux_gs(self._h, C.byref(o), r.reshape(-1), int(cadouxIterations),
+                                                 C.byref(res), C.byref(it))
+        elif isinstance(solver, ProjectedGradient):
+            o = solver.options(True)
+            st = lib().bogus_gpu_solve_cadoux_pg(self._h, C.byref(o), r.reshape(-1), int(cadouxIterations),
+                                                 C.byref(res), C.byref(it))
         else:
             raise TypeError("solver must be GaussSeidel or ProjectedGradient")
         _check(st)

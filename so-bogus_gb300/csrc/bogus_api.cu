@@ -150,6 +150,8 @@ struct bogus_gpu_problem {
   DevBuf<int> bptr, bent;
   DevBuf<double> a_prox, a_f, a_w, a_mu, a_invmu, a_x, a_r, a_ut, a_z, a_zacc, a_zprev, a_yprev;
   DevBuf<ADMMOut> admm_out;
+  // Cadoux fixed point: the original right-hand side while the inner solves use COV(u) + b
+  DevBuf<double> cad_b;
   // adjoint: per-contact basis, CG vectors, the last solution r and s = dL/db (device and host copies)
   DevBuf<double> adj_V, adj_Pc, adj_D, adj_K, adj_P, adj_R, adj_Z, adj_Dir, adj_Y, adj_Q, adj_S, adj_dmu, adj_r, adj_g;
   DevBuf<AdjOut> adj_out;
@@ -749,6 +751,7 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   h->bptr.release();
   h->bent.release();
   h->admm_out.release();
+  h->cad_b.release();
   for (auto* b : {&h->adj_V, &h->adj_Pc, &h->adj_D, &h->adj_K, &h->adj_P, &h->adj_R, &h->adj_Z, &h->adj_Dir,
                   &h->adj_Y, &h->adj_Q, &h->adj_S, &h->adj_dmu, &h->adj_r, &h->adj_g})
     b->release();
@@ -956,38 +959,21 @@ int bogus_gpu_coloring(bogus_gpu_problem* h, int* perm, int* colors, int* ncolor
   return BOGUS_GPU_OK;
 }
 
-int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* r, double* residual,
-                       unsigned* iters) {
-  if (int e = check_handle(h)) return e;
+}  // extern "C"
+
+namespace {
+
+int check_gs_options(const bogus_gpu_gs_options* o) {
   if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
-  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
   if (o->eval_every == 0) return fail(BOGUS_GPU_BAD_INPUT, "eval_every must be >= 1");
   if (o->local_strategy < 0 || o->local_strategy > 3) return fail(BOGUS_GPU_BAD_INPUT, "unknown local strategy");
-  if (int e = set_device(h)) return e;
-  const int n = h->W.n;
-  const size_t n3 = 3 * (size_t)n;
-  if (n == 0) {
-    if (residual) *residual = 0.0;
-    if (iters) *iters = 0;
-    return BOGUS_GPU_OK;
-  }
-  if (int e = check_finite(r, n3, "r")) return e;
-  if (int e = prepare_gs(h, o->auto_regularization, o->use_coloring ? 1 : 0)) return e;
+  return BOGUS_GPU_OK;
+}
+
+GSArgs gs_args(bogus_gpu_problem* h, const bogus_gpu_gs_options* o) {
   GSCache& g = h->gs;
-  cudaStream_t s = h->stream;
-  h->last_launches = 0;
-  // r in the permuted (color-contiguous) order
-  std::vector<double> pr(n3);
-  for (int i = 0; i < n; ++i)
-    for (int k = 0; k < 3; ++k) pr[3 * (size_t)i + k] = r[3 * (size_t)g.perm[i] + k];
-  BG_CUDA(cudaMemcpyAsync(g.x.p, pr.data(), sizeof(double) * n3, cudaMemcpyHostToDevice, s));
-  const int ntiles = (n + kGSTile - 1) / kGSTile;
-  BG_CUDA(cudaMemsetAsync(g.tile_max.p, 0, sizeof(unsigned long long) * 2 * ntiles, s));
-  BG_CUDA(cudaMemsetAsync(g.ndx_ref.p, 0, sizeof(double) * 2, s));
-  BG_CUDA(cudaMemsetAsync(g.skip.p, 0, n, s));
-  BG_CUDA(cudaEventRecord(h->ev0, s));
   GSArgs a{};
-  a.n = n;
+  a.n = h->W.n;
   a.rowptr = g.rowptr.p;
   a.col = g.col.p;
   a.val = g.val.p;
@@ -1006,6 +992,22 @@ int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, doub
   a.order = g.order.p;
   a.desaxce = o->static_problem ? 0 : 1;
   a.strat = o->local_strategy;
+  return a;
+}
+
+// GaussSeidel::solve (GaussSeidel.impl.hpp:144-205) on the prepared (permuted) problem, rhs g.b, from g.x;
+// leaves the result in g.x and the (iteration, error) pairs in *trace.
+int run_gs_core(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* residual, unsigned* iters,
+                std::vector<std::pair<unsigned, double>>* trace, bool* converged_out) {
+  GSCache& g = h->gs;
+  cudaStream_t s = h->stream;
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  const int ntiles = (n + kGSTile - 1) / kGSTile;
+  BG_CUDA(cudaMemsetAsync(g.tile_max.p, 0, sizeof(unsigned long long) * 2 * ntiles, s));
+  BG_CUDA(cudaMemsetAsync(g.ndx_ref.p, 0, sizeof(double) * 2, s));
+  BG_CUDA(cudaMemsetAsync(g.skip.p, 0, n, s));
+  const GSArgs a = gs_args(h, o);
   const bool desaxce = !o->static_problem;
   const bool use_inf = o->use_infinity_norm != 0;
   // initial evaluation and tryZero (GaussSeidel.impl.hpp:152-167)
@@ -1036,8 +1038,7 @@ int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, doub
       BG_CUDA(cudaMemcpyAsync(g.x.p, g.xbest.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
     }
   }
-  std::vector<std::pair<unsigned, double>> trace;
-  trace.push_back({0u, err_best});
+  if (trace) trace->push_back({0u, err_best});
   const double abs_skip_tol = dmin(o->skip_tol, o->tol);
   const int abs_skip_iters = (int)dmin((double)o->skip_iters, (double)(unsigned)std::sqrt((double)n));
   // settings baked into the captured sweeps
@@ -1064,7 +1065,7 @@ int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, doub
         err_best = err;
         has_best = true;
       }
-      trace.push_back({it, err});
+      if (trace) trace->push_back({it, err});
       if (err < o->tol) {
         converged = true;
         break;
@@ -1073,19 +1074,215 @@ int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, doub
       h->last_launches += 1;
     }
   }
-  const double* result = g.x.p;
-  if (it > o->max_iters && has_best) result = g.xbest.p;
-  BG_CUDA(cudaEventRecord(h->ev1, s));
-  BG_CUDA(cudaMemcpyAsync(pr.data(), result, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
-  BG_CUDA(cudaStreamSynchronize(s));
-  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
-  for (int i = 0; i < n; ++i)
-    for (int k = 0; k < 3; ++k) r[3 * (size_t)g.perm[i] + k] = pr[3 * (size_t)i + k];
+  if (it > o->max_iters && has_best)
+    BG_CUDA(cudaMemcpyAsync(g.x.p, g.xbest.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
   if (residual) *residual = err_best;
   if (iters) *iters = it > o->max_iters ? o->max_iters : it;
+  if (converged_out) *converged_out = converged;
+  return BOGUS_GPU_OK;
+}
+
+// r (caller's order, host) <-> g.x (sweep order, device)
+int gs_load_x(bogus_gpu_problem* h, const double* r) {
+  GSCache& g = h->gs;
+  const int n = h->W.n;
+  std::vector<double> pr(3 * (size_t)n);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) pr[3 * (size_t)i + k] = r[3 * (size_t)g.perm[i] + k];
+  BG_CUDA(cudaMemcpyAsync(g.x.p, pr.data(), sizeof(double) * pr.size(), cudaMemcpyHostToDevice, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  return BOGUS_GPU_OK;
+}
+int gs_store_x(bogus_gpu_problem* h, double* r) {
+  GSCache& g = h->gs;
+  const int n = h->W.n;
+  std::vector<double> pr(3 * (size_t)n);
+  BG_CUDA(cudaMemcpyAsync(pr.data(), g.x.p, sizeof(double) * pr.size(), cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) r[3 * (size_t)g.perm[i] + k] = pr[3 * (size_t)i + k];
+  return BOGUS_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* r, double* residual,
+                       unsigned* iters) {
+  if (int e = check_handle(h)) return e;
+  if (int e = check_gs_options(o)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (int e = set_device(h)) return e;
+  const int n = h->W.n;
+  if (n == 0) {
+    if (residual) *residual = 0.0;
+    if (iters) *iters = 0;
+    return BOGUS_GPU_OK;
+  }
+  if (int e = check_finite(r, 3 * (size_t)n, "r")) return e;
+  if (int e = prepare_gs(h, o->auto_regularization, o->use_coloring ? 1 : 0)) return e;
+  h->last_launches = 0;
+  if (int e = gs_load_x(h, r)) return e;
+  BG_CUDA(cudaEventRecord(h->ev0, h->stream));
+  std::vector<std::pair<unsigned, double>> trace;
+  bool converged = false;
+  if (int e = run_gs_core(h, o, residual, iters, &trace, &converged)) return e;
+  BG_CUDA(cudaEventRecord(h->ev1, h->stream));
+  if (int e = gs_store_x(h, r)) return e;
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
   if (h->callback)
     for (auto& t : trace) h->callback(t.first, t.second, h->callback_user);
   return converged ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
+}
+
+// ---- Cadoux fixed point (Interfaces/Cadoux.hpp:44-91, DualFrictionProblem::solveCadoux,
+//      FrictionProblem.impl.hpp:76-92) -----------------------------------------------------------------
+int bogus_gpu_solve_cadoux_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* r, unsigned cadoux_iters,
+                              double* residual, unsigned* iters) {
+  if (int e = check_handle(h)) return e;
+  if (int e = check_gs_options(o)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (int e = set_device(h)) return e;
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  if (n == 0) {
+    if (residual) *residual = 0.0;
+    if (iters) *iters = 0;
+    return BOGUS_GPU_OK;
+  }
+  if (int e = check_finite(r, n3, "r")) return e;
+  if (int e = prepare_gs(h, o->auto_regularization, o->use_coloring ? 1 : 0)) return e;
+  GSCache& g = h->gs;
+  cudaStream_t s = h->stream;
+  h->last_launches = 0;
+  if (int e = gs_load_x(h, r)) return e;
+  BG_CUDA(h->cad_b.ensure(n3));
+  BG_CUDA(cudaMemcpyAsync(h->cad_b.p, g.b.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  bogus_gpu_gs_options oi = *o;
+  oi.static_problem = 1;  // inner problems: SOCLaw<3, false>
+  const GSArgs a = gs_args(h, &oi);
+  const bool use_inf = o->use_infinity_norm != 0;
+  std::vector<std::pair<unsigned, double>> trace;
+  double res = 0;
+  int st = gs_eval(h, a, g.x.p, h->cad_b.p, true, use_inf, &res);  // Coulomb error at (r, W r + b)
+  trace.push_back({0u, res});
+  const double tol = o->tol;
+  unsigned it = 0;
+  for (; st == BOGUS_GPU_OK && it < cadoux_iters; ++it) {
+    oi.tol = 1.e-1 * dmax(tol, dmin(res, 1.));
+    if (launch_cadoux_rhs(n, g.y.p, g.mu.p, h->cad_b.p, g.b.p, s) != cudaSuccess) {
+      st = fail(BOGUS_GPU_CUDA_ERROR, "Cadoux right-hand side");
+      break;
+    }
+    h->last_launches += 1;
+    st = run_gs_core(h, &oi, nullptr, nullptr, nullptr, nullptr);
+    if (st != BOGUS_GPU_OK) break;
+    st = gs_eval(h, a, g.x.p, h->cad_b.p, true, use_inf, &res);
+    trace.push_back({it + 1, res});
+    if (res < tol) {
+      ++it;
+      break;
+    }
+  }
+  BG_CUDA(cudaMemcpyAsync(g.b.p, h->cad_b.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+  if (st != BOGUS_GPU_OK) return st;
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  if (int e = gs_store_x(h, r)) return e;
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  if (residual) *residual = res;
+  if (iters) *iters = it;
+  if (h->callback)
+    for (auto& t : trace) h->callback(t.first, t.second, h->callback_user);
+  return res < tol ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
+}
+
+int bogus_gpu_solve_cadoux_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, unsigned cadoux_iters,
+                              double* residual, unsigned* iters) {
+  if (int e = check_handle(h)) return e;
+  if (int e = check_pg_options(o)) return e;
+  if (o->mixed_precision) return fail(BOGUS_GPU_BAD_INPUT, "the Cadoux fixed point runs its inner solves in FP64");
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (int e = set_device(h)) return e;
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  if (n == 0) {
+    if (residual) *residual = 0.0;
+    if (iters) *iters = 0;
+    return BOGUS_GPU_OK;
+  }
+  if (int e = check_finite(r, n3, "r")) return e;
+  if (int e = ensure_pg_work(h, o->max_iters)) return e;
+  cudaStream_t s = h->stream;
+  const int C = (n + 31) / 32;
+  BG_CUDA(h->cad_b.ensure(n3));
+  BG_CUDA(h->vx.ensure(n3));
+  BG_CUDA(h->vy.ensure(n3));
+  BG_CUDA(h->chunk.ensure(C + 1));
+  BG_CUDA(h->scalar.ensure(2));
+  BG_CUDA(cudaMemcpyAsync(h->cad_b.p, h->b.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(h->vx.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  const bool use_inf = o->use_infinity_norm != 0;
+  // Coulomb error at (x, W x + b) with the solver's scalings
+  auto coulomb_error = [&](double* err) -> int {
+    BG_CUDA(launch_spmv(h->W, h->vx.p, h->cad_b.p, h->vy.p, s));
+    BG_CUDA(launch_eval_chunks(n, h->vx.p, h->vy.p, h->mu.p, h->scaling.p, true, use_inf, h->chunk.p, s));
+    BG_CUDA(launch_combine(h->chunk.p, C, use_inf, use_inf ? 0.0 : (double)(1 + n), h->scalar.p, s));
+    BG_CUDA(cudaMemcpyAsync(err, h->scalar.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+    return BOGUS_GPU_OK;
+  };
+  const bogus_gpu_callback cb = h->callback;
+  h->callback = nullptr;  // the inner solves report nothing; the fixed point reports its own iterations
+  std::vector<std::pair<unsigned, double>> trace;
+  double res = 0;
+  float total_ms = 0.f;
+  unsigned launches = 3;
+  int st = coulomb_error(&res);
+  trace.push_back({0u, res});
+  bogus_gpu_pg_options oi = *o;
+  oi.static_problem = 1;  // inner problems: SOCLaw<3, false>
+  const double tol = o->tol;
+  unsigned it = 0;
+  for (; st == BOGUS_GPU_OK && it < cadoux_iters; ++it) {
+    oi.tol = 1.e-1 * dmax(tol, dmin(res, 1.));
+    if (launch_cadoux_rhs(n, h->vy.p, h->mu.p, h->cad_b.p, h->b.p, s) != cudaSuccess ||
+        cudaMemcpyAsync(h->X.p, h->vx.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+      st = fail(BOGUS_GPU_CUDA_ERROR, "Cadoux right-hand side");
+      break;
+    }
+    const double* best = nullptr;
+    const int ps = run_pg(h, &oi, nullptr, nullptr, &best);
+    if (ps != BOGUS_GPU_OK && ps != BOGUS_GPU_NOT_CONVERGED) {
+      st = ps;
+      break;
+    }
+    total_ms += h->last_ms;
+    launches += h->last_launches + 4;
+    if (cudaMemcpyAsync(h->vx.p, best, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+      st = fail(BOGUS_GPU_CUDA_ERROR, "Cadoux iterate copy");
+      break;
+    }
+    st = coulomb_error(&res);
+    trace.push_back({it + 1, res});
+    if (res < tol) {
+      ++it;
+      break;
+    }
+  }
+  h->callback = cb;
+  BG_CUDA(cudaMemcpyAsync(h->b.p, h->cad_b.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+  if (st != BOGUS_GPU_OK) return st;
+  BG_CUDA(cudaMemcpyAsync(r, h->vx.p, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  h->last_ms = total_ms;
+  h->last_launches = launches;
+  if (residual) *residual = res;
+  if (iters) *iters = it;
+  if (h->callback)
+    for (auto& t : trace) h->callback(t.first, t.second, h->callback_user);
+  return res < tol ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
 }
 
 // ---- primal data and Delassus assembly ---------------------------------------------------------------

@@ -95,6 +95,7 @@ cudaError_t launch_combine(const double* chunk, int nchunks, bool is_max, double
                            cudaStream_t s);
 cudaError_t launch_diag_and_scaling(const DevBSR& W, double* scaling, cudaStream_t s);
 cudaError_t launch_add(int m, const double* a, const double* b, double* y, cudaStream_t s);
+cudaError_t launch_cadoux_rhs(int n, const double* y, const double* mu, const double* b, double* out, cudaStream_t s);
 
 // Persistent solvers (kernels_pg.cu)
 cudaError_t launch_pg_persistent(const PGArgs& a, int grid, cudaStream_t s);

@@ -68,6 +68,25 @@ cudaError_t launch_interleave(const DevBSR& W, const long long* slot0, int* icol
   return cudaGetLastError();
 }
 
+// Right-hand side of an inner solve of the Cadoux fixed point (Interfaces/Cadoux.hpp:73-76): out_i = COV(y_i) + b_i
+// with SOCLaw::dualityCOV, COV(y) = (mu |y_T|, 0, 0).
+__global__ void k_cadoux_rhs(int n, const double* __restrict__ y, const double* __restrict__ mu,
+                             const double* __restrict__ b, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double yy[3] = {y[3 * i], y[3 * i + 1], y[3 * i + 2]};
+  const double s0 = duality_cov(true, mu[i], yy);
+  out[3 * i] = s0 + b[3 * i];
+  out[3 * i + 1] = 0.0 + b[3 * i + 1];
+  out[3 * i + 2] = 0.0 + b[3 * i + 2];
+}
+
+cudaError_t launch_cadoux_rhs(int n, const double* y, const double* mu, const double* b, double* out, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_cadoux_rhs<<<(n + 255) / 256, 256, 0, s>>>(n, y, mu, b, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_spmv(const DevBSR& W, const double* x, const double* init, double* y, cudaStream_t s) {
   if (W.n == 0) return cudaSuccess;
   const int chunks = (W.n + 31) / 32;

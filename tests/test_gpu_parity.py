@@ -136,6 +136,48 @@ def test_mixed_precision_converges_to_fp64_residual(bg, oracle, c1, static):
     assert res3 == res3_o and np.array_equal(r3, r3_o)
 
 
+@pytest.mark.parametrize("minimizer", ["gs", "gs_colored", "pg"])
+def test_cadoux_bitwise(bg, oracle, c1, minimizer):
+    """DualFrictionProblem::solveCadoux with each minimizer: iterate, Coulomb error, fixed-point iteration count
+    and the per-iteration trace equal the oracle's."""
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    trace_gpu = []
+    tr = oracle.Trace()
+    r0 = np.zeros(3 * d.n)
+    if minimizer == "pg":
+        solver = bg.ProjectedGradient()
+        solver.setTol(1e-8)
+        solver.setMaxIters(200)
+        solver.callback().connect(lambda it, res: trace_gpu.append((it, res)))
+        r = r0.copy()
+        res = D.solveCadoux(solver, r, 6)
+        res_o, r_o, it_o = O.solve_cadoux_pg(r0, 6, tol=1e-8, max_iters=200, trace=tr)
+    else:
+        solver = bg.GaussSeidel()
+        solver.setTol(1e-8)
+        solver.setMaxIters(100)
+        solver.doTryZeroAsWell(False)
+        solver.coloring().update(minimizer == "gs_colored")
+        solver.callback().connect(lambda it, res: trace_gpu.append((it, res)))
+        r = r0.copy()
+        res = D.solveCadoux(solver, r, 6)
+        res_o, r_o, it_o = O.solve_cadoux_gs(r0, 6, tol=1e-8, max_iters=100, coloring=minimizer == "gs_colored",
+                                             trace=tr)
+    assert res == res_o
+    assert D.last_iterations == it_o
+    assert np.array_equal(r, r_o)
+    assert trace_gpu == tr.items
+    # the problem's own right-hand side is intact afterwards: a plain solve still matches the oracle
+    pg = bg.ProjectedGradient()
+    pg.setMaxIters(50)
+    r2 = np.zeros(3 * d.n)
+    res2 = D.solveWith(pg, r2)
+    res2_o, r2_o, _ = O.solve_pg(np.zeros(3 * d.n), variant=3, coulomb=False, max_iters=50)
+    assert res2 == res2_o and np.array_equal(r2, r2_o)
+
+
 def test_mixed_precision_rejects_zero_refinement(bg, c1):
     d, rp, cl, vl = c1
     D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)

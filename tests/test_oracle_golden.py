@@ -161,6 +161,21 @@ def test_small_friction_projected_gradient(oracle, golden, variant):
     assert res < 1e-8
 
 
+# ---- Cadoux fixed point (Interfaces/Cadoux.hpp:44-91); the reference has no test of its own, so the result is
+# held to the Coulomb solution of tests/SmallFrictionPb.hpp (the one GaussSeidel.cpp checks) ------------------
+@pytest.mark.parametrize("minimizer", ["gs", "pg"])
+def test_small_friction_cadoux_reaches_the_coulomb_solution(oracle, golden, minimizer):
+    s = golden["small_friction_pb"]
+    D = oracle.DualProblem(*small_friction_dual(golden, oracle))
+    if minimizer == "gs":
+        res, r, it = D.solve_cadoux_gs(np.ones(6), 50, tol=1e-10, max_iters=1000)
+    else:
+        res, r, it = D.solve_cadoux_pg(np.ones(6), 50, tol=1e-10, max_iters=3000)
+    assert res < 1e-10 and it <= 50
+    assert isApprox(s["sol"], r, s["sol_rel_tol"])
+    assert D.eval(r, coulomb=True) < 1e-9
+
+
 # ---- tests/ADMM.cpp:16-60 (primal AMA with lambda = 0, ADMM with lambda = 0.1) ---------------------------
 def _small_primal(oracle, golden):
     s = golden["small_friction_pb"]
