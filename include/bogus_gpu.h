@@ -299,6 +299,52 @@ int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int* d_rowptr,
                                const bogus_gpu_pg_options* opts, double* d_r, double* residual, unsigned* iters,
                                void* stream);
 
+/* ---- MecheFrictionProblem facade (Interfaces/MecheInterface.hpp:40-170, MecheInterface.cpp:97-367) ---------
+ * The raw-pointer caller of the reference: a primal problem in world coordinates (contact frames E), solved
+ * with the dual assembled on the device. Per handle; bogus_gpu_meche_from_primal replaces the handle's
+ * primal and dual problems. */
+typedef enum bogus_gpu_meche_algorithm { /* MecheFrictionProblem::Algorithm */
+  BOGUS_GPU_MECHE_GAUSS_SEIDEL = 0,
+  BOGUS_GPU_MECHE_PROJECTED_GRADIENT = 1,
+  BOGUS_GPU_MECHE_MATRIX_FREE_GAUSS_SEIDEL = 2, /* not available on the GPU: BAD_INPUT */
+  BOGUS_GPU_MECHE_ADMM = 3,
+  BOGUS_GPU_MECHE_DUAL_AMA = 4                  /* not available on the GPU: BAD_INPUT */
+} bogus_gpu_meche_algorithm;
+
+/* MecheFrictionProblem::Options (MecheInterface.hpp:44-69) and its defaults (MecheInterface.cpp:51-63). */
+typedef struct bogus_gpu_meche_options {
+  int max_threads;            /* 0; Gauss-Seidel uses the coloring order when != 1 and gs_coloring */
+  unsigned max_iters;         /* 0: the solver's default */
+  unsigned cadoux_iters;      /* 0; > 0 with a non-static problem: the Cadoux fixed point */
+  double tolerance;           /* 0: the solver's default */
+  int use_infinity_norm;      /* 0 */
+  int algorithm;              /* bogus_gpu_meche_algorithm, Gauss-Seidel */
+  double gs_regularization;   /* 0: GaussSeidel::setAutoRegularization */
+  int gs_coloring;            /* 0 */
+  int gs_skip_iters;          /* -1: the solver's default */
+  int try_zero_as_well;       /* 1 */
+  int pg_variant;             /* bogus_gpu_pg_variant, SPG */
+  double admm_proj_step_size; /* 1 */
+  double admm_fp_step_size;   /* 1e-3 (DualAMA only) */
+} bogus_gpu_meche_options;
+void bogus_gpu_meche_options_default(bogus_gpu_meche_options* opts);
+
+/* MecheFrictionProblem::fromPrimal: nobj objects with ndof[k] (1..12) degrees of freedom and column-major mass
+ * matrices mass[k]; f: sum of ndof entries (NULL: 0); n contacts with friction mu, frames E ((3n x 3) column-
+ * major: the n local-basis blocks, world to local), w (3n, world), objects objA[i] and objB[i] (-1: external)
+ * and column-major 3 x ndof Jacobian blocks HA[i], HB[i] in world coordinates. The mass blocks are inverted and
+ * H = E^T HA / -E^T HB (E^T (HA - HB) when objA[i] == objB[i]) is formed on the device. */
+int bogus_gpu_meche_from_primal(bogus_gpu_problem* h, unsigned nobj, const unsigned* ndof, const double* const* mass,
+                                const double* f, unsigned n, const double* mu, const double* E, const double* w,
+                                const int* objA, const int* objB, const double* const* HA, const double* const* HB);
+
+/* MecheFrictionProblem::solve(r, v, options, staticProblem, problemRegularization): r (3n, world) is in/out;
+ * v (sum of ndof; NULL: not returned) receives M^-1 (H^T r - f), or is ADMM's warm start and result. The dual,
+ * with problem_regularization added to W's diagonal, is computed at the first Gauss-Seidel or projected-gradient
+ * solve after fromPrimal and kept, as in the reference. *residual: the solver's error. */
+int bogus_gpu_meche_solve(bogus_gpu_problem* h, double* r, double* v, const bogus_gpu_meche_options* opts,
+                          int static_problem, double problem_regularization, double* residual);
+
 #ifdef __cplusplus
 }
 #endif

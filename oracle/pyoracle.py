@@ -60,6 +60,14 @@ def lib():
     L.oracle_dual_solve_cadoux_pg.restype = C.c_double
     L.oracle_dual_solve_cadoux_pg.argtypes = [vp, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_double,
                                               C.c_double, C.c_int, C.c_uint, _dp, C.POINTER(C.c_uint), CALLBACK, vp]
+    L.oracle_meche_create.restype = vp
+    L.oracle_meche_create.argtypes = [C.c_int, np.ctypeslib.ndpointer(dtype=np.uint32), _dp, _dp, C.c_int, _dp, _dp,
+                                      _dp, _ip, _ip, _dp, _dp]
+    L.oracle_meche_destroy.argtypes = [vp]
+    L.oracle_meche_solve.restype = C.c_double
+    L.oracle_meche_solve.argtypes = [vp, _dp, vp, C.c_int, C.c_uint, C.c_uint, C.c_double, C.c_int, C.c_int,
+                                     C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double,
+                                     CALLBACK, vp]
     L.oracle_dual_solve_gs.restype = C.c_double
     L.oracle_dual_solve_gs.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_uint,
                                        C.c_double, C.c_int, C.c_int, C.c_int, _dp, C.POINTER(C.c_uint), CALLBACK,
@@ -279,3 +287,47 @@ class PrimalProblem:
                                              _f64(w).reshape(-1), tol, max_iters, step, int(accelerated),
                                              int(inf_norm), v, r, C.byref(it), cb, None)
         return res, v, r, it.value
+
+
+class MecheProblem:
+    """MecheFrictionProblem::fromPrimal / solve (Interfaces/MecheInterface.cpp) restated (oracle/src/oracle_meche.hpp).
+    mass: list of (ndof, ndof) arrays; HA / HB: lists of (3, ndof) arrays (HB[i] None when objB[i] == -1);
+    E: (n, 3, 3) frames (rows: world -> local, E[i][a][b] as the reference's E block); f packed by body; w (3n)
+    in world coordinates."""
+
+    def __init__(self, mass, f, mu, E, w, objA, objB, HA, HB):
+        ndof = np.array([m.shape[0] for m in mass], np.uint32)
+        n = len(objA)
+        Ecm = np.zeros((3, 3 * n))  # the reference's (3n x 3) column-major layout
+        E = np.asarray(E, np.float64)
+        for i in range(n):
+            Ecm[:, 3 * i:3 * i + 3] = E[i].T
+        self.h = lib().oracle_meche_create(len(mass), ndof, np.concatenate([np.asarray(m, np.float64).T.ravel()
+                                                                             for m in mass]),
+                                           _f64(f).reshape(-1), n, _f64(mu), Ecm.ravel(), _f64(w).reshape(-1),
+                                           _i32(objA), _i32(objB),
+                                           np.concatenate([np.asarray(h, np.float64).T.ravel() for h in HA]),
+                                           np.concatenate([np.zeros(0)] + [np.asarray(h, np.float64).T.ravel()
+                                                                           for h in HB if h is not None]))
+        if not self.h:
+            raise ValueError("singular mass block")
+        self.m = int(ndof.sum())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.oracle_meche_destroy(self.h)
+            self.h = None
+
+    def solve(self, r, with_v=True, max_threads=0, max_iters=0, cadoux_iters=0, tolerance=0.0, inf_norm=False,
+              algorithm=0, gs_regularization=0.0, gs_coloring=False, gs_skip_iters=-1, try_zero=True, pg_variant=4,
+              admm_step=1.0, static=False, regularization=0.0, v=None, trace: Trace | None = None):
+        r = _f64(r).copy()
+        vv = None
+        if with_v:
+            vv = np.zeros(self.m) if v is None else _f64(v).copy()
+        cb = trace._cb if trace else _NO_CB
+        res = lib().oracle_meche_solve(self.h, r, None if vv is None else vv.ctypes.data_as(C.c_void_p), max_threads,
+                                       max_iters, cadoux_iters, tolerance, int(inf_norm), algorithm, gs_regularization,
+                                       int(gs_coloring), gs_skip_iters, int(try_zero), pg_variant, admm_step,
+                                       int(static), regularization, cb, None)
+        return res, r, vv

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "oracle_math.hpp"
+#include "oracle_meche.hpp"
 #include "oracle_solvers.hpp"
 #include "oracle_sparse.hpp"
 
@@ -226,6 +227,148 @@ double oracle_dual_solve_cadoux_pg(void* h, int variant, double tol, unsigned ma
   pg.lsArmijoCoefficient = armijo;
   pg.useInfinityNorm = useInfinityNorm != 0;
   return solveCadoux(pg, p->full, p->b.data(), p->mu.data(), RevHybrid, r, cadouxIters, wrap(cb, user), iters);
+}
+
+// ---- MecheFrictionProblem (Interfaces/MecheInterface.cpp) -------------------------------------------
+// mass: the bodies' column-major blocks one after the other; HA / HB: the contacts' column-major 3 x ndof blocks
+// one after the other (HB: none for objB == -1, 3 x ndof[objA] when objB == objA). Returns null on a singular
+// mass block.
+void* oracle_meche_create(int nobj, const unsigned* ndof, const double* mass, const double* f, int n,
+                          const double* mu, const double* E, const double* w, const int* objA, const int* objB,
+                          const double* HA, const double* HB) {
+  std::vector<const double*> mp(nobj), hap(n), hbp(n);
+  size_t off = 0;
+  for (int k = 0; k < nobj; ++k) {
+    mp[k] = mass + off;
+    off += (size_t)ndof[k] * ndof[k];
+  }
+  size_t oa = 0, ob = 0;
+  for (int i = 0; i < n; ++i) {
+    hap[i] = HA + oa;
+    oa += 3 * (size_t)ndof[objA[i]];
+    hbp[i] = HB + ob;
+    if (objB[i] >= 0) ob += 3 * (size_t)ndof[objB[i] == objA[i] ? objA[i] : objB[i]];
+  }
+  auto* m = new Meche();
+  if (!mecheFromPrimal(*m, nobj, ndof, mp.data(), f, n, mu, E, w, objA, objB, hap.data(), hbp.data())) {
+    delete m;
+    return nullptr;
+  }
+  return m;
+}
+void oracle_meche_destroy(void* h) { delete static_cast<Meche*>(h); }
+
+// MecheFrictionProblem::solve(r, v, options, staticProblem, problemRegularization) (:226-367); algorithm 0 GS,
+// 1 PG, 3 ADMM. v: unpadded (sum of ndof), may be null. Returns the solver's residual.
+double oracle_meche_solve(void* h, double* r, double* v, int maxThreads, unsigned maxIters, unsigned cadouxIters,
+                          double tolerance, int useInfinityNorm, int algorithm, double gsRegularization,
+                          int gsColoring, int gsSkipIters, int tryZeroAsWell, int pgVariant, double admmProjStepSize,
+                          int staticProblem, double problemRegularization, oracle_callback cb, void* user) {
+  auto* m = static_cast<Meche*>(h);
+  const Primal& P = m->P;
+  const int n = P.ncontacts, d = P.ndof;
+  const size_t n3 = 3 * (size_t)n, md = (size_t)P.nbodies * d;
+  std::vector<double> rl(n3), wl(n3);
+  for (int i = 0; i < n; ++i) {
+    frameT(&m->E[9 * (size_t)i], r + 3 * i, &rl[3 * (size_t)i]);
+    frameT(&m->E[9 * (size_t)i], &m->w[3 * (size_t)i], &wl[3 * (size_t)i]);
+  }
+  std::vector<double> vp(md, 0.0);
+  double res = -1;
+  const Callback callback = wrap(cb, user);
+  if (algorithm == 3) {
+    // v given (unpadded) or M^-1 (H^T r - f)
+    if (v) {
+      size_t off = 0;
+      for (int k = 0; k < P.nbodies; ++k) {
+        for (int a = 0; a < m->ndof[k]; ++a) vp[(size_t)k * d + a] = v[off + a];
+        off += m->ndof[k];
+      }
+    } else {
+      mecheVelocity(*m, rl.data(), vp.data());
+    }
+    ADMMSolver s;
+    s.P = &P;
+    s.stepSize = admmProjStepSize;
+    if (tolerance != 0.) s.tol = tolerance;
+    if (maxIters != 0) s.maxIters = maxIters;
+    s.useInfinityNorm = useInfinityNorm != 0;
+    s.callback = callback;
+    std::vector<double> invMu(n);
+    for (int i = 0; i < n; ++i) invMu[i] = 1. / m->mu[i];
+    res = s.solve(invMu.data(), P.minv, 0., m->f.data(), wl.data(), vp.data(), rl.data());
+  } else {
+    if (!m->hasDual) {
+      m->low = assembleW(P);
+      if (problemRegularization > 0.)
+        for (int i = 0; i < n; ++i) {
+          double* B = &m->low.val[9 * (size_t)(m->low.rowptr[i + 1] - 1)];
+          B[0] = B[0] + problemRegularization;
+          B[4] = B[4] + problemRegularization;
+          B[8] = B[8] + problemRegularization;
+        }
+      m->full = expandSymmetric(m->low);
+      m->b = assembleB(P, m->f.data(), wl.data());
+      m->hasDual = true;
+    }
+    const bool cadoux = !staticProblem && cadouxIters > 0;
+    if (algorithm == 1) {
+      ProjectedGradient pg;
+      pg.setMatrix(m->full);
+      if (tolerance != 0.) pg.tol = tolerance;
+      if (maxIters != 0) pg.maxIters = maxIters;
+      pg.useInfinityNorm = useInfinityNorm != 0;
+      pg.variant = pgVariant;
+      if (!cadoux) {
+        pg.callback = callback;
+        Law law{staticProblem == 0, RevHybrid, m->mu.data()};
+        res = pg.solve(law, m->b.data(), rl.data());
+      } else {
+        res = solveCadoux(pg, m->full, m->b.data(), m->mu.data(), RevHybrid, rl.data(), cadouxIters, callback);
+      }
+    } else {
+      GaussSeidel gs;
+      if (tolerance != 0.) gs.tol = tolerance;
+      if (maxIters != 0) gs.maxIters = maxIters;
+      if (gsSkipIters >= 0) gs.skipIters = (unsigned)gsSkipIters;
+      gs.autoRegularization = gsRegularization;
+      gs.useInfinityNorm = useInfinityNorm != 0;
+      const bool useColoring = maxThreads != 1 && gsColoring;
+      std::vector<int> perm(n), colors{0, n};
+      for (int i = 0; i < n; ++i) perm[i] = i;
+      if (useColoring) greedyColoring(m->low, perm, colors);
+      const BSR plow = permuteSymmetric(m->low, perm);
+      const BSR pfull = expandSymmetric(plow);
+      const std::vector<double> pb = permuteSegments(m->b, perm, 3);
+      const std::vector<double> pmu = permuteSegments(m->mu, perm, 1);
+      std::vector<double> pr = permuteSegments(rl, perm, 3);
+      gs.perm.resize(n);
+      for (int i = 0; i < n; ++i) gs.perm[i] = i;
+      gs.colors = colors;
+      gs.setMatrix(pfull);
+      if (!cadoux) {
+        gs.tryZeroAsWell = tryZeroAsWell != 0;
+        gs.callback = callback;
+        Law law{staticProblem == 0, RevHybrid, pmu.data()};
+        res = gs.solve(law, pb.data(), pr.data());
+      } else {
+        gs.tryZeroAsWell = false;
+        res = solveCadoux(gs, pfull, pb.data(), pmu.data(), RevHybrid, pr.data(), cadouxIters, callback);
+      }
+      for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) rl[3 * (size_t)perm[i] + k] = pr[3 * (size_t)i + k];
+    }
+    if (v) mecheVelocity(*m, rl.data(), vp.data());
+  }
+  if (v) {
+    size_t off = 0;
+    for (int k = 0; k < P.nbodies; ++k) {
+      for (int a = 0; a < m->ndof[k]; ++a) v[off + a] = vp[(size_t)k * d + a];
+      off += m->ndof[k];
+    }
+  }
+  for (int i = 0; i < n; ++i) frame(&m->E[9 * (size_t)i], &rl[3 * (size_t)i], r + 3 * i);
+  return res;
 }
 
 // ---- per-contact mathematics -------------------------------------------------------------------

@@ -27,6 +27,8 @@ OK, NOT_CONVERGED, BAD_INPUT, NONFINITE, CUDA_ERROR, TIMEOUT, NO_DEVICE, NO_PROB
 STANDARD, DESCENT, CONJUGATED, APGD, SPG = range(5)            # projected_gradient::Variant
 PURE_NEWTON, PURE_ENUMERATIVE, HYBRID, REV_HYBRID = range(4)   # local_soc_solver::Strategy
 ADMM_STANDARD, ADMM_ACCELERATED = range(2)                     # admm::Variant
+# MecheFrictionProblem::Algorithm
+MECHE_GAUSS_SEIDEL, MECHE_PROJECTED_GRADIENT, MECHE_MATRIX_FREE_GAUSS_SEIDEL, MECHE_ADMM, MECHE_DUAL_AMA = range(5)
 
 
 class BogusGpuError(RuntimeError):
@@ -58,6 +60,18 @@ class AdjointOptions(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint)]
 
 
+class MecheOptions(C.Structure):
+    """MecheFrictionProblem::Options (Interfaces/MecheInterface.hpp:44-69) with the reference's defaults."""
+    _fields_ = [("maxThreads", C.c_int), ("maxIters", C.c_uint), ("cadouxIters", C.c_uint), ("tolerance", C.c_double),
+                ("useInfinityNorm", C.c_int), ("algorithm", C.c_int), ("gsRegularization", C.c_double),
+                ("gsColoring", C.c_int), ("gsSkipIters", C.c_int), ("tryZeroAsWell", C.c_int),
+                ("pgVariant", C.c_int), ("admmProjStepSize", C.c_double), ("admmFpStepSize", C.c_double)]
+
+    def __init__(self):
+        super().__init__()
+        lib().bogus_gpu_meche_options_default(C.byref(self))
+
+
 class SolveStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("kernel_launches", C.c_uint), ("iterations", C.c_uint),
                 ("w_passes", C.c_uint), ("algorithmic_bytes", C.c_double), ("fp64_fma", C.c_double),
@@ -81,6 +95,7 @@ EXPORTED = [
     "bogus_gpu_admm_options_default", "bogus_gpu_solve_admm", "bogus_gpu_adjoint_options_default",
     "bogus_gpu_adjoint", "bogus_gpu_adjoint_device", "bogus_gpu_adjoint_dual_lower", "bogus_gpu_adjoint_primal",
     "bogus_gpu_add_compliance", "bogus_gpu_solve_cadoux_gs", "bogus_gpu_solve_cadoux_pg",
+    "bogus_gpu_meche_options_default", "bogus_gpu_meche_from_primal", "bogus_gpu_meche_solve",
 ]
 
 
@@ -130,6 +145,13 @@ def lib():
                                             C.POINTER(C.c_uint)]
     L.bogus_gpu_solve_cadoux_pg.argtypes = [vp, C.POINTER(PgOptions), _dp, C.c_uint, C.POINTER(C.c_double),
                                             C.POINTER(C.c_uint)]
+    L.bogus_gpu_meche_options_default.argtypes = [C.POINTER(MecheOptions)]
+    L.bogus_gpu_meche_options_default.restype = None
+    L.bogus_gpu_meche_from_primal.argtypes = [vp, C.c_uint, np.ctypeslib.ndpointer(dtype=np.uint32),
+                                              C.POINTER(C.c_void_p), vp, C.c_uint, _dp, _dp, _dp, _ip, _ip,
+                                              C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
+    L.bogus_gpu_meche_solve.argtypes = [vp, _dp, vp, C.POINTER(MecheOptions), C.c_int, C.c_double,
+                                        C.POINTER(C.c_double)]
     L.bogus_gpu_admm_options_default.argtypes = [C.POINTER(AdmmOptions)]
     L.bogus_gpu_admm_options_default.restype = None
     L.bogus_gpu_solve_admm.argtypes = [vp, C.POINTER(AdmmOptions), C.c_double, vp, vp, _dp, _dp, _dp, _dp,
@@ -597,3 +619,74 @@ def measure_fp64_peak(device: int = 0) -> float:
     v = C.c_double()
     _check(lib().bogus_gpu_measure_fp64_peak(int(device), C.byref(v)), False)
     return v.value
+
+
+class MecheFrictionProblem:
+    """MecheFrictionProblem (Interfaces/MecheInterface.hpp:40-170) on one GPU: fromPrimal() with world-coordinate
+    data (contact frames E), solve(r, v, options, staticProblem, problemRegularization)."""
+
+    def __init__(self, device: int = 0):
+        self._dual = DualFrictionProblem(device)
+        self._keep = None
+        self.m = 0
+        self.n = 0
+
+    def fromPrimal(self, mass, f, mu, E, w, objA, objB, HA, HB) -> None:
+        """mass: list of (ndof, ndof) arrays; f: (sum ndof) or None; mu: (n); E: (n, 3, 3) contact frames
+        (world to local, E[i][a][b] as the reference's E blocks); w: (3n) world; objA / objB: (n) (-1: external);
+        HA / HB: lists of (3, ndof) world Jacobian blocks (HB[i] None when objB[i] == -1)."""
+        mass = [np.asfortranarray(np.asarray(m_, np.float64)) for m_ in mass]
+        ndof = np.array([m_.shape[0] for m_ in mass], np.uint32)
+        n = len(objA)
+        E = np.asarray(E, np.float64).reshape(n, 3, 3)
+        Ecm = np.zeros((3, 3 * n))
+        for i in range(n):
+            Ecm[:, 3 * i:3 * i + 3] = E[i].T
+        HA = [np.asfortranarray(np.asarray(h, np.float64)) for h in HA]
+        HB = [None if h is None else np.asfortranarray(np.asarray(h, np.float64)) for h in HB]
+        fv = None if f is None else _f64(f).reshape(-1)
+        mp = (C.c_void_p * len(mass))(*[m_.ctypes.data for m_ in mass])
+        hap = (C.c_void_p * max(1, n))(*[h.ctypes.data for h in HA])
+        hbp = (C.c_void_p * max(1, n))(*[0 if h is None else h.ctypes.data for h in HB])
+        self._keep = (mass, HA, HB, fv)
+        _check(lib().bogus_gpu_meche_from_primal(self._dual.handle, len(mass), ndof, mp,
+                                                 None if fv is None else fv.ctypes.data_as(C.c_void_p), n,
+                                                 _f64(mu), Ecm.ravel(), _f64(w).reshape(-1), _i32(objA), _i32(objB),
+                                                 hap, hbp), False)
+        self.m, self.n = int(ndof.sum()), n
+
+    def solve(self, r, v=None, options: MecheOptions | None = None, staticProblem: bool = False,
+              problemRegularization: float = 0.0) -> float:
+        """r: (3n) world, solved in place; v: (sum ndof) array receiving the velocities (ADMM: also its warm
+        start) or None. Returns the solver's residual; the callback connected through callback() fires per
+        iteration."""
+        if not (isinstance(r, np.ndarray) and r.dtype == np.float64 and r.flags.c_contiguous):
+            raise TypeError("r must be a C-contiguous float64 numpy array (solved in place)")
+        if v is not None and not (isinstance(v, np.ndarray) and v.dtype == np.float64 and v.flags.c_contiguous
+                                  and v.size == self.m):
+            raise TypeError("v must be a C-contiguous float64 numpy array of the problem's dofs")
+        o = options or MecheOptions()
+        res = C.c_double()
+        st = lib().bogus_gpu_meche_solve(self._dual.handle, r.reshape(-1),
+                                         None if v is None else v.ctypes.data_as(C.c_void_p), C.byref(o),
+                                         int(staticProblem), float(problemRegularization), C.byref(res))
+        _check(st)
+        self.last_status = st
+        return res.value
+
+    def callback(self, fn) -> None:
+        """Connects fn(iteration, residual) to the solver callbacks (MecheFrictionProblem::callback())."""
+        sig = Signal()
+        sig.connect(fn)
+
+        class _Holder:
+            def callback(self_inner):
+                return sig
+
+        self._dual._bind(_Holder())
+
+    def nContacts(self) -> int:
+        return self.n
+
+    def nDegreesOfFreedom(self) -> int:
+        return self.m

@@ -152,6 +152,11 @@ struct bogus_gpu_problem {
   DevBuf<ADMMOut> admm_out;
   // Cadoux fixed point: the original right-hand side while the inner solves use COV(u) + b
   DevBuf<double> cad_b;
+  // MecheFrictionProblem facade: frames, world w (then local), padded f, per-body dofs; dual built at first use
+  bool meche_valid = false, meche_dual = false;
+  DevBuf<double> meche_E, meche_w, meche_r, meche_v, meche_fd;
+  std::vector<double> meche_wloc, meche_f, meche_mu;
+  std::vector<unsigned> meche_ndof;
   // adjoint: per-contact basis, CG vectors, the last solution r and s = dL/db (device and host copies)
   DevBuf<double> adj_V, adj_Pc, adj_D, adj_K, adj_P, adj_R, adj_Z, adj_Dir, adj_Y, adj_Q, adj_S, adj_dmu, adj_r, adj_g;
   DevBuf<AdjOut> adj_out;
@@ -245,6 +250,7 @@ int ensure_pg_work(bogus_gpu_problem* h, unsigned max_iters) {
 }
 
 int ensure_interleaved(bogus_gpu_problem* h);
+int ensure_incidence(bogus_gpu_problem* h);
 
 // Algorithmic bytes and W passes of one persistent solve from its phase counters. A W pass reads nnzb blocks
 // (9 values + a column index) and the n + 1 row pointers; the per-contact vector bytes of each pass kind
@@ -752,6 +758,7 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   h->bent.release();
   h->admm_out.release();
   h->cad_b.release();
+  for (auto* b : {&h->meche_E, &h->meche_w, &h->meche_r, &h->meche_v, &h->meche_fd}) b->release();
   for (auto* b : {&h->adj_V, &h->adj_Pc, &h->adj_D, &h->adj_K, &h->adj_P, &h->adj_R, &h->adj_Z, &h->adj_Dir,
                   &h->adj_Y, &h->adj_Q, &h->adj_S, &h->adj_dmu, &h->adj_r, &h->adj_g})
     b->release();
@@ -1283,6 +1290,249 @@ int bogus_gpu_solve_cadoux_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* 
   if (h->callback)
     for (auto& t : trace) h->callback(t.first, t.second, h->callback_user);
   return res < tol ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
+}
+
+// ---- MecheFrictionProblem facade (Interfaces/MecheInterface.hpp:40-170, MecheInterface.cpp:97-367) ----------
+void bogus_gpu_meche_options_default(bogus_gpu_meche_options* o) {
+  if (!o) return;
+  o->max_threads = 0;
+  o->max_iters = 0;
+  o->cadoux_iters = 0;
+  o->tolerance = 0.0;
+  o->use_infinity_norm = 0;
+  o->algorithm = BOGUS_GPU_MECHE_GAUSS_SEIDEL;
+  o->gs_regularization = 0.0;
+  o->gs_coloring = 0;
+  o->gs_skip_iters = -1;
+  o->try_zero_as_well = 1;
+  o->pg_variant = BOGUS_GPU_PG_SPG;
+  o->admm_proj_step_size = 1.0;
+  o->admm_fp_step_size = 1.e-3;
+}
+
+int bogus_gpu_meche_from_primal(bogus_gpu_problem* h, unsigned nobj, const unsigned* ndof,
+                                const double* const* mass, const double* f, unsigned n, const double* mu,
+                                const double* E, const double* w, const int* objA, const int* objB,
+                                const double* const* HA, const double* const* HB) {
+  if (int e = check_handle(h)) return e;
+  if (nobj == 0 || !ndof || !mass) return fail(BOGUS_GPU_BAD_INPUT, "no objects");
+  if (n > 0 && (!mu || !E || !w || !objA || !objB || !HA || !HB)) return fail(BOGUS_GPU_BAD_INPUT, "null contact array");
+  unsigned d = 1;
+  size_t m = 0;
+  for (unsigned k = 0; k < nobj; ++k) {
+    if (ndof[k] == 0 || ndof[k] > 12 || !mass[k]) return fail(BOGUS_GPU_BAD_INPUT, "object dofs must be in 1..12");
+    d = std::max(d, ndof[k]);
+    m += ndof[k];
+  }
+  for (unsigned i = 0; i < n; ++i) {
+    if (objA[i] < 0 || objA[i] >= (int)nobj || objB[i] < -1 || objB[i] >= (int)nobj)
+      return fail(BOGUS_GPU_BAD_INPUT, "object index out of range");
+    if (!HA[i] || (objB[i] >= 0 && !HB[i])) return fail(BOGUS_GPU_BAD_INPUT, "null Jacobian block");
+  }
+  if (int e = check_finite(E, 9 * (size_t)n, "E")) return e;
+  if (int e = check_finite(w, 3 * (size_t)n, "w")) return e;
+  if (int e = check_finite(mu, n, "mu")) return e;
+  if (f)
+    if (int e = check_finite(f, m, "f")) return e;
+  // inverse mass blocks (PrimalFrictionProblem::computeMInv), padded to d dofs with inert (zero) entries
+  std::vector<double> minv((size_t)nobj * d * d, 0.0), fpad((size_t)nobj * d, 0.0);
+  {
+    size_t off = 0;
+    for (unsigned k = 0; k < nobj; ++k) {
+      const int dk = (int)ndof[k];
+      if (int e = check_finite(mass[k], (size_t)dk * dk, "mass")) return e;
+      std::vector<double> Mk((size_t)dk * dk), inv((size_t)dk * dk);
+      for (int a = 0; a < dk; ++a)
+        for (int c = 0; c < dk; ++c) Mk[(size_t)a * dk + c] = mass[k][(size_t)c * dk + a];
+      if (!invert_gauss_jordan(dk, Mk.data(), inv.data())) return fail(BOGUS_GPU_BAD_INPUT, "singular mass block");
+      for (int a = 0; a < dk; ++a) {
+        for (int c = 0; c < dk; ++c) minv[(size_t)k * d * d + a * d + c] = inv[(size_t)a * dk + c];
+        if (f) fpad[(size_t)k * d + a] = f[off + a];
+      }
+      off += ndof[k];
+    }
+  }
+  // frames (row-major per contact) and padded row-major world Jacobian blocks
+  const size_t hs = 3 * (size_t)d;
+  std::vector<double> Er(9 * (size_t)n), HAw(n * hs, 0.0), HBw(n * hs, 0.0);
+  std::vector<int> cbh(2 * (size_t)n), oA(objA, objA + n), oB(objB, objB + n);
+  for (unsigned i = 0; i < n; ++i) {
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c) Er[9 * (size_t)i + 3 * a + c] = E[(size_t)c * 3 * n + 3 * i + a];
+    const int A = objA[i], B = objB[i];
+    for (unsigned c = 0; c < ndof[A]; ++c)
+      for (int k = 0; k < 3; ++k) HAw[i * hs + k * d + c] = HA[i][(size_t)c * 3 + k];
+    if (B >= 0) {
+      const unsigned dB = ndof[B == A ? A : B];
+      for (unsigned c = 0; c < dB; ++c)
+        for (int k = 0; k < 3; ++k) HBw[i * hs + k * d + c] = HB[i][(size_t)c * 3 + k];
+    }
+    const bool two = B >= 0 && B != A;
+    cbh[2 * (size_t)i] = two ? std::min(A, B) : A;
+    cbh[2 * (size_t)i + 1] = two ? std::max(A, B) : -1;
+  }
+  if (int e = check_finite(HAw.data(), HAw.size(), "HA")) return e;
+  if (int e = check_finite(HBw.data(), HBw.size(), "HB")) return e;
+  if (int e = set_device(h)) return e;
+  cudaStream_t s = h->stream;
+  DevBuf<double> dHA, dHB;
+  DevBuf<int> dA, dB;
+  const size_t nn = n > 0 ? n : 1;
+  BG_CUDA(h->meche_E.ensure(9 * nn));
+  BG_CUDA(h->minv.ensure((size_t)nobj * d * d));
+  BG_CUDA(h->H.ensure(2 * nn * hs));
+  BG_CUDA(h->cb.ensure(2 * nn));
+  BG_CUDA(dHA.ensure(nn * hs));
+  BG_CUDA(dHB.ensure(nn * hs));
+  BG_CUDA(dA.ensure(nn));
+  BG_CUDA(dB.ensure(nn));
+  BG_CUDA(h->meche_w.ensure(3 * nn));
+  BG_CUDA(cudaMemcpyAsync(h->minv.p, minv.data(), sizeof(double) * minv.size(), cudaMemcpyHostToDevice, s));
+  if (n > 0) {
+    BG_CUDA(cudaMemcpyAsync(h->meche_E.p, Er.data(), sizeof(double) * Er.size(), cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(dHA.p, HAw.data(), sizeof(double) * HAw.size(), cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(dHB.p, HBw.data(), sizeof(double) * HBw.size(), cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(dA.p, objA, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(dB.p, objB, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->cb.p, cbh.data(), sizeof(int) * cbh.size(), cudaMemcpyHostToDevice, s));
+    BG_CUDA(launch_meche_h((int)n, (int)d, h->meche_E.p, dHA.p, dHB.p, dA.p, dB.p, h->H.p, s));
+    // w to the local basis once: E^T w
+    BG_CUDA(cudaMemcpyAsync(h->meche_w.p, w, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+    BG_CUDA(launch_frame((int)n, h->meche_E.p, h->meche_w.p, h->meche_w.p, true, s));
+  }
+  h->meche_wloc.assign(3 * (size_t)n, 0.0);
+  if (n > 0)
+    BG_CUDA(cudaMemcpyAsync(h->meche_wloc.data(), h->meche_w.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  h->nbodies = (int)nobj;
+  h->ndof = (int)d;
+  h->ncontacts = (int)n;
+  h->h_cb = std::move(cbh);
+  h->h_objA = std::move(oA);
+  h->admm_incidence_valid = false;
+  h->meche_ndof.assign(ndof, ndof + nobj);
+  h->meche_f = std::move(fpad);
+  h->meche_mu.assign(mu, mu + n);
+  h->meche_valid = true;
+  h->meche_dual = false;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_meche_solve(bogus_gpu_problem* h, double* r, double* v, const bogus_gpu_meche_options* o,
+                          int static_problem, double problem_regularization, double* residual) {
+  if (int e = check_handle(h)) return e;
+  if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
+  if (!h->meche_valid) return fail(BOGUS_GPU_NO_PROBLEM, "no problem set (bogus_gpu_meche_from_primal)");
+  if (o->algorithm == BOGUS_GPU_MECHE_MATRIX_FREE_GAUSS_SEIDEL || o->algorithm == BOGUS_GPU_MECHE_DUAL_AMA)
+    return fail(BOGUS_GPU_BAD_INPUT, "MatrixFreeGaussSeidel and DualAMA are not available on the GPU");
+  if (o->algorithm != BOGUS_GPU_MECHE_GAUSS_SEIDEL && o->algorithm != BOGUS_GPU_MECHE_PROJECTED_GRADIENT &&
+      o->algorithm != BOGUS_GPU_MECHE_ADMM)
+    return fail(BOGUS_GPU_BAD_INPUT, "unknown algorithm");
+  const int n = h->ncontacts, nb = h->nbodies, d = h->ndof;
+  const size_t n3 = 3 * (size_t)n, md = (size_t)nb * d;
+  if (n > 0 && !r) return fail(BOGUS_GPU_BAD_INPUT, "null r");
+  if (int e = check_finite(r, n3, "r")) return e;
+  if (int e = set_device(h)) return e;
+  cudaStream_t s = h->stream;
+  BG_CUDA(h->meche_r.ensure(n3 > 0 ? n3 : 1));
+  BG_CUDA(h->meche_v.ensure(md));
+  BG_CUDA(h->meche_fd.ensure(md));
+  BG_CUDA(cudaMemcpyAsync(h->meche_fd.p, h->meche_f.data(), sizeof(double) * md, cudaMemcpyHostToDevice, s));
+  std::vector<double> rl(n3), vp(md, 0.0);
+  // r to local coordinates: E^T r
+  if (n > 0) {
+    BG_CUDA(cudaMemcpyAsync(h->meche_r.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+    BG_CUDA(launch_frame(n, h->meche_E.p, h->meche_r.p, h->meche_r.p, true, s));
+    BG_CUDA(cudaMemcpyAsync(rl.data(), h->meche_r.p, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
+  }
+  BG_CUDA(cudaStreamSynchronize(s));
+  auto velocity = [&]() -> int {  // v = M^-1 (H^T r_loc - f) into vp
+    if (int e = ensure_incidence(h)) return e;
+    BG_CUDA(launch_body_transpose(nb, d, h->bptr.p, h->bent.p, h->H.p, h->minv.p, h->meche_r.p, h->meche_fd.p,
+                                  h->meche_v.p, s));
+    BG_CUDA(cudaMemcpyAsync(vp.data(), h->meche_v.p, sizeof(double) * md, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+    return BOGUS_GPU_OK;
+  };
+  auto pad_v = [&]() {
+    size_t off = 0;
+    for (int k = 0; k < nb; ++k) {
+      for (unsigned a = 0; a < h->meche_ndof[k]; ++a) vp[(size_t)k * d + a] = v[off + a];
+      off += h->meche_ndof[k];
+    }
+  };
+  int st = BOGUS_GPU_OK;
+  double res = -1.0;
+  if (o->algorithm == BOGUS_GPU_MECHE_ADMM) {
+    if (v) pad_v();
+    else if (int e = velocity()) return e;
+    bogus_gpu_admm_options ao;
+    bogus_gpu_admm_options_default(&ao);
+    ao.step_size = o->admm_proj_step_size;
+    if (o->tolerance != 0.) ao.tol = o->tolerance;
+    if (o->max_iters != 0) ao.max_iters = o->max_iters;
+    ao.use_infinity_norm = o->use_infinity_norm;
+    st = bogus_gpu_solve_admm(h, &ao, 0.0, nullptr, h->meche_f.data(), h->meche_wloc.data(), h->meche_mu.data(),
+                              vp.data(), rl.data(), &res, nullptr);
+    if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+    if (n > 0) BG_CUDA(cudaMemcpyAsync(h->meche_r.p, rl.data(), sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  } else {
+    if (!h->meche_dual) {
+      if (int e = bogus_gpu_assemble_dual(h, h->meche_f.data(), h->meche_wloc.data(), h->meche_mu.data())) return e;
+      if (problem_regularization > 0. && n > 0) {
+        std::vector<double> c(n, problem_regularization);
+        if (int e = bogus_gpu_add_compliance(h, c.data())) return e;
+      }
+      h->meche_dual = true;
+    }
+    const bool cadoux = !static_problem && o->cadoux_iters > 0;
+    if (o->algorithm == BOGUS_GPU_MECHE_PROJECTED_GRADIENT) {
+      bogus_gpu_pg_options po;
+      bogus_gpu_pg_options_default(&po);
+      if (o->tolerance != 0.) po.tol = o->tolerance;
+      if (o->max_iters != 0) po.max_iters = o->max_iters;
+      po.use_infinity_norm = o->use_infinity_norm;
+      po.variant = o->pg_variant;
+      po.static_problem = static_problem ? 1 : 0;
+      st = cadoux ? bogus_gpu_solve_cadoux_pg(h, &po, rl.data(), o->cadoux_iters, &res, nullptr)
+                  : bogus_gpu_solve_pg(h, &po, rl.data(), &res, nullptr);
+    } else {
+      bogus_gpu_gs_options go;
+      bogus_gpu_gs_options_default(&go);
+      if (o->tolerance != 0.) go.tol = o->tolerance;
+      if (o->max_iters != 0) go.max_iters = o->max_iters;
+      if (o->gs_skip_iters >= 0) go.skip_iters = (unsigned)o->gs_skip_iters;
+      go.auto_regularization = o->gs_regularization;
+      go.use_infinity_norm = o->use_infinity_norm;
+      go.use_coloring = (o->max_threads != 1 && o->gs_coloring) ? 1 : 0;
+      go.static_problem = static_problem ? 1 : 0;
+      go.try_zero_as_well = cadoux ? 0 : o->try_zero_as_well;
+      st = cadoux ? bogus_gpu_solve_cadoux_gs(h, &go, rl.data(), o->cadoux_iters, &res, nullptr)
+                  : bogus_gpu_solve_gs(h, &go, rl.data(), &res, nullptr);
+    }
+    if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+    if (n > 0) {
+      BG_CUDA(cudaMemcpyAsync(h->meche_r.p, rl.data(), sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+      BG_CUDA(cudaStreamSynchronize(s));
+    }
+    if (v)
+      if (int e = velocity()) return e;
+  }
+  if (v) {
+    size_t off = 0;
+    for (int k = 0; k < nb; ++k) {
+      for (unsigned a = 0; a < h->meche_ndof[k]; ++a) v[off + a] = vp[(size_t)k * d + a];
+      off += h->meche_ndof[k];
+    }
+  }
+  // r back to world coordinates: E r_loc
+  if (n > 0) {
+    BG_CUDA(launch_frame(n, h->meche_E.p, h->meche_r.p, h->meche_r.p, false, s));
+    BG_CUDA(cudaMemcpyAsync(r, h->meche_r.p, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+  }
+  if (residual) *residual = res;
+  return st;
 }
 
 // ---- primal data and Delassus assembly ---------------------------------------------------------------

@@ -158,4 +158,44 @@ inline HostBSR permute_lower(const HostBSR& low, const std::vector<int>& perm) {
   return out;
 }
 
+// Inverse of a d x d row-major matrix by Gauss-Jordan elimination with partial pivoting (the first largest
+// |pivot| in the column; the pivot row scaled by the pivot's reciprocal; row updates a_jk - f a_ik); false when
+// a column has no non-zero pivot. Used for the mass blocks of the MecheFrictionProblem facade.
+inline bool invert_gauss_jordan(int d, const double* M, double* inv) {
+  std::vector<double> a(M, M + (size_t)d * d), b((size_t)d * d, 0.0);
+  for (int i = 0; i < d; ++i) b[(size_t)i * d + i] = 1.0;
+  for (int c = 0; c < d; ++c) {
+    int piv = c;
+    double best = std::fabs(a[(size_t)c * d + c]);
+    for (int row = c + 1; row < d; ++row) {
+      const double m = std::fabs(a[(size_t)row * d + c]);
+      if (m > best) {
+        best = m;
+        piv = row;
+      }
+    }
+    if (!(best > 0.0)) return false;
+    if (piv != c)
+      for (int k = 0; k < d; ++k) {
+        std::swap(a[(size_t)piv * d + k], a[(size_t)c * d + k]);
+        std::swap(b[(size_t)piv * d + k], b[(size_t)c * d + k]);
+      }
+    const double rp = 1.0 / a[(size_t)c * d + c];
+    for (int k = 0; k < d; ++k) {
+      a[(size_t)c * d + k] = a[(size_t)c * d + k] * rp;
+      b[(size_t)c * d + k] = b[(size_t)c * d + k] * rp;
+    }
+    for (int row = 0; row < d; ++row) {
+      if (row == c) continue;
+      const double g = a[(size_t)row * d + c];
+      for (int k = 0; k < d; ++k) {
+        a[(size_t)row * d + k] = a[(size_t)row * d + k] - g * a[(size_t)c * d + k];
+        b[(size_t)row * d + k] = b[(size_t)row * d + k] - g * b[(size_t)c * d + k];
+      }
+    }
+  }
+  std::copy(b.begin(), b.end(), inv);
+  return true;
+}
+
 }  // namespace bogus_gpu

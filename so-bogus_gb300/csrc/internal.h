@@ -207,6 +207,10 @@ cudaError_t launch_body_transpose(int nbodies, int d, const int* bptr, const int
 cudaError_t launch_h_gradient(int n, int d, const int* cb, const double* s, const double* r, const double* vr,
                               const double* vs, double* dH, cudaStream_t st);
 cudaError_t launch_add_diagonal(const DevBSR& W, const double* c, cudaStream_t s);
+// MecheFrictionProblem frames (kernels_grad.cu): y_i = E_i^T x_i or E_i x_i; H slots from world Jacobians
+cudaError_t launch_frame(int n, const double* E, const double* x, double* y, bool transpose, cudaStream_t s);
+cudaError_t launch_meche_h(int n, int d, const double* E, const double* HAw, const double* HBw, const int* objA,
+                           const int* objB, double* H, cudaStream_t s);
 
 // Records the message returned by bogus_gpu_last_error() on this thread.
 void set_last_error(const std::string& msg);

@@ -92,3 +92,70 @@ cudaError_t launch_add_diagonal(const DevBSR& W, const double* c, cudaStream_t s
 }
 
 }  // namespace bogus_gpu
+
+// ---- MecheFrictionProblem (Interfaces/MecheInterface.cpp) -----------------------------------------------
+namespace bogus_gpu {
+
+namespace {
+
+// y_i = E_i^T x_i (transpose) or E_i x_i, E_i row-major 3x3, with the dot3 chain
+__global__ void k_frame(int n, const double* __restrict__ E, const double* __restrict__ x, double* __restrict__ y,
+                        int transpose) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* e = E + 9 * (size_t)i;
+  const double v[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+  for (int a = 0; a < 3; ++a)
+    y[3 * i + a] = transpose ? fma(e[6 + a], v[2], fma(e[3 + a], v[1], e[a] * v[0]))
+                             : fma(e[3 * a + 2], v[2], fma(e[3 * a + 1], v[1], e[3 * a] * v[0]));
+}
+
+// Local-basis Jacobian slots of contact i (MecheInterface.cpp:161-176): H_A = E^T HA, H_B = -E^T HB, or
+// E^T (HA - HB) when both objects are the same; slot 0 / 1 ordered by body index as in the primal layout.
+// HAw / HBw: world blocks, row-major 3 x d (padded), per contact.
+__global__ void k_meche_h(int n, int d, const double* __restrict__ E, const double* __restrict__ HAw,
+                          const double* __restrict__ HBw, const int* __restrict__ objA, const int* __restrict__ objB,
+                          double* __restrict__ H) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* e = E + 9 * (size_t)i;
+  const int A = objA[i], B = objB[i];
+  const bool two = B >= 0 && B != A;
+  const int sA = (two && B < A) ? 1 : 0;  // slot of body A
+  const size_t hs = 3 * (size_t)d;
+  double* outA = H + (2 * (size_t)i + sA) * hs;
+  double* outB = H + (2 * (size_t)i + (1 - sA)) * hs;
+  for (int c = 0; c < d; ++c) {
+    double h[3];
+    for (int k = 0; k < 3; ++k) {
+      h[k] = HAw[(size_t)i * hs + k * d + c];
+      if (B == A) h[k] = h[k] - HBw[(size_t)i * hs + k * d + c];
+    }
+    for (int a = 0; a < 3; ++a) outA[a * d + c] = fma(e[6 + a], h[2], fma(e[3 + a], h[1], e[a] * h[0]));
+    for (int a = 0; a < 3; ++a) {
+      if (two) {
+        const double hb[3] = {HBw[(size_t)i * hs + c], HBw[(size_t)i * hs + d + c], HBw[(size_t)i * hs + 2 * d + c]};
+        outB[a * d + c] = -fma(e[6 + a], hb[2], fma(e[3 + a], hb[1], e[a] * hb[0]));
+      } else {
+        outB[a * d + c] = 0.0;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_frame(int n, const double* E, const double* x, double* y, bool transpose, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_frame<<<(n + 255) / 256, 256, 0, s>>>(n, E, x, y, transpose ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_meche_h(int n, int d, const double* E, const double* HAw, const double* HBw, const int* objA,
+                           const int* objB, double* H, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_meche_h<<<(n + 127) / 128, 128, 0, s>>>(n, d, E, HAw, HBw, objA, objB, H);
+  return cudaGetLastError();
+}
+
+}  // namespace bogus_gpu

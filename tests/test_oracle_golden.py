@@ -271,3 +271,66 @@ def test_canonical_sum_matches_its_definition(oracle):
         got = oracle.canonical_sum(v)
         assert got == total
         assert got == pytest.approx(float(np.sum(v)), abs=1e-9 * max(1, n))
+
+
+# ---- MecheFrictionProblem (Interfaces/MecheInterface.cpp:97-367); the reference has no test of its own, so the
+# facade is held to the Coulomb solution of tests/SmallFrictionPb.hpp, posed in world coordinates ------------
+def small_friction_world():
+    """SmallFrictionPb in world coordinates: contact frames E_i (a random rotation, the fixture's own frame),
+    world Jacobians HA = E H_A, HB = -E H_B, world w = E w_local. Returns the Meche inputs and the frames."""
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(__file__), "golden", "reference_fixtures.json")) as fh:
+        s = json.load(fh)["small_friction_pb"]
+    nd = s["ndof_padded"]
+    dofs = s["dofs"]
+    minv = np.array(s["minv"])
+    mass = [np.linalg.inv(minv[k, :dofs[k], :dofs[k]]) for k in range(2)]
+    HA = np.array(s["HA"])
+    HB = np.array(s["HB"])
+    q, _ = np.linalg.qr(np.random.default_rng(3).standard_normal((3, 3)))
+    E = np.stack([q, np.array([[0.0, 0, 1], [1, 0, 0], [0, 1, 0]])])
+    HAw = [E[0] @ HA[0][:, :dofs[0]], E[1] @ HA[1][:, :dofs[0]]]
+    HBw = [-(E[0] @ HB[0][:, :dofs[1]]), None]
+    w = np.array(s["w"])
+    ww = np.concatenate([E[i] @ w[3 * i:3 * i + 3] for i in range(2)])
+    f = np.array(s["f_padded"])
+    fp = np.concatenate([f[:dofs[0]], f[nd:nd + dofs[1]]])
+    return s, dict(mass=mass, f=fp, mu=np.array(s["mu"]), E=E, w=ww, objA=[0, 0], objB=[1, -1], HA=HAw, HB=HBw)
+
+
+@pytest.mark.parametrize("algorithm, cadoux", [(0, 0), (1, 40)])  # Gauss-Seidel; projected gradient + Cadoux
+def test_meche_reaches_the_coulomb_solution(oracle, algorithm, cadoux):
+    s, inp = small_friction_world()
+    M = oracle.MecheProblem(**inp)
+    res, r, v = M.solve(np.zeros(6), algorithm=algorithm, cadoux_iters=cadoux, tolerance=1e-10, max_iters=3000,
+                        pg_variant=3)
+    assert res < 1e-10
+    E = inp["E"]
+    r_loc = np.concatenate([E[i].T @ r[3 * i:3 * i + 3] for i in range(2)])
+    assert isApprox(s["sol"], r_loc, s["sol_rel_tol"])
+    # v = M^-1 (H^T r - f) in the bodies' own dofs
+    Hd = np.zeros((6, 6))
+    Hd[0:3, 0:4] = E[0].T @ inp["HA"][0]
+    Hd[0:3, 4:6] = -(E[0].T @ inp["HB"][0])
+    Hd[3:6, 0:4] = E[1].T @ inp["HA"][1]
+    Mi = np.zeros((6, 6))
+    Mi[:4, :4] = np.linalg.inv(inp["mass"][0])
+    Mi[4:, 4:] = np.linalg.inv(inp["mass"][1])
+    assert np.allclose(v, Mi @ (Hd.T @ r_loc - inp["f"]), rtol=0, atol=1e-12)
+
+
+def test_meche_admm_matches_the_primal_solver(oracle):
+    """Algorithm ADMM: PrimalFrictionProblem::solveWith(ADMM&, 0, v, E^T r) on the local problem."""
+    s, inp = small_friction_world()
+    M = oracle.MecheProblem(**inp)
+    res, r, v = M.solve(np.zeros(6), algorithm=3, tolerance=1e-9, max_iters=2000, admm_step=1e-2, static=True)
+    assert res < 1e-9
+    P = oracle.PrimalProblem(np.array(s["minv"]), s["objA"], s["objB"], np.array(s["HA"]), np.array(s["HB"]))
+    minv = np.array(s["minv"])
+    res_o, v_o, r_o, _ = P.solve_admm(minv, 0.0, np.array(s["mu"]), np.array(s["f_padded"]), np.array(s["w"]),
+                                      np.zeros(8), np.zeros(6), tol=1e-9, max_iters=2000, step=1e-2)
+    E = inp["E"]
+    r_loc = np.concatenate([E[i].T @ r[3 * i:3 * i + 3] for i in range(2)])
+    assert np.allclose(r_loc, r_o, rtol=0, atol=1e-6)
