@@ -193,6 +193,13 @@ int bogus_gpu_solve_cadoux_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* 
 int bogus_gpu_solve_cadoux_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* opts, double* r,
                               unsigned cadoux_iters, double* residual, unsigned* iters);
 
+/* PrimalFrictionProblem::solveWith(ProductGaussSeidelType&, r, staticProblem) (Interfaces/PrimalFrictionProblem.cpp:
+ * 41-59, Core/BlockSolvers/ProductGaussSeidel.impl.hpp:108-296): Gauss-Seidel on W = H M^-1 H^T without forming W,
+ * on the handle's primal data (bogus_gpu_set_primal), b = w - H M^-1 f (f NULL: 0). The contacts are swept in their
+ * own order (use_coloring must be 0); the other options as bogus_gpu_solve_gs (static_problem 0: Coulomb). */
+int bogus_gpu_solve_product_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* opts, const double* f,
+                               const double* w, const double* mu, double* r, double* residual, unsigned* iters);
+
 /* Greedy coloring used by bogus_gpu_solve_gs: perm[n] (contact order, colors contiguous) and colors[ncolors+1]
  * offsets; colors must hold n + 1 ints. */
 int bogus_gpu_coloring(bogus_gpu_problem* h, int* perm, int* colors, int* ncolors);
@@ -306,7 +313,7 @@ int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int* d_rowptr,
 typedef enum bogus_gpu_meche_algorithm { /* MecheFrictionProblem::Algorithm */
   BOGUS_GPU_MECHE_GAUSS_SEIDEL = 0,
   BOGUS_GPU_MECHE_PROJECTED_GRADIENT = 1,
-  BOGUS_GPU_MECHE_MATRIX_FREE_GAUSS_SEIDEL = 2, /* not available on the GPU: BAD_INPUT */
+  BOGUS_GPU_MECHE_MATRIX_FREE_GAUSS_SEIDEL = 2,
   BOGUS_GPU_MECHE_ADMM = 3,
   BOGUS_GPU_MECHE_DUAL_AMA = 4                  /* not available on the GPU: BAD_INPUT */
 } bogus_gpu_meche_algorithm;

@@ -68,6 +68,10 @@ def lib():
     L.oracle_meche_solve.argtypes = [vp, _dp, vp, C.c_int, C.c_uint, C.c_uint, C.c_double, C.c_int, C.c_int,
                                      C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double,
                                      CALLBACK, vp]
+    L.oracle_primal_solve_product_gs.restype = C.c_double
+    L.oracle_primal_solve_product_gs.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint,
+                                                 C.c_double, C.c_uint, C.c_double, C.c_int, C.c_int, _dp,
+                                                 C.POINTER(C.c_uint), CALLBACK, vp]
     L.oracle_dual_solve_gs.restype = C.c_double
     L.oracle_dual_solve_gs.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_uint,
                                        C.c_double, C.c_int, C.c_int, C.c_int, _dp, C.POINTER(C.c_uint), CALLBACK,
@@ -276,6 +280,19 @@ class PrimalProblem:
         b = np.zeros(3 * self.n)
         lib().oracle_primal_rhs(self.h, _f64(f).reshape(-1), _f64(w).reshape(-1), b)
         return b
+
+    def solve_product_gs(self, f, w, mu, r, coulomb=True, strategy=3, tol=1e-6, max_iters=250, eval_every=25,
+                         skip_tol=1e-6, skip_iters=10, auto_reg=0.0, try_zero=True, inf_norm=False,
+                         trace: Trace | None = None):
+        """PrimalFrictionProblem::solveWith(ProductGaussSeidelType&, r, staticProblem = not coulomb)."""
+        r = _f64(r).copy()
+        it = C.c_uint(0)
+        cb = trace._cb if trace else _NO_CB
+        res = lib().oracle_primal_solve_product_gs(self.h, _f64(f).reshape(-1), _f64(w).reshape(-1), _f64(mu),
+                                                   int(coulomb), strategy, tol, max_iters, eval_every, skip_tol,
+                                                   skip_iters, auto_reg, int(try_zero), int(inf_norm), r,
+                                                   C.byref(it), cb, None)
+        return res, r, it.value
 
     def solve_admm(self, prox_inv, lam, mu, f, w, v, r, tol=1e-6, max_iters=300, step=1e-2, accelerated=True,
                    inf_norm=False, trace: Trace | None = None):

@@ -297,6 +297,21 @@ double oracle_meche_solve(void* h, double* r, double* v, int maxThreads, unsigne
     std::vector<double> invMu(n);
     for (int i = 0; i < n; ++i) invMu[i] = 1. / m->mu[i];
     res = s.solve(invMu.data(), P.minv, 0., m->f.data(), wl.data(), vp.data(), rl.data());
+  } else if (algorithm == 2) {
+    // PrimalFrictionProblem::solveWith(ProductGaussSeidelType&, r_loc, staticProblem)
+    ProductGaussSeidel gs;
+    if (tolerance != 0.) gs.tol = tolerance;
+    if (maxIters != 0) gs.maxIters = maxIters;
+    if (gsSkipIters >= 0) gs.skipIters = (unsigned)gsSkipIters;
+    gs.useInfinityNorm = useInfinityNorm != 0;
+    gs.autoRegularization = gsRegularization;
+    gs.tryZeroAsWell = tryZeroAsWell != 0;
+    gs.callback = callback;
+    gs.setPrimal(P);
+    const std::vector<double> b = assembleB(P, m->f.data(), wl.data());
+    Law law{staticProblem == 0, RevHybrid, m->mu.data()};
+    res = gs.solve(law, b.data(), rl.data());
+    if (v) mecheVelocity(*m, rl.data(), vp.data());
   } else {
     if (!m->hasDual) {
       m->low = assembleW(P);
@@ -433,6 +448,29 @@ int oracle_primal_assemble(void* h, int* rowptr, int* col, double* val) {
 void oracle_primal_rhs(void* h, const double* f, const double* w, double* b) {
   const std::vector<double> bb = assembleB(*static_cast<Primal*>(h), f, w);
   std::memcpy(b, bb.data(), sizeof(double) * bb.size());
+}
+
+// PrimalFrictionProblem::solveWith(ProductGaussSeidelType&, r, staticProblem): b = w - H M^-1 f, then the
+// matrix-free Gauss-Seidel (desaxce: the Coulomb law, else SOC).
+double oracle_primal_solve_product_gs(void* h, const double* f, const double* w, const double* mu, int desaxce,
+                                      int strat, double tol, unsigned maxIters, unsigned evalEvery, double skipTol,
+                                      unsigned skipIters, double autoReg, int tryZero, int useInfinityNorm, double* r,
+                                      unsigned* iters, oracle_callback cb, void* user) {
+  auto* P = static_cast<Primal*>(h);
+  const std::vector<double> b = assembleB(*P, f, w);
+  ProductGaussSeidel gs;
+  gs.tol = tol;
+  gs.maxIters = maxIters;
+  gs.evalEvery = evalEvery;
+  gs.skipTol = skipTol;
+  gs.skipIters = skipIters;
+  gs.autoRegularization = autoReg;
+  gs.tryZeroAsWell = tryZero != 0;
+  gs.useInfinityNorm = useInfinityNorm != 0;
+  gs.callback = wrap(cb, user);
+  gs.setPrimal(*P);
+  Law law{desaxce != 0, strat, mu};
+  return gs.solve(law, b.data(), r, iters);
 }
 
 // PrimalFrictionProblem::solveWith(ADMM&, lambda, v, r): proxInv = (M + lambda I)^-1 blocks

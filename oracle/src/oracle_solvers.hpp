@@ -503,6 +503,186 @@ struct ProjectedGradient : SolverBase {
 };
 
 // ---------------------------------------------------------------------------------------------
+// ProductGaussSeidel<HType, MInvType, true> (Core/BlockSolvers/ProductGaussSeidel.impl.hpp:108-296), as
+// PrimalFrictionProblem::solveWith(ProductGaussSeidelType&, r, staticProblem) (PrimalFrictionProblem.cpp:41-59)
+// runs it: Gauss-Seidel on W = H M^-1 H^T without forming W. It keeps Mx = M^-1 H^T x (DMt x) per body:
+//   local_i = sum_t H_t T_t (T = M^-1 H^T per slot; W's diagonal block as assembleW forms it) + reg I;
+//   contact i: lb = b_i - local_i x_i + H_i Mx (rowMultiply), local solve, x_i += dx, Mx += T_i dx (colMultiply);
+//   every evalEvery sweeps Mx is recomputed from x and y = b + H Mx gives the error.
+// Orders: Mx_b chains over b's contacts in increasing index, then the 3 components; H_i Mx adds, slot by slot
+// in body order, the dof chain sum to lb; T_i dx is the dot3 chain, added to Mx; local_i x_i is the dot3 chain
+// per row, subtracted from b_i. The sweep visits the contacts in their own order (no coloring).
+// ---------------------------------------------------------------------------------------------
+struct ProductGaussSeidel : SolverBase {
+  unsigned evalEvery = 25;
+  double skipTol = 1e-6;
+  unsigned skipIters = 10;
+  double autoRegularization = 0.0;
+  bool tryZeroAsWell = true;
+  const Primal* P = nullptr;
+  BSR shape;                  // n only (SolverBase::eval)
+  std::vector<double> T;      // slots, d x 3
+  std::vector<double> local;  // 9 n (+ regularization)
+  std::vector<double> reg;    // n
+  std::vector<std::vector<std::pair<int, int>>> byBody;  // (contact, slot), increasing contact
+
+  ProductGaussSeidel() { tol = 1e-6; maxIters = 250; }
+
+  void setPrimal(const Primal& Pr) {
+    P = &Pr;
+    const int n = Pr.ncontacts, d = Pr.ndof;
+    shape.n = n;
+    W = &shape;
+    T = slotT(Pr);
+    byBody.assign(Pr.nbodies, {});
+    local.assign(9 * (size_t)n, 0.0);
+    reg.assign(n, 0.0);
+    scaling.assign(n, 1.0);
+    for (int i = 0; i < n; ++i) {
+      int bodies[2]; const double* H[2]; int nb;
+      contactBodies(Pr, i, bodies, H, nb);
+      for (int t = 0; t < nb; ++t) byBody[bodies[t]].push_back({i, t});
+      double* L = &local[9 * (size_t)i];
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+          double a = 0.0;
+          for (int t = 0; t < nb; ++t) {
+            const double* Tt = &T[((size_t)i * 2 + t) * d * 3];
+            for (int m = 0; m < d; ++m) a = std::fma(H[t][r * d + m], Tt[m * 3 + c], a);
+          }
+          L[3 * r + c] = a;
+        }
+      scaling[i] = dmax(1.0, ((L[0] + L[4]) + L[8]) / 3.0);
+      if (autoRegularization > 0.) {
+        reg[i] = dmax(0.0, autoRegularization - GaussSeidel::minEigenSymmetric3(L));
+        L[0] += reg[i];
+        L[4] += reg[i];
+        L[8] += reg[i];
+      }
+    }
+  }
+
+  void computeMx(const double* x, double* Mx) const {
+    const int d = P->ndof;
+    for (int b = 0; b < P->nbodies; ++b)
+      for (int m = 0; m < d; ++m) {
+        double a = 0.0;
+        for (const auto& it : byBody[b]) {
+          const double* Tt = &T[((size_t)it.first * 2 + it.second) * d * 3];
+          const double* xi = &x[3 * (size_t)it.first];
+          a = std::fma(Tt[m * 3], xi[0], a);
+          a = std::fma(Tt[m * 3 + 1], xi[1], a);
+          a = std::fma(Tt[m * 3 + 2], xi[2], a);
+        }
+        Mx[(size_t)b * d + m] = a;
+      }
+  }
+  void rowMul(int i, const double* Mx, double* v) const {
+    const int d = P->ndof;
+    int bodies[2]; const double* H[2]; int nb;
+    contactBodies(*P, i, bodies, H, nb);
+    for (int t = 0; t < nb; ++t)
+      for (int r = 0; r < 3; ++r) {
+        double s = 0.0;
+        for (int m = 0; m < d; ++m) s = std::fma(H[t][r * d + m], Mx[(size_t)bodies[t] * d + m], s);
+        v[r] = v[r] + s;
+      }
+  }
+  void colMul(int i, const double* dx, double* Mx) const {
+    const int d = P->ndof;
+    int bodies[2]; const double* H[2]; int nb;
+    contactBodies(*P, i, bodies, H, nb);
+    for (int t = 0; t < nb; ++t) {
+      const double* Tt = &T[((size_t)i * 2 + t) * d * 3];
+      for (int m = 0; m < d; ++m) {
+        const double s = std::fma(Tt[m * 3 + 2], dx[2], std::fma(Tt[m * 3 + 1], dx[1], Tt[m * 3] * dx[0]));
+        Mx[(size_t)bodies[t] * d + m] = Mx[(size_t)bodies[t] * d + m] + s;
+      }
+    }
+  }
+  void velocity(const double* b, const double* Mx, double* y) const {  // y = b + H Mx
+    std::copy(b, b + 3 * (size_t)P->ncontacts, y);
+    for (int i = 0; i < P->ncontacts; ++i) rowMul(i, Mx, &y[3 * (size_t)i]);
+  }
+
+  double solve(const Law& law, const double* b, double* x, unsigned* itersOut = nullptr) const {
+    const int N = P->ncontacts;
+    const size_t n3 = 3 * (size_t)N;
+    std::vector<double> Mx((size_t)P->nbodies * P->ndof), y(n3), x_best;
+    double err_best = DBL_MAX;
+    computeMx(x, Mx.data());
+    velocity(b, Mx.data(), y.data());
+    {
+      const double err = eval(law, y.data(), x);
+      if (err < err_best) {
+        x_best.assign(x, x + n3);
+        err_best = err;
+      }
+    }
+    if (tryZeroAsWell) {
+      std::vector<double> zero(n3, 0.0);
+      const double err_zero = eval(law, b, zero.data());
+      if (err_zero < err_best) {
+        err_best = err_zero;
+        x_best.assign(n3, 0.0);
+        std::fill(x, x + n3, 0.0);
+        std::fill(Mx.begin(), Mx.end(), 0.0);
+      } else {
+        std::copy(x_best.begin(), x_best.end(), x);
+      }
+    }
+    trigger(0, err_best);
+    std::vector<unsigned char> skip(N, 0);
+    double ndxRef = 0;
+    const double absSkipTol = dmin(skipTol, tol);
+    const double absSkipIters = dmin((double)skipIters, (double)(unsigned)std::sqrt((double)N));
+    unsigned GSIter;
+    for (GSIter = 1; GSIter <= maxIters; ++GSIter) {
+      for (int i = 0; i < N; ++i) {
+        if (skip[i]) {
+          --skip[i];
+          continue;
+        }
+        double lx[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+        const double* L = &local[9 * (size_t)i];
+        double lb[3];
+        for (int r = 0; r < 3; ++r) lb[r] = b[3 * i + r] - dot3(&L[3 * r], lx);
+        rowMul(i, Mx.data(), lb);
+        double ldx[3] = {-lx[0], -lx[1], -lx[2]};
+        const bool ok = lawSolveLocal(law.desaxce, law.strat, L, lb, lx, law.mu[i], scaling[i]);
+        for (int k = 0; k < 3; ++k) ldx[k] = ldx[k] + lx[k];
+        if (!ok) {
+          ldx[0] *= .5; ldx[1] *= .5; ldx[2] *= .5;
+        }
+        for (int k = 0; k < 3; ++k) x[3 * i + k] = x[3 * i + k] + ldx[k];
+        colMul(i, ldx, Mx.data());
+        const double s2 = scaling[i] * scaling[i];
+        const double nx2 = s2 * sq3(lx);
+        const double ndx2 = s2 * sq3(ldx);
+        if (ndx2 > ndxRef) ndxRef = ndx2;
+        if (dmin(nx2, ndx2) < absSkipTol || ndx2 < skipTol * dmin(nx2, ndxRef))
+          skip[i] = (unsigned char)absSkipIters;
+      }
+      if (0 == (GSIter % evalEvery)) {
+        computeMx(x, Mx.data());
+        velocity(b, Mx.data(), y.data());
+        const double err = eval(law, y.data(), x);
+        if (err < err_best) {
+          x_best.assign(x, x + n3);
+          err_best = err;
+        }
+        trigger(GSIter, err);
+        if (err < tol) break;
+        ndxRef /= evalEvery;
+      }
+    }
+    if (GSIter > maxIters) std::copy(x_best.begin(), x_best.end(), x);
+    if (itersOut) *itersOut = GSIter > maxIters ? maxIters : GSIter;
+    return err_best;
+  }
+};
+
+// ---------------------------------------------------------------------------------------------
 // Cadoux fixed point (Interfaces/Cadoux.hpp:44-91): a Coulomb problem solved as a sequence of SOCQP problems
 // whose right-hand side carries the De Saxce change of variable of the previous velocity:
 //   s = W r + b, res = eval(Coulomb, s, r)

@@ -312,16 +312,9 @@ inline void contactBodies(const Primal& P, int i, int* bodies, const double** H,
   }
 }
 
-inline BSR assembleW(const Primal& P) {
+// T = M^-1 H^T for every (contact, slot): d x 3 row-major blocks at (2 j + t) d 3, slots in body order.
+inline std::vector<double> slotT(const Primal& P) {
   const int n = P.ncontacts, d = P.ndof;
-  // body -> contacts incidence
-  std::vector<std::vector<int>> byBody(P.nbodies);
-  for (int i = 0; i < n; ++i) {
-    int bodies[2]; const double* H[2]; int nb;
-    contactBodies(P, i, bodies, H, nb);
-    for (int t = 0; t < nb; ++t) byBody[bodies[t]].push_back(i);
-  }
-  // T_jk for every (contact, body)
   std::vector<double> T((size_t)n * 2 * d * 3, 0.0);
   for (int j = 0; j < n; ++j) {
     int bodies[2]; const double* H[2]; int nb;
@@ -337,6 +330,20 @@ inline BSR assembleW(const Primal& P) {
         }
     }
   }
+  return T;
+}
+
+inline BSR assembleW(const Primal& P) {
+  const int n = P.ncontacts, d = P.ndof;
+  // body -> contacts incidence
+  std::vector<std::vector<int>> byBody(P.nbodies);
+  for (int i = 0; i < n; ++i) {
+    int bodies[2]; const double* H[2]; int nb;
+    contactBodies(P, i, bodies, H, nb);
+    for (int t = 0; t < nb; ++t) byBody[bodies[t]].push_back(i);
+  }
+  // T_jk for every (contact, body)
+  const std::vector<double> T = slotT(P);
   BSR low;
   low.n = n;
   low.rowptr.assign(n + 1, 0);

@@ -96,6 +96,7 @@ EXPORTED = [
     "bogus_gpu_adjoint", "bogus_gpu_adjoint_device", "bogus_gpu_adjoint_dual_lower", "bogus_gpu_adjoint_primal",
     "bogus_gpu_add_compliance", "bogus_gpu_solve_cadoux_gs", "bogus_gpu_solve_cadoux_pg",
     "bogus_gpu_meche_options_default", "bogus_gpu_meche_from_primal", "bogus_gpu_meche_solve",
+    "bogus_gpu_solve_product_gs",
 ]
 
 
@@ -152,6 +153,8 @@ def lib():
                                               C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
     L.bogus_gpu_meche_solve.argtypes = [vp, _dp, vp, C.POINTER(MecheOptions), C.c_int, C.c_double,
                                         C.POINTER(C.c_double)]
+    L.bogus_gpu_solve_product_gs.argtypes = [vp, C.POINTER(GsOptions), vp, _dp, _dp, _dp, C.POINTER(C.c_double),
+                                             C.POINTER(C.c_uint)]
     L.bogus_gpu_admm_options_default.argtypes = [C.POINTER(AdmmOptions)]
     L.bogus_gpu_admm_options_default.restype = None
     L.bogus_gpu_solve_admm.argtypes = [vp, C.POINTER(AdmmOptions), C.c_double, vp, vp, _dp, _dp, _dp, _dp,
@@ -293,6 +296,12 @@ class GaussSeidel(_SolverBase):
         return o
 
 
+class ProductGaussSeidel(GaussSeidel):
+    """ProductGaussSeidel<HType, MInvType, true> (Core/BlockSolvers/ProductGaussSeidel.hpp): Gauss-Seidel on
+    W = H M^-1 H^T without forming W, for PrimalFrictionProblem.solveWith(pgs, r, staticProblem). Same setters and
+    defaults as GaussSeidel; the contacts are swept in their own order."""
+
+
 class ADMM(_SolverBase):
     """ADMM<HType> (Core/BlockSolvers/ADMM.hpp:41-110): tol 1e-6, 300 iterations, step size 1e-2,
     Accelerated variant."""
@@ -341,7 +350,33 @@ class PrimalFrictionProblem:
             self._gpu = g
         return self._gpu
 
-    def solveWith(self, admm: "ADMM", lambda_: float, v, r, prox=None) -> float:
+    def solveWith(self, solver, *args, **kwargs) -> float:
+        """PrimalFrictionProblem::solveWith:
+        - solveWith(ADMM, lambda_, v, r, prox=None): primal ADMM (see _solve_admm);
+        - solveWith(ProductGaussSeidel, r, staticProblem=False): the matrix-free Gauss-Seidel."""
+        if isinstance(solver, ProductGaussSeidel):
+            return self._solve_product_gs(solver, *args, **kwargs)
+        return self._solve_admm(solver, *args, **kwargs)
+
+    def _solve_product_gs(self, gs: "ProductGaussSeidel", r, staticProblem: bool = False) -> float:
+        if not (isinstance(r, np.ndarray) and r.dtype == np.float64 and r.flags.c_contiguous):
+            raise TypeError("r must be a C-contiguous float64 numpy array (solved in place)")
+        if r.size != 3 * self.objA.size:
+            raise ValueError("inconsistent r size")
+        g = self._uploaded()
+        g._bind(gs)
+        o = gs.options(staticProblem)
+        o.use_coloring = 0
+        res = C.c_double()
+        it = C.c_uint()
+        fptr = None if self.f is None else self.f.ctypes.data_as(C.c_void_p)
+        st = lib().bogus_gpu_solve_product_gs(g.handle, C.byref(o), fptr, self.w, self.mu, r.reshape(-1),
+                                              C.byref(res), C.byref(it))
+        _check(st)
+        self.last_status, self.last_iterations = st, it.value
+        return res.value
+
+    def _solve_admm(self, admm: "ADMM", lambda_: float, v, r, prox=None) -> float:
         """PrimalFrictionProblem::solveWith(ADMMType&, lambda, v, r): v (nbodies * ndof) and r (3n) are solved in
         place (float64, C-contiguous); returns the residual. prox: the QuadraticProxOp operator blocks
         [nbodies, ndof, ndof] of ADMM::solve(law, op, w, v, r) (default M^-1, as the reference passes)."""

@@ -139,6 +139,8 @@ struct bogus_gpu_problem {
   // misc work
   DevBuf<double> vx, vy, chunk, scalar;
   GSCache gs;
+  GSCache pgs;          // matrix-free Gauss-Seidel (levels from shared bodies, local matrices from H and M^-1)
+  DevBuf<double> pgs_Mx;
   // primal data for the assembly
   int nbodies = 0, ndof = 0, ncontacts = 0;
   DevBuf<double> minv, H, T, mf;
@@ -612,9 +614,8 @@ int prepare_gs(bogus_gpu_problem* h, double auto_reg, int use_coloring) {
 
 // One sweep: every level in order, then the skip update. Captured once per parity into a CUDA graph and
 // replayed (the arguments never change between sweeps of the same settings).
-int launch_sweep(bogus_gpu_problem* h, const GSArgs& a, int parity, double abs_skip_tol, double skip_tol,
-                 int abs_skip_iters, long long key) {
-  GSCache& g = h->gs;
+int launch_sweep(bogus_gpu_problem* h, GSCache& g, const GSArgs& a, int parity, double abs_skip_tol,
+                 double skip_tol, int abs_skip_iters, long long key, bool product) {
   cudaStream_t s = h->stream;
   const int nlevels = (int)g.level_off.size() - 1;
   if (g.sweep_key != key) g.drop_graphs();
@@ -622,7 +623,9 @@ int launch_sweep(bogus_gpu_problem* h, const GSArgs& a, int parity, double abs_s
     cudaGraph_t graph = nullptr;
     BG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    for (int L = 0; L < nlevels && e == cudaSuccess; ++L) e = launch_gs_level(a, g.level_off[L], g.level_off[L + 1], parity, s);
+    for (int L = 0; L < nlevels && e == cudaSuccess; ++L)
+      e = product ? launch_pgs_level(a, g.level_off[L], g.level_off[L + 1], parity, s)
+                  : launch_gs_level(a, g.level_off[L], g.level_off[L + 1], parity, s);
     if (e == cudaSuccess) e = launch_gs_skip(a, parity, abs_skip_tol, skip_tol, abs_skip_iters, s);
     const cudaError_t e2 = cudaStreamEndCapture(s, &graph);
     if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -777,6 +780,8 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   h->barrier.release();
   h->status.release();
   h->gs.release();
+  h->pgs.release();
+  h->pgs_Mx.release();
   cudaEventDestroy(h->ev0);
   cudaEventDestroy(h->ev1);
   cudaStreamDestroy(h->stream);
@@ -1063,7 +1068,7 @@ int run_gs_core(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* res
   int parity = 0;
   bool converged = false;
   for (it = 1; it <= o->max_iters; ++it) {
-    if (int e = launch_sweep(h, a, parity, abs_skip_tol, o->skip_tol, abs_skip_iters, key)) return e;
+    if (int e = launch_sweep(h, h->gs, a, parity, abs_skip_tol, o->skip_tol, abs_skip_iters, key, false)) return e;
     parity ^= 1;
     if (0 == (it % o->eval_every)) {
       if (int e = gs_eval(h, a, g.x.p, g.b.p, desaxce, use_inf, &err)) return e;
@@ -1138,6 +1143,247 @@ int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, doub
   BG_CUDA(cudaEventRecord(h->ev1, h->stream));
   if (int e = gs_store_x(h, r)) return e;
   BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  if (h->callback)
+    for (auto& t : trace) h->callback(t.first, t.second, h->callback_user);
+  return converged ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
+}
+
+// ---- matrix-free Gauss-Seidel (ProductGaussSeidel<HType, MInvType, true>; PrimalFrictionProblem::solveWith,
+//      PrimalFrictionProblem.cpp:41-59) ------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+// Levels from the contacts' bodies (two contacts depend on each other when they share a body), T = M^-1 H^T per
+// slot, local matrices sum_t H_t T_t with their scalings and regularisation.
+int prepare_pgs(bogus_gpu_problem* h, double auto_reg) {
+  GSCache& g = h->pgs;
+  if (g.valid && g.auto_reg == auto_reg) return BOGUS_GPU_OK;
+  g.drop_graphs();
+  const int n = h->ncontacts, nb = h->nbodies, d = h->ndof;
+  const size_t n3 = 3 * (size_t)n;
+  cudaStream_t s = h->stream;
+  if (int e = ensure_incidence(h)) return e;
+  BG_CUDA(h->T.ensure(2 * (size_t)n * d * 3));
+  BG_CUDA(launch_assembly_T(n, d, h->minv.p, h->cb.p, h->H.p, h->T.p, s));
+  BG_CUDA(g.local.ensure(9 * (size_t)n));
+  BG_CUDA(launch_pgs_local(n, d, h->cb.p, h->H.p, h->T.p, g.local.p, s));
+  std::vector<double> local(9 * (size_t)n), reg(n, 0.0), sc(n, 1.0);
+  BG_CUDA(cudaMemcpyAsync(local.data(), g.local.p, sizeof(double) * local.size(), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < n; ++i) {
+    double* D = &local[9 * (size_t)i];
+    sc[i] = dmax(1.0, ((D[0] + D[4]) + D[8]) / 3.0);
+    if (auto_reg > 0.) {
+      reg[i] = dmax(0.0, auto_reg - min_eigen_symmetric3(D));
+      D[0] += reg[i];
+      D[4] += reg[i];
+      D[8] += reg[i];
+    }
+  }
+  std::vector<int> last(nb, -1), level(n, 0);
+  int nlevels = n > 0 ? 1 : 0;
+  for (int i = 0; i < n; ++i) {
+    int lv = 0;
+    for (int t = 0; t < 2; ++t) {
+      const int b = h->h_cb[2 * (size_t)i + t];
+      if (b >= 0 && last[b] + 1 > lv) lv = last[b] + 1;
+    }
+    level[i] = lv;
+    for (int t = 0; t < 2; ++t) {
+      const int b = h->h_cb[2 * (size_t)i + t];
+      if (b >= 0 && lv > last[b]) last[b] = lv;
+    }
+    if (lv + 1 > nlevels) nlevels = lv + 1;
+  }
+  g.level_off.assign(nlevels + 1, 0);
+  for (int i = 0; i < n; ++i) ++g.level_off[level[i] + 1];
+  for (int L = 0; L < nlevels; ++L) g.level_off[L + 1] += g.level_off[L];
+  std::vector<int> order(n), fill(g.level_off.begin(), g.level_off.end() - 1);
+  for (int i = 0; i < n; ++i) order[fill[level[i]]++] = i;
+  const int ntiles = (n + kGSTile - 1) / kGSTile;
+  BG_CUDA(g.order.ensure(n));
+  BG_CUDA(g.reg.ensure(n));
+  BG_CUDA(g.scaling.ensure(n));
+  BG_CUDA(g.b.ensure(n3));
+  BG_CUDA(g.mu.ensure(n));
+  BG_CUDA(g.x.ensure(n3));
+  BG_CUDA(g.xbest.ensure(n3));
+  BG_CUDA(g.y.ensure(n3));
+  BG_CUDA(g.nx2.ensure(n));
+  BG_CUDA(g.ndx2.ensure(n));
+  BG_CUDA(g.skip.ensure(n));
+  BG_CUDA(g.processed.ensure(n));
+  BG_CUDA(g.tile_max.ensure(2 * (size_t)(ntiles > 0 ? ntiles : 1)));
+  BG_CUDA(g.ndx_ref.ensure(2));
+  BG_CUDA(g.chunk.ensure((n + 31) / 32 + 1));
+  BG_CUDA(g.scalar.ensure(2));
+  BG_CUDA(h->pgs_Mx.ensure((size_t)nb * d));
+  BG_CUDA(h->mf.ensure((size_t)nb * d));
+  BG_CUDA(cudaMemcpyAsync(g.order.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(g.local.p, local.data(), sizeof(double) * local.size(), cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(g.reg.p, reg.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(g.scaling.p, sc.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  g.auto_reg = auto_reg;
+  g.use_coloring = 0;
+  g.valid = true;
+  return BOGUS_GPU_OK;
+}
+
+// error at x with y = b + H Mx after recomputing Mx = M^-1 H^T x (ProductGaussSeidel.impl.hpp:249-252, 283-285)
+int pgs_eval(bogus_gpu_problem* h, bool desaxce, bool use_inf, double* err) {
+  GSCache& g = h->pgs;
+  const int n = h->ncontacts;
+  cudaStream_t s = h->stream;
+  BG_CUDA(launch_pgs_mx(h->nbodies, h->ndof, h->bptr.p, h->bent.p, h->T.p, g.x.p, h->pgs_Mx.p, s));
+  BG_CUDA(launch_pgs_y(n, h->ndof, h->cb.p, h->H.p, h->pgs_Mx.p, g.b.p, g.y.p, s));
+  BG_CUDA(launch_eval_chunks(n, g.x.p, g.y.p, g.mu.p, g.scaling.p, desaxce, use_inf, g.chunk.p, s));
+  BG_CUDA(launch_combine(g.chunk.p, (n + 31) / 32, use_inf, use_inf ? 0.0 : (double)(1 + n), g.scalar.p, s));
+  BG_CUDA(cudaMemcpyAsync(err, g.scalar.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  h->last_launches += 4;
+  return BOGUS_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bogus_gpu_solve_product_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, const double* f,
+                               const double* w, const double* mu, double* r, double* residual, unsigned* iters) {
+  if (int e = check_handle(h)) return e;
+  if (int e = check_gs_options(o)) return e;
+  if (o->use_coloring)
+    return fail(BOGUS_GPU_BAD_INPUT, "the matrix-free sweep visits the contacts in their own order (no coloring)");
+  if (h->nbodies == 0) return fail(BOGUS_GPU_NO_PROBLEM, "no primal problem set (bogus_gpu_set_primal)");
+  const int n = h->ncontacts, nb = h->nbodies, d = h->ndof;
+  const size_t n3 = 3 * (size_t)n, m = (size_t)nb * d;
+  if (n == 0) {
+    if (residual) *residual = 0.0;
+    if (iters) *iters = 0;
+    return BOGUS_GPU_OK;
+  }
+  if (!w || !mu || !r) return fail(BOGUS_GPU_BAD_INPUT, "null w, mu or r");
+  if (int e = check_finite(w, n3, "w")) return e;
+  if (int e = check_finite(mu, n, "mu")) return e;
+  if (int e = check_finite(r, n3, "r")) return e;
+  if (f)
+    if (int e = check_finite(f, m, "f")) return e;
+  if (int e = set_device(h)) return e;
+  if (int e = prepare_pgs(h, o->auto_regularization)) return e;
+  GSCache& g = h->pgs;
+  cudaStream_t s = h->stream;
+  h->last_launches = 0;
+  // b = w - H M^-1 f (the dual's right-hand side, PrimalFrictionProblem.cpp:44-45)
+  DevBuf<double> dw, df;
+  BG_CUDA(dw.ensure(n3));
+  BG_CUDA(cudaMemcpyAsync(dw.p, w, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  if (f) {
+    BG_CUDA(df.ensure(m));
+    BG_CUDA(cudaMemcpyAsync(df.p, f, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  }
+  BG_CUDA(launch_assembly_b(n, nb, d, h->minv.p, f ? df.p : nullptr, h->cb.p, h->H.p, dw.p, h->mf.p, g.b.p, s));
+  BG_CUDA(cudaMemcpyAsync(g.mu.p, mu, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(g.x.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  const int ntiles = (n + kGSTile - 1) / kGSTile;
+  BG_CUDA(cudaMemsetAsync(g.tile_max.p, 0, sizeof(unsigned long long) * 2 * ntiles, s));
+  BG_CUDA(cudaMemsetAsync(g.ndx_ref.p, 0, sizeof(double) * 2, s));
+  BG_CUDA(cudaMemsetAsync(g.skip.p, 0, n, s));
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  GSArgs a{};
+  a.n = n;
+  a.local = g.local.p;
+  a.reg = g.reg.p;
+  a.scaling = g.scaling.p;
+  a.b = g.b.p;
+  a.mu = g.mu.p;
+  a.x = g.x.p;
+  a.nx2 = g.nx2.p;
+  a.ndx2 = g.ndx2.p;
+  a.skip = g.skip.p;
+  a.processed = g.processed.p;
+  a.tile_max = g.tile_max.p;
+  a.ndx_ref = g.ndx_ref.p;
+  a.order = g.order.p;
+  a.desaxce = o->static_problem ? 0 : 1;
+  a.strat = o->local_strategy;
+  a.H = h->H.p;
+  a.T = h->T.p;
+  a.cb = h->cb.p;
+  a.Mx = h->pgs_Mx.p;
+  a.d = d;
+  const bool desaxce = !o->static_problem;
+  const bool use_inf = o->use_infinity_norm != 0;
+  double err_best = DBL_MAX, err = 0;
+  bool has_best = false;
+  if (int e = pgs_eval(h, desaxce, use_inf, &err)) return e;
+  if (err < err_best) {
+    BG_CUDA(cudaMemcpyAsync(g.xbest.p, g.x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+    err_best = err;
+    has_best = true;
+  }
+  if (o->try_zero_as_well) {
+    BG_CUDA(cudaMemsetAsync(g.y.p, 0, sizeof(double) * n3, s));
+    BG_CUDA(launch_eval_chunks(n, g.y.p, g.b.p, g.mu.p, g.scaling.p, desaxce, use_inf, g.chunk.p, s));
+    BG_CUDA(launch_combine(g.chunk.p, (n + 31) / 32, use_inf, use_inf ? 0.0 : (double)(1 + n), g.scalar.p, s));
+    double err_zero = 0;
+    BG_CUDA(cudaMemcpyAsync(&err_zero, g.scalar.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+    h->last_launches += 2;
+    if (err_zero < err_best) {
+      err_best = err_zero;
+      BG_CUDA(cudaMemsetAsync(g.xbest.p, 0, sizeof(double) * n3, s));
+      BG_CUDA(cudaMemsetAsync(g.x.p, 0, sizeof(double) * n3, s));
+      BG_CUDA(cudaMemsetAsync(h->pgs_Mx.p, 0, sizeof(double) * m, s));
+      has_best = true;
+    } else if (has_best) {
+      BG_CUDA(cudaMemcpyAsync(g.x.p, g.xbest.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  std::vector<std::pair<unsigned, double>> trace;
+  trace.push_back({0u, err_best});
+  const double abs_skip_tol = dmin(o->skip_tol, o->tol);
+  const int abs_skip_iters = (int)dmin((double)o->skip_iters, (double)(unsigned)std::sqrt((double)n));
+  long long key = 0;
+  {
+    double st = o->skip_tol, ast = abs_skip_tol;
+    unsigned long long b1, b2;
+    std::memcpy(&b1, &st, 8);
+    std::memcpy(&b2, &ast, 8);
+    key = (long long)((b1 * 1000003ull) ^ (b2 * 10007ull) ^ ((unsigned long long)abs_skip_iters << 8) ^
+                      ((unsigned long long)a.desaxce << 4) ^ (unsigned long long)a.strat);
+    if (key < 0) key = -key - 1;
+  }
+  unsigned it;
+  int parity = 0;
+  bool converged = false;
+  for (it = 1; it <= o->max_iters; ++it) {
+    if (int e = launch_sweep(h, g, a, parity, abs_skip_tol, o->skip_tol, abs_skip_iters, key, true)) return e;
+    parity ^= 1;
+    if (0 == (it % o->eval_every)) {
+      if (int e = pgs_eval(h, desaxce, use_inf, &err)) return e;
+      if (err < err_best) {
+        BG_CUDA(cudaMemcpyAsync(g.xbest.p, g.x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+        err_best = err;
+        has_best = true;
+      }
+      trace.push_back({it, err});
+      if (err < o->tol) {
+        converged = true;
+        break;
+      }
+      BG_CUDA(launch_scale_scalar(g.ndx_ref.p + parity, (double)o->eval_every, s));
+      h->last_launches += 1;
+    }
+  }
+  const double* result = (it > o->max_iters && has_best) ? g.xbest.p : g.x.p;
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  BG_CUDA(cudaMemcpyAsync(r, result, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  if (residual) *residual = err_best;
+  if (iters) *iters = it > o->max_iters ? o->max_iters : it;
   if (h->callback)
     for (auto& t : trace) h->callback(t.first, t.second, h->callback_user);
   return converged ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
@@ -1408,6 +1654,7 @@ int bogus_gpu_meche_from_primal(bogus_gpu_problem* h, unsigned nobj, const unsig
   h->ndof = (int)d;
   h->ncontacts = (int)n;
   h->h_cb = std::move(cbh);
+  h->pgs.valid = false;
   h->h_objA = std::move(oA);
   h->admm_incidence_valid = false;
   h->meche_ndof.assign(ndof, ndof + nobj);
@@ -1423,10 +1670,10 @@ int bogus_gpu_meche_solve(bogus_gpu_problem* h, double* r, double* v, const bogu
   if (int e = check_handle(h)) return e;
   if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
   if (!h->meche_valid) return fail(BOGUS_GPU_NO_PROBLEM, "no problem set (bogus_gpu_meche_from_primal)");
-  if (o->algorithm == BOGUS_GPU_MECHE_MATRIX_FREE_GAUSS_SEIDEL || o->algorithm == BOGUS_GPU_MECHE_DUAL_AMA)
-    return fail(BOGUS_GPU_BAD_INPUT, "MatrixFreeGaussSeidel and DualAMA are not available on the GPU");
+  if (o->algorithm == BOGUS_GPU_MECHE_DUAL_AMA)
+    return fail(BOGUS_GPU_BAD_INPUT, "DualAMA is not available on the GPU");
   if (o->algorithm != BOGUS_GPU_MECHE_GAUSS_SEIDEL && o->algorithm != BOGUS_GPU_MECHE_PROJECTED_GRADIENT &&
-      o->algorithm != BOGUS_GPU_MECHE_ADMM)
+      o->algorithm != BOGUS_GPU_MECHE_ADMM && o->algorithm != BOGUS_GPU_MECHE_MATRIX_FREE_GAUSS_SEIDEL)
     return fail(BOGUS_GPU_BAD_INPUT, "unknown algorithm");
   const int n = h->ncontacts, nb = h->nbodies, d = h->ndof;
   const size_t n3 = 3 * (size_t)n, md = (size_t)nb * d;
@@ -1476,6 +1723,26 @@ int bogus_gpu_meche_solve(bogus_gpu_problem* h, double* r, double* v, const bogu
                               vp.data(), rl.data(), &res, nullptr);
     if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
     if (n > 0) BG_CUDA(cudaMemcpyAsync(h->meche_r.p, rl.data(), sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  } else if (o->algorithm == BOGUS_GPU_MECHE_MATRIX_FREE_GAUSS_SEIDEL) {
+    // PrimalFrictionProblem::solveWith(ProductGaussSeidelType&, r_loc, staticProblem) (MecheInterface.cpp:290-302)
+    bogus_gpu_gs_options go;
+    bogus_gpu_gs_options_default(&go);
+    if (o->tolerance != 0.) go.tol = o->tolerance;
+    if (o->max_iters != 0) go.max_iters = o->max_iters;
+    if (o->gs_skip_iters >= 0) go.skip_iters = (unsigned)o->gs_skip_iters;
+    go.use_infinity_norm = o->use_infinity_norm;
+    go.auto_regularization = o->gs_regularization;
+    go.try_zero_as_well = o->try_zero_as_well;
+    go.static_problem = static_problem ? 1 : 0;
+    st = bogus_gpu_solve_product_gs(h, &go, h->meche_f.data(), h->meche_wloc.data(), h->meche_mu.data(), rl.data(),
+                                    &res, nullptr);
+    if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+    if (n > 0) {
+      BG_CUDA(cudaMemcpyAsync(h->meche_r.p, rl.data(), sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+      BG_CUDA(cudaStreamSynchronize(s));
+    }
+    if (v)
+      if (int e = velocity()) return e;
   } else {
     if (!h->meche_dual) {
       if (int e = bogus_gpu_assemble_dual(h, h->meche_f.data(), h->meche_wloc.data(), h->meche_mu.data())) return e;
@@ -1580,6 +1847,7 @@ int bogus_gpu_set_primal(bogus_gpu_problem* h, int nbodies, int ndof, const doub
   h->ndof = ndof;
   h->ncontacts = ncontacts;
   h->h_cb = std::move(cbh);
+  h->pgs.valid = false;
   h->h_objA.assign(objA, objA + ncontacts);
   h->admm_incidence_valid = false;
   return BOGUS_GPU_OK;

@@ -129,12 +129,27 @@ struct GSArgs {
   double* ndx_ref;               // 2 (sweep parity)
   const int* order;              // contacts grouped by level (sweep positions)
   int desaxce, strat;
+  // matrix-free sweep (ProductGaussSeidel): slot Jacobians H (3 x d), T = M^-1 H^T (d x 3), slot bodies cb,
+  // Mx = M^-1 H^T x per body (nbodies x d)
+  const double* H;
+  const double* T;
+  const int* cb;
+  double* Mx;
+  int d;
 };
 constexpr int kGSTile = 1024;
 cudaError_t launch_gs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s);
 cudaError_t launch_gs_skip(const GSArgs& a, int parity, double abs_skip_tol, double skip_tol, int abs_skip_iters,
                            cudaStream_t s);
 cudaError_t launch_scale_scalar(double* p, double divisor, cudaStream_t s);
+// matrix-free Gauss-Seidel (kernels_gs.cu)
+cudaError_t launch_pgs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s);
+cudaError_t launch_pgs_local(int n, int d, const int* cb, const double* H, const double* T, double* local,
+                             cudaStream_t s);
+cudaError_t launch_pgs_mx(int nbodies, int d, const int* bptr, const int* bent, const double* T, const double* x,
+                          double* Mx, cudaStream_t s);
+cudaError_t launch_pgs_y(int n, int d, const int* cb, const double* H, const double* Mx, const double* b, double* y,
+                         cudaStream_t s);
 cudaError_t measure_fp64_peak(int device, double* tflops);
 
 // Primal ADMM / AMA (kernels_admm.cu): Core/BlockSolvers/ADMM.impl.hpp:54-127 with QuadraticProxOp

@@ -148,4 +148,155 @@ cudaError_t launch_gs_skip(const GSArgs& a, int parity, double abs_skip_tol, dou
   return cudaGetLastError();
 }
 
+// ---- matrix-free sweep (ProductGaussSeidel<HType, MInvType, true>, ProductGaussSeidel.impl.hpp:108-296) -----
+// Same levels as the assembled sweep (contacts sharing a body never share a level), so in one level every body's
+// Mx = M^-1 H^T x is read and updated by at most one contact:
+//   lb = b_i - local_i x_i + sum_t H_t Mx_(body t)  (rowMultiply), local solve, x_i += dx,
+//   Mx_(body t) += T_t dx  (colMultiply, T = M^-1 H^T).
+// Orders: local_i x_i per row with the dot3 chain, subtracted from b_i; each slot's H_t Mx row as a chain over the
+// dofs from 0, added to lb; T_t dx with the dot3 chain, added to Mx.
+__global__ void __launch_bounds__(32) k_pgs_level(GSArgs a, int l0, int l1, int parity) {
+  const int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= l1) return;
+  const int i = a.order[t];
+  if (a.skip[i]) {
+    a.skip[i] = (unsigned char)(a.skip[i] - 1);
+    a.processed[i] = 0;
+    return;
+  }
+  const int d = a.d;
+  double lx[3] = {a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2]};
+  double A[9];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) A[e] = a.local[9 * (size_t)i + e];
+  double lb[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) lb[r] = a.b[3 * i + r] - dot3(&A[3 * r], lx);
+  for (int sl = 0; sl < 2; ++sl) {
+    const int body = a.cb[2 * i + sl];
+    if (body < 0) continue;
+    const double* Hs = a.H + (2 * (size_t)i + sl) * 3 * d;
+    const double* mx = a.Mx + (size_t)body * d;
+    for (int r = 0; r < 3; ++r) {
+      double s = 0.0;
+      for (int m = 0; m < d; ++m) s = fma(Hs[r * d + m], mx[m], s);
+      lb[r] = lb[r] + s;
+    }
+  }
+  double ldx[3] = {-lx[0], -lx[1], -lx[2]};
+  const double sc = a.scaling[i];
+  const bool ok = law_solve_local(a.desaxce != 0, a.strat, A, lb, lx, a.mu[i], sc);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) ldx[k] = ldx[k] + lx[k];
+  if (!ok) {
+    ldx[0] *= .5;
+    ldx[1] *= .5;
+    ldx[2] *= .5;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) a.x[3 * i + k] = a.x[3 * i + k] + ldx[k];
+  for (int sl = 0; sl < 2; ++sl) {
+    const int body = a.cb[2 * i + sl];
+    if (body < 0) continue;
+    const double* Ts = a.T + (2 * (size_t)i + sl) * d * 3;
+    double* mx = a.Mx + (size_t)body * d;
+    for (int m = 0; m < d; ++m) mx[m] = mx[m] + fma(Ts[m * 3 + 2], ldx[2], fma(Ts[m * 3 + 1], ldx[1], Ts[m * 3] * ldx[0]));
+  }
+  const double s2 = sc * sc;
+  const double nx2 = s2 * sq3(lx);
+  const double ndx2 = s2 * sq3(ldx);
+  a.nx2[i] = nx2;
+  a.ndx2[i] = ndx2;
+  a.processed[i] = 1;
+  if (ndx2 > 0.0) {
+    const int ntiles = (a.n + kGSTile - 1) / kGSTile;
+    atomicMax(a.tile_max + parity * ntiles + i / kGSTile, dbits(ndx2));
+  }
+}
+
+cudaError_t launch_pgs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s) {
+  if (l1 <= l0) return cudaSuccess;
+  k_pgs_level<<<(l1 - l0 + 31) / 32, 32, 0, s>>>(a, l0, l1, parity);
+  return cudaGetLastError();
+}
+
+// local_i = sum_t H_t T_t: W's diagonal block in the order of the assembly (slots in body order, dofs inner)
+__global__ void k_pgs_local(int n, int d, const int* __restrict__ cb, const double* __restrict__ H,
+                            const double* __restrict__ T, double* __restrict__ local) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      double acc = 0.0;
+      for (int sl = 0; sl < 2; ++sl) {
+        if (cb[2 * i + sl] < 0) continue;
+        const double* Hs = H + (2 * (size_t)i + sl) * 3 * d;
+        const double* Ts = T + (2 * (size_t)i + sl) * d * 3;
+        for (int m = 0; m < d; ++m) acc = fma(Hs[r * d + m], Ts[m * 3 + c], acc);
+      }
+      local[9 * (size_t)i + 3 * r + c] = acc;
+    }
+}
+
+cudaError_t launch_pgs_local(int n, int d, const int* cb, const double* H, const double* T, double* local,
+                             cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_pgs_local<<<(n + 127) / 128, 128, 0, s>>>(n, d, cb, H, T, local);
+  return cudaGetLastError();
+}
+
+// Mx_b = sum over b's incidences (increasing contact) of T x_i, one fma chain per dof
+__global__ void k_pgs_mx(int nbodies, int d, const int* __restrict__ bptr, const int* __restrict__ bent,
+                         const double* __restrict__ T, const double* __restrict__ x, double* __restrict__ Mx) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbodies) return;
+  for (int m = 0; m < d; ++m) {
+    double acc = 0.0;
+    for (int e = bptr[b]; e < bptr[b + 1]; ++e) {
+      const int ent = bent[e];
+      const int i = ent >> 1;
+      const double* Ts = T + (size_t)ent * d * 3;
+      acc = fma(Ts[m * 3], x[3 * i], acc);
+      acc = fma(Ts[m * 3 + 1], x[3 * i + 1], acc);
+      acc = fma(Ts[m * 3 + 2], x[3 * i + 2], acc);
+    }
+    Mx[(size_t)b * d + m] = acc;
+  }
+}
+
+cudaError_t launch_pgs_mx(int nbodies, int d, const int* bptr, const int* bent, const double* T, const double* x,
+                          double* Mx, cudaStream_t s) {
+  if (nbodies <= 0) return cudaSuccess;
+  k_pgs_mx<<<(nbodies + 127) / 128, 128, 0, s>>>(nbodies, d, bptr, bent, T, x, Mx);
+  return cudaGetLastError();
+}
+
+// y = b + H Mx, each slot's row chain added to y_i
+__global__ void k_pgs_y(int n, int d, const int* __restrict__ cb, const double* __restrict__ H,
+                        const double* __restrict__ Mx, const double* __restrict__ b, double* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v[3] = {b[3 * i], b[3 * i + 1], b[3 * i + 2]};
+  for (int sl = 0; sl < 2; ++sl) {
+    const int body = cb[2 * i + sl];
+    if (body < 0) continue;
+    const double* Hs = H + (2 * (size_t)i + sl) * 3 * d;
+    for (int r = 0; r < 3; ++r) {
+      double s = 0.0;
+      for (int m = 0; m < d; ++m) s = fma(Hs[r * d + m], Mx[(size_t)body * d + m], s);
+      v[r] = v[r] + s;
+    }
+  }
+  y[3 * i] = v[0];
+  y[3 * i + 1] = v[1];
+  y[3 * i + 2] = v[2];
+}
+
+cudaError_t launch_pgs_y(int n, int d, const int* cb, const double* H, const double* Mx, const double* b, double* y,
+                         cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_pgs_y<<<(n + 127) / 128, 128, 0, s>>>(n, d, cb, H, Mx, b, y);
+  return cudaGetLastError();
+}
+
 }  // namespace bogus_gpu

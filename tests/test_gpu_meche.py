@@ -69,6 +69,7 @@ def assert_same(g, o):
     (1, {"pg_variant": 3}),                     # projected gradient (APGD)
     (1, {"cadoux_iters": 8}),                   # projected gradient (SPG, the facade's default) + Cadoux
     (0, {"cadoux_iters": 5}),                   # Gauss-Seidel + Cadoux
+    (2, {}),                                    # matrix-free Gauss-Seidel
 ])
 def test_small_friction_world_bitwise(bg, oracle, algorithm, extra):
     _, inp = small_friction_world()
@@ -84,7 +85,7 @@ def test_small_friction_world_admm_bitwise(bg, oracle):
     assert g[0] < 1e-9
 
 
-@pytest.mark.parametrize("case", ["gs", "gs_colored_regularized", "pg_static", "gs_cadoux", "admm_v0"])
+@pytest.mark.parametrize("case", ["gs", "gs_colored_regularized", "pg_static", "gs_cadoux", "admm_v0", "matrix_free"])
 def test_random_world_problem_bitwise(bg, oracle, case):
     inp = random_world_problem()
     n = len(inp["objA"])
@@ -97,6 +98,8 @@ def test_random_world_problem_bitwise(bg, oracle, case):
     elif case == "pg_static":
         g, o = run_pair(bg, oracle, inp, r0, static=True, algorithm=1, pg_variant=3, tolerance=1e-8,
                         max_iters=300, inf_norm=True)
+    elif case == "matrix_free":
+        g, o = run_pair(bg, oracle, inp, r0, algorithm=2, tolerance=1e-8, max_iters=75, gs_regularization=1e-3)
     elif case == "gs_cadoux":
         g, o = run_pair(bg, oracle, inp, r0, algorithm=0, cadoux_iters=4, tolerance=1e-8, max_iters=60)
     else:
@@ -110,7 +113,7 @@ def test_meche_rejects_unavailable_algorithms_and_singular_mass(bg):
     _, inp = small_friction_world()
     M = bg.MecheFrictionProblem()
     M.fromPrimal(**inp)
-    for alg in (bg.MECHE_MATRIX_FREE_GAUSS_SEIDEL, bg.MECHE_DUAL_AMA):
+    for alg in (bg.MECHE_DUAL_AMA,):
         o = bg.MecheOptions()
         o.algorithm = alg
         with pytest.raises(bg.BogusGpuError):

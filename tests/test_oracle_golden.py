@@ -334,3 +334,15 @@ def test_meche_admm_matches_the_primal_solver(oracle):
     E = inp["E"]
     r_loc = np.concatenate([E[i].T @ r[3 * i:3 * i + 3] for i in range(2)])
     assert np.allclose(r_loc, r_o, rtol=0, atol=1e-6)
+
+
+# ---- ProductGaussSeidel (Core/BlockSolvers/ProductGaussSeidel.impl.hpp): the matrix-free sweep reaches the
+# Coulomb solution of tests/SmallFrictionPb.hpp, as Gauss-Seidel on the assembled W does ---------------------
+@pytest.mark.parametrize("strategy", [0, 3])
+def test_small_friction_product_gauss_seidel(oracle, golden, strategy):
+    s = golden["small_friction_pb"]
+    P = oracle.PrimalProblem(np.array(s["minv"]), s["objA"], s["objB"], np.array(s["HA"]), np.array(s["HB"]))
+    res, r, _ = P.solve_product_gs(np.array(s["f_padded"]), np.array(s["w"]), np.array(s["mu"]), np.ones(6),
+                                   coulomb=True, strategy=strategy, tol=1e-8)
+    assert res < s["res_tol"]
+    assert isApprox(s["sol"], r, s["sol_rel_tol"])
