@@ -21,37 +21,63 @@ namespace bogus_gpu {
 
 __device__ __forceinline__ unsigned long long dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
 
-// One warp per CTA: a level is latency bound (long dependent FP64 chains per contact), so its contacts are
-// spread over as many SMs as possible.
+// One warp per contact (a CTA of 32 threads): a level is latency bound (long dependent FP64 chains per contact),
+// so its contacts are spread over as many SMs as possible, and contacts whose local solves take different
+// branches never share a warp. The lanes stage up to 32 blocks of the row (and the x of their columns) at a
+// time in shared memory; lane 0 accumulates them in column order and runs the local solve.
 __global__ void __launch_bounds__(32) k_gs_level(GSArgs a, int l0, int l1, int parity) {
-  const int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = l0 + blockIdx.x;
   if (t >= l1) return;
+  const int lane = threadIdx.x;
   const int i = a.order[t];
-  if (a.skip[i]) {
-    a.skip[i] = (unsigned char)(a.skip[i] - 1);
-    a.processed[i] = 0;
+  const unsigned char sk = a.skip[i];
+  __syncwarp();  // every lane has read the counter before lane 0 changes it: the branch below is warp-uniform
+  if (sk) {
+    if (lane == 0) {
+      a.skip[i] = (unsigned char)(sk - 1);
+      a.processed[i] = 0;
+    }
     return;
   }
+  __shared__ double sB[32][12];
+  __shared__ int sJ[32];
   double lx[3] = {a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2]};
   const double reg = a.reg[i];
   double lb[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) lb[k] = a.b[3 * i + k] - reg * lx[k];
-  const int k1 = a.rowptr[i + 1];
-  for (int k = a.rowptr[i]; k < k1; ++k) {
-    const int j = a.col[k];
-    if (j == i) continue;
-    const double* B = a.val + 9 * (size_t)k;
-    const double x0 = a.x[3 * j], x1 = a.x[3 * j + 1], x2 = a.x[3 * j + 2];
+  const int k0 = a.rowptr[i], k1 = a.rowptr[i + 1];
+  for (int base = k0; base < k1; base += 32) {
+    const int k = base + lane;
+    if (k < k1) {
+      const int j = a.col[k];
+      sJ[lane] = j;
+      const double* B = a.val + 9 * (size_t)k;
 #pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      double s = lb[r];
-      s = fma(B[3 * r + 0], x0, s);
-      s = fma(B[3 * r + 1], x1, s);
-      s = fma(B[3 * r + 2], x2, s);
-      lb[r] = s;
+      for (int e = 0; e < 9; ++e) sB[lane][e] = B[e];
+      sB[lane][9] = a.x[3 * j];
+      sB[lane][10] = a.x[3 * j + 1];
+      sB[lane][11] = a.x[3 * j + 2];
     }
+    __syncwarp();
+    if (lane == 0) {
+      const int cnt = min(32, k1 - base);
+      for (int q = 0; q < cnt; ++q) {
+        if (sJ[q] == i) continue;
+        const double* B = sB[q];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          double s = lb[r];
+          s = fma(B[3 * r + 0], B[9], s);
+          s = fma(B[3 * r + 1], B[10], s);
+          s = fma(B[3 * r + 2], B[11], s);
+          lb[r] = s;
+        }
+      }
+    }
+    __syncwarp();
   }
+  if (lane != 0) return;
   double A[9];
 #pragma unroll
   for (int e = 0; e < 9; ++e) A[e] = a.local[9 * (size_t)i + e];
@@ -82,7 +108,7 @@ __global__ void __launch_bounds__(32) k_gs_level(GSArgs a, int l0, int l1, int p
 
 cudaError_t launch_gs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s) {
   if (l1 <= l0) return cudaSuccess;
-  k_gs_level<<<(l1 - l0 + 31) / 32, 32, 0, s>>>(a, l0, l1, parity);
+  k_gs_level<<<l1 - l0, 32, 0, s>>>(a, l0, l1, parity);
   return cudaGetLastError();
 }
 
@@ -156,8 +182,9 @@ cudaError_t launch_gs_skip(const GSArgs& a, int parity, double abs_skip_tol, dou
 // Orders: local_i x_i per row with the dot3 chain, subtracted from b_i; each slot's H_t Mx row as a chain over the
 // dofs from 0, added to lb; T_t dx with the dot3 chain, added to Mx.
 __global__ void __launch_bounds__(32) k_pgs_level(GSArgs a, int l0, int l1, int parity) {
-  const int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= l1) return;
+  // one contact per warp (lane 0): contacts whose local solves branch differently never share a warp
+  const int t = l0 + blockIdx.x;
+  if (t >= l1 || threadIdx.x != 0) return;
   const int i = a.order[t];
   if (a.skip[i]) {
     a.skip[i] = (unsigned char)(a.skip[i] - 1);
@@ -216,7 +243,7 @@ __global__ void __launch_bounds__(32) k_pgs_level(GSArgs a, int l0, int l1, int 
 
 cudaError_t launch_pgs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s) {
   if (l1 <= l0) return cudaSuccess;
-  k_pgs_level<<<(l1 - l0 + 31) / 32, 32, 0, s>>>(a, l0, l1, parity);
+  k_pgs_level<<<l1 - l0, 32, 0, s>>>(a, l0, l1, parity);
   return cudaGetLastError();
 }
 
