@@ -347,6 +347,16 @@ def run_batch(args) -> None:
     torch.cuda.synchronize()
     batched_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     st = D.solve_stats()
+    # the FP32-refined batch (500 FP32 iterations, then up to 50 FP64 ones per problem)
+    pgm = bogus_gpu.ProjectedGradient()
+    pgm.setTol(TOL)
+    pgm.setMaxIters(MAX_ITERS)
+    pgm.setMixedPrecision(True, 50)
+    for _ in range(2):
+        with torch.cuda.stream(stream):
+            r.zero_()
+        res_m, its_m = D.solveBatch_device(pgm, r.data_ptr())
+    st_m = D.solve_stats()
     # the single-problem path, problem by problem, on every 16th problem by size (stratified), scaled by 16
     rp, cl, vl = D.W_lower()
     vl = vl.reshape(-1, 9)
@@ -379,7 +389,10 @@ def run_batch(args) -> None:
         "loop_single_gpu_ms_est": t_single * 1e3 * scale, "cpu_oracle_ms_est": t_cpu * 1e3 * scale,
         "cpu_threads": pyoracle.num_threads(), "sample": f"{len(sample)} problems (every 16th by size), scaled",
         "speedup_vs_loop": t_single * 1e3 * scale / batched_ms, "identical_on_sample": bool(same),
-        "algorithmic_gbs": st["algorithmic_bytes"] / (st["device_ms"] * 1e-3) / 1e9}), flush=True)
+        "algorithmic_gbs": st["algorithmic_bytes"] / (st["device_ms"] * 1e-3) / 1e9,
+        "fp32_refined": {"kernel_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"],
+                         "converged_fraction": float(np.mean(res_m < TOL)),
+                         "speedup_vs_fp64_batch": st["device_ms"] / st_m["device_ms"]}}), flush=True)
 
 
 def run_gs(args) -> None:

@@ -133,6 +133,8 @@ struct bogus_gpu_problem {
   // FP32 copies of W (interleaved), b, mu, scalings and FP32 work (mixed precision), valid while W is unchanged
   bool fp32_valid = false;
   DevBuf<float> val32, b32, mu32, sc32, X32, MX32, Y32, S032, XB32, Wv32;
+  DevBuf<float> val32p;  // FP32 copy of W's plain BSR values (batched FP32 solves)
+  bool fp32p_valid = false;
   DevBuf<PGOut> pgout;
   DevBuf<unsigned> barrier;
   DevBuf<int> status;
@@ -221,6 +223,7 @@ int upload_full(bogus_gpu_problem* h, const HostBSR& f, const double* b, const d
   h->gs.valid = false;
   h->nproblems = 0;
   h->fp32_valid = false;
+  h->fp32p_valid = false;
   h->il_valid = false;
   h->adj_valid = false;
   return BOGUS_GPU_OK;
@@ -748,7 +751,8 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   for (auto* b : {&h->val, &h->b, &h->mu, &h->scaling, &h->X, &h->MX, &h->Y, &h->S0, &h->XB, &h->Wv, &h->csum,
                   &h->scal, &h->trace, &h->vx, &h->vy, &h->chunk, &h->scalar, &h->minv, &h->H, &h->T, &h->mf})
     b->release();
-  for (auto* b : {&h->val32, &h->b32, &h->mu32, &h->sc32, &h->X32, &h->MX32, &h->Y32, &h->S032, &h->XB32, &h->Wv32})
+  for (auto* b : {&h->val32, &h->b32, &h->mu32, &h->sc32, &h->X32, &h->MX32, &h->Y32, &h->S032, &h->XB32, &h->Wv32,
+                  &h->val32p})
     b->release();
   h->slot0.release();
   h->chunk_order.release();
@@ -854,6 +858,7 @@ int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* 
   h->gs.valid = false;
   h->nproblems = 0;
   h->fp32_valid = false;
+  h->fp32p_valid = false;
   h->il_valid = false;
   h->adj_valid = false;
   return BOGUS_GPU_OK;
@@ -2152,6 +2157,7 @@ int bogus_gpu_add_compliance(bogus_gpu_problem* h, const double* c) {
   }
   h->gs.valid = false;
   h->fp32_valid = false;
+  h->fp32p_valid = false;
   h->il_valid = false;
   h->adj_valid = false;
   return BOGUS_GPU_OK;
@@ -2430,6 +2436,7 @@ int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double*
   h->gs.valid = false;
   h->nproblems = 0;
   h->fp32_valid = false;
+  h->fp32p_valid = false;
   h->il_valid = false;
   h->adj_valid = false;
   return BOGUS_GPU_OK;
@@ -2563,7 +2570,7 @@ int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
   if (int e = check_pg_options(o)) return e;
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
   if (h->nproblems == 0 && h->W.n > 0) return fail(BOGUS_GPU_NO_PROBLEM, "no batch partition set (bogus_gpu_set_batch)");
-  if (o->mixed_precision) return fail(BOGUS_GPU_BAD_INPUT, "batched solves run in FP64 only");
+
   if (int e = set_device(h)) return e;
   const int n = h->W.n;
   BG_CUDA(h->X.ensure(3 * 3 * (size_t)n));
@@ -2580,6 +2587,105 @@ int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
 
 }  // namespace
 
+}  // extern "C"
+
+namespace {
+
+// FP32-refined batched solve: every problem first runs up to max_iters FP32 iterations (one CTA per problem, W,
+// iterates and per-contact law in FP32, reductions and decisions in FP64), then up to refine_max_iters FP64
+// iterations from its FP32 result. Per-problem iteration counts add both parts; residuals are FP64.
+int run_pg_batch_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residuals, unsigned* iters) {
+  const int n = h->W.n;
+  const size_t n3 = 3 * (size_t)n;
+  const int np = h->nproblems;
+  cudaStream_t s = h->stream;
+  BG_CUDA(h->X32.ensure(3 * n3));
+  BG_CUDA(h->MX32.ensure(2 * n3));
+  BG_CUDA(h->Y32.ensure(n3));
+  BG_CUDA(h->S032.ensure(n));
+  BG_CUDA(h->XB32.ensure(n3));
+  BG_CUDA(h->Wv32.ensure(n3));
+  if (!h->fp32p_valid) {
+    BG_CUDA(h->val32p.ensure(9 * (size_t)h->W.nnzb));
+    BG_CUDA(h->b32.ensure(n3));
+    BG_CUDA(h->mu32.ensure(n));
+    BG_CUDA(h->sc32.ensure(n));
+    BG_CUDA(launch_convert(9 * (size_t)h->W.nnzb, h->W.val, h->val32p.p, s));
+    BG_CUDA(launch_convert(n3, h->b.p, h->b32.p, s));
+    BG_CUDA(launch_convert((size_t)n, h->mu.p, h->mu32.p, s));
+    BG_CUDA(launch_convert((size_t)n, h->scaling.p, h->sc32.p, s));
+    h->fp32p_valid = true;
+    h->fp32_valid = false;  // b32 / mu32 / sc32 are shared with the interleaved FP32 copy: rebuild it when needed
+  }
+  PGBatchArgs32 ba{};
+  PGArgs32& a = ba.base;
+  a.rowptr = h->W.rowptr;
+  a.col = h->col_local.p;
+  a.val = h->val32p.p;
+  a.b = h->b32.p;
+  a.mu = h->mu32.p;
+  a.scaling = h->sc32.p;
+  a.X0 = h->X32.p;
+  a.X1 = h->X32.p + n3;
+  a.X2 = h->X32.p + 2 * n3;
+  a.MX0 = h->MX32.p;
+  a.MX1 = h->MX32.p + n3;
+  a.Y = h->Y32.p;
+  a.S0 = h->S032.p;
+  a.XB = h->XB32.p;
+  a.Wv = h->Wv32.p;
+  a.csum = h->csum.p;
+  a.out = h->batch_out.p;
+  a.desaxce = o->static_problem ? 0 : 1;
+  a.variant = o->variant;
+  a.use_inf = o->use_infinity_norm ? 1 : 0;
+  a.tol = o->tol;
+  a.opt = o->ls_optimistic_factor;
+  a.pess = o->ls_pessimistic_factor;
+  a.max_iters = o->max_iters;
+  a.ls_iters = o->ls_iters;
+  ba.nproblems = np;
+  ba.contact_ptr = h->contact_ptr.p;
+  ba.chunk_ptr = h->chunk_ptr.p;
+  ba.queue = h->queue.p;
+  ba.next = h->next.p;
+  ba.r = h->X32.p;
+  int grid = pg_batched_grid(h->device, true);
+  if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "occupancy query failed");
+  if (np < grid) grid = np > 0 ? np : 1;
+  BG_CUDA(launch_convert(n3, h->X.p, h->X32.p, s));
+  BG_CUDA(cudaMemsetAsync(h->next.p, 0, sizeof(int), s));
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  BG_CUDA(launch_pg_batched(ba, grid, s));
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  std::vector<PGOut> out32(np);
+  if (np) BG_CUDA(cudaMemcpyAsync(out32.data(), h->batch_out.p, sizeof(PGOut) * np, cudaMemcpyDeviceToHost, s));
+  BG_CUDA(launch_convert(n3, h->X32.p, h->X.p, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  float ms32 = 0.f;
+  BG_CUDA(cudaEventElapsedTime(&ms32, h->ev0, h->ev1));
+  bogus_gpu_pg_options o64 = *o;
+  o64.max_iters = o->refine_max_iters;
+  o64.mixed_precision = 0;
+  const int st = run_pg_batch(h, &o64, residuals, iters);
+  if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+  unsigned maxit = 0;
+  for (int p = 0; p < np; ++p) {
+    if (iters) iters[p] += out32[p].iters;
+    maxit = std::max(maxit, out32[p].iters);
+  }
+  h->last_stats.refine_iterations = h->last_stats.iterations;
+  h->last_stats.iterations += maxit;
+  h->last_stats.fp32_device_ms = ms32;
+  h->last_ms += ms32;
+  h->last_launches += 1;
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
 int bogus_gpu_solve_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, double* residuals,
                              unsigned* iters) {
   if (int e = batch_checks(h, o)) return e;
@@ -2587,7 +2693,7 @@ int bogus_gpu_solve_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o
   if (n3 == 0) return BOGUS_GPU_OK;
   if (int e = check_finite(r, n3, "r")) return e;
   BG_CUDA(cudaMemcpyAsync(h->X.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, h->stream));
-  const int st = run_pg_batch(h, o, residuals, iters);
+  const int st = o->mixed_precision ? run_pg_batch_mixed(h, o, residuals, iters) : run_pg_batch(h, o, residuals, iters);
   if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
   BG_CUDA(cudaMemcpyAsync(r, h->X.p, sizeof(double) * n3, cudaMemcpyDeviceToHost, h->stream));
   BG_CUDA(cudaStreamSynchronize(h->stream));
@@ -2600,7 +2706,7 @@ int bogus_gpu_solve_pg_batch_device(bogus_gpu_problem* h, const bogus_gpu_pg_opt
   const size_t n3 = 3 * (size_t)h->W.n;
   if (n3 == 0) return BOGUS_GPU_OK;
   BG_CUDA(cudaMemcpyAsync(h->X.p, d_r, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
-  const int st = run_pg_batch(h, o, residuals, iters);
+  const int st = o->mixed_precision ? run_pg_batch_mixed(h, o, residuals, iters) : run_pg_batch(h, o, residuals, iters);
   if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
   BG_CUDA(cudaMemcpyAsync(d_r, h->X.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
   BG_CUDA(cudaStreamSynchronize(h->stream));

@@ -440,6 +440,34 @@ def test_batched_matches_single_problem_solves(bg, oracle, variant):
         assert np.array_equal(r[3 * c0:3 * c1], r_o), p
 
 
+def test_batched_mixed_precision_matches_single_problem_solves(bg):
+    """FP32-refined batch: each problem's residual, iteration count and iterate equal its own FP32-refined
+    single-problem solve (same FP32 order, same FP64 refinement)."""
+    from bogus_gpu import generator
+
+    d, cptr = generator.batch(nproblems=16, nmin=16, nmax=300, seed=9)
+    D = bg.DualFrictionProblem()
+    D.computeFrom(bg.PrimalFrictionProblem.from_generated(d))
+    D.setBatch(cptr)
+    pg = bg.ProjectedGradient()
+    pg.setTol(1e-8)
+    pg.setMaxIters(200)
+    pg.setMixedPrecision(True, 40)
+    r = np.zeros(3 * d.n)
+    res, its = D.solveBatchWith(pg, r, staticProblem=True)
+    rp, cl, vl = D.W_lower()
+    vl = vl.reshape(-1, 9)
+    single = bg.DualFrictionProblem()
+    for p in range(len(cptr) - 1):
+        c0, c1 = cptr[p], cptr[p + 1]
+        single.set(rp[c0:c1 + 1] - rp[c0], cl[rp[c0]:rp[c1]] - c0, vl[rp[c0]:rp[c1]].reshape(-1), d.b[c0:c1],
+                   d.mu[c0:c1])
+        rs = np.zeros(3 * (c1 - c0))
+        res_s = single.solveWith(pg, rs)
+        assert res[p] == res_s and its[p] == single.last_iterations, p
+        assert np.array_equal(r[3 * c0:3 * c1], rs), p
+
+
 def test_batch_rejects_coupled_partition(bg):
     from bogus_gpu import generator
 
