@@ -108,12 +108,26 @@ typedef struct bogus_gpu_admm_options {
   int use_infinity_norm;          /* 0 */
 } bogus_gpu_admm_options;
 
+/* DualAMA setters and defaults (Core/BlockSolvers/ADMM.hpp:170-236). */
+typedef struct bogus_gpu_dual_ama_options {
+  double tol;                     /* 1e-6 */
+  unsigned max_iters;             /* 300 */
+  double fp_step_size;            /* 1e-1 (gamma) */
+  double proj_step_size;          /* 1e-1 (lambda) */
+  unsigned ls_iters;              /* 6 (0: no line search) */
+  double ls_optimistic_factor;    /* 1.25 */
+  double ls_pessimistic_factor;   /* 0.5 */
+  int variant;                    /* bogus_gpu_admm_variant, Accelerated */
+  int use_infinity_norm;          /* 0 */
+} bogus_gpu_dual_ama_options;
+
 typedef struct bogus_gpu_problem bogus_gpu_problem;
 
 /* Option defaults, identical to the reference's constructors. */
 void bogus_gpu_pg_options_default(bogus_gpu_pg_options* opts);
 void bogus_gpu_gs_options_default(bogus_gpu_gs_options* opts);
 void bogus_gpu_admm_options_default(bogus_gpu_admm_options* opts);
+void bogus_gpu_dual_ama_options_default(bogus_gpu_dual_ama_options* opts);
 
 const char* bogus_gpu_status_string(int status);
 /* Last CUDA / validation message recorded on this thread. */
@@ -210,6 +224,13 @@ int bogus_gpu_coloring(bogus_gpu_problem* h, int* perm, int* colors, int* ncolor
 int bogus_gpu_set_primal(bogus_gpu_problem* h, int nbodies, int ndof, const double* minv, int ncontacts,
                          const int* objA, const int* objB, const double* HA, const double* HB);
 
+/* The bodies' own dof counts of a padded primal problem. The reference's H has column blocks of varying
+ * width (PrimalFrictionProblem<3>::HType, Interfaces/FrictionProblem.hpp:65-66); bogus_gpu_set_primal pads every
+ * body to ndof dofs, and body k then uses its first ndof_k <= ndof dofs, the Jacobian columns and M^-1 entries
+ * past them being zero. Only the error-function scalings of ADMM / DualAMA (their square-matrix test,
+ * ConstrainedSolverBase.impl.hpp:84-118) and DualAMA's gap normalisation depend on it. Default: ndof each. */
+int bogus_gpu_set_body_dofs(bogus_gpu_problem* h, const int* ndof_k);
+
 /* DualFrictionProblem::computeFrom (Interfaces/FrictionProblem.cpp:30-40): W = H M^-1 H^T assembled on the
  * device and b = w - H M^-1 f (w in the local basis, E = I; f may be NULL for f = 0); mu copied. The result
  * replaces the handle's dual problem. */
@@ -227,6 +248,19 @@ int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double*
 int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* opts, double lambda,
                          const double* prox, const double* f, const double* w, const double* mu, double* v,
                          double* r, double* residual, unsigned* iters);
+
+/* PrimalFrictionProblem::solveWith(DualAMAType&, v, r, staticProblem) (Interfaces/PrimalFrictionProblem.cpp:
+ * 78-99), DualAMA::solve(law, M, f, w, v, r) (Core/BlockSolvers/ADMM.impl.hpp:128-303): dual accelerated
+ * minimisation on the handle's primal data, law SOCLaw<3, !static_problem> on mu.
+ *  - mass: nbodies x ndof x ndof mass blocks M (row-major; required);
+ *  - f: nbodies x ndof (NULL: 0); w: 3 n (local basis); mu: n;
+ *  - v (nbodies x ndof) and r (3 n) are in/out; on return they hold the iterate of least residual;
+ *  - the error function's scalings are 1 unless H is square at the block level (3 n == the bodies' dofs and
+ *    n == nbodies), as ConstrainedSolverBase::updateScalings sets them;
+ *  - the callback, when set, fires once per iteration. */
+int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_options* opts, const double* mass,
+                             const double* f, const double* w, const double* mu, int static_problem, double* v,
+                             double* r, double* residual, unsigned* iters);
 
 /* ---- Adjoint of the SOC solve (no counterpart in the reference, which has no differentiation) ------------
  * r solves min 1/2 r^T W r + b^T r over r_i in K_mu_i = {|x_T| <= mu x_N} (the SOCLaw<3> problem that
@@ -315,7 +349,7 @@ typedef enum bogus_gpu_meche_algorithm { /* MecheFrictionProblem::Algorithm */
   BOGUS_GPU_MECHE_PROJECTED_GRADIENT = 1,
   BOGUS_GPU_MECHE_MATRIX_FREE_GAUSS_SEIDEL = 2,
   BOGUS_GPU_MECHE_ADMM = 3,
-  BOGUS_GPU_MECHE_DUAL_AMA = 4                  /* not available on the GPU: BAD_INPUT */
+  BOGUS_GPU_MECHE_DUAL_AMA = 4
 } bogus_gpu_meche_algorithm;
 
 /* MecheFrictionProblem::Options (MecheInterface.hpp:44-69) and its defaults (MecheInterface.cpp:51-63). */

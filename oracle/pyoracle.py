@@ -66,12 +66,16 @@ def lib():
     L.oracle_meche_destroy.argtypes = [vp]
     L.oracle_meche_solve.restype = C.c_double
     L.oracle_meche_solve.argtypes = [vp, _dp, vp, C.c_int, C.c_uint, C.c_uint, C.c_double, C.c_int, C.c_int,
-                                     C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double,
-                                     CALLBACK, vp]
+                                     C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                     C.c_double, CALLBACK, vp]
     L.oracle_primal_solve_product_gs.restype = C.c_double
     L.oracle_primal_solve_product_gs.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint,
                                                  C.c_double, C.c_uint, C.c_double, C.c_int, C.c_int, _dp,
                                                  C.POINTER(C.c_uint), CALLBACK, vp]
+    L.oracle_primal_solve_dual_ama.restype = C.c_double
+    L.oracle_primal_solve_dual_ama.argtypes = [vp, _dp, _dp, _dp, _dp, C.c_int, C.c_double, C.c_uint, C.c_double,
+                                               C.c_double, C.c_uint, C.c_double, C.c_double, C.c_int, C.c_int, vp,
+                                               _dp, _dp, C.POINTER(C.c_uint), CALLBACK, vp]
     L.oracle_dual_solve_gs.restype = C.c_double
     L.oracle_dual_solve_gs.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_uint,
                                        C.c_double, C.c_int, C.c_int, C.c_int, _dp, C.POINTER(C.c_uint), CALLBACK,
@@ -96,7 +100,7 @@ def lib():
     L.oracle_primal_rhs.argtypes = [vp, _dp, _dp, _dp]
     L.oracle_primal_solve_admm.restype = C.c_double
     L.oracle_primal_solve_admm.argtypes = [vp, _dp, C.c_double, _dp, _dp, _dp, C.c_double, C.c_uint, C.c_double,
-                                           C.c_int, C.c_int, _dp, _dp, C.POINTER(C.c_uint), CALLBACK, C.c_void_p]
+                                           C.c_int, C.c_int, vp, _dp, _dp, C.POINTER(C.c_uint), CALLBACK, C.c_void_p]
     _lib = L
     return L
 
@@ -294,15 +298,35 @@ class PrimalProblem:
                                                    C.byref(it), cb, None)
         return res, r, it.value
 
-    def solve_admm(self, prox_inv, lam, mu, f, w, v, r, tol=1e-6, max_iters=300, step=1e-2, accelerated=True,
-                   inf_norm=False, trace: Trace | None = None):
+    def solve_dual_ama(self, mass, mu, f, w, v, r, static=False, tol=1e-6, max_iters=300, fp_step=0.1,
+                       proj_step=0.1, ls_iters=6, optimistic=1.25, pessimistic=0.5, accelerated=True, inf_norm=False,
+                       true_dofs=None, trace: Trace | None = None):
+        """PrimalFrictionProblem::solveWith(DualAMAType&, v, r, staticProblem): returns (res, v, r, iterations)."""
         v = _f64(v).copy()
         r = _f64(r).copy()
         it = C.c_uint(0)
         cb = trace._cb if trace else _NO_CB
+        td = None if true_dofs is None else _i32(true_dofs)
+        res = lib().oracle_primal_solve_dual_ama(self.h, _f64(mass).reshape(-1), _f64(mu), _f64(f).reshape(-1),
+                                                 _f64(w).reshape(-1), int(static), tol, max_iters, fp_step, proj_step,
+                                                 ls_iters, optimistic, pessimistic, int(accelerated), int(inf_norm),
+                                                 None if td is None else td.ctypes.data_as(C.c_void_p), v, r,
+                                                 C.byref(it), cb, None)
+        return res, v, r, it.value
+
+    def solve_admm(self, prox_inv, lam, mu, f, w, v, r, tol=1e-6, max_iters=300, step=1e-2, accelerated=True,
+                   inf_norm=False, true_dofs=None, trace: Trace | None = None):
+        """PrimalFrictionProblem::solveWith(ADMM&, lambda, v, r): returns (res, v, r, iterations). true_dofs: the
+        bodies' own dof counts of a padded problem (the error function's scalings), default all ndof."""
+        v = _f64(v).copy()
+        r = _f64(r).copy()
+        it = C.c_uint(0)
+        cb = trace._cb if trace else _NO_CB
+        td = None if true_dofs is None else _i32(true_dofs)
         res = lib().oracle_primal_solve_admm(self.h, _f64(prox_inv).reshape(-1), lam, _f64(mu), _f64(f).reshape(-1),
                                              _f64(w).reshape(-1), tol, max_iters, step, int(accelerated),
-                                             int(inf_norm), v, r, C.byref(it), cb, None)
+                                             int(inf_norm), None if td is None else td.ctypes.data_as(C.c_void_p),
+                                             v, r, C.byref(it), cb, None)
         return res, v, r, it.value
 
 
@@ -337,7 +361,8 @@ class MecheProblem:
 
     def solve(self, r, with_v=True, max_threads=0, max_iters=0, cadoux_iters=0, tolerance=0.0, inf_norm=False,
               algorithm=0, gs_regularization=0.0, gs_coloring=False, gs_skip_iters=-1, try_zero=True, pg_variant=4,
-              admm_step=1.0, static=False, regularization=0.0, v=None, trace: Trace | None = None):
+              admm_step=1.0, admm_fp_step=1e-3, static=False, regularization=0.0, v=None,
+              trace: Trace | None = None):
         r = _f64(r).copy()
         vv = None
         if with_v:
@@ -346,5 +371,5 @@ class MecheProblem:
         res = lib().oracle_meche_solve(self.h, r, None if vv is None else vv.ctypes.data_as(C.c_void_p), max_threads,
                                        max_iters, cadoux_iters, tolerance, int(inf_norm), algorithm, gs_regularization,
                                        int(gs_coloring), gs_skip_iters, int(try_zero), pg_variant, admm_step,
-                                       int(static), regularization, cb, None)
+                                       admm_fp_step, int(static), regularization, cb, None)
         return res, r, vv

@@ -259,11 +259,13 @@ void* oracle_meche_create(int nobj, const unsigned* ndof, const double* mass, co
 void oracle_meche_destroy(void* h) { delete static_cast<Meche*>(h); }
 
 // MecheFrictionProblem::solve(r, v, options, staticProblem, problemRegularization) (:226-367); algorithm 0 GS,
-// 1 PG, 3 ADMM. v: unpadded (sum of ndof), may be null. Returns the solver's residual.
+// 1 PG, 2 matrix-free GS, 3 ADMM, 4 DualAMA. v: unpadded (sum of ndof), may be null. Returns the solver's
+// residual.
 double oracle_meche_solve(void* h, double* r, double* v, int maxThreads, unsigned maxIters, unsigned cadouxIters,
                           double tolerance, int useInfinityNorm, int algorithm, double gsRegularization,
                           int gsColoring, int gsSkipIters, int tryZeroAsWell, int pgVariant, double admmProjStepSize,
-                          int staticProblem, double problemRegularization, oracle_callback cb, void* user) {
+                          double admmFpStepSize, int staticProblem, double problemRegularization, oracle_callback cb,
+                          void* user) {
   auto* m = static_cast<Meche*>(h);
   const Primal& P = m->P;
   const int n = P.ncontacts, d = P.ndof;
@@ -276,7 +278,7 @@ double oracle_meche_solve(void* h, double* r, double* v, int maxThreads, unsigne
   std::vector<double> vp(md, 0.0);
   double res = -1;
   const Callback callback = wrap(cb, user);
-  if (algorithm == 3) {
+  if (algorithm == 3 || algorithm == 4) {
     // v given (unpadded) or M^-1 (H^T r - f)
     if (v) {
       size_t off = 0;
@@ -289,14 +291,32 @@ double oracle_meche_solve(void* h, double* r, double* v, int maxThreads, unsigne
     }
     ADMMSolver s;
     s.P = &P;
-    s.stepSize = admmProjStepSize;
-    if (tolerance != 0.) s.tol = tolerance;
-    if (maxIters != 0) s.maxIters = maxIters;
-    s.useInfinityNorm = useInfinityNorm != 0;
-    s.callback = callback;
-    std::vector<double> invMu(n);
-    for (int i = 0; i < n; ++i) invMu[i] = 1. / m->mu[i];
-    res = s.solve(invMu.data(), P.minv, 0., m->f.data(), wl.data(), vp.data(), rl.data());
+    s.setScalings(m->ndof);
+    if (algorithm == 4) {
+      // MecheInterface.cpp:249-261: DualAMA without line search, the facade's step sizes
+      DualAMASolver dama;
+      dama.P = &P;
+      if (tolerance != 0.) dama.tol = tolerance;
+      if (maxIters != 0) dama.maxIters = maxIters;
+      dama.useInfinityNorm = useInfinityNorm != 0;
+      dama.lsIters = 0;
+      dama.fpStepSize = admmFpStepSize;
+      dama.projStepSize = admmProjStepSize;
+      dama.callback = callback;
+      dama.scalings = s.scalings;
+      dama.mTrue = 0;
+      for (int k : m->ndof) dama.mTrue += k;
+      res = dama.solve(m->mu.data(), staticProblem == 0, m->mass, m->f.data(), wl.data(), vp.data(), rl.data());
+    } else {
+      s.stepSize = admmProjStepSize;
+      if (tolerance != 0.) s.tol = tolerance;
+      if (maxIters != 0) s.maxIters = maxIters;
+      s.useInfinityNorm = useInfinityNorm != 0;
+      s.callback = callback;
+      std::vector<double> invMu(n);
+      for (int i = 0; i < n; ++i) invMu[i] = 1. / m->mu[i];
+      res = s.solve(invMu.data(), P.minv, 0., m->f.data(), wl.data(), vp.data(), rl.data());
+    }
   } else if (algorithm == 2) {
     // PrimalFrictionProblem::solveWith(ProductGaussSeidelType&, r_loc, staticProblem)
     ProductGaussSeidel gs;
@@ -473,11 +493,44 @@ double oracle_primal_solve_product_gs(void* h, const double* f, const double* w,
   return gs.solve(law, b.data(), r, iters);
 }
 
-// PrimalFrictionProblem::solveWith(ADMM&, lambda, v, r): proxInv = (M + lambda I)^-1 blocks
+// PrimalFrictionProblem::solveWith(DualAMAType&, v, r, staticProblem): mass blocks M (nbodies x d x d),
+// trueDofs: the bodies' own dof counts (for the scalings; null: all d).
+double oracle_primal_solve_dual_ama(void* h, const double* mass, const double* mu, const double* f, const double* w,
+                                   int staticProblem, double tol, unsigned maxIters, double fpStep, double projStep,
+                                   unsigned lsIters, double optimistic, double pessimistic, int accelerated,
+                                   int useInfinityNorm, const int* trueDofs, double* v, double* r, unsigned* iters,
+                                   oracle_callback cb, void* user) {
+  auto* P = static_cast<Primal*>(h);
+  DualAMASolver s;
+  s.P = P;
+  s.tol = tol;
+  s.maxIters = maxIters;
+  s.fpStepSize = fpStep;
+  s.projStepSize = projStep;
+  s.lsIters = lsIters;
+  s.lsOptimisticFactor = optimistic;
+  s.lsPessimisticFactor = pessimistic;
+  s.accelerated = accelerated != 0;
+  s.useInfinityNorm = useInfinityNorm != 0;
+  s.callback = wrap(cb, user);
+  ADMMSolver sc;
+  sc.P = P;
+  std::vector<int> td(P->nbodies, P->ndof);
+  if (trueDofs) td.assign(trueDofs, trueDofs + P->nbodies);
+  sc.setScalings(td);
+  s.scalings = sc.scalings;
+  s.mTrue = 0;
+  for (int k : td) s.mTrue += k;
+  std::vector<double> M(mass, mass + (size_t)P->nbodies * P->ndof * P->ndof);
+  return s.solve(mu, staticProblem == 0, M, f, w, v, r, iters);
+}
+
+// PrimalFrictionProblem::solveWith(ADMM&, lambda, v, r): proxInv = (M + lambda I)^-1 blocks; trueDofs: the
+// bodies' own dof counts (for the scalings; null: all d).
 double oracle_primal_solve_admm(void* h, const double* proxInv, double lambda, const double* mu, const double* f,
                                 const double* w, double tol, unsigned maxIters, double stepSize, int accelerated,
-                                int useInfinityNorm, double* v, double* r, unsigned* iters, oracle_callback cb,
-                                void* user) {
+                                int useInfinityNorm, const int* trueDofs, double* v, double* r, unsigned* iters,
+                                oracle_callback cb, void* user) {
   auto* P = static_cast<Primal*>(h);
   ADMMSolver s;
   s.P = P;
@@ -490,6 +543,9 @@ double oracle_primal_solve_admm(void* h, const double* proxInv, double lambda, c
   std::vector<double> invMu(P->ncontacts);
   for (int i = 0; i < P->ncontacts; ++i) invMu[i] = 1. / mu[i];
   std::vector<double> pinv(proxInv, proxInv + (size_t)P->nbodies * P->ndof * P->ndof);
+  std::vector<int> td(P->nbodies, P->ndof);
+  if (trueDofs) td.assign(trueDofs, trueDofs + P->nbodies);
+  s.setScalings(td);
   return s.solve(invMu.data(), pinv, lambda, f, w, v, r, iters);
 }
 

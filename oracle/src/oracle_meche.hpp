@@ -7,8 +7,9 @@
 // mass), which changes nothing in W, b or v.
 // solve (:226-367): r to local coordinates (E^T r), the dual computed once per primal (W + reg I when reg > 0),
 // the solver chosen by the options (Gauss-Seidel with the coloring order when maxThreads != 1 and gsColoring,
-// projected gradient, Cadoux for a non-static problem with cadouxIters > 0, primal ADMM), v = M^-1 (H^T r - f),
-// r back to world coordinates (E r).
+// projected gradient, Cadoux for a non-static problem with cadouxIters > 0, primal ADMM, DualAMA without line
+// search), v = M^-1 (H^T r - f), r back to world coordinates (E r). ADMM and DualAMA scale their error function
+// as ConstrainedSolverBase::updateScalings does for this H (the bodies' own dofs, padding excluded).
 //
 // Evaluation order (shared with the GPU facade): a 3x3 frame block is applied row by row with the dot3 chain,
 // E^T x: y_a = fma(E[2][a], x2, fma(E[1][a], x1, E[0][a] x0)), E x: y_a = fma(E[a][2], x2, fma(E[a][1], x1,
@@ -75,6 +76,7 @@ struct Meche {
   std::vector<int> ndof;     // per body
   std::vector<double> E;     // 9 per contact, row-major E_i[a][b]
   std::vector<double> f;     // nbodies x d (padded)
+  std::vector<double> mass;  // nbodies x d x d mass blocks, row-major, padded with zeros
   std::vector<double> w;     // world, 3 n
   std::vector<double> mu;
   bool hasDual = false;
@@ -95,6 +97,7 @@ inline bool mecheFromPrimal(Meche& m, int nobj, const unsigned* ndof, const doub
   P.ncontacts = n;
   m.ndof.assign(ndof, ndof + nobj);
   P.minv.assign((size_t)nobj * d * d, 0.0);
+  m.mass.assign((size_t)nobj * d * d, 0.0);
   m.f.assign((size_t)nobj * d, 0.0);
   for (int k = 0; k < nobj; ++k) {
     const int dk = (int)ndof[k];
@@ -103,7 +106,10 @@ inline bool mecheFromPrimal(Meche& m, int nobj, const unsigned* ndof, const doub
       for (int c = 0; c < dk; ++c) Mk[(size_t)a * dk + c] = mass[k][(size_t)c * dk + a];
     if (!invertGaussJordan(dk, Mk.data(), inv.data())) return false;
     for (int a = 0; a < dk; ++a)
-      for (int c = 0; c < dk; ++c) P.minv[(size_t)k * d * d + a * d + c] = inv[(size_t)a * dk + c];
+      for (int c = 0; c < dk; ++c) {
+        P.minv[(size_t)k * d * d + a * d + c] = inv[(size_t)a * dk + c];
+        m.mass[(size_t)k * d * d + a * d + c] = Mk[(size_t)a * dk + c];
+      }
   }
   // f is given packed by body (ndof[0] + ndof[1] + ... entries); pad it
   if (f) {

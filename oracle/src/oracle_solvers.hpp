@@ -789,6 +789,29 @@ struct ADMMSolver {
     }
   }
 
+  // Scalings of ConstrainedSolverBase::updateScalings for H (ConstrainedSolverBase.impl.hpp:84-118): 1, unless
+  // H is square at the block level (3 n == total dofs and n == nbodies), where contact i takes
+  // max(1, trace(H_(i, body i)) / 3) when it involves body i. trueDofs: the bodies' own dof counts (unpadded).
+  std::vector<double> scalings;
+  void setScalings(const std::vector<int>& trueDofs) {
+    const int n = P->ncontacts, d = P->ndof;
+    scalings.assign(n, 1.0);
+    long long m = 0;
+    for (int k : trueDofs) m += k;
+    if (!(3LL * n == m && n == P->nbodies)) return;
+    for (int i = 0; i < n; ++i) {
+      int bodies[2]; const double* H[2]; int nb;
+      contactBodies(*P, i, bodies, H, nb);
+      for (int t = 0; t < nb; ++t)
+        if (bodies[t] == i) {
+          const int kk = std::min(3, trueDofs[i]);
+          double tr = 0.0;
+          for (int k = 0; k < kk; ++k) tr = tr + H[t][k * d + k];
+          scalings[i] = dmax(1.0, tr / 3.0);
+        }
+    }
+  }
+
   double solve(const double* invMu, const std::vector<double>& proxInv, double lambda, const double* f,
                const double* w, double* x, double* r, unsigned* itersOut = nullptr) const {
     const int n = P->ncontacts;
@@ -820,7 +843,11 @@ struct ADMMSolver {
       prox(proxInv, prox_arg.data(), f, x);
       Hmul(x, w, ut.data());
       // eval(law, r, ut): per contact FB(1/mu, ut_i (scaling 1), r_i) with SOC law
-      for (int i = 0; i < n; ++i) ev[i] = lawEval(false, invMu[i], &ut[3 * i], &r[3 * i]);
+      for (int i = 0; i < n; ++i) {
+        const double sc = scalings.empty() ? 1.0 : scalings[i];
+        const double lx[3] = {ut[3 * i] * sc, ut[3 * i + 1] * sc, ut[3 * i + 2] * sc};
+        ev[i] = lawEval(false, invMu[i], lx, &r[3 * i]);
+      }
       double e = useInfinityNorm ? maxOf(ev.data(), n) : canonicalSum(ev.data(), n) / (double)(1 + n);
       std::vector<double> gap(n);
       for (int i = 0; i < n; ++i) {
@@ -850,6 +877,151 @@ struct ADMMSolver {
     }
     if (itersOut) *itersOut = it;
     return res;
+  }
+};
+
+// ---------------------------------------------------------------------------------------------
+// DualAMA (Core/BlockSolvers/ADMM.hpp:170-236, ADMM.impl.hpp:128-303) as
+// PrimalFrictionProblem::solveWith(DualAMAType&, v, r, staticProblem) (PrimalFrictionProblem.cpp:78-99) calls
+// it: A = M, B = 0, trivial preconditioner, law SOCLaw<3> on mu (with the De Saxce change of variable unless
+// static). Per iteration: x = f + M v, z = H^T r - x, u = w + H v, res = eval(u, r) + |z|^2 / (1 + m) (max
+// norms with the infinity norm), g = u + COV(u) + gamma H z, then r = P(r - lambda g) with the line search on
+// |H^T r - f - M y|^2 (y = v + gamma z over-relaxed by beta), z = H^T r - x, y = v + gamma z,
+// v = y + beta (y - y_prev). The best (r, v) by residual is returned.
+// Orders: M v and H z as fma chains from 0, then added (x = f + Mv, gap = (H^T r - f) - My, g = fma(gamma, Hz, g));
+// H v and H^T r as the ADMM restatement's products; dof norms |z|^2 and |gap|^2 as each body's dofs summed
+// left to right, then the canonical sum over bodies; over-relaxation y + beta (y - y_prev) unfused.
+// ---------------------------------------------------------------------------------------------
+struct DualAMASolver {
+  const Primal* P = nullptr;
+  double tol = 1e-6;
+  unsigned maxIters = 300;
+  double fpStepSize = 1.e-1;    // gamma
+  double projStepSize = 1.e-1;  // lambda
+  unsigned lsIters = 6;
+  double lsOptimisticFactor = 1.25;
+  double lsPessimisticFactor = .5;
+  bool accelerated = true;
+  bool useInfinityNorm = false;
+  Callback callback;
+  std::vector<double> scalings;  // as ADMMSolver::setScalings
+  long long mTrue = -1;          // the bodies' own dof count (the gap term's 1 + m); -1: nbodies x ndof
+
+  void Mmul(const std::vector<double>& M, const double* v, double* out) const {
+    const int d = P->ndof;
+    for (int k = 0; k < P->nbodies; ++k)
+      for (int a = 0; a < d; ++a) {
+        double acc = 0.0;
+        for (int q = 0; q < d; ++q) acc = std::fma(M[(size_t)k * d * d + a * d + q], v[(size_t)k * d + q], acc);
+        out[(size_t)k * d + a] = acc;
+      }
+  }
+
+  double solve(const double* mu, bool desaxce, const std::vector<double>& M, const double* f, const double* w,
+               double* v, double* r, unsigned* itersOut = nullptr) const {
+    ADMMSolver h;
+    h.P = P;
+    const int n = P->ncontacts;
+    const size_t n3 = 3 * (size_t)n, m = (size_t)P->nbodies * P->ndof;
+    double lambda = projStepSize;
+    const double gamma = fpStepSize;
+    double res = -1, min_res = -1;
+    std::vector<double> r_best(r, r + n3), v_best(v, v + m);
+    std::vector<double> z(m), x(m), ut(n3), gap(m), HrBp(m), g(n3), Mv(m), y(m), y_prev(v, v + m), rs(n3);
+    const int nb = P->nbodies, d = P->ndof;
+    std::vector<double> tmp(m), zz(nb), ev(n), Hz(n3);
+    double theta_prev = 1., res_prev = -1;
+    // dof norms: each body's dofs left to right, then the canonical sum over bodies (or the maximum)
+    auto dofnorm = [&](const std::vector<double>& a) {
+      for (int b = 0; b < nb; ++b) {
+        double p = 0.0;
+        for (int k = 0; k < d; ++k) {
+          const double e = a[(size_t)b * d + k];
+          p = useInfinityNorm ? dmax(std::fabs(e), p) : p + e * e;
+        }
+        zz[b] = p;
+      }
+      return useInfinityNorm ? maxOf(zz.data(), nb) : canonicalSum(zz.data(), nb);
+    };
+    auto sqnorm = [&](const std::vector<double>& a) {
+      for (int b = 0; b < nb; ++b) {
+        double p = 0.0;
+        for (int k = 0; k < d; ++k) p = p + a[(size_t)b * d + k] * a[(size_t)b * d + k];
+        zz[b] = p;
+      }
+      return canonicalSum(zz.data(), nb);
+    };
+    h.HTmul(r, nullptr, HrBp.data());
+    unsigned it;
+    for (it = 0; it < maxIters; ++it) {
+      Mmul(M, v, Mv.data());
+      for (size_t k = 0; k < m; ++k) x[k] = f[k] + Mv[k];
+      for (size_t k = 0; k < m; ++k) z[k] = HrBp[k] - x[k];
+      h.Hmul(v, w, ut.data());
+      for (int i = 0; i < n; ++i) {
+        const double sc = scalings.empty() ? 1.0 : scalings[i];
+        const double lx[3] = {r[3 * i] * sc, r[3 * i + 1] * sc, r[3 * i + 2] * sc};
+        ev[i] = lawEval(desaxce, mu[i], lx, &ut[3 * i]);
+      }
+      res = useInfinityNorm ? maxOf(ev.data(), n) : canonicalSum(ev.data(), n) / (double)(1 + n);
+      const double zn = dofnorm(z);
+      res += useInfinityNorm ? zn : zn / (double)(1 + (mTrue >= 0 ? (size_t)mTrue : m));
+      if (callback) callback(it, res);
+      if (res < min_res || it == 0) {
+        std::copy(r, r + n3, r_best.begin());
+        std::copy(v, v + m, v_best.begin());
+        min_res = res;
+        if (res < tol) break;
+      } else if (res > 1.e50) {
+        break;
+      }
+      double beta = 0;
+      if (accelerated && res < res_prev) beta = nesterovInertia(theta_prev, 0.);
+      else theta_prev = 1;
+      // g = ut + COV(ut) + gamma H z
+      h.Hmul(z.data(), nullptr, Hz.data());
+      for (int i = 0; i < n; ++i) {
+        double s[3];
+        dualityCOV(desaxce, mu[i], &ut[3 * i], s);
+        for (int k = 0; k < 3; ++k) g[3 * i + k] = std::fma(gamma, Hz[3 * i + k], ut[3 * i + k] + s[k]);
+      }
+      if (lsIters == 0) {
+        for (size_t k = 0; k < n3; ++k) r[k] = r[k] - lambda * g[k];
+        for (int i = 0; i < n; ++i) projectCone(mu[i], &r[3 * i]);
+        h.HTmul(r, nullptr, HrBp.data());
+      } else {
+        for (size_t k = 0; k < m; ++k) gap[k] = HrBp[k] - x[k];
+        const double h0 = sqnorm(gap);  // the squared norm, whatever the residual's norm
+        lambda *= lsOptimisticFactor;
+        for (unsigned ls = 0; ls < lsIters; ++ls) {
+          for (size_t k = 0; k < n3; ++k) rs[k] = r[k] - lambda * g[k];
+          for (int i = 0; i < n; ++i) projectCone(mu[i], &rs[3 * i]);
+          h.HTmul(rs.data(), nullptr, HrBp.data());
+          for (size_t k = 0; k < m; ++k) {
+            const double zk = HrBp[k] - x[k];
+            const double yk = v[k] + gamma * zk;
+            y[k] = yk + beta * (yk - y_prev[k]);
+          }
+          Mmul(M, y.data(), tmp.data());
+          for (size_t k = 0; k < m; ++k) gap[k] = (HrBp[k] - f[k]) - tmp[k];
+          const double hh = sqnorm(gap);
+          if (hh < h0) break;
+          lambda *= lsPessimisticFactor;
+        }
+        std::copy(rs.begin(), rs.end(), r);
+      }
+      for (size_t k = 0; k < m; ++k) {
+        z[k] = HrBp[k] - x[k];
+        const double yk = v[k] + gamma * z[k];
+        v[k] = yk + beta * (yk - y_prev[k]);
+        y_prev[k] = yk;
+      }
+      res_prev = res;
+    }
+    std::copy(r_best.begin(), r_best.end(), r);
+    std::copy(v_best.begin(), v_best.end(), v);
+    if (itersOut) *itersOut = it;
+    return min_res;
   }
 };
 

@@ -56,6 +56,12 @@ class AdmmOptions(C.Structure):
                 ("use_infinity_norm", C.c_int)]
 
 
+class DualAmaOptions(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint), ("fp_step_size", C.c_double),
+                ("proj_step_size", C.c_double), ("ls_iters", C.c_uint), ("ls_optimistic_factor", C.c_double),
+                ("ls_pessimistic_factor", C.c_double), ("variant", C.c_int), ("use_infinity_norm", C.c_int)]
+
+
 class AdjointOptions(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint)]
 
@@ -96,7 +102,8 @@ EXPORTED = [
     "bogus_gpu_adjoint", "bogus_gpu_adjoint_device", "bogus_gpu_adjoint_dual_lower", "bogus_gpu_adjoint_primal",
     "bogus_gpu_add_compliance", "bogus_gpu_solve_cadoux_gs", "bogus_gpu_solve_cadoux_pg",
     "bogus_gpu_meche_options_default", "bogus_gpu_meche_from_primal", "bogus_gpu_meche_solve",
-    "bogus_gpu_solve_product_gs",
+    "bogus_gpu_solve_product_gs", "bogus_gpu_dual_ama_options_default", "bogus_gpu_solve_dual_ama",
+    "bogus_gpu_set_body_dofs",
 ]
 
 
@@ -159,6 +166,11 @@ def lib():
     L.bogus_gpu_admm_options_default.restype = None
     L.bogus_gpu_solve_admm.argtypes = [vp, C.POINTER(AdmmOptions), C.c_double, vp, vp, _dp, _dp, _dp, _dp,
                                        C.POINTER(C.c_double), C.POINTER(C.c_uint)]
+    L.bogus_gpu_dual_ama_options_default.argtypes = [C.POINTER(DualAmaOptions)]
+    L.bogus_gpu_dual_ama_options_default.restype = None
+    L.bogus_gpu_solve_dual_ama.argtypes = [vp, C.POINTER(DualAmaOptions), _dp, vp, _dp, _dp, C.c_int, _dp, _dp,
+                                           C.POINTER(C.c_double), C.POINTER(C.c_uint)]
+    L.bogus_gpu_set_body_dofs.argtypes = [vp, _ip]
     L.bogus_gpu_solve_pg_batch.argtypes = [vp, C.POINTER(PgOptions), _dp, _dp, np.ctypeslib.ndpointer(dtype=np.uint32)]
     L.bogus_gpu_solve_pg_batch_device.argtypes = [vp, C.POINTER(PgOptions), vp, _dp,
                                                   np.ctypeslib.ndpointer(dtype=np.uint32)]
@@ -323,13 +335,45 @@ class ADMM(_SolverBase):
         return o
 
 
+class DualAMA(_SolverBase):
+    """DualAMA<HType> (Core/BlockSolvers/ADMM.hpp:170-236): tol 1e-6, 300 iterations, fp step size 1e-1,
+    projection step size 1e-1, 6 line-search iterations (factors 1.25 / 0.5), Accelerated variant."""
+
+    def __init__(self):
+        super().__init__(1e-6, 300)
+        self._fp, self._proj = 1e-1, 1e-1
+        self._ls, self._opt, self._pess = 6, 1.25, .5
+        self._variant = ADMM_ACCELERATED
+
+    def setFpStepSize(self, s: float) -> None: self._fp = float(s)
+    def setProjStepSize(self, s: float) -> None: self._proj = float(s)
+    def setLineSearchIterations(self, n: int) -> None: self._ls = int(n)
+    def setLineSearchOptimisticFactor(self, f: float) -> None: self._opt = float(f)
+    def setLineSearchPessimisticFactor(self, f: float) -> None: self._pess = float(f)
+    def setDefaultVariant(self, v: int) -> None: self._variant = int(v)
+    def fpStepSize(self) -> float: return self._fp
+    def projStepSize(self) -> float: return self._proj
+
+    def options(self) -> "DualAmaOptions":
+        o = DualAmaOptions()
+        lib().bogus_gpu_dual_ama_options_default(C.byref(o))
+        o.tol, o.max_iters, o.fp_step_size, o.proj_step_size = self._tol, self._max_iters, self._fp, self._proj
+        o.ls_iters, o.ls_optimistic_factor, o.ls_pessimistic_factor = self._ls, self._opt, self._pess
+        o.variant, o.use_infinity_norm = self._variant, int(self._inf)
+        return o
+
+
 class PrimalFrictionProblem:
     """PrimalFrictionProblem<3> for rigid bodies (Interfaces/FrictionProblem.hpp:55-116): M^-1 blocks,
     per-contact Jacobian blocks for one or two bodies, f, w (local contact basis), mu. The arrays are uploaded
-    to the GPU on the first solveWith; call invalidate() after changing them."""
+    to the GPU on the first solveWith; call invalidate() after changing them. M: the mass blocks (DualAMA needs
+    them; computeMInv(M) sets both). body_dofs: the bodies' own dof counts when they are padded to ndof (the
+    reference's H has column blocks of varying width); default ndof each."""
 
-    def __init__(self, minv, objA, objB, HA, HB, w, mu, f=None, device: int = 0):
+    def __init__(self, minv, objA, objB, HA, HB, w, mu, f=None, device: int = 0, M=None, body_dofs=None):
         self.minv = _f64(minv)
+        self.M = None if M is None else _f64(M)
+        self.body_dofs = None if body_dofs is None else _i32(body_dofs)
         self.objA, self.objB = _i32(objA), _i32(objB)
         self.HA, self.HB = _f64(HA), _f64(HB)
         self.w, self.mu = _f64(w).reshape(-1), _f64(mu).reshape(-1)
@@ -347,16 +391,44 @@ class PrimalFrictionProblem:
             nb, ndof = self.minv.shape[0], self.minv.shape[1]
             _check(lib().bogus_gpu_set_primal(g.handle, nb, ndof, self.minv.reshape(-1), self.objA.size, self.objA,
                                               self.objB, self.HA.reshape(-1), self.HB.reshape(-1)), False)
+            if self.body_dofs is not None:
+                _check(lib().bogus_gpu_set_body_dofs(g.handle, self.body_dofs), False)
             self._gpu = g
         return self._gpu
 
     def solveWith(self, solver, *args, **kwargs) -> float:
         """PrimalFrictionProblem::solveWith:
         - solveWith(ADMM, lambda_, v, r, prox=None): primal ADMM (see _solve_admm);
-        - solveWith(ProductGaussSeidel, r, staticProblem=False): the matrix-free Gauss-Seidel."""
+        - solveWith(ProductGaussSeidel, r, staticProblem=False): the matrix-free Gauss-Seidel;
+        - solveWith(DualAMA, v, r, staticProblem=False): the dual AMA solver (see _solve_dual_ama)."""
         if isinstance(solver, ProductGaussSeidel):
             return self._solve_product_gs(solver, *args, **kwargs)
+        if isinstance(solver, DualAMA):
+            return self._solve_dual_ama(solver, *args, **kwargs)
         return self._solve_admm(solver, *args, **kwargs)
+
+    def _solve_dual_ama(self, dama: "DualAMA", v, r, staticProblem: bool = False) -> float:
+        """PrimalFrictionProblem::solveWith(DualAMAType&, v, r, staticProblem): v (nbodies * ndof) and r (3n) are
+        solved in place (float64, C-contiguous; the iterate of least residual); returns the residual."""
+        for a, name in ((v, "v"), (r, "r")):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+                raise TypeError(f"{name} must be a C-contiguous float64 numpy array (solved in place)")
+        if v.size != self.minv.shape[0] * self.minv.shape[1] or r.size != 3 * self.objA.size:
+            raise ValueError("inconsistent v / r sizes")
+        if self.M is None:
+            raise ValueError("DualAMA needs the mass blocks M (constructor argument or computeMInv(M))")
+        g = self._uploaded()
+        g._bind(dama)
+        o = dama.options()
+        res = C.c_double()
+        it = C.c_uint()
+        fptr = None if self.f is None else self.f.ctypes.data_as(C.c_void_p)
+        st = lib().bogus_gpu_solve_dual_ama(g.handle, C.byref(o), self.M.reshape(-1), fptr, self.w, self.mu,
+                                            int(bool(staticProblem)), v.reshape(-1), r.reshape(-1), C.byref(res),
+                                            C.byref(it))
+        _check(st)
+        self.last_status, self.last_iterations = st, it.value
+        return res.value
 
     def _solve_product_gs(self, gs: "ProductGaussSeidel", r, staticProblem: bool = False) -> float:
         if not (isinstance(r, np.ndarray) and r.dtype == np.float64 and r.flags.c_contiguous):
@@ -410,8 +482,9 @@ class PrimalFrictionProblem:
         return cls(data.minv, data.objA, data.objB, data.HA, data.HB, data.b, data.mu)
 
     def computeMInv(self, M) -> None:
-        """Sets the inverse mass blocks from mass blocks M[nbodies, ndof, ndof] (PrimalFrictionProblem::computeMInv)."""
-        self.minv = _f64(np.linalg.inv(_f64(M)))
+        """Sets the mass blocks M[nbodies, ndof, ndof] and their inverses (PrimalFrictionProblem::computeMInv)."""
+        self.M = _f64(M).copy()
+        self.minv = _f64(np.linalg.inv(self.M))
 
 
 class DualFrictionProblem:

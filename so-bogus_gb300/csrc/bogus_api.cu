@@ -154,12 +154,21 @@ struct bogus_gpu_problem {
   DevBuf<int> bptr, bent;
   DevBuf<double> a_prox, a_f, a_w, a_mu, a_invmu, a_x, a_r, a_ut, a_z, a_zacc, a_zprev, a_yprev;
   DevBuf<ADMMOut> admm_out;
+  // error-function scalings of ADMM / DualAMA (ConstrainedSolverBase::updateScalings), per contact, and the
+  // bodies' own dof count (padding excluded), both set with the incidences
+  DevBuf<double> a_sc;
+  long long true_dofs = 0;
+  std::vector<int> body_dofs;  // the bodies' own dof counts (d each unless set otherwise)
+  // DualAMA: mass blocks, affine part and work
+  DevBuf<double> dm_M, dm_f, dm_v, dm_rs, dm_x, dm_hr, dm_g, dm_yp, dm_rb, dm_vb;
+  DevBuf<DamaOut> dama_out;
   // Cadoux fixed point: the original right-hand side while the inner solves use COV(u) + b
   DevBuf<double> cad_b;
   // MecheFrictionProblem facade: frames, world w (then local), padded f, per-body dofs; dual built at first use
   bool meche_valid = false, meche_dual = false;
   DevBuf<double> meche_E, meche_w, meche_r, meche_v, meche_fd;
   std::vector<double> meche_wloc, meche_f, meche_mu;
+  std::vector<double> meche_mass;  // mass blocks, row-major, padded to d dofs with zeros
   std::vector<unsigned> meche_ndof;
   // adjoint: per-contact basis, CG vectors, the last solution r and s = dL/db (device and host copies)
   DevBuf<double> adj_V, adj_Pc, adj_D, adj_K, adj_P, adj_R, adj_Z, adj_Dir, adj_Y, adj_Q, adj_S, adj_dmu, adj_r, adj_g;
@@ -1586,7 +1595,7 @@ int bogus_gpu_meche_from_primal(bogus_gpu_problem* h, unsigned nobj, const unsig
   if (f)
     if (int e = check_finite(f, m, "f")) return e;
   // inverse mass blocks (PrimalFrictionProblem::computeMInv), padded to d dofs with inert (zero) entries
-  std::vector<double> minv((size_t)nobj * d * d, 0.0), fpad((size_t)nobj * d, 0.0);
+  std::vector<double> minv((size_t)nobj * d * d, 0.0), mpad((size_t)nobj * d * d, 0.0), fpad((size_t)nobj * d, 0.0);
   {
     size_t off = 0;
     for (unsigned k = 0; k < nobj; ++k) {
@@ -1597,7 +1606,10 @@ int bogus_gpu_meche_from_primal(bogus_gpu_problem* h, unsigned nobj, const unsig
         for (int c = 0; c < dk; ++c) Mk[(size_t)a * dk + c] = mass[k][(size_t)c * dk + a];
       if (!invert_gauss_jordan(dk, Mk.data(), inv.data())) return fail(BOGUS_GPU_BAD_INPUT, "singular mass block");
       for (int a = 0; a < dk; ++a) {
-        for (int c = 0; c < dk; ++c) minv[(size_t)k * d * d + a * d + c] = inv[(size_t)a * dk + c];
+        for (int c = 0; c < dk; ++c) {
+          minv[(size_t)k * d * d + a * d + c] = inv[(size_t)a * dk + c];
+          mpad[(size_t)k * d * d + a * d + c] = Mk[(size_t)a * dk + c];
+        }
         if (f) fpad[(size_t)k * d + a] = f[off + a];
       }
       off += ndof[k];
@@ -1663,7 +1675,9 @@ int bogus_gpu_meche_from_primal(bogus_gpu_problem* h, unsigned nobj, const unsig
   h->h_objA = std::move(oA);
   h->admm_incidence_valid = false;
   h->meche_ndof.assign(ndof, ndof + nobj);
+  h->body_dofs.assign(ndof, ndof + nobj);
   h->meche_f = std::move(fpad);
+  h->meche_mass = std::move(mpad);
   h->meche_mu.assign(mu, mu + n);
   h->meche_valid = true;
   h->meche_dual = false;
@@ -1675,10 +1689,9 @@ int bogus_gpu_meche_solve(bogus_gpu_problem* h, double* r, double* v, const bogu
   if (int e = check_handle(h)) return e;
   if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
   if (!h->meche_valid) return fail(BOGUS_GPU_NO_PROBLEM, "no problem set (bogus_gpu_meche_from_primal)");
-  if (o->algorithm == BOGUS_GPU_MECHE_DUAL_AMA)
-    return fail(BOGUS_GPU_BAD_INPUT, "DualAMA is not available on the GPU");
   if (o->algorithm != BOGUS_GPU_MECHE_GAUSS_SEIDEL && o->algorithm != BOGUS_GPU_MECHE_PROJECTED_GRADIENT &&
-      o->algorithm != BOGUS_GPU_MECHE_ADMM && o->algorithm != BOGUS_GPU_MECHE_MATRIX_FREE_GAUSS_SEIDEL)
+      o->algorithm != BOGUS_GPU_MECHE_ADMM && o->algorithm != BOGUS_GPU_MECHE_MATRIX_FREE_GAUSS_SEIDEL &&
+      o->algorithm != BOGUS_GPU_MECHE_DUAL_AMA)
     return fail(BOGUS_GPU_BAD_INPUT, "unknown algorithm");
   const int n = h->ncontacts, nb = h->nbodies, d = h->ndof;
   const size_t n3 = 3 * (size_t)n, md = (size_t)nb * d;
@@ -1715,7 +1728,23 @@ int bogus_gpu_meche_solve(bogus_gpu_problem* h, double* r, double* v, const bogu
   };
   int st = BOGUS_GPU_OK;
   double res = -1.0;
-  if (o->algorithm == BOGUS_GPU_MECHE_ADMM) {
+  if (o->algorithm == BOGUS_GPU_MECHE_DUAL_AMA) {
+    // MecheInterface.cpp:237-261: v given or M^-1 (H^T r - f); no line search, the facade's step sizes
+    if (v) pad_v();
+    else if (int e = velocity()) return e;
+    bogus_gpu_dual_ama_options da;
+    bogus_gpu_dual_ama_options_default(&da);
+    if (o->tolerance != 0.) da.tol = o->tolerance;
+    if (o->max_iters != 0) da.max_iters = o->max_iters;
+    da.use_infinity_norm = o->use_infinity_norm;
+    da.ls_iters = 0;
+    da.fp_step_size = o->admm_fp_step_size;
+    da.proj_step_size = o->admm_proj_step_size;
+    st = bogus_gpu_solve_dual_ama(h, &da, h->meche_mass.data(), h->meche_f.data(), h->meche_wloc.data(),
+                                  h->meche_mu.data(), static_problem, vp.data(), rl.data(), &res, nullptr);
+    if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
+    if (n > 0) BG_CUDA(cudaMemcpyAsync(h->meche_r.p, rl.data(), sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  } else if (o->algorithm == BOGUS_GPU_MECHE_ADMM) {
     if (v) pad_v();
     else if (int e = velocity()) return e;
     bogus_gpu_admm_options ao;
@@ -1855,6 +1884,20 @@ int bogus_gpu_set_primal(bogus_gpu_problem* h, int nbodies, int ndof, const doub
   h->pgs.valid = false;
   h->h_objA.assign(objA, objA + ncontacts);
   h->admm_incidence_valid = false;
+  h->body_dofs.assign(nbodies, ndof);
+  h->meche_valid = false;
+  h->meche_dual = false;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_set_body_dofs(bogus_gpu_problem* h, const int* ndof) {
+  if (int e = check_handle(h)) return e;
+  if (h->nbodies == 0) return fail(BOGUS_GPU_NO_PROBLEM, "no primal problem set (bogus_gpu_set_primal)");
+  if (!ndof) return fail(BOGUS_GPU_BAD_INPUT, "null ndof");
+  for (int k = 0; k < h->nbodies; ++k)
+    if (ndof[k] < 1 || ndof[k] > h->ndof) return fail(BOGUS_GPU_BAD_INPUT, "body dof count out of range");
+  h->body_dofs.assign(ndof, ndof + h->nbodies);
+  h->admm_incidence_valid = false;
   return BOGUS_GPU_OK;
 }
 
@@ -1884,7 +1927,32 @@ int ensure_incidence(bogus_gpu_problem* h) {
   BG_CUDA(h->bent.ensure(be.size()));
   BG_CUDA(cudaMemcpyAsync(h->bptr.p, bp.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, s));
   BG_CUDA(cudaMemcpyAsync(h->bent.p, be.data(), sizeof(int) * be.size(), cudaMemcpyHostToDevice, s));
+  // scalings (ConstrainedSolverBase.impl.hpp:84-118): 1, unless H is square at the block level (3 n rows ==
+  // the bodies' dofs, n == nbodies), where contact i with a block on body i takes max(1, trace / 3) of it
+  const int d = h->ndof;
+  const bool own = h->body_dofs.size() == (size_t)nb;
+  long long m = 0;
+  for (int k = 0; k < nb; ++k) m += own ? h->body_dofs[k] : d;
+  std::vector<double> sc(n > 0 ? n : 1, 1.0);
+  if (n > 0 && 3LL * n == m && n == nb) {
+    std::vector<double> Hh(2 * (size_t)n * 3 * d);
+    BG_CUDA(cudaMemcpyAsync(Hh.data(), h->H.p, sizeof(double) * Hh.size(), cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; ++i)
+      for (int t = 0; t < 2; ++t)
+        if (h->h_cb[2 * (size_t)i + t] == i) {
+          const int dk = own ? h->body_dofs[i] : d;
+          const int kk = dk < 3 ? dk : 3;
+          const double* Hb = &Hh[(2 * (size_t)i + t) * 3 * d];
+          double tr = 0.0;
+          for (int k = 0; k < kk; ++k) tr = tr + Hb[k * d + k];
+          sc[i] = std::max(1.0, tr / 3.0);
+        }
+  }
+  BG_CUDA(h->a_sc.ensure(sc.size()));
+  BG_CUDA(cudaMemcpyAsync(h->a_sc.p, sc.data(), sizeof(double) * sc.size(), cudaMemcpyHostToDevice, s));
   BG_CUDA(cudaStreamSynchronize(s));
+  h->true_dofs = m;
   h->admm_ninc = (size_t)bp[nb];
   h->admm_incidence_valid = true;
   return BOGUS_GPU_OK;
@@ -2196,8 +2264,6 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   if (int e = set_device(h)) return e;
   cudaStream_t s = h->stream;
   if (int e = ensure_incidence(h)) return e;
-  {
-  }
   const size_t nv = n3 > 0 ? n3 : 1;
   for (auto* b : {&h->a_w, &h->a_r, &h->a_ut, &h->a_z, &h->a_zacc, &h->a_zprev, &h->a_yprev}) BG_CUDA(b->ensure(nv));
   BG_CUDA(h->a_mu.ensure(n > 0 ? n : 1));
@@ -2251,6 +2317,7 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   a.max_iters = o->max_iters;
   a.accelerated = o->variant == BOGUS_GPU_ADMM_ACCELERATED;
   a.use_inf = o->use_infinity_norm ? 1 : 0;
+  a.scaling = h->a_sc.p;
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   int grid = admm_max_grid(h->device, d);
@@ -2296,6 +2363,155 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
     for (unsigned k = 0; k < count; ++k) h->callback(k, tr[k], h->callback_user);
   }
   return out.converged ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
+}
+
+void bogus_gpu_dual_ama_options_default(bogus_gpu_dual_ama_options* o) {
+  if (!o) return;
+  o->tol = 1e-6;
+  o->max_iters = 300;
+  o->fp_step_size = 1.e-1;
+  o->proj_step_size = 1.e-1;
+  o->ls_iters = 6;
+  o->ls_optimistic_factor = 1.25;
+  o->ls_pessimistic_factor = .5;
+  o->variant = BOGUS_GPU_ADMM_ACCELERATED;
+  o->use_infinity_norm = 0;
+}
+
+int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_options* o, const double* mass,
+                             const double* f, const double* w, const double* mu, int static_problem, double* v,
+                             double* r, double* residual, unsigned* iters) {
+  if (int e = check_handle(h)) return e;
+  if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
+  if (h->nbodies == 0) return fail(BOGUS_GPU_NO_PROBLEM, "no primal problem set (bogus_gpu_set_primal)");
+  if (o->variant != BOGUS_GPU_ADMM_STANDARD && o->variant != BOGUS_GPU_ADMM_ACCELERATED)
+    return fail(BOGUS_GPU_BAD_INPUT, "unknown DualAMA variant");
+  if (!(o->fp_step_size > 0) || !(o->proj_step_size > 0) || !(o->tol >= 0) || !(o->ls_optimistic_factor > 0) ||
+      !(o->ls_pessimistic_factor > 0) || !std::isfinite(o->fp_step_size) || !std::isfinite(o->proj_step_size))
+    return fail(BOGUS_GPU_BAD_INPUT, "invalid DualAMA step sizes, factors or tolerance");
+  const int n = h->ncontacts, nb = h->nbodies, d = h->ndof;
+  const size_t n3 = 3 * (size_t)n, m = (size_t)nb * d;
+  if ((n > 0 && (!w || !mu || !r)) || !v || !mass) return fail(BOGUS_GPU_BAD_INPUT, "null mass, w, mu, v or r");
+  if (int e = check_finite(mass, m * d, "mass")) return e;
+  if (int e = check_finite(w, n3, "w")) return e;
+  if (int e = check_finite(mu, n, "mu")) return e;
+  if (int e = check_finite(v, m, "v")) return e;
+  if (int e = check_finite(r, n3, "r")) return e;
+  if (f)
+    if (int e = check_finite(f, m, "f")) return e;
+  if (int e = set_device(h)) return e;
+  cudaStream_t s = h->stream;
+  if (int e = ensure_incidence(h)) return e;
+  const size_t nv = n3 > 0 ? n3 : 1;
+  for (auto* b : {&h->a_w, &h->a_r, &h->a_ut, &h->dm_rs, &h->dm_g, &h->dm_rb}) BG_CUDA(b->ensure(nv));
+  for (auto* b : {&h->dm_f, &h->dm_v, &h->dm_x, &h->dm_hr, &h->dm_yp, &h->dm_vb}) BG_CUDA(b->ensure(m));
+  BG_CUDA(h->dm_M.ensure(m * d));
+  BG_CUDA(h->a_mu.ensure(n > 0 ? n : 1));
+  const int C = (n + 31) / 32, CB = (nb + 31) / 32;
+  const int CC = C > CB ? C : CB;
+  BG_CUDA(h->csum.ensure(3 * (size_t)(CC > 0 ? CC : 1)));
+  BG_CUDA(h->scal.ensure(8));
+  BG_CUDA(h->trace.ensure((size_t)o->max_iters + 1));
+  BG_CUDA(h->dama_out.ensure(1));
+  BG_CUDA(h->barrier.ensure(4));
+  BG_CUDA(h->status.ensure(1));
+  if (n > 0) {
+    BG_CUDA(cudaMemcpyAsync(h->a_w.p, w, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->a_mu.p, mu, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->a_r.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->dm_rb.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  }
+  BG_CUDA(cudaMemcpyAsync(h->dm_v.p, v, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(h->dm_vb.p, v, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(h->dm_yp.p, v, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(h->dm_M.p, mass, sizeof(double) * m * d, cudaMemcpyHostToDevice, s));
+  if (f) BG_CUDA(cudaMemcpyAsync(h->dm_f.p, f, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+  else BG_CUDA(cudaMemsetAsync(h->dm_f.p, 0, sizeof(double) * m, s));
+  DamaArgs a{};
+  a.n = n;
+  a.nbodies = nb;
+  a.d = d;
+  a.cb = h->cb.p;
+  a.H = h->H.p;
+  a.bptr = h->bptr.p;
+  a.bent = h->bent.p;
+  a.M = h->dm_M.p;
+  a.f = h->dm_f.p;
+  a.w = h->a_w.p;
+  a.mu = h->a_mu.p;
+  a.scaling = h->a_sc.p;
+  a.v = h->dm_v.p;
+  a.r = h->a_r.p;
+  a.rs = h->dm_rs.p;
+  a.x = h->dm_x.p;
+  a.HrBp = h->dm_hr.p;
+  a.ut = h->a_ut.p;
+  a.g = h->dm_g.p;
+  a.y_prev = h->dm_yp.p;
+  a.r_best = h->dm_rb.p;
+  a.v_best = h->dm_vb.p;
+  a.csum = h->csum.p;
+  a.scal = h->scal.p;
+  a.trace = h->trace.p;
+  a.out = h->dama_out.p;
+  a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.tol = o->tol;
+  a.gamma = o->fp_step_size;
+  a.lambda0 = o->proj_step_size;
+  a.opt = o->ls_optimistic_factor;
+  a.pess = o->ls_pessimistic_factor;
+  a.m_true = (double)h->true_dofs;
+  a.max_iters = o->max_iters;
+  a.ls_iters = o->ls_iters;
+  a.accelerated = o->variant == BOGUS_GPU_ADMM_ACCELERATED;
+  a.use_inf = o->use_infinity_norm ? 1 : 0;
+  a.desaxce = static_problem ? 0 : 1;
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), s));
+  BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
+  int grid = dama_max_grid(h->device, d);
+  if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
+  const int want = (CC + 7) / 8;
+  if (want < grid) grid = want < 1 ? 1 : want;
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  BG_CUDA(launch_dama(a, grid, s));
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  DamaOut out{};
+  int st = 0;
+  BG_CUDA(cudaMemcpyAsync(&out, h->dama_out.p, sizeof(DamaOut), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaMemcpyAsync(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  h->last_launches = 1;
+  if (st != 0) return fail(st, "device-side wait timed out in the DualAMA kernel");
+  BG_CUDA(cudaMemcpy(v, h->dm_vb.p, sizeof(double) * m, cudaMemcpyDeviceToHost));
+  if (n > 0) BG_CUDA(cudaMemcpy(r, h->dm_rb.p, sizeof(double) * n3, cudaMemcpyDeviceToHost));
+  {
+    // per iteration: Q1 reads M, f, v, H^T r per body and writes x; reads w, H and v of the bodies, r, mu and
+    // the scaling and writes u per contact; Q2 reads u, mu, H and (H^T r, x) of the bodies, writes g; per
+    // line-search trial Q3 reads r, g, mu and writes r_s, Q4 reads the incidences, H rows and r_s per
+    // incidence, x, v, y_prev, f and M per body and writes H^T r_s; Q5 reads H^T r, x, v, y_prev and writes
+    // v, y_prev
+    const double inc = (double)h->admm_ninc, dd = (double)d, nn = (double)n, bb = (double)nb;
+    const double q1 = bb * (8.0 * dd * dd + 32.0 * dd) + inc * (24.0 * dd + 8.0 * dd) + nn * (24.0 * 3 + 16.0);
+    const double q2 = inc * (24.0 * dd + 16.0 * dd) + nn * (24.0 + 8.0 + 24.0);
+    const double q34 = nn * (24.0 * 3 + 8.0) + inc * (4.0 + 24.0 * dd + 24.0) + bb * (8.0 * dd * dd + 48.0 * dd);
+    const double q5 = bb * 48.0 * dd;
+    h->last_stats.iterations = out.iters;
+    h->last_stats.refine_iterations = 0;
+    h->last_stats.fp32_device_ms = 0.0;
+    h->last_stats.w_passes = 0;
+    h->last_stats.algorithmic_bytes = out.iters * (q1 + q2 + q5) + (double)out.trials * q34 + q1;
+    h->last_stats.fp64_fma = (double)out.iters * inc * 3.0 * dd * 3.0 + (double)out.trials * inc * 3.0 * dd;
+  }
+  if (residual) *residual = out.min_res;
+  if (iters) *iters = out.iters;
+  if (h->callback) {
+    const unsigned count = out.iters < o->max_iters ? out.iters + 1 : out.iters;
+    std::vector<double> tr(count);
+    if (count) BG_CUDA(cudaMemcpy(tr.data(), h->trace.p, sizeof(double) * count, cudaMemcpyDeviceToHost));
+    for (unsigned k = 0; k < count; ++k) h->callback(k, tr[k], h->callback_user);
+  }
+  return out.min_res >= 0 && out.min_res < o->tol ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
 }
 
 int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double* w, const double* mu) {

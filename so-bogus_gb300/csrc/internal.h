@@ -179,9 +179,41 @@ struct ADMMArgs {
   double lambda, gamma, tol;
   unsigned max_iters;
   int accelerated, use_inf;
+  const double* scaling;  // n: the error function's scalings (1 unless H is square at the block level)
 };
 cudaError_t launch_admm(const ADMMArgs& a, int grid, cudaStream_t s);
 int admm_max_grid(int device, int d);
+
+// DualAMA (kernels_admm.cu): Core/BlockSolvers/ADMM.impl.hpp:128-303 with A = M, B = 0, trivial preconditioner.
+struct DamaOut {
+  double min_res;
+  unsigned iters;
+  int stopped;     // the loop ended before max_iters (tolerance reached or divergence)
+  unsigned trials; // line-search trials over all iterations
+};
+struct DamaArgs {
+  int n, nbodies, d;
+  const int* cb;
+  const double* H;
+  const int* bptr;
+  const int* bent;
+  const double* M;        // nbodies x d x d mass blocks
+  const double* f;        // nbodies x d
+  const double* w;        // 3 n
+  const double* mu;       // n
+  const double* scaling;  // n
+  double *v, *r, *rs, *x, *HrBp, *ut, *g, *y_prev, *r_best, *v_best;
+  double* csum;           // 3 x max(contact chunks, body chunks)
+  double* scal;
+  double* trace;          // max_iters
+  DamaOut* out;
+  GridBarrier gb;
+  double tol, gamma, lambda0, opt, pess, m_true;
+  unsigned max_iters, ls_iters;
+  int accelerated, use_inf, desaxce;
+};
+cudaError_t launch_dama(const DamaArgs& a, int grid, cudaStream_t s);
+int dama_max_grid(int device, int d);
 
 // Adjoint of the SOC solve (kernels_adjoint.cu).
 struct AdjOut {

@@ -192,7 +192,9 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
         store3(a.ut, i, ut);
         load3(a.r, i, r);
         load3(a.z, i, z);
-        ev = law_eval(false, ldcg(a.inv_mu + i), ut, r);
+        const double sc = __ldg(a.scaling + i);
+        const double lx[3] = {ut[0] * sc, ut[1] * sc, ut[2] * sc};
+        ev = law_eval(false, ldcg(a.inv_mu + i), lx, r);
         const double d3[3] = {ut[0] - z[0], ut[1] - z[1], ut[2] - z[2]};
         gap = a.use_inf ? dmax(dmax(fabs(d3[0]), fabs(d3[1])), fabs(d3[2])) : sq3(d3);
       }
@@ -263,6 +265,315 @@ __global__ void __launch_bounds__(256) k_admm_persistent(ADMMArgs a) {
   admm_body<D>(a, ctx);
 }
 
+
+// ---- DualAMA --------------------------------------------------------------------------------------------
+// PrimalFrictionProblem::solveWith(DualAMAType&, v, r, staticProblem) (PrimalFrictionProblem.cpp:78-99).
+// Phases of one iteration (one lane per body in body phases, 32-contact chunks in contact phases):
+//   Q1 bodies + contacts  x = f + M v, z = H^T r - x and its norms; u = w + H v, law error at (r, u) .... reduce
+//   Q2 contacts + bodies  g = u + COV(u) + gamma H z; the best (r, v) kept ............................ barrier
+//   line search, trial by trial:
+//     Q3 contacts         r_s = P(r - lambda g) ....................................................... barrier
+//     Q4 bodies           H^T r_s, y = v + gamma (H^T r_s - x) over-relaxed, |(H^T r_s - f) - M y|^2 .. reduce
+//   (no line search: Q3 writes r = P(r - lambda g), Q5 forms H^T r)
+//   Q5 bodies             z = H^T r - x, y = v + gamma z, v = y + beta (y - y_prev) ..................... barrier
+// Orders: M v chains over the dofs from 0 and is added to f (subtracted from H^T r - f); H^T r per dof over the
+// body's contacts in increasing order, rows inner; H z and H v as the ADMM kernel's products; dof norms each body's
+// dofs left to right, then the canonical sum over bodies.
+template <int D>
+__device__ void dama_body(const DamaArgs& a, double* smem8) {
+  constexpr int DM = D > 0 ? D : kMaxDof;
+  const int d = D > 0 ? D : a.d;
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  const int C = (a.n + 31) / 32, CB = (a.nbodies + 31) / 32;
+  const int CC = C > CB ? C : CB;
+  const bool inf = a.use_inf != 0, desaxce = a.desaxce != 0;
+  const bool writer = blockIdx.x == 0 && threadIdx.x == 0;
+  auto put = [&](int q, int c, double v, bool is_max) {
+    v = is_max ? warp_max_butterfly(v) : warp_sum_butterfly(v);
+    if (lane == 0) a.csum[q * CC + c] = v;
+  };
+  auto sync = [&]() { return grid_barrier(a.gb, [] {}); };
+    // value 0 over count0 chunks, values 1.. over count1 chunks
+  auto sync_reduce = [&](int K, int count0, int count1, unsigned maxmask) {
+    return grid_barrier(a.gb, [&] {
+      for (int q = 0; q < K; ++q) {
+        const double v = block8_combine(a.csum + q * CC, q == 0 ? count0 : count1, (maxmask >> q) & 1u, smem8);
+        if (threadIdx.x == 0) a.scal[q] = v;
+      }
+    });
+  };
+  // H^T src for body b (d values): per dof, contacts in increasing order, rows inner
+  auto body_HT = [&](int b, const double* src, double* out) {
+#pragma unroll
+    for (int q = 0; q < DM; ++q)
+      if (q < d) out[q] = 0.0;
+    const int e0 = __ldg(a.bptr + b), e1 = __ldg(a.bptr + b + 1);
+    for (int e = e0; e < e1; ++e) {
+      const int ent = __ldg(a.bent + e);
+      const int i = ent >> 1;
+      const double* Hb = a.H + (size_t)ent * 3 * d;
+      const double rv[3] = {ldcg(src + 3 * i), ldcg(src + 3 * i + 1), ldcg(src + 3 * i + 2)};
+#pragma unroll
+      for (int q = 0; q < DM; ++q)
+        if (q < d) {
+          double s = out[q];
+          for (int rr = 0; rr < 3; ++rr) s = fma(__ldg(Hb + rr * d + q), rv[rr], s);
+          out[q] = s;
+        }
+    }
+  };
+  // (M_b src)_a: fma chain over the dofs from 0
+  auto body_M = [&](int b, const double* src, int row) {
+    const double* Mb = a.M + (size_t)b * d * d;
+    double t = 0.0;
+#pragma unroll
+    for (int q = 0; q < DM; ++q)
+      if (q < d) t = fma(__ldg(Mb + row * d + q), src[q], t);
+    return t;
+  };
+  // contact velocity-like product: init + H src (src per body)
+  auto contact_H = [&](int i, const double* init, const double* src, double* out) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) out[r] = init ? __ldg(init + 3 * i + r) : 0.0;
+    for (int t = 0; t < 2; ++t) {
+      const int body = __ldg(a.cb + 2 * i + t);
+      if (body < 0) continue;
+      const double* Hb = a.H + (2 * (size_t)i + t) * 3 * d;
+      double sv[DM];
+#pragma unroll
+      for (int m = 0; m < DM; ++m)
+        if (m < d) sv[m] = ldcg(src + (size_t)body * d + m);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        double acc = out[r];
+#pragma unroll
+        for (int m = 0; m < DM; ++m)
+          if (m < d) acc = fma(__ldg(Hb + r * d + m), sv[m], acc);
+        out[r] = acc;
+      }
+    }
+  };
+
+  double* r = a.r;
+  double* rs = a.rs;
+  // H^T r once
+  for (int c = gwarp; c < CB; c += nwarps) {
+    const int b = 32 * c + lane;
+    if (b < a.nbodies) {
+      double h[DM];
+      body_HT(b, r, h);
+#pragma unroll
+      for (int q = 0; q < DM; ++q)
+        if (q < d) a.HrBp[(size_t)b * d + q] = h[q];
+    }
+  }
+  if (!sync()) return;
+  double lambda = a.lambda0, theta_prev = 1., res_prev = -1., min_res = -1., res = -1.;
+  unsigned it = 0, trials = 0;
+  int stopped = 0;
+  for (; it < a.max_iters; ++it) {
+    // Q1
+    for (int c = gwarp; c < CB; c += nwarps) {
+      const int b = 32 * c + lane;
+      double pz = 0.0, pz2 = 0.0;
+      if (b < a.nbodies) {
+        double vb[DM];
+#pragma unroll
+        for (int q = 0; q < DM; ++q)
+          if (q < d) vb[q] = ldcg(a.v + (size_t)b * d + q);
+#pragma unroll
+        for (int q = 0; q < DM; ++q)
+          if (q < d) {
+            const double xq = __ldg(a.f + (size_t)b * d + q) + body_M(b, vb, q);
+            a.x[(size_t)b * d + q] = xq;
+            const double z = ldcg(a.HrBp + (size_t)b * d + q) - xq;
+            pz = inf ? dmax(fabs(z), pz) : pz + z * z;
+            pz2 = pz2 + z * z;
+          }
+      }
+      put(1, c, pz, inf);
+      put(2, c, pz2, false);
+    }
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      double ev = 0.0;
+      if (i < a.n) {
+        double u[3];
+        contact_H(i, a.w, a.v, u);
+        a.ut[3 * i] = u[0];
+        a.ut[3 * i + 1] = u[1];
+        a.ut[3 * i + 2] = u[2];
+        const double sc = __ldg(a.scaling + i);
+        const double lx[3] = {ldcg(r + 3 * i) * sc, ldcg(r + 3 * i + 1) * sc, ldcg(r + 3 * i + 2) * sc};
+        ev = law_eval(desaxce, __ldg(a.mu + i), lx, u);
+      }
+      put(0, c, ev, inf);
+    }
+    if (!sync_reduce(3, C, CB, inf ? 3u : 0u)) return;
+    {
+      const double e0 = ldcg(a.scal), z0 = ldcg(a.scal + 1);
+      res = (inf ? e0 : e0 / (double)(1 + a.n)) + (inf ? z0 : z0 / (1.0 + a.m_true));
+    }
+    const double h0 = ldcg(a.scal + 2);
+    if (a.trace && writer) a.trace[it] = res;
+    const bool best = res < min_res || it == 0;
+    if (best) min_res = res;
+    const bool done = best && res < a.tol;
+    if (!best && res > 1.e50) {
+      stopped = 1;
+      break;
+    }
+    double beta = 0.0;
+    if (a.accelerated && res < res_prev) beta = nesterov_inertia(theta_prev, 0.);
+    else theta_prev = 1.;
+    // Q2: g (unless done) and the best (r, v)
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      if (i < a.n) {
+        if (best)
+          for (int k = 0; k < 3; ++k) a.r_best[3 * i + k] = ldcg(r + 3 * i + k);
+        if (!done) {
+          double u[3], hz[3];
+          for (int k = 0; k < 3; ++k) u[k] = ldcg(a.ut + 3 * i + k);
+          // H z with z = H^T r - x per body
+          hz[0] = hz[1] = hz[2] = 0.0;
+          for (int t = 0; t < 2; ++t) {
+            const int body = __ldg(a.cb + 2 * i + t);
+            if (body < 0) continue;
+            const double* Hb = a.H + (2 * (size_t)i + t) * 3 * d;
+            double zb[DM];
+#pragma unroll
+            for (int m = 0; m < DM; ++m)
+              if (m < d) zb[m] = ldcg(a.HrBp + (size_t)body * d + m) - ldcg(a.x + (size_t)body * d + m);
+#pragma unroll
+            for (int rr = 0; rr < 3; ++rr) {
+              double acc = hz[rr];
+#pragma unroll
+              for (int m = 0; m < DM; ++m)
+                if (m < d) acc = fma(__ldg(Hb + rr * d + m), zb[m], acc);
+              hz[rr] = acc;
+            }
+          }
+          const double s0 = duality_cov(desaxce, __ldg(a.mu + i), u);
+          a.g[3 * i] = fma(a.gamma, hz[0], u[0] + s0);
+          a.g[3 * i + 1] = fma(a.gamma, hz[1], u[1] + 0.0);
+          a.g[3 * i + 2] = fma(a.gamma, hz[2], u[2] + 0.0);
+        }
+      }
+    }
+    if (best)
+      for (int c = gwarp; c < CB; c += nwarps) {
+        const int b = 32 * c + lane;
+        if (b < a.nbodies)
+          for (int q = 0; q < d; ++q) a.v_best[(size_t)b * d + q] = ldcg(a.v + (size_t)b * d + q);
+      }
+    if (!sync()) return;
+    if (done) {
+      stopped = 1;
+      break;
+    }
+    if (a.ls_iters == 0) {
+      // Q3: r = P(r - lambda g) in place
+      for (int c = gwarp; c < C; c += nwarps) {
+        const int i = 32 * c + lane;
+        if (i < a.n) {
+          double rr[3];
+          for (int k = 0; k < 3; ++k) rr[k] = ldcg(r + 3 * i + k) - lambda * ldcg(a.g + 3 * i + k);
+          project_cone(__ldg(a.mu + i), rr);
+          for (int k = 0; k < 3; ++k) r[3 * i + k] = rr[k];
+        }
+      }
+      if (!sync()) return;
+    } else {
+      lambda *= a.opt;
+      for (unsigned ls = 0; ls < a.ls_iters; ++ls) {
+        ++trials;
+        for (int c = gwarp; c < C; c += nwarps) {
+          const int i = 32 * c + lane;
+          if (i < a.n) {
+            double rr[3];
+            for (int k = 0; k < 3; ++k) rr[k] = ldcg(r + 3 * i + k) - lambda * ldcg(a.g + 3 * i + k);
+            project_cone(__ldg(a.mu + i), rr);
+            for (int k = 0; k < 3; ++k) rs[3 * i + k] = rr[k];
+          }
+        }
+        if (!sync()) return;
+        // Q4
+        for (int c = gwarp; c < CB; c += nwarps) {
+          const int b = 32 * c + lane;
+          double ph = 0.0;
+          if (b < a.nbodies) {
+            double hr[DM], y[DM];
+            body_HT(b, rs, hr);
+#pragma unroll
+            for (int q = 0; q < DM; ++q)
+              if (q < d) {
+                a.HrBp[(size_t)b * d + q] = hr[q];
+                const double zq = hr[q] - ldcg(a.x + (size_t)b * d + q);
+                const double yk = ldcg(a.v + (size_t)b * d + q) + a.gamma * zq;
+                y[q] = yk + beta * (yk - ldcg(a.y_prev + (size_t)b * d + q));
+              }
+#pragma unroll
+            for (int q = 0; q < DM; ++q)
+              if (q < d) {
+                const double gq = (hr[q] - __ldg(a.f + (size_t)b * d + q)) - body_M(b, y, q);
+                ph = ph + gq * gq;
+              }
+          }
+          put(0, c, ph, false);
+        }
+        if (!sync_reduce(1, CB, CB, 0u)) return;
+        const double hh = ldcg(a.scal);
+        if (hh < h0) break;
+        lambda *= a.pess;
+      }
+      double* t = r;  // r = r_s
+      r = rs;
+      rs = t;
+    }
+    // Q5
+    for (int c = gwarp; c < CB; c += nwarps) {
+      const int b = 32 * c + lane;
+      if (b < a.nbodies) {
+        double hr[DM];
+        if (a.ls_iters == 0) {
+          body_HT(b, r, hr);
+        } else {
+#pragma unroll
+          for (int q = 0; q < DM; ++q)
+            if (q < d) hr[q] = ldcg(a.HrBp + (size_t)b * d + q);
+        }
+#pragma unroll
+        for (int q = 0; q < DM; ++q)
+          if (q < d) {
+            a.HrBp[(size_t)b * d + q] = hr[q];
+            const double zq = hr[q] - ldcg(a.x + (size_t)b * d + q);
+            const double yk = ldcg(a.v + (size_t)b * d + q) + a.gamma * zq;
+            const double yp = ldcg(a.y_prev + (size_t)b * d + q);
+            a.v[(size_t)b * d + q] = yk + beta * (yk - yp);
+            a.y_prev[(size_t)b * d + q] = yk;
+          }
+      }
+    }
+    res_prev = res;
+    if (!sync()) return;
+  }
+  if (writer) {
+    a.out->min_res = min_res;
+    a.out->iters = it;
+    a.out->stopped = stopped;
+    a.out->trials = trials;
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_dama_persistent(DamaArgs a) {
+  __shared__ double smem8[8];
+  dama_body<D>(a, smem8);
+}
+
 }  // namespace
 
 cudaError_t launch_admm(const ADMMArgs& a, int grid, cudaStream_t s) {
@@ -277,6 +588,27 @@ int admm_max_grid(int device, int d) {
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
   const cudaError_t e = d == 6 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_admm_persistent<6>, 256, 0)
                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_admm_persistent<0>, 256, 0);
+  if (e != cudaSuccess) return 0;
+  if (per > 2) per = 2;
+  return per * sms;
+}
+
+}  // namespace bogus_gpu
+
+namespace bogus_gpu {
+
+cudaError_t launch_dama(const DamaArgs& a, int grid, cudaStream_t s) {
+  DamaArgs copy = a;
+  void* args[] = {&copy};
+  const void* fn = a.d == 6 ? (const void*)k_dama_persistent<6> : (const void*)k_dama_persistent<0>;
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s);
+}
+
+int dama_max_grid(int device, int d) {
+  int sms = 0, per = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  const cudaError_t e = d == 6 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dama_persistent<6>, 256, 0)
+                               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dama_persistent<0>, 256, 0);
   if (e != cudaSuccess) return 0;
   if (per > 2) per = 2;
   return per * sms;

@@ -43,7 +43,8 @@ def run_pair(bg, oracle, inp, r0, with_v=True, static=False, regularization=0.0,
     o = bg.MecheOptions()
     names = {"max_threads": "maxThreads", "max_iters": "maxIters", "cadoux_iters": "cadouxIters",
              "tolerance": "tolerance", "algorithm": "algorithm", "gs_coloring": "gsColoring",
-             "pg_variant": "pgVariant", "admm_step": "admmProjStepSize", "inf_norm": "useInfinityNorm",
+             "pg_variant": "pgVariant", "admm_step": "admmProjStepSize", "admm_fp_step": "admmFpStepSize",
+             "inf_norm": "useInfinityNorm",
              "gs_regularization": "gsRegularization", "try_zero": "tryZeroAsWell"}
     for k, val in opts.items():
         setattr(o, names[k], val)
@@ -85,7 +86,17 @@ def test_small_friction_world_admm_bitwise(bg, oracle):
     assert g[0] < 1e-9
 
 
-@pytest.mark.parametrize("case", ["gs", "gs_colored_regularized", "pg_static", "gs_cadoux", "admm_v0", "matrix_free"])
+@pytest.mark.parametrize("static, with_v", [(True, True), (False, False)])
+def test_small_friction_world_dual_ama_bitwise(bg, oracle, static, with_v):
+    """Algorithm DualAMA (MecheInterface.cpp:249-261): no line search, the facade's two step sizes."""
+    _, inp = small_friction_world()
+    g, o = run_pair(bg, oracle, inp, np.zeros(6), with_v=with_v, static=static, algorithm=4, tolerance=1e-12,
+                    max_iters=3000, admm_step=1e-2, admm_fp_step=1e-1)
+    assert_same(g, o)
+
+
+@pytest.mark.parametrize("case", ["gs", "gs_colored_regularized", "pg_static", "gs_cadoux", "admm_v0", "matrix_free",
+                                  "dual_ama"])
 def test_random_world_problem_bitwise(bg, oracle, case):
     inp = random_world_problem()
     n = len(inp["objA"])
@@ -100,6 +111,9 @@ def test_random_world_problem_bitwise(bg, oracle, case):
                         max_iters=300, inf_norm=True)
     elif case == "matrix_free":
         g, o = run_pair(bg, oracle, inp, r0, algorithm=2, tolerance=1e-8, max_iters=75, gs_regularization=1e-3)
+    elif case == "dual_ama":
+        g, o = run_pair(bg, oracle, inp, r0, algorithm=4, tolerance=1e-10, max_iters=150, admm_step=1e-2,
+                        admm_fp_step=1e-1)
     elif case == "gs_cadoux":
         g, o = run_pair(bg, oracle, inp, r0, algorithm=0, cadoux_iters=4, tolerance=1e-8, max_iters=60)
     else:
@@ -109,11 +123,11 @@ def test_random_world_problem_bitwise(bg, oracle, case):
     assert_same(g, o)
 
 
-def test_meche_rejects_unavailable_algorithms_and_singular_mass(bg):
+def test_meche_rejects_unknown_algorithms_and_singular_mass(bg):
     _, inp = small_friction_world()
     M = bg.MecheFrictionProblem()
     M.fromPrimal(**inp)
-    for alg in (bg.MECHE_DUAL_AMA,):
+    for alg in (-1, 5):
         o = bg.MecheOptions()
         o.algorithm = alg
         with pytest.raises(bg.BogusGpuError):

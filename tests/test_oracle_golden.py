@@ -330,10 +330,24 @@ def test_meche_admm_matches_the_primal_solver(oracle):
     P = oracle.PrimalProblem(np.array(s["minv"]), s["objA"], s["objB"], np.array(s["HA"]), np.array(s["HB"]))
     minv = np.array(s["minv"])
     res_o, v_o, r_o, _ = P.solve_admm(minv, 0.0, np.array(s["mu"]), np.array(s["f_padded"]), np.array(s["w"]),
-                                      np.zeros(8), np.zeros(6), tol=1e-9, max_iters=2000, step=1e-2)
+                                      np.zeros(8), np.zeros(6), tol=1e-9, max_iters=2000, step=1e-2,
+                                      true_dofs=[4, 2])
     E = inp["E"]
     r_loc = np.concatenate([E[i].T @ r[3 * i:3 * i + 3] for i in range(2)])
     assert np.allclose(r_loc, r_o, rtol=0, atol=1e-6)
+
+
+def test_meche_dual_ama_reaches_the_coulomb_solution(oracle):
+    """Algorithm DualAMA (MecheInterface.cpp:249-261: no line search, admmProjStepSize / admmFpStepSize) on the
+    Coulomb problem reaches the reference solution of tests/SmallFrictionPb.hpp."""
+    s, inp = small_friction_world()
+    M = oracle.MecheProblem(**inp)
+    res, r, v = M.solve(np.zeros(6), with_v=False, algorithm=4, tolerance=1e-12, max_iters=3000, admm_step=1e-2,
+                        admm_fp_step=1e-1)
+    assert res < 1e-12
+    E = inp["E"]
+    r_loc = np.concatenate([E[i].T @ r[3 * i:3 * i + 3] for i in range(2)])
+    assert isApprox(s["sol"], r_loc, s["sol_rel_tol"])
 
 
 # ---- ProductGaussSeidel (Core/BlockSolvers/ProductGaussSeidel.impl.hpp): the matrix-free sweep reaches the
@@ -346,3 +360,27 @@ def test_small_friction_product_gauss_seidel(oracle, golden, strategy):
                                    coulomb=True, strategy=strategy, tol=1e-8)
     assert res < s["res_tol"]
     assert isApprox(s["sol"], r, s["sol_rel_tol"])
+
+
+# ---- tests/ADMM.cpp:135-189: DualAMA on SmallFrictionPb (its own 4 + 2 dofs), Standard with line search and
+# Accelerated without, on the SOC cone and the Coulomb law; the Coulomb results at the reference solution -----
+@pytest.mark.parametrize("name, variant_acc, ls, proj, coulomb", [
+    ("Std-Kmu", False, 4, 1.0, False), ("Std-Cmu", False, 4, 1.0, True),
+    ("Acc-Kmu", True, 0, 1e-1, False), ("Acc-Cmu", True, 0, 1e-2, True)])
+def test_small_friction_dual_ama(oracle, golden, name, variant_acc, ls, proj, coulomb):
+    s = golden["small_friction_pb"]
+    minv = np.array(s["minv"])
+    P = oracle.PrimalProblem(minv, s["objA"], s["objB"], np.array(s["HA"]), np.array(s["HB"]))
+    dofs = s["dofs"]
+    nd = s["ndof_padded"]
+    mass = np.zeros_like(minv)
+    for k, dk in enumerate(dofs):
+        mass[k, :dk, :dk] = np.linalg.inv(minv[k, :dk, :dk])
+    f = np.array(s["f_padded"])
+    v0 = np.concatenate([-(minv[k] @ f[nd * k:nd * k + nd]) for k in range(2)])  # M^-1 (H^T 0 - f)
+    res, v, r, _ = P.solve_dual_ama(mass, np.array(s["mu"]), f, np.array(s["w"]), v0, np.zeros(6),
+                                    static=not coulomb, tol=1e-16, fp_step=1e-1, proj_step=proj, ls_iters=ls,
+                                    optimistic=1.25, accelerated=variant_acc, true_dofs=dofs)
+    assert res < 1e-8, name
+    if coulomb:
+        assert isApprox(s["sol"], r, 1e-4), name
