@@ -79,6 +79,9 @@ struct GSCache {
   DevBuf<unsigned char> skip, processed;
   DevBuf<unsigned long long> tile_max;
   DevBuf<double> ndx_ref;
+  DevBuf<unsigned> flow, done;  // dataflow sweep: position counter and tag, per-contact visit tags
+  DevBuf<int> pdep;             // matrix-free sweep: previous contact on each slot's body
+  int flow_grid = 0;
   double auto_reg = -1.0;
   int use_coloring = -1;
   // one captured sweep per ndxRef parity, keyed by the law / strategy / skip settings baked into it
@@ -98,6 +101,7 @@ struct GSCache {
     rowptr.release(); col.release(); val.release(); local.release(); reg.release(); scaling.release();
     b.release(); mu.release(); x.release(); nx2.release(); ndx2.release(); y.release(); chunk.release();
     scalar.release(); xbest.release(); skip.release(); processed.release(); tile_max.release(); ndx_ref.release();
+    flow.release(); done.release(); pdep.release();
     valid = false;
   }
 };
@@ -603,7 +607,17 @@ int prepare_gs(bogus_gpu_problem* h, double auto_reg, int use_coloring) {
   BG_CUDA(g.ndx_ref.ensure(2));
   BG_CUDA(g.chunk.ensure((n + 31) / 32 + 1));
   BG_CUDA(g.scalar.ensure(2));
+  BG_CUDA(g.flow.ensure(2));
+  BG_CUDA(g.done.ensure(n > 0 ? n : 1));
+  BG_CUDA(h->status.ensure(1));
+  g.flow_grid = gs_flow_grid(h->device);
+  if (g.flow_grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "occupancy query failed (Gauss-Seidel sweep)");
   cudaStream_t s = h->stream;
+  {
+    const unsigned f0[2] = {0u, 1u};
+    BG_CUDA(cudaMemcpyAsync(g.flow.p, f0, sizeof(f0), cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemsetAsync(g.done.p, 0, sizeof(unsigned) * (n > 0 ? n : 1), s));
+  }
   BG_CUDA(cudaMemcpyAsync(g.rowptr.p, pf.rowptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
   if (nnz) {
     BG_CUDA(cudaMemcpyAsync(g.col.p, pf.col.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
@@ -624,8 +638,8 @@ int prepare_gs(bogus_gpu_problem* h, double auto_reg, int use_coloring) {
   return BOGUS_GPU_OK;
 }
 
-// One sweep: every level in order, then the skip update. Captured once per parity into a CUDA graph and
-// replayed (the arguments never change between sweeps of the same settings).
+// One sweep (the dataflow kernel of the assembled or the matrix-free sweep), then the skip update. Captured once
+// per parity into a CUDA graph and replayed (the arguments never change between sweeps of the same settings).
 int launch_sweep(bogus_gpu_problem* h, GSCache& g, const GSArgs& a, int parity, double abs_skip_tol,
                  double skip_tol, int abs_skip_iters, long long key, bool product) {
   cudaStream_t s = h->stream;
@@ -635,9 +649,7 @@ int launch_sweep(bogus_gpu_problem* h, GSCache& g, const GSArgs& a, int parity, 
     cudaGraph_t graph = nullptr;
     BG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    for (int L = 0; L < nlevels && e == cudaSuccess; ++L)
-      e = product ? launch_pgs_level(a, g.level_off[L], g.level_off[L + 1], parity, s)
-                  : launch_gs_level(a, g.level_off[L], g.level_off[L + 1], parity, s);
+    e = product ? launch_pgs_flow(a, g.flow_grid, parity, s) : launch_gs_flow(a, g.flow_grid, parity, s);
     if (e == cudaSuccess) e = launch_gs_skip(a, parity, abs_skip_tol, skip_tol, abs_skip_iters, s);
     const cudaError_t e2 = cudaStreamEndCapture(s, &graph);
     if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -650,7 +662,7 @@ int launch_sweep(bogus_gpu_problem* h, GSCache& g, const GSArgs& a, int parity, 
     g.sweep_key = key;
   }
   BG_CUDA(cudaGraphLaunch(g.sweep[parity], s));
-  h->last_launches += nlevels + 1;
+  h->last_launches += 2;
   return BOGUS_GPU_OK;
 }
 
@@ -1018,6 +1030,9 @@ GSArgs gs_args(bogus_gpu_problem* h, const bogus_gpu_gs_options* o) {
   a.order = g.order.p;
   a.desaxce = o->static_problem ? 0 : 1;
   a.strat = o->local_strategy;
+  a.flow = g.flow.p;
+  a.done = g.done.p;
+  a.status = h->status.p;
   return a;
 }
 
@@ -1033,7 +1048,16 @@ int run_gs_core(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* res
   BG_CUDA(cudaMemsetAsync(g.tile_max.p, 0, sizeof(unsigned long long) * 2 * ntiles, s));
   BG_CUDA(cudaMemsetAsync(g.ndx_ref.p, 0, sizeof(double) * 2, s));
   BG_CUDA(cudaMemsetAsync(g.skip.p, 0, n, s));
+  BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   const GSArgs a = gs_args(h, o);
+  // a wait of the dataflow sweep that ran out (BOGUS_GPU_TIMEOUT), read when the host synchronises anyway
+  auto sweep_status = [&]() -> int {
+    int st = 0;
+    BG_CUDA(cudaMemcpyAsync(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+    if (st != 0) return fail(st, "device-side wait timed out in the Gauss-Seidel sweep");
+    return BOGUS_GPU_OK;
+  };
   const bool desaxce = !o->static_problem;
   const bool use_inf = o->use_infinity_norm != 0;
   // initial evaluation and tryZero (GaussSeidel.impl.hpp:152-167)
@@ -1086,6 +1110,7 @@ int run_gs_core(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* res
     parity ^= 1;
     if (0 == (it % o->eval_every)) {
       if (int e = gs_eval(h, a, g.x.p, g.b.p, desaxce, use_inf, &err)) return e;
+      if (int e = sweep_status()) return e;
       if (err < err_best) {
         BG_CUDA(cudaMemcpyAsync(g.xbest.p, g.x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
         err_best = err;
@@ -1100,6 +1125,7 @@ int run_gs_core(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* res
       h->last_launches += 1;
     }
   }
+  if (int e = sweep_status()) return e;
   if (it > o->max_iters && has_best)
     BG_CUDA(cudaMemcpyAsync(g.x.p, g.xbest.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
   if (residual) *residual = err_best;
@@ -1195,18 +1221,21 @@ int prepare_pgs(bogus_gpu_problem* h, double auto_reg) {
       D[8] += reg[i];
     }
   }
-  std::vector<int> last(nb, -1), level(n, 0);
+  // levels (the order contacts are handed out) and, per slot, the previous contact on the slot's body
+  std::vector<int> last(nb, -1), prev(nb, -1), level(n, 0), pdep(2 * (size_t)(n > 0 ? n : 1), -1);
   int nlevels = n > 0 ? 1 : 0;
   for (int i = 0; i < n; ++i) {
     int lv = 0;
     for (int t = 0; t < 2; ++t) {
       const int b = h->h_cb[2 * (size_t)i + t];
       if (b >= 0 && last[b] + 1 > lv) lv = last[b] + 1;
+      if (b >= 0) pdep[2 * (size_t)i + t] = prev[b];
     }
     level[i] = lv;
     for (int t = 0; t < 2; ++t) {
       const int b = h->h_cb[2 * (size_t)i + t];
       if (b >= 0 && lv > last[b]) last[b] = lv;
+      if (b >= 0) prev[b] = i;
     }
     if (lv + 1 > nlevels) nlevels = lv + 1;
   }
@@ -1234,6 +1263,18 @@ int prepare_pgs(bogus_gpu_problem* h, double auto_reg) {
   BG_CUDA(g.scalar.ensure(2));
   BG_CUDA(h->pgs_Mx.ensure((size_t)nb * d));
   BG_CUDA(h->mf.ensure((size_t)nb * d));
+  BG_CUDA(g.flow.ensure(2));
+  BG_CUDA(g.done.ensure(n > 0 ? n : 1));
+  BG_CUDA(g.pdep.ensure(pdep.size()));
+  BG_CUDA(h->status.ensure(1));
+  g.flow_grid = pgs_flow_grid(h->device);
+  if (g.flow_grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "occupancy query failed (matrix-free sweep)");
+  {
+    const unsigned f0[2] = {0u, 1u};
+    BG_CUDA(cudaMemcpyAsync(g.flow.p, f0, sizeof(f0), cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemsetAsync(g.done.p, 0, sizeof(unsigned) * (n > 0 ? n : 1), s));
+  }
+  BG_CUDA(cudaMemcpyAsync(g.pdep.p, pdep.data(), sizeof(int) * pdep.size(), cudaMemcpyHostToDevice, s));
   BG_CUDA(cudaMemcpyAsync(g.order.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
   BG_CUDA(cudaMemcpyAsync(g.local.p, local.data(), sizeof(double) * local.size(), cudaMemcpyHostToDevice, s));
   BG_CUDA(cudaMemcpyAsync(g.reg.p, reg.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
@@ -1304,7 +1345,15 @@ int bogus_gpu_solve_product_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options*
   BG_CUDA(cudaMemsetAsync(g.tile_max.p, 0, sizeof(unsigned long long) * 2 * ntiles, s));
   BG_CUDA(cudaMemsetAsync(g.ndx_ref.p, 0, sizeof(double) * 2, s));
   BG_CUDA(cudaMemsetAsync(g.skip.p, 0, n, s));
+  BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   BG_CUDA(cudaEventRecord(h->ev0, s));
+  auto sweep_status = [&]() -> int {
+    int st = 0;
+    BG_CUDA(cudaMemcpyAsync(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+    if (st != 0) return fail(st, "device-side wait timed out in the matrix-free sweep");
+    return BOGUS_GPU_OK;
+  };
   GSArgs a{};
   a.n = n;
   a.local = g.local.p;
@@ -1327,6 +1376,10 @@ int bogus_gpu_solve_product_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options*
   a.cb = h->cb.p;
   a.Mx = h->pgs_Mx.p;
   a.d = d;
+  a.flow = g.flow.p;
+  a.done = g.done.p;
+  a.status = h->status.p;
+  a.pdep = g.pdep.p;
   const bool desaxce = !o->static_problem;
   const bool use_inf = o->use_infinity_norm != 0;
   double err_best = DBL_MAX, err = 0;
@@ -1377,6 +1430,7 @@ int bogus_gpu_solve_product_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options*
     parity ^= 1;
     if (0 == (it % o->eval_every)) {
       if (int e = pgs_eval(h, desaxce, use_inf, &err)) return e;
+      if (int e = sweep_status()) return e;
       if (err < err_best) {
         BG_CUDA(cudaMemcpyAsync(g.xbest.p, g.x.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
         err_best = err;
@@ -1391,6 +1445,7 @@ int bogus_gpu_solve_product_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options*
       h->last_launches += 1;
     }
   }
+  if (int e = sweep_status()) return e;
   const double* result = (it > o->max_iters && has_best) ? g.xbest.p : g.x.p;
   BG_CUDA(cudaEventRecord(h->ev1, s));
   BG_CUDA(cudaMemcpyAsync(r, result, sizeof(double) * n3, cudaMemcpyDeviceToHost, s));

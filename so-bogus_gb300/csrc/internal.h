@@ -127,7 +127,7 @@ struct GSArgs {
   unsigned char* processed;
   unsigned long long* tile_max;  // 2 * ntiles (sweep parity)
   double* ndx_ref;               // 2 (sweep parity)
-  const int* order;              // contacts grouped by level (sweep positions)
+  const int* order;              // contacts grouped by level (sweep positions): the order contacts are handed out
   int desaxce, strat;
   // matrix-free sweep (ProductGaussSeidel): slot Jacobians H (3 x d), T = M^-1 H^T (d x 3), slot bodies cb,
   // Mx = M^-1 H^T x per body (nbodies x d)
@@ -136,14 +136,23 @@ struct GSArgs {
   const int* cb;
   double* Mx;
   int d;
+  // dataflow sweep: flow[0] = next sweep position to hand out, flow[1] = the sweep's tag; done[i] = tag once
+  // contact i has been visited in this sweep; status records a wait that ran out
+  unsigned* flow;
+  unsigned* done;
+  int* status;
+  const int* pdep;  // matrix-free sweep: per contact slot, the previous contact on that body (-1: none)
 };
 constexpr int kGSTile = 1024;
-cudaError_t launch_gs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s);
+constexpr int kGSFlowWarps = 4;  // warps per CTA of the dataflow sweep
+cudaError_t launch_gs_flow(const GSArgs& a, int grid, int parity, cudaStream_t s);
+int gs_flow_grid(int device);
 cudaError_t launch_gs_skip(const GSArgs& a, int parity, double abs_skip_tol, double skip_tol, int abs_skip_iters,
                            cudaStream_t s);
 cudaError_t launch_scale_scalar(double* p, double divisor, cudaStream_t s);
 // matrix-free Gauss-Seidel (kernels_gs.cu)
-cudaError_t launch_pgs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s);
+cudaError_t launch_pgs_flow(const GSArgs& a, int grid, int parity, cudaStream_t s);
+int pgs_flow_grid(int device);
 cudaError_t launch_pgs_local(int n, int d, const int* cb, const double* H, const double* T, double* local,
                              cudaStream_t s);
 cudaError_t launch_pgs_mx(int nbodies, int d, const int* bptr, const int* bent, const double* T, const double* x,

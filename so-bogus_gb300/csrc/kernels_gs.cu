@@ -1,19 +1,19 @@
-// Projected Gauss-Seidel sweep (Core/BlockSolvers/GaussSeidel.impl.hpp:62-124), level by level.
+// Projected Gauss-Seidel sweep (Core/BlockSolvers/GaussSeidel.impl.hpp:62-124).
 //
 // The sweep order is the contacts' own order or, with coloring, the order of Coloring::compute after the
 // contact permutation (MecheInterface.cpp:330-337); the problem is renumbered so that the sweep visits
 // contacts 0, 1, 2, ... In the sequential sweep, contact i reads the new value of every neighbour visited
 // before it and the old value of every neighbour visited after it. Give each contact the level
-// 1 + max(level of its earlier neighbours): contacts of one level share no block of W, and processing the
-// levels in increasing order gives every contact exactly the values the sequential sweep gives it. So one
-// launch per level reproduces the sequential result bit for bit: thread i gathers its split row
-// b_i - reg_i x_i + sum_{j != i} W_ij x_j (columns in increasing order, canonical chain), runs the local
-// Coulomb / SOC solver and applies the (possibly halved) update.
+// 1 + max(level of its earlier neighbours): contacts of one level share no block of W, and any schedule that
+// visits a contact after its earlier neighbours and before its later ones gives every contact exactly the
+// values the sequential sweep gives it, so the result is the same bit for bit. Visiting contact i: gather its
+// split row b_i - reg_i x_i + sum_{j != i} W_ij x_j (columns in increasing order, canonical chain), run the
+// local Coulomb / SOC solver and apply the (possibly halved) update.
 //
 // The skip heuristic (:107-117) depends on ndxRef, a running maximum over the contacts already visited in
-// the sweep. It is reproduced exactly after each sweep: the level kernels record every solved contact's
-// step norm and a per-tile maximum (max is order-independent), and k_gs_skip turns them into the
-// sequential prefix maximum and the skip counters.
+// the sweep. It is reproduced exactly after each sweep: the sweep records every solved contact's step norm
+// and a per-tile maximum (max is order-independent), and k_gs_skip turns them into the sequential prefix
+// maximum and the skip counters.
 #include "internal.h"
 #include "soc_device.cuh"
 
@@ -21,95 +21,137 @@ namespace bogus_gpu {
 
 __device__ __forceinline__ unsigned long long dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
 
-// One warp per contact (a CTA of 32 threads): a level is latency bound (long dependent FP64 chains per contact),
-// so its contacts are spread over as many SMs as possible, and contacts whose local solves take different
-// branches never share a warp. The lanes stage up to 32 blocks of the row (and the x of their columns) at a
-// time in shared memory; lane 0 accumulates them in column order and runs the local solve.
-__global__ void __launch_bounds__(32) k_gs_level(GSArgs a, int l0, int l1, int parity) {
-  const int t = l0 + blockIdx.x;
-  if (t >= l1) return;
-  const int lane = threadIdx.x;
-  const int i = a.order[t];
-  const unsigned char sk = a.skip[i];
-  __syncwarp();  // every lane has read the counter before lane 0 changes it: the branch below is warp-uniform
-  if (sk) {
-    if (lane == 0) {
-      a.skip[i] = (unsigned char)(sk - 1);
-      a.processed[i] = 0;
-    }
-    return;
-  }
-  __shared__ double sB[32][12];
-  __shared__ int sJ[32];
-  double lx[3] = {a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2]};
-  const double reg = a.reg[i];
-  double lb[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) lb[k] = a.b[3 * i + k] - reg * lx[k];
-  const int k0 = a.rowptr[i], k1 = a.rowptr[i + 1];
-  for (int base = k0; base < k1; base += 32) {
-    const int k = base + lane;
-    if (k < k1) {
-      const int j = a.col[k];
-      sJ[lane] = j;
-      const double* B = a.val + 9 * (size_t)k;
-#pragma unroll
-      for (int e = 0; e < 9; ++e) sB[lane][e] = B[e];
-      sB[lane][9] = a.x[3 * j];
-      sB[lane][10] = a.x[3 * j + 1];
-      sB[lane][11] = a.x[3 * j + 2];
-    }
-    __syncwarp();
-    if (lane == 0) {
-      const int cnt = min(32, k1 - base);
-      for (int q = 0; q < cnt; ++q) {
-        if (sJ[q] == i) continue;
-        const double* B = sB[q];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          double s = lb[r];
-          s = fma(B[3 * r + 0], B[9], s);
-          s = fma(B[3 * r + 1], B[10], s);
-          s = fma(B[3 * r + 2], B[11], s);
-          lb[r] = s;
-        }
+// Dataflow sweep: one launch visits every contact. Each warp takes the next contact in level order from a
+// counter and waits only for the earlier neighbours of its contact (flags set when they are visited): a
+// contact starts as soon as its own earlier neighbours are done, not when the slowest contact of the previous
+// level is (a launch per level would wait for it; the sweep is latency bound, the local solves being long
+// dependent FP64 chains). Level order rather than sweep order keeps the contacts in flight mostly independent
+// (consecutive contacts of the sweep often share a body). An earlier neighbour has been visited (its flag was
+// set after its x was written), a later neighbour has not (it waits for this contact's flag), so every contact
+// sees the values of the sequential sweep. A warp waits only for contacts of lower levels, handed out before its own and so already taken by
+// running warps: the sweep always progresses. Every wait is bounded (kBarrierTimeoutNs); a wait that runs
+// out records BOGUS_GPU_TIMEOUT and the warp stops.
+__device__ __forceinline__ bool gs_wait_done(const unsigned* f, unsigned tag, const int* status) {
+  if (ld_acquire_u32(f) == tag) return true;
+  const unsigned long long t0 = global_timer_ns();
+  unsigned spins = 0;
+  for (;;) {
+    __nanosleep(64);
+    if (ld_acquire_u32(f) == tag) return true;
+    if ((++spins & 63u) == 0) {
+      if (ld_relaxed_i32(status) != 0) return false;
+      if (global_timer_ns() - t0 > kBarrierTimeoutNs) {
+        atomicCAS(const_cast<int*>(status), 0, (int)BOGUS_GPU_TIMEOUT);
+        return false;
       }
     }
-    __syncwarp();
-  }
-  if (lane != 0) return;
-  double A[9];
-#pragma unroll
-  for (int e = 0; e < 9; ++e) A[e] = a.local[9 * (size_t)i + e];
-  double ldx[3] = {-lx[0], -lx[1], -lx[2]};
-  const double sc = a.scaling[i];
-  const bool ok = law_solve_local(a.desaxce != 0, a.strat, A, lb, lx, a.mu[i], sc);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) ldx[k] = ldx[k] + lx[k];
-  if (!ok) {
-    ldx[0] *= .5;
-    ldx[1] *= .5;
-    ldx[2] *= .5;
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) a.x[3 * i + k] = a.x[3 * i + k] + ldx[k];
-  const double s2 = sc * sc;
-  const double nx2 = s2 * sq3(lx);
-  const double ndx2 = s2 * sq3(ldx);
-  a.nx2[i] = nx2;
-  a.ndx2[i] = ndx2;
-  a.processed[i] = 1;
-  // ndxRef only grows through "if (ndx2 > ndxRef)": NaN never enters; non-negative doubles order as their bits
-  if (ndx2 > 0.0) {
-    const int ntiles = (a.n + kGSTile - 1) / kGSTile;
-    atomicMax(a.tile_max + parity * ntiles + i / kGSTile, dbits(ndx2));
   }
 }
 
-cudaError_t launch_gs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s) {
-  if (l1 <= l0) return cudaSuccess;
-  k_gs_level<<<l1 - l0, 32, 0, s>>>(a, l0, l1, parity);
+__global__ void __launch_bounds__(32 * kGSFlowWarps) k_gs_flow(GSArgs a, int parity) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ double sB[kGSFlowWarps][32][12];
+  __shared__ int sJ[kGSFlowWarps][32];
+  const unsigned tag = ld_acquire_u32(a.flow + 1);
+  const int ntiles = (a.n + kGSTile - 1) / kGSTile;
+  for (;;) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(a.flow, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= (unsigned)a.n) return;
+    const int i = a.order[t];
+    const unsigned char sk = a.skip[i];
+    __syncwarp();  // every lane has read the counter before lane 0 changes it: the branch below is warp-uniform
+    if (sk) {
+      if (lane == 0) {
+        a.skip[i] = (unsigned char)(sk - 1);
+        a.processed[i] = 0;
+        st_release_u32(a.done + i, tag);
+      }
+      continue;
+    }
+    double lx[3] = {ldcg(a.x + 3 * i), ldcg(a.x + 3 * i + 1), ldcg(a.x + 3 * i + 2)};
+    const double reg = a.reg[i];
+    double lb[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) lb[k] = a.b[3 * i + k] - reg * lx[k];
+    const int k0 = a.rowptr[i], k1 = a.rowptr[i + 1];
+    bool ok_wait = true;
+    for (int base = k0; base < k1; base += 32) {
+      const int k = base + lane;
+      if (k < k1) {
+        const int j = a.col[k];
+        if (j < i && !gs_wait_done(a.done + j, tag, a.status)) ok_wait = false;
+        sJ[w][lane] = j;
+        const double* B = a.val + 9 * (size_t)k;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) sB[w][lane][e] = B[e];
+        sB[w][lane][9] = ldcg(a.x + 3 * j);
+        sB[w][lane][10] = ldcg(a.x + 3 * j + 1);
+        sB[w][lane][11] = ldcg(a.x + 3 * j + 2);
+      }
+      if (!__all_sync(0xffffffffu, ok_wait)) return;
+      if (lane == 0) {
+        const int cnt = min(32, k1 - base);
+        for (int q = 0; q < cnt; ++q) {
+          if (sJ[w][q] == i) continue;
+          const double* B = sB[w][q];
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            double s = lb[r];
+            s = fma(B[3 * r + 0], B[9], s);
+            s = fma(B[3 * r + 1], B[10], s);
+            s = fma(B[3 * r + 2], B[11], s);
+            lb[r] = s;
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      double A[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) A[e] = a.local[9 * (size_t)i + e];
+      double ldx[3] = {-lx[0], -lx[1], -lx[2]};
+      const double sc = a.scaling[i];
+      const bool ok = law_solve_local(a.desaxce != 0, a.strat, A, lb, lx, a.mu[i], sc);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) ldx[k] = ldx[k] + lx[k];
+      if (!ok) {
+        ldx[0] *= .5;
+        ldx[1] *= .5;
+        ldx[2] *= .5;
+      }
+      double xn[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) xn[k] = ldcg(a.x + 3 * i + k) + ldx[k];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) a.x[3 * i + k] = xn[k];
+      const double s2 = sc * sc;
+      const double nx2 = s2 * sq3(lx);
+      const double ndx2 = s2 * sq3(ldx);
+      a.nx2[i] = nx2;
+      a.ndx2[i] = ndx2;
+      a.processed[i] = 1;
+      if (ndx2 > 0.0) atomicMax(a.tile_max + parity * ntiles + i / kGSTile, dbits(ndx2));
+      __threadfence();
+      st_release_u32(a.done + i, tag);
+    }
+    __syncwarp();
+  }
+}
+
+cudaError_t launch_gs_flow(const GSArgs& a, int grid, int parity, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  k_gs_flow<<<grid, 32 * kGSFlowWarps, 0, s>>>(a, parity);
   return cudaGetLastError();
+}
+
+int gs_flow_grid(int device) {
+  int sms = 0, per = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_gs_flow, 32 * kGSFlowWarps, 0) != cudaSuccess) return 0;
+  return per * sms;
 }
 
 // One CTA per tile of kGSTile contacts (sweep order). ndxRef entering the tile is the maximum of the
@@ -164,6 +206,11 @@ __global__ void __launch_bounds__(kGSTile) k_gs_skip(GSArgs a, int parity, doubl
     if (dmin(nx2, nd) < abs_skip_tol || nd < skip_tol * dmin(nx2, ref)) a.skip[i] = (unsigned char)abs_skip_iters;
   }
   if (threadIdx.x == 0) a.tile_max[(1 - parity) * ntiles + t] = 0ull;
+  // the next dataflow sweep hands out positions from 0 under a new tag
+  if (t == 0 && threadIdx.x == 0 && a.flow) {
+    a.flow[0] = 0u;
+    a.flow[1] = a.flow[1] + 1u;
+  }
 }
 
 cudaError_t launch_gs_skip(const GSArgs& a, int parity, double abs_skip_tol, double skip_tol, int abs_skip_iters,
@@ -175,76 +222,102 @@ cudaError_t launch_gs_skip(const GSArgs& a, int parity, double abs_skip_tol, dou
 }
 
 // ---- matrix-free sweep (ProductGaussSeidel<HType, MInvType, true>, ProductGaussSeidel.impl.hpp:108-296) -----
-// Same levels as the assembled sweep (contacts sharing a body never share a level), so in one level every body's
-// Mx = M^-1 H^T x is read and updated by at most one contact:
+// Levels from the shared bodies (contacts sharing a body never share a level); every body's Mx = M^-1 H^T x is
+// read and updated by one contact at a time, in sweep order:
 //   lb = b_i - local_i x_i + sum_t H_t Mx_(body t)  (rowMultiply), local solve, x_i += dx,
 //   Mx_(body t) += T_t dx  (colMultiply, T = M^-1 H^T).
 // Orders: local_i x_i per row with the dot3 chain, subtracted from b_i; each slot's H_t Mx row as a chain over the
 // dofs from 0, added to lb; T_t dx with the dot3 chain, added to Mx.
-__global__ void __launch_bounds__(32) k_pgs_level(GSArgs a, int l0, int l1, int parity) {
-  // one contact per warp (lane 0): contacts whose local solves branch differently never share a warp
-  const int t = l0 + blockIdx.x;
-  if (t >= l1 || threadIdx.x != 0) return;
-  const int i = a.order[t];
-  if (a.skip[i]) {
-    a.skip[i] = (unsigned char)(a.skip[i] - 1);
-    a.processed[i] = 0;
-    return;
-  }
+// Same dataflow schedule as k_gs_flow. Two contacts depend on each other when they share a body, and the
+// updates of Mx_b by the contacts on body b form a chain in sweep order, so contact i waits only for the
+// previous contact on each of its bodies (pdep, -1 when none): when that one is done, every earlier update of
+// Mx_b is in. A later contact on the body waits (directly or along the chain) for this one.
+__global__ void __launch_bounds__(32 * kGSFlowWarps) k_pgs_flow(GSArgs a, int parity) {
+  // one worker per warp (lane 0): contacts whose local solves branch differently never share a warp
+  if ((threadIdx.x & 31) != 0) return;
+  const unsigned tag = ld_acquire_u32(a.flow + 1);
+  const int ntiles = (a.n + kGSTile - 1) / kGSTile;
   const int d = a.d;
-  double lx[3] = {a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2]};
-  double A[9];
-#pragma unroll
-  for (int e = 0; e < 9; ++e) A[e] = a.local[9 * (size_t)i + e];
-  double lb[3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r) lb[r] = a.b[3 * i + r] - dot3(&A[3 * r], lx);
-  for (int sl = 0; sl < 2; ++sl) {
-    const int body = a.cb[2 * i + sl];
-    if (body < 0) continue;
-    const double* Hs = a.H + (2 * (size_t)i + sl) * 3 * d;
-    const double* mx = a.Mx + (size_t)body * d;
-    for (int r = 0; r < 3; ++r) {
-      double s = 0.0;
-      for (int m = 0; m < d; ++m) s = fma(Hs[r * d + m], mx[m], s);
-      lb[r] = lb[r] + s;
+  for (;;) {
+    const unsigned t = atomicAdd(a.flow, 1u);
+    if (t >= (unsigned)a.n) return;
+    const int i = a.order[t];
+    bool ok_wait = true;
+    for (int sl = 0; sl < 2; ++sl) {
+      const int j = a.pdep[2 * i + sl];
+      if (j >= 0 && !gs_wait_done(a.done + j, tag, a.status)) ok_wait = false;
     }
-  }
-  double ldx[3] = {-lx[0], -lx[1], -lx[2]};
-  const double sc = a.scaling[i];
-  const bool ok = law_solve_local(a.desaxce != 0, a.strat, A, lb, lx, a.mu[i], sc);
+    if (!ok_wait) return;
+    if (a.skip[i]) {
+      a.skip[i] = (unsigned char)(a.skip[i] - 1);
+      a.processed[i] = 0;
+      st_release_u32(a.done + i, tag);
+      continue;
+    }
+    double lx[3] = {ldcg(a.x + 3 * i), ldcg(a.x + 3 * i + 1), ldcg(a.x + 3 * i + 2)};
+    double A[9];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) ldx[k] = ldx[k] + lx[k];
-  if (!ok) {
-    ldx[0] *= .5;
-    ldx[1] *= .5;
-    ldx[2] *= .5;
-  }
+    for (int e = 0; e < 9; ++e) A[e] = a.local[9 * (size_t)i + e];
+    double lb[3];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) a.x[3 * i + k] = a.x[3 * i + k] + ldx[k];
-  for (int sl = 0; sl < 2; ++sl) {
-    const int body = a.cb[2 * i + sl];
-    if (body < 0) continue;
-    const double* Ts = a.T + (2 * (size_t)i + sl) * d * 3;
-    double* mx = a.Mx + (size_t)body * d;
-    for (int m = 0; m < d; ++m) mx[m] = mx[m] + fma(Ts[m * 3 + 2], ldx[2], fma(Ts[m * 3 + 1], ldx[1], Ts[m * 3] * ldx[0]));
-  }
-  const double s2 = sc * sc;
-  const double nx2 = s2 * sq3(lx);
-  const double ndx2 = s2 * sq3(ldx);
-  a.nx2[i] = nx2;
-  a.ndx2[i] = ndx2;
-  a.processed[i] = 1;
-  if (ndx2 > 0.0) {
-    const int ntiles = (a.n + kGSTile - 1) / kGSTile;
-    atomicMax(a.tile_max + parity * ntiles + i / kGSTile, dbits(ndx2));
+    for (int r = 0; r < 3; ++r) lb[r] = a.b[3 * i + r] - dot3(&A[3 * r], lx);
+    for (int sl = 0; sl < 2; ++sl) {
+      const int body = a.cb[2 * i + sl];
+      if (body < 0) continue;
+      const double* Hs = a.H + (2 * (size_t)i + sl) * 3 * d;
+      const double* mx = a.Mx + (size_t)body * d;
+      for (int r = 0; r < 3; ++r) {
+        double s = 0.0;
+        for (int m = 0; m < d; ++m) s = fma(Hs[r * d + m], ldcg(mx + m), s);
+        lb[r] = lb[r] + s;
+      }
+    }
+    double ldx[3] = {-lx[0], -lx[1], -lx[2]};
+    const double sc = a.scaling[i];
+    const bool ok = law_solve_local(a.desaxce != 0, a.strat, A, lb, lx, a.mu[i], sc);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) ldx[k] = ldx[k] + lx[k];
+    if (!ok) {
+      ldx[0] *= .5;
+      ldx[1] *= .5;
+      ldx[2] *= .5;
+    }
+    double xn[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) xn[k] = ldcg(a.x + 3 * i + k) + ldx[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) a.x[3 * i + k] = xn[k];
+    for (int sl = 0; sl < 2; ++sl) {
+      const int body = a.cb[2 * i + sl];
+      if (body < 0) continue;
+      const double* Ts = a.T + (2 * (size_t)i + sl) * d * 3;
+      double* mx = a.Mx + (size_t)body * d;
+      for (int m = 0; m < d; ++m)
+        mx[m] = ldcg(mx + m) + fma(Ts[m * 3 + 2], ldx[2], fma(Ts[m * 3 + 1], ldx[1], Ts[m * 3] * ldx[0]));
+    }
+    const double s2 = sc * sc;
+    const double nx2 = s2 * sq3(lx);
+    const double ndx2 = s2 * sq3(ldx);
+    a.nx2[i] = nx2;
+    a.ndx2[i] = ndx2;
+    a.processed[i] = 1;
+    if (ndx2 > 0.0) atomicMax(a.tile_max + parity * ntiles + i / kGSTile, dbits(ndx2));
+    __threadfence();
+    st_release_u32(a.done + i, tag);
   }
 }
 
-cudaError_t launch_pgs_level(const GSArgs& a, int l0, int l1, int parity, cudaStream_t s) {
-  if (l1 <= l0) return cudaSuccess;
-  k_pgs_level<<<l1 - l0, 32, 0, s>>>(a, l0, l1, parity);
+cudaError_t launch_pgs_flow(const GSArgs& a, int grid, int parity, cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  k_pgs_flow<<<grid, 32 * kGSFlowWarps, 0, s>>>(a, parity);
   return cudaGetLastError();
+}
+
+int pgs_flow_grid(int device) {
+  int sms = 0, per = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pgs_flow, 32 * kGSFlowWarps, 0) != cudaSuccess) return 0;
+  return per * sms;
 }
 
 // local_i = sum_t H_t T_t: W's diagonal block in the order of the assembly (slots in body order, dofs inner)
