@@ -125,6 +125,10 @@ struct bogus_gpu_problem {
   bool has_dual = false;
   bool host_lower_valid = false;
   HostBSR host_lower;  // lower triangle (for the coloring); kept when W came from host arrays or assembly
+  // lower triangle as uploaded by bogus_gpu_set_dual, copied to host_lower when first needed
+  bool low_pending = false;
+  DevBuf<int> low_rowptr, low_col, full_src;
+  DevBuf<double> low_val;
   std::vector<double> host_b, host_mu;
   // projected-gradient work
   DevBuf<double> X, MX, Y, S0, XB, Wv, csum, scal, trace;
@@ -239,6 +243,111 @@ int upload_full(bogus_gpu_problem* h, const HostBSR& f, const double* b, const d
   h->fp32p_valid = false;
   h->il_valid = false;
   h->adj_valid = false;
+  return BOGUS_GPU_OK;
+}
+
+int check_finite(const double* v, size_t m, const char* what);
+
+// bogus_gpu_set_dual from the lower triangle. The host checks the structure and computes the pattern of both
+// triangles (integers only); the values go to the device once, where they are checked for NaN / infinity and
+// expanded. The host copy of the lower triangle (coloring, Gauss-Seidel, adjoint) is downloaded when first
+// needed (ensure_host_lower).
+int set_dual_lower(bogus_gpu_problem* h, int n, const int* rowptr, const int* colidx, const double* blocks,
+                   const double* b, const double* mu) {
+  const std::string err = validate_bsr_structure(n, rowptr, colidx, true);
+  if (!err.empty()) return fail(BOGUS_GPU_BAD_INPUT, err);
+  if (int e = check_finite(b, 3 * (size_t)n, "b")) return e;
+  if (int e = check_finite(mu, n, "mu")) return e;
+  if (int e = set_device(h)) return e;
+  cudaStream_t s = h->stream;
+  const int nlow = n > 0 ? rowptr[n] : 0;
+  std::vector<int> frowptr, fcol, src;
+  expand_lower_pattern(n, rowptr, colidx, frowptr, fcol, src);
+  const int nnz = (int)fcol.size();
+  BG_CUDA(h->low_rowptr.ensure(n + 1));
+  BG_CUDA(h->low_col.ensure(nlow > 0 ? nlow : 1));
+  BG_CUDA(h->low_val.ensure(9 * (size_t)(nlow > 0 ? nlow : 1)));
+  BG_CUDA(h->full_src.ensure(nnz > 0 ? nnz : 1));
+  BG_CUDA(h->status.ensure(1));
+  BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
+  BG_CUDA(cudaMemcpyAsync(h->low_rowptr.p, rowptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+  if (nlow) {
+    BG_CUDA(cudaMemcpyAsync(h->low_col.p, colidx, sizeof(int) * nlow, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->low_val.p, blocks, sizeof(double) * 9 * (size_t)nlow, cudaMemcpyHostToDevice, s));
+  }
+  BG_CUDA(launch_any_nonfinite(9 * (size_t)nlow, h->low_val.p, h->status.p, s));
+  int bad = 0;
+  BG_CUDA(cudaMemcpyAsync(&bad, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  if (bad) {
+    // the uploaded lower triangle replaced the one a pending host copy would come from: no problem is left set
+    h->has_dual = false;
+    h->host_lower_valid = false;
+    h->low_pending = false;
+    h->gs.valid = false;
+    return fail(BOGUS_GPU_NONFINITE, "non-finite block value");
+  }
+  BG_CUDA(h->rowptr.ensure(n + 1));
+  BG_CUDA(h->col.ensure(nnz));
+  BG_CUDA(h->val.ensure(9 * (size_t)nnz));
+  BG_CUDA(h->diag.ensure(n));
+  BG_CUDA(h->b.ensure(3 * (size_t)n));
+  BG_CUDA(h->mu.ensure(n));
+  BG_CUDA(h->scaling.ensure(n));
+  BG_CUDA(cudaMemcpyAsync(h->rowptr.p, frowptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+  if (nnz) {
+    BG_CUDA(cudaMemcpyAsync(h->col.p, fcol.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->full_src.p, src.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+  }
+  BG_CUDA(launch_expand_lower(nnz, h->full_src.p, h->low_val.p, h->val.p, s));
+  if (n) {
+    BG_CUDA(cudaMemcpyAsync(h->b.p, b, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->mu.p, mu, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  }
+  h->W.n = n;
+  h->W.nnzb = nnz;
+  h->W.rowptr = h->rowptr.p;
+  h->W.col = h->col.p;
+  h->W.val = h->val.p;
+  h->W.diag = h->diag.p;
+  BG_CUDA(launch_diag_and_scaling(h->W, h->scaling.p, s));
+  h->host_b.assign(b, b + 3 * (size_t)n);
+  h->host_mu.assign(mu, mu + n);
+  BG_CUDA(cudaStreamSynchronize(s));
+  h->host_lower_valid = false;
+  h->low_pending = true;
+  h->host_lower.n = n;
+  h->has_dual = true;
+  h->gs.valid = false;
+  h->nproblems = 0;
+  h->fp32_valid = false;
+  h->fp32p_valid = false;
+  h->il_valid = false;
+  h->adj_valid = false;
+  return BOGUS_GPU_OK;
+}
+
+// The host copy of W's lower triangle, downloaded after bogus_gpu_set_dual at first use.
+int ensure_host_lower(bogus_gpu_problem* h) {
+  if (h->host_lower_valid) return BOGUS_GPU_OK;
+  if (!h->low_pending) return fail(BOGUS_GPU_NO_PROBLEM, "no host copy of W (set W from host arrays or by assembly)");
+  if (int e = set_device(h)) return e;
+  HostBSR& l = h->host_lower;
+  const int n = l.n;
+  cudaStream_t s = h->stream;
+  l.rowptr.resize(n + 1);
+  BG_CUDA(cudaMemcpyAsync(l.rowptr.data(), h->low_rowptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  const int nlow = l.rowptr[n];
+  l.col.resize(nlow);
+  l.val.resize(9 * (size_t)nlow);
+  if (nlow) {
+    BG_CUDA(cudaMemcpyAsync(l.col.data(), h->low_col.p, sizeof(int) * nlow, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaMemcpyAsync(l.val.data(), h->low_val.p, sizeof(double) * 9 * (size_t)nlow, cudaMemcpyDeviceToHost, s));
+  }
+  BG_CUDA(cudaStreamSynchronize(s));
+  h->host_lower_valid = true;
+  h->low_pending = false;
   return BOGUS_GPU_OK;
 }
 
@@ -538,7 +647,7 @@ int check_pg_options(const bogus_gpu_pg_options* o) {
 int prepare_gs(bogus_gpu_problem* h, double auto_reg, int use_coloring) {
   GSCache& g = h->gs;
   if (g.valid && g.auto_reg == auto_reg && g.use_coloring == use_coloring) return BOGUS_GPU_OK;
-  if (!h->host_lower_valid) return fail(BOGUS_GPU_BAD_INPUT, "Gauss-Seidel needs W set from host arrays");
+  if (int e = ensure_host_lower(h)) return e;
   g.drop_graphs();
   const HostBSR& low = h->host_lower;
   const int n = low.n;
@@ -819,19 +928,14 @@ int bogus_gpu_set_dual(bogus_gpu_problem* h, int n, const int* rowptr, const int
   if (int e = check_handle(h)) return e;
   if (n < 0 || (n > 0 && (!rowptr || !b || !mu))) return fail(BOGUS_GPU_BAD_INPUT, "null input array");
   if (n > 0 && rowptr[n] > 0 && (!colidx || !blocks)) return fail(BOGUS_GPU_BAD_INPUT, "null block arrays");
-  const std::string err = validate_bsr(n, rowptr, colidx, blocks, symmetric_lower != 0);
+  if (symmetric_lower) return set_dual_lower(h, n, rowptr, colidx, blocks, b, mu);
+  const std::string err = validate_bsr(n, rowptr, colidx, blocks, false);
   if (!err.empty()) return fail(err.find("non-finite") != std::string::npos ? BOGUS_GPU_NONFINITE : BOGUS_GPU_BAD_INPUT, err);
   if (int e = check_finite(b, 3 * (size_t)n, "b")) return e;
   if (int e = check_finite(mu, n, "mu")) return e;
   if (int e = set_device(h)) return e;
   HostBSR full;
-  if (symmetric_lower) {
-    full = expand_lower(n, rowptr, colidx, blocks);
-    h->host_lower.n = n;
-    h->host_lower.rowptr.assign(rowptr, rowptr + n + 1);
-    h->host_lower.col.assign(colidx, colidx + rowptr[n]);
-    h->host_lower.val.assign(blocks, blocks + 9 * (size_t)rowptr[n]);
-  } else {
+  {
     full.n = n;
     full.rowptr.assign(rowptr, rowptr + n + 1);
     full.col.assign(colidx, colidx + rowptr[n]);
@@ -839,6 +943,7 @@ int bogus_gpu_set_dual(bogus_gpu_problem* h, int n, const int* rowptr, const int
     h->host_lower = lower_of(full);
   }
   h->host_lower_valid = true;
+  h->low_pending = false;
   h->host_b.assign(b, b + 3 * (size_t)n);
   h->host_mu.assign(mu, mu + n);
   return upload_full(h, full, b, mu);
@@ -876,6 +981,7 @@ int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* 
   BG_CUDA(cudaStreamSynchronize(s));
   h->has_dual = true;
   h->host_lower_valid = false;
+  h->low_pending = false;
   h->gs.valid = false;
   h->nproblems = 0;
   h->fp32_valid = false;
@@ -988,7 +1094,7 @@ int bogus_gpu_solve_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, doub
 
 int bogus_gpu_coloring(bogus_gpu_problem* h, int* perm, int* colors, int* ncolors) {
   if (int e = check_handle(h)) return e;
-  if (!h->host_lower_valid) return fail(BOGUS_GPU_BAD_INPUT, "coloring needs W set from host arrays");
+  if (int e = ensure_host_lower(h)) return e;
   std::vector<int> p, c;
   greedy_coloring(h->host_lower, p, c);
   if (perm) std::memcpy(perm, p.data(), sizeof(int) * p.size());
@@ -2171,7 +2277,7 @@ int bogus_gpu_adjoint_device(bogus_gpu_problem* h, const bogus_gpu_adjoint_optio
 int bogus_gpu_adjoint_dual_lower(bogus_gpu_problem* h, double* dW) {
   if (int e = check_handle(h)) return e;
   if (!h->adj_valid) return fail(BOGUS_GPU_NO_PROBLEM, "no adjoint computed (bogus_gpu_adjoint)");
-  if (!h->host_lower_valid) return fail(BOGUS_GPU_NO_PROBLEM, "no host copy of W");
+  if (int e = ensure_host_lower(h)) return e;
   if (!dW) return fail(BOGUS_GPU_BAD_INPUT, "null output");
   const HostBSR& l = h->host_lower;
   const size_t n3 = 3 * (size_t)l.n;
@@ -2265,6 +2371,8 @@ int bogus_gpu_add_compliance(bogus_gpu_problem* h, const double* c) {
   DevBuf<double> dc;
   BG_CUDA(dc.ensure(n > 0 ? n : 1));
   if (n) BG_CUDA(cudaMemcpyAsync(dc.p, c, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  if (h->low_pending)  // the host copy of the lower triangle takes the same diagonal terms
+    if (int e = ensure_host_lower(h)) return e;
   BG_CUDA(launch_add_diagonal(h->W, dc.p, h->stream));
   BG_CUDA(launch_diag_and_scaling(h->W, h->scaling.p, h->stream));
   BG_CUDA(cudaStreamSynchronize(h->stream));
@@ -2700,6 +2808,7 @@ int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double*
   for (int k = 0; k < nlow; ++k) std::copy(&fullval[9 * (size_t)pos_ij[k]], &fullval[9 * (size_t)pos_ij[k]] + 9, &low.val[9 * (size_t)k]);
   h->host_lower = std::move(low);
   h->host_lower_valid = true;
+  h->low_pending = false;
   h->host_mu.assign(mu, mu + n);
   d_li.release(); d_lj.release(); d_off.release(); d_ti.release(); d_tj.release(); d_pij.release(); d_pji.release();
   d_w.release(); d_f.release();
@@ -2986,7 +3095,7 @@ int bogus_gpu_solve_pg_batch_device(bogus_gpu_problem* h, const bogus_gpu_pg_opt
 
 int bogus_gpu_get_dual_lower(bogus_gpu_problem* h, int* rowptr, int* colidx, double* blocks, int* nnzb_lower) {
   if (int e = check_handle(h)) return e;
-  if (!h->host_lower_valid) return fail(BOGUS_GPU_NO_PROBLEM, "no host copy of W");
+  if (int e = ensure_host_lower(h)) return e;
   const HostBSR& l = h->host_lower;
   if (nnzb_lower) *nnzb_lower = l.nnzb();
   if (rowptr) std::memcpy(rowptr, l.rowptr.data(), sizeof(int) * (l.n + 1));

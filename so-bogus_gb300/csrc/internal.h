@@ -94,6 +94,8 @@ cudaError_t launch_eval_chunks(int n, const double* x, const double* u, const do
 cudaError_t launch_combine(const double* chunk, int nchunks, bool is_max, double scale_div, double* out,
                            cudaStream_t s);
 cudaError_t launch_diag_and_scaling(const DevBSR& W, double* scaling, cudaStream_t s);
+cudaError_t launch_any_nonfinite(size_t m, const double* v, int* flag, cudaStream_t s);
+cudaError_t launch_expand_lower(int nnz, const int* src, const double* low, double* full, cudaStream_t s);
 cudaError_t launch_add(int m, const double* a, const double* b, double* y, cudaStream_t s);
 cudaError_t launch_cadoux_rhs(int n, const double* y, const double* mu, const double* b, double* out, cudaStream_t s);
 

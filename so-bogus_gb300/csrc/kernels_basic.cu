@@ -151,6 +151,47 @@ __global__ void k_diag_scaling(int n, const int* __restrict__ rowptr, const int*
   scaling[i] = s;
 }
 
+// *flag = 1 when some value is NaN or infinite (exponent field all ones).
+__global__ void k_any_nonfinite(size_t m, const double* __restrict__ v, int* flag) {
+  bool bad = false;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < m; k += (size_t)gridDim.x * blockDim.x)
+    bad |= ((__double_as_longlong(v[k]) >> 52) & 0x7ff) == 0x7ff;
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) *flag = 1;
+}
+
+cudaError_t launch_any_nonfinite(size_t m, const double* v, int* flag, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  const size_t blocks = (m + 255) / 256;
+  k_any_nonfinite<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(m, v, flag);
+  return cudaGetLastError();
+}
+
+// Both triangles from the lower one: block p is lower block src[p], or lower block ~src[p] transposed when
+// src[p] < 0 (the placement of the host's symmetric expansion: rows sorted by column).
+__global__ void k_expand_lower(int nnz, const int* __restrict__ src, const double* __restrict__ low,
+                               double* __restrict__ full) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nnz) return;
+  const int q = src[p];
+  const double* B = low + 9 * (size_t)(q >= 0 ? q : ~q);
+  double* F = full + 9 * (size_t)p;
+  if (q >= 0) {
+#pragma unroll
+    for (int e = 0; e < 9; ++e) F[e] = B[e];
+  } else {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) F[3 * r + c] = B[3 * c + r];
+  }
+}
+
+cudaError_t launch_expand_lower(int nnz, const int* src, const double* low, double* full, cudaStream_t s) {
+  if (nnz <= 0) return cudaSuccess;
+  k_expand_lower<<<(nnz + 255) / 256, 256, 0, s>>>(nnz, src, low, full);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_diag_and_scaling(const DevBSR& W, double* scaling, cudaStream_t s) {
   if (W.n == 0) return cudaSuccess;
   k_diag_scaling<<<(W.n + 255) / 256, 256, 0, s>>>(W.n, W.rowptr, W.col, W.val, W.diag, scaling);

@@ -321,6 +321,31 @@ def test_bad_inputs_raise(bg):
     pg.setLineSearchIterations(0)
     with pytest.raises(bg.BogusGpuError):
         D.solveWith(pg, np.zeros(3))
+    # a non-finite block is found on the device after the upload: the handle is left without a problem
+    blocks = np.eye(3).reshape(-1).copy()
+    blocks[4] = np.inf
+    with pytest.raises(bg.BogusGpuError) as e:
+        D.set([0, 1], [0], blocks, np.zeros(3), np.ones(1))
+    assert e.value.status == bg.NONFINITE
+    with pytest.raises(bg.BogusGpuError) as e:
+        D.solveWith(bg.ProjectedGradient(), np.zeros(3))
+    assert e.value.status == bg.NO_PROBLEM
+    D.set([0, 1], [0], np.eye(3).reshape(-1), np.array([-1.0, 0, 0]), np.ones(1))
+    r = np.zeros(3)
+    assert D.solveWith(bg.GaussSeidel(), r) < 1e-12 and np.allclose(r, [1.0, 0, 0])
+
+
+def test_lower_upload_expands_like_the_host(bg, oracle, c1):
+    """W from the lower triangle, expanded on the device: the same both-triangle matrix as the oracle's
+    expansion (products bit-identical), and the host copy of the lower triangle (downloaded at first use)
+    equal to what was uploaded."""
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    x = np.random.default_rng(2).standard_normal(3 * d.n)
+    assert np.array_equal(D.multiply(x), O.spmv(x))
+    rp2, cl2, vl2 = D.W_lower()
+    assert np.array_equal(rp2, rp) and np.array_equal(cl2, cl) and np.array_equal(vl2.reshape(-1), vl.reshape(-1))
 
 
 def test_repeatable(bg, c1):
