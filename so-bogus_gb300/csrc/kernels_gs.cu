@@ -48,10 +48,15 @@ __device__ __forceinline__ bool gs_wait_done(const unsigned* f, unsigned tag, co
   }
 }
 
+// The whole warp works on its contact: lanes stage the row's blocks (before waiting, they do not change) and the
+// neighbours' x (after); lanes 0-2 accumulate one component of the split row each (the three chains of the
+// scalar loop); every lane then runs the same local solve, whose eigenvalue step is shared across the lanes
+// (local_solve<true>), and lane 0 writes the result.
 __global__ void __launch_bounds__(32 * kGSFlowWarps) k_gs_flow(GSArgs a, int parity) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   __shared__ double sB[kGSFlowWarps][32][12];
   __shared__ int sJ[kGSFlowWarps][32];
+  __shared__ double sHq[kGSFlowWarps][16];
   const unsigned tag = ld_acquire_u32(a.flow + 1);
   const int ntiles = (a.n + kGSTile - 1) / kGSTile;
   for (;;) {
@@ -72,49 +77,48 @@ __global__ void __launch_bounds__(32 * kGSFlowWarps) k_gs_flow(GSArgs a, int par
     }
     double lx[3] = {ldcg(a.x + 3 * i), ldcg(a.x + 3 * i + 1), ldcg(a.x + 3 * i + 2)};
     const double reg = a.reg[i];
-    double lb[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) lb[k] = a.b[3 * i + k] - reg * lx[k];
+    const int rc = lane < 3 ? lane : 0;  // the component lanes 0-2 accumulate
+    double lbr = a.b[3 * i + rc] - reg * lx[rc];
     const int k0 = a.rowptr[i], k1 = a.rowptr[i + 1];
     bool ok_wait = true;
     for (int base = k0; base < k1; base += 32) {
       const int k = base + lane;
+      int j = i;
       if (k < k1) {
-        const int j = a.col[k];
-        if (j < i && !gs_wait_done(a.done + j, tag, a.status)) ok_wait = false;
+        j = a.col[k];
         sJ[w][lane] = j;
         const double* B = a.val + 9 * (size_t)k;
 #pragma unroll
         for (int e = 0; e < 9; ++e) sB[w][lane][e] = B[e];
+        if (j < i && !gs_wait_done(a.done + j, tag, a.status)) ok_wait = false;
         sB[w][lane][9] = ldcg(a.x + 3 * j);
         sB[w][lane][10] = ldcg(a.x + 3 * j + 1);
         sB[w][lane][11] = ldcg(a.x + 3 * j + 2);
       }
       if (!__all_sync(0xffffffffu, ok_wait)) return;
-      if (lane == 0) {
+      if (lane < 3) {
         const int cnt = min(32, k1 - base);
+        double s = lbr;
         for (int q = 0; q < cnt; ++q) {
           if (sJ[w][q] == i) continue;
           const double* B = sB[w][q];
-#pragma unroll
-          for (int r = 0; r < 3; ++r) {
-            double s = lb[r];
-            s = fma(B[3 * r + 0], B[9], s);
-            s = fma(B[3 * r + 1], B[10], s);
-            s = fma(B[3 * r + 2], B[11], s);
-            lb[r] = s;
-          }
+          s = fma(B[3 * rc + 0], B[9], s);
+          s = fma(B[3 * rc + 1], B[10], s);
+          s = fma(B[3 * rc + 2], B[11], s);
         }
+        lbr = s;
       }
       __syncwarp();
     }
-    if (lane == 0) {
-      double A[9];
+    const double lb[3] = {__shfl_sync(0xffffffffu, lbr, 0), __shfl_sync(0xffffffffu, lbr, 1),
+                          __shfl_sync(0xffffffffu, lbr, 2)};
+    double A[9];
 #pragma unroll
-      for (int e = 0; e < 9; ++e) A[e] = a.local[9 * (size_t)i + e];
-      double ldx[3] = {-lx[0], -lx[1], -lx[2]};
-      const double sc = a.scaling[i];
-      const bool ok = law_solve_local(a.desaxce != 0, a.strat, A, lb, lx, a.mu[i], sc);
+    for (int e = 0; e < 9; ++e) A[e] = a.local[9 * (size_t)i + e];
+    double ldx[3] = {-lx[0], -lx[1], -lx[2]};
+    const double sc = a.scaling[i];
+    const bool ok = law_solve_local<true>(a.desaxce != 0, a.strat, A, lb, lx, a.mu[i], sc, sHq[w]);
+    if (lane == 0) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) ldx[k] = ldx[k] + lx[k];
       if (!ok) {
@@ -233,48 +237,55 @@ cudaError_t launch_gs_skip(const GSArgs& a, int parity, double abs_skip_tol, dou
 // previous contact on each of its bodies (pdep, -1 when none): when that one is done, every earlier update of
 // Mx_b is in. A later contact on the body waits (directly or along the chain) for this one.
 __global__ void __launch_bounds__(32 * kGSFlowWarps) k_pgs_flow(GSArgs a, int parity) {
-  // one worker per warp (lane 0): contacts whose local solves branch differently never share a warp
-  if ((threadIdx.x & 31) != 0) return;
+  // the whole warp works on its contact, as in k_gs_flow: lanes 0-2 form one component of lb each, every lane
+  // runs the same local solve, lanes 0..d-1 update one dof of Mx each
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ double sHq[kGSFlowWarps][16];
   const unsigned tag = ld_acquire_u32(a.flow + 1);
   const int ntiles = (a.n + kGSTile - 1) / kGSTile;
   const int d = a.d;
   for (;;) {
-    const unsigned t = atomicAdd(a.flow, 1u);
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(a.flow, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= (unsigned)a.n) return;
     const int i = a.order[t];
     bool ok_wait = true;
-    for (int sl = 0; sl < 2; ++sl) {
-      const int j = a.pdep[2 * i + sl];
+    if (lane < 2) {
+      const int j = a.pdep[2 * i + lane];
       if (j >= 0 && !gs_wait_done(a.done + j, tag, a.status)) ok_wait = false;
     }
-    if (!ok_wait) return;
-    if (a.skip[i]) {
-      a.skip[i] = (unsigned char)(a.skip[i] - 1);
-      a.processed[i] = 0;
-      st_release_u32(a.done + i, tag);
+    if (!__all_sync(0xffffffffu, ok_wait)) return;
+    const unsigned char sk = a.skip[i];
+    __syncwarp();  // every lane has read the counter before lane 0 changes it: the branch below is warp-uniform
+    if (sk) {
+      if (lane == 0) {
+        a.skip[i] = (unsigned char)(sk - 1);
+        a.processed[i] = 0;
+        st_release_u32(a.done + i, tag);
+      }
       continue;
     }
     double lx[3] = {ldcg(a.x + 3 * i), ldcg(a.x + 3 * i + 1), ldcg(a.x + 3 * i + 2)};
     double A[9];
 #pragma unroll
     for (int e = 0; e < 9; ++e) A[e] = a.local[9 * (size_t)i + e];
-    double lb[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) lb[r] = a.b[3 * i + r] - dot3(&A[3 * r], lx);
+    const int rc = lane < 3 ? lane : 0;
+    double lbr = a.b[3 * i + rc] - dot3(&A[3 * rc], lx);
     for (int sl = 0; sl < 2; ++sl) {
       const int body = a.cb[2 * i + sl];
       if (body < 0) continue;
       const double* Hs = a.H + (2 * (size_t)i + sl) * 3 * d;
       const double* mx = a.Mx + (size_t)body * d;
-      for (int r = 0; r < 3; ++r) {
-        double s = 0.0;
-        for (int m = 0; m < d; ++m) s = fma(Hs[r * d + m], ldcg(mx + m), s);
-        lb[r] = lb[r] + s;
-      }
+      double s = 0.0;
+      for (int m = 0; m < d; ++m) s = fma(Hs[rc * d + m], ldcg(mx + m), s);
+      lbr = lbr + s;
     }
+    const double lb[3] = {__shfl_sync(0xffffffffu, lbr, 0), __shfl_sync(0xffffffffu, lbr, 1),
+                          __shfl_sync(0xffffffffu, lbr, 2)};
     double ldx[3] = {-lx[0], -lx[1], -lx[2]};
     const double sc = a.scaling[i];
-    const bool ok = law_solve_local(a.desaxce != 0, a.strat, A, lb, lx, a.mu[i], sc);
+    const bool ok = law_solve_local<true>(a.desaxce != 0, a.strat, A, lb, lx, a.mu[i], sc, sHq[w]);
 #pragma unroll
     for (int k = 0; k < 3; ++k) ldx[k] = ldx[k] + lx[k];
     if (!ok) {
@@ -282,28 +293,33 @@ __global__ void __launch_bounds__(32 * kGSFlowWarps) k_pgs_flow(GSArgs a, int pa
       ldx[1] *= .5;
       ldx[2] *= .5;
     }
-    double xn[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) xn[k] = ldcg(a.x + 3 * i + k) + ldx[k];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) a.x[3 * i + k] = xn[k];
     for (int sl = 0; sl < 2; ++sl) {
       const int body = a.cb[2 * i + sl];
-      if (body < 0) continue;
+      if (body < 0 || lane >= d) continue;
       const double* Ts = a.T + (2 * (size_t)i + sl) * d * 3;
       double* mx = a.Mx + (size_t)body * d;
-      for (int m = 0; m < d; ++m)
-        mx[m] = ldcg(mx + m) + fma(Ts[m * 3 + 2], ldx[2], fma(Ts[m * 3 + 1], ldx[1], Ts[m * 3] * ldx[0]));
+      const int m = lane;
+      mx[m] = ldcg(mx + m) + fma(Ts[m * 3 + 2], ldx[2], fma(Ts[m * 3 + 1], ldx[1], Ts[m * 3] * ldx[0]));
     }
-    const double s2 = sc * sc;
-    const double nx2 = s2 * sq3(lx);
-    const double ndx2 = s2 * sq3(ldx);
-    a.nx2[i] = nx2;
-    a.ndx2[i] = ndx2;
-    a.processed[i] = 1;
-    if (ndx2 > 0.0) atomicMax(a.tile_max + parity * ntiles + i / kGSTile, dbits(ndx2));
     __threadfence();
-    st_release_u32(a.done + i, tag);
+    __syncwarp();
+    if (lane == 0) {
+      double xn[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) xn[k] = ldcg(a.x + 3 * i + k) + ldx[k];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) a.x[3 * i + k] = xn[k];
+      const double s2 = sc * sc;
+      const double nx2 = s2 * sq3(lx);
+      const double ndx2 = s2 * sq3(ldx);
+      a.nx2[i] = nx2;
+      a.ndx2[i] = ndx2;
+      a.processed[i] = 1;
+      if (ndx2 > 0.0) atomicMax(a.tile_max + parity * ntiles + i / kGSTile, dbits(ndx2));
+      __threadfence();
+      st_release_u32(a.done + i, tag);
+    }
+    __syncwarp();
   }
 }
 

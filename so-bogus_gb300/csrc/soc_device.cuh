@@ -235,13 +235,216 @@ BG_HD int hessenberg_eigenvalues(double* a, int n, double* wr, double* wi) {
 #undef BG_A
 }
 
-BG_HD int real_roots_monic(const double* c, int dim, double* roots, int filter) {
+#ifdef __CUDACC__
+// hessenberg_eigenvalues run by a whole (converged) warp on a matrix in the warp's shared memory. Every lane
+// holds the same scalars and follows the same control flow; the independent operations of a step run on
+// different lanes of one instruction: the deflation tests of every row, the three (or five) divisions by the
+// scale (or by s and p), the three squares of the norm, one column of the row modification, one row of the
+// column modification. On GB300 an FP64 instruction occupies the sub-partition's FP64 unit for the same time
+// with one active lane or many, so a step costs a fraction of the scalar chain. Each value goes through the
+// same operations in the same order as in the scalar version, so the eigenvalues are identical.
+__device__ __forceinline__ double warp_bcast(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+__device__ inline int hessenberg_eigenvalues_warp(double* a, int n, double* wr, double* wi) {
+#define BG_A(i, j) a[(i) * n + (j)]
+  const int lane = threadIdx.x & 31;
+  double anorm = 0.0;
+  for (int i = 0; i < n; ++i)
+    for (int j = (i > 0 ? i - 1 : 0); j < n; ++j) anorm += fabs(BG_A(i, j));
+  int nn = n - 1;
+  double t = 0.0;
+  int total = 0;
+  while (nn >= 0) {
+    int its = 0, l;
+    for (;;) {
+      {  // lane c tests l = c + 1; the scalar search stops at the largest l that passes (0 when none does)
+        const int L = lane + 1;
+        bool pass = false;
+        if (L <= nn) {
+          double s = fabs(BG_A(L - 1, L - 1)) + fabs(BG_A(L, L));
+          if (s == 0.0) s = anorm;
+          pass = fabs(BG_A(L, L - 1)) + s == s;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, pass);
+        l = m ? 32 - __clz((int)m) : 0;
+        __syncwarp();
+        if (l >= 1 && lane == 0) BG_A(l, l - 1) = 0.0;
+        __syncwarp();
+      }
+      double x = BG_A(nn, nn);
+      if (l == nn) {
+        wr[nn] = x + t;
+        wi[nn] = 0.0;
+        --nn;
+        break;
+      }
+      double y = BG_A(nn - 1, nn - 1);
+      double w = BG_A(nn, nn - 1) * BG_A(nn - 1, nn);
+      if (l == nn - 1) {
+        const double p = 0.5 * (y - x);
+        const double q = p * p + w;
+        double z = sqrt(fabs(q));
+        x += t;
+        if (q >= 0.0) {
+          z = p + (p >= 0.0 ? fabs(z) : -fabs(z));
+          wr[nn - 1] = wr[nn] = x + z;
+          if (z != 0.0) wr[nn] = x - w / z;
+          wi[nn - 1] = wi[nn] = 0.0;
+        } else {
+          wr[nn - 1] = wr[nn] = x + p;
+          wi[nn - 1] = -z;
+          wi[nn] = z;
+        }
+        nn -= 2;
+        break;
+      }
+      if (its == 30 || total >= 40 * n) return -1;
+      if (its == 10 || its == 20) {
+        t += x;
+        __syncwarp();
+        if (lane <= nn) BG_A(lane, lane) -= x;
+        __syncwarp();
+        const double s = fabs(BG_A(nn, nn - 1)) + fabs(BG_A(nn - 1, nn - 2));
+        x = y = 0.75 * s;
+        w = -0.4375 * s * s;
+      }
+      ++its;
+      ++total;
+      int m;
+      double p = 0, q = 0, r = 0, z;
+      for (m = nn - 2; m >= l; --m) {
+        z = BG_A(m, m);
+        const double rr = x - z;
+        const double ss = y - z;
+        p = (rr * ss - w) / BG_A(m + 1, m) + BG_A(m, m + 1);
+        q = BG_A(m + 1, m + 1) - z - rr - ss;
+        r = BG_A(m + 2, m + 1);
+        const double sc = fabs(p) + fabs(q) + fabs(r);
+        {
+          const double v = (lane == 0 ? p : (lane == 1 ? q : r)) / sc;
+          p = warp_bcast(v, 0);
+          q = warp_bcast(v, 1);
+          r = warp_bcast(v, 2);
+        }
+        if (m == l) break;
+        const double u = fabs(BG_A(m, m - 1)) * (fabs(q) + fabs(r));
+        const double v = fabs(p) * (fabs(BG_A(m - 1, m - 1)) + fabs(z) + fabs(BG_A(m + 1, m + 1)));
+        if (u + v == v) break;
+      }
+      __syncwarp();
+      {
+        const int i = m + 2 + lane;
+        if (i <= nn) {
+          BG_A(i, i - 2) = 0.0;
+          if (i != m + 2) BG_A(i, i - 3) = 0.0;
+        }
+      }
+      __syncwarp();
+      for (int k = m; k <= nn - 1; ++k) {
+        if (k != m) {
+          p = BG_A(k, k - 1);
+          q = BG_A(k + 1, k - 1);
+          r = 0.0;
+          if (k != nn - 1) r = BG_A(k + 2, k - 1);
+          x = fabs(p) + fabs(q) + fabs(r);
+          if (x != 0.0) {
+            const double v = (lane == 0 ? p : (lane == 1 ? q : r)) / x;
+            p = warp_bcast(v, 0);
+            q = warp_bcast(v, 1);
+            r = warp_bcast(v, 2);
+          }
+        }
+        double nrm;
+        {  // sqrt(p * p + q * q + r * r), evaluated as (p*p + q*q) + r*r
+          const double c = lane == 0 ? p : (lane == 1 ? q : r);
+          const double sq = c * c;
+          nrm = sqrt((warp_bcast(sq, 0) + warp_bcast(sq, 1)) + warp_bcast(sq, 2));
+        }
+        const double s = (p >= 0.0 ? nrm : -nrm);
+        if (s != 0.0) {
+          __syncwarp();
+          if (lane == 0) {
+            if (k == m) {
+              if (l != m) BG_A(k, k - 1) = -BG_A(k, k - 1);
+            } else {
+              BG_A(k, k - 1) = -s * x;
+            }
+          }
+          p += s;
+          {  // x = p / s, y = q / s, z = r / s, q = q / p, r = r / p
+            const double num = lane == 0 ? p : (lane == 1 || lane == 3 ? q : r);
+            const double v = num / (lane < 3 ? s : p);
+            x = warp_bcast(v, 0);
+            y = warp_bcast(v, 1);
+            z = warp_bcast(v, 2);
+            q = warp_bcast(v, 3);
+            r = warp_bcast(v, 4);
+          }
+          __syncwarp();
+          {  // row modification, column j = k + lane
+            const int j = k + lane;
+            if (j <= nn) {
+              double pj = BG_A(k, j) + q * BG_A(k + 1, j);
+              if (k != nn - 1) {
+                pj += r * BG_A(k + 2, j);
+                BG_A(k + 2, j) -= pj * z;
+              }
+              BG_A(k + 1, j) -= pj * y;
+              BG_A(k, j) -= pj * x;
+            }
+          }
+          __syncwarp();
+          const int mmin = nn < k + 3 ? nn : k + 3;
+          {  // column modification, row i = l + lane
+            const int i = l + lane;
+            if (i <= mmin) {
+              double pi = x * BG_A(i, k) + y * BG_A(i, k + 1);
+              if (k != nn - 1) {
+                pi += z * BG_A(i, k + 2);
+                BG_A(i, k + 2) -= pi * r;
+              }
+              BG_A(i, k + 1) -= pi * q;
+              BG_A(i, k) -= pi;
+            }
+          }
+          __syncwarp();
+        }
+      }
+    }
+  }
+  return 0;
+#undef BG_A
+}
+#endif
+
+// Eigenvalues of the companion matrix of the monic polynomial c[0] + c[1] t + ... + t^dim. Warp: the whole
+// warp runs hessenberg_eigenvalues_warp on the matrix in sa (its shared memory, dim * dim doubles).
+template <bool Warp>
+BG_HD int companion_eigenvalues(const double* c, int dim, double* wr, double* wi, double* sa) {
+#ifdef __CUDA_ARCH__
+  if constexpr (Warp) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    for (int e = lane; e < dim * dim; e += 32) {
+      const int i = e / dim, j = e - (e / dim) * dim;
+      sa[e] = (j == dim - 1) ? -c[i] : (j == i - 1 ? 1.0 : 0.0);
+    }
+    __syncwarp();
+    return hessenberg_eigenvalues_warp(sa, dim, wr, wi);
+  }
+#endif
+  (void)sa;
   double a[16];
   for (int i = 0; i < dim * dim; ++i) a[i] = 0.0;
   for (int i = 1; i < dim; ++i) a[i * dim + (i - 1)] = 1.0;
   for (int i = 0; i < dim; ++i) a[i * dim + (dim - 1)] = -c[i];
+  return hessenberg_eigenvalues(a, dim, wr, wi);
+}
+
+template <bool Warp = false>
+BG_HD int real_roots_monic(const double* c, int dim, double* roots, int filter, double* sa = nullptr) {
   double wr[4], wi[4];
-  if (hessenberg_eigenvalues(a, dim, wr, wi) != 0) return 0;
+  if (companion_eigenvalues<Warp>(c, dim, wr, wi, sa) != 0) return 0;
   int count = 0;
   for (int i = 0; i < dim; ++i) {
     if (is_zero(wi[i])) {
@@ -252,7 +455,8 @@ BG_HD int real_roots_monic(const double* c, int dim, double* roots, int filter) 
   return count;
 }
 
-BG_HD int real_roots_degenerate(double* c, int dim, double* roots, int filter) {
+template <bool Warp = false>
+BG_HD int real_roots_degenerate(double* c, int dim, double* roots, int filter, double* sa = nullptr) {
   while (dim > 0 && is_zero(c[dim])) --dim;
   if (dim == 0) {
     roots[0] = 0.0;
@@ -260,7 +464,7 @@ BG_HD int real_roots_degenerate(double* c, int dim, double* roots, int filter) {
   }
   const double inv = 1.0 / c[dim];
   for (int k = 0; k < dim; ++k) c[k] *= inv;
-  return real_roots_monic(c, dim, roots, filter);
+  return real_roots_monic<Warp>(c, dim, roots, filter, sa);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -508,7 +712,8 @@ BG_HD double newton_solve(const LocalFB& f, double tol, double* x) {
   return Phi_best;
 }
 
-BG_HD bool analytic_coulomb(const double* W, const double* b, double* r, double mu) {
+template <bool Warp = false>
+BG_HD bool analytic_coulomb(const double* W, const double* b, double* r, double mu, double* sa = nullptr) {
   const double wN = W[0];
   if (wN < kEps) return false;
   const double wT0 = W[3], wT1 = W[6];
@@ -534,7 +739,7 @@ BG_HD bool analytic_coulomb(const double* W, const double* b, double* r, double 
   coeffs[2] = (2.0 * C + A * A) - D * dot2(bb0, bb1, bb0, bb1);
   coeffs[3] = 2.0 * A;
   double roots[4];
-  const int nRoots = real_roots_monic(coeffs, 4, roots, kStrictlyPositiveRoots);
+  const int nRoots = real_roots_monic<Warp>(coeffs, 4, roots, kStrictlyPositiveRoots, sa);
   if (nRoots == 0) return false;
   double alpha = roots[0];
   for (int i = 1; i < nRoots; ++i)
@@ -551,7 +756,8 @@ BG_HD bool analytic_coulomb(const double* W, const double* b, double* r, double 
   return true;
 }
 
-BG_HD bool analytic_soc(const double* W, const double* b, double* r, double mu) {
+template <bool Warp = false>
+BG_HD bool analytic_soc(const double* W, const double* b, double* r, double mu, double* sa = nullptr) {
 #define BG_W(i, j) W[3 * (i) + (j)]
   const double A = ((b[1] * BG_W(1, 2) - b[2] * BG_W(1, 1)) * mu * mu + b[0] * BG_W(0, 2)) - b[2] * BG_W(0, 0);
   const double B = ((b[0] * BG_W(1, 2) + b[1] * BG_W(0, 2)) - 2.0 * b[2] * BG_W(0, 1)) * mu;
@@ -560,7 +766,7 @@ BG_HD bool analytic_soc(const double* W, const double* b, double* r, double mu) 
   const double E = -6.0 * (b[0] * BG_W(1, 2) - b[1] * BG_W(0, 2)) * mu;
   double coeffs[5] = {A + B, C - D, E, C + D, B - A};
   double roots[4];
-  const int nRoots = real_roots_degenerate(coeffs, 4, roots, kAllRoots);
+  const int nRoots = real_roots_degenerate<Warp>(coeffs, 4, roots, kAllRoots, sa);
   for (int i = 0; i < nRoots; ++i) {
     const double t = roots[i];
     const double den = 1.0 + t * t;
@@ -594,8 +800,11 @@ BG_HD bool analytic_soc(const double* W, const double* b, double* r, double mu) 
 enum { kPureNewton = 0, kPureEnumerative = 1, kHybrid = 2, kRevHybrid = 3 };
 
 // LocalSOCSolver<3, double, DeSaxce, Strat>::solve (mu < 0: full-pivoting LU solve of A x = -b)
+// Warp: called by a whole converged warp with identical arguments (every lane computes the same values; the
+// companion-matrix eigenvalues use the warp's shared scratch sa, 16 doubles).
+template <bool Warp = false>
 BG_HD double local_solve(bool desaxce, int strat, const double* A, const double* b, double* x, double mu, double tol,
-                         double scaling) {
+                         double scaling, double* sa = nullptr) {
   if (mu < 0) {
     SmallLU<3> lu;
     lu.compute(A);
@@ -635,7 +844,7 @@ BG_HD double local_solve(bool desaxce, int strat, const double* A, const double*
     lu.solve(mb, x);
   }
   if (mu * x[0] >= norm2(x[1], x[2])) return 0.0;
-  const bool ok = desaxce ? analytic_coulomb(A, b, x, mu) : analytic_soc(A, b, x, mu);
+  const bool ok = desaxce ? analytic_coulomb<Warp>(A, b, x, mu, sa) : analytic_soc<Warp>(A, b, x, mu, sa);
   if (!ok) { x[0] = x0[0]; x[1] = x0[1]; x[2] = x0[2]; }
   if (strat == kRevHybrid) {
     res = newton_solve(fb, tol, x);
@@ -647,9 +856,10 @@ BG_HD double local_solve(bool desaxce, int strat, const double* A, const double*
   return res;
 }
 
+template <bool Warp = false>
 BG_HD bool law_solve_local(bool desaxce, int strat, const double* A, const double* b, double* x, double mu,
-                           double scaling) {
-  return kLocalTol > local_solve(desaxce, strat, A, b, x, mu, kLocalTol, scaling);
+                           double scaling, double* sa = nullptr) {
+  return kLocalTol > local_solve<Warp>(desaxce, strat, A, b, x, mu, kLocalTol, scaling, sa);
 }
 
 BG_HD double nesterov_inertia(double& theta, double q) {
