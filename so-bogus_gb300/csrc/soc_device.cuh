@@ -312,24 +312,38 @@ __device__ inline int hessenberg_eigenvalues_warp(double* a, int n, double* wr, 
       ++total;
       int m;
       double p = 0, q = 0, r = 0, z;
-      for (m = nn - 2; m >= l; --m) {
-        z = BG_A(m, m);
-        const double rr = x - z;
-        const double ss = y - z;
-        p = (rr * ss - w) / BG_A(m + 1, m) + BG_A(m, m + 1);
-        q = BG_A(m + 1, m + 1) - z - rr - ss;
-        r = BG_A(m + 2, m + 1);
-        const double sc = fabs(p) + fabs(q) + fabs(r);
-        {
-          const double v = (lane == 0 ? p : (lane == 1 ? q : r)) / sc;
-          p = warp_bcast(v, 0);
-          q = warp_bcast(v, 1);
-          r = warp_bcast(v, 2);
+      {
+        // The scalar search tries m = nn - 2, nn - 3, ..., l and stops at the first m that passes its test (m = l
+        // always does). Candidate values do not depend on one another: lane group g (lanes 3g..3g+2) evaluates
+        // m = nn - 2 - g, lane 3g + c normalising component c; the search's m is the first group that passes.
+        const int g = lane / 3, c = lane - 3 * g;
+        const bool valid = lane < 30 && nn - 2 - g >= l;
+        const int mc = valid ? nn - 2 - g : l;
+        const double zc = BG_A(mc, mc);
+        const double rr = x - zc;
+        const double ss = y - zc;
+        const double pc = (rr * ss - w) / BG_A(mc + 1, mc) + BG_A(mc, mc + 1);
+        const double qc = BG_A(mc + 1, mc + 1) - zc - rr - ss;
+        const double rc = BG_A(mc + 2, mc + 1);
+        const double sc = fabs(pc) + fabs(qc) + fabs(rc);
+        const double vn = (c == 0 ? pc : (c == 1 ? qc : rc)) / sc;
+        const int g0 = lane < 30 ? 3 * g : 0;
+        const double pn = __shfl_sync(0xffffffffu, vn, g0);
+        const double qn = __shfl_sync(0xffffffffu, vn, g0 + 1);
+        const double rn = __shfl_sync(0xffffffffu, vn, g0 + 2);
+        bool stop = valid && mc == l;
+        if (valid && mc != l) {
+          const double u = fabs(BG_A(mc, mc - 1)) * (fabs(qn) + fabs(rn));
+          const double v = fabs(pn) * (fabs(BG_A(mc - 1, mc - 1)) + fabs(zc) + fabs(BG_A(mc + 1, mc + 1)));
+          stop = u + v == v;
         }
-        if (m == l) break;
-        const double u = fabs(BG_A(m, m - 1)) * (fabs(q) + fabs(r));
-        const double v = fabs(p) * (fabs(BG_A(m - 1, m - 1)) + fabs(z) + fabs(BG_A(m + 1, m + 1)));
-        if (u + v == v) break;
+        const unsigned hit = __ballot_sync(0xffffffffu, stop && c == 0);
+        const int src = __ffs((int)hit) - 1;  // the leader lane of the first group that stops
+        m = nn - 2 - src / 3;
+        p = __shfl_sync(0xffffffffu, pn, src);
+        q = __shfl_sync(0xffffffffu, qn, src);
+        r = __shfl_sync(0xffffffffu, rn, src);
+        z = __shfl_sync(0xffffffffu, zc, src);
       }
       __syncwarp();
       {
