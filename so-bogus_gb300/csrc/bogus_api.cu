@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -125,10 +126,13 @@ struct bogus_gpu_problem {
   bool has_dual = false;
   bool host_lower_valid = false;
   HostBSR host_lower;  // lower triangle (for the coloring); kept when W came from host arrays or assembly
-  // lower triangle as uploaded by bogus_gpu_set_dual, copied to host_lower when first needed
+  // lower triangle as uploaded by bogus_gpu_set_dual (two sets: the next upload is checked in the other one),
+  // copied to host_lower when first needed; work of the device-side expansion
   bool low_pending = false;
-  DevBuf<int> low_rowptr, low_col, full_src;
-  DevBuf<double> low_val;
+  int low_cur = 0;
+  DevBuf<int> low_rowptr[2], low_col[2];
+  DevBuf<double> low_val[2];
+  DevBuf<int> full_src, pat_upper, pat_cursor, pat_check;
   std::vector<double> host_b, host_mu;
   // projected-gradient work
   DevBuf<double> X, MX, Y, S0, XB, Wv, csum, scal, trace;
@@ -248,58 +252,64 @@ int upload_full(bogus_gpu_problem* h, const HostBSR& f, const double* b, const d
 
 int check_finite(const double* v, size_t m, const char* what);
 
-// bogus_gpu_set_dual from the lower triangle. The host checks the structure and computes the pattern of both
-// triangles (integers only); the values go to the device once, where they are checked for NaN / infinity and
-// expanded. The host copy of the lower triangle (coloring, Gauss-Seidel, adjoint) is downloaded when first
-// needed (ensure_host_lower).
+// bogus_gpu_set_dual from the lower triangle. The host checks rowptr (n + 1 integers) and b, mu; the blocks
+// cross to the device once, into the staging set of the lower-triangle buffers, where their columns (range,
+// lower triangle, strictly increasing) and values (finite) are checked. On an error the handle keeps its
+// problem (the exact message comes from the host check of the structure). Then the device builds the pattern
+// of both triangles and expands the values. The host copy of the lower triangle (coloring, Gauss-Seidel,
+// adjoint) is downloaded when first needed (ensure_host_lower).
 int set_dual_lower(bogus_gpu_problem* h, int n, const int* rowptr, const int* colidx, const double* blocks,
                    const double* b, const double* mu) {
-  const std::string err = validate_bsr_structure(n, rowptr, colidx, true);
-  if (!err.empty()) return fail(BOGUS_GPU_BAD_INPUT, err);
+  if (rowptr[0] != 0) return fail(BOGUS_GPU_BAD_INPUT, "rowptr[0] must be 0");
+  for (int i = 0; i < n; ++i)
+    if (rowptr[i + 1] < rowptr[i]) return fail(BOGUS_GPU_BAD_INPUT, "rowptr not monotone at row " + std::to_string(i));
   if (int e = check_finite(b, 3 * (size_t)n, "b")) return e;
   if (int e = check_finite(mu, n, "mu")) return e;
   if (int e = set_device(h)) return e;
   cudaStream_t s = h->stream;
-  const int nlow = n > 0 ? rowptr[n] : 0;
-  std::vector<int> frowptr, fcol, src;
-  expand_lower_pattern(n, rowptr, colidx, frowptr, fcol, src);
-  const int nnz = (int)fcol.size();
-  BG_CUDA(h->low_rowptr.ensure(n + 1));
-  BG_CUDA(h->low_col.ensure(nlow > 0 ? nlow : 1));
-  BG_CUDA(h->low_val.ensure(9 * (size_t)(nlow > 0 ? nlow : 1)));
-  BG_CUDA(h->full_src.ensure(nnz > 0 ? nnz : 1));
+  const int nlow = rowptr[n];
+  const int nx = 1 - h->low_cur;
+  BG_CUDA(h->low_rowptr[nx].ensure(n + 1));
+  BG_CUDA(h->low_col[nx].ensure(nlow > 0 ? nlow : 1));
+  BG_CUDA(h->low_val[nx].ensure(9 * (size_t)(nlow > 0 ? nlow : 1)));
   BG_CUDA(h->status.ensure(1));
+  BG_CUDA(h->pat_check.ensure(2));
+  const int check0[2] = {INT_MAX, 0};
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
-  BG_CUDA(cudaMemcpyAsync(h->low_rowptr.p, rowptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(h->pat_check.p, check0, sizeof(check0), cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaMemcpyAsync(h->low_rowptr[nx].p, rowptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
   if (nlow) {
-    BG_CUDA(cudaMemcpyAsync(h->low_col.p, colidx, sizeof(int) * nlow, cudaMemcpyHostToDevice, s));
-    BG_CUDA(cudaMemcpyAsync(h->low_val.p, blocks, sizeof(double) * 9 * (size_t)nlow, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->low_col[nx].p, colidx, sizeof(int) * nlow, cudaMemcpyHostToDevice, s));
+    BG_CUDA(cudaMemcpyAsync(h->low_val[nx].p, blocks, sizeof(double) * 9 * (size_t)nlow, cudaMemcpyHostToDevice, s));
   }
-  BG_CUDA(launch_any_nonfinite(9 * (size_t)nlow, h->low_val.p, h->status.p, s));
-  int bad = 0;
+  BG_CUDA(launch_check_lower(n, h->low_rowptr[nx].p, h->low_col[nx].p, h->pat_check.p, s));
+  BG_CUDA(launch_any_nonfinite(9 * (size_t)nlow, h->low_val[nx].p, h->status.p, s));
+  int check[2] = {0, 0}, bad = 0;
+  BG_CUDA(cudaMemcpyAsync(check, h->pat_check.p, sizeof(check), cudaMemcpyDeviceToHost, s));
   BG_CUDA(cudaMemcpyAsync(&bad, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   BG_CUDA(cudaStreamSynchronize(s));
-  if (bad) {
-    // the uploaded lower triangle replaced the one a pending host copy would come from: no problem is left set
-    h->has_dual = false;
-    h->host_lower_valid = false;
-    h->low_pending = false;
-    h->gs.valid = false;
-    return fail(BOGUS_GPU_NONFINITE, "non-finite block value");
+  if (check[0] != INT_MAX) {
+    const std::string err = validate_bsr_structure(n, rowptr, colidx, true);
+    return fail(BOGUS_GPU_BAD_INPUT, err.empty() ? "invalid lower-triangle structure" : err);
   }
+  if (bad) return fail(BOGUS_GPU_NONFINITE, "non-finite block value");
+  // the staged upload becomes the problem
+  h->low_cur = nx;
+  const int nnz = 2 * nlow - check[1];
   BG_CUDA(h->rowptr.ensure(n + 1));
   BG_CUDA(h->col.ensure(nnz));
   BG_CUDA(h->val.ensure(9 * (size_t)nnz));
+  BG_CUDA(h->full_src.ensure(nnz > 0 ? nnz : 1));
+  BG_CUDA(h->pat_upper.ensure(n > 0 ? n : 1));
+  BG_CUDA(h->pat_cursor.ensure(n > 0 ? n : 1));
   BG_CUDA(h->diag.ensure(n));
   BG_CUDA(h->b.ensure(3 * (size_t)n));
   BG_CUDA(h->mu.ensure(n));
   BG_CUDA(h->scaling.ensure(n));
-  BG_CUDA(cudaMemcpyAsync(h->rowptr.p, frowptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
-  if (nnz) {
-    BG_CUDA(cudaMemcpyAsync(h->col.p, fcol.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
-    BG_CUDA(cudaMemcpyAsync(h->full_src.p, src.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
-  }
-  BG_CUDA(launch_expand_lower(nnz, h->full_src.p, h->low_val.p, h->val.p, s));
+  if (n == 0) BG_CUDA(cudaMemsetAsync(h->rowptr.p, 0, sizeof(int), s));
+  BG_CUDA(launch_full_pattern(n, h->low_rowptr[nx].p, h->low_col[nx].p, h->pat_upper.p, h->pat_cursor.p, h->rowptr.p,
+                              h->col.p, h->full_src.p, s));
+  BG_CUDA(launch_expand_lower(nnz, h->full_src.p, h->low_val[nx].p, h->val.p, s));
   if (n) {
     BG_CUDA(cudaMemcpyAsync(h->b.p, b, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, s));
     BG_CUDA(cudaMemcpyAsync(h->mu.p, mu, sizeof(double) * n, cudaMemcpyHostToDevice, s));
@@ -336,14 +346,15 @@ int ensure_host_lower(bogus_gpu_problem* h) {
   const int n = l.n;
   cudaStream_t s = h->stream;
   l.rowptr.resize(n + 1);
-  BG_CUDA(cudaMemcpyAsync(l.rowptr.data(), h->low_rowptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaMemcpyAsync(l.rowptr.data(), h->low_rowptr[h->low_cur].p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
   BG_CUDA(cudaStreamSynchronize(s));
   const int nlow = l.rowptr[n];
   l.col.resize(nlow);
   l.val.resize(9 * (size_t)nlow);
   if (nlow) {
-    BG_CUDA(cudaMemcpyAsync(l.col.data(), h->low_col.p, sizeof(int) * nlow, cudaMemcpyDeviceToHost, s));
-    BG_CUDA(cudaMemcpyAsync(l.val.data(), h->low_val.p, sizeof(double) * 9 * (size_t)nlow, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaMemcpyAsync(l.col.data(), h->low_col[h->low_cur].p, sizeof(int) * nlow, cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaMemcpyAsync(l.val.data(), h->low_val[h->low_cur].p, sizeof(double) * 9 * (size_t)nlow,
+                            cudaMemcpyDeviceToHost, s));
   }
   BG_CUDA(cudaStreamSynchronize(s));
   h->host_lower_valid = true;
@@ -928,6 +939,7 @@ int bogus_gpu_set_dual(bogus_gpu_problem* h, int n, const int* rowptr, const int
   if (int e = check_handle(h)) return e;
   if (n < 0 || (n > 0 && (!rowptr || !b || !mu))) return fail(BOGUS_GPU_BAD_INPUT, "null input array");
   if (n > 0 && rowptr[n] > 0 && (!colidx || !blocks)) return fail(BOGUS_GPU_BAD_INPUT, "null block arrays");
+  if (!rowptr) return fail(BOGUS_GPU_BAD_INPUT, "null row pointer");
   if (symmetric_lower) return set_dual_lower(h, n, rowptr, colidx, blocks, b, mu);
   const std::string err = validate_bsr(n, rowptr, colidx, blocks, false);
   if (!err.empty()) return fail(err.find("non-finite") != std::string::npos ? BOGUS_GPU_NONFINITE : BOGUS_GPU_BAD_INPUT, err);

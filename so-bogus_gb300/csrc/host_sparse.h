@@ -34,36 +34,6 @@ inline std::string validate_bsr_structure(int n, const int* rowptr, const int* c
   return std::string();
 }
 
-// Pattern of the both-triangle matrix of a (valid) lower triangle, the blocks placed as expand_lower places
-// them: src[p] = k when block p is lower block k, ~k (= -k - 1) when it is lower block k transposed.
-inline void expand_lower_pattern(int n, const int* rowptr, const int* col, std::vector<int>& frowptr,
-                                 std::vector<int>& fcol, std::vector<int>& src) {
-  std::vector<int> cnt(n + 1, 0);
-  for (int i = 0; i < n; ++i)
-    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
-      ++cnt[i + 1];
-      if (col[k] != i) ++cnt[col[k] + 1];
-    }
-  frowptr.assign(n + 1, 0);
-  for (int i = 0; i < n; ++i) frowptr[i + 1] = frowptr[i] + cnt[i + 1];
-  const int nnz = frowptr[n];
-  fcol.resize(nnz);
-  src.resize(nnz);
-  std::vector<int> pos(frowptr.begin(), frowptr.end() - 1);
-  for (int i = 0; i < n; ++i)
-    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
-      const int j = col[k];
-      int p = pos[i]++;
-      fcol[p] = j;
-      src[p] = k;
-      if (j != i) {
-        p = pos[j]++;
-        fcol[p] = i;
-        src[p] = ~k;
-      }
-    }
-}
-
 // Checks rowptr/col (monotone rows, sorted unique columns in range, lower triangle when asked) and finite
 // values; returns an empty string when valid.
 inline std::string validate_bsr(int n, const int* rowptr, const int* col, const double* val, bool lower) {

@@ -95,6 +95,9 @@ cudaError_t launch_combine(const double* chunk, int nchunks, bool is_max, double
                            cudaStream_t s);
 cudaError_t launch_diag_and_scaling(const DevBSR& W, double* scaling, cudaStream_t s);
 cudaError_t launch_any_nonfinite(size_t m, const double* v, int* flag, cudaStream_t s);
+cudaError_t launch_check_lower(int n, const int* rowptr, const int* col, int* out, cudaStream_t s);
+cudaError_t launch_full_pattern(int n, const int* rowptr, const int* col, int* upper, int* cursor, int* frowptr,
+                                int* fcol, int* src, cudaStream_t s);
 cudaError_t launch_expand_lower(int nnz, const int* src, const double* low, double* full, cudaStream_t s);
 cudaError_t launch_add(int m, const double* a, const double* b, double* y, cudaStream_t s);
 cudaError_t launch_cadoux_rhs(int n, const double* y, const double* mu, const double* b, double* out, cudaStream_t s);

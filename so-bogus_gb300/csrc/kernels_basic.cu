@@ -151,6 +151,117 @@ __global__ void k_diag_scaling(int n, const int* __restrict__ rowptr, const int*
   scaling[i] = s;
 }
 
+// ---- W from its lower triangle: structure checks and the pattern of both triangles on the device ----------
+// rowptr has been checked on the host (starts at 0, monotone), so every row's blocks lie in the uploaded col.
+// out[0] = the smallest row whose columns are out of range, above the diagonal or not strictly increasing
+// (unchanged when none is); out[1] += the number of diagonal blocks.
+__global__ void k_check_lower(int n, const int* __restrict__ rowptr, const int* __restrict__ col, int* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k0 = rowptr[i], k1 = rowptr[i + 1];
+  for (int k = k0; k < k1; ++k) {
+    const int j = col[k];
+    if (j < 0 || j > i || (k > k0 && col[k - 1] >= j)) {
+      atomicMin(out, i);
+      return;
+    }
+  }
+  if (k1 > k0 && col[k1 - 1] == i) atomicAdd(out + 1, 1);
+}
+
+// upper[j] = number of blocks (i, j), i > j, of the lower triangle (the transposed blocks row j receives)
+__global__ void k_count_upper(int n, const int* __restrict__ rowptr, const int* __restrict__ col, int* upper) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
+    if (col[k] != i) atomicAdd(upper + col[k], 1);
+}
+
+// frowptr = exclusive prefix sum of the full row lengths (lower length + upper[i]), one CTA of 1024 threads:
+// each thread sums a contiguous range, the range totals are scanned in shared memory, the ranges written.
+__global__ void __launch_bounds__(1024) k_full_rowptr(int n, const int* __restrict__ rowptr,
+                                                      const int* __restrict__ upper, int* frowptr) {
+  __shared__ int part[1024];
+  const int t = threadIdx.x;
+  const int per = (n + 1023) / 1024;
+  const int b = t * per, e = min(n, b + per);
+  int sum = 0;
+  for (int i = b; i < e; ++i) sum += (rowptr[i + 1] - rowptr[i]) + upper[i];
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int v = t >= off ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int run = part[t] - sum;  // exclusive prefix of this thread's range
+  for (int i = b; i < e; ++i) {
+    frowptr[i] = run;
+    run += (rowptr[i + 1] - rowptr[i]) + upper[i];
+  }
+  if (t == 1023) frowptr[n] = part[1023];
+}
+
+// Row i of the full matrix: its lower blocks (columns <= i, in order), then the transposed blocks (i, j) of
+// rows j > i in increasing j. The lower part is placed directly; the upper part by a cursor per row, then
+// sorted by column (rows of the upper part are short), so the layout is that of the host's expansion.
+__global__ void k_place_lower(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                              const int* __restrict__ frowptr, int* fcol, int* src, int* cursor) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k0 = rowptr[i], k1 = rowptr[i + 1];
+  for (int k = k0; k < k1; ++k) {
+    const int p = frowptr[i] + (k - k0);
+    fcol[p] = col[k];
+    src[p] = k;
+    const int j = col[k];
+    if (j != i) {
+      const int q = frowptr[j] + (rowptr[j + 1] - rowptr[j]) + atomicAdd(cursor + j, 1);
+      fcol[q] = i;
+      src[q] = ~k;
+    }
+  }
+}
+
+__global__ void k_sort_upper(int n, const int* __restrict__ rowptr, const int* __restrict__ frowptr, int* fcol,
+                             int* src) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int b = frowptr[j] + (rowptr[j + 1] - rowptr[j]), e = frowptr[j + 1];
+  for (int p = b + 1; p < e; ++p) {
+    const int c = fcol[p], s = src[p];
+    int q = p - 1;
+    while (q >= b && fcol[q] > c) {
+      fcol[q + 1] = fcol[q];
+      src[q + 1] = src[q];
+      --q;
+    }
+    fcol[q + 1] = c;
+    src[q + 1] = s;
+  }
+}
+
+cudaError_t launch_check_lower(int n, const int* rowptr, const int* col, int* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_check_lower<<<(n + 255) / 256, 256, 0, s>>>(n, rowptr, col, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_full_pattern(int n, const int* rowptr, const int* col, int* upper, int* cursor, int* frowptr,
+                                int* fcol, int* src, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(upper, 0, sizeof(int) * n, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(cursor, 0, sizeof(int) * n, s);
+  if (e != cudaSuccess) return e;
+  const int g = (n + 255) / 256;
+  k_count_upper<<<g, 256, 0, s>>>(n, rowptr, col, upper);
+  k_full_rowptr<<<1, 1024, 0, s>>>(n, rowptr, upper, frowptr);
+  k_place_lower<<<g, 256, 0, s>>>(n, rowptr, col, frowptr, fcol, src, cursor);
+  k_sort_upper<<<g, 256, 0, s>>>(n, rowptr, frowptr, fcol, src);
+  return cudaGetLastError();
+}
+
 // *flag = 1 when some value is NaN or infinite (exponent field all ones).
 __global__ void k_any_nonfinite(size_t m, const double* __restrict__ v, int* flag) {
   bool bad = false;

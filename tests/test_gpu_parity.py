@@ -321,18 +321,20 @@ def test_bad_inputs_raise(bg):
     pg.setLineSearchIterations(0)
     with pytest.raises(bg.BogusGpuError):
         D.solveWith(pg, np.zeros(3))
-    # a non-finite block is found on the device after the upload: the handle is left without a problem
+    # blocks are checked on the device after the upload, in a staging copy: a rejected W leaves the problem set
+    D.set([0, 1], [0], np.eye(3).reshape(-1), np.array([-1.0, 0, 0]), np.ones(1))
     blocks = np.eye(3).reshape(-1).copy()
     blocks[4] = np.inf
     with pytest.raises(bg.BogusGpuError) as e:
         D.set([0, 1], [0], blocks, np.zeros(3), np.ones(1))
     assert e.value.status == bg.NONFINITE
-    with pytest.raises(bg.BogusGpuError) as e:
-        D.solveWith(bg.ProjectedGradient(), np.zeros(3))
-    assert e.value.status == bg.NO_PROBLEM
-    D.set([0, 1], [0], np.eye(3).reshape(-1), np.array([-1.0, 0, 0]), np.ones(1))
+    with pytest.raises(bg.BogusGpuError) as e:  # columns not increasing in row 1
+        D.set([0, 1, 3], [0, 1, 0], np.tile(np.eye(3).reshape(-1), 3), np.zeros(6), np.ones(2))
+    assert e.value.status == bg.BAD_INPUT and "row 1" in str(e.value)
     r = np.zeros(3)
     assert D.solveWith(bg.GaussSeidel(), r) < 1e-12 and np.allclose(r, [1.0, 0, 0])
+    rp, cl, vl = D.W_lower()
+    assert list(rp) == [0, 1] and list(cl) == [0] and np.array_equal(vl.reshape(-1), np.eye(3).reshape(-1))
 
 
 def test_lower_upload_expands_like_the_host(bg, oracle, c1):
