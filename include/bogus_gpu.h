@@ -139,7 +139,8 @@ int bogus_gpu_destroy(bogus_gpu_problem* h);
 
 /* DualFrictionProblem<3> members W, b, mu (Interfaces/FrictionProblem.hpp:140-150), from host arrays.
  * symmetric_lower != 0: blocks hold the lower triangle incl. diagonal, rows sorted by column
- * (SparseBlockMatrix<Matrix3d RowMajor, SYMMETRIC>); 0: both triangles, rows sorted. */
+ * (SparseBlockMatrix<Matrix3d RowMajor, SYMMETRIC>); 0: both triangles, rows sorted. A malformed structure
+ * (BAD_INPUT) or a non-finite value (NONFINITE) is rejected and the handle keeps the problem it had. */
 int bogus_gpu_set_dual(bogus_gpu_problem* h, int n, const int* rowptr, const int* colidx, const double* blocks,
                        int symmetric_lower, const double* b, const double* mu);
 
