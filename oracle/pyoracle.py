@@ -347,7 +347,8 @@ class MecheProblem:
                                                                              for m in mass]),
                                            _f64(f).reshape(-1), n, _f64(mu), Ecm.ravel(), _f64(w).reshape(-1),
                                            _i32(objA), _i32(objB),
-                                           np.concatenate([np.asarray(h, np.float64).T.ravel() for h in HA]),
+                                           np.concatenate([np.zeros(0)] + [np.asarray(h, np.float64).T.ravel()
+                                                                           for h in HA]),
                                            np.concatenate([np.zeros(0)] + [np.asarray(h, np.float64).T.ravel()
                                                                            for h in HB if h is not None]))
         if not self.h:

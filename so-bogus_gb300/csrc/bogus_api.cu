@@ -2692,7 +2692,7 @@ int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_opti
 int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double* w, const double* mu) {
   if (int e = check_handle(h)) return e;
   if (h->ncontacts == 0 && h->nbodies == 0) return fail(BOGUS_GPU_NO_PROBLEM, "no primal problem set");
-  if (!w || !mu) return fail(BOGUS_GPU_BAD_INPUT, "null w or mu");
+  if (h->ncontacts > 0 && (!w || !mu)) return fail(BOGUS_GPU_BAD_INPUT, "null w or mu");
   if (int e = set_device(h)) return e;
   const int n = h->ncontacts, nb = h->nbodies, d = h->ndof;
   if (int e = check_finite(w, 3 * (size_t)n, "w")) return e;
