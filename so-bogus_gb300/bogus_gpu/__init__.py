@@ -276,7 +276,7 @@ class Coloring:
 class GaussSeidel(_SolverBase):
     """GaussSeidel<WType> (Core/BlockSolvers/GaussSeidel.hpp, GaussSeidelBase.hpp:39-91): tol 1e-6,
     250 sweeps, evalEvery 25, skipTol 1e-6, skipIters 10, tryZeroAsWell; the sequential sweep of the reference,
-    run level by level on the GPU."""
+    run on the GPU as one launch in which each contact waits only for its earlier neighbours (same result)."""
 
     def __init__(self):
         super().__init__(1e-6, 250)
