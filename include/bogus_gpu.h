@@ -148,6 +148,16 @@ int bogus_gpu_set_dual(bogus_gpu_problem* h, int n, const int* rowptr, const int
 int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* d_rowptr, const int* d_colidx,
                               const double* d_blocks, const double* d_b, const double* d_mu);
 
+/* DualFrictionProblem::applyPermutation / undoPermutation / permuted (Interfaces/FrictionProblem.hpp:198-207,
+ * FrictionProblem.cpp:102-125): contact k of the stored problem becomes contact perm[k] of the current one
+ * (W' = P W P^T, b' = P b, mu' = P mu). While permuted, bogus_gpu_solve_gs / _pg / _pg_device / _cadoux_* and
+ * bogus_gpu_eval take and return r in the caller's order (FrictionProblem.impl.hpp:38-91); bogus_gpu_spmv and
+ * bogus_gpu_get_dual_lower work on the stored (permuted) W, as W.multiply does. Batched solves and the adjoint
+ * need the contacts in their own order (BAD_INPUT while permuted). Setting a new problem clears the permutation. */
+int bogus_gpu_apply_permutation(bogus_gpu_problem* h, const int* perm);
+int bogus_gpu_undo_permutation(bogus_gpu_problem* h);
+int bogus_gpu_permuted(const bogus_gpu_problem* h, int* permuted);
+
 /* Number of stored blocks of the both-triangle W held on the device. */
 int bogus_gpu_nnzb(const bogus_gpu_problem* h, int* nnzb);
 

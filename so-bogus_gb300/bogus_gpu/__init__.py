@@ -103,7 +103,7 @@ EXPORTED = [
     "bogus_gpu_add_compliance", "bogus_gpu_solve_cadoux_gs", "bogus_gpu_solve_cadoux_pg",
     "bogus_gpu_meche_options_default", "bogus_gpu_meche_from_primal", "bogus_gpu_meche_solve",
     "bogus_gpu_solve_product_gs", "bogus_gpu_dual_ama_options_default", "bogus_gpu_solve_dual_ama",
-    "bogus_gpu_set_body_dofs",
+    "bogus_gpu_set_body_dofs", "bogus_gpu_apply_permutation", "bogus_gpu_undo_permutation", "bogus_gpu_permuted",
 ]
 
 
@@ -171,6 +171,9 @@ def lib():
     L.bogus_gpu_solve_dual_ama.argtypes = [vp, C.POINTER(DualAmaOptions), _dp, vp, _dp, _dp, C.c_int, _dp, _dp,
                                            C.POINTER(C.c_double), C.POINTER(C.c_uint)]
     L.bogus_gpu_set_body_dofs.argtypes = [vp, _ip]
+    L.bogus_gpu_apply_permutation.argtypes = [vp, _ip]
+    L.bogus_gpu_undo_permutation.argtypes = [vp]
+    L.bogus_gpu_permuted.argtypes = [vp, C.POINTER(C.c_int)]
     L.bogus_gpu_solve_pg_batch.argtypes = [vp, C.POINTER(PgOptions), _dp, _dp, np.ctypeslib.ndpointer(dtype=np.uint32)]
     L.bogus_gpu_solve_pg_batch_device.argtypes = [vp, C.POINTER(PgOptions), vp, _dp,
                                                   np.ctypeslib.ndpointer(dtype=np.uint32)]
@@ -547,8 +550,24 @@ class DualFrictionProblem:
         _check(lib().bogus_gpu_nnzb(self._h, C.byref(v)), False)
         return v.value
 
+    def applyPermutation(self, permutation) -> None:
+        """DualFrictionProblem::applyPermutation: contact k of the stored problem becomes contact permutation[k];
+        solveWith / evalWith keep taking r in the original order until undoPermutation()."""
+        p = _i32(permutation)
+        if p.size != self.n:
+            raise ValueError("the permutation must have one entry per contact")
+        _check(lib().bogus_gpu_apply_permutation(self._h, p), False)
+
+    def undoPermutation(self) -> None:
+        _check(lib().bogus_gpu_undo_permutation(self._h), False)
+
+    def permuted(self) -> bool:
+        out = C.c_int()
+        _check(lib().bogus_gpu_permuted(self._h, C.byref(out)), False)
+        return bool(out.value)
+
     def multiply(self, x) -> np.ndarray:
-        """y = W x."""
+        """y = W x (the stored W: permuted while a permutation is applied)."""
         x = _f64(x).reshape(-1)
         y = np.zeros_like(x)
         _check(lib().bogus_gpu_spmv(self._h, x, y), False)

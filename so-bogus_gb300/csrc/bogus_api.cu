@@ -130,6 +130,11 @@ struct bogus_gpu_problem {
   // copied to host_lower when first needed; work of the device-side expansion
   bool low_pending = false;
   int low_cur = 0;
+  // DualFrictionProblem::applyPermutation: contact k of the stored problem is contact perm[k] of the caller's
+  bool permuted = false;
+  std::vector<int> perm, inv_perm;
+  DevBuf<int> d_perm, d_inv_perm;
+  DevBuf<double> perm_r;
   DevBuf<int> low_rowptr[2], low_col[2];
   DevBuf<double> low_val[2];
   DevBuf<int> full_src, pat_upper, pat_cursor, pat_check;
@@ -934,9 +939,23 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   return BOGUS_GPU_OK;
 }
 
+static int set_dual_any(bogus_gpu_problem* h, int n, const int* rowptr, const int* colidx, const double* blocks,
+                        int symmetric_lower, const double* b, const double* mu);
+
 int bogus_gpu_set_dual(bogus_gpu_problem* h, int n, const int* rowptr, const int* colidx, const double* blocks,
                        int symmetric_lower, const double* b, const double* mu) {
   if (int e = check_handle(h)) return e;
+  const int st = set_dual_any(h, n, rowptr, colidx, blocks, symmetric_lower, b, mu);
+  if (st == BOGUS_GPU_OK) {
+    h->permuted = false;
+    h->perm.clear();
+    h->inv_perm.clear();
+  }
+  return st;
+}
+
+static int set_dual_any(bogus_gpu_problem* h, int n, const int* rowptr, const int* colidx, const double* blocks,
+                        int symmetric_lower, const double* b, const double* mu) {
   if (n < 0 || (n > 0 && (!rowptr || !b || !mu))) return fail(BOGUS_GPU_BAD_INPUT, "null input array");
   if (n > 0 && rowptr[n] > 0 && (!colidx || !blocks)) return fail(BOGUS_GPU_BAD_INPUT, "null block arrays");
   if (!rowptr) return fail(BOGUS_GPU_BAD_INPUT, "null row pointer");
@@ -992,6 +1011,7 @@ int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* 
   BG_CUDA(launch_diag_and_scaling(h->W, h->scaling.p, s));
   BG_CUDA(cudaStreamSynchronize(s));
   h->has_dual = true;
+  h->permuted = false;
   h->host_lower_valid = false;
   h->low_pending = false;
   h->gs.valid = false;
@@ -1031,7 +1051,7 @@ int bogus_gpu_spmv(bogus_gpu_problem* h, const double* x, double* y) {
   return BOGUS_GPU_OK;
 }
 
-int bogus_gpu_eval(bogus_gpu_problem* h, const double* r, int static_problem, int use_inf, double* residual) {
+static int eval_stored(bogus_gpu_problem* h, const double* r, int static_problem, int use_inf, double* residual) {
   if (int e = check_handle(h)) return e;
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
   if (int e = set_device(h)) return e;
@@ -1059,8 +1079,8 @@ int bogus_gpu_eval(bogus_gpu_problem* h, const double* r, int static_problem, in
   return BOGUS_GPU_OK;
 }
 
-int bogus_gpu_solve_pg_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* d_r, double* residual,
-                              unsigned* iters) {
+static int solve_pg_device_stored(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* d_r, double* residual,
+                                  unsigned* iters) {
   if (int e = check_handle(h)) return e;
   if (int e = check_pg_options(o)) return e;
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
@@ -1081,8 +1101,8 @@ int bogus_gpu_solve_pg_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* 
   return st;
 }
 
-int bogus_gpu_solve_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, double* residual,
-                       unsigned* iters) {
+static int solve_pg_stored(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, double* residual,
+                           unsigned* iters) {
   if (int e = check_handle(h)) return e;
   if (int e = check_pg_options(o)) return e;
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
@@ -1278,8 +1298,8 @@ int gs_store_x(bogus_gpu_problem* h, double* r) {
 
 extern "C" {
 
-int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* r, double* residual,
-                       unsigned* iters) {
+static int solve_gs_stored(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* r, double* residual,
+                           unsigned* iters) {
   if (int e = check_handle(h)) return e;
   if (int e = check_gs_options(o)) return e;
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
@@ -1578,8 +1598,8 @@ int bogus_gpu_solve_product_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options*
 
 // ---- Cadoux fixed point (Interfaces/Cadoux.hpp:44-91, DualFrictionProblem::solveCadoux,
 //      FrictionProblem.impl.hpp:76-92) -----------------------------------------------------------------
-int bogus_gpu_solve_cadoux_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* r, unsigned cadoux_iters,
-                              double* residual, unsigned* iters) {
+static int solve_cadoux_gs_stored(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* r, unsigned cadoux_iters,
+                                  double* residual, unsigned* iters) {
   if (int e = check_handle(h)) return e;
   if (int e = check_gs_options(o)) return e;
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
@@ -1638,8 +1658,8 @@ int bogus_gpu_solve_cadoux_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* 
   return res < tol ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
 }
 
-int bogus_gpu_solve_cadoux_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, unsigned cadoux_iters,
-                              double* residual, unsigned* iters) {
+static int solve_cadoux_pg_stored(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, unsigned cadoux_iters,
+                                  double* residual, unsigned* iters) {
   if (int e = check_handle(h)) return e;
   if (int e = check_pg_options(o)) return e;
   if (o->mixed_precision) return fail(BOGUS_GPU_BAD_INPUT, "the Cadoux fixed point runs its inner solves in FP64");
@@ -1853,6 +1873,7 @@ int bogus_gpu_meche_from_primal(bogus_gpu_problem* h, unsigned nobj, const unsig
   h->meche_mass = std::move(mpad);
   h->meche_mu.assign(mu, mu + n);
   h->meche_valid = true;
+  h->permuted = false;
   h->meche_dual = false;
   return BOGUS_GPU_OK;
 }
@@ -1968,8 +1989,8 @@ int bogus_gpu_meche_solve(bogus_gpu_problem* h, double* r, double* v, const bogu
       po.use_infinity_norm = o->use_infinity_norm;
       po.variant = o->pg_variant;
       po.static_problem = static_problem ? 1 : 0;
-      st = cadoux ? bogus_gpu_solve_cadoux_pg(h, &po, rl.data(), o->cadoux_iters, &res, nullptr)
-                  : bogus_gpu_solve_pg(h, &po, rl.data(), &res, nullptr);
+      st = cadoux ? solve_cadoux_pg_stored(h, &po, rl.data(), o->cadoux_iters, &res, nullptr)
+                  : solve_pg_stored(h, &po, rl.data(), &res, nullptr);
     } else {
       bogus_gpu_gs_options go;
       bogus_gpu_gs_options_default(&go);
@@ -1981,8 +2002,8 @@ int bogus_gpu_meche_solve(bogus_gpu_problem* h, double* r, double* v, const bogu
       go.use_coloring = (o->max_threads != 1 && o->gs_coloring) ? 1 : 0;
       go.static_problem = static_problem ? 1 : 0;
       go.try_zero_as_well = cadoux ? 0 : o->try_zero_as_well;
-      st = cadoux ? bogus_gpu_solve_cadoux_gs(h, &go, rl.data(), o->cadoux_iters, &res, nullptr)
-                  : bogus_gpu_solve_gs(h, &go, rl.data(), &res, nullptr);
+      st = cadoux ? solve_cadoux_gs_stored(h, &go, rl.data(), o->cadoux_iters, &res, nullptr)
+                  : solve_gs_stored(h, &go, rl.data(), &res, nullptr);
     }
     if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
     if (n > 0) {
@@ -2220,6 +2241,7 @@ int adjoint_checks(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o) {
   if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
   if (!(o->tol >= 0)) return fail(BOGUS_GPU_BAD_INPUT, "invalid tolerance");
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (h->permuted) return fail(BOGUS_GPU_BAD_INPUT, "the adjoint needs the contacts in their own order (undo the permutation)");
   return set_device(h);
 }
 
@@ -2821,6 +2843,7 @@ int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double*
   h->host_lower = std::move(low);
   h->host_lower_valid = true;
   h->low_pending = false;
+  h->permuted = false;
   h->host_mu.assign(mu, mu + n);
   d_li.release(); d_lj.release(); d_off.release(); d_ti.release(); d_tj.release(); d_pij.release(); d_pji.release();
   d_w.release(); d_f.release();
@@ -2836,6 +2859,7 @@ int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double*
 
 int bogus_gpu_set_batch(bogus_gpu_problem* h, int nproblems, const int* cptr) {
   if (int e = check_handle(h)) return e;
+  if (h->permuted) return fail(BOGUS_GPU_BAD_INPUT, "batched solves need the contacts in their own order (undo the permutation)");
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
   if (nproblems < 0 || (nproblems > 0 && !cptr)) return fail(BOGUS_GPU_BAD_INPUT, "invalid batch partition");
   const int n = h->W.n;
@@ -3139,6 +3163,137 @@ int bogus_gpu_measure_fp64_peak(int device, double* tflops) {
     return fail(BOGUS_GPU_NO_DEVICE, "no such CUDA device");
   BG_CUDA(measure_fp64_peak(device, tflops));
   return BOGUS_GPU_OK;
+}
+
+// ---- contact permutation (DualFrictionProblem::applyPermutation / undoPermutation, FrictionProblem.cpp:102-125)
+// The stored problem becomes W' = P W P^T, b' = P b, mu' = P mu with contact k of the stored problem being
+// contact perm[k] of the caller's (the layout of SparseBlockMatrixBase::applyPermutation: blocks moved above the
+// diagonal are stored transposed in the lower triangle). While permuted, the solves and the error evaluation
+// take and return r in the caller's order (FrictionProblem.impl.hpp:38-91).
+namespace {
+int permute_stored(bogus_gpu_problem* h, const std::vector<int>& p) {
+  if (int e = ensure_host_lower(h)) return e;
+  const int n = h->W.n;
+  const HostBSR plow = permute_lower(h->host_lower, p);
+  std::vector<double> pb(3 * (size_t)n), pmu(n);
+  for (int k = 0; k < n; ++k) {
+    for (int c = 0; c < 3; ++c) pb[3 * (size_t)k + c] = h->host_b[3 * (size_t)p[k] + c];
+    pmu[k] = h->host_mu[p[k]];
+  }
+  return set_dual_lower(h, n, plow.rowptr.data(), plow.col.data(), plow.val.data(), pb.data(), pmu.data());
+}
+
+// r (3 n, caller's order) <-> the stored order
+void to_stored(const bogus_gpu_problem* h, const double* r, double* out) {
+  const int n = h->W.n;
+  for (int k = 0; k < n; ++k)
+    for (int c = 0; c < 3; ++c) out[3 * (size_t)k + c] = r[3 * (size_t)h->perm[k] + c];
+}
+void from_stored(const bogus_gpu_problem* h, const double* in, double* r) {
+  const int n = h->W.n;
+  for (int k = 0; k < n; ++k)
+    for (int c = 0; c < 3; ++c) r[3 * (size_t)h->perm[k] + c] = in[3 * (size_t)k + c];
+}
+bool solved(int st) { return st == BOGUS_GPU_OK || st == BOGUS_GPU_NOT_CONVERGED; }
+}  // namespace
+
+int bogus_gpu_apply_permutation(bogus_gpu_problem* h, const int* perm) {
+  if (int e = check_handle(h)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  if (h->permuted) return fail(BOGUS_GPU_BAD_INPUT, "the problem is already permuted (undo the permutation first)");
+  const int n = h->W.n;
+  if (n > 0 && !perm) return fail(BOGUS_GPU_BAD_INPUT, "null permutation");
+  std::vector<int> p(perm, perm + n), inv(n, -1);
+  for (int k = 0; k < n; ++k) {
+    if (p[k] < 0 || p[k] >= n || inv[p[k]] >= 0) return fail(BOGUS_GPU_BAD_INPUT, "not a permutation of the contacts");
+    inv[p[k]] = k;
+  }
+  if (int e = permute_stored(h, p)) return e;
+  h->permuted = true;
+  h->perm = std::move(p);
+  h->inv_perm = std::move(inv);
+  BG_CUDA(h->d_perm.ensure(n > 0 ? n : 1));
+  if (n) BG_CUDA(cudaMemcpyAsync(h->d_perm.p, h->perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_undo_permutation(bogus_gpu_problem* h) {
+  if (int e = check_handle(h)) return e;
+  if (!h->permuted) return BOGUS_GPU_OK;
+  if (int e = permute_stored(h, h->inv_perm)) return e;
+  h->permuted = false;
+  h->perm.clear();
+  h->inv_perm.clear();
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_permuted(const bogus_gpu_problem* h, int* permuted) {
+  if (int e = check_handle(h)) return e;
+  if (!permuted) return fail(BOGUS_GPU_BAD_INPUT, "null output");
+  *permuted = h->permuted ? 1 : 0;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_eval(bogus_gpu_problem* h, const double* r, int static_problem, int use_inf, double* residual) {
+  if (!h || !h->permuted || !r) return eval_stored(h, r, static_problem, use_inf, residual);
+  std::vector<double> rs(3 * (size_t)h->W.n);
+  to_stored(h, r, rs.data());
+  return eval_stored(h, rs.data(), static_problem, use_inf, residual);
+}
+
+int bogus_gpu_solve_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, double* residual,
+                       unsigned* iters) {
+  if (!h || !h->permuted || !r) return solve_pg_stored(h, o, r, residual, iters);
+  std::vector<double> rs(3 * (size_t)h->W.n);
+  to_stored(h, r, rs.data());
+  const int st = solve_pg_stored(h, o, rs.data(), residual, iters);
+  if (solved(st)) from_stored(h, rs.data(), r);
+  return st;
+}
+
+int bogus_gpu_solve_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* r, double* residual,
+                       unsigned* iters) {
+  if (!h || !h->permuted || !r) return solve_gs_stored(h, o, r, residual, iters);
+  std::vector<double> rs(3 * (size_t)h->W.n);
+  to_stored(h, r, rs.data());
+  const int st = solve_gs_stored(h, o, rs.data(), residual, iters);
+  if (solved(st)) from_stored(h, rs.data(), r);
+  return st;
+}
+
+int bogus_gpu_solve_cadoux_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options* o, double* r, unsigned cadoux_iters,
+                              double* residual, unsigned* iters) {
+  if (!h || !h->permuted || !r) return solve_cadoux_gs_stored(h, o, r, cadoux_iters, residual, iters);
+  std::vector<double> rs(3 * (size_t)h->W.n);
+  to_stored(h, r, rs.data());
+  const int st = solve_cadoux_gs_stored(h, o, rs.data(), cadoux_iters, residual, iters);
+  if (solved(st)) from_stored(h, rs.data(), r);
+  return st;
+}
+
+int bogus_gpu_solve_cadoux_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, unsigned cadoux_iters,
+                              double* residual, unsigned* iters) {
+  if (!h || !h->permuted || !r) return solve_cadoux_pg_stored(h, o, r, cadoux_iters, residual, iters);
+  std::vector<double> rs(3 * (size_t)h->W.n);
+  to_stored(h, r, rs.data());
+  const int st = solve_cadoux_pg_stored(h, o, rs.data(), cadoux_iters, residual, iters);
+  if (solved(st)) from_stored(h, rs.data(), r);
+  return st;
+}
+
+int bogus_gpu_solve_pg_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* d_r, double* residual,
+                              unsigned* iters) {
+  if (!h || !h->permuted || !d_r) return solve_pg_device_stored(h, o, d_r, residual, iters);
+  const int n = h->W.n;
+  BG_CUDA(h->perm_r.ensure(3 * (size_t)(n > 0 ? n : 1)));
+  BG_CUDA(launch_permute3(n, h->d_perm.p, d_r, h->perm_r.p, false, h->stream));
+  const int st = solve_pg_device_stored(h, o, h->perm_r.p, residual, iters);
+  if (solved(st)) {
+    BG_CUDA(launch_permute3(n, h->d_perm.p, h->perm_r.p, d_r, true, h->stream));
+    BG_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  return st;
 }
 
 }  // extern "C"

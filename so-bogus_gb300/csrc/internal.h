@@ -95,6 +95,7 @@ cudaError_t launch_combine(const double* chunk, int nchunks, bool is_max, double
                            cudaStream_t s);
 cudaError_t launch_diag_and_scaling(const DevBSR& W, double* scaling, cudaStream_t s);
 cudaError_t launch_any_nonfinite(size_t m, const double* v, int* flag, cudaStream_t s);
+cudaError_t launch_permute3(int n, const int* perm, const double* src, double* dst, bool inverse, cudaStream_t s);
 cudaError_t launch_check_lower(int n, const int* rowptr, const int* col, int* out, cudaStream_t s);
 cudaError_t launch_full_pattern(int n, const int* rowptr, const int* col, int* upper, int* cursor, int* frowptr,
                                 int* fcol, int* src, cudaStream_t s);

@@ -262,6 +262,24 @@ cudaError_t launch_full_pattern(int n, const int* rowptr, const int* col, int* u
   return cudaGetLastError();
 }
 
+// 3-vectors between the caller's contact order and a permuted one: dst_k = src_perm[k] (or dst_perm[k] = src_k)
+__global__ void k_permute3(int n, const int* __restrict__ perm, const double* __restrict__ src, double* dst,
+                           int inverse) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int p = perm[k];
+  for (int c = 0; c < 3; ++c) {
+    if (inverse) dst[3 * (size_t)p + c] = src[3 * (size_t)k + c];
+    else dst[3 * (size_t)k + c] = src[3 * (size_t)p + c];
+  }
+}
+
+cudaError_t launch_permute3(int n, const int* perm, const double* src, double* dst, bool inverse, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_permute3<<<(n + 255) / 256, 256, 0, s>>>(n, perm, src, dst, inverse ? 1 : 0);
+  return cudaGetLastError();
+}
+
 // *flag = 1 when some value is NaN or infinite (exponent field all ones).
 __global__ void k_any_nonfinite(size_t m, const double* __restrict__ v, int* flag) {
   bool bad = false;
