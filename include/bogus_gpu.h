@@ -242,6 +242,13 @@ int bogus_gpu_set_primal(bogus_gpu_problem* h, int nbodies, int ndof, const doub
  * ConstrainedSolverBase.impl.hpp:84-118) and DualAMA's gap normalisation depend on it. Default: ndof each. */
 int bogus_gpu_set_body_dofs(bogus_gpu_problem* h, const int* ndof_k);
 
+/* PrimalFrictionProblem::E (Interfaces/FrictionProblem.hpp:62-63): per-contact frames, contact basis to world
+ * coordinates, n x 3 x 3 row-major (E_i[a][b]); NULL: identity (the default). With frames set, the w given to
+ * bogus_gpu_assemble_dual, _solve_admm, _solve_dual_ama and _solve_product_gs is in world coordinates and is
+ * taken to the contact basis as E^T w (PrimalFrictionProblem.cpp:44, 64, 82; FrictionProblem.cpp:35-36), each
+ * component the chain fma(E[2][a], w2, fma(E[1][a], w1, E[0][a] w0)). H is given in the contact basis. */
+int bogus_gpu_set_frames(bogus_gpu_problem* h, const double* E);
+
 /* DualFrictionProblem::computeFrom (Interfaces/FrictionProblem.cpp:30-40): W = H M^-1 H^T assembled on the
  * device and b = w - H M^-1 f (w in the local basis, E = I; f may be NULL for f = 0); mu copied. The result
  * replaces the handle's dual problem. */

@@ -64,6 +64,8 @@ def lib():
     L.oracle_meche_create.argtypes = [C.c_int, np.ctypeslib.ndpointer(dtype=np.uint32), _dp, _dp, C.c_int, _dp, _dp,
                                       _dp, _ip, _ip, _dp, _dp]
     L.oracle_meche_destroy.argtypes = [vp]
+    L.oracle_frame_t.restype = None
+    L.oracle_frame_t.argtypes = [C.c_int, _dp, _dp, _dp]
     L.oracle_meche_solve.restype = C.c_double
     L.oracle_meche_solve.argtypes = [vp, _dp, vp, C.c_int, C.c_uint, C.c_uint, C.c_double, C.c_int, C.c_int,
                                      C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
@@ -328,6 +330,15 @@ class PrimalProblem:
                                              int(inf_norm), None if td is None else td.ctypes.data_as(C.c_void_p),
                                              v, r, C.byref(it), cb, None)
         return res, v, r, it.value
+
+
+def frame_t(E, x):
+    """E^T x per contact (E: (n, 3, 3), x: 3n) with the facade's frame chain."""
+    E = _f64(E).reshape(-1)
+    x = _f64(x).reshape(-1)
+    y = np.zeros_like(x)
+    lib().oracle_frame_t(x.size // 3, E, x, y)
+    return y
 
 
 class MecheProblem:

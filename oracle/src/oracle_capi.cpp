@@ -258,6 +258,11 @@ void* oracle_meche_create(int nobj, const unsigned* ndof, const double* mass, co
 }
 void oracle_meche_destroy(void* h) { delete static_cast<Meche*>(h); }
 
+// y = E^T x per contact (E: n x 3 x 3 row-major), the frame chain of the facade (oracle_meche.hpp: frameT)
+void oracle_frame_t(int n, const double* E, const double* x, double* y) {
+  for (int i = 0; i < n; ++i) frameT(E + 9 * (size_t)i, x + 3 * (size_t)i, y + 3 * (size_t)i);
+}
+
 // MecheFrictionProblem::solve(r, v, options, staticProblem, problemRegularization) (:226-367); algorithm 0 GS,
 // 1 PG, 2 matrix-free GS, 3 ADMM, 4 DualAMA. v: unpadded (sum of ndof), may be null. Returns the solver's
 // residual.

@@ -103,7 +103,7 @@ EXPORTED = [
     "bogus_gpu_add_compliance", "bogus_gpu_solve_cadoux_gs", "bogus_gpu_solve_cadoux_pg",
     "bogus_gpu_meche_options_default", "bogus_gpu_meche_from_primal", "bogus_gpu_meche_solve",
     "bogus_gpu_solve_product_gs", "bogus_gpu_dual_ama_options_default", "bogus_gpu_solve_dual_ama",
-    "bogus_gpu_set_body_dofs", "bogus_gpu_apply_permutation", "bogus_gpu_undo_permutation", "bogus_gpu_permuted",
+    "bogus_gpu_set_body_dofs", "bogus_gpu_set_frames", "bogus_gpu_apply_permutation", "bogus_gpu_undo_permutation", "bogus_gpu_permuted",
 ]
 
 
@@ -171,6 +171,7 @@ def lib():
     L.bogus_gpu_solve_dual_ama.argtypes = [vp, C.POINTER(DualAmaOptions), _dp, vp, _dp, _dp, C.c_int, _dp, _dp,
                                            C.POINTER(C.c_double), C.POINTER(C.c_uint)]
     L.bogus_gpu_set_body_dofs.argtypes = [vp, _ip]
+    L.bogus_gpu_set_frames.argtypes = [vp, _dp]
     L.bogus_gpu_apply_permutation.argtypes = [vp, _ip]
     L.bogus_gpu_undo_permutation.argtypes = [vp]
     L.bogus_gpu_permuted.argtypes = [vp, C.POINTER(C.c_int)]
@@ -371,10 +372,12 @@ class PrimalFrictionProblem:
     per-contact Jacobian blocks for one or two bodies, f, w (local contact basis), mu. The arrays are uploaded
     to the GPU on the first solveWith; call invalidate() after changing them. M: the mass blocks (DualAMA needs
     them; computeMInv(M) sets both). body_dofs: the bodies' own dof counts when they are padded to ndof (the
-    reference's H has column blocks of varying width); default ndof each."""
+    reference's H has column blocks of varying width); default ndof each. E: per-contact frames (n, 3, 3),
+    contact basis to world; w is then in world coordinates (default: E = I, w in the contact basis)."""
 
-    def __init__(self, minv, objA, objB, HA, HB, w, mu, f=None, device: int = 0, M=None, body_dofs=None):
+    def __init__(self, minv, objA, objB, HA, HB, w, mu, f=None, device: int = 0, M=None, body_dofs=None, E=None):
         self.minv = _f64(minv)
+        self.E = None if E is None else _f64(E).reshape(-1, 3, 3)
         self.M = None if M is None else _f64(M)
         self.body_dofs = None if body_dofs is None else _i32(body_dofs)
         self.objA, self.objB = _i32(objA), _i32(objB)
@@ -396,6 +399,10 @@ class PrimalFrictionProblem:
                                               self.objB, self.HA.reshape(-1), self.HB.reshape(-1)), False)
             if self.body_dofs is not None:
                 _check(lib().bogus_gpu_set_body_dofs(g.handle, self.body_dofs), False)
+            if self.E is not None:
+                if self.E.shape[0] != self.objA.size:
+                    raise ValueError("E must hold one 3 x 3 frame per contact")
+                _check(lib().bogus_gpu_set_frames(g.handle, self.E.reshape(-1)), False)
             self._gpu = g
         return self._gpu
 
@@ -523,12 +530,14 @@ class DualFrictionProblem:
         self.n = n
 
     def computeFrom(self, primal: PrimalFrictionProblem) -> None:
-        """W = H M^-1 H^T and b = w - H M^-1 f on the GPU (DualFrictionProblem::computeFrom)."""
+        """W = H M^-1 H^T and b = E^T w - H M^-1 f on the GPU (DualFrictionProblem::computeFrom)."""
         L = lib()
         nb, ndof = primal.minv.shape[0], primal.minv.shape[1]
         n = primal.objA.size
         _check(L.bogus_gpu_set_primal(self._h, nb, ndof, primal.minv.reshape(-1), n, primal.objA, primal.objB,
                                       primal.HA.reshape(-1), primal.HB.reshape(-1)), False)
+        if primal.E is not None:
+            _check(L.bogus_gpu_set_frames(self._h, primal.E.reshape(-1)), False)
         fptr = None if primal.f is None else primal.f.ctypes.data_as(C.c_void_p)
         _check(L.bogus_gpu_assemble_dual(self._h, fptr, primal.w, primal.mu), False)
         self.n = n

@@ -176,6 +176,10 @@ struct bogus_gpu_problem {
   DevBuf<double> a_sc;
   long long true_dofs = 0;
   std::vector<int> body_dofs;  // the bodies' own dof counts (d each unless set otherwise)
+  // PrimalFrictionProblem::E: per-contact frames (local to world, row-major 3 x 3); w is given in world
+  // coordinates and taken to the local basis (E^T w) by the primal solves and the assembly
+  bool frames_valid = false;
+  DevBuf<double> frames;
   // DualAMA: mass blocks, affine part and work
   DevBuf<double> dm_M, dm_f, dm_v, dm_rs, dm_x, dm_hr, dm_g, dm_yp, dm_rb, dm_vb;
   DevBuf<DamaOut> dama_out;
@@ -1472,6 +1476,7 @@ int bogus_gpu_solve_product_gs(bogus_gpu_problem* h, const bogus_gpu_gs_options*
   DevBuf<double> dw, df;
   BG_CUDA(dw.ensure(n3));
   BG_CUDA(cudaMemcpyAsync(dw.p, w, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  if (h->frames_valid) BG_CUDA(launch_frame(n, h->frames.p, dw.p, dw.p, true, s));
   if (f) {
     BG_CUDA(df.ensure(m));
     BG_CUDA(cudaMemcpyAsync(df.p, f, sizeof(double) * m, cudaMemcpyHostToDevice, s));
@@ -1874,6 +1879,7 @@ int bogus_gpu_meche_from_primal(bogus_gpu_problem* h, unsigned nobj, const unsig
   h->meche_mu.assign(mu, mu + n);
   h->meche_valid = true;
   h->permuted = false;
+  h->frames_valid = false;
   h->meche_dual = false;
   return BOGUS_GPU_OK;
 }
@@ -2079,6 +2085,7 @@ int bogus_gpu_set_primal(bogus_gpu_problem* h, int nbodies, int ndof, const doub
   h->h_objA.assign(objA, objA + ncontacts);
   h->admm_incidence_valid = false;
   h->body_dofs.assign(nbodies, ndof);
+  h->frames_valid = false;
   h->meche_valid = false;
   h->meche_dual = false;
   return BOGUS_GPU_OK;
@@ -2092,6 +2099,23 @@ int bogus_gpu_set_body_dofs(bogus_gpu_problem* h, const int* ndof) {
     if (ndof[k] < 1 || ndof[k] > h->ndof) return fail(BOGUS_GPU_BAD_INPUT, "body dof count out of range");
   h->body_dofs.assign(ndof, ndof + h->nbodies);
   h->admm_incidence_valid = false;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_set_frames(bogus_gpu_problem* h, const double* E) {
+  if (int e = check_handle(h)) return e;
+  if (h->nbodies == 0) return fail(BOGUS_GPU_NO_PROBLEM, "no primal problem set (bogus_gpu_set_primal)");
+  const int n = h->ncontacts;
+  if (!E) {
+    h->frames_valid = false;
+    return BOGUS_GPU_OK;
+  }
+  if (int e = check_finite(E, 9 * (size_t)n, "E")) return e;
+  if (int e = set_device(h)) return e;
+  BG_CUDA(h->frames.ensure(9 * (size_t)(n > 0 ? n : 1)));
+  if (n) BG_CUDA(cudaMemcpyAsync(h->frames.p, E, sizeof(double) * 9 * n, cudaMemcpyHostToDevice, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  h->frames_valid = true;
   return BOGUS_GPU_OK;
 }
 
@@ -2477,6 +2501,7 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   BG_CUDA(h->status.ensure(1));
   if (n > 0) {
     BG_CUDA(cudaMemcpyAsync(h->a_w.p, w, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+    if (h->frames_valid) BG_CUDA(launch_frame(n, h->frames.p, h->a_w.p, h->a_w.p, true, s));
     BG_CUDA(cudaMemcpyAsync(h->a_mu.p, mu, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     BG_CUDA(cudaMemcpyAsync(h->a_r.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
   }
@@ -2614,6 +2639,7 @@ int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_opti
   BG_CUDA(h->status.ensure(1));
   if (n > 0) {
     BG_CUDA(cudaMemcpyAsync(h->a_w.p, w, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+    if (h->frames_valid) BG_CUDA(launch_frame(n, h->frames.p, h->a_w.p, h->a_w.p, true, s));
     BG_CUDA(cudaMemcpyAsync(h->a_mu.p, mu, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     BG_CUDA(cudaMemcpyAsync(h->a_r.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
     BG_CUDA(cudaMemcpyAsync(h->dm_rb.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
@@ -2813,6 +2839,7 @@ int bogus_gpu_assemble_dual(bogus_gpu_problem* h, const double* f, const double*
   DevBuf<double> d_w, d_f;
   BG_CUDA(d_w.ensure(3 * (size_t)n));
   BG_CUDA(up(d_w.p, w, sizeof(double) * 3 * n));
+  if (h->frames_valid) BG_CUDA(launch_frame(n, h->frames.p, d_w.p, d_w.p, true, s));
   if (f) {
     BG_CUDA(d_f.ensure((size_t)nb * d));
     BG_CUDA(up(d_f.p, f, sizeof(double) * nb * d));

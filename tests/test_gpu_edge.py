@@ -103,3 +103,42 @@ def test_meche_without_contacts(bg, oracle, algorithm):
     O = oracle.MecheProblem(**inp)
     res_o, r_o, v_o = O.solve(np.zeros(0), algorithm=algorithm)
     assert res == res_o and np.array_equal(v, v_o)
+
+
+def test_frames_rotate_w(bg, oracle):
+    """PrimalFrictionProblem::E: w in world coordinates, taken to the contact basis as E^T w by the assembly and
+    the primal solvers; the same as the problem posed with the rotated w."""
+    from bogus_gpu import generator
+
+    d = generator.make("c1")
+    rng = np.random.default_rng(31)
+    q, rr = np.linalg.qr(rng.standard_normal((d.n, 3, 3)))
+    E = q * np.sign(np.einsum("nii->ni", rr))[:, None, :]
+    w_world = rng.standard_normal(3 * d.n)
+    w_loc = oracle.frame_t(E, w_world)
+    f = rng.standard_normal(d.nbodies * 6) * 0.1
+    M = np.linalg.inv(d.minv)
+    PE = bg.PrimalFrictionProblem(d.minv, d.objA, d.objB, d.HA, d.HB, w_world, d.mu, f=f, M=M, E=E)
+    PL = bg.PrimalFrictionProblem(d.minv, d.objA, d.objB, d.HA, d.HB, w_loc, d.mu, f=f, M=M)
+    # assembly: b = E^T w - H M^-1 f
+    DE, DL = bg.DualFrictionProblem(), bg.DualFrictionProblem()
+    DE.computeFrom(PE)
+    DL.computeFrom(PL)
+    r = np.abs(rng.standard_normal(3 * d.n)) * 0.01
+    pg = bg.ProjectedGradient()
+    assert DE.evalWith(pg, r) == DL.evalWith(pg, r)
+    # primal solvers
+    for solver, args in ((bg.ADMM(), (0.0,)), (bg.DualAMA(), ()), (bg.ProductGaussSeidel(), ())):
+        solver.setMaxIters(40)
+        outs = []
+        for P in (PE, PL):
+            v, rr_ = np.zeros(d.nbodies * 6), np.zeros(3 * d.n)
+            if isinstance(solver, bg.ProductGaussSeidel):
+                res = P.solveWith(solver, rr_)
+            elif args:
+                res = P.solveWith(solver, *args, v, rr_)
+            else:
+                res = P.solveWith(solver, v, rr_)
+            outs.append((res, v, rr_))
+        assert outs[0][0] == outs[1][0] and np.array_equal(outs[0][2], outs[1][2])
+        assert np.array_equal(outs[0][1], outs[1][1])
