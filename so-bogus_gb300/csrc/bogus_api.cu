@@ -201,6 +201,9 @@ struct bogus_gpu_problem {
   std::vector<int> h_contact_ptr, h_problem_nnz;
   DevBuf<int> contact_ptr, chunk_ptr, queue, col_local, next;
   DevBuf<PGOut> batch_out;
+  DevBuf<unsigned> team_cnt;  // team schedule of the batched solve: counters, jobs, published scalars
+  DevBuf<int> team_job;
+  DevBuf<double> team_scal;
   bogus_gpu_callback callback = nullptr;
   void* callback_user = nullptr;
   float last_ms = 0.f;
@@ -2936,6 +2939,49 @@ int bogus_gpu_set_batch(bogus_gpu_problem* h, int nproblems, const int* cptr) {
 
 namespace {
 
+// Schedule of a batched solve: one CTA per problem (k_pg_batched) when there are at least as many problems as
+// half the resident CTAs, else teams of `size` CTAs per problem (k_pg_team), sized so that the teams fill the
+// GPU and each CTA's warps still have a chunk of the largest problem each. Launches the chosen kernel.
+int launch_batch_schedule(bogus_gpu_problem* h, const PGBatchArgs* ba64, const PGBatchArgs32* ba32) {
+  const bool fp32 = ba32 != nullptr;
+  const int np = h->nproblems;
+  cudaStream_t s = h->stream;
+  const int gmax = pg_team_grid(h->device, fp32);
+  if (gmax <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "occupancy query failed");
+  int maxchunks = 0;
+  for (int p = 0; p < np; ++p)
+    maxchunks = std::max(maxchunks, (h->h_contact_ptr[p + 1] - h->h_contact_ptr[p] + 31) / 32);
+  int size = np > 0 ? gmax / np : 0;
+  size = std::min(size, std::min(16, std::max(1, maxchunks / 8)));
+  if (size < 2) {
+    int grid = pg_batched_grid(h->device, fp32);
+    if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "occupancy query failed");
+    if (np < grid) grid = np > 0 ? np : 1;
+    BG_CUDA(cudaMemsetAsync(h->next.p, 0, sizeof(int), s));
+    BG_CUDA(cudaEventRecord(h->ev0, s));
+    BG_CUDA(fp32 ? launch_pg_batched(*ba32, grid, s) : launch_pg_batched(*ba64, grid, s));
+    BG_CUDA(cudaEventRecord(h->ev1, s));
+    return BOGUS_GPU_OK;
+  }
+  const int teams = std::min(np, gmax / size);
+  BG_CUDA(h->team_cnt.ensure(4 * (size_t)teams));
+  BG_CUDA(h->team_job.ensure(teams));
+  BG_CUDA(h->team_scal.ensure(8 * (size_t)teams));
+  BG_CUDA(h->status.ensure(1));
+  BG_CUDA(cudaMemsetAsync(h->team_cnt.p, 0, sizeof(unsigned) * 4 * teams, s));
+  BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
+  BG_CUDA(cudaMemsetAsync(h->next.p, 0, sizeof(int), s));
+  const PGTeamArgs ta{size, h->team_cnt.p, h->team_job.p, h->team_scal.p, h->status.p};
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  BG_CUDA(fp32 ? launch_pg_team(*ba32, ta, teams * size, s) : launch_pg_team(*ba64, ta, teams * size, s));
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  int st = 0;
+  BG_CUDA(cudaMemcpyAsync(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  if (st != 0) return fail(st, "device-side wait timed out in the batched solve");
+  return BOGUS_GPU_OK;
+}
+
 int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residuals, unsigned* iters) {
   const int n = h->W.n;
   const size_t n3 = 3 * (size_t)n;
@@ -2973,13 +3019,7 @@ int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   ba.queue = h->queue.p;
   ba.next = h->next.p;
   ba.r = h->X.p;  // each problem's best iterate is copied over its initial iterate
-  int grid = pg_batched_grid(h->device);
-  if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "occupancy query failed");
-  if (np < grid) grid = np > 0 ? np : 1;
-  BG_CUDA(cudaMemsetAsync(h->next.p, 0, sizeof(int), h->stream));
-  BG_CUDA(cudaEventRecord(h->ev0, h->stream));
-  BG_CUDA(launch_pg_batched(ba, grid, h->stream));
-  BG_CUDA(cudaEventRecord(h->ev1, h->stream));
+  if (int e = launch_batch_schedule(h, &ba, nullptr)) return e;
   std::vector<PGOut> out(np);
   if (np) BG_CUDA(cudaMemcpyAsync(out.data(), h->batch_out.p, sizeof(PGOut) * np, cudaMemcpyDeviceToHost, h->stream));
   BG_CUDA(cudaStreamSynchronize(h->stream));
@@ -3093,14 +3133,8 @@ int run_pg_batch_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, doub
   ba.queue = h->queue.p;
   ba.next = h->next.p;
   ba.r = h->X32.p;
-  int grid = pg_batched_grid(h->device, true);
-  if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "occupancy query failed");
-  if (np < grid) grid = np > 0 ? np : 1;
   BG_CUDA(launch_convert(n3, h->X.p, h->X32.p, s));
-  BG_CUDA(cudaMemsetAsync(h->next.p, 0, sizeof(int), s));
-  BG_CUDA(cudaEventRecord(h->ev0, s));
-  BG_CUDA(launch_pg_batched(ba, grid, s));
-  BG_CUDA(cudaEventRecord(h->ev1, s));
+  if (int e = launch_batch_schedule(h, nullptr, &ba)) return e;
   std::vector<PGOut> out32(np);
   if (np) BG_CUDA(cudaMemcpyAsync(out32.data(), h->batch_out.p, sizeof(PGOut) * np, cudaMemcpyDeviceToHost, s));
   BG_CUDA(launch_convert(n3, h->X32.p, h->X.p, s));

@@ -178,6 +178,7 @@ struct GridBarrier {
   unsigned* count;
   unsigned* gen;
   int* status;
+  unsigned parties;  // CTAs taking part (0: the whole grid)
 };
 
 template <class LastFn>
@@ -190,7 +191,7 @@ __device__ __forceinline__ bool grid_barrier(const GridBarrier& gb, LastFn&& las
     const unsigned my_gen = ld_acquire_u32(gb.gen);
     s_gen = my_gen;
     const unsigned prev = atom_add_acq_rel_u32(gb.count, 1u);
-    s_last = (prev == gridDim.x - 1) ? 1 : 0;
+    s_last = (prev == (gb.parties ? gb.parties : gridDim.x) - 1) ? 1 : 0;
     s_ok = 1;
     if (!s_last) {
       const unsigned long long t0 = global_timer_ns();

@@ -87,6 +87,20 @@ struct PGBatchArgsT {
 using PGBatchArgs = PGBatchArgsT<double>;
 using PGBatchArgs32 = PGBatchArgsT<float>;
 
+// Team schedule of the batched solve, for batches with fewer problems than resident CTAs: `size` CTAs of one
+// cooperative launch solve one problem at a time, with a barrier, ticket counters and published scalars per
+// team (the single-problem schedule on a slice of the GPU).
+struct PGTeamArgs {
+  int size;            // CTAs per team
+  unsigned* counters;  // 4 per team: barrier count, barrier generation, tickets of phase parity 0 and 1
+  int* job;            // 1 per team: the problem the team solves
+  double* scal;        // 8 per team: the scalars published by the team's last barrier
+  int* status;
+};
+cudaError_t launch_pg_team(const PGBatchArgs& b, const PGTeamArgs& t, int grid, cudaStream_t s);
+cudaError_t launch_pg_team(const PGBatchArgs32& b, const PGTeamArgs& t, int grid, cudaStream_t s);
+int pg_team_grid(int device, bool fp32);
+
 // Launchers (kernels_basic.cu)
 cudaError_t launch_spmv(const DevBSR& W, const double* x, const double* init, double* y, cudaStream_t s);
 cudaError_t launch_eval_chunks(int n, const double* x, const double* u, const double* mu, const double* scaling,

@@ -544,6 +544,121 @@ __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgsT<T> ba) {
   }
 }
 
+// Team schedule: CTAs [team * size, team * size + size) solve one problem at a time with the single-problem
+// context (dynamic chunk tickets, bounded barrier, scalars published by the team's last CTA), on counters of
+// their own. The last CTA to reach the barrier before a job takes the next problem from the queue. The
+// arithmetic is that of the other schedules, so each problem's result is the same bit for bit.
+template <class T>
+struct TeamCtx {
+  const PGArgsT<T>& a;
+  double* smem8;
+  ChunkScratchT<T>* cs;
+  unsigned* tickets;  // 2
+  double* sc;         // 8
+  GridBarrier gb;
+  int rank;
+  unsigned phase = 0;
+  __device__ int ticket() {
+    int c = 0;
+    if ((threadIdx.x & 31) == 0) c = (int)atomicAdd(tickets + (phase & 1u), 1u);
+    return __shfl_sync(0xffffffffu, c, 0);
+  }
+  __device__ int first_chunk() { return ticket(); }
+  __device__ int next_chunk(int) { return ticket(); }
+  __device__ bool writer() const { return rank == 0 && threadIdx.x == 0; }
+  __device__ void clear_tickets() {
+    if (threadIdx.x == 0) tickets[phase & 1u] = 0u;
+  }
+  __device__ bool sync() {
+    const bool ok = grid_barrier(gb, [&] { clear_tickets(); });
+    ++phase;
+    return ok;
+  }
+  __device__ bool sync_reduce(int K, unsigned maxmask) {
+    const bool ok = grid_barrier(gb, [&] {
+      block8_combine_k(a.csum, a.nchunks, K, maxmask, smem8, sc);
+      clear_tickets();
+    });
+    ++phase;
+    return ok;
+  }
+  __device__ double scal(int q) const { return ldcg(sc + q); }
+};
+
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_pg_team(PGBatchArgsT<T> ba, PGTeamArgs ta) {
+  __shared__ double smem8[32];
+  __shared__ ChunkScratchT<T> cs[8];
+  const int team = blockIdx.x / ta.size, rank = blockIdx.x - team * ta.size;
+  unsigned* cnt = ta.counters + 4 * (size_t)team;
+  const GridBarrier gb{cnt, cnt + 1, ta.status, (unsigned)ta.size};
+  for (;;) {
+    if (!grid_barrier(gb, [&] {
+          if (threadIdx.x == 0) ta.job[team] = (int)atomicAdd((unsigned*)ba.next, 1u);
+        }))
+      return;
+    const int job = *(volatile int*)(ta.job + team);
+    if (job >= ba.nproblems) return;
+    const int p = ba.queue[job];
+    const int c0 = ba.contact_ptr[p];
+    const int n = ba.contact_ptr[p + 1] - c0;
+    PGArgsT<T> a = ba.base;
+    a.n = n;
+    a.nchunks = (n + 31) / 32;
+    a.rowptr = ba.base.rowptr + c0;
+    a.b = ba.base.b + 3 * (size_t)c0;
+    a.mu = ba.base.mu + c0;
+    a.scaling = ba.base.scaling + c0;
+    a.X0 = ba.base.X0 + 3 * (size_t)c0;
+    a.X1 = ba.base.X1 + 3 * (size_t)c0;
+    a.X2 = ba.base.X2 + 3 * (size_t)c0;
+    a.MX0 = ba.base.MX0 + 3 * (size_t)c0;
+    a.MX1 = ba.base.MX1 + 3 * (size_t)c0;
+    a.Y = ba.base.Y + 3 * (size_t)c0;
+    a.S0 = ba.base.S0 + c0;
+    a.XB = ba.base.XB + 3 * (size_t)c0;
+    a.Wv = ba.base.Wv + 3 * (size_t)c0;
+    a.csum = ba.base.csum + 4 * (size_t)ba.chunk_ptr[p];
+    a.trace = nullptr;
+    a.out = ba.base.out + p;
+    TeamCtx<T> ctx{a, smem8, cs, cnt + 2, ta.scal + 8 * (size_t)team, gb, rank};
+    const int best = pg_body<T, false>(a, ctx);
+    if (best < 0) return;  // a wait ran out (status recorded)
+    if (n == 0) continue;
+    const T* src = best == 3 ? a.XB : (best == 4 ? a.Wv : (best == 0 ? a.X0 : (best == 1 ? a.X1 : a.X2)));
+    T* dst = ba.r + 3 * (size_t)c0;
+    for (int k = rank * (int)blockDim.x + (int)threadIdx.x; k < 3 * n; k += ta.size * (int)blockDim.x)
+      dst[k] = ldcg(src + k);
+  }
+}
+
+template <class T>
+cudaError_t launch_team_t(const PGBatchArgsT<T>& b, const PGTeamArgs& t, int grid, cudaStream_t s) {
+  PGBatchArgsT<T> bc = b;
+  PGTeamArgs tc = t;
+  void* args[] = {&bc, &tc};
+  return cudaLaunchCooperativeKernel((const void*)k_pg_team<T>, dim3(grid), dim3(256), args, 0, s);
+}
+
+cudaError_t launch_pg_team(const PGBatchArgs& b, const PGTeamArgs& t, int grid, cudaStream_t s) {
+  return launch_team_t(b, t, grid, s);
+}
+
+cudaError_t launch_pg_team(const PGBatchArgs32& b, const PGTeamArgs& t, int grid, cudaStream_t s) {
+  return launch_team_t(b, t, grid, s);
+}
+
+int pg_team_grid(int device, bool fp32) {
+  int sms = 0, per = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_team<float>, 256, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_team<double>, 256, 0);
+  if (e != cudaSuccess) return 0;
+  const int cap = fp32 ? 4 : 3;
+  if (per > cap) per = cap;
+  return per * sms;
+}
+
 cudaError_t launch_pg_batched(const PGBatchArgs& b, int grid, cudaStream_t s) {
   k_pg_batched<double><<<grid, 256, 0, s>>>(b);
   return cudaGetLastError();

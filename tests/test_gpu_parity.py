@@ -495,6 +495,42 @@ def test_batched_mixed_precision_matches_single_problem_solves(bg):
         assert np.array_equal(r[3 * c0:3 * c1], rs), p
 
 
+@pytest.mark.parametrize("variant, mixed", [(3, False), (4, False), (3, True)])
+def test_team_batch_matches_single_problem_solves(bg, oracle, variant, mixed):
+    """Few large problems: the batch runs several CTAs per problem (team schedule); each problem's result equals
+    its own single-problem solve (and, in FP64, the oracle's) bit for bit."""
+    from bogus_gpu import generator
+
+    d, cptr = generator.batch(nproblems=5, nmin=1500, nmax=3000, seed=13)
+    D = bg.DualFrictionProblem()
+    D.computeFrom(bg.PrimalFrictionProblem.from_generated(d))
+    D.setBatch(cptr)
+    pg = bg.ProjectedGradient()
+    pg.setDefaultVariant(variant)
+    pg.setTol(1e-8)
+    pg.setMaxIters(150)
+    if mixed:
+        pg.setMixedPrecision(True, 40)
+    r = np.zeros(3 * d.n)
+    res, its = D.solveBatchWith(pg, r, staticProblem=True)
+    rp, cl, vl = D.W_lower()
+    vl = vl.reshape(-1, 9)
+    single = bg.DualFrictionProblem()
+    for p in range(len(cptr) - 1):
+        c0, c1 = cptr[p], cptr[p + 1]
+        prp, pcl, pvl = rp[c0:c1 + 1] - rp[c0], cl[rp[c0]:rp[c1]] - c0, vl[rp[c0]:rp[c1]].reshape(-1)
+        single.set(prp, pcl, pvl, d.b[c0:c1], d.mu[c0:c1])
+        rs = np.zeros(3 * (c1 - c0))
+        res_s = single.solveWith(pg, rs)
+        assert res[p] == res_s and its[p] == single.last_iterations, p
+        assert np.array_equal(r[3 * c0:3 * c1], rs), p
+        if not mixed and p == 0:
+            O = oracle.DualProblem(prp, pcl, pvl, d.b[c0:c1], d.mu[c0:c1])
+            res_o, r_o, it_o = O.solve_pg(np.zeros(3 * (c1 - c0)), variant=variant, coulomb=False, tol=1e-8,
+                                          max_iters=150)
+            assert res[p] == res_o and its[p] == it_o and np.array_equal(rs, r_o)
+
+
 def test_batch_rejects_coupled_partition(bg):
     from bogus_gpu import generator
 
