@@ -395,30 +395,40 @@ __device__ inline int hessenberg_eigenvalues_warp(double* a, int n, double* wr, 
             r = warp_bcast(v, 4);
           }
           __syncwarp();
-          {  // row modification, column j = k + lane
-            const int j = k + lane;
-            if (j <= nn) {
-              double pj = BG_A(k, j) + q * BG_A(k + 1, j);
-              if (k != nn - 1) {
-                pj += r * BG_A(k + 2, j);
-                BG_A(k + 2, j) -= pj * z;
-              }
-              BG_A(k + 1, j) -= pj * y;
-              BG_A(k, j) -= pj * x;
+          // Row and column modifications: lane 4u + c takes column (row) c of the step and, once every lane has
+          // read the old values, applies the u-th of its three independent updates; the updates are selected
+          // without branching, so the three run as one instruction stream (x 1.0 is exact: a - p * 1.0 = a - p).
+          const int c4 = lane & 3, u4 = lane >> 2;
+          {  // row modification, column j = k + c4
+            const int j = k + c4;
+            const bool on = lane < 12 && j <= nn;
+            double pj = 0.0;
+            if (on) {
+              pj = BG_A(k, j) + q * BG_A(k + 1, j);
+              if (k != nn - 1) pj += r * BG_A(k + 2, j);
+            }
+            __syncwarp();
+            if (on && (u4 != 0 || k != nn - 1)) {
+              const int row = k + 2 - u4;
+              const double f = u4 == 0 ? z : (u4 == 1 ? y : x);
+              BG_A(row, j) -= pj * f;
             }
           }
           __syncwarp();
           const int mmin = nn < k + 3 ? nn : k + 3;
-          {  // column modification, row i = l + lane
-            const int i = l + lane;
-            if (i <= mmin) {
-              double pi = x * BG_A(i, k) + y * BG_A(i, k + 1);
-              if (k != nn - 1) {
-                pi += z * BG_A(i, k + 2);
-                BG_A(i, k + 2) -= pi * r;
-              }
-              BG_A(i, k + 1) -= pi * q;
-              BG_A(i, k) -= pi;
+          {  // column modification, row i = l + c4
+            const int i = l + c4;
+            const bool on = lane < 12 && i <= mmin;
+            double pi = 0.0;
+            if (on) {
+              pi = x * BG_A(i, k) + y * BG_A(i, k + 1);
+              if (k != nn - 1) pi += z * BG_A(i, k + 2);
+            }
+            __syncwarp();
+            if (on && (u4 != 0 || k != nn - 1)) {
+              const int col = k + 2 - u4;
+              const double f = u4 == 0 ? r : (u4 == 1 ? q : 1.0);
+              BG_A(i, col) -= pi * f;
             }
           }
           __syncwarp();
