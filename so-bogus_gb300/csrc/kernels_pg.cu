@@ -467,9 +467,9 @@ struct GridCtx {
   __device__ double scal(int q) const { return ldcg(a.scal + q); }
 };
 
-// Occupancy targets: 3 resident CTAs per SM for FP64, 4 for FP32 (see pg_max_grid).
+// Occupancy target: 3 resident CTAs per SM (see pg_max_grid).
 template <class T, bool IL>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_pg_persistent(PGArgsT<T> a) {
+__global__ void __launch_bounds__(256, 3) k_pg_persistent(PGArgsT<T> a) {
   __shared__ double smem8[32];
   __shared__ ChunkScratchT<T> cs[8];
   GridCtx<T> ctx{a, smem8, cs};
@@ -586,7 +586,7 @@ struct TeamCtx {
 };
 
 template <class T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_pg_team(PGBatchArgsT<T> ba, PGTeamArgs ta) {
+__global__ void __launch_bounds__(256, 3) k_pg_team(PGBatchArgsT<T> ba, PGTeamArgs ta) {
   __shared__ double smem8[32];
   __shared__ ChunkScratchT<T> cs[8];
   const int team = blockIdx.x / ta.size, rank = blockIdx.x - team * ta.size;
@@ -654,7 +654,7 @@ int pg_team_grid(int device, bool fp32) {
   const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_team<float>, 256, 0)
                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_team<double>, 256, 0);
   if (e != cudaSuccess) return 0;
-  const int cap = fp32 ? 4 : 3;
+  const int cap = 3;
   if (per > cap) per = cap;
   return per * sms;
 }
@@ -701,9 +701,10 @@ int pg_max_grid(int device, bool fp32, bool interleaved) {
   const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
   if (e != cudaSuccess) return 0;
   // Measured on the 200 000-contact problem: 3 resident CTAs per SM for FP64 (0.388 ms per APGD iteration
-  // against 0.411 with 2 and 0.502 with 1) and 4 for FP32 at 64 registers (0.132 ms against 0.141 with 5 at
-  // 48 registers and 0.232 with 2); more warps hide the gather latency of the products.
-  const int cap = fp32 ? 4 : 3;
+  // against 0.411 with 2 and 0.502 with 1). FP32: 3 CTAs at 80 registers with the block values and x loaded
+  // two blocks ahead, 0.120 ms per iteration, against 0.126 at 4 CTAs (64 registers, one block ahead), 0.137
+  // at 4 CTAs with only x ahead, 0.141 with 5 at 48 registers and 0.232 with 2.
+  const int cap = 3;
   if (per > cap) per = cap;
   return per * sms;
 }

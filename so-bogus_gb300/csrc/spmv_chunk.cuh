@@ -94,28 +94,35 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, Src s
   bool open = false;
   // The next block's column index and gathered x are loaded one block ahead, so the dependent col -> x load
   // chain of block k + 1 overlaps the accumulation of block k (the arithmetic order is unchanged).
-  T xn[3] = {T(0), T(0), T(0)};
-  if (k0 < e) gather(src.column(k0, 0), xn);
-  // FP32: the block values are loaded one block ahead too (the FP32 solve is bound by load latency; the FP64
-  // one by its FMA pipe, where the extra registers would cost occupancy)
+  // FP32: the block values and gathered x are loaded two blocks ahead (the FP32 solve is bound by load
+  // latency); FP64: x one block ahead (the FP64 solve is bound by its FMA pipe; registers set occupancy)
   constexpr bool kAhead = sizeof(T) == 4;
-  T bn[9];
+  T xn[3] = {T(0), T(0), T(0)}, xm[3] = {T(0), T(0), T(0)};
+  T bn[9], bm[9];
+  if (k0 < e) gather(src.column(k0, 0), xn);
   if (kAhead) {
+    if (k0 + 1 < e) gather(src.column(k0 + 1, 1), xm);
 #pragma unroll
     for (int e2 = 0; e2 < 9; ++e2) bn[e2] = k0 < e ? src.value(k0, 0, e2) : T(0);
+#pragma unroll
+    for (int e2 = 0; e2 < 9; ++e2) bm[e2] = k0 + 1 < e ? src.value(k0 + 1, 1, e2) : T(0);
   }
   for (int step = 0; step < S; ++step) {
     const int k = k0 + step;
     const bool valid = k < e;
     const T x[3] = {xn[0], xn[1], xn[2]};
-    if (k + 1 < e) gather(src.column(k + 1, step + 1), xn);
     T b[9];
     if (kAhead) {
 #pragma unroll
       for (int e2 = 0; e2 < 9; ++e2) b[e2] = bn[e2];
 #pragma unroll
-      for (int e2 = 0; e2 < 9; ++e2) bn[e2] = k + 1 < e ? src.value(k + 1, step + 1, e2) : T(0);
+      for (int e2 = 0; e2 < 9; ++e2) bn[e2] = bm[e2];
+      xn[0] = xm[0]; xn[1] = xm[1]; xn[2] = xm[2];
+      if (k + 2 < e) gather(src.column(k + 2, step + 2), xm);
+#pragma unroll
+      for (int e2 = 0; e2 < 9; ++e2) bm[e2] = k + 2 < e ? src.value(k + 2, step + 2, e2) : T(0);
     } else {
+      if (k + 1 < e) gather(src.column(k + 1, step + 1), xn);
 #pragma unroll
       for (int e2 = 0; e2 < 9; ++e2) b[e2] = valid ? src.value(k, step, e2) : T(0);
     }
