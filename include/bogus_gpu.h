@@ -336,6 +336,12 @@ int bogus_gpu_get_stream(const bogus_gpu_problem* h, void** stream);
  * on GPUs whose FP64 rate is below their memory bandwidth's need (no counterpart in the reference). */
 int bogus_gpu_measure_fp64_peak(int device, double* tflops);
 
+/* Compares the library's integer-pipe FP64 division, square root and exact scalings (by 1/2, by 2, + 0.0),
+ * used by the solvers' per-contact law work, with the GPU's own IEEE operations on n generated operands;
+ * mismatches[0..2] receive the differing results of division, square root and scalings (all zero when the
+ * implementation is exact). A diagnostic with no counterpart in the reference. */
+int bogus_gpu_check_fp64_ops(int device, long long n, unsigned long long seed, long long* mismatches);
+
 /* ---- Allocation-free projected-gradient solve (no counterpart in the reference) --------------------------
  * For callers that must not allocate GPU memory while solving: simulation steps run under a fixed device-memory
  * budget, real-time loops where cudaMalloc's implicit synchronisation would stall the frame, or hosts that hand

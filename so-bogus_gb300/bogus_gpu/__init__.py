@@ -96,7 +96,7 @@ EXPORTED = [
     "bogus_gpu_set_dual_device", "bogus_gpu_nnzb", "bogus_gpu_set_callback", "bogus_gpu_spmv", "bogus_gpu_eval",
     "bogus_gpu_solve_pg", "bogus_gpu_solve_pg_device", "bogus_gpu_solve_gs", "bogus_gpu_coloring",
     "bogus_gpu_set_primal", "bogus_gpu_assemble_dual", "bogus_gpu_get_dual_lower", "bogus_gpu_get_solve_stats",
-    "bogus_gpu_get_stream", "bogus_gpu_measure_fp64_peak", "bogus_gpu_solve_pg_noalloc",
+    "bogus_gpu_get_stream", "bogus_gpu_measure_fp64_peak", "bogus_gpu_check_fp64_ops", "bogus_gpu_solve_pg_noalloc",
     "bogus_gpu_set_batch", "bogus_gpu_solve_pg_batch", "bogus_gpu_solve_pg_batch_device",
     "bogus_gpu_admm_options_default", "bogus_gpu_solve_admm", "bogus_gpu_adjoint_options_default",
     "bogus_gpu_adjoint", "bogus_gpu_adjoint_device", "bogus_gpu_adjoint_dual_lower", "bogus_gpu_adjoint_primal",
@@ -139,6 +139,7 @@ def lib():
     L.bogus_gpu_get_solve_stats.argtypes = [vp, C.POINTER(SolveStats)]
     L.bogus_gpu_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.bogus_gpu_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.bogus_gpu_check_fp64_ops.argtypes = [C.c_int, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
     L.bogus_gpu_set_batch.argtypes = [vp, C.c_int, _ip]
     L.bogus_gpu_adjoint_options_default.argtypes = [C.POINTER(AdjointOptions)]
     L.bogus_gpu_adjoint_options_default.restype = None
@@ -755,6 +756,14 @@ def measure_fp64_peak(device: int = 0) -> float:
     v = C.c_double()
     _check(lib().bogus_gpu_measure_fp64_peak(int(device), C.byref(v)), False)
     return v.value
+
+
+def check_fp64_ops(n: int, seed: int = 0, device: int = 0) -> tuple:
+    """Mismatches (division, square root, scalings) of the integer-pipe FP64 operations against the GPU's IEEE
+    operations on n generated operands; all zero when they are exact."""
+    out = (C.c_longlong * 3)()
+    _check(lib().bogus_gpu_check_fp64_ops(int(device), int(n), int(seed), out), False)
+    return tuple(int(v) for v in out)
 
 
 class MecheFrictionProblem:

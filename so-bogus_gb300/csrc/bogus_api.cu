@@ -3226,6 +3226,15 @@ int bogus_gpu_measure_fp64_peak(int device, double* tflops) {
   return BOGUS_GPU_OK;
 }
 
+int bogus_gpu_check_fp64_ops(int device, long long n, unsigned long long seed, long long* mismatches) {
+  if (!mismatches || n < 0) return fail(BOGUS_GPU_BAD_INPUT, "null output or negative count");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
+    return fail(BOGUS_GPU_NO_DEVICE, "no such CUDA device");
+  BG_CUDA(check_fp64_ops(device, n, seed, mismatches));
+  return BOGUS_GPU_OK;
+}
+
 // ---- contact permutation (DualFrictionProblem::applyPermutation / undoPermutation, FrictionProblem.cpp:102-125)
 // The stored problem becomes W' = P W P^T, b' = P b, mu' = P mu with contact k of the stored problem being
 // contact perm[k] of the caller's (the layout of SparseBlockMatrixBase::applyPermutation: blocks moved above the

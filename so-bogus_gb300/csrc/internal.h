@@ -180,6 +180,7 @@ cudaError_t launch_pgs_mx(int nbodies, int d, const int* bptr, const int* bent, 
 cudaError_t launch_pgs_y(int n, int d, const int* cb, const double* H, const double* Mx, const double* b, double* y,
                          cudaStream_t s);
 cudaError_t measure_fp64_peak(int device, double* tflops);
+cudaError_t check_fp64_ops(int device, long long n, unsigned long long seed, long long* mismatches);
 
 // Primal ADMM / AMA (kernels_admm.cu): Core/BlockSolvers/ADMM.impl.hpp:54-127 with QuadraticProxOp
 // (:29-38) as PrimalFrictionProblem::solveWith(ADMM&, lambda, v, r) calls it (PrimalFrictionProblem.cpp:61-73).

@@ -5,6 +5,7 @@
 // per-lane pieces of the canonical chunk-segmented order (spmv_chunk.cuh), starting from 0 (y = W x) or from
 // init_i (y = init + W x).
 #include "internal.h"
+#include "fp64_int.cuh"
 #include "soc_device.cuh"
 #include "spmv_chunk.cuh"
 
@@ -403,6 +404,73 @@ cudaError_t measure_fp64_peak(int device, double* tflops) {
   cudaEventDestroy(e1);
   cudaFree(out);
   *tflops = 2.0 * 8.0 * iters * (double)nb * nt / (best * 1e-3) / 1e12;
+  return e;
+}
+
+// Integer-pipe division, square root and exact scalings (fp64_int.cuh) against the hardware operations on
+// n generated operands: uniformly random bit patterns, exponents near 1, extreme mantissas, and quotients and
+// roots close to exact. out[0], out[1], out[2] count the mismatches of division, square root and scalings.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__global__ void k_check_fp64_ops(long long n, unsigned long long seed, unsigned long long* out) {
+  using namespace ipipe;
+  unsigned long long bad[3] = {0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const uint64_t r = seed + 8 * (uint64_t)i;
+    uint64_t ua = mix64(r), ub = mix64(r + 1);
+    const int mode = (int)(i & 7);
+    if (mode == 1 || mode == 2) {
+      ua = (ua & ~(0x7FFull << 52)) | ((uint64_t)(923 + mix64(r + 2) % 200) << 52);
+      ub = (ub & ~(0x7FFull << 52)) | ((uint64_t)(923 + mix64(r + 3) % 200) << 52);
+    } else if (mode == 3) {
+      const uint64_t pat[6] = {0, kMant, kMant - 1, 1, kMant >> 1, (kMant >> 1) + 1};
+      ua = (ua & ~kMant & ~(0x7FFull << 52)) | ((uint64_t)(1000 + mix64(r + 2) % 48) << 52) | pat[mix64(r + 3) % 6];
+      ub = (ub & ~kMant & ~(0x7FFull << 52)) | ((uint64_t)(1000 + mix64(r + 4) % 48) << 52) | pat[mix64(r + 5) % 6];
+    } else if (mode == 4) {
+      const double b = from_bits((ub & kMant) | (1023ull << 52));
+      const double q = (double)(long long)(mix64(r + 2) >> 40) + 0.5 * (double)(mix64(r + 3) & 1);
+      ua = to_bits(__dmul_rn(q, b)) + mix64(r + 4) % 3 - 1;
+      ub = to_bits(b);
+    }
+    const double a = from_bits(ua), b = from_bits(ub);
+    const double q0 = a / b, q1 = div_rn(a, b);
+    if (to_bits(q0) != to_bits(q1) && q0 == q0) ++bad[0];
+    uint64_t ux = ua & ~(1ull << 63);
+    if (mode == 5) {
+      const double t = (double)(long long)(mix64(r + 5) >> 37);
+      ux = to_bits(__dmul_rn(t, t)) + mix64(r + 6) % 3 - 1;
+    }
+    const double x = from_bits(ux);
+    const double s0 = sqrt(x), s1 = sqrt_rn(x);
+    if (to_bits(s0) != to_bits(s1) && s0 == s0) ++bad[1];
+    if (a == a) {
+      if (to_bits(scale2<-1>(a)) != to_bits(__dmul_rn(a, 0.5))) ++bad[2];
+      if (to_bits(scale2<1>(a)) != to_bits(__dmul_rn(a, 2.0))) ++bad[2];
+      if (__dadd_rn(a, -a) == 0.0 && to_bits(plus_zero(a)) != to_bits(__dadd_rn(a, 0.0))) ++bad[2];
+    }
+  }
+  for (int k = 0; k < 3; ++k)
+    if (bad[k]) atomicAdd(out + k, bad[k]);
+}
+
+cudaError_t check_fp64_ops(int device, long long n, unsigned long long seed, long long* mismatches) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return e;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  unsigned long long* out = nullptr;
+  if ((e = cudaMalloc(&out, 3 * sizeof(unsigned long long))) != cudaSuccess) return e;
+  cudaMemset(out, 0, 3 * sizeof(unsigned long long));
+  k_check_fp64_ops<<<sms * 8, 256>>>(n, seed, out);
+  unsigned long long h[3] = {0, 0, 0};
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(h, out, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(out);
+  for (int k = 0; k < 3; ++k) mismatches[k] = (long long)h[k];
   return e;
 }
 

@@ -193,8 +193,8 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     res_i = Ops::law_eval(desaxce, mu, lx, y);
     const T s0 = Ops::cov(desaxce, mu, y);
     y[0] = y[0] + s0;
-    y[1] = y[1] + T(0);
-    y[2] = y[2] + T(0);
+    y[1] = Ops::plus0(y[1]);
+    y[2] = Ops::plus0(y[2]);
     const T na = T(-alpha_t);
     T xs[3] = {fma(na, y[0], x[0]), fma(na, y[1], x[1]), fma(na, y[2], x[2])};
     Ops::project(mu, xs);
@@ -207,7 +207,8 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
       const T d[3] = {xs[0] - pv[0], xs[1] - pv[1], xs[2] - pv[2]};
       second_i = Ops::dot3(d, y);
     } else {
-      const T t[3] = {(T(0.5) * Mx[0] + bb[0]) + s0, (T(0.5) * Mx[1] + bb[1]) + T(0), (T(0.5) * Mx[2] + bb[2]) + T(0)};
+      const T t[3] = {(Ops::half(Mx[0]) + bb[0]) + s0, Ops::plus0(Ops::half(Mx[1]) + bb[1]),
+                      Ops::plus0(Ops::half(Mx[2]) + bb[2])};
       second_i = Ops::dot3(x, t);
     }
   };
@@ -271,8 +272,8 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
             load3cg(B.X(iprev), i, pv);
             load3cg(a.Y, i, y);
             const T s0 = ldcg(a.S0 + i);
-            const T t[3] = {(T(0.5) * acc[0] + __ldg(a.b + 3 * i)) + s0, (T(0.5) * acc[1] + __ldg(a.b + 3 * i + 1)) + T(0),
-                            (T(0.5) * acc[2] + __ldg(a.b + 3 * i + 2)) + T(0)};
+            const T t[3] = {(Ops::half(acc[0]) + __ldg(a.b + 3 * i)) + s0, Ops::plus0(Ops::half(acc[1]) + __ldg(a.b + 3 * i + 1)),
+                            Ops::plus0(Ops::half(acc[2]) + __ldg(a.b + 3 * i + 2))};
             v0 = Ops::dot3(xs, t);
             const T d[3] = {xs[0] - x[0], xs[1] - x[1], xs[2] - x[2]};
             v1 = Ops::dot3(y, d);

@@ -6,11 +6,15 @@
 // denominator):
 //   dot3(a,b) = fma(a2,b2, fma(a1,b1, a0*b0)),  3x3 rows the same, squared norms dot3(a,a).
 // The translation unit is compiled with --fmad=false, so no other contraction happens; division and
-// sqrt are the IEEE correctly rounded CUDA operations. Every function is __host__ __device__ so the CPU
-// test helper can run the identical code.
+// sqrt are IEEE correctly rounded: in the law and projection functions (the per-iteration work of the
+// iterative solvers) through the integer-pipe implementations of fp64_int.cuh, elsewhere the CUDA
+// operations. Multiplications by 1/2 and 2 and the zero test are exact bit operations there too. Every
+// function is __host__ __device__ so the CPU test helper can run the identical code.
 #pragma once
 
 #include <cmath>
+
+#include "fp64_int.cuh"
 
 #ifdef __CUDACC__
 #define BG_HD __host__ __device__ __forceinline__
@@ -23,13 +27,16 @@ namespace bogus_gpu {
 constexpr double kEps = 2.220446049250313080847e-16;       // NumTraits<double>::epsilon()
 constexpr double kLocalTol = 1.8189894035458565e-12;      // pow(eps, 0.75) == 2^-39 (SOCLaw local tolerance)
 
-BG_HD bool is_zero(double s) { return fabs(s) < kEps; }
+// fabs(s) < eps, compared as bit patterns (non-negative doubles order like their bits; NaN compares false)
+BG_HD bool is_zero(double s) {
+  return (ipipe::to_bits(s) & ~(uint64_t(1) << 63)) < ipipe::to_bits(kEps);
+}
 BG_HD double dmax(double a, double b) { return (a < b) ? b : a; }
 BG_HD double dmin(double a, double b) { return (b < a) ? b : a; }
 BG_HD double dot3(const double* a, const double* b) { return fma(a[2], b[2], fma(a[1], b[1], a[0] * b[0])); }
 BG_HD double sq3(const double* a) { return dot3(a, a); }
 BG_HD double dot2(double a0, double a1, double b0, double b1) { return fma(a1, b1, a0 * b0); }
-BG_HD double norm2(double a0, double a1) { return sqrt(dot2(a0, a1, a0, a1)); }
+BG_HD double norm2(double a0, double a1) { return ipipe::sqrt_rn(dot2(a0, a1, a0, a1)); }
 BG_HD void matvec3(const double* A, const double* x, double* y) {
 #pragma unroll
   for (int r = 0; r < 3; ++r) y[r] = fma(A[3 * r + 2], x[2], fma(A[3 * r + 1], x[1], A[3 * r] * x[0]));
@@ -507,14 +514,15 @@ BG_HD void fb_canonical(const double* x, const double* y, double* fb, double* dx
     om1[1] = -0.5; om1[2] = 0.0;
     om2[1] = 0.5;  om2[2] = 0.0;
   } else {
-    const double inv = 1.0 / nz2t;
+    const double inv = ipipe::div_rn(1.0, nz2t);
     const double t1 = z2[1] * inv, t2 = z2[2] * inv;
-    om1[1] = -0.5 * t1; om1[2] = -0.5 * t2;
-    om2[1] = 0.5 * t1;  om2[2] = 0.5 * t2;
+    om2[1] = ipipe::scale2<-1>(t1);  om2[2] = ipipe::scale2<-1>(t2);
+    om1[1] = -om2[1]; om1[2] = -om2[2];  // -0.5 t == -(0.5 t) exactly
   }
-  const double l1 = z2[0] - 2.0 * nz2t;
-  const double rl1 = sqrt(l1 > 0.0 ? l1 : 0.0);
-  const double rl2 = sqrt(z2[0] + 2.0 * nz2t);
+  const double nz2t2 = ipipe::scale2<1>(nz2t);
+  const double l1 = z2[0] - nz2t2;
+  const double rl1 = ipipe::sqrt_rn(l1 > 0.0 ? l1 : 0.0);
+  const double rl2 = ipipe::sqrt_rn(z2[0] + nz2t2);
   double z[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) z[k] = fma(rl2, om2[k], rl1 * om1[k]);
@@ -527,7 +535,7 @@ BG_HD void fb_canonical(const double* x, const double* y, double* fb, double* dx
     return;
   }
   if (is_zero(rl1)) {
-    const double izn = 1.0 / dot2(x[0], y[0], x[0], y[0]);
+    const double izn = ipipe::div_rn(1.0, dot2(x[0], y[0], x[0], y[0]));
     const double cx = 1.0 - x[0] * izn, cy = 1.0 - y[0] * izn;
 #pragma unroll
     for (int k = 0; k < 9; ++k) dx[k] = dy[k] = 0.0;
@@ -536,8 +544,8 @@ BG_HD void fb_canonical(const double* x, const double* y, double* fb, double* dx
     return;
   }
   const double det = rl1 * rl2;
-  const double inv_det = 1.0 / det;
-  const double inv_z0 = 1.0 / z[0];
+  const double inv_det = ipipe::div_rn(1.0, det);
+  const double inv_z0 = ipipe::div_rn(1.0, z[0]);
   double iL[9];
   iL[0] = z[0] * inv_det;
   iL[1] = -z[1] * inv_det;
@@ -565,7 +573,7 @@ BG_HD void fb_canonical(const double* x, const double* y, double* fb, double* dx
 
 BG_HD void fb_mu(double mu, const double* x, const double* y, double* fb) {
   if (is_zero(mu)) {
-    fb[0] = (x[0] + y[0]) - sqrt(dot2(x[0], y[0], x[0], y[0]));
+    fb[0] = (x[0] + y[0]) - ipipe::sqrt_rn(dot2(x[0], y[0], x[0], y[0]));
     fb[1] = x[1];
     fb[2] = x[2];
   } else {
@@ -577,7 +585,7 @@ BG_HD void fb_mu(double mu, const double* x, const double* y, double* fb) {
 
 BG_HD void fb_mu_jacobian(double mu, const double* x, const double* y, double* fb, double* dx, double* dy) {
   if (is_zero(mu)) {
-    const double z = sqrt(dot2(x[0], y[0], x[0], y[0]));
+    const double z = ipipe::sqrt_rn(dot2(x[0], y[0], x[0], y[0]));
     fb[0] = (x[0] + y[0]) - z;
     fb[1] = x[1];
     fb[2] = x[2];
@@ -585,7 +593,7 @@ BG_HD void fb_mu_jacobian(double mu, const double* x, const double* y, double* f
     for (int k = 0; k < 9; ++k) { dx[k] = 0.0; dy[k] = 0.0; }
     dx[0] = dx[4] = dx[8] = 1.0;
     if (!is_zero(z)) {
-      const double iz = 1.0 / z;
+      const double iz = ipipe::div_rn(1.0, z);
       dx[0] = 1.0 - x[0] * iz;
       dy[0] = 1.0 - y[0] * iz;
     }
@@ -627,9 +635,9 @@ BG_HD void project_cone(double mu, double* x) {
   if (nxt <= mu * xn) return;
   if (mu * nxt <= -xn) { x[0] = x[1] = x[2] = 0.0; return; }
   const double den2 = fma(mu, mu, 1.0);
-  const double proj = fma(mu, nxt, xn) / den2;
+  const double proj = ipipe::div_rn(fma(mu, nxt, xn), den2);
   x[0] = proj;
-  const double f = (proj * mu) / nxt;
+  const double f = ipipe::div_rn(proj * mu, nxt);
   x[1] *= f;
   x[2] *= f;
 }

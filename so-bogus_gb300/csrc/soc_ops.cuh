@@ -26,6 +26,9 @@ struct SocOps<double> {
   static __device__ __forceinline__ void project(double mu, double* x) { project_cone(mu, x); }
   static __device__ __forceinline__ double dot3(const double* a, const double* b) { return bogus_gpu::dot3(a, b); }
   static __device__ __forceinline__ double sq3(const double* a) { return bogus_gpu::sq3(a); }
+  // 0.5 v and v + 0.0, exact bit operations off the FP64 pipe
+  static __device__ __forceinline__ double half(double v) { return ipipe::scale2<-1>(v); }
+  static __device__ __forceinline__ double plus0(double v) { return ipipe::plus_zero(v); }
 };
 
 template <>
@@ -35,6 +38,8 @@ struct SocOps<float> {
     return fmaf(a[2], b[2], fmaf(a[1], b[1], a[0] * b[0]));
   }
   static __device__ __forceinline__ float sq3(const float* a) { return dot3(a, a); }
+  static __device__ __forceinline__ float half(float v) { return 0.5f * v; }
+  static __device__ __forceinline__ float plus0(float v) { return v + 0.f; }
   static __device__ __forceinline__ float norm2(float a0, float a1) { return sqrtf(fmaf(a1, a1, a0 * a0)); }
 
   static __device__ __forceinline__ void fb_canonical(const float* x, const float* y, float* fb) {
