@@ -391,10 +391,10 @@ int ensure_pg_work(bogus_gpu_problem* h, unsigned max_iters) {
   BG_CUDA(h->XB.ensure(n3));
   BG_CUDA(h->Wv.ensure(n3));
   BG_CUDA(h->csum.ensure(4 * (size_t)C));
-  BG_CUDA(h->scal.ensure(8));
+  BG_CUDA(h->scal.ensure(8 + 32));  // scalars, then the stripe sums of grid_barrier_combine
   BG_CUDA(h->trace.ensure((size_t)max_iters + 1));
   BG_CUDA(h->pgout.ensure(1));
-  BG_CUDA(h->barrier.ensure(4));
+  BG_CUDA(h->barrier.ensure(8));
   BG_CUDA(h->status.ensure(1));
   return BOGUS_GPU_OK;
 }
@@ -459,6 +459,8 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.out = h->pgout.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
   a.tickets = h->barrier.p + 2;
+  a.combine_count = h->barrier.p + 4;
+  a.stripes = h->scal.p + 8;
   a.desaxce = o->static_problem ? 0 : 1;
   a.variant = o->variant;
   a.use_inf = o->use_infinity_norm ? 1 : 0;
@@ -467,7 +469,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.pess = o->ls_pessimistic_factor;
   a.max_iters = o->max_iters;
   a.ls_iters = o->ls_iters;
-  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), h->stream));
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 8 * sizeof(unsigned), h->stream));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
   int grid = pg_max_grid(h->device, false, true);
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
@@ -614,9 +616,11 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   a.out = h->pgout.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
   a.tickets = h->barrier.p + 2;
+  a.combine_count = h->barrier.p + 4;
+  a.stripes = h->scal.p + 8;
   fill_args(a, o);
   BG_CUDA(launch_convert(n3, h->X.p, h->X32.p, s));
-  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), s));
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 8 * sizeof(unsigned), s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   int grid = pg_max_grid(h->device, true, true);
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");

@@ -226,4 +226,120 @@ __device__ __forceinline__ bool grid_barrier(const GridBarrier& gb, LastFn&& las
   return ok;
 }
 
+// Bounded grid barrier that also reduces K <= 4 quantities of chunk sums (s + q * C, chunk order) into
+// out[0..K) in the canonical order of block8_combine_k: 8 stripes of ceil(C / 8) chunks, lane l of a stripe
+// summing chunks start + l, start + l + 32, ... in turn, a butterfly per stripe, the 8 stripe sums left to
+// right. The combination is spread over the last m = min(8, parties) CTAs to arrive: each waits until every
+// CTA has arrived, then reduces stripes role, role + m, ... with one warp per quantity (the chains of a
+// stripe run on different SM sub-partitions, and the 8 stripes on different SMs), and writes the stripe sums
+// to stripes[8 q + k]. The last of them to finish adds the stripe sums, runs `last_fn` and releases the
+// grid. The order of every addition is the one block8_combine_k uses, so the totals are identical. Every
+// wait is bounded as in grid_barrier.
+template <class LastFn>
+__device__ __forceinline__ bool grid_barrier_combine(const GridBarrier& gb, unsigned* combine_count, const double* s,
+                                                     int C, int K, unsigned maxmask, double* stripes, double* out,
+                                                     LastFn&& last_fn) {
+  __shared__ int s_role, s_ok, s_final;
+  __shared__ unsigned s_gen;
+  const unsigned P = gb.parties ? gb.parties : gridDim.x;
+  const unsigned m = P < 8u ? P : 8u;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned my_gen = ld_acquire_u32(gb.gen);
+    s_gen = my_gen;
+    const unsigned prev = atom_add_acq_rel_u32(gb.count, 1u);
+    s_role = prev >= P - m ? (int)(prev - (P - m)) : -1;
+    s_ok = 1;
+    s_final = 0;
+    if (s_role >= 0) {  // wait for every CTA's chunk sums
+      const unsigned long long t0 = global_timer_ns();
+      unsigned spins = 0;
+      while (ld_acquire_u32(gb.count) < P) {
+        if (ld_relaxed_i32(gb.status) != 0) { s_ok = 0; break; }
+        if ((++spins & 255u) == 0 && global_timer_ns() - t0 > kBarrierTimeoutNs) {
+          atomicCAS(gb.status, 0, (int)BOGUS_GPU_TIMEOUT);
+          s_ok = 0;
+          break;
+        }
+        __nanosleep(20);
+      }
+      __threadfence();
+    }
+  }
+  __syncthreads();
+  if (s_role >= 0 && s_ok) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int per = (C + 7) / 8;
+    for (int st = s_role; st < 8; st += (int)m) {
+      if (warp < K) {
+        const bool mx = (maxmask >> warp) & 1u;
+        const double* q = s + (size_t)warp * C;
+        const int e = min(C, st * per + per);
+        double p = 0.0;
+        int c = st * per + lane;
+        for (; c + 96 < e; c += 128) {
+          double v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) v[u] = ldcg(q + c + 32 * u);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) p = mx ? ((v[u] < p) ? p : v[u]) : p + v[u];
+        }
+        for (; c < e; c += 32) {
+          const double v = ldcg(q + c);
+          p = mx ? ((v < p) ? p : v) : p + v;
+        }
+        p = mx ? warp_max_butterfly(p) : warp_sum_butterfly(p);
+        if (lane == 0) stripes[8 * warp + st] = p;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      s_final = atom_add_acq_rel_u32(combine_count, 1u) == m - 1u ? 1 : 0;
+      if (s_final) __threadfence();
+    }
+    __syncthreads();
+    if (s_final) {
+      if ((int)threadIdx.x < K) {
+        const int q = threadIdx.x;
+        const bool mx = (maxmask >> q) & 1u;
+        double total = ldcg(stripes + 8 * q);
+        for (int k = 1; k < 8; ++k) {
+          const double v = ldcg(stripes + 8 * q + k);
+          total = mx ? ((v < total) ? total : v) : total + v;
+        }
+        out[q] = total;
+      }
+      last_fn();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        *gb.count = 0u;
+        *combine_count = 0u;
+        __threadfence();
+        st_release_u32(gb.gen, s_gen + 1u);
+      }
+    }
+  }
+  if (threadIdx.x == 0 && !s_final && s_ok) {
+    const unsigned long long t0 = global_timer_ns();
+    unsigned spins = 0;
+    while (ld_acquire_u32(gb.gen) == s_gen) {
+      if (ld_relaxed_i32(gb.status) != 0) { s_ok = 0; break; }
+      if ((++spins & 255u) == 0 && global_timer_ns() - t0 > kBarrierTimeoutNs) {
+        atomicCAS(gb.status, 0, (int)BOGUS_GPU_TIMEOUT);
+        s_ok = 0;
+        break;
+      }
+      __nanosleep(40);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_ok = (s_ok != 0 && ld_relaxed_i32(gb.status) == 0) ? 1 : 0;
+  __syncthreads();
+  const bool ok = s_ok != 0;
+  __syncthreads();
+  return ok;
+}
+
 }  // namespace bogus_gpu

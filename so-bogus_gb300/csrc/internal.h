@@ -65,6 +65,8 @@ struct PGArgsT {
   PGOut* out;
   GridBarrier gb;
   unsigned* tickets;  // 2 chunk counters (phase parity) for dynamic work distribution; zero at launch
+  unsigned* combine_count;  // CTAs done with their stripes of a reduction (grid_barrier_combine); zero at launch
+  double* stripes;          // 8 stripe sums per reduced quantity (32 doubles)
   int desaxce, variant, use_inf;
   double tol, opt, pess;
   unsigned max_iters, ls_iters;

@@ -423,8 +423,9 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
 }
 
 
-// Single problem: the whole GPU, phases separated by the bounded grid barrier; the last CTA to arrive
-// publishes the reduced scalars in global memory. Warps take 32-contact chunks from a ticket counter (one
+// Single problem: the whole GPU, phases separated by the bounded grid barrier; at a reducing barrier the
+// last CTAs to arrive combine the chunk sums, one stripe each (grid_barrier_combine), and the last of them
+// publishes the scalars in global memory. Warps take 32-contact chunks from a ticket counter (one
 // per phase parity, cleared by the last CTA of the barrier that ends the phase), so SMs that finish early
 // take more chunks; tickets map to chunks largest first (chunk_order), so the last chunks of a phase are
 // the short ones. Every cross-phase dependency goes through a barrier, and the reduction order does not
@@ -449,19 +450,14 @@ struct GridCtx {
   __device__ void clear_tickets() {
     if (threadIdx.x == 0) a.tickets[phase & 1u] = 0u;
   }
-  __device__ void publish(int K, unsigned maxmask) {
-    block8_combine_k(a.csum, a.nchunks, K, maxmask, smem8, a.scal);
-  }
   __device__ bool sync() {
     const bool ok = grid_barrier(a.gb, [&] { clear_tickets(); });
     ++phase;
     return ok;
   }
   __device__ bool sync_reduce(int K, unsigned maxmask) {
-    const bool ok = grid_barrier(a.gb, [&] {
-      publish(K, maxmask);
-      clear_tickets();
-    });
+    const bool ok = grid_barrier_combine(a.gb, a.combine_count, a.csum, a.nchunks, K, maxmask, a.stripes, a.scal,
+                                         [&] { clear_tickets(); });
     ++phase;
     return ok;
   }

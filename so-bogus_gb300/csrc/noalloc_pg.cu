@@ -47,7 +47,7 @@ constexpr size_t kOffScaling = kOffWv + kVec3;
 constexpr size_t kOffDiag = kOffScaling + kVec1;     // int32 per contact (stored in double slots)
 constexpr size_t kOffCsum = kOffDiag + round32((size_t)kMaxContacts / 2 + 1);
 constexpr size_t kOffScal = kOffCsum + round32(4 * (size_t)kMaxChunks);
-constexpr size_t kOffTrace = kOffScal + 32;
+constexpr size_t kOffTrace = kOffScal + 64;  // 8 scalars, 32 stripe sums
 constexpr size_t kOffOut = kOffTrace + round32((size_t)kMaxIters + 1);
 constexpr size_t kOffWords = kOffOut + round32(sizeof(PGOut) / sizeof(double) + 1);  // barrier count, gen, status
 constexpr size_t kScratchDoubles = kOffWords + 32;
@@ -125,7 +125,7 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   }
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   const size_t n3 = 3 * (size_t)n;
-  unsigned* words = reinterpret_cast<unsigned*>(s + kOffWords);  // [0] count, [1] gen, [2] status, [3..4] tickets
+  unsigned* words = reinterpret_cast<unsigned*>(s + kOffWords);  // [0] count, [1] gen, [2] status, [3..4] tickets, [5] combine
   // diagonal positions and scalings into the scratch
   DevBSR W;
   W.n = n;
@@ -136,7 +136,7 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   W.diag = reinterpret_cast<int*>(s + kOffDiag);
   NA_CUDA(launch_diag_and_scaling(W, s + kOffScaling, cs));
   NA_CUDA(cudaMemcpyAsync(s + kOffX, d_r, sizeof(double) * n3, cudaMemcpyDeviceToDevice, cs));
-  NA_CUDA(cudaMemsetAsync(words, 0, 5 * sizeof(unsigned), cs));
+  NA_CUDA(cudaMemsetAsync(words, 0, 6 * sizeof(unsigned), cs));
   PGArgs a{};
   a.n = n;
   a.nchunks = (n + 31) / 32;
@@ -161,6 +161,8 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   a.out = reinterpret_cast<PGOut*>(s + kOffOut);
   a.gb = GridBarrier{words, words + 1, reinterpret_cast<int*>(words + 2)};
   a.tickets = words + 3;
+  a.combine_count = words + 5;
+  a.stripes = s + kOffScal + 8;
   a.desaxce = o->static_problem ? 0 : 1;
   a.variant = o->variant;
   a.use_inf = o->use_infinity_norm ? 1 : 0;

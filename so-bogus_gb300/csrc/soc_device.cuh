@@ -7,8 +7,10 @@
 //   dot3(a,b) = fma(a2,b2, fma(a1,b1, a0*b0)),  3x3 rows the same, squared norms dot3(a,a).
 // The translation unit is compiled with --fmad=false, so no other contraction happens; division and
 // sqrt are IEEE correctly rounded: in the law and projection functions (the per-iteration work of the
-// iterative solvers) through the integer-pipe implementations of fp64_int.cuh, elsewhere the CUDA
-// operations. Multiplications by 1/2 and 2 and the zero test are exact bit operations there too. Every
+// iterative solvers, throughput bound) through the integer-pipe implementations of fp64_int.cuh, elsewhere
+// (the local solvers' QR, LU and closed forms, latency bound along the Gauss-Seidel chains, where the
+// integer sequence is slower than the hardware's) the CUDA operations. Multiplications by 1/2 and 2 and the
+// zero test are exact bit operations. Every
 // function is __host__ __device__ so the CPU test helper can run the identical code.
 #pragma once
 
