@@ -2197,8 +2197,8 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   BG_CUDA(h->adj_out.ensure(1));
   const int C = (n + 31) / 32;
   BG_CUDA(h->csum.ensure(4 * (size_t)(C > 0 ? C : 1)));
-  BG_CUDA(h->scal.ensure(8));
-  BG_CUDA(h->barrier.ensure(4));
+  BG_CUDA(h->scal.ensure(8 + 32));  // scalars, then the stripe sums of grid_barrier_combine
+  BG_CUDA(h->barrier.ensure(8));
   BG_CUDA(h->status.ensure(1));
   if (int e = ensure_interleaved(h)) return e;
   AdjArgs a{};
@@ -2231,9 +2231,11 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   a.scal = h->scal.p;
   a.out = h->adj_out.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.combine_count = h->barrier.p + 4;
+  a.stripes = h->scal.p + 8;
   a.tol = o->tol;
   a.max_iters = o->max_iters;
-  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), s));
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 8 * sizeof(unsigned), s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   int grid = adjoint_max_grid(h->device);
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
@@ -2501,10 +2503,10 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   if (prox) BG_CUDA(h->a_prox.ensure(m * d));
   const int C = (n + 31) / 32;
   BG_CUDA(h->csum.ensure(2 * (size_t)(C > 0 ? C : 1)));
-  BG_CUDA(h->scal.ensure(8));
+  BG_CUDA(h->scal.ensure(8 + 32));  // scalars, then the stripe sums of grid_barrier_combine
   BG_CUDA(h->trace.ensure((size_t)o->max_iters + 1));
   BG_CUDA(h->admm_out.ensure(1));
-  BG_CUDA(h->barrier.ensure(4));
+  BG_CUDA(h->barrier.ensure(8));
   BG_CUDA(h->status.ensure(1));
   if (n > 0) {
     BG_CUDA(cudaMemcpyAsync(h->a_w.p, w, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
@@ -2540,6 +2542,8 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   a.trace = h->trace.p;
   a.out = h->admm_out.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.combine_count = h->barrier.p + 4;
+  a.stripes = h->scal.p + 8;
   a.lambda = lambda;
   a.gamma = o->step_size;
   a.tol = o->tol;
@@ -2547,7 +2551,7 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   a.accelerated = o->variant == BOGUS_GPU_ADMM_ACCELERATED;
   a.use_inf = o->use_infinity_norm ? 1 : 0;
   a.scaling = h->a_sc.p;
-  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), s));
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 8 * sizeof(unsigned), s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   int grid = admm_max_grid(h->device, d);
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
@@ -2639,10 +2643,10 @@ int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_opti
   const int C = (n + 31) / 32, CB = (nb + 31) / 32;
   const int CC = C > CB ? C : CB;
   BG_CUDA(h->csum.ensure(3 * (size_t)(CC > 0 ? CC : 1)));
-  BG_CUDA(h->scal.ensure(8));
+  BG_CUDA(h->scal.ensure(8 + 32));  // scalars, then the stripe sums of grid_barrier_combine
   BG_CUDA(h->trace.ensure((size_t)o->max_iters + 1));
   BG_CUDA(h->dama_out.ensure(1));
-  BG_CUDA(h->barrier.ensure(4));
+  BG_CUDA(h->barrier.ensure(8));
   BG_CUDA(h->status.ensure(1));
   if (n > 0) {
     BG_CUDA(cudaMemcpyAsync(h->a_w.p, w, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
@@ -2685,6 +2689,8 @@ int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_opti
   a.trace = h->trace.p;
   a.out = h->dama_out.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.combine_count = h->barrier.p + 4;
+  a.stripes = h->scal.p + 8;
   a.tol = o->tol;
   a.gamma = o->fp_step_size;
   a.lambda0 = o->proj_step_size;
@@ -2696,7 +2702,7 @@ int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_opti
   a.accelerated = o->variant == BOGUS_GPU_ADMM_ACCELERATED;
   a.use_inf = o->use_infinity_norm ? 1 : 0;
   a.desaxce = static_problem ? 0 : 1;
-  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 4 * sizeof(unsigned), s));
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 8 * sizeof(unsigned), s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   int grid = dama_max_grid(h->device, d);
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");

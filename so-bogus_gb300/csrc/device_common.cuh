@@ -226,8 +226,9 @@ __device__ __forceinline__ bool grid_barrier(const GridBarrier& gb, LastFn&& las
   return ok;
 }
 
-// Bounded grid barrier that also reduces K <= 4 quantities of chunk sums (s + q * C, chunk order) into
-// out[0..K) in the canonical order of block8_combine_k: 8 stripes of ceil(C / 8) chunks, lane l of a stripe
+// Bounded grid barrier that also reduces K <= 4 quantities of chunk sums into out[0..K) in the canonical
+// order of block8_combine / block8_combine_k. Quantity q's sums are at s + q * stride, over count0 chunks for
+// q = 0 and count1 chunks for q > 0. Each is split into 8 stripes of ceil(count / 8) chunks, lane l of a stripe
 // summing chunks start + l, start + l + 32, ... in turn, a butterfly per stripe, the 8 stripe sums left to
 // right. The combination is spread over the last m = min(8, parties) CTAs to arrive: each waits until every
 // CTA has arrived, then reduces stripes role, role + m, ... with one warp per quantity (the chains of a
@@ -237,8 +238,8 @@ __device__ __forceinline__ bool grid_barrier(const GridBarrier& gb, LastFn&& las
 // wait is bounded as in grid_barrier.
 template <class LastFn>
 __device__ __forceinline__ bool grid_barrier_combine(const GridBarrier& gb, unsigned* combine_count, const double* s,
-                                                     int C, int K, unsigned maxmask, double* stripes, double* out,
-                                                     LastFn&& last_fn) {
+                                                     size_t stride, int count0, int count1, int K, unsigned maxmask,
+                                                     double* stripes, double* out, LastFn&& last_fn) {
   __shared__ int s_role, s_ok, s_final;
   __shared__ unsigned s_gen;
   const unsigned P = gb.parties ? gb.parties : gridDim.x;
@@ -270,11 +271,12 @@ __device__ __forceinline__ bool grid_barrier_combine(const GridBarrier& gb, unsi
   __syncthreads();
   if (s_role >= 0 && s_ok) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int C = warp == 0 ? count0 : count1;
     const int per = (C + 7) / 8;
     for (int st = s_role; st < 8; st += (int)m) {
       if (warp < K) {
         const bool mx = (maxmask >> warp) & 1u;
-        const double* q = s + (size_t)warp * C;
+        const double* q = s + (size_t)warp * stride;
         const int e = min(C, st * per + per);
         double p = 0.0;
         int c = st * per + lane;

@@ -205,6 +205,8 @@ struct ADMMArgs {
   double *x, *r, *ut, *z, *zacc, *zprev, *yprev;
   double* csum;        // 2 x nchunks
   double* scal;        // published scalars
+  unsigned* combine_count;  // grid_barrier_combine's counter; zero at launch
+  double* stripes;          // 8 stripe sums per reduced quantity
   double* trace;       // max_iters entries, or null
   ADMMOut* out;
   GridBarrier gb;
@@ -237,6 +239,8 @@ struct DamaArgs {
   double *v, *r, *rs, *x, *HrBp, *ut, *g, *y_prev, *r_best, *v_best;
   double* csum;           // 3 x max(contact chunks, body chunks)
   double* scal;
+  unsigned* combine_count;  // grid_barrier_combine's counter; zero at launch
+  double* stripes;          // 8 stripe sums per reduced quantity
   double* trace;          // max_iters
   DamaOut* out;
   GridBarrier gb;
@@ -272,6 +276,8 @@ struct AdjArgs {
   double* dmu;         // out: dL/dmu
   double* csum;
   double* scal;
+  unsigned* combine_count;  // grid_barrier_combine's counter; zero at launch
+  double* stripes;          // 8 stripe sums per reduced quantity
   AdjOut* out;
   GridBarrier gb;
   double tol;

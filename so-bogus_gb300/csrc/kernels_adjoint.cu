@@ -142,12 +142,8 @@ struct AdjCtx {
   double* smem8;
   __device__ bool sync() { return grid_barrier(a.gb, [] {}); }
   __device__ bool sync_reduce(int K) {
-    return grid_barrier(a.gb, [&] {
-      for (int q = 0; q < K; ++q) {
-        const double v = block8_combine(a.csum + q * a.nchunks, a.nchunks, false, smem8);
-        if (threadIdx.x == 0) a.scal[q] = v;
-      }
-    });
+    return grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)a.nchunks, a.nchunks, a.nchunks, K, 0u,
+                                a.stripes, a.scal, [] {});
   }
 };
 

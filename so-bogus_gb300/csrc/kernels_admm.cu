@@ -29,12 +29,8 @@ struct AdmmCtx {
   int nchunks;
   __device__ bool sync() { return grid_barrier(a.gb, [] {}); }
   __device__ bool sync_reduce2(unsigned maxmask) {
-    return grid_barrier(a.gb, [&] {
-      for (int q = 0; q < 2; ++q) {
-        const double v = block8_combine(a.csum + q * nchunks, nchunks, (maxmask >> q) & 1u, smem8);
-        if (threadIdx.x == 0) a.scal[q] = v;
-      }
-    });
+    return grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)nchunks, nchunks, nchunks, 2, maxmask,
+                                a.stripes, a.scal, [] {});
   }
 };
 
@@ -297,12 +293,8 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
   auto sync = [&]() { return grid_barrier(a.gb, [] {}); };
     // value 0 over count0 chunks, values 1.. over count1 chunks
   auto sync_reduce = [&](int K, int count0, int count1, unsigned maxmask) {
-    return grid_barrier(a.gb, [&] {
-      for (int q = 0; q < K; ++q) {
-        const double v = block8_combine(a.csum + q * CC, q == 0 ? count0 : count1, (maxmask >> q) & 1u, smem8);
-        if (threadIdx.x == 0) a.scal[q] = v;
-      }
-    });
+    return grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)CC, count0, count1, K, maxmask, a.stripes,
+                                a.scal, [] {});
   };
   // H^T src for body b (d values): per dof, contacts in increasing order, rows inner
   auto body_HT = [&](int b, const double* src, double* out) {

@@ -456,8 +456,8 @@ struct GridCtx {
     return ok;
   }
   __device__ bool sync_reduce(int K, unsigned maxmask) {
-    const bool ok = grid_barrier_combine(a.gb, a.combine_count, a.csum, a.nchunks, K, maxmask, a.stripes, a.scal,
-                                         [&] { clear_tickets(); });
+    const bool ok = grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)a.nchunks, a.nchunks, a.nchunks, K,
+                                         maxmask, a.stripes, a.scal, [&] { clear_tickets(); });
     ++phase;
     return ok;
   }
