@@ -130,6 +130,17 @@ def traffic_from_profiles(algorithmic_bytes):
     return None
 
 
+def pinned_copy(a, keep: list):
+    """A copy of the host array `a` in page-locked memory (torch's pinned allocator); `keep` holds the buffer."""
+    import torch
+
+    t = torch.empty(max(1, a.nbytes), dtype=torch.uint8, pin_memory=True)
+    keep.append(t)
+    p = t.numpy()[: a.nbytes].view(a.dtype).reshape(a.shape)
+    p[...] = a
+    return p
+
+
 def max_over_ranks(value: float, world: int, device: str = "cpu") -> float:
     """The maximum of a per-rank value over all ranks (every rank gets it); the value itself when world == 1.
     The tensor lives on `device` (a CUDA device under NCCL, the CPU under gloo)."""
@@ -244,21 +255,24 @@ def run_ours(args, rank, world, local_rank):
     ck = clocks.stop()
     ms_step = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, f"cuda:{dev}")
 
-    # end to end through the C ABI with host buffers: upload W (lower), b, mu and r, solve, download r
+    # end to end through the C ABI with host buffers: upload W (lower), b, mu and r, solve, download r. The
+    # host arrays live in pinned (page-locked) memory, as a simulation that streams problems to the GPU keeps them.
     rp, cl, vl = D.W_lower()
-    vl = np.ascontiguousarray(vl.reshape(-1))
+    keep = []
+    rp, cl, vl = (pinned_copy(a, keep) for a in (rp, cl, np.ascontiguousarray(vl.reshape(-1))))
+    bh, muh = pinned_copy(d.b.reshape(-1), keep), pinned_copy(d.mu, keep)
+    rh = pinned_copy(np.zeros(3 * n), keep)
     e2e_steps = max(1, min(args.steps, 3))
-    h2d = rp.nbytes + cl.nbytes + vl.nbytes + d.b.nbytes + d.mu.nbytes + 3 * n * 8
-    d2h = 3 * n * 8
+    h2d = rp.nbytes + cl.nbytes + vl.nbytes + bh.nbytes + muh.nbytes + rh.nbytes
+    d2h = rh.nbytes
     E = bogus_gpu.DualFrictionProblem(dev)
-    rh = np.zeros(3 * n)
-    E.set(rp, cl, vl, d.b, d.mu)  # warm (allocations)
+    E.set(rp, cl, vl, bh, muh)  # warm (allocations)
     E.solveWith(pg, rh)
     e2e_ms = []
     for _ in range(e2e_steps):
-        rh = np.zeros(3 * n)
+        rh[...] = 0.0
         t0 = time.perf_counter()
-        E.set(rp, cl, vl, d.b, d.mu)
+        E.set(rp, cl, vl, bh, muh)
         E.solveWith(pg, rh)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     del E

@@ -178,30 +178,66 @@ __global__ void k_count_upper(int n, const int* __restrict__ rowptr, const int* 
     if (col[k] != i) atomicAdd(upper + col[k], 1);
 }
 
-// frowptr = exclusive prefix sum of the full row lengths (lower length + upper[i]), one CTA of 1024 threads:
-// each thread sums a contiguous range, the range totals are scanned in shared memory, the ranges written.
-__global__ void __launch_bounds__(1024) k_full_rowptr(int n, const int* __restrict__ rowptr,
-                                                      const int* __restrict__ upper, int* frowptr) {
-  __shared__ int part[1024];
-  const int t = threadIdx.x;
-  const int per = (n + 1023) / 1024;
-  const int b = t * per, e = min(n, b + per);
-  int sum = 0;
-  for (int i = b; i < e; ++i) sum += (rowptr[i + 1] - rowptr[i]) + upper[i];
-  part[t] = sum;
+// frowptr = exclusive prefix sum of the full row lengths (lower length + upper[i]), in three coalesced passes:
+// the sum of each tile of 1024 rows, an exclusive scan of the tile sums (one CTA), then each tile's scan plus
+// its offset. frowptr[n] receives the total.
+__device__ __forceinline__ int full_row_length(int i, int n, const int* __restrict__ rowptr, const int* __restrict__ upper) {
+  return i < n ? (__ldg(rowptr + i + 1) - __ldg(rowptr + i)) + __ldg(upper + i) : 0;
+}
+// inclusive scan of v over the 1024 threads of the CTA; warp totals in ws[32]
+__device__ __forceinline__ int cta_inclusive_scan(int v, int* ws) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  if (lane == 31) ws[warp] = v;
   __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    const int v = t >= off ? part[t - off] : 0;
+  if (warp == 0) {
+    int w = ws[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += u;
+    }
+    ws[lane] = w;
+  }
+  __syncthreads();
+  return v + (warp > 0 ? ws[warp - 1] : 0);
+}
+__global__ void __launch_bounds__(1024) k_rowlen_tiles(int n, const int* __restrict__ rowptr,
+                                                       const int* __restrict__ upper, int* tile_sum) {
+  __shared__ int ws[32];
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  const int v = cta_inclusive_scan(full_row_length(i, n, rowptr, upper), ws);
+  if (threadIdx.x == 1023) tile_sum[blockIdx.x] = v;
+}
+__global__ void __launch_bounds__(1024) k_scan_tiles(int ntiles, int* tile_sum) {
+  __shared__ int ws[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < ntiles; base += 1024) {
+    const int k = base + threadIdx.x;
+    const int v = k < ntiles ? tile_sum[k] : 0;
+    const int inc = cta_inclusive_scan(v, ws);
+    const int c = carry;
+    if (k < ntiles) tile_sum[k] = c + inc - v;  // exclusive
     __syncthreads();
-    part[t] += v;
+    if (threadIdx.x == 1023) carry = c + inc;
     __syncthreads();
   }
-  int run = part[t] - sum;  // exclusive prefix of this thread's range
-  for (int i = b; i < e; ++i) {
-    frowptr[i] = run;
-    run += (rowptr[i + 1] - rowptr[i]) + upper[i];
-  }
-  if (t == 1023) frowptr[n] = part[1023];
+}
+__global__ void __launch_bounds__(1024) k_rowptr_tiles(int n, const int* __restrict__ rowptr,
+                                                       const int* __restrict__ upper, const int* __restrict__ tile_off,
+                                                       int* frowptr) {
+  __shared__ int ws[32];
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  const int v = full_row_length(i, n, rowptr, upper);
+  const int inc = cta_inclusive_scan(v, ws) + tile_off[blockIdx.x];
+  if (i < n) frowptr[i] = inc - v;
+  if (i == n - 1) frowptr[n] = inc;
 }
 
 // Row i of the full matrix: its lower blocks (columns <= i, in order), then the transposed blocks (i, j) of
@@ -253,11 +289,15 @@ cudaError_t launch_full_pattern(int n, const int* rowptr, const int* col, int* u
                                 int* fcol, int* src, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(upper, 0, sizeof(int) * n, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(cursor, 0, sizeof(int) * n, s);
   if (e != cudaSuccess) return e;
   const int g = (n + 255) / 256;
   k_count_upper<<<g, 256, 0, s>>>(n, rowptr, col, upper);
-  k_full_rowptr<<<1, 1024, 0, s>>>(n, rowptr, upper, frowptr);
+  // the tile sums use `cursor` (n ints; ceil(n / 1024) <= n), zeroed afterwards for k_place_lower
+  const int ntiles = (n + 1023) / 1024;
+  k_rowlen_tiles<<<ntiles, 1024, 0, s>>>(n, rowptr, upper, cursor);
+  k_scan_tiles<<<1, 1024, 0, s>>>(ntiles, cursor);
+  k_rowptr_tiles<<<ntiles, 1024, 0, s>>>(n, rowptr, upper, cursor, frowptr);
+  if ((e = cudaMemsetAsync(cursor, 0, sizeof(int) * n, s)) != cudaSuccess) return e;
   k_place_lower<<<g, 256, 0, s>>>(n, rowptr, col, frowptr, fcol, src, cursor);
   k_sort_upper<<<g, 256, 0, s>>>(n, rowptr, frowptr, fcol, src);
   return cudaGetLastError();
