@@ -280,6 +280,13 @@ __device__ __forceinline__ bool grid_barrier_combine(const GridBarrier& gb, unsi
         const int e = min(C, st * per + per);
         double p = 0.0;
         int c = st * per + lane;
+        for (; c + 224 < e; c += 256) {  // 8 loads in flight per lane, added in chunk order
+          double v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) v[u] = ldcg(q + c + 32 * u);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) p = mx ? ((v[u] < p) ? p : v[u]) : p + v[u];
+        }
         for (; c + 96 < e; c += 128) {
           double v[4];
 #pragma unroll
