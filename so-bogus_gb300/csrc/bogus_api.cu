@@ -2974,11 +2974,11 @@ int launch_batch_schedule(bogus_gpu_problem* h, const PGBatchArgs* ba64, const P
     return BOGUS_GPU_OK;
   }
   const int teams = std::min(np, gmax / size);
-  BG_CUDA(h->team_cnt.ensure(4 * (size_t)teams));
+  BG_CUDA(h->team_cnt.ensure(8 * (size_t)teams));
   BG_CUDA(h->team_job.ensure(teams));
-  BG_CUDA(h->team_scal.ensure(8 * (size_t)teams));
+  BG_CUDA(h->team_scal.ensure(40 * (size_t)teams));
   BG_CUDA(h->status.ensure(1));
-  BG_CUDA(cudaMemsetAsync(h->team_cnt.p, 0, sizeof(unsigned) * 4 * teams, s));
+  BG_CUDA(cudaMemsetAsync(h->team_cnt.p, 0, sizeof(unsigned) * 8 * teams, s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   BG_CUDA(cudaMemsetAsync(h->next.p, 0, sizeof(int), s));
   const PGTeamArgs ta{size, h->team_cnt.p, h->team_job.p, h->team_scal.p, h->status.p};

@@ -94,9 +94,9 @@ using PGBatchArgs32 = PGBatchArgsT<float>;
 // team (the single-problem schedule on a slice of the GPU).
 struct PGTeamArgs {
   int size;            // CTAs per team
-  unsigned* counters;  // 4 per team: barrier count, barrier generation, tickets of phase parity 0 and 1
+  unsigned* counters;  // 8 per team: barrier count, barrier generation, tickets of phase parity 0 and 1, combine count
   int* job;            // 1 per team: the problem the team solves
-  double* scal;        // 8 per team: the scalars published by the team's last barrier
+  double* scal;        // 40 per team: the scalars published by the team's last barrier, then 32 stripe sums
   int* status;
 };
 cudaError_t launch_pg_team(const PGBatchArgs& b, const PGTeamArgs& t, int grid, cudaStream_t s);

@@ -542,16 +542,17 @@ __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgsT<T> ba) {
 }
 
 // Team schedule: CTAs [team * size, team * size + size) solve one problem at a time with the single-problem
-// context (dynamic chunk tickets, bounded barrier, scalars published by the team's last CTA), on counters of
-// their own. The last CTA to reach the barrier before a job takes the next problem from the queue. The
+// context (dynamic chunk tickets, bounded barrier, chunk sums combined by the team's last CTAs to arrive
+// (grid_barrier_combine), scalars published in the team's slot), on counters of their own. The last CTA to reach the barrier before a job takes the next problem from the queue. The
 // arithmetic is that of the other schedules, so each problem's result is the same bit for bit.
 template <class T>
 struct TeamCtx {
   const PGArgsT<T>& a;
   double* smem8;
   ChunkScratchT<T>* cs;
-  unsigned* tickets;  // 2
-  double* sc;         // 8
+  unsigned* tickets;        // 2
+  unsigned* combine_count;  // 1
+  double* sc;               // 8 scalars, then 32 stripe sums
   GridBarrier gb;
   int rank;
   unsigned phase = 0;
@@ -572,10 +573,8 @@ struct TeamCtx {
     return ok;
   }
   __device__ bool sync_reduce(int K, unsigned maxmask) {
-    const bool ok = grid_barrier(gb, [&] {
-      block8_combine_k(a.csum, a.nchunks, K, maxmask, smem8, sc);
-      clear_tickets();
-    });
+    const bool ok = grid_barrier_combine(gb, combine_count, a.csum, (size_t)a.nchunks, a.nchunks, a.nchunks, K, maxmask,
+                                         sc + 8, sc, [&] { clear_tickets(); });
     ++phase;
     return ok;
   }
@@ -587,7 +586,7 @@ __global__ void __launch_bounds__(256, 3) k_pg_team(PGBatchArgsT<T> ba, PGTeamAr
   __shared__ double smem8[32];
   __shared__ ChunkScratchT<T> cs[8];
   const int team = blockIdx.x / ta.size, rank = blockIdx.x - team * ta.size;
-  unsigned* cnt = ta.counters + 4 * (size_t)team;
+  unsigned* cnt = ta.counters + 8 * (size_t)team;
   const GridBarrier gb{cnt, cnt + 1, ta.status, (unsigned)ta.size};
   for (;;) {
     if (!grid_barrier(gb, [&] {
@@ -618,7 +617,7 @@ __global__ void __launch_bounds__(256, 3) k_pg_team(PGBatchArgsT<T> ba, PGTeamAr
     a.csum = ba.base.csum + 4 * (size_t)ba.chunk_ptr[p];
     a.trace = nullptr;
     a.out = ba.base.out + p;
-    TeamCtx<T> ctx{a, smem8, cs, cnt + 2, ta.scal + 8 * (size_t)team, gb, rank};
+    TeamCtx<T> ctx{a, smem8, cs, cnt + 2, cnt + 4, ta.scal + 40 * (size_t)team, gb, rank};
     const int best = pg_body<T, false>(a, ctx);
     if (best < 0) return;  // a wait ran out (status recorded)
     if (n == 0) continue;
