@@ -394,7 +394,7 @@ int ensure_pg_work(bogus_gpu_problem* h, unsigned max_iters) {
   BG_CUDA(h->scal.ensure(8 + 32));  // scalars, then the stripe sums of grid_barrier_combine
   BG_CUDA(h->trace.ensure((size_t)max_iters + 1));
   BG_CUDA(h->pgout.ensure(1));
-  BG_CUDA(h->barrier.ensure(8));
+  BG_CUDA(h->barrier.ensure(16));  // [0..7] barrier words, [8..13] three 64-bit monotonic counters
   BG_CUDA(h->status.ensure(1));
   return BOGUS_GPU_OK;
 }
@@ -461,6 +461,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.tickets = h->barrier.p + 2;
   a.combine_count = h->barrier.p + 4;
   a.stripes = h->scal.p + 8;
+  a.mono = reinterpret_cast<unsigned long long*>(h->barrier.p + 8);
   a.desaxce = o->static_problem ? 0 : 1;
   a.variant = o->variant;
   a.use_inf = o->use_infinity_norm ? 1 : 0;
@@ -469,7 +470,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.pess = o->ls_pessimistic_factor;
   a.max_iters = o->max_iters;
   a.ls_iters = o->ls_iters;
-  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 8 * sizeof(unsigned), h->stream));
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 16 * sizeof(unsigned), h->stream));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
   int grid = pg_max_grid(h->device, false, true);
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
@@ -618,9 +619,10 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   a.tickets = h->barrier.p + 2;
   a.combine_count = h->barrier.p + 4;
   a.stripes = h->scal.p + 8;
+  a.mono = reinterpret_cast<unsigned long long*>(h->barrier.p + 8);
   fill_args(a, o);
   BG_CUDA(launch_convert(n3, h->X.p, h->X32.p, s));
-  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 8 * sizeof(unsigned), s));
+  BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 16 * sizeof(unsigned), s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   int grid = pg_max_grid(h->device, true, true);
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");

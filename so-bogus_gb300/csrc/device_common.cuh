@@ -36,6 +36,19 @@ __device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v
   asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
   return old;
 }
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long atom_add_acq_rel_u64(unsigned long long* p, unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.add.acq_rel.gpu.global.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+  return old;
+}
 __device__ __forceinline__ unsigned long long global_timer_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -349,6 +362,157 @@ __device__ __forceinline__ bool grid_barrier_combine(const GridBarrier& gb, unsi
   const bool ok = s_ok != 0;
   __syncthreads();
   return ok;
+}
+
+// ---- grid barrier on monotonic counters (single-problem persistent solvers) ------------------------------
+// mono[0] counts CTA arrivals, mono[1] finished stripe combinations, mono[2] published reductions; all start
+// at zero at launch and only grow. Barrier k of a launch is complete when mono[0] reaches parties (k + 1),
+// reduction r is published when mono[2] reaches r + 1. Since no counter is ever reset, a CTA may leave a
+// barrier as soon as every CTA has arrived, while the reduction of that barrier is still being combined (a
+// split reduction): the next phase's work that does not need the scalars overlaps the combination, and a warp
+// waits for the publication (mono_await) only where it needs them. Every wait is bounded as in grid_barrier.
+struct MonoBarrier {
+  unsigned long long* mono;
+  int* status;
+  unsigned parties;
+};
+
+// one thread: wait until *p >= target; false (and status set on a timeout) when the wait ends otherwise
+__device__ __forceinline__ bool spin_until_geq(const unsigned long long* p, unsigned long long target, int* status,
+                                               unsigned sleep_ns) {
+  const unsigned long long t0 = global_timer_ns();
+  unsigned spins = 0;
+  while (ld_acquire_u64(p) < target) {
+    if (ld_relaxed_i32(status) != 0) return false;
+    if ((++spins & 255u) == 0 && global_timer_ns() - t0 > kBarrierTimeoutNs) {
+      atomicCAS(status, 0, (int)BOGUS_GPU_TIMEOUT);
+      return false;
+    }
+    __nanosleep(sleep_ns);
+  }
+  return true;
+}
+
+// Barrier k without a reduction; the last CTA to arrive runs `last_fn` (all its threads), which must not be
+// needed by the other CTAs before the next barrier.
+template <class LastFn>
+__device__ __forceinline__ bool mono_barrier(const MonoBarrier& mb, unsigned k, LastFn&& last_fn) {
+  __shared__ int s_ok, s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned long long target = (unsigned long long)mb.parties * (k + 1ull);
+    const unsigned long long prev = atom_add_acq_rel_u64(mb.mono, 1ull);
+    s_last = prev == target - 1 ? 1 : 0;
+    s_ok = s_last ? 1 : (spin_until_geq(mb.mono, target, mb.status, 20) ? 1 : 0);
+  }
+  __syncthreads();
+  if (s_last) last_fn();
+  if (threadIdx.x == 0) s_ok = (s_ok != 0 && ld_relaxed_i32(mb.status) == 0) ? 1 : 0;
+  __syncthreads();
+  const bool ok = s_ok != 0;
+  __syncthreads();
+  return ok;
+}
+
+// Barrier k with reduction r of K <= 4 quantities, in the canonical order of grid_barrier_combine (the last
+// min(8, parties) CTAs to arrive combine one stripe each; the last of them to finish adds the stripe sums into
+// out[0..K) and publishes). split = false: every CTA leaves after the publication. split = true: a CTA leaves
+// once every CTA has arrived (the combining CTAs after their stripe), and reads out[] after mono_await(r + 1).
+template <class LastFn>
+__device__ __forceinline__ bool mono_barrier_combine(const MonoBarrier& mb, unsigned k, unsigned r, bool split,
+                                                     const double* s, size_t stride, int count0, int count1, int K,
+                                                     unsigned maxmask, double* stripes, double* out, LastFn&& last_fn) {
+  __shared__ int s_role, s_ok, s_final, s_last;
+  const unsigned P = mb.parties;
+  const unsigned m = P < 8u ? P : 8u;
+  const unsigned long long target = (unsigned long long)P * (k + 1ull);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned long long prev = atom_add_acq_rel_u64(mb.mono, 1ull);
+    s_last = prev == target - 1 ? 1 : 0;
+    s_role = prev >= target - m ? (int)(prev - (target - m)) : -1;
+    s_ok = 1;
+    s_final = 0;
+    if (s_role >= 0) {  // every CTA's chunk sums are needed
+      if (!s_last) s_ok = spin_until_geq(mb.mono, target, mb.status, 20) ? 1 : 0;
+      __threadfence();
+    }
+  }
+  __syncthreads();
+  if (s_last) last_fn();
+  if (s_role >= 0 && s_ok) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int C = warp == 0 ? count0 : count1;
+    const int per = (C + 7) / 8;
+    for (int st = s_role; st < 8; st += (int)m) {
+      if (warp < K) {
+        const bool mx = (maxmask >> warp) & 1u;
+        const double* q = s + (size_t)warp * stride;
+        const int e = min(C, st * per + per);
+        double p = 0.0;
+        int c = st * per + lane;
+        for (; c + 224 < e; c += 256) {  // 8 loads in flight per lane, added in chunk order
+          double v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) v[u] = ldcg(q + c + 32 * u);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) p = mx ? ((v[u] < p) ? p : v[u]) : p + v[u];
+        }
+        for (; c < e; c += 32) {
+          const double v = ldcg(q + c);
+          p = mx ? ((v < p) ? p : v) : p + v;
+        }
+        p = mx ? warp_max_butterfly(p) : warp_sum_butterfly(p);
+        if (lane == 0) stripes[8 * warp + st] = p;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      s_final = atom_add_acq_rel_u64(mb.mono + 1, 1ull) == (unsigned long long)m * (r + 1ull) - 1 ? 1 : 0;
+      if (s_final) __threadfence();
+    }
+    __syncthreads();
+    if (s_final) {
+      if ((int)threadIdx.x < K) {
+        const int q = threadIdx.x;
+        const bool mx = (maxmask >> q) & 1u;
+        double total = ldcg(stripes + 8 * q);
+        for (int j = 1; j < 8; ++j) {
+          const double v = ldcg(stripes + 8 * q + j);
+          total = mx ? ((v < total) ? total : v) : total + v;
+        }
+        out[q] = total;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        st_release_u64(mb.mono + 2, r + 1ull);
+      }
+    }
+  }
+  if (threadIdx.x == 0 && s_ok) {
+    if (!split) s_ok = spin_until_geq(mb.mono + 2, r + 1ull, mb.status, 40) ? 1 : 0;
+    else if (s_role < 0) s_ok = spin_until_geq(mb.mono, target, mb.status, 20) ? 1 : 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_ok = (s_ok != 0 && ld_relaxed_i32(mb.status) == 0) ? 1 : 0;
+  __syncthreads();
+  const bool ok = s_ok != 0;
+  __syncthreads();
+  return ok;
+}
+
+// One warp: wait until reduction `published` - 1 is published (mono[2] >= published). Every lane of the warp
+// must call it; the lanes read the scalars after it returns.
+__device__ __forceinline__ bool mono_await(const MonoBarrier& mb, unsigned long long published) {
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) ok = spin_until_geq(mb.mono + 2, published, mb.status, 40) ? 1 : 0;
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
 }
 
 }  // namespace bogus_gpu

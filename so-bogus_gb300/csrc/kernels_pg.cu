@@ -92,7 +92,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
   const auto blocks = BlocksOf<T, IL>::make(a);
   // y = W x of chunk c for every lane (row 32c + lane), x gathered from a buffer written earlier in the kernel
   auto product = [&](int c, const T* __restrict__ xsrc, T* acc) {
-    spmv_chunk<1>(a.rowptr, blocks, a.n, c, sh, [&](int j, T* x) { load3cg(xsrc, j, x); }, acc);
+    spmv_chunk<1, true>(a.rowptr, blocks, a.n, c, sh, [&](int j, T* x) { load3cg(xsrc, j, x); }, acc);
   };
   const int lane = threadIdx.x & 31;
   const bool desaxce = a.desaxce != 0;
@@ -121,6 +121,8 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
   };
   auto sync = [&]() -> bool { return ctx.sync(); };
   auto sync_reduce = [&](int K, unsigned maxmask) -> bool { return ctx.sync_reduce(K, maxmask); };
+  // split: the CTAs may go on before the scalars are published; read them after ctx.await_scalars()
+  auto sync_reduce_split = [&](int K, unsigned maxmask) -> bool { return ctx.sync_reduce_split(K, maxmask); };
   auto scal = [&](int q) { return ctx.scal(q); };
   // ConstrainedSolverBase::eval: sum / (1 + n), or the maximum with the infinity norm
   auto residual_of = [&](double reduced) { return a.use_inf ? reduced : reduced / (double)(1 + a.n); };
@@ -158,7 +160,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     const int i = 32 * c + lane;
     double v0 = 0.0, v1 = 0.0;
     T acc[3] = {T(0), T(0), T(0)}, accd[3] = {T(0), T(0), T(0)};
-    spmv_chunk<2>(a.rowptr, blocks, a.n, c, sh, [&](int j, T* x) { load3cg(a.X0, j, x); }, acc, accd);
+    spmv_chunk<2, true>(a.rowptr, blocks, a.n, c, sh, [&](int j, T* x) { load3cg(a.X0, j, x); }, acc, accd);
     if (i < a.n) {
       store3(a.MX0, i, acc);
       v0 = Ops::sq3(accd);
@@ -213,7 +215,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     }
   };
 
-  auto runA = [&](double alpha_t) -> bool {  // A as its own pass (Mx already in MX(imx))
+  auto runA = [&](double alpha_t, bool split) -> bool {  // A as its own pass (Mx already in MX(imx))
     ph[2]++;
     for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
       const int i = 32 * c + lane;
@@ -225,7 +227,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
       }
       put2(c, r, q, res_mask != 0);
     }
-    return sync_reduce(2, res_mask);
+    return split ? sync_reduce_split(2, res_mask) : sync_reduce(2, res_mask);
   };
 
   double min_res = -1.0, theta = 1.0;
@@ -237,19 +239,29 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     // APGD's momentum point x = xs + beta (xs - prev) (:137-139) is formed speculatively by every trial
     // product (C) into the spare buffer ispec, with beta from the Nesterov sequence (it needs no reduction);
     // when the line search ends with momentum, that buffer becomes x without a pass of its own.
+    // A (alone or fused with E) ends with a split reduction: the trial product of the next C phase does not
+    // need the residual and objective, so a warp reads them (iteration top: trace, best iterate, convergence)
+    // after the product of its first chunk, or after the phase when it gets no chunk.
     int ispec = 4;
     double alpha_t = alpha * a.opt;
-    if (!runA(alpha_t)) return -1;
+    if (!runA(alpha_t, true)) return -1;
     for (;;) {
-      const double res = residual_of(scal(0)), J = scal(1);
-      if (a.trace && ctx.writer()) a.trace[it] = res;
-      if (it == 0 || res < min_res) {
-        min_res = res;
-        best_pending = true;
-      }
-      if (res < a.tol) {
-        return finish(min_res, it, best_pending ? ix : 3, 1);
-      }
+      double res = 0.0, J = 0.0;
+      bool top_done = false, converged = false;
+      auto top = [&]() -> bool {
+        if (top_done) return true;
+        if (!ctx.await_scalars()) return false;
+        res = residual_of(scal(0));
+        J = scal(1);
+        if (a.trace && ctx.writer()) a.trace[it] = res;
+        if (it == 0 || res < min_res) {
+          min_res = res;
+          best_pending = true;
+        }
+        converged = res < a.tol;
+        top_done = true;
+        return true;
+      };
       alpha = alpha_t;
       unsigned ls = 0;
       double decr2 = 0.0;
@@ -258,12 +270,13 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
       const T bt = T(beta_spec);
       for (;;) {
         // C: Mxs = W xs, the line-search terms and the speculative momentum point
-        ph[3]++;
         for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
           T acc[3] = {T(0), T(0), T(0)};
           product(c, B.X(ixs), acc);
+          if (!top()) return -1;
+          if (converged) break;
           if (i < a.n) {
             store3(B.MX(1 - imx), i, acc);
             T x[3], xs[3], pv[3], y[3];
@@ -288,6 +301,9 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
           }
           put4(c, v0, v1, v2, v3);
         }
+        if (!top()) return -1;
+        if (converged) return finish(min_res, it, best_pending ? ix : 3, 1);
+        ph[3]++;
         best_pending = false;
         if (!sync_reduce(4, 0u)) return -1;
         const double Js = scal(0), decr = scal(1), nrm = scal(2);
@@ -335,7 +351,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
           }
           put2(c, r, q, res_mask != 0);
         }
-        if (!sync_reduce(2, res_mask)) return -1;
+        if (!sync_reduce_split(2, res_mask)) return -1;
       } else {
         theta = 1.;
         ix = ixs;
@@ -344,7 +360,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
         two_free(ix, iprev, ixs, ispec);
         if (!more) break;
         alpha_t = alpha * a.opt;
-        if (!runA(alpha_t)) return -1;
+        if (!runA(alpha_t, true)) return -1;
       }
     }
     return finish(min_res, it, 3, 0);
@@ -353,7 +369,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
   // ------------------------------------------------------------------ SPG (:288-351)
   const double a_min = 1.e-6, a_max = 1.e6;
   for (;;) {
-    if (!runA(alpha)) return -1;  // y, residual, s, xs = P(x - alpha y), (xs - prev).y
+    if (!runA(alpha, false)) return -1;  // y, residual, s, xs = P(x - alpha y), (xs - prev).y
     const double res = residual_of(scal(0)), decr = scal(1);
     if (a.trace && ctx.writer()) a.trace[it] = res;
     if (it == 0 || res < min_res) {
@@ -423,9 +439,10 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
 }
 
 
-// Single problem: the whole GPU, phases separated by the bounded grid barrier; at a reducing barrier the
-// last CTAs to arrive combine the chunk sums, one stripe each (grid_barrier_combine), and the last of them
-// publishes the scalars in global memory. Warps take 32-contact chunks from a ticket counter (one
+// Single problem: the whole GPU, phases separated by bounded grid barriers on monotonic counters
+// (mono_barrier); at a reducing barrier the last CTAs to arrive combine the chunk sums, one stripe each, and
+// the last of them publishes the scalars in global memory. After a split reduction the CTAs go on once every
+// CTA has arrived, and each warp waits for the publication only where it reads the scalars. Warps take 32-contact chunks from a ticket counter (one
 // per phase parity, cleared by the last CTA of the barrier that ends the phase), so SMs that finish early
 // take more chunks; tickets map to chunks largest first (chunk_order), so the last chunks of a phase are
 // the short ones. Every cross-phase dependency goes through a barrier, and the reduction order does not
@@ -450,16 +467,28 @@ struct GridCtx {
   __device__ void clear_tickets() {
     if (threadIdx.x == 0) a.tickets[phase & 1u] = 0u;
   }
+  unsigned reductions = 0;  // reductions published or pending (identical in every CTA)
+  bool pending = false;     // this warp has not yet waited for the last (split) reduction
+  __device__ MonoBarrier mb() const { return MonoBarrier{a.mono, a.gb.status, gridDim.x}; }
   __device__ bool sync() {
-    const bool ok = grid_barrier(a.gb, [&] { clear_tickets(); });
+    const bool ok = mono_barrier(mb(), phase, [&] { clear_tickets(); });
     ++phase;
     return ok;
   }
-  __device__ bool sync_reduce(int K, unsigned maxmask) {
-    const bool ok = grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)a.nchunks, a.nchunks, a.nchunks, K,
-                                         maxmask, a.stripes, a.scal, [&] { clear_tickets(); });
+  __device__ bool reduce(int K, unsigned maxmask, bool split) {
+    const bool ok = mono_barrier_combine(mb(), phase, reductions, split, a.csum, (size_t)a.nchunks, a.nchunks,
+                                         a.nchunks, K, maxmask, a.stripes, a.scal, [&] { clear_tickets(); });
     ++phase;
+    ++reductions;
+    pending = split;
     return ok;
+  }
+  __device__ bool sync_reduce(int K, unsigned maxmask) { return reduce(K, maxmask, false); }
+  __device__ bool sync_reduce_split(int K, unsigned maxmask) { return reduce(K, maxmask, true); }
+  __device__ bool await_scalars() {
+    if (!pending) return true;
+    pending = false;
+    return mono_await(mb(), reductions);
   }
   __device__ double scal(int q) const { return ldcg(a.scal + q); }
 };
@@ -493,6 +522,8 @@ struct BlockCtx {
     block8_combine_k(a.csum, a.nchunks, K, maxmask, smem8, sscal);
     return true;
   }
+  __device__ bool sync_reduce_split(int K, unsigned maxmask) { return sync_reduce(K, maxmask); }
+  __device__ bool await_scalars() const { return true; }
   __device__ double scal(int q) const { return sscal[q]; }
 };
 
@@ -578,6 +609,8 @@ struct TeamCtx {
     ++phase;
     return ok;
   }
+  __device__ bool sync_reduce_split(int K, unsigned maxmask) { return sync_reduce(K, maxmask); }
+  __device__ bool await_scalars() const { return true; }
   __device__ double scal(int q) const { return ldcg(sc + q); }
 };
 

@@ -13,6 +13,7 @@
 #pragma once
 
 #include "device_common.cuh"
+#include "fp64_int.cuh"
 
 namespace bogus_gpu {
 
@@ -57,10 +58,16 @@ struct InterleavedBlocks {
   }
 };
 
+// 0 + v for the first piece of a row when the initial value is +0: v itself with -0 turned into +0, as a bit
+// operation for FP64 (off the FP64 unit), the plain addition for FP32.
+__device__ __forceinline__ double zero_plus(double v) { return ipipe::plus_zero(v); }
+__device__ __forceinline__ float zero_plus(float v) { return 0.f + v; }
+
 // NP = 1: y = init + W x. NP = 2: additionally y2 = init2 + W (x - 1) (both from the same pass over W).
 // Every lane of the warp must call it (warp-uniform c). acc (and acc2) hold init on entry, the result on
-// exit, for row 32c + lane (lanes past n get unspecified values).
-template <int NP, class T, class Src, class Gather>
+// exit, for row 32c + lane (lanes past n get unspecified values). ZeroInit: every init is +0, so the first
+// piece of a row is placed rather than added (the same value).
+template <int NP, bool ZeroInit = false, class T, class Src, class Gather>
 __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, Src src, int n, int c,
                                            ChunkScratchT<T>& sh, Gather&& gather, T* acc, T* acc2 = nullptr) {
   const int lane = threadIdx.x & 31;
@@ -176,6 +183,17 @@ __device__ __forceinline__ void spmv_chunk(const int* __restrict__ rowptr, Src s
       const int lf = (rs - B0) / S, ll = (re - 1 - B0) / S;
       for (int l = lf; l <= ll; ++l) {
         const T* s = sh.part[lane + l];
+        if (ZeroInit && l == lf) {
+          acc[0] = zero_plus(s[0]);
+          acc[1] = zero_plus(s[1]);
+          acc[2] = zero_plus(s[2]);
+          if (NP == 2) {
+            acc2[0] = zero_plus(s[3]);
+            acc2[1] = zero_plus(s[4]);
+            acc2[2] = zero_plus(s[5]);
+          }
+          continue;
+        }
         acc[0] = acc[0] + s[0];
         acc[1] = acc[1] + s[1];
         acc[2] = acc[2] + s[2];
