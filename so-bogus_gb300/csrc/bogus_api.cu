@@ -459,7 +459,6 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.out = h->pgout.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
   a.tickets = h->barrier.p + 2;
-  a.combine_count = h->barrier.p + 4;
   a.stripes = h->scal.p + 8;
   a.mono = reinterpret_cast<unsigned long long*>(h->barrier.p + 8);
   a.desaxce = o->static_problem ? 0 : 1;
@@ -617,7 +616,6 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   a.out = h->pgout.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
   a.tickets = h->barrier.p + 2;
-  a.combine_count = h->barrier.p + 4;
   a.stripes = h->scal.p + 8;
   a.mono = reinterpret_cast<unsigned long long*>(h->barrier.p + 8);
   fill_args(a, o);

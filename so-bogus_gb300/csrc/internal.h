@@ -65,7 +65,6 @@ struct PGArgsT {
   PGOut* out;
   GridBarrier gb;
   unsigned* tickets;  // 2 chunk counters (phase parity) for dynamic work distribution; zero at launch
-  unsigned* combine_count;  // CTAs done with their stripes of a reduction (grid_barrier_combine); zero at launch
   double* stripes;          // 8 stripe sums per reduced quantity (32 doubles)
   unsigned long long* mono; // 3 monotonic counters of the single-problem kernel's barriers (MonoBarrier); zero at launch
   int desaxce, variant, use_inf;

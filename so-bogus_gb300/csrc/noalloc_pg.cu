@@ -125,7 +125,7 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   }
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   const size_t n3 = 3 * (size_t)n;
-  unsigned* words = reinterpret_cast<unsigned*>(s + kOffWords);  // [0] count, [1] gen, [2] status, [3..4] tickets, [5] combine, [8..13] 3 monotonic u64
+  unsigned* words = reinterpret_cast<unsigned*>(s + kOffWords);  // [0] count, [1] gen, [2] status, [3..4] tickets, [8..13] 3 monotonic u64
   // diagonal positions and scalings into the scratch
   DevBSR W;
   W.n = n;
@@ -161,7 +161,6 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   a.out = reinterpret_cast<PGOut*>(s + kOffOut);
   a.gb = GridBarrier{words, words + 1, reinterpret_cast<int*>(words + 2)};
   a.tickets = words + 3;
-  a.combine_count = words + 5;
   a.mono = reinterpret_cast<unsigned long long*>(words + 8);
   a.stripes = s + kOffScal + 8;
   a.desaxce = o->static_problem ? 0 : 1;

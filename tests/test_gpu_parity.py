@@ -540,3 +540,41 @@ def test_batch_rejects_coupled_partition(bg):
     with pytest.raises(bg.BogusGpuError) as e:
         D.setBatch([0, 250, d.n])  # random pairs couple the two halves
     assert e.value.status == bg.BAD_INPUT
+
+
+@pytest.fixture(scope="module")
+def grid20k(oracle):
+    """A 20 000-contact grid problem: 625 chunks, enough CTAs that the reductions run on 8 combining CTAs."""
+    from bogus_gpu import generator
+
+    d = generator.grid(nbodies=5_000, ncontacts=20_000, seed=7)
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    rp, cl, vl = P.assemble()
+    return d, rp, cl, vl
+
+
+@pytest.mark.parametrize("variant", [3, 1])  # APGD, Descent: reductions after the A phases are split
+@pytest.mark.parametrize("tol, max_iters", [(1e3, 50), (1e-30, 1), (1e-30, 2), (1e-30, 3), (1e-30, 7), (0.1, 60)])
+def test_projected_gradient_early_exits_bitwise(bg, oracle, grid20k, variant, tol, max_iters):
+    """Solves that stop at the first residual check (the warps drop the trial product they started before
+    the residual was published), after a few iterations, or on convergence part way: iterate, residual,
+    iteration count and callback trace equal the oracle's."""
+    d, rp, cl, vl = grid20k
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    for static in (True, False):
+        pg = bg.ProjectedGradient()
+        pg.setDefaultVariant(variant)
+        pg.setTol(tol)
+        pg.setMaxIters(max_iters)
+        trace_gpu = []
+        pg.callback().connect(lambda it, res: trace_gpu.append((it, res)))
+        r0 = np.random.default_rng(5).standard_normal(3 * d.n) * 0.05
+        r = r0.copy()
+        res = D.solveWith(pg, r, staticProblem=static)
+        tr = oracle.Trace()
+        res_o, r_o, it_o = O.solve_pg(r0, variant=variant, coulomb=not static, tol=tol, max_iters=max_iters, trace=tr)
+        assert res == res_o
+        assert D.last_iterations == it_o
+        assert np.array_equal(r, r_o)
+        assert trace_gpu == tr.items
