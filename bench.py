@@ -433,12 +433,25 @@ def run_gs(args) -> None:
         r = np.zeros(3 * d.n)
         res = D.solveWith(gs, r)
         gpu_ms = D.solve_stats()["device_ms"]
-        t0 = time.perf_counter()
-        res_o, r_o, _ = O.solve_gs(np.zeros(3 * d.n), max_iters=25, coloring=coloring)
-        cpu_ms = (time.perf_counter() - t0) * 1e3
-        out["colored" if coloring else "natural_order"] = {
-            "sweeps": 25, "gpu_ms_per_sweep": gpu_ms / 25, "cpu_oracle_ms_per_sweep": cpu_ms / 25,
-            "residual": res, "identical": bool(res == res_o and np.array_equal(r, r_o))}
+
+        def cpu_sweep_ms(threads):
+            # per sweep, without the one-off setup (coloring, permutation, local blocks, first evaluation)
+            pyoracle.set_gs_threads(threads)
+            res_o, r_o, _ = O.solve_gs(np.zeros(3 * d.n), max_iters=25, coloring=coloring)
+            pyoracle.set_gs_threads(1)
+            return pyoracle.last_gs_sweep_ms() / 25, res_o, r_o
+
+        cpu_ms, res_o, r_o = cpu_sweep_ms(1)
+        entry = {"sweeps": 25, "gpu_ms_per_sweep": gpu_ms / 25, "cpu_oracle_ms_per_sweep": cpu_ms,
+                 "residual": res, "identical": bool(res == res_o and np.array_equal(r, r_o))}
+        if coloring:
+            # the reference's per-color OpenMP loop on every host core (its iterates depend on thread timing)
+            threads = os.cpu_count() or 1
+            ms_par, res_par, _ = cpu_sweep_ms(threads)
+            entry["cpu_threads"] = threads
+            entry["cpu_parallel_ms_per_sweep"] = ms_par
+            entry["cpu_parallel_residual"] = res_par
+        out["colored" if coloring else "natural_order"] = entry
     # matrix-free sweep (ProductGaussSeidel) on the primal data: no W, M^-1 H^T x kept per body
     P = bogus_gpu.PrimalFrictionProblem.from_generated(d)
     pgs = bogus_gpu.ProductGaussSeidel()
@@ -450,8 +463,11 @@ def run_gs(args) -> None:
     gpu_ms = P.solve_stats()["device_ms"]
     PO = pyoracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
     t0 = time.perf_counter()
+    PO.solve_product_gs(np.zeros(d.nbodies * 6), d.b.reshape(-1), d.mu, np.zeros(3 * d.n), max_iters=0)
+    t1 = time.perf_counter()
     res_o, r_o, _ = PO.solve_product_gs(np.zeros(d.nbodies * 6), d.b.reshape(-1), d.mu, np.zeros(3 * d.n), max_iters=25)
-    cpu_ms = (time.perf_counter() - t0) * 1e3
+    t2 = time.perf_counter()
+    cpu_ms = ((t2 - t1) - (t1 - t0)) * 1e3
     out["matrix_free"] = {"sweeps": 25, "gpu_ms_per_sweep": gpu_ms / 25, "cpu_oracle_ms_per_sweep": cpu_ms / 25,
                           "residual": res, "identical": bool(res == res_o and np.array_equal(r, r_o))}
     print(json.dumps(out), flush=True)

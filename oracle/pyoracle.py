@@ -38,6 +38,8 @@ def lib():
     vp = C.c_void_p
     L.oracle_num_threads.restype = C.c_int
     L.oracle_set_num_threads.argtypes = [C.c_int]
+    L.oracle_set_gs_threads.argtypes = [C.c_int]
+    L.oracle_last_gs_sweep_ms.restype = C.c_double
     L.oracle_dual_create.restype = vp
     L.oracle_dual_create.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp]
     L.oracle_dual_destroy.argtypes = [vp]
@@ -117,6 +119,18 @@ def _i32(a):
 
 def set_num_threads(t: int) -> None:
     lib().oracle_set_num_threads(int(t))
+
+
+def set_gs_threads(t: int) -> None:
+    """Threads of the colored Gauss-Seidel sweeps that follow: 1 (default) is the sequential sweep the tests
+    compare against; more runs the reference's per-color OpenMP loop, whose iterates depend on the thread
+    timing (CPU timing baseline only)."""
+    lib().oracle_set_gs_threads(int(t))
+
+
+def last_gs_sweep_ms() -> float:
+    """Wall time (ms) of the sweeps and evaluations of the last dual Gauss-Seidel solve, without its setup."""
+    return float(lib().oracle_last_gs_sweep_ms())
 
 
 def num_threads() -> int:

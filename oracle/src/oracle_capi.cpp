@@ -54,6 +54,14 @@ int oracle_num_threads() {
 #endif
 }
 
+// Threads of the colored Gauss-Seidel sweeps that follow (1, the default: the sequential sweep the parity
+// tests compare against; more: the reference's per-color OpenMP loop, for CPU timing only).
+static int g_gs_threads = 1;
+void oracle_set_gs_threads(int t) { g_gs_threads = t > 1 ? t : 1; }
+// Wall time (ms) of the sweeps and evaluations of the last Gauss-Seidel solve, without its setup.
+static double g_gs_sweep_ms = 0.0;
+double oracle_last_gs_sweep_ms() { return g_gs_sweep_ms; }
+
 void oracle_set_num_threads(int t) {
 #ifdef _OPENMP
   if (t > 0) omp_set_num_threads(t);
@@ -151,10 +159,13 @@ double oracle_dual_solve_gs(void* h, int desaxce, int strat, double tol, unsigne
   gs.tryZeroAsWell = tryZero != 0;
   gs.useInfinityNorm = useInfinityNorm != 0;
   gs.callback = wrap(cb, user);
+  gs.threads = g_gs_threads;
   if (!useColoring) {
     gs.setMatrix(p->full);
     Law law{desaxce != 0, strat, p->mu.data()};
-    return gs.solve(law, p->b.data(), r, iters);
+    const double res = gs.solve(law, p->b.data(), r, iters);
+    g_gs_sweep_ms = gs.sweepSeconds * 1e3;
+    return res;
   }
   std::vector<int> perm, colors;
   greedyColoring(p->low, perm, colors);
@@ -170,6 +181,7 @@ double oracle_dual_solve_gs(void* h, int desaxce, int strat, double tol, unsigne
   gs.setMatrix(pfull);
   Law law{desaxce != 0, strat, pmu.data()};
   const double res = gs.solve(law, pb.data(), pr.data(), iters);
+  g_gs_sweep_ms = gs.sweepSeconds * 1e3;
   for (int i = 0; i < n; ++i)
     for (int k = 0; k < 3; ++k) r[3 * (size_t)perm[i] + k] = pr[3 * (size_t)i + k];
   return res;

@@ -9,6 +9,7 @@
 // per-contact values; per-contact values use the evaluation order of oracle_math.hpp.
 #pragma once
 
+#include <chrono>
 #include <cfloat>
 #include <functional>
 #include <vector>
@@ -95,6 +96,13 @@ struct GaussSeidel : SolverBase {
   std::vector<int> perm, colors;   // Coloring: permutation + color offsets
   std::vector<double> local;       // 9 n, diagonal blocks (+ regularization)
   std::vector<double> reg;         // n
+  // > 1: with two colors or more, each color's contacts are updated by that many OpenMP threads, as
+  // GaussSeidel::innerLoop does with maxThreads != 1 (GaussSeidel.impl.hpp:77-114, one `omp for` per color).
+  // The step-size reference ndxRef is shared between the threads, as there, so which contacts skip the next
+  // sweeps, and hence the iterates, depend on the thread timing: a CPU timing baseline only, never a parity
+  // reference.
+  int threads = 1;
+  mutable double sweepSeconds = 0.0;  // wall time of the last solve's sweeps and evaluations (no setup)
 
   GaussSeidel() { tol = 1e-6; maxIters = 250; }
 
@@ -167,6 +175,46 @@ struct GaussSeidel : SolverBase {
   void innerLoop(const Law& law, const double* b, std::vector<unsigned char>& skip, double& ndxRef, double* x) const {
     const double absSkipTol = dmin(skipTol, tol);
     const double absSkipIters = dmin((double)skipIters, (double)(unsigned)std::sqrt((double)skip.size()));
+    if (threads > 1 && colors.size() > 2 && (size_t)n() > (size_t)threads * (size_t)threads) {
+      double ndx = ndxRef;
+#pragma omp parallel num_threads(threads)
+      for (size_t c = 0; c + 1 < colors.size(); ++c) {
+#pragma omp for schedule(static)
+        for (int pi = colors[c]; pi < colors[c + 1]; ++pi) {
+          const int i = perm[pi];
+          if (skip[i]) {
+            --skip[i];
+            continue;
+          }
+          double lx[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+          double lb[3];
+          for (int k = 0; k < 3; ++k) lb[k] = b[3 * i + k] - reg[i] * lx[k];
+          splitRowMultiply(*W, i, x, lb);
+          double ldx[3] = {-lx[0], -lx[1], -lx[2]};
+          const bool ok = lawSolveLocal(law.desaxce, law.strat, &local[9 * (size_t)i], lb, lx, law.mu[i], scaling[i]);
+          for (int k = 0; k < 3; ++k) ldx[k] = ldx[k] + lx[k];
+          if (!ok) {
+            ldx[0] *= .5; ldx[1] *= .5; ldx[2] *= .5;
+          }
+          for (int k = 0; k < 3; ++k) x[3 * i + k] = x[3 * i + k] + ldx[k];
+          const double s2 = scaling[i] * scaling[i];
+          const double nx2 = s2 * sq3(lx);
+          const double ndx2 = s2 * sq3(ldx);
+          double ref;
+#pragma omp atomic read
+          ref = ndx;
+          if (ndx2 > ref) {
+#pragma omp atomic write
+            ndx = ndx2;
+            ref = ndx2;
+          }
+          if (dmin(nx2, ndx2) < absSkipTol || ndx2 < skipTol * dmin(nx2, ref))
+            skip[i] = (unsigned char)absSkipIters;
+        }
+      }
+      ndxRef = ndx;
+      return;
+    }
     for (size_t c = 0; c + 1 < colors.size(); ++c) {
       for (int pi = colors[c]; pi < colors[c + 1]; ++pi) {
         const int i = perm[pi];
@@ -218,6 +266,7 @@ struct GaussSeidel : SolverBase {
     std::vector<unsigned char> skip(N, 0);
     double ndxRef = 0;
     unsigned GSIter;
+    const auto t0 = std::chrono::steady_clock::now();
     for (GSIter = 1; GSIter <= maxIters; ++GSIter) {
       innerLoop(law, b, skip, ndxRef, x);
       if (0 == (GSIter % evalEvery)) {
@@ -228,6 +277,7 @@ struct GaussSeidel : SolverBase {
         ndxRef /= evalEvery;
       }
     }
+    sweepSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (GSIter > maxIters) std::copy(x_best.begin(), x_best.end(), x);
     if (itersOut) *itersOut = GSIter > maxIters ? maxIters : GSIter;
     return err_best;
