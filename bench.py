@@ -553,7 +553,7 @@ def run_admm(args) -> None:
         "workload": "admm_200k_contacts", "iterations": st["iterations"], "residual": res,
         "gpu_ms": st["device_ms"], "gpu_ms_per_iteration": st["device_ms"] / max(1, st["iterations"]),
         "algorithmic_gbs": st["algorithmic_bytes"] / (st["device_ms"] * 1e-3) / 1e9,
-        "cpu_oracle_ms": cpu_ms, "cpu_cores": 1, "identical": bool(res == res_o),
+        "cpu_oracle_ms": cpu_ms, "cpu_cores": pyoracle.num_threads(), "identical": bool(res == res_o),
         "timing": f"best of {args.steps} after {args.warmup} warm-up solves (CUDA events); oracle once"}),
         flush=True)
 
@@ -591,7 +591,7 @@ def run_dama(args) -> None:
         "workload": "dual_ama_200k_contacts", "iterations": st["iterations"], "residual": res,
         "gpu_ms": st["device_ms"], "gpu_ms_per_iteration": st["device_ms"] / max(1, st["iterations"]),
         "algorithmic_gbs": st["algorithmic_bytes"] / (st["device_ms"] * 1e-3) / 1e9,
-        "cpu_oracle_ms": cpu_ms, "cpu_cores": 1,
+        "cpu_oracle_ms": cpu_ms, "cpu_cores": pyoracle.num_threads(),
         "identical": bool(res == res_o and np.array_equal(v, v_o) and np.array_equal(r, r_o)),
         "timing": f"best of {args.steps} after {args.warmup} warm-up solves (CUDA events); oracle once"}),
         flush=True)

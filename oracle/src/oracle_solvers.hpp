@@ -795,9 +795,10 @@ struct ADMMSolver {
   bool useInfinityNorm = false;
   Callback callback;
 
-  // ut = w + H v
+  // ut = w + H v (contacts independent; OpenMP threads)
   void Hmul(const double* v, const double* w, double* ut) const {
     const int n = P->ncontacts, d = P->ndof;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
       int bodies[2]; const double* H[2]; int nb;
       contactBodies(*P, i, bodies, H, nb);
@@ -809,25 +810,56 @@ struct ADMMSolver {
       }
     }
   }
-  // out = init + H^T r, accumulated body by body over its contacts in increasing contact index
-  void HTmul(const double* r, const double* init, double* out) const {
-    const int n = P->ncontacts, d = P->ndof;
-    const size_t m = (size_t)P->nbodies * d;
-    for (size_t k = 0; k < m; ++k) out[k] = init ? init[k] : 0.0;
+  // out = init + H^T r, accumulated body by body over its (contact, slot) pairs in increasing contact index,
+  // then slot: each body gathers its own pairs (bodyPairs), so the bodies run on OpenMP threads with the order
+  // of the sequential scatter over contacts.
+  mutable std::vector<int> pairPtr, pairContact, pairSlot;
+  void bodyPairs() const {
+    if (!pairPtr.empty()) return;
+    const int n = P->ncontacts, nbod = P->nbodies;
+    pairPtr.assign(nbod + 1, 0);
     for (int i = 0; i < n; ++i) {
       int bodies[2]; const double* H[2]; int nb;
       contactBodies(*P, i, bodies, H, nb);
-      for (int t = 0; t < nb; ++t)
+      for (int t = 0; t < nb; ++t) ++pairPtr[bodies[t] + 1];
+    }
+    for (int b = 0; b < nbod; ++b) pairPtr[b + 1] += pairPtr[b];
+    pairContact.assign(pairPtr[nbod], 0);
+    pairSlot.assign(pairPtr[nbod], 0);
+    std::vector<int> cur(pairPtr.begin(), pairPtr.end() - 1);
+    for (int i = 0; i < n; ++i) {
+      int bodies[2]; const double* H[2]; int nb;
+      contactBodies(*P, i, bodies, H, nb);
+      for (int t = 0; t < nb; ++t) {
+        const int p = cur[bodies[t]]++;
+        pairContact[p] = i;
+        pairSlot[p] = t;
+      }
+    }
+  }
+  void HTmul(const double* r, const double* init, double* out) const {
+    const int d = P->ndof, nbod = P->nbodies;
+    bodyPairs();
+#pragma omp parallel for schedule(static)
+    for (int b = 0; b < nbod; ++b) {
+      for (int q = 0; q < d; ++q) out[(size_t)b * d + q] = init ? init[(size_t)b * d + q] : 0.0;
+      for (int p = pairPtr[b]; p < pairPtr[b + 1]; ++p) {
+        const int i = pairContact[p];
+        int bodies[2]; const double* H[2]; int nb;
+        contactBodies(*P, i, bodies, H, nb);
+        const double* Ht = H[pairSlot[p]];
         for (int q = 0; q < d; ++q) {
-          double a = out[(size_t)bodies[t] * d + q];
-          for (int rr = 0; rr < 3; ++rr) a = std::fma(H[t][rr * d + q], r[3 * i + rr], a);
-          out[(size_t)bodies[t] * d + q] = a;
+          double a = out[(size_t)b * d + q];
+          for (int rr = 0; rr < 3; ++rr) a = std::fma(Ht[rr * d + q], r[3 * i + rr], a);
+          out[(size_t)b * d + q] = a;
         }
+      }
     }
   }
   // res = proxInv (rhs - f), block diagonal
   void prox(const std::vector<double>& proxInv, const double* rhs, const double* f, double* res) const {
     const int d = P->ndof;
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < P->nbodies; ++k) {
       double t[16];
       for (int q = 0; q < d; ++q) t[q] = rhs[(size_t)k * d + q] - f[(size_t)k * d + q];
@@ -870,8 +902,11 @@ struct ADMMSolver {
     double res = -1;
     std::vector<double> ut(n3), prox_arg(m), z(n3), y(n3), y_prev(n3), zacc, z_prev, tmp(n3);
     Hmul(x, w, ut.data());
+    #pragma omp parallel for schedule(static)
     for (size_t k = 0; k < n3; ++k) z[k] = ut[k] - inv_gamma * r[k];
+    #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) projectCone(invMu[i], &z[3 * i]);
+    #pragma omp parallel for schedule(static)
     for (size_t k = 0; k < n3; ++k) y_prev[k] = -inv_gamma * r[k];
     zacc = z;
     z_prev = z;
@@ -883,16 +918,19 @@ struct ADMMSolver {
       if (lambda < kEps) {
         HTmul(r, nullptr, prox_arg.data());
       } else {
+        #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < n3; ++k) tmp[k] = std::fma(gamma, zacc[k] - ut[k], r[k]);
         // prox_arg = x / lambda ... multiply<true>(ut, prox_arg, 1, 1/lambda): prox_arg = (1/lambda) x + H^T ut
         std::vector<double> sx(m);
         const double il = 1. / lambda;
+        #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < m; ++k) sx[k] = il * x[k];
         HTmul(tmp.data(), sx.data(), prox_arg.data());
       }
       prox(proxInv, prox_arg.data(), f, x);
       Hmul(x, w, ut.data());
       // eval(law, r, ut): per contact FB(1/mu, ut_i (scaling 1), r_i) with SOC law
+#pragma omp parallel for schedule(static)
       for (int i = 0; i < n; ++i) {
         const double sc = scalings.empty() ? 1.0 : scalings[i];
         const double lx[3] = {ut[3 * i] * sc, ut[3 * i + 1] * sc, ut[3 * i + 2] * sc};
@@ -900,6 +938,7 @@ struct ADMMSolver {
       }
       double e = useInfinityNorm ? maxOf(ev.data(), n) : canonicalSum(ev.data(), n) / (double)(1 + n);
       std::vector<double> gap(n);
+#pragma omp parallel for schedule(static)
       for (int i = 0; i < n; ++i) {
         const double d3[3] = {ut[3 * i] - z[3 * i], ut[3 * i + 1] - z[3 * i + 1], ut[3 * i + 2] - z[3 * i + 2]};
         gap[i] = useInfinityNorm ? dmax(dmax(std::fabs(d3[0]), std::fabs(d3[1])), std::fabs(d3[2])) : sq3(d3);
@@ -907,19 +946,26 @@ struct ADMMSolver {
       res = e + (useInfinityNorm ? maxOf(gap.data(), n) : canonicalSum(gap.data(), n) / (double)(1 + n3));
       if (callback) callback(it, res);
       if (res < tol) break;
+      #pragma omp parallel for schedule(static)
       for (size_t k = 0; k < n3; ++k) z[k] = ut[k] - inv_gamma * r[k];
+      #pragma omp parallel for schedule(static)
       for (int i = 0; i < n; ++i) projectCone(invMu[i], &z[3 * i]);
       if (accelerated && res < res_prev) {
+        #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < n3; ++k) y[k] = (ut[k] - z[k]) - inv_gamma * r[k];
         const double beta = nesterovInertia(theta_prev, 0.);
+        #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < n3; ++k) r[k] = -gamma * std::fma(beta, y[k] - y_prev[k], y[k]);
         y_prev = y;
+        #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < n3; ++k) zacc[k] = std::fma(beta, z[k] - z_prev[k], z[k]);
         z_prev = z;
       } else {
+        #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < n3; ++k) r[k] = std::fma(gamma, z[k] - ut[k], r[k]);
         zacc = z;
         z_prev = z;
+        #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < n3; ++k) y_prev[k] = -inv_gamma * r[k];
         theta_prev = 1;
       }
@@ -959,6 +1005,7 @@ struct DualAMASolver {
 
   void Mmul(const std::vector<double>& M, const double* v, double* out) const {
     const int d = P->ndof;
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < P->nbodies; ++k)
       for (int a = 0; a < d; ++a) {
         double acc = 0.0;
@@ -983,6 +1030,7 @@ struct DualAMASolver {
     double theta_prev = 1., res_prev = -1;
     // dof norms: each body's dofs left to right, then the canonical sum over bodies (or the maximum)
     auto dofnorm = [&](const std::vector<double>& a) {
+      #pragma omp parallel for schedule(static)
       for (int b = 0; b < nb; ++b) {
         double p = 0.0;
         for (int k = 0; k < d; ++k) {
@@ -994,6 +1042,7 @@ struct DualAMASolver {
       return useInfinityNorm ? maxOf(zz.data(), nb) : canonicalSum(zz.data(), nb);
     };
     auto sqnorm = [&](const std::vector<double>& a) {
+      #pragma omp parallel for schedule(static)
       for (int b = 0; b < nb; ++b) {
         double p = 0.0;
         for (int k = 0; k < d; ++k) p = p + a[(size_t)b * d + k] * a[(size_t)b * d + k];
@@ -1005,9 +1054,12 @@ struct DualAMASolver {
     unsigned it;
     for (it = 0; it < maxIters; ++it) {
       Mmul(M, v, Mv.data());
+      #pragma omp parallel for schedule(static)
       for (size_t k = 0; k < m; ++k) x[k] = f[k] + Mv[k];
+      #pragma omp parallel for schedule(static)
       for (size_t k = 0; k < m; ++k) z[k] = HrBp[k] - x[k];
       h.Hmul(v, w, ut.data());
+#pragma omp parallel for schedule(static)
       for (int i = 0; i < n; ++i) {
         const double sc = scalings.empty() ? 1.0 : scalings[i];
         const double lx[3] = {r[3 * i] * sc, r[3 * i + 1] * sc, r[3 * i + 2] * sc};
@@ -1030,29 +1082,37 @@ struct DualAMASolver {
       else theta_prev = 1;
       // g = ut + COV(ut) + gamma H z
       h.Hmul(z.data(), nullptr, Hz.data());
+#pragma omp parallel for schedule(static)
       for (int i = 0; i < n; ++i) {
         double s[3];
         dualityCOV(desaxce, mu[i], &ut[3 * i], s);
         for (int k = 0; k < 3; ++k) g[3 * i + k] = std::fma(gamma, Hz[3 * i + k], ut[3 * i + k] + s[k]);
       }
       if (lsIters == 0) {
+        #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < n3; ++k) r[k] = r[k] - lambda * g[k];
+        #pragma omp parallel for schedule(static)
         for (int i = 0; i < n; ++i) projectCone(mu[i], &r[3 * i]);
         h.HTmul(r, nullptr, HrBp.data());
       } else {
+        #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < m; ++k) gap[k] = HrBp[k] - x[k];
         const double h0 = sqnorm(gap);  // the squared norm, whatever the residual's norm
         lambda *= lsOptimisticFactor;
         for (unsigned ls = 0; ls < lsIters; ++ls) {
+          #pragma omp parallel for schedule(static)
           for (size_t k = 0; k < n3; ++k) rs[k] = r[k] - lambda * g[k];
+#pragma omp parallel for schedule(static)
           for (int i = 0; i < n; ++i) projectCone(mu[i], &rs[3 * i]);
           h.HTmul(rs.data(), nullptr, HrBp.data());
+          #pragma omp parallel for schedule(static)
           for (size_t k = 0; k < m; ++k) {
             const double zk = HrBp[k] - x[k];
             const double yk = v[k] + gamma * zk;
             y[k] = yk + beta * (yk - y_prev[k]);
           }
           Mmul(M, y.data(), tmp.data());
+          #pragma omp parallel for schedule(static)
           for (size_t k = 0; k < m; ++k) gap[k] = (HrBp[k] - f[k]) - tmp[k];
           const double hh = sqnorm(gap);
           if (hh < h0) break;
@@ -1060,6 +1120,7 @@ struct DualAMASolver {
         }
         std::copy(rs.begin(), rs.end(), r);
       }
+      #pragma omp parallel for schedule(static)
       for (size_t k = 0; k < m; ++k) {
         z[k] = HrBp[k] - x[k];
         const double yk = v[k] + gamma * z[k];
