@@ -239,6 +239,46 @@ __device__ __forceinline__ bool grid_barrier(const GridBarrier& gb, LastFn&& las
   return ok;
 }
 
+// The stripe stage of the canonical reduction, for a CTA that combines stripes role, role + m, ... < 8:
+// warp q < K reduces quantity q (chunk sums at s + q * stride; count0 chunks for q = 0, count1 for q > 0),
+// stripes of ceil(count / 8) chunks, lane l adding chunks start + l, start + l + 32, ... in turn from 0
+// (sum, or maximum where bit q of maxmask is set), then a butterfly; the stripe sum goes to
+// stripes[8 q + stripe]. Loads are issued 8 (then 4) per lane ahead of their additions, which keep the order.
+__device__ __forceinline__ void combine_stripes(const double* s, size_t stride, int count0, int count1, int K,
+                                                unsigned maxmask, int role, int m, double* stripes) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp >= K) return;
+  const int C = warp == 0 ? count0 : count1;
+  const int per = (C + 7) / 8;
+  const bool mx = (maxmask >> warp) & 1u;
+  const double* q = s + (size_t)warp * stride;
+  for (int st = role; st < 8; st += m) {
+    const int e = min(C, st * per + per);
+    double p = 0.0;
+    int c = st * per + lane;
+    for (; c + 224 < e; c += 256) {
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = ldcg(q + c + 32 * u);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) p = mx ? ((v[u] < p) ? p : v[u]) : p + v[u];
+    }
+    for (; c + 96 < e; c += 128) {
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = ldcg(q + c + 32 * u);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) p = mx ? ((v[u] < p) ? p : v[u]) : p + v[u];
+    }
+    for (; c < e; c += 32) {
+      const double v = ldcg(q + c);
+      p = mx ? ((v < p) ? p : v) : p + v;
+    }
+    p = mx ? warp_max_butterfly(p) : warp_sum_butterfly(p);
+    if (lane == 0) stripes[8 * warp + st] = p;
+  }
+}
+
 // Bounded grid barrier that also reduces K <= 4 quantities of chunk sums into out[0..K) in the canonical
 // order of block8_combine / block8_combine_k. Quantity q's sums are at s + q * stride, over count0 chunks for
 // q = 0 and count1 chunks for q > 0. Each is split into 8 stripes of ceil(count / 8) chunks, lane l of a stripe
@@ -283,38 +323,7 @@ __device__ __forceinline__ bool grid_barrier_combine(const GridBarrier& gb, unsi
   }
   __syncthreads();
   if (s_role >= 0 && s_ok) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int C = warp == 0 ? count0 : count1;
-    const int per = (C + 7) / 8;
-    for (int st = s_role; st < 8; st += (int)m) {
-      if (warp < K) {
-        const bool mx = (maxmask >> warp) & 1u;
-        const double* q = s + (size_t)warp * stride;
-        const int e = min(C, st * per + per);
-        double p = 0.0;
-        int c = st * per + lane;
-        for (; c + 224 < e; c += 256) {  // 8 loads in flight per lane, added in chunk order
-          double v[8];
-#pragma unroll
-          for (int u = 0; u < 8; ++u) v[u] = ldcg(q + c + 32 * u);
-#pragma unroll
-          for (int u = 0; u < 8; ++u) p = mx ? ((v[u] < p) ? p : v[u]) : p + v[u];
-        }
-        for (; c + 96 < e; c += 128) {
-          double v[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) v[u] = ldcg(q + c + 32 * u);
-#pragma unroll
-          for (int u = 0; u < 4; ++u) p = mx ? ((v[u] < p) ? p : v[u]) : p + v[u];
-        }
-        for (; c < e; c += 32) {
-          const double v = ldcg(q + c);
-          p = mx ? ((v < p) ? p : v) : p + v;
-        }
-        p = mx ? warp_max_butterfly(p) : warp_sum_butterfly(p);
-        if (lane == 0) stripes[8 * warp + st] = p;
-      }
-    }
+    combine_stripes(s, stride, count0, count1, K, maxmask, s_role, (int)m, stripes);
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
@@ -443,31 +452,7 @@ __device__ __forceinline__ bool mono_barrier_combine(const MonoBarrier& mb, unsi
   __syncthreads();
   if (s_last) last_fn();
   if (s_role >= 0 && s_ok) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int C = warp == 0 ? count0 : count1;
-    const int per = (C + 7) / 8;
-    for (int st = s_role; st < 8; st += (int)m) {
-      if (warp < K) {
-        const bool mx = (maxmask >> warp) & 1u;
-        const double* q = s + (size_t)warp * stride;
-        const int e = min(C, st * per + per);
-        double p = 0.0;
-        int c = st * per + lane;
-        for (; c + 224 < e; c += 256) {  // 8 loads in flight per lane, added in chunk order
-          double v[8];
-#pragma unroll
-          for (int u = 0; u < 8; ++u) v[u] = ldcg(q + c + 32 * u);
-#pragma unroll
-          for (int u = 0; u < 8; ++u) p = mx ? ((v[u] < p) ? p : v[u]) : p + v[u];
-        }
-        for (; c < e; c += 32) {
-          const double v = ldcg(q + c);
-          p = mx ? ((v < p) ? p : v) : p + v;
-        }
-        p = mx ? warp_max_butterfly(p) : warp_sum_butterfly(p);
-        if (lane == 0) stripes[8 * warp + st] = p;
-      }
-    }
+    combine_stripes(s, stride, count0, count1, K, maxmask, s_role, (int)m, stripes);
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
