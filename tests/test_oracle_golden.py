@@ -384,3 +384,54 @@ def test_small_friction_dual_ama(oracle, golden, name, variant_acc, ls, proj, co
     assert res < 1e-8, name
     if coulomb:
         assert isApprox(s["sol"], r, 1e-4), name
+
+
+def test_oracle_threads_do_not_change_primal_solvers(oracle):
+    """The oracle's ADMM and DualAMA run their H, H^T, body and contact loops on OpenMP threads; every result
+    must be the same bit for bit whatever the thread count (H^T r gathers each body's contacts in the order
+    of the sequential scatter), since the GPU parity tests compare against it."""
+    from bogus_gpu import generator
+
+    d = generator.grid(nbodies=600, ncontacts=2_400, seed=9)
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    mass = np.linalg.inv(d.minv)
+    f = np.random.default_rng(2).standard_normal(d.nbodies * 6) * 0.1
+    w = d.b.reshape(-1)
+    saved = oracle.num_threads()
+    outs = []
+    try:
+        for t in (1, 3, max(2, saved)):
+            oracle.set_num_threads(t)
+            a = P.solve_admm(d.minv, 0.0, d.mu, np.zeros(d.nbodies * 6), w, np.zeros(d.nbodies * 6),
+                             np.zeros(3 * d.n), max_iters=30)
+            b = P.solve_dual_ama(mass, d.mu, f, w, np.zeros(d.nbodies * 6), np.zeros(3 * d.n), max_iters=30)
+            outs.append((a, b))
+    finally:
+        oracle.set_num_threads(saved)
+    for (a, b) in outs[1:]:
+        assert a[0] == outs[0][0][0] and a[3] == outs[0][0][3]
+        assert np.array_equal(a[1], outs[0][0][1]) and np.array_equal(a[2], outs[0][0][2])
+        assert b[0] == outs[0][1][0] and b[3] == outs[0][1][3]
+        assert np.array_equal(b[1], outs[0][1][1]) and np.array_equal(b[2], outs[0][1][2])
+
+
+def test_parallel_colored_gauss_seidel_timing_path(oracle):
+    """The timing-only per-color OpenMP sweep (the reference's parallel loop) reaches the sequential sweep's
+    accuracy; its iterates may differ (the shared step-size reference decides which contacts skip)."""
+    from bogus_gpu import generator
+
+    d = generator.grid(nbodies=1_500, ncontacts=6_000, seed=3)
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    rp, cl, vl = P.assemble()
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    res_seq, _, _ = O.solve_gs(np.zeros(3 * d.n), max_iters=50, coloring=True)
+    assert oracle.last_gs_sweep_ms() > 0.0
+    try:
+        oracle.set_gs_threads(4)
+        res_par, r_par, _ = O.solve_gs(np.zeros(3 * d.n), max_iters=50, coloring=True)
+    finally:
+        oracle.set_gs_threads(1)
+    assert np.all(np.isfinite(r_par))
+    assert res_par < 2.0 * res_seq + 1e-12
+    res_again, _, _ = O.solve_gs(np.zeros(3 * d.n), max_iters=50, coloring=True)
+    assert res_again == res_seq  # back to the sequential sweep
