@@ -169,6 +169,7 @@ struct bogus_gpu_problem {
   bool admm_incidence_valid = false;
   size_t admm_ninc = 0;
   DevBuf<int> bptr, bent;
+  DevBuf<int> border;  // bodies by decreasing contact count (the ADMM body phase's lane order)
   DevBuf<double> a_prox, a_f, a_w, a_mu, a_invmu, a_x, a_r, a_ut, a_z, a_zacc, a_zprev, a_yprev;
   DevBuf<ADMMOut> admm_out;
   // error-function scalings of ADMM / DualAMA (ConstrainedSolverBase::updateScalings), per contact, and the
@@ -920,6 +921,7 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
     b->release();
   h->bptr.release();
   h->bent.release();
+  h->border.release();
   h->admm_out.release();
   h->cad_b.release();
   for (auto* b : {&h->meche_E, &h->meche_w, &h->meche_r, &h->meche_v, &h->meche_fd}) b->release();
@@ -2152,6 +2154,18 @@ int ensure_incidence(bogus_gpu_problem* h) {
   BG_CUDA(h->bent.ensure(be.size()));
   BG_CUDA(cudaMemcpyAsync(h->bptr.p, bp.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, s));
   BG_CUDA(cudaMemcpyAsync(h->bent.p, be.data(), sizeof(int) * be.size(), cudaMemcpyHostToDevice, s));
+  // bodies by decreasing contact count, stable: a warp's 32 bodies then loop over about as many contacts
+  // each, so the lanes of the H^T r loop stay busy (a body's own arithmetic does not depend on the order)
+  {
+    int maxdeg = 0;
+    for (int k = 0; k < nb; ++k) maxdeg = std::max(maxdeg, bp[k + 1] - bp[k]);
+    std::vector<int> cnt(maxdeg + 2, 0), ord(nb > 0 ? nb : 1);
+    for (int k = 0; k < nb; ++k) ++cnt[maxdeg - (bp[k + 1] - bp[k]) + 1];
+    for (int q = 0; q <= maxdeg; ++q) cnt[q + 1] += cnt[q];
+    for (int k = 0; k < nb; ++k) ord[cnt[maxdeg - (bp[k + 1] - bp[k])]++] = k;
+    BG_CUDA(h->border.ensure(ord.size()));
+    BG_CUDA(cudaMemcpyAsync(h->border.p, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice, s));
+  }
   // scalings (ConstrainedSolverBase.impl.hpp:84-118): 1, unless H is square at the block level (3 n rows ==
   // the bodies' dofs, n == nbodies), where contact i with a block on body i takes max(1, trace / 3) of it
   const int d = h->ndof;
@@ -2525,6 +2539,7 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   a.H = h->H.p;
   a.bptr = h->bptr.p;
   a.bent = h->bent.p;
+  a.border = h->border.p;
   a.prox = prox ? h->a_prox.p : h->minv.p;
   a.f = f ? h->a_f.p : nullptr;
   a.w = h->a_w.p;

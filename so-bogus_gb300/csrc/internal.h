@@ -197,6 +197,7 @@ struct ADMMArgs {
   const double* H;     // 2 n x 3 x d: slot blocks, row-major
   const int* bptr;     // nbodies + 1
   const int* bent;     // incidences of each body, increasing contact index: 2 i + slot
+  const int* border;   // nbodies: the order in which the body phase takes the bodies (null: natural)
   const double* prox;  // nbodies x d x d: the prox operator's blocks (M^-1)
   const double* f;     // nbodies x d, or null (f = 0)
   const double* w;     // 3 n

@@ -121,10 +121,11 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
   double theta_prev = 1., res_prev = -1., res = -1.;
   unsigned it = 0;
   for (it = 0; it < a.max_iters; ++it) {
-    // P1: x = prox(prox_arg) per body
+    // P1: x = prox(prox_arg) per body (lane order a.border: bodies of similar contact counts share a warp)
     for (int c = gwarp; c < CB; c += nwarps) {
-      const int b = 32 * c + lane;
-      if (b < a.nbodies) {
+      const int slot = 32 * c + lane;
+      if (slot < a.nbodies) {
+        const int b = a.border ? __ldg(a.border + slot) : slot;
         double acc[DM];
         const double* xb = a.x + (size_t)b * d;
 #pragma unroll
