@@ -144,7 +144,10 @@ int bogus_gpu_destroy(bogus_gpu_problem* h);
 int bogus_gpu_set_dual(bogus_gpu_problem* h, int n, const int* rowptr, const int* colidx, const double* blocks,
                        int symmetric_lower, const double* b, const double* mu);
 
-/* Same, from device pointers (full both-triangle BSR already on the device; copied into the handle). */
+/* Same, from device pointers (full both-triangle BSR already on the device; copied into the handle). The
+ * arrays are checked on the device before the copy: row pointers in order and in range, columns in range and
+ * strictly increasing, a diagonal block in every row (BOGUS_GPU_BAD_INPUT otherwise), finite W, b and mu
+ * (BOGUS_GPU_NONFINITE); a rejected problem leaves the handle's problem in place. */
 int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* d_rowptr, const int* d_colidx,
                               const double* d_blocks, const double* d_b, const double* d_mu);
 
@@ -314,6 +317,11 @@ int bogus_gpu_add_compliance(bogus_gpu_problem* h, const double* c);
  * pass NULL arrays first to get the size). */
 int bogus_gpu_get_dual_lower(bogus_gpu_problem* h, int* rowptr, int* colidx, double* blocks, int* nnzb_lower);
 
+/* Copies the device-held b (3 n) and mu (n) back, in the stored order of bogus_gpu_get_dual_lower: the
+ * DualFrictionProblem members b and mu (Interfaces/FrictionProblem.hpp:145-150) after bogus_gpu_assemble_dual
+ * computed them. Either output may be NULL. */
+int bogus_gpu_get_dual_rhs(bogus_gpu_problem* h, double* b, double* mu);
+
 /* Measurements of the last solve, spmv or assembly (no counterpart in the reference, which only offers
  * MecheFrictionProblem::lastSolveTime, Interfaces/MecheInterface.hpp:173). */
 typedef struct bogus_gpu_solve_stats {
@@ -331,6 +339,21 @@ int bogus_gpu_get_solve_stats(const bogus_gpu_problem* h, bogus_gpu_solve_stats*
 /* The CUDA stream (cudaStream_t) the handle launches on, so callers can order and time their own work
  * with it (no counterpart in the reference). */
 int bogus_gpu_get_stream(const bogus_gpu_problem* h, void** stream);
+
+/* Limit of every device-side wait of the library's kernels on `device` (grid barriers of the persistent
+ * solvers, the Gauss-Seidel sweep's flag waits), in seconds within [1e-6, 3600]; default 4. A wait that runs
+ * out makes the kernel record BOGUS_GPU_TIMEOUT and return, and the call reports TIMEOUT; the CUDA context
+ * stays usable. The setting holds for every handle and the allocation-free entry point on that device until
+ * changed; set it while no solve runs there. The caller's current device is left as it was. No counterpart
+ * in the reference (its solvers run on the host). */
+int bogus_gpu_set_wait_limit(int device, double seconds);
+
+/* Test of the timeout path (no counterpart in the reference). While `on` is non-zero, the single-problem
+ * projected-gradient solves of this handle (bogus_gpu_solve_pg / _pg_device, FP64) launch their kernel with
+ * barriers that wait for one CTA more than the launch holds: the first barrier can never complete, its
+ * bounded wait runs out after the wait limit, and the solve returns BOGUS_GPU_TIMEOUT without touching r.
+ * Turn it off to solve normally again on the same handle. */
+int bogus_gpu_test_wait_timeout(bogus_gpu_problem* h, int on);
 
 /* Measures the FP64 fused multiply-add throughput of `device` in TFLOP/s: the ceiling of the FP64 kernels
  * on GPUs whose FP64 rate is below their memory bandwidth's need (no counterpart in the reference). */
@@ -355,6 +378,12 @@ int bogus_gpu_check_fp64_ops(int device, long long n, unsigned long long seed, l
  *    current; make that first call before any stream capture.
  *  - Calls on one device share the array and it keeps the last call's contents (each call clears what must
  *    start at zero): calls whose GPU work overlaps race and must not be issued.
+ *  - The remembered address lives in the device's CUDA context: after cudaDeviceReset on that device the
+ *    entry point must not be called again in the process.
+ *  - W, b, mu and r are checked on the device first (row pointers in order and in range, columns in range and
+ *    strictly increasing, a diagonal block in every row, finite values); a malformed W returns
+ *    BOGUS_GPU_BAD_INPUT and a non-finite value BOGUS_GPU_NONFINITE, with r untouched.
+ *  - `device` is made current for the call's work; the caller's current device is restored before returning.
  *  - No callback. stream: a cudaStream_t, or NULL for the default stream; the call returns when the solve is
  *    done and r holds the result. */
 #define BOGUS_GPU_NOALLOC_MAX_CONTACTS 65536

@@ -104,6 +104,7 @@ EXPORTED = [
     "bogus_gpu_meche_options_default", "bogus_gpu_meche_from_primal", "bogus_gpu_meche_solve",
     "bogus_gpu_solve_product_gs", "bogus_gpu_dual_ama_options_default", "bogus_gpu_solve_dual_ama",
     "bogus_gpu_set_body_dofs", "bogus_gpu_set_frames", "bogus_gpu_apply_permutation", "bogus_gpu_undo_permutation", "bogus_gpu_permuted",
+    "bogus_gpu_set_wait_limit", "bogus_gpu_test_wait_timeout", "bogus_gpu_get_dual_rhs",
 ]
 
 
@@ -181,6 +182,9 @@ def lib():
                                                   np.ctypeslib.ndpointer(dtype=np.uint32)]
     L.bogus_gpu_solve_pg_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, C.POINTER(PgOptions), vp,
                                              C.POINTER(C.c_double), C.POINTER(C.c_uint), vp]
+    L.bogus_gpu_set_wait_limit.argtypes = [C.c_int, C.c_double]
+    L.bogus_gpu_test_wait_timeout.argtypes = [vp, C.c_int]
+    L.bogus_gpu_get_dual_rhs.argtypes = [vp, vp, vp]
     _lib = L
     return L
 

@@ -207,6 +207,7 @@ struct bogus_gpu_problem {
   DevBuf<double> team_scal;
   bogus_gpu_callback callback = nullptr;
   void* callback_user = nullptr;
+  bool test_wait_timeout = false;  // bogus_gpu_test_wait_timeout
   float last_ms = 0.f;
   unsigned last_launches = 0;
   bogus_gpu_solve_stats last_stats{};
@@ -470,6 +471,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.pess = o->ls_pessimistic_factor;
   a.max_iters = o->max_iters;
   a.ls_iters = o->ls_iters;
+  a.phantom_ctas = h->test_wait_timeout ? 1u : 0u;
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 16 * sizeof(unsigned), h->stream));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
   int grid = pg_max_grid(h->device, false, true);
@@ -997,7 +999,27 @@ int bogus_gpu_set_dual_device(bogus_gpu_problem* h, int n, int nnzb, const int* 
                               const double* d_blocks, const double* d_b, const double* d_mu) {
   if (int e = check_handle(h)) return e;
   if (n < 0 || nnzb < 0) return fail(BOGUS_GPU_BAD_INPUT, "negative size");
+  if (n > 0 && (!d_rowptr || !d_b || !d_mu || (nnzb > 0 && (!d_colidx || !d_blocks))))
+    return fail(BOGUS_GPU_BAD_INPUT, "null device pointer");
   if (int e = set_device(h)) return e;
+  {
+    // the caller's arrays are checked where they lie, before anything is copied: a rejected problem leaves the
+    // handle's problem in place
+    cudaStream_t s = h->stream;
+    BG_CUDA(h->pat_check.ensure(2));
+    BG_CUDA(launch_check_full(n, nnzb, d_rowptr, d_colidx, h->pat_check.p, s));
+    BG_CUDA(cudaMemsetAsync(h->pat_check.p + 1, 0, sizeof(int), s));
+    BG_CUDA(launch_any_nonfinite(9 * (size_t)nnzb, d_blocks, h->pat_check.p + 1, s));
+    BG_CUDA(launch_any_nonfinite(3 * (size_t)n, d_b, h->pat_check.p + 1, s));
+    BG_CUDA(launch_any_nonfinite((size_t)n, d_mu, h->pat_check.p + 1, s));
+    int check[2] = {0, 0};
+    BG_CUDA(cudaMemcpyAsync(check, h->pat_check.p, sizeof(check), cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaStreamSynchronize(s));
+    if (n > 0 && check[0] < n)
+      return fail(BOGUS_GPU_BAD_INPUT, "row " + std::to_string(check[0]) + " of W is malformed (row pointers out of "
+                  "order or range, a column out of range or not increasing, or no diagonal block)");
+    if (check[1]) return fail(BOGUS_GPU_NONFINITE, "non-finite value in W, b or mu");
+  }
   BG_CUDA(h->rowptr.ensure(n + 1));
   BG_CUDA(h->col.ensure(nnzb));
   BG_CUDA(h->val.ensure(9 * (size_t)nnzb));
@@ -3226,6 +3248,18 @@ int bogus_gpu_get_dual_lower(bogus_gpu_problem* h, int* rowptr, int* colidx, dou
   return BOGUS_GPU_OK;
 }
 
+int bogus_gpu_get_dual_rhs(bogus_gpu_problem* h, double* b, double* mu) {
+  if (int e = check_handle(h)) return e;
+  if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
+  const int n = h->W.n;
+  if (n == 0) return BOGUS_GPU_OK;
+  if (int e = set_device(h)) return e;
+  if (b) BG_CUDA(cudaMemcpyAsync(b, h->b.p, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+  if (mu) BG_CUDA(cudaMemcpyAsync(mu, h->mu.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  return BOGUS_GPU_OK;
+}
+
 int bogus_gpu_get_solve_stats(const bogus_gpu_problem* h, bogus_gpu_solve_stats* out) {
   if (int e = check_handle(h)) return e;
   if (!out) return fail(BOGUS_GPU_BAD_INPUT, "null output");
@@ -3239,6 +3273,31 @@ int bogus_gpu_get_stream(const bogus_gpu_problem* h, void** stream) {
   if (int e = check_handle(h)) return e;
   if (!stream) return fail(BOGUS_GPU_BAD_INPUT, "null output");
   *stream = (void*)h->stream;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_set_wait_limit(int device, double seconds) {
+  if (!(seconds >= 1e-6 && seconds <= 3600.0))
+    return fail(BOGUS_GPU_BAD_INPUT, "wait limit must lie in [1e-6, 3600] seconds");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
+    return fail(BOGUS_GPU_NO_DEVICE, "no such CUDA device");
+  int prev = -1;
+  BG_CUDA(cudaGetDevice(&prev));
+  BG_CUDA(cudaSetDevice(device));
+  const unsigned long long ns = (unsigned long long)(seconds * 1e9);
+  cudaError_t e = set_wait_limit_pg(ns);
+  if (e == cudaSuccess) e = set_wait_limit_gs(ns);
+  if (e == cudaSuccess) e = set_wait_limit_admm(ns);
+  if (e == cudaSuccess) e = set_wait_limit_adjoint(ns);
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) return fail(BOGUS_GPU_CUDA_ERROR, std::string("setting the wait limit: ") + cudaGetErrorString(e));
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_test_wait_timeout(bogus_gpu_problem* h, int on) {
+  if (int e = check_handle(h)) return e;
+  h->test_wait_timeout = on != 0;
   return BOGUS_GPU_OK;
 }
 

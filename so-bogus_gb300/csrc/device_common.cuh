@@ -180,12 +180,24 @@ __device__ __forceinline__ void block8_combine_k(const double* s, int C, int K, 
   __syncthreads();
 }
 
+// Limit of every device-side wait (grid barriers, flag waits), in nanoseconds of %globaltimer. Each
+// translation unit holds its own copy in its module; the host sets them all, per device, through
+// bogus_gpu_set_wait_limit (the setters are defined by BOGUS_GPU_WAIT_LIMIT_SETTER in the kernel files).
+constexpr unsigned long long kDefaultWaitLimitNs = 4000000000ull;
+static __device__ unsigned long long g_wait_limit_ns = kDefaultWaitLimitNs;
+__device__ __forceinline__ unsigned long long wait_limit_ns() {
+  return *reinterpret_cast<const volatile unsigned long long*>(&g_wait_limit_ns);
+}
+#define BOGUS_GPU_WAIT_LIMIT_SETTER(name)                                 \
+  cudaError_t name(unsigned long long ns) {                               \
+    return cudaMemcpyToSymbol(g_wait_limit_ns, &ns, sizeof(ns));          \
+  }
+
 // Bounded grid barrier for cooperative launches. The last CTA to arrive runs `last_fn` (with all its
 // threads) before releasing the others, so final reductions cost one CTA's work, not a second barrier.
-// Every wait is bounded: after kBarrierTimeoutNs the waiting CTA records BOGUS_GPU_TIMEOUT in *status and
+// Every wait is bounded: after wait_limit_ns() the waiting CTA records BOGUS_GPU_TIMEOUT in *status and
 // returns false; a CTA that sees a non-zero status also returns false. All threads of a CTA get the
 // same return value.
-constexpr unsigned long long kBarrierTimeoutNs = 4000000000ull;
 
 struct GridBarrier {
   unsigned* count;
@@ -211,7 +223,7 @@ __device__ __forceinline__ bool grid_barrier(const GridBarrier& gb, LastFn&& las
       unsigned spins = 0;
       while (ld_acquire_u32(gb.gen) == my_gen) {
         if (ld_relaxed_i32(gb.status) != 0) { s_ok = 0; break; }
-        if ((++spins & 255u) == 0 && global_timer_ns() - t0 > kBarrierTimeoutNs) {
+        if ((++spins & 255u) == 0 && global_timer_ns() - t0 > wait_limit_ns()) {
           atomicCAS(gb.status, 0, (int)BOGUS_GPU_TIMEOUT);
           s_ok = 0;
           break;
@@ -311,7 +323,7 @@ __device__ __forceinline__ bool grid_barrier_combine(const GridBarrier& gb, unsi
       unsigned spins = 0;
       while (ld_acquire_u32(gb.count) < P) {
         if (ld_relaxed_i32(gb.status) != 0) { s_ok = 0; break; }
-        if ((++spins & 255u) == 0 && global_timer_ns() - t0 > kBarrierTimeoutNs) {
+        if ((++spins & 255u) == 0 && global_timer_ns() - t0 > wait_limit_ns()) {
           atomicCAS(gb.status, 0, (int)BOGUS_GPU_TIMEOUT);
           s_ok = 0;
           break;
@@ -357,7 +369,7 @@ __device__ __forceinline__ bool grid_barrier_combine(const GridBarrier& gb, unsi
     unsigned spins = 0;
     while (ld_acquire_u32(gb.gen) == s_gen) {
       if (ld_relaxed_i32(gb.status) != 0) { s_ok = 0; break; }
-      if ((++spins & 255u) == 0 && global_timer_ns() - t0 > kBarrierTimeoutNs) {
+      if ((++spins & 255u) == 0 && global_timer_ns() - t0 > wait_limit_ns()) {
         atomicCAS(gb.status, 0, (int)BOGUS_GPU_TIMEOUT);
         s_ok = 0;
         break;
@@ -393,7 +405,7 @@ __device__ __forceinline__ bool spin_until_geq(const unsigned long long* p, unsi
   unsigned spins = 0;
   while (ld_acquire_u64(p) < target) {
     if (ld_relaxed_i32(status) != 0) return false;
-    if ((++spins & 255u) == 0 && global_timer_ns() - t0 > kBarrierTimeoutNs) {
+    if ((++spins & 255u) == 0 && global_timer_ns() - t0 > wait_limit_ns()) {
       atomicCAS(status, 0, (int)BOGUS_GPU_TIMEOUT);
       return false;
     }

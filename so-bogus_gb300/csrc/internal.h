@@ -70,6 +70,9 @@ struct PGArgsT {
   int desaxce, variant, use_inf;
   double tol, opt, pess;
   unsigned max_iters, ls_iters;
+  // test of the timeout path (single-problem kernel): the barriers count this many CTAs more than the launch
+  // has, so the first one never completes and its bounded wait runs out; 0 in every solve
+  unsigned phantom_ctas;
 };
 using PGArgs = PGArgsT<double>;
 using PGArgs32 = PGArgsT<float>;
@@ -113,6 +116,9 @@ cudaError_t launch_diag_and_scaling(const DevBSR& W, double* scaling, cudaStream
 cudaError_t launch_any_nonfinite(size_t m, const double* v, int* flag, cudaStream_t s);
 cudaError_t launch_permute3(int n, const int* perm, const double* src, double* dst, bool inverse, cudaStream_t s);
 cudaError_t launch_check_lower(int n, const int* rowptr, const int* col, int* out, cudaStream_t s);
+// Structure check of a both-triangle BSR in device memory (k_check_full): *out = the smallest malformed row, or a
+// value above n when every row is well formed (rows in range and sorted, columns in [0, n), diagonal present).
+cudaError_t launch_check_full(int n, int nnzb, const int* rowptr, const int* col, int* out, cudaStream_t s);
 cudaError_t launch_full_pattern(int n, const int* rowptr, const int* col, int* upper, int* cursor, int* frowptr,
                                 int* fcol, int* src, cudaStream_t s);
 cudaError_t launch_expand_lower(int nnz, const int* src, const double* low, double* full, cudaStream_t s);
@@ -297,6 +303,12 @@ cudaError_t launch_add_diagonal(const DevBSR& W, const double* c, cudaStream_t s
 cudaError_t launch_frame(int n, const double* E, const double* x, double* y, bool transpose, cudaStream_t s);
 cudaError_t launch_meche_h(int n, int d, const double* E, const double* HAw, const double* HBw, const int* objA,
                            const int* objB, double* H, cudaStream_t s);
+
+// Device-side wait limits (nanoseconds) of the kernel files, set on the current device.
+cudaError_t set_wait_limit_pg(unsigned long long ns);
+cudaError_t set_wait_limit_gs(unsigned long long ns);
+cudaError_t set_wait_limit_admm(unsigned long long ns);
+cudaError_t set_wait_limit_adjoint(unsigned long long ns);
 
 // Records the message returned by bogus_gpu_last_error() on this thread.
 void set_last_error(const std::string& msg);

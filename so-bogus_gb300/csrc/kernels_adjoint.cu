@@ -337,4 +337,7 @@ int adjoint_max_grid(int device) {
   return per * sms;
 }
 
+// Sets this file's copy of the device-side wait limit on the current device.
+BOGUS_GPU_WAIT_LIMIT_SETTER(set_wait_limit_adjoint)
+
 }  // namespace bogus_gpu

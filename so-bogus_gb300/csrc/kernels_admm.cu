@@ -607,4 +607,7 @@ int dama_max_grid(int device, int d) {
   return per * sms;
 }
 
+// Sets this file's copy of the device-side wait limit on the current device.
+BOGUS_GPU_WAIT_LIMIT_SETTER(set_wait_limit_admm)
+
 }  // namespace bogus_gpu

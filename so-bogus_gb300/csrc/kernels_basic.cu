@@ -170,6 +170,31 @@ __global__ void k_check_lower(int n, const int* __restrict__ rowptr, const int* 
   if (k1 > k0 && col[k1 - 1] == i) atomicAdd(out + 1, 1);
 }
 
+// Structure of a both-triangle BSR handed over in device memory (rowptr: n + 1 entries, col: nnzb): every row
+// must have 0 <= rowptr[i] <= rowptr[i + 1] <= nnzb with rowptr[0] = 0 and rowptr[n] = nnzb, strictly increasing
+// columns in [0, n) and its diagonal block. out[0] receives the smallest offending row (it must start above
+// n, e.g. 0x7f7f7f7f from a byte memset). Columns are read only inside [0, nnzb), whatever rowptr holds.
+__global__ void k_check_full(int n, int nnzb, const int* __restrict__ rowptr, const int* __restrict__ col, int* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k0 = rowptr[i], k1 = rowptr[i + 1];
+  bool bad = k0 < 0 || k1 < k0 || k1 > nnzb || (i == 0 && k0 != 0) || (i == n - 1 && k1 != nnzb);
+  bool diag = false;
+  if (!bad) {
+    int prev = -1;
+    for (int k = k0; k < k1; ++k) {
+      const int j = col[k];
+      if (j < 0 || j >= n || j <= prev) {
+        bad = true;
+        break;
+      }
+      diag |= j == i;
+      prev = j;
+    }
+  }
+  if (bad || !diag) atomicMin(out, i);
+}
+
 // upper[j] = number of blocks (i, j), i > j, of the lower triangle (the transposed blocks row j receives)
 __global__ void k_count_upper(int n, const int* __restrict__ rowptr, const int* __restrict__ col, int* upper) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -282,6 +307,13 @@ __global__ void k_sort_upper(int n, const int* __restrict__ rowptr, const int* _
 cudaError_t launch_check_lower(int n, const int* rowptr, const int* col, int* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_check_lower<<<(n + 255) / 256, 256, 0, s>>>(n, rowptr, col, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_check_full(int n, int nnzb, const int* rowptr, const int* col, int* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0x7f, sizeof(int), s);
+  if (e != cudaSuccess || n <= 0) return e;
+  k_check_full<<<(n + 255) / 256, 256, 0, s>>>(n, nnzb, rowptr, col, out);
   return cudaGetLastError();
 }
 

@@ -29,7 +29,7 @@ __device__ __forceinline__ unsigned long long dbits(double v) { return (unsigned
 // (consecutive contacts of the sweep often share a body). An earlier neighbour has been visited (its flag was
 // set after its x was written), a later neighbour has not (it waits for this contact's flag), so every contact
 // sees the values of the sequential sweep. A warp waits only for contacts of lower levels, handed out before its own and so already taken by
-// running warps: the sweep always progresses. Every wait is bounded (kBarrierTimeoutNs); a wait that runs
+// running warps: the sweep always progresses. Every wait is bounded (wait_limit_ns()); a wait that runs
 // out records BOGUS_GPU_TIMEOUT and the warp stops.
 __device__ __forceinline__ bool gs_wait_done(const unsigned* f, unsigned tag, const int* status) {
   if (ld_acquire_u32(f) == tag) return true;
@@ -40,7 +40,7 @@ __device__ __forceinline__ bool gs_wait_done(const unsigned* f, unsigned tag, co
     if (ld_acquire_u32(f) == tag) return true;
     if ((++spins & 63u) == 0) {
       if (ld_relaxed_i32(status) != 0) return false;
-      if (global_timer_ns() - t0 > kBarrierTimeoutNs) {
+      if (global_timer_ns() - t0 > wait_limit_ns()) {
         atomicCAS(const_cast<int*>(status), 0, (int)BOGUS_GPU_TIMEOUT);
         return false;
       }
@@ -414,5 +414,8 @@ cudaError_t launch_pgs_y(int n, int d, const int* cb, const double* H, const dou
   k_pgs_y<<<(n + 127) / 128, 128, 0, s>>>(n, d, cb, H, Mx, b, y);
   return cudaGetLastError();
 }
+
+// Sets this file's copy of the device-side wait limit on the current device.
+BOGUS_GPU_WAIT_LIMIT_SETTER(set_wait_limit_gs)
 
 }  // namespace bogus_gpu

@@ -469,7 +469,7 @@ struct GridCtx {
   }
   unsigned reductions = 0;  // reductions published or pending (identical in every CTA)
   bool pending = false;     // this warp has not yet waited for the last (split) reduction
-  __device__ MonoBarrier mb() const { return MonoBarrier{a.mono, a.gb.status, gridDim.x}; }
+  __device__ MonoBarrier mb() const { return MonoBarrier{a.mono, a.gb.status, gridDim.x + a.phantom_ctas}; }
   __device__ bool sync() {
     const bool ok = mono_barrier(mb(), phase, [&] { clear_tickets(); });
     ++phase;
@@ -737,5 +737,8 @@ int pg_max_grid(int device, bool fp32, bool interleaved) {
   if (per > cap) per = cap;
   return per * sms;
 }
+
+// Sets this file's copy of the device-side wait limit on the current device.
+BOGUS_GPU_WAIT_LIMIT_SETTER(set_wait_limit_pg)
 
 }  // namespace bogus_gpu

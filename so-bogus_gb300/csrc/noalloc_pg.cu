@@ -12,9 +12,18 @@
 // reuse it. Because that first call does this set-up, it should come before any stream capture.
 //
 // Every call on a device shares the same array. Its contents persist from one call to the next, so each
-// call clears the parts that must start at zero (the grid-barrier words, the chunk counters and the error status) before
-// launching; two calls whose work overlaps on the GPU (different streams, or different host threads) race
-// on the array and must not be issued.
+// call clears the parts that must start at zero (the grid-barrier words, the chunk counters, the error status
+// and the words of the input check) before launching; two calls whose work overlaps on the GPU (different
+// streams, or different host threads) race on the array and must not be issued.
+//
+// The remembered address belongs to the device's current CUDA context: cudaDeviceReset destroys that context
+// and with it the array, so a process that resets a device must not call this entry point on it afterwards.
+//
+// The caller's W is checked on the device before it is used (row pointers in order and in range, columns in
+// range and increasing, a diagonal block in every row, finite values in W, b and mu); the check's results go
+// to words of the same fixed array, so a malformed problem is rejected with BOGUS_GPU_BAD_INPUT (or NONFINITE)
+// before any kernel reads out of bounds, still without allocating. The entry point makes `device` current
+// for its work and restores the caller's current device before it returns.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -89,6 +98,12 @@ double* scratch_for_device(int device, int* status) {
 
 using namespace bogus_gpu;
 
+namespace {
+int solve_on_current_device(int device, int n, int nnzb, const int* d_rowptr, const int* d_colidx,
+                            const double* d_blocks, const double* d_b, const double* d_mu, const bogus_gpu_pg_options* o,
+                            double* d_r, double* residual, unsigned* iters, void* stream);
+}  // namespace
+
 #define NA_CUDA(call)                                                                            \
   do {                                                                                           \
     cudaError_t e_ = (call);                                                                     \
@@ -114,7 +129,20 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
     return fail(BOGUS_GPU_BAD_INPUT, "invalid projected-gradient factors");
   if (n > 0 && (!d_rowptr || !d_b || !d_mu || !d_r || (nnzb > 0 && (!d_colidx || !d_blocks))))
     return fail(BOGUS_GPU_BAD_INPUT, "null device pointer");
+  int prev_device = -1;
+  NA_CUDA(cudaGetDevice(&prev_device));
   NA_CUDA(cudaSetDevice(device));
+  const int st = solve_on_current_device(device, n, nnzb, d_rowptr, d_colidx, d_blocks, d_b, d_mu, o, d_r, residual,
+                                         iters, stream);
+  cudaSetDevice(prev_device);
+  return st;
+}
+
+namespace {
+
+int solve_on_current_device(int device, int n, int nnzb, const int* d_rowptr, const int* d_colidx,
+                            const double* d_blocks, const double* d_b, const double* d_mu, const bogus_gpu_pg_options* o,
+                            double* d_r, double* residual, unsigned* iters, void* stream) {
   int st = 0;
   double* s = scratch_for_device(device, &st);
   if (!s) return st;
@@ -125,7 +153,26 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   }
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   const size_t n3 = 3 * (size_t)n;
-  unsigned* words = reinterpret_cast<unsigned*>(s + kOffWords);  // [0] count, [1] gen, [2] status, [3..4] tickets, [8..13] 3 monotonic u64
+  // [0] count, [1] gen, [2] status, [3..4] tickets, [8..13] 3 monotonic u64, [16] the first malformed row of W,
+  // [17] the non-finite flag of the input check
+  unsigned* words = reinterpret_cast<unsigned*>(s + kOffWords);
+  {
+    int* chk = reinterpret_cast<int*>(words + 16);
+    NA_CUDA(launch_check_full(n, nnzb, d_rowptr, d_colidx, chk, cs));
+    NA_CUDA(cudaMemsetAsync(chk + 1, 0, sizeof(int), cs));
+    NA_CUDA(launch_any_nonfinite(9 * (size_t)nnzb, d_blocks, chk + 1, cs));
+    NA_CUDA(launch_any_nonfinite(n3, d_b, chk + 1, cs));
+    NA_CUDA(launch_any_nonfinite((size_t)n, d_mu, chk + 1, cs));
+    NA_CUDA(launch_any_nonfinite(n3, d_r, chk + 1, cs));
+    int check[2] = {0, 0};
+    NA_CUDA(cudaMemcpyAsync(check, chk, sizeof(check), cudaMemcpyDeviceToHost, cs));
+    NA_CUDA(cudaStreamSynchronize(cs));
+    if (check[0] < n)
+      return fail(BOGUS_GPU_BAD_INPUT, "bogus_gpu_solve_pg_noalloc: row " + std::to_string(check[0]) + " of W is "
+                  "malformed (row pointers out of order or range, a column out of range or not increasing, or no "
+                  "diagonal block)");
+    if (check[1]) return fail(BOGUS_GPU_NONFINITE, "bogus_gpu_solve_pg_noalloc: non-finite value in W, b, mu or r");
+  }
   // diagonal positions and scalings into the scratch
   DevBSR W;
   W.n = n;
@@ -191,3 +238,5 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   if (iters) *iters = out.iters;
   return out.converged ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
 }
+
+}  // namespace
