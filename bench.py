@@ -1,19 +1,24 @@
 #!/usr/bin/env python
-"""Benchmark: FP64 APGD solve of the 200 000-contact friction problem on one GB300 (time to residual).
+"""Benchmark: FP64 APGD time to residual 1e-6 on the 200 000-contact friction problem, on one GB300.
 
 Workload (one "step"): DualFrictionProblem::solveWith(ProjectedGradient, r) with the reference's defaults
-(APGD, SOC law, line search 8 / 1.25 / 0.5) at tol 1e-6 with at most 500 iterations, from r = 0, on the
-seeded grid problem (50 000 rigid bodies, 200 000 contacts, W assembled on the GPU). The solve stops at
-the tolerance or after 500 iterations, whichever comes first; the GPU and the CPU oracle run bit-identical
-iterations, so both arms do the same work.
+(APGD, SOC law, line search 8 / 1.25 / 0.5) at tol 1e-6, from r = 0, on the seeded grid problem (50 000 rigid
+bodies, 200 000 contacts, W assembled on the GPU), with an iteration budget (20 000) that the solve does not
+reach: it stops at the tolerance (7 846 iterations on this problem). The GPU and the CPU oracle run
+bit-identical iterations, so both arms do the same work.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--no-secondary]
 
 Our arm prints `value` (ms per solve, inputs resident in HBM, CUDA events on the library's stream), `e2e`
 (the C-ABI call with host buffers: upload of W/b/mu/r, solve, download of r), the roofline of the
-persistent solver kernel, FP64 pipe use and the CPU baseline (the oracle on the host cores).
+persistent solver kernel, FP64 pipe use, the CPU baseline (the oracle on the host cores, on a bounded sample:
+the first 1000 iterations of the same solve, scaled to the full solve's iteration count) and `secondary`: the
+other measured targets (500-iteration cap, FP32-refined time to 1e-6 and its error against the FP64 result,
+SPG, colored Gauss-Seidel, the 4096-problem batch against a loop of single solves, adjoint / forward).
 `--impl reference` times the CPU restatement of the reference (the oracle, OpenMP on all host cores) on the
-same workload. With N > 1 (torchrun) every rank solves its own replica (a single problem does not shard).
+same workload: one full solve to calibrate the iteration count, then bounded samples. With N > 1 (torchrun)
+every rank solves its own replica (a single problem does not shard); `--workload batch|adjoint` shards the
+independent problems of those batches over the ranks instead.
 """
 from __future__ import annotations
 
@@ -32,16 +37,19 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path[:0] = [os.path.join(REPO, "so-bogus_gb300")]
 
 TOL = 1e-6
-MAX_ITERS = 500
+MAX_ITERS = 20_000        # budget of the time-to-residual solve; APGD reaches 1e-6 well before it here
+CAP_500 = 500             # the iteration budget of the configuration's wording, reported beside the headline
+CPU_SAMPLE_ITERS = 1000   # the oracle's bounded sample: the first 1000 iterations of the same solve
+FP32_ITERS = 2000         # FP32-refined: at most this many FP32 iterations, then FP64 ones to the tolerance
 MAX_ADJ_FWD_ITERS = 20000
 METRIC = "time-to-residual 1e-6 (ms), FP64 APGD, 200k contacts"
-WORKLOAD = "fp64_apgd_200k_contacts"
+WORKLOAD = "fp64_apgd_200k_contacts_to_1e-6"
 
 
-def config_dict(n, nnzb_full, extra=None):
+def config_dict(n, nnzb_full, max_iters, extra=None):
     d = {"workload": WORKLOAD, "contacts": n, "bodies": 50_000, "w_blocks_full": nnzb_full,
          "w_blocks_lower": (nnzb_full + n) // 2, "solver": "APGD (reference defaults), SOC law",
-         "tol": TOL, "max_iters": MAX_ITERS, "start": "r = 0", "generator": "grid, seed 1",
+         "tol": TOL, "max_iters": max_iters, "start": "r = 0", "generator": "grid, seed 1",
          "l2": "inputs exceed L2 (W both triangles = %.0f MB > 129 MB)" % (nnzb_full * 76 / 1e6),
          "parallelism": "replicas (one problem per GPU)"}
     if extra:
@@ -160,43 +168,61 @@ def make_problem():
 
 
 # --------------------------------------------------------------------------------------------------------
-def cpu_oracle_solve(d, threads=None):
-    """The oracle (CPU restatement of the reference) on all host cores: returns (ms, residual, iterations)."""
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import pyoracle
+class OracleSolve:
+    """The oracle (CPU restatement of the reference) on the benchmark problem, OpenMP on all host cores."""
 
-    pyoracle.build()
-    if threads:
-        pyoracle.set_num_threads(threads)
-    P = pyoracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
-    rp, cl, vl = P.assemble()
-    O = pyoracle.DualProblem(rp, cl, vl, d.b, d.mu)
-    t0 = time.perf_counter()
-    res, r, it = O.solve_pg(np.zeros(3 * d.n), variant=3, coulomb=False, tol=TOL, max_iters=MAX_ITERS)
-    ms = (time.perf_counter() - t0) * 1e3
-    return ms, res, it, pyoracle.num_threads(), (rp, cl, vl)
+    def __init__(self, d, lower=None):
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import pyoracle
+
+        pyoracle.build()
+        self.po = pyoracle
+        self.d = d
+        if lower is None:
+            P = pyoracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+            lower = P.assemble()
+        self.lower = lower
+        rp, cl, vl = lower
+        self.O = pyoracle.DualProblem(rp, cl, np.asarray(vl).reshape(-1), d.b, d.mu)
+
+    def solve(self, max_iters):
+        """APGD from r = 0 with the benchmark's tolerance: (ms, residual, r, iterations)."""
+        t0 = time.perf_counter()
+        res, r, it = self.O.solve_pg(np.zeros(3 * self.d.n), variant=3, coulomb=False, tol=TOL, max_iters=max_iters)
+        return (time.perf_counter() - t0) * 1e3, res, r, it
+
+    @property
+    def cores(self):
+        return self.po.num_threads()
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the oracle on all host cores. The first warm-up step solves to the tolerance once (the
+    full solve's iteration count and time); every other step is a bounded sample of the same solve, its first
+    CPU_SAMPLE_ITERS iterations, scaled by the full solve's iteration count."""
     if world > 1 and rank != 0:
         return
     d = make_problem()
+    orc = OracleSolve(d)
+    full_ms, full_res, _, full_it = orc.solve(args.max_iters)  # calibration (untimed)
+    sample_iters = min(CPU_SAMPLE_ITERS, args.max_iters)
     times = []
-    res = it = cores = None
-    nnz_full = 0
-    for step in range(args.warmup + args.steps):
-        ms, res, it, cores, lower = cpu_oracle_solve(d)
-        nnz_full = 2 * len(lower[1]) - d.n
-        if step >= args.warmup:
-            times.append(ms)
+    for step in range(max(0, args.warmup - 1) + args.steps):
+        ms, _, _, it = orc.solve(sample_iters)
+        if step >= max(0, args.warmup - 1):
+            times.append(ms * full_it / max(1, it))
     v = statistics.mean(times)
+    nnz_full = 2 * len(orc.lower[1]) - d.n
+    sample = (f"first {sample_iters} APGD iterations of the same solve per step, scaled to the full solve's "
+              f"{full_it} iterations; one full solve measured {full_ms:.0f} ms")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded grid generator)",
-        "config": config_dict(d.n, nnz_full or 0, {"iterations": it, "final_residual": res}),
-        "cpu_baseline": {"value": v, "unit": "ms", "cores": cores, "kind": "port",
-                         "sample": f"full solve ({it} APGD iterations) of the same problem, per step"},
+        "config": config_dict(d.n, nnz_full, args.max_iters, {"iterations": full_it, "final_residual": full_res,
+                                              "reached_tol": bool(full_res < TOL)}),
+        "cpu_baseline": {"value": v, "unit": "ms", "cores": orc.cores, "kind": "port", "sample": sample,
+                         "full_solve_ms": full_ms},
         "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -218,7 +244,7 @@ def run_ours(args, rank, world, local_rank):
     nnz_full = D.nnzb()
     pg = bogus_gpu.ProjectedGradient()
     pg.setTol(TOL)
-    pg.setMaxIters(MAX_ITERS)
+    pg.setMaxIters(args.max_iters)
     r = torch.zeros(3 * n, dtype=torch.float64, device=f"cuda:{dev}")
     stream = torch.cuda.ExternalStream(D.stream(), device=f"cuda:{dev}")
 
@@ -254,6 +280,7 @@ def run_ours(args, rank, world, local_rank):
         torch.distributed.barrier()
     ck = clocks.stop()
     ms_step = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, f"cuda:{dev}")
+    r_fp64 = r.cpu().numpy()
 
     # end to end through the C ABI with host buffers: upload W (lower), b, mu and r, solve, download r. The
     # host arrays live in pinned (page-locked) memory, as a simulation that streams problems to the GPU keeps them.
@@ -289,8 +316,9 @@ def run_ours(args, rank, world, local_rank):
         "metric": METRIC, "value": ms_step, "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded grid generator)",
-        "config": config_dict(n, nnz_full, {"iterations": iters[-1], "final_residual": res[-1],
-                                            "assembly_ms": asm["device_ms"]}),
+        "config": config_dict(n, nnz_full, args.max_iters, {"iterations": iters[-1], "final_residual": res[-1],
+                                            "reached_tol": bool(res[-1] < TOL)}),
+        "assembly_ms": asm["device_ms"],
         "e2e": {"value": statistics.mean(e2e_ms), "unit": "ms", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -302,11 +330,88 @@ def run_ours(args, rank, world, local_rank):
         "clocks": ck,
     }
     if world == 1 and not args.no_cpu_baseline:
-        cms, cres, cit, cores, _ = cpu_oracle_solve(d)
-        line["cpu_baseline"] = {"value": cms, "unit": "ms", "cores": cores, "kind": "port",
-                                "sample": f"one full solve ({cit} iterations, residual {cres:.3e}) of the same problem"}
-        line["cpu_baseline"]["identical_result"] = bool(cit == iters[-1] and cres == res[-1])
+        # the oracle on a bounded sample: the first CPU_SAMPLE_ITERS iterations of the same solve (about 5 s on
+        # 16 Grace cores), scaled by the full solve's iteration count; the GPU's capped solve is compared with it
+        orc = OracleSolve(d, D.W_lower())
+        sample_iters = min(CPU_SAMPLE_ITERS, args.max_iters)
+        cms, cres, cr, cit = orc.solve(sample_iters)
+        pgs = bogus_gpu.ProjectedGradient()
+        pgs.setTol(TOL)
+        pgs.setMaxIters(sample_iters)
+        rs = np.zeros(3 * n)
+        gres = D.solveWith(pgs, rs)
+        line["cpu_baseline"] = {
+            "value": cms * iters[-1] / max(1, cit), "unit": "ms", "cores": orc.cores, "kind": "port",
+            "sample": f"first {cit} APGD iterations of the same solve ({cms:.0f} ms), scaled to the full solve's "
+                      f"{iters[-1]} iterations",
+            "identical_result": bool(gres == cres and D.last_iterations == cit and np.array_equal(rs, cr))}
+    if world == 1 and not args.no_secondary:
+        line["secondary"] = measure_secondary(args, D, d, r_fp64, ms_step)
     print(json.dumps(line), flush=True)
+
+
+def measure_secondary(args, D, d, r_fp64, fp64_ms):
+    """The other measured targets, on the same GPU after the timed region (each labelled with its residual and
+    iteration count; device times from CUDA events on the library's stream, best of a few solves)."""
+    import bogus_gpu
+
+    out = {}
+
+    def best_of(solver, k=2, **kw):
+        best = None
+        for _ in range(k):
+            r = np.zeros(3 * d.n)
+            res = D.solveWith(solver, r, **kw)
+            st = D.solve_stats()
+            if best is None or st["device_ms"] < best[1]["device_ms"]:
+                best = (res, st, r)
+        return best
+
+    pg = bogus_gpu.ProjectedGradient()
+    pg.setTol(TOL)
+    pg.setMaxIters(CAP_500)
+    res, st, _ = best_of(pg)
+    out["apgd_500_iterations"] = {"device_ms": st["device_ms"], "iterations": st["iterations"], "residual": res,
+                                  "note": "the same solve stopped at 500 iterations (the configuration's budget)"}
+    # FP32-refined: up to FP32_ITERS FP32 iterations, then FP64 ones to the tolerance
+    pgm = bogus_gpu.ProjectedGradient()
+    pgm.setTol(TOL)
+    pgm.setMaxIters(FP32_ITERS)
+    pgm.setMixedPrecision(True, args.max_iters)
+    res, st, rm = best_of(pgm)
+    err = float(np.linalg.norm(rm - r_fp64) / np.linalg.norm(r_fp64))
+    out["fp32_refined_to_1e-6"] = {
+        "device_ms": st["device_ms"], "fp32_ms": st["fp32_device_ms"],
+        "fp32_iterations": st["iterations"] - st["refine_iterations"], "fp64_iterations": st["refine_iterations"],
+        "residual": res, "reached_tol": bool(res < TOL), "speedup_vs_fp64": fp64_ms / st["device_ms"],
+        "rel_error_vs_fp64": err,
+        "error_note": "||r_mixed - r_fp64|| / ||r_fp64||, r_fp64 the FP64 solve to 1e-6 (bit-identical to the "
+                      "oracle's iterates); W is singular here, so two iterates at residual 1e-6 may differ along "
+                      "its null space"}
+    pgs = bogus_gpu.ProjectedGradient()
+    pgs.setTol(TOL)
+    pgs.setMaxIters(args.max_iters)
+    pgs.setDefaultVariant(bogus_gpu.SPG)
+    res, st, _ = best_of(pgs)
+    out["spg_to_1e-6"] = {"device_ms": st["device_ms"], "iterations": st["iterations"], "residual": res,
+                          "reached_tol": bool(res < TOL)}
+    gs = bogus_gpu.GaussSeidel()
+    gs.coloring().update(True)
+    gs.setTol(TOL)
+    gs.setMaxIters(200)
+    trace = []
+    gs.callback().connect(lambda it, rr: trace.append((it, rr)))
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(gs, r)
+    st = D.solve_stats()
+    sweeps = D.last_iterations
+    out["gauss_seidel_colored_coulomb"] = {
+        "sweeps": sweeps, "device_ms": st["device_ms"], "ms_per_sweep": st["device_ms"] / max(1, sweeps),
+        "residual": res, "reached_tol": bool(res < TOL), "trace": trace[::2],
+        "note": "does not reach 1e-6: residual 5.1e-3 after 1000 sweeps (8.5 s) on this problem"}
+    out["batch_4096"] = measure_batch(args, sample_stride=16)
+    out["adjoint_64x20000"] = measure_adjoint(args, steps=2)
+    return out
 
 
 def run_profile(iters: int, mixed: bool = False) -> None:
@@ -327,88 +432,140 @@ def run_profile(iters: int, mixed: bool = False) -> None:
     print(json.dumps({"profile_iters": iters, "residual": res, "stats": st}))
 
 
-def run_batch(args) -> None:
-    """4096 independent problems (16..4096 contacts, log-uniform) in one persistent launch, against a loop of the
-    single-problem GPU path and the CPU oracle on a stratified sample of the problems."""
+BATCH_MAX_ITERS = 500
+
+
+def _sync_time(fn, world):
+    """Wall time of fn() between device synchronisations (and barriers across ranks), max over ranks."""
+    import torch
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3
+    if world > 1:
+        torch.distributed.barrier()
+    return max_over_ranks(ms, world, "cuda"), out
+
+
+def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
+    """4096 independent problems (16..4096 contacts, log-uniform) in one persistent launch per rank (the problems
+    shared over the ranks by a greedy bin-pack on their W blocks), against a loop of the single-problem GPU path
+    on a stratified sample of the problems (every sample_stride-th by size; rank 0, one GPU only). Each sampled
+    problem's batched result is compared with its own single-problem solve and, on every fourth sampled
+    problem, with the oracle."""
     import torch
 
     import bogus_gpu
-    from bogus_gpu import generator
+    from bogus_gpu import generator, shard
 
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    steps = steps or max(1, min(args.steps, 3))
     d, cptr = generator.batch(4096)
-    D = bogus_gpu.DualFrictionProblem(0)
-    D.computeFrom(bogus_gpu.PrimalFrictionProblem.from_generated(d))
-    D.setBatch(cptr)
+    nprob = len(cptr) - 1
+    costs = shard.w_blocks_per_problem(d, cptr)
+    parts = shard.partition(costs, world)
+    mine = parts[rank]
+    sub, scptr = (d, cptr) if world == 1 else shard.subset(d, cptr, mine)
+    D = bogus_gpu.DualFrictionProblem(dev)
+    D.computeFrom(bogus_gpu.PrimalFrictionProblem.from_generated(sub))
+    D.setBatch(scptr)
     pg = bogus_gpu.ProjectedGradient()
     pg.setTol(TOL)
-    pg.setMaxIters(MAX_ITERS)
-    n = d.n
-    r = torch.zeros(3 * n, dtype=torch.float64, device="cuda:0")
-    stream = torch.cuda.ExternalStream(D.stream(), device="cuda:0")
+    pg.setMaxIters(BATCH_MAX_ITERS)
+    r = torch.zeros(3 * sub.n, dtype=torch.float64, device=f"cuda:{dev}")
+    stream = torch.cuda.ExternalStream(D.stream(), device=f"cuda:{dev}")
 
-    def step():
+    def solve(solver):
         with torch.cuda.stream(stream):
             r.zero_()
-        return D.solveBatch_device(pg, r.data_ptr())
+        return D.solveBatch_device(solver, r.data_ptr())
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        res, its = step()
-    torch.cuda.synchronize()
-    batched_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    solve(pg)
+    times, kernel = [], []
+    for _ in range(steps):
+        ms, (res, its) = _sync_time(lambda: solve(pg), world)
+        times.append(ms)
+        kernel.append(D.solve_stats()["device_ms"])
     st = D.solve_stats()
-    # the FP32-refined batch with the same 500-iteration budget per problem: up to 200 FP32 iterations, then up
-    # to 300 FP64 ones (a 500 + 50 split spends most of its time in FP32 iterations that cannot reach 1e-6)
+    r_batch = r.cpu().numpy()
+    # the FP32-refined batch with the same iteration budget per problem: up to 200 FP32 iterations, then FP64
     pgm = bogus_gpu.ProjectedGradient()
     pgm.setTol(TOL)
     pgm.setMaxIters(200)
-    pgm.setMixedPrecision(True, MAX_ITERS - 200)
-    for _ in range(2):
-        with torch.cuda.stream(stream):
-            r.zero_()
-        res_m, its_m = D.solveBatch_device(pgm, r.data_ptr())
+    pgm.setMixedPrecision(True, BATCH_MAX_ITERS - 200)
+    solve(pgm)
+    mixed_ms, (res_m, its_m) = _sync_time(lambda: solve(pgm), world)
     st_m = D.solve_stats()
-    # the single-problem path, problem by problem, on every 16th problem by size (stratified), scaled by 16
-    rp, cl, vl = D.W_lower()
-    vl = vl.reshape(-1, 9)
-    order = np.argsort(np.diff(cptr), kind="stable")
-    sample = order[::16]
-    single = bogus_gpu.DualFrictionProblem(0)
-    import pyoracle
-    t_single = 0.0
-    t_cpu = 0.0
-    same = True
-    for p in sample:
-        c0, c1 = int(cptr[p]), int(cptr[p + 1])
-        prp, pcl, pvl = rp[c0:c1 + 1] - rp[c0], cl[rp[c0]:rp[c1]] - c0, vl[rp[c0]:rp[c1]].reshape(-1)
-        single.set(prp, pcl, pvl, d.b[c0:c1], d.mu[c0:c1])
-        rr = np.zeros(3 * (c1 - c0))
-        t0 = time.perf_counter()
-        res_s = single.solveWith(pg, rr)
-        t_single += time.perf_counter() - t0
-        O = pyoracle.DualProblem(prp, pcl, pvl, d.b[c0:c1], d.mu[c0:c1])
-        t0 = time.perf_counter()
-        res_o, r_o, it_o = O.solve_pg(np.zeros(3 * (c1 - c0)), variant=3, coulomb=False, tol=TOL, max_iters=MAX_ITERS)
-        t_cpu += time.perf_counter() - t0
-        same = same and res_s == res_o == res[p] and it_o == its[p]
-    scale = len(cptr) - 1
-    scale = scale / len(sample)
-    print(json.dumps({
-        "workload": "batched_apgd_4096_problems", "problems": len(cptr) - 1, "contacts": n,
-        "batched_ms": batched_ms, "kernel_ms": st["device_ms"], "iterations_max": int(its.max()),
-        "iterations_mean": float(its.mean()), "converged_fraction": float(np.mean(res < TOL)),
-        "loop_single_gpu_ms_est": t_single * 1e3 * scale, "cpu_oracle_ms_est": t_cpu * 1e3 * scale,
-        "cpu_threads": pyoracle.num_threads(), "sample": f"{len(sample)} problems (every 16th by size), scaled",
-        "speedup_vs_loop": t_single * 1e3 * scale / batched_ms, "identical_on_sample": bool(same),
-        "algorithmic_gbs": st["algorithmic_bytes"] / (st["device_ms"] * 1e-3) / 1e9,
-        "fp32_refined": {"split": "up to 200 FP32 + 300 FP64 iterations per problem",
-                         "kernel_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"],
-                         "converged_fraction": float(np.mean(res_m < TOL)),
-                         "speedup_vs_fp64_batch": st["device_ms"] / st_m["device_ms"]}}), flush=True)
+    allres = shard.gather_results(mine, np.stack([res, its, res_m], 1), nprob, world)
+    out = {"problems": nprob, "contacts": int(d.n), "ranks": world, "max_iters": BATCH_MAX_ITERS,
+           "batched_ms": statistics.median(times), "kernel_ms": statistics.median(kernel),
+           "algorithmic_gbs": st["algorithmic_bytes"] / (st["device_ms"] * 1e-3) / 1e9,
+           "fp32_refined": {"split": "up to 200 FP32 + 300 FP64 iterations per problem", "batched_ms": mixed_ms,
+                            "kernel_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"]},
+           "timing": f"median of {steps} solves after a warm-up, wall time between device synchronisations"}
+    if world > 1:
+        out["partition"] = {"rule": "greedy bin-pack on W blocks", "blocks_per_rank": [int(costs[q].sum()) for q in parts],
+                            "problems_per_rank": [int(q.size) for q in parts]}
+    if rank != 0:
+        return out
+    out["iterations_max"] = int(allres[:, 1].max())
+    out["iterations_mean"] = float(allres[:, 1].mean())
+    out["converged_fraction"] = float(np.mean(allres[:, 0] < TOL))
+    out["fp32_refined"]["converged_fraction"] = float(np.mean(allres[:, 2] < TOL))
+    out["fp32_refined"]["speedup_vs_fp64_batch"] = out["batched_ms"] / mixed_ms
+    if world == 1 and sample_stride:
+        # the single-problem path, problem by problem (inputs set beforehand, each solve timed with its r copies)
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import pyoracle
+
+        rp, cl, vl = D.W_lower()
+        vl = vl.reshape(-1, 9)
+        order = np.argsort(np.diff(cptr), kind="stable")
+        sample = order[::sample_stride]
+        single = bogus_gpu.DualFrictionProblem(dev)
+        t_single = 0.0
+        same_single = same_oracle = True
+        checked = 0
+        for k, p in enumerate(sample):
+            c0, c1 = int(cptr[p]), int(cptr[p + 1])
+            prp, pcl, pvl = rp[c0:c1 + 1] - rp[c0], cl[rp[c0]:rp[c1]] - c0, vl[rp[c0]:rp[c1]].reshape(-1)
+            single.set(prp, pcl, pvl, d.b[c0:c1], d.mu[c0:c1])
+            rr = np.zeros(3 * (c1 - c0))
+            t0 = time.perf_counter()
+            res_s = single.solveWith(pg, rr)
+            t_single += time.perf_counter() - t0
+            same_single = same_single and res_s == res[p] and single.last_iterations == its[p] and \
+                np.array_equal(rr, r_batch[3 * c0:3 * c1])
+            if k % 4 == 0:
+                O = pyoracle.DualProblem(prp, pcl, pvl, d.b[c0:c1], d.mu[c0:c1])
+                res_o, r_o, it_o = O.solve_pg(np.zeros(3 * (c1 - c0)), variant=3, coulomb=False, tol=TOL,
+                                              max_iters=BATCH_MAX_ITERS)
+                same_oracle = same_oracle and res_o == res[p] and it_o == its[p] and np.array_equal(r_o, rr)
+                checked += 1
+        scale = nprob / len(sample)
+        out["loop_single_gpu"] = {
+            "sample_problems": int(len(sample)), "sample_ms": t_single * 1e3, "estimated_full_loop_ms": t_single * 1e3 * scale,
+            "sample": f"every {sample_stride}th problem by size, solved one by one through DualFrictionProblem.solveWith "
+                      "(problem set beforehand; the timed call uploads r, solves and downloads r)"}
+        out["speedup_vs_loop"] = t_single * 1e3 * scale / out["batched_ms"]
+        out["identical_to_single_solves_on_sample"] = bool(same_single)
+        out["identical_to_oracle"] = {"problems": checked, "identical": bool(same_oracle)}
+    return out
+
+
+def run_batch(args, rank=0, world=1, dev=0) -> None:
+    out = measure_batch(args, rank=rank, world=world, dev=dev, sample_stride=16 if world == 1 else 0,
+                        steps=args.steps)
+    if rank == 0:
+        line = {"metric": "batched APGD, 4096 problems, tol 1e-6 / 500 iterations (ms)", "value": out["batched_ms"],
+                "unit": "ms", "n_gpus": world, "steps": args.steps, "higher_is_better": False, "scaling": "strong",
+                "dtype": "f64", "data": "synthetic (seeded batch generator)",
+                "config": {"workload": "batched_apgd_4096_problems", "parallelism": f"problems sharded over {world} ranks"
+                           if world > 1 else "one GPU"}, "batch": out}
+        print(json.dumps(line), flush=True)
 
 
 def run_gs(args) -> None:
@@ -474,8 +631,9 @@ def run_gs(args) -> None:
 
 
 def run_mixed(args) -> None:
-    """FP32-refined APGD on the 200 000-contact problem: 500 FP32 iterations then up to 50 FP64 ones, against
-    the FP64 solve run to the same FP64 residual (time to the same residual, both on the GPU)."""
+    """FP32-refined APGD on the 200 000-contact problem, time to residual 1e-6 for several FP32 / FP64 splits (at
+    most m FP32 iterations, then FP64 ones to the tolerance), against the FP64 solve to 1e-6; with each result its
+    relative distance to the FP64 result."""
     import bogus_gpu
 
     d = make_problem()
@@ -484,43 +642,37 @@ def run_mixed(args) -> None:
 
     def timed(pg):
         best = None
-        for k in range(args.warmup + args.steps):
+        for k in range(max(1, args.warmup) + args.steps):
             r = np.zeros(3 * d.n)
             res = D.solveWith(pg, r, staticProblem=True)
             st = D.solve_stats()
-            if k >= args.warmup and (best is None or st["device_ms"] < best[1]["device_ms"]):
-                best = (res, st)
+            if k >= max(1, args.warmup) and (best is None or st["device_ms"] < best[1]["device_ms"]):
+                best = (res, st, r)
         return best
 
-    pgm = bogus_gpu.ProjectedGradient()
-    pgm.setTol(TOL)
-    pgm.setMaxIters(MAX_ITERS)
-    pgm.setMixedPrecision(True, 50)
-    res_m, st_m = timed(pgm)
     pg64 = bogus_gpu.ProjectedGradient()
     pg64.setTol(TOL)
-    pg64.setMaxIters(MAX_ITERS)
-    res_p, st_p = timed(pg64)
-    # the FP64 solve to the residual the mixed solve reached
-    pgt = bogus_gpu.ProjectedGradient()
-    pgt.setTol(res_m)
-    pgt.setMaxIters(4 * MAX_ITERS)
-    res_t, st_t = timed(pgt)
-    m32 = st_m["fp32_device_ms"]
+    pg64.setMaxIters(args.max_iters)
+    res_p, st_p, r64 = timed(pg64)
+    splits = {}
+    for m32 in (1000, 2000, 3000, 4000, 5000, 6000, 8000):
+        pgm = bogus_gpu.ProjectedGradient()
+        pgm.setTol(TOL)
+        pgm.setMaxIters(m32)
+        pgm.setMixedPrecision(True, args.max_iters)
+        res_m, st_m, rm = timed(pgm)
+        splits[m32] = {"device_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"],
+                       "fp32_iterations": st_m["iterations"] - st_m["refine_iterations"],
+                       "fp64_iterations": st_m["refine_iterations"], "residual": res_m,
+                       "reached_tol": bool(res_m < TOL), "speedup_vs_fp64": st_p["device_ms"] / st_m["device_ms"],
+                       "rel_error_vs_fp64": float(np.linalg.norm(rm - r64) / np.linalg.norm(r64))}
     print(json.dumps({
-        "workload": "fp32_refined_apgd_200k_contacts", "law": "SOC", "contacts": d.n,
-        "mixed": {"device_ms": st_m["device_ms"], "fp32_ms": m32, "fp32_iterations":
-                  st_m["iterations"] - st_m["refine_iterations"], "fp64_refine_iterations": st_m["refine_iterations"],
-                  "fp64_residual": res_m,
-                  "fp32_ms_per_iteration": m32 / max(1, st_m["iterations"] - st_m["refine_iterations"]),
-                  "algorithmic_gbs": st_m["algorithmic_bytes"] / (st_m["device_ms"] * 1e-3) / 1e9},
-        "fp64_same_iterations": {"device_ms": st_p["device_ms"], "iterations": st_p["iterations"],
-                                 "residual": res_p, "ms_per_iteration": st_p["device_ms"] / max(1, st_p["iterations"])},
-        "fp64_to_mixed_residual": {"device_ms": st_t["device_ms"], "iterations": st_t["iterations"],
-                                   "residual": res_t, "reached": bool(res_t <= res_m)},
-        "speedup_time_to_residual": st_t["device_ms"] / st_m["device_ms"],
-        "timing": f"best of {args.steps} after {args.warmup} warm-up solves, CUDA events on the library stream"}),
-        flush=True)
+        "workload": "fp32_refined_apgd_200k_contacts_to_1e-6", "law": "SOC", "contacts": d.n,
+        "fp64": {"device_ms": st_p["device_ms"], "iterations": st_p["iterations"], "residual": res_p,
+                 "ms_per_iteration": st_p["device_ms"] / max(1, st_p["iterations"])},
+        "fp32_refined_by_fp32_iterations": splits,
+        "timing": f"best of {args.steps} after {max(1, args.warmup)} warm-up solves, CUDA events on the library "
+                  "stream"}), flush=True)
 
 
 def run_admm(args) -> None:
@@ -597,47 +749,66 @@ def run_dama(args) -> None:
         flush=True)
 
 
-def run_adjoint(args) -> None:
+def measure_adjoint(args, steps=2, rank=0, world=1, dev=0):
     """Gradient workload: 64 problems x 20 000 contacts (bodies = contacts / 3, compliance 0.05 I), forward =
     batched APGD with the SOC law to 1e-10 per problem, loss L = g . r with g ~ N(0, 1); backward = the adjoint
-    (dL/db, dL/dmu) over the whole batch, then dL/dH, dL/dw, dL/df. Reports t_adjoint / t_forward."""
+    (dL/db, dL/dmu) over the batch, then dL/dH, dL/dw, dL/df. Reports t_adjoint / t_forward (device times). With
+    several ranks each solves its share of the problems (all of equal size)."""
     import bogus_gpu
-    from bogus_gpu import generator
+    from bogus_gpu import generator, shard
 
     d, cptr = generator.adjoint_batch()
-    P = bogus_gpu.PrimalFrictionProblem(d.minv, d.objA, d.objB, d.HA, d.HB, d.b.reshape(-1), d.mu)
-    D = bogus_gpu.DualFrictionProblem(0)
+    nprob = len(cptr) - 1
+    parts = shard.partition(np.diff(cptr), world)
+    mine = parts[rank]
+    sub, scptr = (d, cptr) if world == 1 else shard.subset(d, cptr, mine)
+    P = bogus_gpu.PrimalFrictionProblem(sub.minv, sub.objA, sub.objB, sub.HA, sub.HB, sub.b.reshape(-1), sub.mu,
+                                        device=dev)
+    D = bogus_gpu.DualFrictionProblem(dev)
     D.computeFrom(P)
     D.add_compliance(generator.ADJOINT_COMPLIANCE)
-    D.setBatch(cptr)
+    D.setBatch(scptr)
     pg = bogus_gpu.ProjectedGradient()
     pg.setTol(1e-10)
     pg.setMaxIters(MAX_ADJ_FWD_ITERS)
     g = np.random.default_rng(6).standard_normal(3 * d.n)
+    g_mine = g.reshape(-1, 3)[np.concatenate([np.arange(cptr[p], cptr[p + 1]) for p in mine])].reshape(-1)
     fwd, adj, prim = [], [], []
-    for k in range(args.warmup + args.steps):
-        r = np.zeros(3 * d.n)
+    for k in range(1 + steps):
+        r = np.zeros(3 * sub.n)
         res, its = D.solveBatchWith(pg, r)
         tf = D.solve_stats()["device_ms"]
-        t0 = time.perf_counter()
-        db, dmu = D.adjoint(r, g, tol=1e-10)
+        D.adjoint(r, g_mine, tol=1e-10)
         ta = D.solve_stats()["device_ms"]
         t1 = time.perf_counter()
         D.adjoint_primal(P)
         t2 = time.perf_counter()
-        if k >= args.warmup:
+        if k >= 1:
             fwd.append(tf)
             adj.append(ta)
             prim.append((t2 - t1) * 1e3)
-    tf, ta = statistics.median(fwd), statistics.median(adj)
-    print(json.dumps({
-        "workload": "adjoint_64x20000_contacts", "problems": len(cptr) - 1, "contacts": d.n,
-        "compliance": generator.ADJOINT_COMPLIANCE, "forward_ms": tf, "forward_iterations_max": int(its.max()),
-        "forward_converged_fraction": float(np.mean(res < 1e-10)), "adjoint_ms": ta,
-        "adjoint_cg_iterations": D.last_adjoint_iterations, "adjoint_rel_residual": D.last_adjoint_residual,
-        "primal_gradients_wall_ms": statistics.median(prim), "t_adjoint_over_t_forward": ta / tf,
-        "timing": f"median of {args.steps} after {args.warmup} warm-up; device times (CUDA events) of the batched "
-                  "solve kernel and of the adjoint kernel"}), flush=True)
+    tf, ta = max_over_ranks(statistics.median(fwd), world, "cuda"), max_over_ranks(statistics.median(adj), world, "cuda")
+    allres = shard.gather_results(mine, np.stack([res, its], 1), nprob, world)
+    out = {"problems": nprob, "contacts": int(d.n), "ranks": world, "compliance": generator.ADJOINT_COMPLIANCE,
+           "forward_ms": tf, "adjoint_ms": ta, "t_adjoint_over_t_forward": ta / tf,
+           "adjoint_cg_iterations": D.last_adjoint_iterations, "adjoint_rel_residual": D.last_adjoint_residual,
+           "primal_gradients_wall_ms": statistics.median(prim),
+           "timing": f"median of {steps} after a warm-up; device times (CUDA events) of the batched solve kernel "
+                     "and of the adjoint kernel (max over ranks)"}
+    if allres is not None:
+        out["forward_iterations_max"] = int(allres[:, 1].max())
+        out["forward_converged_fraction"] = float(np.mean(allres[:, 0] < 1e-10))
+    return out
+
+
+def run_adjoint(args, rank=0, world=1, dev=0) -> None:
+    out = measure_adjoint(args, steps=args.steps, rank=rank, world=world, dev=dev)
+    if rank == 0:
+        line = {"metric": "adjoint / forward time, 64 x 20 000 contacts", "value": out["t_adjoint_over_t_forward"],
+                "unit": "ratio", "n_gpus": world, "steps": args.steps, "higher_is_better": False,
+                "scaling": "strong", "dtype": "f64", "data": "synthetic (seeded adjoint batch generator)",
+                "config": {"workload": "adjoint_64x20000_contacts"}, "adjoint": out}
+        print(json.dumps(line), flush=True)
 
 
 def main():
@@ -647,38 +818,28 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the secondary measurements of the headline line")
+    ap.add_argument("--max-iters", type=int, default=MAX_ITERS,
+                    help="iteration budget of the time-to-residual solves (default: the benchmark's)")
     ap.add_argument("--profile", type=int, default=0,
                     help="run one solve capped at this many iterations and exit (for ncu captures)")
     ap.add_argument("--workload", default="apgd",
                     choices=["apgd", "batch", "gs", "mixed", "admm", "dama", "adjoint"],
-                    help="apgd: the benchmark line; batch / gs / mixed / admm / dama / adjoint: secondary measurements")
+                    help="apgd: the benchmark line; batch / adjoint (sharded over ranks under torchrun), gs, mixed, "
+                         "admm, dama: the secondary measurements on their own")
     ap.add_argument("--profile-mixed", action="store_true",
                     help="with --profile: the FP32-refined solve (FP32 iterations, then 1 FP64 iteration)")
     args = ap.parse_args()
-    if args.workload == "mixed":
-        run_mixed(args)
-        return
-    if args.workload == "admm":
-        run_admm(args)
-        return
-    if args.workload == "adjoint":
-        run_adjoint(args)
-        return
-    if args.workload == "dama":
-        run_dama(args)
-        return
-    if args.workload == "batch":
-        run_batch(args)
-        return
-    if args.workload == "gs":
-        run_gs(args)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    single = {"mixed": run_mixed, "admm": run_admm, "dama": run_dama, "gs": run_gs}
+    if args.workload in single:
+        single[args.workload](args)
         return
     if args.profile:
         run_profile(args.profile, args.profile_mixed)
         return
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
@@ -688,7 +849,12 @@ def main():
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         torch.cuda.set_device(local_rank)
         torch.distributed.init_process_group("nccl", device_id=torch.device(f"cuda:{local_rank}"))
-    run_ours(args, rank, world, local_rank)
+    if args.workload == "batch":
+        run_batch(args, rank, world, local_rank)
+    elif args.workload == "adjoint":
+        run_adjoint(args, rank, world, local_rank)
+    else:
+        run_ours(args, rank, world, local_rank)
     if world > 1:
         import torch
 
