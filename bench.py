@@ -410,7 +410,7 @@ def measure_secondary(args, D, d, r_fp64, fp64_ms):
         "residual": res, "reached_tol": bool(res < TOL), "trace": trace[::2],
         "note": "does not reach 1e-6: residual 5.1e-3 after 1000 sweeps (8.5 s) on this problem"}
     out["batch_4096"] = measure_batch(args, sample_stride=16)
-    out["adjoint_64x20000"] = measure_adjoint(args, steps=2)
+    out["adjoint_64x20000"] = measure_adjoint(args, steps=1)
     return out
 
 
@@ -499,9 +499,46 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
     solve(pgm)
     mixed_ms, (res_m, its_m) = _sync_time(lambda: solve(pgm), world)
     st_m = D.solve_stats()
+    # the launch shape chosen by the tuner (measured on this batch) against the default rule, same results
+    rule_shape = D.batchShape()
+    D.setBatchTuning(True)
+    t0 = time.perf_counter()
+    solve(pg)  # tunes (candidates measured at 30 iterations each), then solves
+    torch.cuda.synchronize()
+    tune_wall_ms = (time.perf_counter() - t0) * 1e3
+    tuned_times = []
+    for _ in range(steps):
+        ms, (res_t, its_t) = _sync_time(lambda: solve(pg), world)
+        tuned_times.append(ms)
+    tuned_same = bool(np.array_equal(res_t, res) and np.array_equal(its_t, its) and
+                      np.array_equal(r.cpu().numpy(), r_batch))
+    tuned = {"shape": D.batchShape(), "rule_shape": rule_shape, "batched_ms": statistics.median(tuned_times),
+             "tuning_wall_ms": tune_wall_ms, "candidates": [[list(sh), ms] for sh, ms in D.batchTuningLog()],
+             "identical_results": tuned_same,
+             "shape_key": "(schedule 0: one CTA per problem / 1: teams, CTAs per SM, team size)"}
+    D.setBatchTuning(False)
+    # the captured CUDA graph (upload of r, solve, download of r and results) against the plain host-buffer call
+    keep = []
+    rh = pinned_copy(np.zeros(3 * sub.n), keep)
+    plain, graph = [], []
+    for k in range(steps + 1):
+        rh[...] = 0.0
+        t0 = time.perf_counter()
+        D.solveBatchWith(pg, rh)
+        plain.append((time.perf_counter() - t0) * 1e3)
+        rh[...] = 0.0
+        t0 = time.perf_counter()
+        res_g, its_g = D.solveBatchGraph(pg, rh)
+        graph.append((time.perf_counter() - t0) * 1e3)
+    graph_same = bool(np.array_equal(res_g, res) and np.array_equal(its_g, its) and np.array_equal(rh, r_batch))
+    graphed = {"plain_call_ms": statistics.median(plain[1:]), "graph_replay_ms": statistics.median(graph[1:]),
+               "capture_call_ms": graph[0], "identical_results": graph_same,
+               "note": "host-buffer calls (pinned r), wall time per call including copies; the first graph call "
+                       "captures"}
     allres = shard.gather_results(mine, np.stack([res, its, res_m], 1), nprob, world)
     out = {"problems": nprob, "contacts": int(d.n), "ranks": world, "max_iters": BATCH_MAX_ITERS,
            "batched_ms": statistics.median(times), "kernel_ms": statistics.median(kernel),
+           "tuned": tuned, "cuda_graph": graphed,
            "algorithmic_gbs": st["algorithmic_bytes"] / (st["device_ms"] * 1e-3) / 1e9,
            "fp32_refined": {"split": "up to 200 FP32 + 300 FP64 iterations per problem", "batched_ms": mixed_ms,
                             "kernel_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"]},
@@ -751,9 +788,10 @@ def run_dama(args) -> None:
 
 def measure_adjoint(args, steps=2, rank=0, world=1, dev=0):
     """Gradient workload: 64 problems x 20 000 contacts (bodies = contacts / 3, compliance 0.05 I), forward =
-    batched APGD with the SOC law to 1e-10 per problem, loss L = g . r with g ~ N(0, 1); backward = the adjoint
-    (dL/db, dL/dmu) over the batch, then dL/dH, dL/dw, dL/df. Reports t_adjoint / t_forward (device times). With
-    several ranks each solves its share of the problems (all of equal size)."""
+    batched APGD to 1e-10 per problem, loss L = g . r with g ~ N(0, 1); backward = the adjoint (dL/db, dL/dmu)
+    over the batch, then dL/dH, dL/dw, dL/df. Both laws: the Coulomb problem (the configuration's law, adjoint by
+    bi-conjugate gradients stabilised) and the SOC problem (conjugate gradients). Reports t_adjoint / t_forward
+    (device times). With several ranks each solves its share of the problems (all of equal size)."""
     import bogus_gpu
     from bogus_gpu import generator, shard
 
@@ -773,38 +811,45 @@ def measure_adjoint(args, steps=2, rank=0, world=1, dev=0):
     pg.setMaxIters(MAX_ADJ_FWD_ITERS)
     g = np.random.default_rng(6).standard_normal(3 * d.n)
     g_mine = g.reshape(-1, 3)[np.concatenate([np.arange(cptr[p], cptr[p + 1]) for p in mine])].reshape(-1)
-    fwd, adj, prim = [], [], []
-    for k in range(1 + steps):
-        r = np.zeros(3 * sub.n)
-        res, its = D.solveBatchWith(pg, r)
-        tf = D.solve_stats()["device_ms"]
-        D.adjoint(r, g_mine, tol=1e-10)
-        ta = D.solve_stats()["device_ms"]
-        t1 = time.perf_counter()
-        D.adjoint_primal(P)
-        t2 = time.perf_counter()
-        if k >= 1:
-            fwd.append(tf)
-            adj.append(ta)
-            prim.append((t2 - t1) * 1e3)
-    tf, ta = max_over_ranks(statistics.median(fwd), world, "cuda"), max_over_ranks(statistics.median(adj), world, "cuda")
-    allres = shard.gather_results(mine, np.stack([res, its], 1), nprob, world)
-    out = {"problems": nprob, "contacts": int(d.n), "ranks": world, "compliance": generator.ADJOINT_COMPLIANCE,
-           "forward_ms": tf, "adjoint_ms": ta, "t_adjoint_over_t_forward": ta / tf,
-           "adjoint_cg_iterations": D.last_adjoint_iterations, "adjoint_rel_residual": D.last_adjoint_residual,
-           "primal_gradients_wall_ms": statistics.median(prim),
-           "timing": f"median of {steps} after a warm-up; device times (CUDA events) of the batched solve kernel "
-                     "and of the adjoint kernel (max over ranks)"}
-    if allres is not None:
-        out["forward_iterations_max"] = int(allres[:, 1].max())
-        out["forward_converged_fraction"] = float(np.mean(allres[:, 0] < 1e-10))
+    out = {"problems": nprob, "contacts": int(d.n), "ranks": world, "compliance": generator.ADJOINT_COMPLIANCE}
+    for law, coulomb in (("coulomb", True), ("soc", False)):
+        fwd, adj, prim = [], [], []
+        # the Coulomb forward runs up to 20 000 iterations (tens of seconds): it is timed without a warm-up
+        warm = 0 if coulomb else 1
+        for k in range(warm + steps):
+            r = np.zeros(3 * sub.n)
+            res, its = D.solveBatchWith(pg, r, staticProblem=not coulomb)
+            tf = D.solve_stats()["device_ms"]
+            D.adjoint(r, g_mine, tol=1e-10, coulomb=coulomb)
+            ta = D.solve_stats()["device_ms"]
+            t1 = time.perf_counter()
+            D.adjoint_primal(P)
+            t2 = time.perf_counter()
+            if k >= warm:
+                fwd.append(tf)
+                adj.append(ta)
+                prim.append((t2 - t1) * 1e3)
+        tf = max_over_ranks(statistics.median(fwd), world, "cuda")
+        ta = max_over_ranks(statistics.median(adj), world, "cuda")
+        allres = shard.gather_results(mine, np.stack([res, its], 1), nprob, world)
+        e = {"forward_ms": tf, "adjoint_ms": ta, "t_adjoint_over_t_forward": ta / tf,
+             "adjoint_iterations": D.last_adjoint_iterations, "adjoint_rel_residual": D.last_adjoint_residual,
+             "adjoint_solver": "BiCGSTAB (2 W passes per iteration)" if coulomb else "CG (1 W pass per iteration)",
+             "primal_gradients_wall_ms": statistics.median(prim)}
+        if allres is not None:
+            e["forward_iterations_max"] = int(allres[:, 1].max())
+            e["forward_converged_fraction"] = float(np.mean(allres[:, 0] < 1e-10))
+        out[law] = e
+    out["timing"] = (f"median of {steps} (SOC: after a warm-up); device times (CUDA events) of the batched solve "
+                     "kernel and of the adjoint kernel (max over ranks)")
+    out["t_adjoint_over_t_forward"] = out["coulomb"]["t_adjoint_over_t_forward"]
     return out
 
 
 def run_adjoint(args, rank=0, world=1, dev=0) -> None:
     out = measure_adjoint(args, steps=args.steps, rank=rank, world=world, dev=dev)
     if rank == 0:
-        line = {"metric": "adjoint / forward time, 64 x 20 000 contacts", "value": out["t_adjoint_over_t_forward"],
+        line = {"metric": "adjoint / forward time, 64 x 20 000 contacts, Coulomb law", "value": out["t_adjoint_over_t_forward"],
                 "unit": "ratio", "n_gpus": world, "steps": args.steps, "higher_is_better": False,
                 "scaling": "strong", "dtype": "f64", "data": "synthetic (seeded adjoint batch generator)",
                 "config": {"workload": "adjoint_64x20000_contacts"}, "adjoint": out}

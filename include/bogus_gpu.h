@@ -210,6 +210,38 @@ int bogus_gpu_solve_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o
 int bogus_gpu_solve_pg_batch_device(bogus_gpu_problem* h, const bogus_gpu_pg_options* opts, double* d_r,
                                     double* residuals, unsigned* iters);
 
+/* Launch shape of the batched solves. schedule 0: one CTA per problem, at most ctas_per_sm resident CTAs per SM;
+ * schedule 1: teams of team_size CTAs per problem (a cooperative launch), at most ctas_per_sm CTAs per SM. Every
+ * shape gives the same results bit for bit: each problem's reductions follow its fixed 32-contact chunk order. */
+typedef struct bogus_gpu_batch_shape {
+  int schedule;
+  int ctas_per_sm;
+  int team_size;
+} bogus_gpu_batch_shape;
+
+/* on != 0: the first batched solve of each precision after bogus_gpu_set_batch measures the candidate shapes on
+ * the batch itself (one CTA per problem at 1..4 CTAs per SM; teams of 2, 4, 8, 16 CTAs at 2 and 3 CTAs per SM;
+ * each run capped at 30 iterations from the same starting iterate, timed with CUDA events) and keeps the fastest,
+ * which later solves reuse; the choice is also cached for the process by device, precision and the batch's size
+ * class (problems, largest problem, total 32-contact chunks). 0 (default): a fixed rule (one CTA per problem when
+ * there are at least half as many problems as resident CTAs, else teams). */
+int bogus_gpu_set_batch_tuning(bogus_gpu_problem* h, int on);
+/* Forces the shape of the following batched solves (NULL: back to tuning or the rule). */
+int bogus_gpu_set_batch_shape(bogus_gpu_problem* h, const bogus_gpu_batch_shape* shape);
+/* The shape of the last batched launch. */
+int bogus_gpu_get_batch_shape(const bogus_gpu_problem* h, bogus_gpu_batch_shape* shape);
+/* The tuner's last measurements: *count shapes and their times in ms (pass NULL arrays to get the count). */
+int bogus_gpu_get_batch_tuning_log(const bogus_gpu_problem* h, bogus_gpu_batch_shape* shapes, double* ms, int* count);
+
+/* bogus_gpu_solve_pg_batch (FP64) with the whole sequence (upload of r, the solve, download of r and of the
+ * per-problem results) captured once into a CUDA graph and replayed by later calls with the same options, host
+ * buffer and batch: for a simulation that solves the same batch layout every step, one graph launch replaces the
+ * separate copies, memsets and kernel launch. r must be page-locked host memory (cudaHostAlloc /
+ * cudaHostRegister; BOGUS_GPU_BAD_INPUT otherwise). The shape (and tuning, when enabled) is settled before the
+ * capture. Results are those of bogus_gpu_solve_pg_batch, bit for bit. */
+int bogus_gpu_solve_pg_batch_graph(bogus_gpu_problem* h, const bogus_gpu_pg_options* opts, double* r,
+                                   double* residuals, unsigned* iters);
+
 /* DualFrictionProblem::solveCadoux (Interfaces/FrictionProblem.impl.hpp:76-92, Interfaces/Cadoux.hpp:44-91): the
  * Coulomb problem solved as up to cadoux_iters SOCQP problems u = W r + (b + COV(u_prev)), each by the
  * Gauss-Seidel or projected-gradient minimizer with its tolerance tightened to 0.1 max(tol, min(res, 1)). r is
@@ -283,16 +315,21 @@ int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_opti
                              const double* f, const double* w, const double* mu, int static_problem, double* v,
                              double* r, double* residual, unsigned* iters);
 
-/* ---- Adjoint of the SOC solve (no counterpart in the reference, which has no differentiation) ------------
+/* ---- Adjoint of the SOC and Coulomb solves (no counterpart in the reference, which has no differentiation) --
  * r solves min 1/2 r^T W r + b^T r over r_i in K_mu_i = {|x_T| <= mu x_N} (the SOCLaw<3> problem that
- * bogus_gpu_solve_pg solves with static_problem = 1). Given that solution r and g = dL/dr of a loss L, the
- * implicit-function gradients dL/db and dL/dmu follow from one linear solve (conjugate gradients on the
- * device, one pass over W per iteration, to relative residual tol). r should be solved tightly: the
+ * bogus_gpu_solve_pg solves with static_problem = 1), or (options.coulomb) the Coulomb friction problem
+ * (static_problem = 0). Given that solution r and g = dL/dr of a loss L, the implicit-function gradients dL/db and
+ * dL/dmu follow from one linear solve on the device, to relative residual tol. r should be solved tightly: the
  * gradients are those of the fixed point at r. W must be positive definite on the contacts' active
  * directions (add a compliance term, bogus_gpu_add_compliance, where H M^-1 H^T is singular). */
 typedef struct bogus_gpu_adjoint_options {
   double tol;                     /* 1e-10 */
   unsigned max_iters;             /* 5000 */
+  int coulomb;                    /* 0: the SOC problem (conjugate gradients). 1: the Coulomb problem that
+                                     bogus_gpu_solve_pg / _gs solve with static_problem = 0, the fixed point
+                                     r = P(r - A (u + s(u))) with the De Saxce term s(u) = (mu |u_T|, 0, 0)
+                                     (SOCLaw::dualityCOV); its linearisation is not symmetric and is solved by
+                                     bi-conjugate gradients stabilised, two passes over W per iteration */
 } bogus_gpu_adjoint_options;
 void bogus_gpu_adjoint_options_default(bogus_gpu_adjoint_options* opts);
 /* dL_db (3 n) and dL_dmu (n) from r and dL_dr (host arrays); residual: final relative CG residual. */

@@ -1,5 +1,5 @@
-"""Dense FP64 implicit-function gradients of the SOC friction solve. Test infrastructure only (the checker of
-the GPU adjoint; only tests/ import it).
+"""Dense FP64 implicit-function gradients of the SOC and Coulomb friction solves. Test infrastructure only (the
+checker of the GPU adjoint; only tests/ import it).
 
 The reference has no differentiation; this oracle defines what the GPU adjoint must compute, independently of
 the GPU's formulation:
@@ -16,7 +16,8 @@ and through W = H M^-1 H^T + C (C constant) and b = w - H M^-1 f, with s = dL/db
 v_s = M^-1 H^T s:
   dL/dH_ik = s_i (v_r - M^-1 f)_k^T + r_i (v_s)_k^T,   dL/dw = s,   dL/df = -v_s.
 The projection Jacobian is written from the closed form of the projection (its values are checked against
-finite differences of the projection in the tests).
+finite differences of the projection in the tests). The Coulomb problem adds the De Saxce term to the fixed
+point (implicit_gradient(coulomb=True)); the primal gradients are the same functions of s = dL/db.
 """
 from __future__ import annotations
 
@@ -59,20 +60,38 @@ def projection_jacobian(mu: float, x: np.ndarray):
 
 
 def implicit_gradient(W: np.ndarray, b: np.ndarray, mu: np.ndarray, r: np.ndarray, g: np.ndarray,
-                      alpha: float = 1.0):
-    """Dense implicit gradients at the solution r: returns (dL/db, dL/dmu, dL/dW dense)."""
+                      alpha: float = 1.0, coulomb: bool = False):
+    """Dense implicit gradients at the solution r: returns (dL/db, dL/dmu, dL/dW dense).
+
+    coulomb=True: r solves the Coulomb friction problem, the fixed point r = P(r - alpha (u + s(u))) with
+    u = W r + b and the De Saxce term s(u) = (mu |u_T|, 0, 0) (SOCLaw::dualityCOV, SOCLaw.hpp:92-99). With
+    T = I + e_N tau^T, tau = (0, mu u_T / |u_T|) (0 where u_T = 0), the linearisation is
+      (I - J + alpha J T W) dr = -alpha J T (dW r + db) + (K - alpha |u_T| J e_N) dmu,
+    so B = I - J + alpha J T W, B^T lam = g, dL/db = -alpha T^T J^T lam,
+    dL/dmu_i = K_i^T lam_i - alpha |u_T,i| (J lam)_i,N and dL/dW = (dL/db) r^T."""
     n = mu.size
-    x = r - alpha * (W @ r + b)
+    u = W @ r + b
+    T = np.eye(3 * n)
+    tn = np.zeros(n)
+    x = r - alpha * u
+    if coulomb:
+        for i in range(n):
+            ui = u[3 * i:3 * i + 3]
+            t = np.linalg.norm(ui[1:])
+            tn[i] = t
+            x[3 * i] -= alpha * mu[i] * t
+            if t > 0:
+                T[3 * i, 3 * i + 1:3 * i + 3] = mu[i] * ui[1:] / t
     J = np.zeros((3 * n, 3 * n))
     K = np.zeros((n, 3))
     for i in range(n):
         Ji, Ki = projection_jacobian(mu[i], x[3 * i:3 * i + 3])
         J[3 * i:3 * i + 3, 3 * i:3 * i + 3] = Ji
         K[i] = Ki
-    B = np.eye(3 * n) - J + alpha * J @ W
+    B = np.eye(3 * n) - J + alpha * J @ T @ W
     lam = np.linalg.solve(B.T, g)
-    s = -alpha * J.T @ lam
-    dmu = np.einsum("ik,ik->i", K, lam.reshape(n, 3))
+    s = -alpha * T.T @ (J.T @ lam)
+    dmu = np.einsum("ik,ik->i", K, lam.reshape(n, 3)) - alpha * tn * (J @ lam).reshape(n, 3)[:, 0]
     return s, dmu, np.outer(s, r)
 
 

@@ -63,7 +63,7 @@ class DualAmaOptions(C.Structure):
 
 
 class AdjointOptions(C.Structure):
-    _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint)]
+    _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint), ("coulomb", C.c_int)]
 
 
 class MecheOptions(C.Structure):
@@ -76,6 +76,10 @@ class MecheOptions(C.Structure):
     def __init__(self):
         super().__init__()
         lib().bogus_gpu_meche_options_default(C.byref(self))
+
+
+class BatchShape(C.Structure):
+    _fields_ = [("schedule", C.c_int), ("ctas_per_sm", C.c_int), ("team_size", C.c_int)]
 
 
 class SolveStats(C.Structure):
@@ -105,6 +109,8 @@ EXPORTED = [
     "bogus_gpu_solve_product_gs", "bogus_gpu_dual_ama_options_default", "bogus_gpu_solve_dual_ama",
     "bogus_gpu_set_body_dofs", "bogus_gpu_set_frames", "bogus_gpu_apply_permutation", "bogus_gpu_undo_permutation", "bogus_gpu_permuted",
     "bogus_gpu_set_wait_limit", "bogus_gpu_test_wait_timeout", "bogus_gpu_get_dual_rhs",
+    "bogus_gpu_set_batch_tuning", "bogus_gpu_set_batch_shape", "bogus_gpu_get_batch_shape",
+    "bogus_gpu_get_batch_tuning_log", "bogus_gpu_solve_pg_batch_graph",
 ]
 
 
@@ -185,6 +191,12 @@ def lib():
     L.bogus_gpu_set_wait_limit.argtypes = [C.c_int, C.c_double]
     L.bogus_gpu_test_wait_timeout.argtypes = [vp, C.c_int]
     L.bogus_gpu_get_dual_rhs.argtypes = [vp, vp, vp]
+    L.bogus_gpu_set_batch_tuning.argtypes = [vp, C.c_int]
+    L.bogus_gpu_set_batch_shape.argtypes = [vp, C.POINTER(BatchShape)]
+    L.bogus_gpu_get_batch_shape.argtypes = [vp, C.POINTER(BatchShape)]
+    L.bogus_gpu_get_batch_tuning_log.argtypes = [vp, vp, vp, C.POINTER(C.c_int)]
+    L.bogus_gpu_solve_pg_batch_graph.argtypes = [vp, C.POINTER(PgOptions), vp, _dp,
+                                                 np.ctypeslib.ndpointer(dtype=np.uint32)]
     _lib = L
     return L
 
@@ -653,12 +665,13 @@ class DualFrictionProblem:
         return res.value
 
     # ---- adjoint of the SOC solve (no counterpart in the reference) ----
-    def adjoint(self, r, dL_dr, tol: float = 1e-10, max_iters: int = 5000):
-        """Implicit-function gradients at the SOC solution r: returns (dL/db [3n], dL/dmu [n]); the final relative
-        residual of the linear solve is in self.last_adjoint_residual."""
+    def adjoint(self, r, dL_dr, tol: float = 1e-10, max_iters: int = 5000, coulomb: bool = False):
+        """Implicit-function gradients at the solution r of the SOC problem (or, coulomb=True, of the Coulomb
+        problem): returns (dL/db [3n], dL/dmu [n]); the final relative residual of the linear solve is in
+        self.last_adjoint_residual."""
         o = AdjointOptions()
         lib().bogus_gpu_adjoint_options_default(C.byref(o))
-        o.tol, o.max_iters = float(tol), int(max_iters)
+        o.tol, o.max_iters, o.coulomb = float(tol), int(max_iters), int(bool(coulomb))
         db = np.zeros(3 * self.n)
         dmu = np.zeros(self.n)
         res = C.c_double()
@@ -753,6 +766,44 @@ class DualFrictionProblem:
         _check(st)
         self.last_status = st
         return res, its
+
+    def solveBatchGraph(self, solver: "ProjectedGradient", r_pinned, staticProblem: bool = True):
+        """solveBatchWith through the captured CUDA graph (bogus_gpu_solve_pg_batch_graph): r_pinned is a float64
+        array in page-locked memory (e.g. a pinned torch tensor's numpy view), solved in place."""
+        res = np.zeros(self.nproblems)
+        its = np.zeros(self.nproblems, np.uint32)
+        o = solver.options(staticProblem)
+        st = lib().bogus_gpu_solve_pg_batch_graph(self._h, C.byref(o), C.c_void_p(r_pinned.ctypes.data), res, its)
+        _check(st)
+        self.last_status = st
+        return res, its
+
+    def setBatchTuning(self, on: bool = True) -> None:
+        """Tune the batched launch shape on the device at the next batched solve of each precision."""
+        _check(lib().bogus_gpu_set_batch_tuning(self._h, int(bool(on))), False)
+
+    def setBatchShape(self, schedule=None, ctas_per_sm: int = 0, team_size: int = 1) -> None:
+        """Force the batched launch shape (schedule 0: one CTA per problem, 1: teams); None: back to the default."""
+        if schedule is None:
+            _check(lib().bogus_gpu_set_batch_shape(self._h, None), False)
+            return
+        sh = BatchShape(int(schedule), int(ctas_per_sm), int(team_size))
+        _check(lib().bogus_gpu_set_batch_shape(self._h, C.byref(sh)), False)
+
+    def batchShape(self) -> tuple:
+        """(schedule, ctas_per_sm, team_size) of the last batched launch."""
+        sh = BatchShape()
+        _check(lib().bogus_gpu_get_batch_shape(self._h, C.byref(sh)), False)
+        return sh.schedule, sh.ctas_per_sm, sh.team_size
+
+    def batchTuningLog(self) -> list:
+        """[((schedule, ctas_per_sm, team_size), ms), ...] measured by the last tuning."""
+        k = C.c_int(0)
+        _check(lib().bogus_gpu_get_batch_tuning_log(self._h, None, None, C.byref(k)), False)
+        shapes = (BatchShape * max(1, k.value))()
+        ms = np.zeros(max(1, k.value))
+        _check(lib().bogus_gpu_get_batch_tuning_log(self._h, shapes, ms.ctypes.data_as(C.c_void_p), C.byref(k)), False)
+        return [((shapes[i].schedule, shapes[i].ctas_per_sm, shapes[i].team_size), float(ms[i])) for i in range(k.value)]
 
 
 def measure_fp64_peak(device: int = 0) -> float:

@@ -10,7 +10,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "bogus_gpu.h"
@@ -194,6 +197,7 @@ struct bogus_gpu_problem {
   std::vector<unsigned> meche_ndof;
   // adjoint: per-contact basis, CG vectors, the last solution r and s = dL/db (device and host copies)
   DevBuf<double> adj_V, adj_Pc, adj_D, adj_K, adj_P, adj_R, adj_Z, adj_Dir, adj_Y, adj_Q, adj_S, adj_dmu, adj_r, adj_g;
+  DevBuf<double> adj_Tc, adj_Rh, adj_Ph, adj_Sv, adj_Sh, adj_Tv;  // Coulomb law: |u_T| and tau, BiCGSTAB vectors
   DevBuf<AdjOut> adj_out;
   bool adj_valid = false;
   std::vector<double> h_adj_s, h_adj_r;
@@ -205,6 +209,22 @@ struct bogus_gpu_problem {
   DevBuf<unsigned> team_cnt;  // team schedule of the batched solve: counters, jobs, published scalars
   DevBuf<int> team_job;
   DevBuf<double> team_scal;
+  // launch shape of the batched solves: forced by the caller, or tuned on the device (per precision) and cached
+  // until the next bogus_gpu_set_batch; the shape of the last batched launch
+  bool batch_tuning = false;
+  BatchShape forced_shape, tuned_shape[2], last_shape;
+  DevBuf<double> tune_x;  // the batch's starting iterate, kept while the tuner tries shapes
+  std::vector<BatchShape> tune_cand;  // the shapes the tuner measured last, and their times (ms)
+  std::vector<double> tune_ms;
+  // the batched solve captured in a CUDA graph (bogus_gpu_solve_pg_batch_graph) and what it was captured with
+  cudaGraphExec_t batch_graph = nullptr;
+  PGBatchArgs graph_args{};
+  PGTeamArgs graph_team{};
+  BatchShape graph_shape;
+  const double* graph_r = nullptr;
+  PGOut* pinned_out = nullptr;  // page-locked copies of the per-problem results and the status word
+  int* pinned_status = nullptr;
+  int pinned_np = 0;
   bogus_gpu_callback callback = nullptr;
   void* callback_user = nullptr;
   bool test_wait_timeout = false;  // bogus_gpu_test_wait_timeout
@@ -908,6 +928,10 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   if (!h) return BOGUS_GPU_OK;
   cudaSetDevice(h->device);
   cudaStreamSynchronize(h->stream);
+  if (h->batch_graph) cudaGraphExecDestroy(h->batch_graph);
+  if (h->pinned_out) cudaFreeHost(h->pinned_out);
+  if (h->pinned_status) cudaFreeHost(h->pinned_status);
+  h->tune_x.release();
   for (auto* b : {&h->val, &h->b, &h->mu, &h->scaling, &h->X, &h->MX, &h->Y, &h->S0, &h->XB, &h->Wv, &h->csum,
                   &h->scal, &h->trace, &h->vx, &h->vy, &h->chunk, &h->scalar, &h->minv, &h->H, &h->T, &h->mf})
     b->release();
@@ -928,7 +952,8 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   h->cad_b.release();
   for (auto* b : {&h->meche_E, &h->meche_w, &h->meche_r, &h->meche_v, &h->meche_fd}) b->release();
   for (auto* b : {&h->adj_V, &h->adj_Pc, &h->adj_D, &h->adj_K, &h->adj_P, &h->adj_R, &h->adj_Z, &h->adj_Dir,
-                  &h->adj_Y, &h->adj_Q, &h->adj_S, &h->adj_dmu, &h->adj_r, &h->adj_g})
+                  &h->adj_Y, &h->adj_Q, &h->adj_S, &h->adj_dmu, &h->adj_r, &h->adj_g, &h->adj_Tc, &h->adj_Rh,
+                  &h->adj_Ph, &h->adj_Sv, &h->adj_Sh, &h->adj_Tv})
     b->release();
   h->adj_out.release();
   h->rowptr.release();
@@ -2229,6 +2254,8 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   for (auto* b : {&h->adj_D, &h->adj_K, &h->adj_P, &h->adj_R, &h->adj_Z, &h->adj_Dir, &h->adj_Y, &h->adj_Q,
                   &h->adj_S})
     BG_CUDA(b->ensure(n3));
+  if (o->coulomb)
+    for (auto* b : {&h->adj_Tc, &h->adj_Rh, &h->adj_Ph, &h->adj_Sv, &h->adj_Sh, &h->adj_Tv}) BG_CUDA(b->ensure(n3));
   BG_CUDA(h->adj_dmu.ensure(n > 0 ? n : 1));
   BG_CUDA(h->adj_out.ensure(1));
   const int C = (n + 31) / 32;
@@ -2271,6 +2298,14 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   a.stripes = h->scal.p + 8;
   a.tol = o->tol;
   a.max_iters = o->max_iters;
+  if (o->coulomb) {
+    a.Tc = h->adj_Tc.p;
+    a.Rh = h->adj_Rh.p;
+    a.Ph = h->adj_Ph.p;
+    a.Sv = h->adj_Sv.p;
+    a.Sh = h->adj_Sh.p;
+    a.Tv = h->adj_Tv.p;
+  }
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 8 * sizeof(unsigned), s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   int grid = adjoint_max_grid(h->device);
@@ -2278,7 +2313,7 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   const int want = (C + 7) / 8;
   if (want < grid) grid = want < 1 ? 1 : want;
   BG_CUDA(cudaEventRecord(h->ev0, s));
-  BG_CUDA(launch_adjoint(a, grid, s));
+  BG_CUDA(o->coulomb ? launch_adjoint_coulomb(a, grid, s) : launch_adjoint(a, grid, s));
   BG_CUDA(cudaEventRecord(h->ev1, s));
   AdjOut out{};
   int st = 0;
@@ -2293,11 +2328,20 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   h->last_stats.iterations = out.iters;
   h->last_stats.refine_iterations = 0;
   h->last_stats.fp32_device_ms = 0.0;
-  h->last_stats.w_passes = out.iters + 2;
-  // per iteration per contact: basis 9 x 2, preconditioner 9, D 3 x 2, vectors (dir, Y, Q, P, R, Z) 3 each,
-  // read and written as the phases need them (about 16 streams)
-  h->last_stats.algorithmic_bytes = (out.iters + 2) * wpass + (double)out.iters * n * 8.0 * (18 + 9 + 6 + 3 * 16);
-  h->last_stats.fp64_fma = (out.iters + 2) * 9.0 * (double)h->W.nnzb;
+  if (o->coulomb) {
+    // per BiCGSTAB iteration: two W passes; per contact the basis (9) x 4, D and tau (6) x 4, the preconditioner
+    // (9) x 2 and about 26 vector streams of 3 values
+    h->last_stats.w_passes = 2 * out.iters + 2;
+    h->last_stats.algorithmic_bytes =
+        (2.0 * out.iters + 2) * wpass + (double)out.iters * n * 8.0 * (36 + 24 + 18 + 3 * 26);
+    h->last_stats.fp64_fma = (2.0 * out.iters + 2) * 9.0 * (double)h->W.nnzb;
+  } else {
+    h->last_stats.w_passes = out.iters + 2;
+    // per iteration per contact: basis 9 x 2, preconditioner 9, D 3 x 2, vectors (dir, Y, Q, P, R, Z) 3 each,
+    // read and written as the phases need them (about 16 streams)
+    h->last_stats.algorithmic_bytes = (out.iters + 2) * wpass + (double)out.iters * n * 8.0 * (18 + 9 + 6 + 3 * 16);
+    h->last_stats.fp64_fma = (out.iters + 2) * 9.0 * (double)h->W.nnzb;
+  }
   h->adj_valid = true;
   if (residual) *residual = out.rel_res;
   if (iters) *iters = out.iters;
@@ -2322,6 +2366,7 @@ void bogus_gpu_adjoint_options_default(bogus_gpu_adjoint_options* o) {
   if (!o) return;
   o->tol = 1e-10;
   o->max_iters = 5000;
+  o->coulomb = 0;
 }
 
 int bogus_gpu_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, const double* r,
@@ -2981,58 +3026,210 @@ int bogus_gpu_set_batch(bogus_gpu_problem* h, int nproblems, const int* cptr) {
   h->nproblems = nproblems;
   h->h_contact_ptr.assign(cptr, cptr + nproblems + 1);
   h->h_problem_nnz = nnz;
+  h->tuned_shape[0] = h->tuned_shape[1] = BatchShape{};
+  h->tune_ms.clear();
+  h->tune_cand.clear();
+  if (h->batch_graph) {
+    cudaGraphExecDestroy(h->batch_graph);
+    h->batch_graph = nullptr;
+  }
   return BOGUS_GPU_OK;
 }
 
+}  // extern "C"
+
 namespace {
 
-// Schedule of a batched solve: one CTA per problem (k_pg_batched) when there are at least as many problems as
-// half the resident CTAs, else teams of `size` CTAs per problem (k_pg_team), sized so that the teams fill the
-// GPU and each CTA's warps still have a chunk of the largest problem each. Launches the chosen kernel.
-int launch_batch_schedule(bogus_gpu_problem* h, const PGBatchArgs* ba64, const PGBatchArgs32* ba32) {
-  const bool fp32 = ba32 != nullptr;
-  const int np = h->nproblems;
-  cudaStream_t s = h->stream;
-  const int gmax = pg_team_grid(h->device, fp32);
-  if (gmax <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "occupancy query failed");
+// ---- launch shape of a batched solve ------------------------------------------------------------------
+int batch_max_chunks(const bogus_gpu_problem* h) {
   int maxchunks = 0;
-  for (int p = 0; p < np; ++p)
+  for (int p = 0; p < h->nproblems; ++p)
     maxchunks = std::max(maxchunks, (h->h_contact_ptr[p + 1] - h->h_contact_ptr[p] + 31) / 32);
+  return maxchunks;
+}
+
+// The default rule: one CTA per problem (k_pg_batched, as many resident CTAs as fit) when there are at least as
+// many problems as half the resident team CTAs (3 per SM), else teams sized so that they fill the GPU and each
+// CTA's warps still have a chunk of the largest problem each.
+BatchShape rule_shape(const bogus_gpu_problem* h, bool fp32) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  const int np = h->nproblems;
+  const int team_per = std::min(3, pg_team_per_sm(h->device, fp32));
+  const int gmax = team_per * sms;
   int size = np > 0 ? gmax / np : 0;
-  size = std::min(size, std::min(16, std::max(1, maxchunks / 8)));
+  size = std::min(size, std::min(16, std::max(1, batch_max_chunks(h) / 8)));
+  BatchShape sh;
   if (size < 2) {
-    int grid = pg_batched_grid(h->device, fp32);
-    if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "occupancy query failed");
-    if (np < grid) grid = np > 0 ? np : 1;
-    BG_CUDA(cudaMemsetAsync(h->next.p, 0, sizeof(int), s));
-    BG_CUDA(cudaEventRecord(h->ev0, s));
-    BG_CUDA(fp32 ? launch_pg_batched(*ba32, grid, s) : launch_pg_batched(*ba64, grid, s));
-    BG_CUDA(cudaEventRecord(h->ev1, s));
-    return BOGUS_GPU_OK;
+    sh.schedule = 0;
+    sh.ctas_per_sm = pg_batched_per_sm(h->device, fp32);
+    sh.team_size = 1;
+  } else {
+    sh.schedule = 1;
+    sh.ctas_per_sm = team_per;
+    sh.team_size = size;
   }
-  const int teams = std::min(np, gmax / size);
+  return sh;
+}
+
+int check_shape(const bogus_gpu_problem* h, const BatchShape& sh, bool fp32) {
+  const int per = sh.schedule == 0 ? pg_batched_per_sm(h->device, fp32) : pg_team_per_sm(h->device, fp32);
+  if (sh.schedule != 0 && sh.schedule != 1) return fail(BOGUS_GPU_BAD_INPUT, "batch schedule must be 0 or 1");
+  if (sh.ctas_per_sm < 1 || sh.ctas_per_sm > per)
+    return fail(BOGUS_GPU_BAD_INPUT, "ctas_per_sm must lie in [1, " + std::to_string(per) + "] for this kernel");
+  if (sh.schedule == 1 && (sh.team_size < 1 || sh.team_size > 64)) return fail(BOGUS_GPU_BAD_INPUT, "team_size must lie in [1, 64]");
+  return BOGUS_GPU_OK;
+}
+
+// Team arguments and grid of a shape (schedule 1); allocates the team counters.
+int team_setup(bogus_gpu_problem* h, const BatchShape& sh, PGTeamArgs* ta, int* grid) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  const int np = h->nproblems;
+  const int teams = std::max(1, std::min(np, sh.ctas_per_sm * sms / sh.team_size));
   BG_CUDA(h->team_cnt.ensure(8 * (size_t)teams));
   BG_CUDA(h->team_job.ensure(teams));
   BG_CUDA(h->team_scal.ensure(40 * (size_t)teams));
+  *ta = PGTeamArgs{sh.team_size, h->team_cnt.p, h->team_job.p, h->team_scal.p, h->status.p};
+  *grid = teams * sh.team_size;
+  return BOGUS_GPU_OK;
+}
+
+// Enqueues one batched launch with the given shape (counters cleared first; nothing waits for it). The status word
+// (a wait of the team schedule that ran out) is read by the caller after the stream is synchronised.
+int launch_shape(bogus_gpu_problem* h, const BatchShape& sh, const PGBatchArgs* ba64, const PGBatchArgs32* ba32,
+                 bool events) {
+  const bool fp32 = ba32 != nullptr;
+  const int np = h->nproblems;
+  cudaStream_t s = h->stream;
   BG_CUDA(h->status.ensure(1));
-  BG_CUDA(cudaMemsetAsync(h->team_cnt.p, 0, sizeof(unsigned) * 8 * teams, s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
   BG_CUDA(cudaMemsetAsync(h->next.p, 0, sizeof(int), s));
-  const PGTeamArgs ta{size, h->team_cnt.p, h->team_job.p, h->team_scal.p, h->status.p};
-  BG_CUDA(cudaEventRecord(h->ev0, s));
-  BG_CUDA(fp32 ? launch_pg_team(*ba32, ta, teams * size, s) : launch_pg_team(*ba64, ta, teams * size, s));
-  BG_CUDA(cudaEventRecord(h->ev1, s));
+  if (sh.schedule == 0) {
+    int sms = 0;
+    BG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+    int grid = sh.ctas_per_sm * sms;
+    if (np < grid) grid = np > 0 ? np : 1;
+    if (events) BG_CUDA(cudaEventRecord(h->ev0, s));
+    BG_CUDA(fp32 ? launch_pg_batched(*ba32, grid, s) : launch_pg_batched(*ba64, grid, s));
+    if (events) BG_CUDA(cudaEventRecord(h->ev1, s));
+  } else {
+    PGTeamArgs ta{};
+    int grid = 0;
+    if (int e = team_setup(h, sh, &ta, &grid)) return e;
+    BG_CUDA(cudaMemsetAsync(h->team_cnt.p, 0, sizeof(unsigned) * 8 * (size_t)(grid / sh.team_size), s));
+    if (events) BG_CUDA(cudaEventRecord(h->ev0, s));
+    BG_CUDA(fp32 ? launch_pg_team(*ba32, ta, grid, s) : launch_pg_team(*ba64, ta, grid, s));
+    if (events) BG_CUDA(cudaEventRecord(h->ev1, s));
+  }
+  h->last_shape = sh;
+  return BOGUS_GPU_OK;
+}
+
+int read_status(bogus_gpu_problem* h) {
   int st = 0;
-  BG_CUDA(cudaMemcpyAsync(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  BG_CUDA(cudaStreamSynchronize(s));
+  BG_CUDA(cudaMemcpy(&st, h->status.p, sizeof(int), cudaMemcpyDeviceToHost));
   if (st != 0) return fail(st, "device-side wait timed out in the batched solve");
   return BOGUS_GPU_OK;
 }
 
-int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residuals, unsigned* iters) {
-  const int n = h->W.n;
-  const size_t n3 = 3 * (size_t)n;
-  const int np = h->nproblems;
+// The candidate shapes the tuner measures: one CTA per problem at 1..occupancy CTAs per SM (up to 4), and teams of
+// 2, 4, 8, 16 CTAs (no larger than a quarter of the largest problem's chunks allows) at 2 and 3 CTAs per SM.
+std::vector<BatchShape> tune_candidates(const bogus_gpu_problem* h, bool fp32) {
+  std::vector<BatchShape> c;
+  const int pb = std::min(4, pg_batched_per_sm(h->device, fp32));
+  for (int k = 1; k <= pb; ++k) c.push_back(BatchShape{0, k, 1});
+  const int pt = std::min(3, pg_team_per_sm(h->device, fp32));
+  const int tmax = std::max(2, batch_max_chunks(h) / 4);
+  for (int t = 2; t <= 16 && t <= tmax; t *= 2)
+    for (int k = 2; k <= pt; ++k) c.push_back(BatchShape{1, k, t});
+  return c;
+}
+
+// Process-wide cache of tuned shapes by device, precision and batch size class (problems, largest problem's and
+// total chunks), so that another handle with a batch of the same make-up reuses the choice.
+struct TuneKey {
+  int device, fp32, np, maxchunks;
+  long long chunks;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(device, fp32, np, maxchunks, chunks) < std::tie(o.device, o.fp32, o.np, o.maxchunks, o.chunks);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, BatchShape> g_tune_cache;
+
+TuneKey tune_key(const bogus_gpu_problem* h, bool fp32) {
+  long long chunks = 0;
+  for (int p = 0; p < h->nproblems; ++p) chunks += (h->h_contact_ptr[p + 1] - h->h_contact_ptr[p] + 31) / 32;
+  return TuneKey{h->device, fp32 ? 1 : 0, h->nproblems, batch_max_chunks(h), chunks};
+}
+
+constexpr unsigned kTuneIters = 30;
+
+int launch_args(bogus_gpu_problem* h, const BatchShape& sh, const PGBatchArgs& ba) {
+  return launch_shape(h, sh, &ba, nullptr, true);
+}
+int launch_args(bogus_gpu_problem* h, const BatchShape& sh, const PGBatchArgs32& ba) {
+  return launch_shape(h, sh, nullptr, &ba, true);
+}
+
+// Measures every candidate shape on the batch itself (each run from the same starting iterate, capped at
+// kTuneIters iterations, timed with CUDA events) and keeps the fastest. The starting iterate (x0, 3 n values of
+// type T) is restored afterwards.
+template <class BA>
+int tune_shape(bogus_gpu_problem* h, BA ba, bool fp32, size_t bytes_x0, void* x0) {
+  cudaStream_t s = h->stream;
+  BG_CUDA(h->tune_x.ensure((bytes_x0 + 7) / 8));
+  BG_CUDA(cudaMemcpyAsync(h->tune_x.p, x0, bytes_x0, cudaMemcpyDeviceToDevice, s));
+  ba.base.max_iters = std::min(ba.base.max_iters, kTuneIters);
+  const std::vector<BatchShape> cand = tune_candidates(h, fp32);
+  h->tune_cand = cand;
+  h->tune_ms.assign(cand.size(), 0.0);
+  int best = -1;
+  for (size_t k = 0; k < cand.size(); ++k) {
+    BG_CUDA(cudaMemcpyAsync(x0, h->tune_x.p, bytes_x0, cudaMemcpyDeviceToDevice, s));
+    if (int e = launch_args(h, cand[k], ba)) return e;
+    BG_CUDA(cudaStreamSynchronize(s));
+    if (int st = read_status(h)) return st;
+    float ms = 0.f;
+    BG_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    h->tune_ms[k] = ms;
+    if (best < 0 || ms < h->tune_ms[best]) best = (int)k;
+  }
+  BG_CUDA(cudaMemcpyAsync(x0, h->tune_x.p, bytes_x0, cudaMemcpyDeviceToDevice, s));
+  h->tuned_shape[fp32 ? 1 : 0] = cand[best];
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune_cache[tune_key(h, fp32)] = cand[best];
+  return BOGUS_GPU_OK;
+}
+
+// The shape of the next batched launch: the caller's, else the tuned one (tuning first when enabled and not yet
+// done for this batch and precision, or taken from the process-wide cache), else the rule.
+template <class BA>
+int choose_shape(bogus_gpu_problem* h, const BA& ba, bool fp32, size_t bytes_x0, void* x0, BatchShape* out) {
+  if (h->forced_shape.schedule >= 0) {
+    if (int e = check_shape(h, h->forced_shape, fp32)) return e;
+    *out = h->forced_shape;
+    return BOGUS_GPU_OK;
+  }
+  if (h->batch_tuning) {
+    BatchShape& t = h->tuned_shape[fp32 ? 1 : 0];
+    if (t.schedule < 0) {
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      auto it = g_tune_cache.find(tune_key(h, fp32));
+      if (it != g_tune_cache.end()) t = it->second;
+    }
+    if (t.schedule < 0)
+      if (int e = tune_shape(h, ba, fp32, bytes_x0, x0)) return e;
+    *out = t;
+    return BOGUS_GPU_OK;
+  }
+  *out = rule_shape(h, fp32);
+  return BOGUS_GPU_OK;
+}
+
+PGBatchArgs batch_args64(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
+  const size_t n3 = 3 * (size_t)h->W.n;
   PGBatchArgs ba{};
   PGArgs& a = ba.base;
   a.rowptr = h->W.rowptr;
@@ -3060,18 +3257,19 @@ int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   a.pess = o->ls_pessimistic_factor;
   a.max_iters = o->max_iters;
   a.ls_iters = o->ls_iters;
-  ba.nproblems = np;
+  ba.nproblems = h->nproblems;
   ba.contact_ptr = h->contact_ptr.p;
   ba.chunk_ptr = h->chunk_ptr.p;
   ba.queue = h->queue.p;
   ba.next = h->next.p;
   ba.r = h->X.p;  // each problem's best iterate is copied over its initial iterate
-  if (int e = launch_batch_schedule(h, &ba, nullptr)) return e;
-  std::vector<PGOut> out(np);
-  if (np) BG_CUDA(cudaMemcpyAsync(out.data(), h->batch_out.p, sizeof(PGOut) * np, cudaMemcpyDeviceToHost, h->stream));
-  BG_CUDA(cudaStreamSynchronize(h->stream));
-  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
-  h->last_launches = 1;
+  return ba;
+}
+
+// Per-problem outputs and the solve statistics from the per-problem results.
+int finish_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, const PGOut* out, double* residuals,
+                 unsigned* iters) {
+  const int np = h->nproblems;
   bool all = true;
   PGTraffic sum;
   unsigned maxit = 0;
@@ -3093,6 +3291,21 @@ int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   h->last_stats.algorithmic_bytes = sum.bytes;
   h->last_stats.fp64_fma = sum.fma;
   return all ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
+}
+
+int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residuals, unsigned* iters) {
+  const int np = h->nproblems;
+  const PGBatchArgs ba = batch_args64(h, o);
+  BatchShape sh;
+  if (int e = choose_shape(h, ba, false, sizeof(double) * 3 * (size_t)h->W.n, h->X.p, &sh)) return e;
+  if (int e = launch_shape(h, sh, &ba, nullptr, true)) return e;
+  std::vector<PGOut> out(np);
+  if (np) BG_CUDA(cudaMemcpyAsync(out.data(), h->batch_out.p, sizeof(PGOut) * np, cudaMemcpyDeviceToHost, h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  if (int e = read_status(h)) return e;
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  h->last_launches = 1;
+  return finish_batch(h, o, out.data(), residuals, iters);
 }
 
 int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
@@ -3117,7 +3330,7 @@ int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
 
 }  // namespace
 
-}  // extern "C"
+
 
 namespace {
 
@@ -3181,11 +3394,14 @@ int run_pg_batch_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, doub
   ba.next = h->next.p;
   ba.r = h->X32.p;
   BG_CUDA(launch_convert(n3, h->X.p, h->X32.p, s));
-  if (int e = launch_batch_schedule(h, nullptr, &ba)) return e;
+  BatchShape sh;
+  if (int e = choose_shape(h, ba, true, sizeof(float) * n3, h->X32.p, &sh)) return e;
+  if (int e = launch_shape(h, sh, nullptr, &ba, true)) return e;
   std::vector<PGOut> out32(np);
   if (np) BG_CUDA(cudaMemcpyAsync(out32.data(), h->batch_out.p, sizeof(PGOut) * np, cudaMemcpyDeviceToHost, s));
   BG_CUDA(launch_convert(n3, h->X32.p, h->X.p, s));
   BG_CUDA(cudaStreamSynchronize(s));
+  if (int e = read_status(h)) return e;
   float ms32 = 0.f;
   BG_CUDA(cudaEventElapsedTime(&ms32, h->ev0, h->ev1));
   bogus_gpu_pg_options o64 = *o;
@@ -3235,6 +3451,139 @@ int bogus_gpu_solve_pg_batch_device(bogus_gpu_problem* h, const bogus_gpu_pg_opt
   BG_CUDA(cudaMemcpyAsync(d_r, h->X.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
   BG_CUDA(cudaStreamSynchronize(h->stream));
   return st;
+}
+
+int bogus_gpu_solve_pg_batch_graph(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* r, double* residuals,
+                                   unsigned* iters) {
+  if (int e = batch_checks(h, o)) return e;
+  if (o->mixed_precision) return fail(BOGUS_GPU_BAD_INPUT, "the captured batched solve is FP64 only");
+  const size_t n3 = 3 * (size_t)h->W.n;
+  const int np = h->nproblems;
+  if (n3 == 0) return BOGUS_GPU_OK;
+  {
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, r) != cudaSuccess || attr.type != cudaMemoryTypeHost) {
+      cudaGetLastError();
+      return fail(BOGUS_GPU_BAD_INPUT, "r must be page-locked host memory (cudaHostAlloc or cudaHostRegister)");
+    }
+  }
+  cudaStream_t s = h->stream;
+  if (h->pinned_np < np) {
+    if (h->pinned_out) cudaFreeHost(h->pinned_out);
+    h->pinned_out = nullptr;
+    h->pinned_np = 0;
+    BG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&h->pinned_out), sizeof(PGOut) * np, cudaHostAllocDefault));
+    h->pinned_np = np;
+  }
+  if (!h->pinned_status) BG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&h->pinned_status), sizeof(int), cudaHostAllocDefault));
+  BG_CUDA(h->status.ensure(1));
+  const PGBatchArgs ba = batch_args64(h, o);
+  // the shape is chosen (and tuned, when enabled) before any capture: tuning synchronises and needs the starting
+  // iterate on the device
+  if (h->forced_shape.schedule < 0 && h->batch_tuning && h->tuned_shape[0].schedule < 0)
+    BG_CUDA(cudaMemcpyAsync(h->X.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s));
+  BatchShape sh;
+  if (int e = choose_shape(h, ba, false, sizeof(double) * n3, h->X.p, &sh)) return e;
+  PGTeamArgs ta{};
+  int tgrid = 0;
+  if (sh.schedule == 1)
+    if (int e = team_setup(h, sh, &ta, &tgrid)) return e;
+  const bool same = h->batch_graph && std::memcmp(&h->graph_args, &ba, sizeof(ba)) == 0 &&
+                    std::memcmp(&h->graph_team, &ta, sizeof(ta)) == 0 && h->graph_shape == sh && h->graph_r == r;
+  if (!same) {
+    if (h->batch_graph) {
+      cudaGraphExecDestroy(h->batch_graph);
+      h->batch_graph = nullptr;
+    }
+    BG_CUDA(cudaStreamSynchronize(s));
+    BG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int e = BOGUS_GPU_OK;
+    {
+      const cudaError_t c = cudaMemcpyAsync(h->X.p, r, sizeof(double) * n3, cudaMemcpyHostToDevice, s);
+      if (c != cudaSuccess) e = fail(BOGUS_GPU_CUDA_ERROR, std::string("capture: ") + cudaGetErrorString(c));
+    }
+    if (!e) e = launch_shape(h, sh, &ba, nullptr, false);
+    if (!e && np) {
+      const cudaError_t c = cudaMemcpyAsync(h->pinned_out, h->batch_out.p, sizeof(PGOut) * np, cudaMemcpyDeviceToHost, s);
+      if (c != cudaSuccess) e = fail(BOGUS_GPU_CUDA_ERROR, std::string("capture: ") + cudaGetErrorString(c));
+    }
+    if (!e) {
+      cudaError_t c = cudaMemcpyAsync(h->pinned_status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (c == cudaSuccess) c = cudaMemcpyAsync(r, h->X.p, sizeof(double) * n3, cudaMemcpyDeviceToHost, s);
+      if (c != cudaSuccess) e = fail(BOGUS_GPU_CUDA_ERROR, std::string("capture: ") + cudaGetErrorString(c));
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (e) {
+      if (graph) cudaGraphDestroy(graph);
+      return e;
+    }
+    if (ce != cudaSuccess) return fail(BOGUS_GPU_CUDA_ERROR, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+    const cudaError_t ie = cudaGraphInstantiate(&h->batch_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+      h->batch_graph = nullptr;
+      return fail(BOGUS_GPU_CUDA_ERROR, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+    }
+    h->graph_args = ba;
+    h->graph_team = ta;
+    h->graph_shape = sh;
+    h->graph_r = r;
+  }
+  BG_CUDA(cudaEventRecord(h->ev0, s));
+  BG_CUDA(cudaGraphLaunch(h->batch_graph, s));
+  BG_CUDA(cudaEventRecord(h->ev1, s));
+  BG_CUDA(cudaStreamSynchronize(s));
+  if (*h->pinned_status != 0) return fail(*h->pinned_status, "device-side wait timed out in the batched solve");
+  BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  h->last_launches = 1;
+  h->last_shape = sh;
+  return finish_batch(h, o, h->pinned_out, residuals, iters);
+}
+
+int bogus_gpu_set_batch_tuning(bogus_gpu_problem* h, int on) {
+  if (int e = check_handle(h)) return e;
+  h->batch_tuning = on != 0;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_set_batch_shape(bogus_gpu_problem* h, const bogus_gpu_batch_shape* shape) {
+  if (int e = check_handle(h)) return e;
+  if (!shape) {
+    h->forced_shape = BatchShape{};
+    return BOGUS_GPU_OK;
+  }
+  const BatchShape sh{shape->schedule, shape->ctas_per_sm, shape->team_size};
+  if (int e = set_device(h)) return e;
+  if (int e = check_shape(h, sh, false)) return e;
+  if (int e = check_shape(h, sh, true)) return e;
+  h->forced_shape = sh;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_get_batch_shape(const bogus_gpu_problem* h, bogus_gpu_batch_shape* shape) {
+  if (int e = check_handle(h)) return e;
+  if (!shape) return fail(BOGUS_GPU_BAD_INPUT, "null output");
+  shape->schedule = h->last_shape.schedule;
+  shape->ctas_per_sm = h->last_shape.ctas_per_sm;
+  shape->team_size = h->last_shape.team_size;
+  return BOGUS_GPU_OK;
+}
+
+int bogus_gpu_get_batch_tuning_log(const bogus_gpu_problem* h, bogus_gpu_batch_shape* shapes, double* ms, int* count) {
+  if (int e = check_handle(h)) return e;
+  if (!count) return fail(BOGUS_GPU_BAD_INPUT, "null output");
+  const int k = (int)h->tune_ms.size();
+  if (shapes || ms) {
+    if (*count < k) return fail(BOGUS_GPU_BAD_INPUT, "output arrays too short");
+    const std::vector<BatchShape>& cand = h->tune_cand;
+    for (int i = 0; i < k && i < (int)cand.size(); ++i) {
+      if (shapes) shapes[i] = bogus_gpu_batch_shape{cand[i].schedule, cand[i].ctas_per_sm, cand[i].team_size};
+      if (ms) ms[i] = h->tune_ms[i];
+    }
+  }
+  *count = k;
+  return BOGUS_GPU_OK;
 }
 
 int bogus_gpu_get_dual_lower(bogus_gpu_problem* h, int* rowptr, int* colidx, double* blocks, int* nnzb_lower) {

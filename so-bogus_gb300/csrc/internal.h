@@ -102,6 +102,19 @@ struct PGTeamArgs {
   double* scal;        // 40 per team: the scalars published by the team's last barrier, then 32 stripe sums
   int* status;
 };
+// Launch shape of a batched solve. schedule 0: one CTA per problem (k_pg_batched), at most ctas_per_sm resident
+// CTAs per SM; schedule 1: teams of team_size CTAs per problem (k_pg_team), at most ctas_per_sm CTAs per SM. Every
+// shape gives the same results bit for bit (the chunk order of each problem's reductions is fixed).
+struct BatchShape {
+  int schedule = -1;  // -1: none
+  int ctas_per_sm = 0;
+  int team_size = 0;
+  bool operator==(const BatchShape& o) const {
+    return schedule == o.schedule && ctas_per_sm == o.ctas_per_sm && team_size == o.team_size;
+  }
+};
+int pg_batched_per_sm(int device, bool fp32);  // occupancy of k_pg_batched (CTAs per SM)
+int pg_team_per_sm(int device, bool fp32);     // occupancy of k_pg_team (CTAs per SM)
 cudaError_t launch_pg_team(const PGBatchArgs& b, const PGTeamArgs& t, int grid, cudaStream_t s);
 cudaError_t launch_pg_team(const PGBatchArgs32& b, const PGTeamArgs& t, int grid, cudaStream_t s);
 int pg_team_grid(int device, bool fp32);
@@ -289,8 +302,13 @@ struct AdjArgs {
   GridBarrier gb;
   double tol;
   unsigned max_iters;
+  // Coulomb law (De Saxce change of variable, bi-conjugate gradients stabilised): per contact (|u_T|, tau) with
+  // tau = mu u_T / |u_T|, and five more work vectors (3 per contact)
+  double* Tc;
+  double *Rh, *Ph, *Sv, *Sh, *Tv;
 };
 cudaError_t launch_adjoint(const AdjArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_adjoint_coulomb(const AdjArgs& a, int grid, cudaStream_t s);
 int adjoint_max_grid(int device);
 // Helpers of the primal gradients and of the compliance term (kernels_grad.cu)
 cudaError_t launch_body_transpose(int nbodies, int d, const int* bptr, const int* bent, const double* H,

@@ -1,4 +1,5 @@
-// Adjoint of the SOC friction solve (no counterpart in the reference, which has no differentiation).
+// Adjoint of the SOC friction solve and of the Coulomb friction solve (no counterpart in the reference, which has
+// no differentiation).
 //
 // r solves min 1/2 r^T W r + b^T r over r_i in K_mu_i (SOCLaw<3>, the problem ProjectedGradient solves with
 // staticProblem), i.e. the fixed point r = P(x), x = r - A (W r + b) for any positive diagonal step A (here
@@ -321,6 +322,312 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
   }
 }
 
+// ---- Coulomb law ----------------------------------------------------------------------------------------
+// With the De Saxce change of variable the fixed point is r = P(x), x = r - A (u + s(u)), u = W r + b,
+// s(u) = (mu |u_T|, 0, 0) (SOCLaw::dualityCOV). Its derivative ds/du = e_N tau^T with tau = (0, mu u_T / |u_T|)
+// (zero where u_T = 0) makes the linearised map non-symmetric: with T = I + e_N tau^T the adjoint system is
+// (I - J + W T^T A J) lam = g. In the basis of J as above, the unmasked components of p = alpha theta lam_hat solve
+//   (D + M V^T W T^T V M) p = M V^T g,
+// by bi-conjugate gradients stabilised (two passes over W per iteration), right-preconditioned with the inverse
+// of the 3 x 3 diagonal blocks diag(D_i) + V_i^T W_ii T_i^T V_i. Then
+//   dL/db = s = -T^T V M p,   lam_hat (masked) = v_k^T (g + W s),   lam_hat (unmasked) = p_k / (alpha theta_k),
+//   dL/dmu_i = K_i^T V_i lam_hat_i - |u_T,i| (V_i M p_i)_N.
+
+// y = T^T V (m o p), T^T y = y + tau y_N (tc = (|u_T|, tau_1, tau_2))
+__device__ __forceinline__ void coulomb_apply(const double* V, const double* D, const double* tc, const double* p,
+                                              double* y) {
+  basis_apply(V, D, p, y);
+  y[1] = fma(tc[1], y[0], y[1]);
+  y[2] = fma(tc[2], y[0], y[2]);
+}
+
+// Inverse of diag(D) + V^T Wii T^T V on the unmasked components (identity on the masked ones), by Gauss-Jordan
+// elimination with partial pivoting; a zero pivot leaves that component unpreconditioned.
+__device__ void precond_block_coulomb(const double* V, const double* D, const double* tc, const double* Wii,
+                                      double* Pinv) {
+  double TV[9];  // T^T V, column k = T^T v_k
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    TV[k] = V[k];
+    TV[3 + k] = fma(tc[1], V[k], V[3 + k]);
+    TV[6 + k] = fma(tc[2], V[k], V[6 + k]);
+  }
+  double WT[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) WT[3 * r + k] = Wii[3 * r] * TV[k] + Wii[3 * r + 1] * TV[3 + k] + Wii[3 * r + 2] * TV[6 + k];
+  double A[3][6];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double v = V[j] * WT[k] + V[3 + j] * WT[3 + k] + V[6 + j] * WT[6 + k];
+      const bool mj = D[j] < 0.0, mk = D[k] < 0.0;
+      A[j][k] = (mj || mk) ? (j == k ? 1.0 : 0.0) : v + (j == k ? D[j] : 0.0);
+      A[j][3 + k] = j == k ? 1.0 : 0.0;
+    }
+  for (int c = 0; c < 3; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < 3; ++r)
+      if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
+    if (!(fabs(A[piv][c]) > 0.0)) continue;
+    if (piv != c)
+      for (int k = 0; k < 6; ++k) {
+        const double t = A[c][k];
+        A[c][k] = A[piv][k];
+        A[piv][k] = t;
+      }
+    const double inv = 1.0 / A[c][c];
+    for (int k = 0; k < 6; ++k) A[c][k] *= inv;
+    for (int r = 0; r < 3; ++r) {
+      if (r == c) continue;
+      const double f = A[r][c];
+      if (f != 0.0)
+        for (int k = 0; k < 6; ++k) A[r][k] = fma(-f, A[c][k], A[r][k]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) Pinv[3 * j + k] = A[j][3 + k];
+}
+
+__global__ void __launch_bounds__(256) k_adjoint_coulomb(AdjArgs a) {
+  __shared__ double smem8[8];
+  __shared__ ChunkScratch cs[8];
+  AdjCtx ctx{a, smem8};
+  ChunkScratch& sh = cs[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  const int C = a.nchunks;
+  const bool writer = blockIdx.x == 0 && threadIdx.x == 0;
+  auto put = [&](int q, int c, double v) {
+    v = warp_sum_butterfly(v);
+    if (lane == 0) a.csum[q * C + c] = v;
+  };
+  auto product = [&](int c, const double* src, double* acc) {
+    spmv_chunk<1>(a.rowptr, InterleavedBlocks<double>{a.icol, a.ival, a.slot0}, a.n, c, sh,
+                  [&](int j, double* x) { ld3(src, j, x); }, acc);
+  };
+  auto load_basis = [&](int i, double* V, double* D, double* tc) {
+    for (int k = 0; k < 9; ++k) V[k] = ldcg(a.V + 9 * (size_t)i + k);
+    ld3(a.D, i, D);
+    ld3(a.Tc, i, tc);
+  };
+  // A q for the current W-operand product: D o q + m o V^T (W Y)
+  auto op_tail = [&](int i, const double* acc, const double* q, double* out) {
+    double V[9], D[3], tc[3], t[3];
+    load_basis(i, V, D, tc);
+    basis_apply_t(V, D, acc, t);
+    for (int k = 0; k < 3; ++k) out[k] = (D[k] < 0.0 ? 0.0 : D[k] * q[k]) + t[k];
+  };
+  // setup: u = W r + b, s(u), x = r - alpha (u + s(u)), the basis, tau, the preconditioner; rhs c = m o V^T g;
+  // p = 0, residual = shadow = c, direction = v = 0
+  for (int c = gwarp; c < C; c += nwarps) {
+    const int i = 32 * c + lane;
+    double acc[3] = {0.0, 0.0, 0.0};
+    product(c, a.r, acc);
+    double rr = 0.0;
+    if (i < a.n) {
+      double r[3], u[3], x[3], V[9], D[3], K[3], g[3], cv[3], Wii[9], Pinv[9], tc[3];
+      ld3(a.r, i, r);
+      const double mu = __ldg(a.mu + i);
+      const double al = 1.0 / __ldg(a.scaling + i);
+      for (int k = 0; k < 3; ++k) u[k] = acc[k] + __ldg(a.b + 3 * i + k);
+      const double t = sqrt(u[1] * u[1] + u[2] * u[2]);
+      const double sN = mu * t;
+      x[0] = r[0] - al * (u[0] + sN);
+      x[1] = r[1] - al * u[1];
+      x[2] = r[2] - al * u[2];
+      tc[0] = t;
+      tc[1] = t > 0.0 ? mu * u[1] / t : 0.0;
+      tc[2] = t > 0.0 ? mu * u[2] / t : 0.0;
+      projection_basis(mu, x, al, V, D, K);
+      const int dk = __ldg(a.diag + i);
+      for (int k = 0; k < 9; ++k) Wii[k] = dk >= 0 ? __ldg(a.val + 9 * (size_t)dk + k) : 0.0;
+      precond_block_coulomb(V, D, tc, Wii, Pinv);
+      for (int k = 0; k < 9; ++k) {
+        a.V[9 * (size_t)i + k] = V[k];
+        a.Pc[9 * (size_t)i + k] = Pinv[k];
+      }
+      st3(a.D, i, D);
+      st3(a.K, i, K);
+      st3(a.Tc, i, tc);
+      ld3(a.g, i, g);
+      basis_apply_t(V, D, g, cv);
+      const double zero[3] = {0.0, 0.0, 0.0};
+      st3(a.P, i, zero);
+      st3(a.R, i, cv);
+      st3(a.Rh, i, cv);
+      st3(a.Dir, i, zero);
+      st3(a.Q, i, zero);
+      rr = cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2];
+    }
+    put(0, c, rr);
+  }
+  if (!ctx.sync_reduce(1)) return;
+  const double rr0 = ldcg(a.scal);
+  double rr = rr0, rho_old = 1.0, alpha = 1.0, omega = 1.0, rho = rr0;
+  unsigned it = 0;
+  const double stop = a.tol * a.tol * rr0;
+  for (; it < a.max_iters; ++it) {
+    if (!(rr > stop)) break;
+    const double beta = (rho / rho_old) * (alpha / omega);
+    // direction = r + beta (direction - omega v); ph = Pinv direction; Y = T^T V (m o ph)
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      if (i < a.n) {
+        double res[3], d[3], v[3], Pinv[9], ph[3], V[9], D[3], tc[3], y[3];
+        ld3(a.R, i, res);
+        ld3(a.Dir, i, d);
+        ld3(a.Q, i, v);
+        for (int k = 0; k < 9; ++k) Pinv[k] = ldcg(a.Pc + 9 * (size_t)i + k);
+        for (int k = 0; k < 3; ++k) d[k] = fma(beta, fma(-omega, v[k], d[k]), res[k]);
+        mat3_apply(Pinv, d, ph);
+        load_basis(i, V, D, tc);
+        coulomb_apply(V, D, tc, ph, y);
+        st3(a.Dir, i, d);
+        st3(a.Ph, i, ph);
+        st3(a.Y, i, y);
+      }
+    }
+    if (!ctx.sync()) return;
+    // v = A ph; shadow . v
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      double acc[3] = {0.0, 0.0, 0.0};
+      product(c, a.Y, acc);
+      double hv = 0.0;
+      if (i < a.n) {
+        double ph[3], v[3], rh[3];
+        ld3(a.Ph, i, ph);
+        op_tail(i, acc, ph, v);
+        st3(a.Q, i, v);
+        ld3(a.Rh, i, rh);
+        hv = rh[0] * v[0] + rh[1] * v[1] + rh[2] * v[2];
+      }
+      put(0, c, hv);
+    }
+    if (!ctx.sync_reduce(1)) return;
+    const double hv = ldcg(a.scal);
+    if (!(hv != 0.0)) break;  // breakdown (or exact convergence)
+    alpha = rho / hv;
+    // s = r - alpha v; sh = Pinv s; Y = T^T V (m o sh)
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      if (i < a.n) {
+        double res[3], v[3], sv[3], Pinv[9], shv[3], V[9], D[3], tc[3], y[3];
+        ld3(a.R, i, res);
+        ld3(a.Q, i, v);
+        for (int k = 0; k < 3; ++k) sv[k] = fma(-alpha, v[k], res[k]);
+        for (int k = 0; k < 9; ++k) Pinv[k] = ldcg(a.Pc + 9 * (size_t)i + k);
+        mat3_apply(Pinv, sv, shv);
+        load_basis(i, V, D, tc);
+        coulomb_apply(V, D, tc, shv, y);
+        st3(a.Sv, i, sv);
+        st3(a.Sh, i, shv);
+        st3(a.Y, i, y);
+      }
+    }
+    if (!ctx.sync()) return;
+    // t = A sh; t . s, t . t
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      double acc[3] = {0.0, 0.0, 0.0};
+      product(c, a.Y, acc);
+      double ts = 0.0, tt = 0.0;
+      if (i < a.n) {
+        double shv[3], tv[3], sv[3];
+        ld3(a.Sh, i, shv);
+        op_tail(i, acc, shv, tv);
+        st3(a.Tv, i, tv);
+        ld3(a.Sv, i, sv);
+        ts = tv[0] * sv[0] + tv[1] * sv[1] + tv[2] * sv[2];
+        tt = tv[0] * tv[0] + tv[1] * tv[1] + tv[2] * tv[2];
+      }
+      put(0, c, ts);
+      put(1, c, tt);
+    }
+    if (!ctx.sync_reduce(2)) return;
+    const double ts = ldcg(a.scal), tt = ldcg(a.scal + 1);
+    omega = tt > 0.0 ? ts / tt : 0.0;
+    // p += alpha ph + omega sh; r = s - omega t; shadow . r, r . r
+    for (int c = gwarp; c < C; c += nwarps) {
+      const int i = 32 * c + lane;
+      double hr = 0.0, r2 = 0.0;
+      if (i < a.n) {
+        double p[3], ph[3], shv[3], sv[3], tv[3], res[3], rh[3];
+        ld3(a.P, i, p);
+        ld3(a.Ph, i, ph);
+        ld3(a.Sh, i, shv);
+        ld3(a.Sv, i, sv);
+        ld3(a.Tv, i, tv);
+        ld3(a.Rh, i, rh);
+        for (int k = 0; k < 3; ++k) {
+          p[k] = fma(omega, shv[k], fma(alpha, ph[k], p[k]));
+          res[k] = fma(-omega, tv[k], sv[k]);
+        }
+        st3(a.P, i, p);
+        st3(a.R, i, res);
+        hr = rh[0] * res[0] + rh[1] * res[1] + rh[2] * res[2];
+        r2 = res[0] * res[0] + res[1] * res[1] + res[2] * res[2];
+      }
+      put(0, c, hr);
+      put(1, c, r2);
+    }
+    if (!ctx.sync_reduce(2)) return;
+    rho_old = rho;
+    rho = ldcg(a.scal);
+    rr = ldcg(a.scal + 1);
+    if (!(omega != 0.0)) {
+      ++it;
+      break;
+    }
+  }
+  // s = dL/db = -T^T V (m o p)
+  for (int c = gwarp; c < C; c += nwarps) {
+    const int i = 32 * c + lane;
+    if (i < a.n) {
+      double V[9], D[3], tc[3], p[3], y[3];
+      load_basis(i, V, D, tc);
+      ld3(a.P, i, p);
+      coulomb_apply(V, D, tc, p, y);
+      const double s[3] = {-y[0], -y[1], -y[2]};
+      st3(a.S, i, s);
+    }
+  }
+  if (!ctx.sync()) return;
+  // lam_hat and dL/dmu = K^T V lam_hat - |u_T| (V m o p)_N
+  for (int c = gwarp; c < C; c += nwarps) {
+    const int i = 32 * c + lane;
+    double acc[3] = {0.0, 0.0, 0.0};
+    product(c, a.S, acc);
+    if (i < a.n) {
+      double V[9], D[3], tc[3], p[3], g[3], K[3], e[3], lh[3], vp[3];
+      load_basis(i, V, D, tc);
+      ld3(a.P, i, p);
+      ld3(a.g, i, g);
+      ld3(a.K, i, K);
+      const double al = 1.0 / __ldg(a.scaling + i);
+      for (int k = 0; k < 3; ++k) e[k] = g[k] + acc[k];
+      for (int k = 0; k < 3; ++k) {
+        if (D[k] < 0.0) lh[k] = V[k] * e[0] + V[3 + k] * e[1] + V[6 + k] * e[2];
+        else lh[k] = p[k] * (1.0 + al * D[k]) / al;  // p / (alpha theta), theta = 1 / (1 + alpha D)
+      }
+      double dm = 0.0;
+      for (int r2 = 0; r2 < 3; ++r2) dm += K[r2] * (V[3 * r2] * lh[0] + V[3 * r2 + 1] * lh[1] + V[3 * r2 + 2] * lh[2]);
+      basis_apply(V, D, p, vp);
+      a.dmu[i] = dm - tc[0] * vp[0];
+    }
+  }
+  if (writer) {
+    a.out->iters = it;
+    a.out->rel_res = rr0 > 0.0 ? sqrt(rr / rr0) : 0.0;
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_adjoint(const AdjArgs& a, int grid, cudaStream_t s) {
@@ -329,10 +636,19 @@ cudaError_t launch_adjoint(const AdjArgs& a, int grid, cudaStream_t s) {
   return cudaLaunchCooperativeKernel((const void*)k_adjoint, dim3(grid), dim3(256), args, 0, s);
 }
 
+cudaError_t launch_adjoint_coulomb(const AdjArgs& a, int grid, cudaStream_t s) {
+  AdjArgs copy = a;
+  void* args[] = {&copy};
+  return cudaLaunchCooperativeKernel((const void*)k_adjoint_coulomb, dim3(grid), dim3(256), args, 0, s);
+}
+
 int adjoint_max_grid(int device) {
   int sms = 0, per = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_adjoint, 256, 0) != cudaSuccess) return 0;
+  int per_c = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_c, k_adjoint_coulomb, 256, 0) != cudaSuccess) return 0;
+  if (per_c < per) per = per_c;
   if (per > 2) per = 2;
   return per * sms;
 }

@@ -622,8 +622,15 @@ __global__ void __launch_bounds__(256, 3) k_pg_team(PGBatchArgsT<T> ba, PGTeamAr
   unsigned* cnt = ta.counters + 8 * (size_t)team;
   const GridBarrier gb{cnt, cnt + 1, ta.status, (unsigned)ta.size};
   for (;;) {
+    // the last CTA to arrive takes the next problem and clears the team's chunk tickets: the final phase of the
+    // previous problem (a converged solve leaves its last product phase without a closing barrier) may have
+    // drawn tickets that no barrier cleared
     if (!grid_barrier(gb, [&] {
-          if (threadIdx.x == 0) ta.job[team] = (int)atomicAdd((unsigned*)ba.next, 1u);
+          if (threadIdx.x == 0) {
+            ta.job[team] = (int)atomicAdd((unsigned*)ba.next, 1u);
+            cnt[2] = 0u;
+            cnt[3] = 0u;
+          }
         }))
       return;
     const int job = *(volatile int*)(ta.job + team);
@@ -675,6 +682,22 @@ cudaError_t launch_pg_team(const PGBatchArgs& b, const PGTeamArgs& t, int grid, 
 
 cudaError_t launch_pg_team(const PGBatchArgs32& b, const PGTeamArgs& t, int grid, cudaStream_t s) {
   return launch_team_t(b, t, grid, s);
+}
+
+int pg_team_per_sm(int device, bool fp32) {
+  int per = 0;
+  (void)device;
+  const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_team<float>, 256, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_team<double>, 256, 0);
+  return e == cudaSuccess ? per : 0;
+}
+
+int pg_batched_per_sm(int device, bool fp32) {
+  int per = 0;
+  (void)device;
+  const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_batched<float>, 256, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_batched<double>, 256, 0);
+  return e == cudaSuccess ? per : 0;
 }
 
 int pg_team_grid(int device, bool fp32) {

@@ -53,10 +53,11 @@ class Problem:
                 vl[9 * k + e] += EPS_COMPLIANCE
         return rp, cl, vl, P.rhs(f, w)
 
-    def solve(self, b, mu, lower=None):
+    def solve(self, b, mu, lower=None, coulomb=False):
         rp, cl, vl = lower if lower is not None else (self.rp, self.cl, self.vl)
         O = self.oracle.DualProblem(rp, cl, vl, b, mu)
-        res, r, _ = O.solve_gs(np.zeros(3 * self.n), coulomb=False, tol=1e-34, max_iters=3000, coloring=False)
+        res, r, _ = O.solve_gs(np.zeros(3 * self.n), coulomb=coulomb, tol=1e-34, max_iters=5000 if coulomb else 3000,
+                               coloring=False)
         assert res < 1e-26
         return r
 
@@ -67,6 +68,13 @@ class Problem:
 @pytest.fixture(scope="module")
 def prob(oracle):
     return Problem(oracle)
+
+
+@pytest.fixture(scope="module")
+def prob_coulomb(prob):
+    """The same problem under the Coulomb law (De Saxce fixed point), solved by Gauss-Seidel to the FP64 floor."""
+    prob.rc = prob.solve(prob.b, prob.mu, coulomb=True)
+    return prob
 
 
 @pytest.fixture(scope="module")
@@ -132,6 +140,44 @@ def test_dense_gradient_matches_finite_differences(adj, prob):
     assert abs(fd(lambda t: primal_fd(f=prob.f + t * e)) - df[k]) <= 1e-5 * max(1.0, abs(df[k]))
 
 
+def test_dense_coulomb_gradient_matches_finite_differences(adj, prob_coulomb):
+    """The Coulomb problem: dL/db, dL/dmu and dL/dHA of the dense oracle (with the De Saxce term) against central
+    differences of the oracle's Coulomb Gauss-Seidel solve (1e-5), and independent of the fixed-point step."""
+    prob = prob_coulomb
+    s, dmu, _ = adj.implicit_gradient(prob.W, prob.b, prob.mu, prob.rc, prob.g, coulomb=True)
+    s2, dmu2, _ = adj.implicit_gradient(prob.W, prob.b, prob.mu, prob.rc, prob.g, alpha=0.37, coulomb=True)
+    assert np.abs(s - s2).max() <= 1e-10 * np.abs(s).max() and np.abs(dmu - dmu2).max() <= 1e-10 * np.abs(dmu).max()
+    d = prob.d
+    dHA, dHB, dw, df = adj.primal_gradients(s, prob.rc, d.minv, d.objA, d.objB, d.HA, d.HB, prob.f)
+    rng = np.random.default_rng(15)
+    h = FD_STEP
+
+    def fd(fn):
+        return (prob.loss(fn(+h)) - prob.loss(fn(-h))) / (2 * h)
+
+    nonzero_b = np.nonzero(np.abs(s) > 1e-3 * np.abs(s).max())[0]
+    for k in rng.choice(nonzero_b, 4, replace=False):
+        e = np.zeros(3 * prob.n)
+        e[k] = 1
+        assert abs(fd(lambda t: prob.solve(prob.b + t * e, prob.mu, coulomb=True)) - s[k]) <= 1e-5 * max(1.0, abs(s[k]))
+    nonzero_mu = np.nonzero(np.abs(dmu) > 1e-3 * np.abs(dmu).max())[0]
+    for i in rng.choice(nonzero_mu, 3, replace=False):
+        e = np.zeros(prob.n)
+        e[i] = 1
+        got = fd(lambda t: prob.solve(prob.b, prob.mu + t * e, coulomb=True))
+        assert abs(got - dmu[i]) <= 1e-5 * max(1.0, abs(dmu[i]))
+    for _ in range(2):
+        i, a, m = rng.integers(prob.n), rng.integers(3), rng.integers(6)
+        E = np.zeros_like(d.HA)
+        E[i, a, m] = 1
+
+        def primal(t):
+            rp, cl, vl, b = prob.assemble(d.HA + t * E, d.HB, prob.w, prob.f)
+            return prob.solve(b, prob.mu, (rp, cl, vl), coulomb=True)
+
+        assert abs(fd(primal) - dHA[i, a, m]) <= 1e-5 * max(1.0, abs(dHA[i, a, m]))
+
+
 # ---- GPU adjoint ---------------------------------------------------------------------------------------
 @pytest.fixture(scope="module")
 def gpu_prob(prob):
@@ -166,6 +212,25 @@ def test_gpu_adjoint_matches_dense_oracle(adj, prob, gpu_prob):
     d = prob.d
     dHA, dHB, dw, df = D.adjoint_primal(P)
     rHA, rHB, rw, rf = adj.primal_gradients(s_o, prob.r, d.minv, d.objA, d.objB, d.HA, d.HB, prob.f)
+    for got, ref in ((dHA, rHA), (dHB, rHB), (dw, rw), (df, rf)):
+        assert np.abs(got - ref).max() <= 1e-7 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.gpu
+def test_gpu_coulomb_adjoint_matches_dense_oracle(adj, prob_coulomb, gpu_prob):
+    """The Coulomb adjoint (bi-conjugate gradients stabilised on the De Saxce linearisation) against the dense
+    oracle: dL/db, dL/dmu and the primal gradients within 1e-8 relative."""
+    prob = prob_coulomb
+    D, P = gpu_prob
+    s_o, dmu_o, _ = adj.implicit_gradient(prob.W, prob.b, prob.mu, prob.rc, prob.g, coulomb=True)
+    s, dmu = D.adjoint(prob.rc, prob.g, tol=1e-13, coulomb=True)
+    assert D.last_adjoint_residual <= 1e-13
+    scale = np.abs(s_o).max()
+    assert np.abs(s - s_o).max() <= 1e-8 * scale
+    assert np.abs(dmu - dmu_o).max() <= 1e-8 * max(1.0, np.abs(dmu_o).max())
+    d = prob.d
+    dHA, dHB, dw, df = D.adjoint_primal(P)
+    rHA, rHB, rw, rf = adj.primal_gradients(s_o, prob.rc, d.minv, d.objA, d.objB, d.HA, d.HB, prob.f)
     for got, ref in ((dHA, rHA), (dHB, rHB), (dw, rw), (df, rf)):
         assert np.abs(got - ref).max() <= 1e-7 * max(1.0, np.abs(ref).max())
 
