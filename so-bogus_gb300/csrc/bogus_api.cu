@@ -2330,16 +2330,16 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   h->last_stats.fp32_device_ms = 0.0;
   if (o->coulomb) {
     // per BiCGSTAB iteration: two W passes; per contact the basis (9) x 4, D and tau (6) x 4, the preconditioner
-    // (9) x 2 and about 26 vector streams of 3 values
+    // (9) x 2 and 27 streams of 3 values over the five phases (6, 4, 5, 4 and 8, the products' gathers counted once)
     h->last_stats.w_passes = 2 * out.iters + 2;
     h->last_stats.algorithmic_bytes =
-        (2.0 * out.iters + 2) * wpass + (double)out.iters * n * 8.0 * (36 + 24 + 18 + 3 * 26);
+        (2.0 * out.iters + 2) * wpass + (double)out.iters * n * 8.0 * (36 + 24 + 18 + 3 * 27);
     h->last_stats.fp64_fma = (2.0 * out.iters + 2) * 9.0 * (double)h->W.nnzb;
   } else {
     h->last_stats.w_passes = out.iters + 2;
-    // per iteration per contact: basis 9 x 2, preconditioner 9, D 3 x 2, vectors (dir, Y, Q, P, R, Z) 3 each,
-    // read and written as the phases need them (about 16 streams)
-    h->last_stats.algorithmic_bytes = (out.iters + 2) * wpass + (double)out.iters * n * 8.0 * (18 + 9 + 6 + 3 * 16);
+    // per iteration per contact: basis 9 x 2, preconditioner 9, D 3 x 2, and 14 streams of 3 values as the phases
+    // read and write them: dir 4, Q 2, P 2, R 2, Z 2, Y 2 (its gather in the product counted once)
+    h->last_stats.algorithmic_bytes = (out.iters + 2) * wpass + (double)out.iters * n * 8.0 * (18 + 9 + 6 + 3 * 14);
     h->last_stats.fp64_fma = (out.iters + 2) * 9.0 * (double)h->W.nnzb;
   }
   h->adj_valid = true;
