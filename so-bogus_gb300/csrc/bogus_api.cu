@@ -2624,6 +2624,7 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   a.trace = h->trace.p;
   a.out = h->admm_out.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.tickets = h->barrier.p + 2;
   a.combine_count = h->barrier.p + 4;
   a.stripes = h->scal.p + 8;
   a.lambda = lambda;
@@ -2771,6 +2772,7 @@ int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_opti
   a.trace = h->trace.p;
   a.out = h->dama_out.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.tickets = h->barrier.p + 2;
   a.combine_count = h->barrier.p + 4;
   a.stripes = h->scal.p + 8;
   a.tol = o->tol;

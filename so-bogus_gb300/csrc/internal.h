@@ -226,6 +226,7 @@ struct ADMMArgs {
   double* csum;        // 2 x nchunks
   double* scal;        // published scalars
   unsigned* combine_count;  // grid_barrier_combine's counter; zero at launch
+  unsigned* tickets;        // 2 chunk-ticket counters (one per phase parity); zero at launch
   double* stripes;          // 8 stripe sums per reduced quantity
   double* trace;       // max_iters entries, or null
   ADMMOut* out;
@@ -260,6 +261,7 @@ struct DamaArgs {
   double* csum;           // 3 x max(contact chunks, body chunks)
   double* scal;
   unsigned* combine_count;  // grid_barrier_combine's counter; zero at launch
+  unsigned* tickets;        // 2 chunk-ticket counters (one per phase parity); zero at launch
   double* stripes;          // 8 stripe sums per reduced quantity
   double* trace;          // max_iters
   DamaOut* out;

@@ -23,14 +23,40 @@ namespace {
 
 constexpr int kMaxDof = 12;
 
+// Dynamic work split: warps take 32-contact (or 32-body) chunks from a ticket counter, one per phase parity,
+// cleared by the last CTA of the barrier that ends the phase (every draw of the phase is done by then), so SMs
+// whose sub-partitions finish early take more chunks. Chunk sums are stored by chunk index, so the reduction
+// order does not depend on which warp handled a chunk.
+struct Tickets {
+  unsigned* t;         // 2 counters, zero at launch
+  unsigned phase = 0;  // barriers passed (identical in every CTA)
+  __device__ int next() {
+    int c = 0;
+    if ((threadIdx.x & 31) == 0) c = (int)atomicAdd(t + (phase & 1u), 1u);
+    return __shfl_sync(0xffffffffu, c, 0);
+  }
+  // run by every thread of the barrier's last CTA
+  __device__ void clear() {
+    if (threadIdx.x == 0) t[phase & 1u] = 0u;
+  }
+};
+
 struct AdmmCtx {
   const ADMMArgs& a;
   double* smem8;
   int nchunks;
-  __device__ bool sync() { return grid_barrier(a.gb, [] {}); }
+  Tickets tk{a.tickets};
+  __device__ int next() { return tk.next(); }
+  __device__ bool sync() {
+    const bool ok = grid_barrier(a.gb, [&] { tk.clear(); });
+    ++tk.phase;
+    return ok;
+  }
   __device__ bool sync_reduce2(unsigned maxmask) {
-    return grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)nchunks, nchunks, nchunks, 2, maxmask,
-                                a.stripes, a.scal, [] {});
+    const bool ok = grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)nchunks, nchunks, nchunks, 2, maxmask,
+                                         a.stripes, a.scal, [&] { tk.clear(); });
+    ++tk.phase;
+    return ok;
   }
 };
 
@@ -83,8 +109,6 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
   constexpr int DM = D > 0 ? D : kMaxDof;
   const int d = dofs<D>(a);
   const int lane = threadIdx.x & 31;
-  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
   const int C = ctx.nchunks;
   const int CB = (a.nbodies + 31) / 32;
   const double gamma = a.gamma;
@@ -98,7 +122,7 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
   };
 
   // Setup (:64-77): ut = w + H x, z = P(ut - r / gamma), y_prev = -r / gamma, zacc = z_prev = z
-  for (int c = gwarp; c < C; c += nwarps) {
+  for (int c = ctx.next(); c < C; c = ctx.next()) {
     const int i = 32 * c + lane;
     if (i < a.n) {
       const double im = 1. / __ldg(a.mu + i);
@@ -122,7 +146,7 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
   unsigned it = 0;
   for (it = 0; it < a.max_iters; ++it) {
     // P1: x = prox(prox_arg) per body (lane order a.border: bodies of similar contact counts share a warp)
-    for (int c = gwarp; c < CB; c += nwarps) {
+    for (int c = ctx.next(); c < CB; c = ctx.next()) {
       const int slot = 32 * c + lane;
       if (slot < a.nbodies) {
         const int b = a.border ? __ldg(a.border + slot) : slot;
@@ -180,7 +204,7 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
     if (!ctx.sync()) return;
 
     // P2: ut = w + H x, error terms
-    for (int c = gwarp; c < C; c += nwarps) {
+    for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       double ev = 0.0, gap = 0.0;
       if (i < a.n) {
@@ -211,7 +235,7 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
     double beta = 0.0;
     if (acc_branch) beta = nesterov_inertia(theta_prev, 0.);
     else theta_prev = 1.;
-    for (int c = gwarp; c < C; c += nwarps) {
+    for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       if (i < a.n) {
         double ut[3], r[3], z[3];
@@ -281,8 +305,6 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
   constexpr int DM = D > 0 ? D : kMaxDof;
   const int d = D > 0 ? D : a.d;
   const int lane = threadIdx.x & 31;
-  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
   const int C = (a.n + 31) / 32, CB = (a.nbodies + 31) / 32;
   const int CC = C > CB ? C : CB;
   const bool inf = a.use_inf != 0, desaxce = a.desaxce != 0;
@@ -291,11 +313,19 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
     v = is_max ? warp_max_butterfly(v) : warp_sum_butterfly(v);
     if (lane == 0) a.csum[q * CC + c] = v;
   };
-  auto sync = [&]() { return grid_barrier(a.gb, [] {}); };
-    // value 0 over count0 chunks, values 1.. over count1 chunks
+  Tickets tk{a.tickets};
+  auto next = [&]() { return tk.next(); };
+  auto sync = [&]() {
+    const bool ok = grid_barrier(a.gb, [&] { tk.clear(); });
+    ++tk.phase;
+    return ok;
+  };
+  // value 0 over count0 chunks, values 1.. over count1 chunks
   auto sync_reduce = [&](int K, int count0, int count1, unsigned maxmask) {
-    return grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)CC, count0, count1, K, maxmask, a.stripes,
-                                a.scal, [] {});
+    const bool ok = grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)CC, count0, count1, K, maxmask,
+                                         a.stripes, a.scal, [&] { tk.clear(); });
+    ++tk.phase;
+    return ok;
   };
   // H^T src for body b (d values): per dof, contacts in increasing order, rows inner
   auto body_HT = [&](int b, const double* src, double* out) {
@@ -352,7 +382,7 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
   double* r = a.r;
   double* rs = a.rs;
   // H^T r once
-  for (int c = gwarp; c < CB; c += nwarps) {
+  for (int c = next(); c < CB; c = next()) {
     const int b = 32 * c + lane;
     if (b < a.nbodies) {
       double h[DM];
@@ -367,8 +397,26 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
   unsigned it = 0, trials = 0;
   int stopped = 0;
   for (; it < a.max_iters; ++it) {
-    // Q1
-    for (int c = gwarp; c < CB; c += nwarps) {
+    // Q1: tickets [0, CB) take body chunks, [CB, CB + C) contact chunks
+    for (int t = next(); t < CB + C; t = next()) {
+      if (t >= CB) {
+        const int c = t - CB;
+        const int i = 32 * c + lane;
+        double ev = 0.0;
+        if (i < a.n) {
+          double u[3];
+          contact_H(i, a.w, a.v, u);
+          a.ut[3 * i] = u[0];
+          a.ut[3 * i + 1] = u[1];
+          a.ut[3 * i + 2] = u[2];
+          const double sc = __ldg(a.scaling + i);
+          const double lx[3] = {ldcg(r + 3 * i) * sc, ldcg(r + 3 * i + 1) * sc, ldcg(r + 3 * i + 2) * sc};
+          ev = law_eval(desaxce, __ldg(a.mu + i), lx, u);
+        }
+        put(0, c, ev, inf);
+        continue;
+      }
+      const int c = t;
       const int b = 32 * c + lane;
       double pz = 0.0, pz2 = 0.0;
       if (b < a.nbodies) {
@@ -389,21 +437,6 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
       put(1, c, pz, inf);
       put(2, c, pz2, false);
     }
-    for (int c = gwarp; c < C; c += nwarps) {
-      const int i = 32 * c + lane;
-      double ev = 0.0;
-      if (i < a.n) {
-        double u[3];
-        contact_H(i, a.w, a.v, u);
-        a.ut[3 * i] = u[0];
-        a.ut[3 * i + 1] = u[1];
-        a.ut[3 * i + 2] = u[2];
-        const double sc = __ldg(a.scaling + i);
-        const double lx[3] = {ldcg(r + 3 * i) * sc, ldcg(r + 3 * i + 1) * sc, ldcg(r + 3 * i + 2) * sc};
-        ev = law_eval(desaxce, __ldg(a.mu + i), lx, u);
-      }
-      put(0, c, ev, inf);
-    }
     if (!sync_reduce(3, C, CB, inf ? 3u : 0u)) return;
     {
       const double e0 = ldcg(a.scal), z0 = ldcg(a.scal + 1);
@@ -421,8 +454,17 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
     double beta = 0.0;
     if (a.accelerated && res < res_prev) beta = nesterov_inertia(theta_prev, 0.);
     else theta_prev = 1.;
-    // Q2: g (unless done) and the best (r, v)
-    for (int c = gwarp; c < C; c += nwarps) {
+    // Q2: g (unless done) and the best (r, v): tickets [0, C) take contact chunks, [C, C + CB) body chunks
+    // (these only when the iterate is the best so far)
+    const int q2_end = C + (best ? CB : 0);
+    for (int t = next(); t < q2_end; t = next()) {
+      if (t >= C) {
+        const int b = 32 * (t - C) + lane;
+        if (b < a.nbodies)
+          for (int q = 0; q < d; ++q) a.v_best[(size_t)b * d + q] = ldcg(a.v + (size_t)b * d + q);
+        continue;
+      }
+      const int c = t;
       const int i = 32 * c + lane;
       if (i < a.n) {
         if (best)
@@ -456,12 +498,6 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
         }
       }
     }
-    if (best)
-      for (int c = gwarp; c < CB; c += nwarps) {
-        const int b = 32 * c + lane;
-        if (b < a.nbodies)
-          for (int q = 0; q < d; ++q) a.v_best[(size_t)b * d + q] = ldcg(a.v + (size_t)b * d + q);
-      }
     if (!sync()) return;
     if (done) {
       stopped = 1;
@@ -469,7 +505,7 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
     }
     if (a.ls_iters == 0) {
       // Q3: r = P(r - lambda g) in place
-      for (int c = gwarp; c < C; c += nwarps) {
+      for (int c = next(); c < C; c = next()) {
         const int i = 32 * c + lane;
         if (i < a.n) {
           double rr[3];
@@ -483,7 +519,7 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
       lambda *= a.opt;
       for (unsigned ls = 0; ls < a.ls_iters; ++ls) {
         ++trials;
-        for (int c = gwarp; c < C; c += nwarps) {
+        for (int c = next(); c < C; c = next()) {
           const int i = 32 * c + lane;
           if (i < a.n) {
             double rr[3];
@@ -494,7 +530,7 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
         }
         if (!sync()) return;
         // Q4
-        for (int c = gwarp; c < CB; c += nwarps) {
+        for (int c = next(); c < CB; c = next()) {
           const int b = 32 * c + lane;
           double ph = 0.0;
           if (b < a.nbodies) {
@@ -527,7 +563,7 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
       rs = t;
     }
     // Q5
-    for (int c = gwarp; c < CB; c += nwarps) {
+    for (int c = next(); c < CB; c = next()) {
       const int b = 32 * c + lane;
       if (b < a.nbodies) {
         double hr[DM];
