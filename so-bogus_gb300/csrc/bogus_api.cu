@@ -173,7 +173,7 @@ struct bogus_gpu_problem {
   size_t admm_ninc = 0;
   DevBuf<int> bptr, bent;
   DevBuf<int> border;  // bodies by decreasing contact count (the ADMM body phase's lane order)
-  DevBuf<double> a_prox, a_f, a_w, a_mu, a_invmu, a_x, a_r, a_ut, a_z, a_zacc, a_zprev, a_yprev;
+  DevBuf<double> a_prox, a_f, a_w, a_mu, a_invmu, a_x, a_r, a_ut, a_z, a_zacc, a_rs1, a_rs2, a_yprev;
   DevBuf<ADMMOut> admm_out;
   // error-function scalings of ADMM / DualAMA (ConstrainedSolverBase::updateScalings), per contact, and the
   // bodies' own dof count (padding excluded), both set with the incidences
@@ -943,7 +943,7 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
   h->icol.release();
   h->ival.release();
   for (auto* b : {&h->a_prox, &h->a_f, &h->a_w, &h->a_mu, &h->a_invmu, &h->a_x, &h->a_r, &h->a_ut, &h->a_z, &h->a_zacc,
-                  &h->a_zprev, &h->a_yprev})
+                  &h->a_rs1, &h->a_rs2, &h->a_yprev})
     b->release();
   h->bptr.release();
   h->bent.release();
@@ -2576,7 +2576,8 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   cudaStream_t s = h->stream;
   if (int e = ensure_incidence(h)) return e;
   const size_t nv = n3 > 0 ? n3 : 1;
-  for (auto* b : {&h->a_w, &h->a_r, &h->a_ut, &h->a_z, &h->a_zacc, &h->a_zprev, &h->a_yprev}) BG_CUDA(b->ensure(nv));
+  for (auto* b : {&h->a_w, &h->a_r, &h->a_ut, &h->a_z, &h->a_zacc, &h->a_rs1, &h->a_rs2, &h->a_yprev})
+    BG_CUDA(b->ensure(nv));
   BG_CUDA(h->a_mu.ensure(n > 0 ? n : 1));
   BG_CUDA(h->a_invmu.ensure(n > 0 ? n : 1));
   BG_CUDA(h->a_x.ensure(m));
@@ -2617,8 +2618,9 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   a.ut = h->a_ut.p;
   a.z = h->a_z.p;
   a.zacc = h->a_zacc.p;
-  a.zprev = h->a_zprev.p;
   a.yprev = h->a_yprev.p;
+  a.r_spare[0] = h->a_rs1.p;
+  a.r_spare[1] = h->a_rs2.p;
   a.csum = h->csum.p;
   a.scal = h->scal.p;
   a.trace = h->trace.p;
@@ -2657,12 +2659,13 @@ int bogus_gpu_solve_admm(bogus_gpu_problem* h, const bogus_gpu_admm_options* o, 
   {
     // per iteration: P1 reads the incidences, 3 x d H rows, r (and zacc, ut with lambda) per incidence,
     // the d x d prox block, f and x per body and writes x; P2 reads H, x of the bodies, w, r, z, 1/mu and
-    // writes ut per contact; P3 reads ut, r (y_prev, z_prev) and writes r, z, zacc, z_prev, y_prev
+    // writes ut per contact; its P3 part writes z and the plain branch's r, and in the accelerated variant
+    // reads y_prev and writes the accelerated branch's r, y_prev and zacc
     const double inc = (double)h->admm_ninc;
     const double p1 = inc * (4.0 + 24.0 * d + 24.0 + (lambda < 2.220446049250313e-16 ? 0.0 : 48.0)) +
                       (double)nb * (8.0 * d * d + (f ? 16.0 : 8.0) * d + 4.0);
     const double p2 = inc * (24.0 * d + 8.0 * d + 4.0) + (double)n * (24.0 * 4 + 8.0);
-    const double p3 = (double)n * (24.0 * 2 + 8.0 + 48.0 + 24.0 * 4);
+    const double p3 = (double)n * (24.0 * 2 + (o->variant == BOGUS_GPU_ADMM_ACCELERATED ? 24.0 * 4 : 0.0));
     h->last_stats.iterations = out.iters;
     h->last_stats.refine_iterations = 0;
     h->last_stats.fp32_device_ms = 0.0;

@@ -222,7 +222,8 @@ struct ADMMArgs {
   const double* w;     // 3 n
   const double* mu;    // n
   double* inv_mu;      // n (written)
-  double *x, *r, *ut, *z, *zacc, *zprev, *yprev;
+  double *x, *r, *ut, *z, *zacc, *yprev;
+  double* r_spare[2];  // 3 n each: the two candidate updates of r (r, r_spare[0], r_spare[1] rotate)
   double* csum;        // 2 x nchunks
   double* scal;        // published scalars
   unsigned* combine_count;  // grid_barrier_combine's counter; zero at launch

@@ -7,9 +7,16 @@
 // Phases of one iteration (ADMM.impl.hpp line numbers):
 //   P1 bodies    prox_arg = H^T r (lambda = 0, :85) or x / lambda + H^T (r + gamma (zacc - ut)) (:87-89),
 //                x = prox (prox_arg - f) (:91) .............................................. barrier
-//   P2 contacts  ut = w + H x (:93), error terms FB(1/mu; ut_i, r_i) and |ut_i - z_i|^2 (:95-98) .. barrier
-//                + reduce: res (:95-98), tolerance test (:100)
-//   P3 contacts  z = P(ut - r / gamma) (:102-103), r / y / zacc update, accelerated or not (:105-122) . barrier
+//   P2 contacts  ut = w + H x (:93), error terms FB(1/mu; ut_i, r_i) and |ut_i - z_i|^2 (:95-98), then
+//                P3 on the same contact: z = P(ut - r / gamma) (:102-103) and the r / y / zacc update of
+//                both branches (:105-122) ................................................... barrier
+//                + reduce: res (:95-98), tolerance test (:100), branch (accelerated when res < res_prev)
+// P3 reads only its own contact's values, so it runs in P2's pass; its branch depends on the reduced
+// residual, so both outcomes are formed: r into two spare buffers (three rotate; the one the branch picks
+// becomes the current r, and a converged solve keeps the r it was tested on), y and zacc of the accelerated
+// branch into their buffers in place, while after a plain step they are derived where they are read
+// (y_prev = -r / gamma with the current r, zacc = z), the same operations the plain branch would store.
+// z_prev is always z (both branches and the setup store the same z in both), so z serves for it.
 // Body b's H^T accumulation runs over its contacts in increasing contact index, rows 0..2, one FMA chain
 // per dof; contact rows accumulate w, then the slots in body order, dofs 0..d-1; the prox product is an FMA
 // chain over the dofs. Sums use the canonical order (32-contact butterflies, 8 stripes), so the GPU's
@@ -121,7 +128,8 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
     if (lane == 0) a.csum[q * C + c] = v;
   };
 
-  // Setup (:64-77): ut = w + H x, z = P(ut - r / gamma), y_prev = -r / gamma, zacc = z_prev = z
+  // Setup (:64-77): ut = w + H x, z = P(ut - r / gamma), y_prev = -r / gamma, zacc = z_prev = z (the last two
+  // derived: plain = true)
   for (int c = ctx.next(); c < C; c = ctx.next()) {
     const int i = 32 * c + lane;
     if (i < a.n) {
@@ -132,19 +140,19 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
       load3(a.r, i, r);
       for (int k = 0; k < 3; ++k) z[k] = ut[k] - inv_gamma * r[k];
       project_cone(im, z);
-      const double yp[3] = {-inv_gamma * r[0], -inv_gamma * r[1], -inv_gamma * r[2]};
       store3(a.ut, i, ut);
       store3(a.z, i, z);
-      store3(a.zacc, i, z);
-      store3(a.zprev, i, z);
-      store3(a.yprev, i, yp);
     }
   }
   if (!ctx.sync()) return;
 
+  double* rb[3] = {a.r, a.r_spare[0], a.r_spare[1]};
+  int cur = 0;
+  bool plain = true;  // y_prev = -r / gamma and zacc = z (the setup, or the last update took the plain branch)
   double theta_prev = 1., res_prev = -1., res = -1.;
   unsigned it = 0;
   for (it = 0; it < a.max_iters; ++it) {
+    const double* rc = rb[cur];
     // P1: x = prox(prox_arg) per body (lane order a.border: bodies of similar contact counts share a warp)
     for (int c = ctx.next(); c < CB; c = ctx.next()) {
       const int slot = 32 * c + lane;
@@ -161,10 +169,10 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
           const int i = ent >> 1;
           const double* Hb = a.H + (size_t)ent * 3 * d;
           double rv[3];
-          load3(a.r, i, rv);
+          load3(rc, i, rv);
           if (with_lambda) {
             double za[3], ut[3];
-            load3(a.zacc, i, za);
+            load3(plain ? a.z : a.zacc, i, za);
             load3(a.ut, i, ut);
             for (int k = 0; k < 3; ++k) rv[k] = fma(gamma, za[k] - ut[k], rv[k]);
           }
@@ -203,7 +211,12 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
     }
     if (!ctx.sync()) return;
 
-    // P2: ut = w + H x, error terms
+    // P2 + P3: ut = w + H x, error terms; z and both branches' updates
+    double theta_spec = theta_prev;
+    const double beta = a.accelerated ? nesterov_inertia(theta_spec, 0.) : 0.0;
+    const int ia = (cur + 1) % 3, ip = a.accelerated ? (cur + 2) % 3 : (cur + 1) % 3;
+    double* r_acc = rb[ia];
+    double* r_plain = rb[ip];
     for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       double ev = 0.0, gap = 0.0;
@@ -211,13 +224,38 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
         double ut[3], r[3], z[3];
         contact_velocity<D>(a, i, ut);
         store3(a.ut, i, ut);
-        load3(a.r, i, r);
+        load3(rc, i, r);
         load3(a.z, i, z);
         const double sc = __ldg(a.scaling + i);
         const double lx[3] = {ut[0] * sc, ut[1] * sc, ut[2] * sc};
-        ev = law_eval(false, ldcg(a.inv_mu + i), lx, r);
+        const double im = ldcg(a.inv_mu + i);
+        ev = law_eval(false, im, lx, r);
         const double d3[3] = {ut[0] - z[0], ut[1] - z[1], ut[2] - z[2]};
         gap = a.use_inf ? dmax(dmax(fabs(d3[0]), fabs(d3[1])), fabs(d3[2])) : sq3(d3);
+        // P3
+        double zn[3];
+        for (int k = 0; k < 3; ++k) zn[k] = ut[k] - inv_gamma * r[k];
+        project_cone(im, zn);
+        if (a.accelerated) {
+          double yp[3], y[3], rn[3], za[3];
+          if (plain) {
+            for (int k = 0; k < 3; ++k) yp[k] = -inv_gamma * r[k];
+          } else {
+            load3(a.yprev, i, yp);
+          }
+          for (int k = 0; k < 3; ++k) {
+            y[k] = (ut[k] - zn[k]) - inv_gamma * r[k];
+            rn[k] = -gamma * fma(beta, y[k] - yp[k], y[k]);
+            za[k] = fma(beta, zn[k] - z[k], zn[k]);
+          }
+          store3(r_acc, i, rn);
+          store3(a.yprev, i, y);
+          store3(a.zacc, i, za);
+        }
+        double rn[3];
+        for (int k = 0; k < 3; ++k) rn[k] = fma(gamma, zn[k] - ut[k], r[k]);
+        store3(r_plain, i, rn);
+        store3(a.z, i, zn);
       }
       put(0, c, ev, a.use_inf != 0);
       put(1, c, gap, a.use_inf != 0);
@@ -229,48 +267,28 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
     }
     if (a.trace && writer) a.trace[it] = res;
     if (res < a.tol) break;
-
-    // P3: z and the dual update
     const bool acc_branch = a.accelerated && res < res_prev;
-    double beta = 0.0;
-    if (acc_branch) beta = nesterov_inertia(theta_prev, 0.);
-    else theta_prev = 1.;
+    if (acc_branch) {
+      theta_prev = theta_spec;
+      cur = ia;
+      plain = false;
+    } else {
+      theta_prev = 1.;
+      cur = ip;
+      plain = true;
+    }
+    res_prev = res;
+  }
+  // the final r in the caller's buffer (nothing reads the spare buffers after the last barrier)
+  if (cur != 0) {
     for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       if (i < a.n) {
-        double ut[3], r[3], z[3];
-        load3(a.ut, i, ut);
-        load3(a.r, i, r);
-        for (int k = 0; k < 3; ++k) z[k] = ut[k] - inv_gamma * r[k];
-        project_cone(ldcg(a.inv_mu + i), z);
-        if (acc_branch) {
-          double yp[3], zp[3], y[3], rn[3], za[3];
-          load3(a.yprev, i, yp);
-          load3(a.zprev, i, zp);
-          for (int k = 0; k < 3; ++k) {
-            y[k] = (ut[k] - z[k]) - inv_gamma * r[k];
-            rn[k] = -gamma * fma(beta, y[k] - yp[k], y[k]);
-            za[k] = fma(beta, z[k] - zp[k], z[k]);
-          }
-          store3(a.r, i, rn);
-          store3(a.yprev, i, y);
-          store3(a.zacc, i, za);
-        } else {
-          double rn[3], yp[3];
-          for (int k = 0; k < 3; ++k) {
-            rn[k] = fma(gamma, z[k] - ut[k], r[k]);
-            yp[k] = -inv_gamma * rn[k];
-          }
-          store3(a.r, i, rn);
-          store3(a.zacc, i, z);
-          store3(a.yprev, i, yp);
-        }
-        store3(a.z, i, z);
-        store3(a.zprev, i, z);
+        double r[3];
+        load3(rb[cur], i, r);
+        store3(a.r, i, r);
       }
     }
-    res_prev = res;
-    if (!ctx.sync()) return;
   }
   if (writer) {
     a.out->res = res;
@@ -291,9 +309,10 @@ __global__ void __launch_bounds__(256) k_admm_persistent(ADMMArgs a) {
 // PrimalFrictionProblem::solveWith(DualAMAType&, v, r, staticProblem) (PrimalFrictionProblem.cpp:78-99).
 // Phases of one iteration (one lane per body in body phases, 32-contact chunks in contact phases):
 //   Q1 bodies + contacts  x = f + M v, z = H^T r - x and its norms; u = w + H v, law error at (r, u) .... reduce
-//   Q2 contacts + bodies  g = u + COV(u) + gamma H z; the best (r, v) kept ............................ barrier
+//   Q2 contacts + bodies  g = u + COV(u) + gamma H z; the best (r, v) kept; the first trial's Q3 on the
+//                         contact's own g ............................................................. barrier
 //   line search, trial by trial:
-//     Q3 contacts         r_s = P(r - lambda g) ....................................................... barrier
+//     Q3 contacts         r_s = P(r - lambda g), from the second trial on ................................ barrier
 //     Q4 bodies           H^T r_s, y = v + gamma (H^T r_s - x) over-relaxed, |(H^T r_s - f) - M y|^2 .. reduce
 //   (no line search: Q3 writes r = P(r - lambda g), Q5 forms H^T r)
 //   Q5 bodies             z = H^T r - x, y = v + gamma z, v = y + beta (y - y_prev) ..................... barrier
@@ -455,7 +474,11 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
     if (a.accelerated && res < res_prev) beta = nesterov_inertia(theta_prev, 0.);
     else theta_prev = 1.;
     // Q2: g (unless done) and the best (r, v): tickets [0, C) take contact chunks, [C, C + CB) body chunks
-    // (these only when the iterate is the best so far)
+    // (these only when the iterate is the best so far). Q3 of the first trial, r_s = P(r - lambda g), needs only
+    // the contact's own g, so it runs here on the g just computed (in place, r = P(r - lambda g), without a
+    // line search).
+    if (!done && a.ls_iters != 0) lambda *= a.opt;
+    double* q3_out = a.ls_iters == 0 ? r : rs;
     const int q2_end = C + (best ? CB : 0);
     for (int t = next(); t < q2_end; t = next()) {
       if (t >= C) {
@@ -467,8 +490,10 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
       const int c = t;
       const int i = 32 * c + lane;
       if (i < a.n) {
+        double rc[3];
+        for (int k = 0; k < 3; ++k) rc[k] = ldcg(r + 3 * i + k);
         if (best)
-          for (int k = 0; k < 3; ++k) a.r_best[3 * i + k] = ldcg(r + 3 * i + k);
+          for (int k = 0; k < 3; ++k) a.r_best[3 * i + k] = rc[k];
         if (!done) {
           double u[3], hz[3];
           for (int k = 0; k < 3; ++k) u[k] = ldcg(a.ut + 3 * i + k);
@@ -492,43 +517,40 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
             }
           }
           const double s0 = duality_cov(desaxce, __ldg(a.mu + i), u);
-          a.g[3 * i] = fma(a.gamma, hz[0], u[0] + s0);
-          a.g[3 * i + 1] = fma(a.gamma, hz[1], u[1] + 0.0);
-          a.g[3 * i + 2] = fma(a.gamma, hz[2], u[2] + 0.0);
+          const double g[3] = {fma(a.gamma, hz[0], u[0] + s0), fma(a.gamma, hz[1], u[1] + 0.0),
+                               fma(a.gamma, hz[2], u[2] + 0.0)};
+          a.g[3 * i] = g[0];
+          a.g[3 * i + 1] = g[1];
+          a.g[3 * i + 2] = g[2];
+          double rr[3];
+          for (int k = 0; k < 3; ++k) rr[k] = rc[k] - lambda * g[k];
+          project_cone(__ldg(a.mu + i), rr);
+          for (int k = 0; k < 3; ++k) q3_out[3 * i + k] = rr[k];
         }
       }
     }
+    if (a.ls_iters != 0 && !done) ++trials;
     if (!sync()) return;
     if (done) {
       stopped = 1;
       break;
     }
-    if (a.ls_iters == 0) {
-      // Q3: r = P(r - lambda g) in place
-      for (int c = next(); c < C; c = next()) {
-        const int i = 32 * c + lane;
-        if (i < a.n) {
-          double rr[3];
-          for (int k = 0; k < 3; ++k) rr[k] = ldcg(r + 3 * i + k) - lambda * ldcg(a.g + 3 * i + k);
-          project_cone(__ldg(a.mu + i), rr);
-          for (int k = 0; k < 3; ++k) r[3 * i + k] = rr[k];
-        }
-      }
-      if (!sync()) return;
-    } else {
-      lambda *= a.opt;
+    if (a.ls_iters != 0) {
       for (unsigned ls = 0; ls < a.ls_iters; ++ls) {
-        ++trials;
-        for (int c = next(); c < C; c = next()) {
-          const int i = 32 * c + lane;
-          if (i < a.n) {
-            double rr[3];
-            for (int k = 0; k < 3; ++k) rr[k] = ldcg(r + 3 * i + k) - lambda * ldcg(a.g + 3 * i + k);
-            project_cone(__ldg(a.mu + i), rr);
-            for (int k = 0; k < 3; ++k) rs[3 * i + k] = rr[k];
+        if (ls > 0) {
+          ++trials;
+          // Q3: r_s = P(r - lambda g) for a later trial
+          for (int c = next(); c < C; c = next()) {
+            const int i = 32 * c + lane;
+            if (i < a.n) {
+              double rr[3];
+              for (int k = 0; k < 3; ++k) rr[k] = ldcg(r + 3 * i + k) - lambda * ldcg(a.g + 3 * i + k);
+              project_cone(__ldg(a.mu + i), rr);
+              for (int k = 0; k < 3; ++k) rs[3 * i + k] = rr[k];
+            }
           }
+          if (!sync()) return;
         }
-        if (!sync()) return;
         // Q4
         for (int c = next(); c < CB; c = next()) {
           const int b = 32 * c + lane;
