@@ -795,7 +795,7 @@ def measure_adjoint(args, steps=2, rank=0, world=1, dev=0):
     import bogus_gpu
     from bogus_gpu import generator, shard
 
-    d, cptr = generator.adjoint_batch()
+    d, cptr = generator.adjoint_batch(nproblems=getattr(args, "adjoint_problems", 64))
     nprob = len(cptr) - 1
     parts = shard.partition(np.diff(cptr), world)
     mine = parts[rank]
@@ -812,7 +812,9 @@ def measure_adjoint(args, steps=2, rank=0, world=1, dev=0):
     g = np.random.default_rng(6).standard_normal(3 * d.n)
     g_mine = g.reshape(-1, 3)[np.concatenate([np.arange(cptr[p], cptr[p + 1]) for p in mine])].reshape(-1)
     out = {"problems": nprob, "contacts": int(d.n), "ranks": world, "compliance": generator.ADJOINT_COMPLIANCE}
-    for law, coulomb in (("coulomb", True), ("soc", False)):
+    laws = (("coulomb", True), ("soc", False))
+    which = getattr(args, "adjoint_law", "both")
+    for law, coulomb in (laws if which == "both" else [lw for lw in laws if lw[0] == which]):
         fwd, adj, prim = [], [], []
         # the Coulomb forward runs up to 20 000 iterations (tens of seconds): it is timed without a warm-up
         warm = 0 if coulomb else 1
@@ -842,17 +844,19 @@ def measure_adjoint(args, steps=2, rank=0, world=1, dev=0):
         out[law] = e
     out["timing"] = (f"median of {steps} (SOC: after a warm-up); device times (CUDA events) of the batched solve "
                      "kernel and of the adjoint kernel (max over ranks)")
-    out["t_adjoint_over_t_forward"] = out["coulomb"]["t_adjoint_over_t_forward"]
+    out["t_adjoint_over_t_forward"] = out["coulomb" if "coulomb" in out else "soc"]["t_adjoint_over_t_forward"]
     return out
 
 
 def run_adjoint(args, rank=0, world=1, dev=0) -> None:
     out = measure_adjoint(args, steps=args.steps, rank=rank, world=world, dev=dev)
     if rank == 0:
-        line = {"metric": "adjoint / forward time, 64 x 20 000 contacts, Coulomb law", "value": out["t_adjoint_over_t_forward"],
+        law = "Coulomb" if "coulomb" in out else "SOC"
+        line = {"metric": f"adjoint / forward time, {out['problems']} x 20 000 contacts, {law} law",
+                "value": out["t_adjoint_over_t_forward"],
                 "unit": "ratio", "n_gpus": world, "steps": args.steps, "higher_is_better": False,
                 "scaling": "strong", "dtype": "f64", "data": "synthetic (seeded adjoint batch generator)",
-                "config": {"workload": "adjoint_64x20000_contacts"}, "adjoint": out}
+                "config": {"workload": f"adjoint_{out['problems']}x20000_contacts"}, "adjoint": out}
         print(json.dumps(line), flush=True)
 
 
@@ -872,6 +876,10 @@ def main():
                     choices=["apgd", "batch", "gs", "mixed", "admm", "dama", "adjoint"],
                     help="apgd: the benchmark line; batch / adjoint (sharded over ranks under torchrun), gs, mixed, "
                          "admm, dama: the secondary measurements on their own")
+    ap.add_argument("--adjoint-problems", type=int, default=64,
+                    help="--workload adjoint: problems of 20 000 contacts in the batch (64: the benchmark's)")
+    ap.add_argument("--adjoint-law", default="both", choices=["both", "coulomb", "soc"],
+                    help="--workload adjoint: the laws to run")
     ap.add_argument("--profile-mixed", action="store_true",
                     help="with --profile: the FP32-refined solve (FP32 iterations, then 1 FP64 iteration)")
     args = ap.parse_args()
