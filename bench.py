@@ -388,6 +388,29 @@ def measure_secondary(args, D, d, r_fp64, fp64_ms):
         "error_note": "||r_mixed - r_fp64|| / ||r_fp64||, r_fp64 the FP64 solve to 1e-6 (bit-identical to the "
                       "oracle's iterates); W is singular here, so two iterates at residual 1e-6 may differ along "
                       "its null space"}
+    # options with no counterpart in the reference: APGD's momentum product formed by linearity (one pass over
+    # W fewer per momentum step; the oracle restates the same variant, tests check it bit for bit), alone and
+    # with the FP32-refined form
+    for key, mixed in (("apgd_momentum_by_linearity_to_1e-6", False),
+                       ("fp32_refined_momentum_by_linearity_to_1e-6", True)):
+        pgl = bogus_gpu.ProjectedGradient()
+        pgl.setTol(TOL)
+        pgl.setMomentumByLinearity(True)
+        if mixed:
+            pgl.setMaxIters(FP32_ITERS)
+            pgl.setMixedPrecision(True, args.max_iters)
+        else:
+            pgl.setMaxIters(args.max_iters)
+        res, st, rl = best_of(pgl)
+        out[key] = {
+            "device_ms": st["device_ms"], "iterations": st["iterations"], "residual": res,
+            "reached_tol": bool(res < TOL), "speedup_vs_fp64": fp64_ms / st["device_ms"],
+            "w_passes_per_iteration": st["w_passes"] / max(1, st["iterations"]),
+            "rel_error_vs_fp64": float(np.linalg.norm(rl - r_fp64) / np.linalg.norm(r_fp64))}
+        if mixed:
+            out[key].update({"fp32_ms": st["fp32_device_ms"],
+                             "fp32_iterations": st["iterations"] - st["refine_iterations"],
+                             "fp64_iterations": st["refine_iterations"]})
     pgs = bogus_gpu.ProjectedGradient()
     pgs.setTol(TOL)
     pgs.setMaxIters(args.max_iters)

@@ -73,6 +73,14 @@ typedef struct bogus_gpu_pg_options {
                                      to max_iters iterations, then up to refine_max_iters FP64 iterations from
                                      the FP32 result (the returned residual is the FP64 error function) */
   unsigned refine_max_iters;      /* 50 */
+  int momentum_by_linearity;      /* 0: APGD's momentum step multiplies W by the new x, as the reference does
+                                     (ProjectedGradient.impl.hpp:141). 1 (not in the reference): the product is
+                                     formed by linearity, W x = W xs + beta (W xs - W prev), from the trial's
+                                     product and the kept product of prev: one pass over W fewer per momentum
+                                     step, iterates that differ from the reference's by rounding (and a returned
+                                     residual evaluated with that product, equal to the error function at the
+                                     returned iterate up to rounding). Single-problem and batched solves; the
+                                     allocation-free entry point rejects it */
 } bogus_gpu_pg_options;
 
 /* GaussSeidel setters and defaults (Core/BlockSolvers/GaussSeidelBase.hpp:39-91) plus the coloring switch

@@ -267,6 +267,8 @@ class ProjectedGradient : public SolverBase {
     mixed_ = on;
     refine_ = refine_max_iters;
   }
+  // extension: APGD's momentum product by linearity (one pass over W fewer per momentum step)
+  void setMomentumByLinearity(bool on) { lin_ = on; }
 
   bogus_gpu_pg_options options(bool static_problem) const {
     bogus_gpu_pg_options o;
@@ -282,6 +284,7 @@ class ProjectedGradient : public SolverBase {
     o.static_problem = static_problem ? 1 : 0;
     o.mixed_precision = mixed_ ? 1 : 0;
     o.refine_max_iters = refine_;
+    o.momentum_by_linearity = lin_ ? 1 : 0;
     return o;
   }
 
@@ -289,7 +292,7 @@ class ProjectedGradient : public SolverBase {
   unsigned ls_iters_ = 8, refine_ = 50;
   double opt_ = 1.25, pess_ = 0.5, armijo_ = 0.5;
   int variant_ = BOGUS_GPU_PG_APGD;
-  bool mixed_ = false;
+  bool mixed_ = false, lin_ = false;
 };
 
 // ADMM<HType> (ADMM.hpp:81-100), defaults of init().

@@ -293,6 +293,11 @@ struct ProjectedGradient : SolverBase {
   unsigned lsIters = 8;
   double lsOptimisticFactor = 1.25, lsPessimisticFactor = .5, lsArmijoCoefficient = .5;
   int variant = APGD;
+  // Not in the reference: APGD's momentum product formed by linearity, W x = W xs + beta (W xs - W prev) with
+  // x = xs + beta (xs - prev), from the trial's product W xs and the kept product of prev, in place of the
+  // product W x of ProjectedGradient.impl.hpp:141 (same fma form as x itself). One pass over W fewer per
+  // momentum step; the iterates differ from the reference's by the rounding of the two forms.
+  bool linMomentum = false;
 
   ProjectedGradient() { tol = 1e-6; maxIters = 300; }
 
@@ -340,11 +345,12 @@ struct ProjectedGradient : SolverBase {
   double solveAPGD(const Law& law, const double* b, double* x, bool apgd, unsigned* itersOut) const {
     const int N = n();
     const size_t n3 = 3 * (size_t)N;
-    std::vector<double> Mx(n3), y(n3), xs(n3), s(n3), prev, x_best;
+    std::vector<double> Mx(n3), y(n3), xs(n3), s(n3), prev, x_best, Mprev;
     projectOnConstraints(law, x);
     spmv(*W, x, Mx.data());
     double theta = 1., q = 0;
     prev.assign(x, x + n3);
+    if (linMomentum) Mprev = Mx;  // W prev
     double alpha = 1.;
     guessAlpha(x, alpha);
     double min_res = -1;
@@ -379,10 +385,20 @@ struct ProjectedGradient : SolverBase {
       if (apgd && decr2 < 0) {
         const double beta = nesterovInertia(theta, q);
         for (size_t k = 0; k < n3; ++k) x[k] = std::fma(beta, xs[k] - prev[k], xs[k]);
-        spmv(*W, x, Mx.data());
+        if (linMomentum) {
+          // Mx holds W xs (the accepted trial's product)
+          for (size_t k = 0; k < n3; ++k) {
+            const double mxs = Mx[k];
+            Mx[k] = std::fma(beta, mxs - Mprev[k], mxs);
+            Mprev[k] = mxs;
+          }
+        } else {
+          spmv(*W, x, Mx.data());
+        }
       } else {
         std::copy(xs.begin(), xs.end(), x);
         theta = 1.;
+        if (linMomentum) Mprev = Mx;
       }
       prev = xs;
     }

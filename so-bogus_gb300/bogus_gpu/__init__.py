@@ -41,7 +41,8 @@ class PgOptions(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iters", C.c_uint), ("ls_iters", C.c_uint),
                 ("ls_optimistic_factor", C.c_double), ("ls_pessimistic_factor", C.c_double),
                 ("ls_armijo_coefficient", C.c_double), ("variant", C.c_int), ("use_infinity_norm", C.c_int),
-                ("static_problem", C.c_int), ("mixed_precision", C.c_int), ("refine_max_iters", C.c_uint)]
+                ("static_problem", C.c_int), ("mixed_precision", C.c_int), ("refine_max_iters", C.c_uint),
+                ("momentum_by_linearity", C.c_int)]
 
 
 class GsOptions(C.Structure):
@@ -259,6 +260,13 @@ class ProjectedGradient(_SolverBase):
         self._opt, self._pess, self._armijo = 1.25, 0.5, 0.5
         self._variant = APGD
         self._mixed, self._refine = False, 50
+        self._lin = False
+
+    def setMomentumByLinearity(self, on: bool = True) -> None:
+        """APGD's momentum product formed by linearity, W x = W xs + beta (W xs - W prev), instead of the product
+        W x of ProjectedGradient.impl.hpp:141: one pass over W fewer per momentum step, iterates that differ
+        from the reference's by rounding. No counterpart in the reference."""
+        self._lin = bool(on)
 
     def setMixedPrecision(self, on: bool = True, refine_max_iters: int = 50) -> None:
         """FP32-refined solve: FP32 W / iterates / per-contact law (FP64 reductions and decisions), then up to
@@ -279,6 +287,7 @@ class ProjectedGradient(_SolverBase):
         o.ls_optimistic_factor, o.ls_pessimistic_factor, o.ls_armijo_coefficient = self._opt, self._pess, self._armijo
         o.variant, o.use_infinity_norm, o.static_problem = self._variant, int(self._inf), int(static_problem)
         o.mixed_precision, o.refine_max_iters = int(self._mixed), self._refine
+        o.momentum_by_linearity = int(self._lin)
         return o
 
 

@@ -396,6 +396,12 @@ int ensure_host_lower(bogus_gpu_problem* h) {
   return BOGUS_GPU_OK;
 }
 
+// APGD's momentum product by linearity (bogus_gpu_pg_options::momentum_by_linearity; no effect on the other
+// variants, which have no momentum product)
+int lin_momentum(const bogus_gpu_pg_options* o) {
+  return o->momentum_by_linearity && o->variant == BOGUS_GPU_PG_APGD ? 1 : 0;
+}
+
 int check_finite(const double* v, size_t m, const char* what) {
   for (size_t k = 0; k < m; ++k)
     if (!std::isfinite(v[k])) return fail(BOGUS_GPU_NONFINITE, std::string("non-finite value in ") + what);
@@ -407,7 +413,7 @@ int ensure_pg_work(bogus_gpu_problem* h, unsigned max_iters) {
   const size_t n3 = 3 * (size_t)n;
   const int C = (n + 31) / 32;
   BG_CUDA(h->X.ensure(3 * n3));
-  BG_CUDA(h->MX.ensure(2 * n3));
+  BG_CUDA(h->MX.ensure(4 * n3));
   BG_CUDA(h->Y.ensure(n3));
   BG_CUDA(h->S0.ensure(n));
   BG_CUDA(h->XB.ensure(n3));
@@ -431,11 +437,12 @@ struct PGTraffic {
   double bytes = 0, fma = 0;
   unsigned passes = 0;
 };
-PGTraffic pg_traffic(const PGOut& out, int n, long long nnzb, int variant, double elem) {
+PGTraffic pg_traffic(const PGOut& out, int n, long long nnzb, int variant, double elem, bool lin = false) {
   const bool spg = variant == BOGUS_GPU_PG_SPG, apgd = variant == BOGUS_GPU_PG_APGD;
   const double wpass = (double)nnzb * (9.0 * elem + 4.0) + 4.0 * (n + 1);
-  // values per contact; APGD's trial product also writes the momentum point
-  const double per_contact[9] = {7, 6, spg ? 21.0 : 18.0, apgd ? 22.0 : 19.0, 10, 9, 18, 15, 12};
+  // values per contact; APGD's trial product also writes the momentum point (and, by linearity, reads the kept
+  // product of prev and writes the momentum product)
+  const double per_contact[9] = {7, 6, spg ? 21.0 : 18.0, apgd ? (lin ? 28.0 : 22.0) : 19.0, 10, 9, 18, 15, 12};
   const bool has_w[9] = {false, true, false, true, false, false, true, false, true};
   PGTraffic t;
   for (int k = 0; k < 9; ++k) {
@@ -471,6 +478,8 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.X2 = h->X.p + 2 * n3;
   a.MX0 = h->MX.p;
   a.MX1 = h->MX.p + n3;
+  a.MX2 = h->MX.p + 2 * n3;
+  a.MX3 = h->MX.p + 3 * n3;
   a.Y = h->Y.p;
   a.S0 = h->S0.p;
   a.XB = h->XB.p;
@@ -491,6 +500,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.pess = o->ls_pessimistic_factor;
   a.max_iters = o->max_iters;
   a.ls_iters = o->ls_iters;
+  a.lin_momentum = lin_momentum(o);
   a.phantom_ctas = h->test_wait_timeout ? 1u : 0u;
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 16 * sizeof(unsigned), h->stream));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
@@ -510,7 +520,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   h->last_launches = 1;
   if (st != 0) return fail(st, "device-side wait timed out in the projected-gradient kernel");
   {
-    const PGTraffic t = pg_traffic(out, n, h->W.nnzb, o->variant, 8.0);
+    const PGTraffic t = pg_traffic(out, n, h->W.nnzb, o->variant, 8.0, lin_momentum(o) != 0);
     h->last_stats.iterations = out.iters;
     h->last_stats.refine_iterations = 0;
     h->last_stats.fp32_device_ms = 0.0;
@@ -571,7 +581,7 @@ int ensure_fp32(bogus_gpu_problem* h) {
   const size_t n3 = 3 * (size_t)n;
   cudaStream_t s = h->stream;
   BG_CUDA(h->X32.ensure(3 * n3));
-  BG_CUDA(h->MX32.ensure(2 * n3));
+  BG_CUDA(h->MX32.ensure(4 * n3));
   BG_CUDA(h->Y32.ensure(n3));
   BG_CUDA(h->S032.ensure(n));
   BG_CUDA(h->XB32.ensure(n3));
@@ -600,6 +610,7 @@ void fill_args(PGArgsT<T>& a, const bogus_gpu_pg_options* o) {
   a.pess = o->ls_pessimistic_factor;
   a.max_iters = o->max_iters;
   a.ls_iters = o->ls_iters;
+  a.lin_momentum = lin_momentum(o);
 }
 
 // Mixed precision: FP32 solve from X[0] (double), its best iterate back into X[0], then the FP64 solve from
@@ -629,6 +640,8 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   a.X2 = h->X32.p + 2 * n3;
   a.MX0 = h->MX32.p;
   a.MX1 = h->MX32.p + n3;
+  a.MX2 = h->MX32.p + 2 * n3;
+  a.MX3 = h->MX32.p + 3 * n3;
   a.Y = h->Y32.p;
   a.S0 = h->S032.p;
   a.XB = h->XB32.p;
@@ -668,7 +681,7 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   const unsigned it32 = out.iters;
   const int rst = run_pg(h, &o64, residual, iters, best);
   if (rst != BOGUS_GPU_OK && rst != BOGUS_GPU_NOT_CONVERGED) return rst;
-  const PGTraffic t32 = pg_traffic(out, n, h->W.nnzb, o->variant, 4.0);
+  const PGTraffic t32 = pg_traffic(out, n, h->W.nnzb, o->variant, 4.0, lin_momentum(o) != 0);
   h->last_stats.refine_iterations = h->last_stats.iterations;
   h->last_stats.iterations = it32 + h->last_stats.iterations;
   h->last_stats.w_passes += t32.passes;
@@ -867,6 +880,7 @@ void bogus_gpu_pg_options_default(bogus_gpu_pg_options* o) {
   o->static_problem = 1;
   o->mixed_precision = 0;
   o->refine_max_iters = 50;
+  o->momentum_by_linearity = 0;
 }
 
 void bogus_gpu_gs_options_default(bogus_gpu_gs_options* o) {
@@ -3248,12 +3262,15 @@ PGBatchArgs batch_args64(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
   a.X2 = h->X.p + 2 * n3;
   a.MX0 = h->MX.p;
   a.MX1 = h->MX.p + n3;
+  a.MX2 = h->MX.p + 2 * n3;
+  a.MX3 = h->MX.p + 3 * n3;
   a.Y = h->Y.p;
   a.S0 = h->S0.p;
   a.XB = h->XB.p;
   a.Wv = h->Wv.p;
   a.csum = h->csum.p;
   a.out = h->batch_out.p;
+  a.lin_momentum = lin_momentum(o);
   a.desaxce = o->static_problem ? 0 : 1;
   a.variant = o->variant;
   a.use_inf = o->use_infinity_norm ? 1 : 0;
@@ -3283,7 +3300,7 @@ int finish_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, const PGOu
     if (iters) iters[p] = out[p].iters;
     all = all && (out[p].converged || h->h_contact_ptr[p + 1] == h->h_contact_ptr[p]);
     const int np_c = h->h_contact_ptr[p + 1] - h->h_contact_ptr[p];
-    const PGTraffic t = pg_traffic(out[p], np_c, h->h_problem_nnz[p], o->variant, 8.0);
+    const PGTraffic t = pg_traffic(out[p], np_c, h->h_problem_nnz[p], o->variant, 8.0, lin_momentum(o) != 0);
     sum.bytes += t.bytes;
     sum.fma += t.fma;
     sum.passes += t.passes;
@@ -3322,7 +3339,7 @@ int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
   if (int e = set_device(h)) return e;
   const int n = h->W.n;
   BG_CUDA(h->X.ensure(3 * 3 * (size_t)n));
-  BG_CUDA(h->MX.ensure(2 * 3 * (size_t)n));
+  BG_CUDA(h->MX.ensure(4 * 3 * (size_t)n));
   BG_CUDA(h->Y.ensure(3 * (size_t)n));
   BG_CUDA(h->S0.ensure(n));
   BG_CUDA(h->XB.ensure(3 * (size_t)n));
@@ -3348,7 +3365,7 @@ int run_pg_batch_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, doub
   const int np = h->nproblems;
   cudaStream_t s = h->stream;
   BG_CUDA(h->X32.ensure(3 * n3));
-  BG_CUDA(h->MX32.ensure(2 * n3));
+  BG_CUDA(h->MX32.ensure(4 * n3));
   BG_CUDA(h->Y32.ensure(n3));
   BG_CUDA(h->S032.ensure(n));
   BG_CUDA(h->XB32.ensure(n3));
@@ -3378,12 +3395,15 @@ int run_pg_batch_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, doub
   a.X2 = h->X32.p + 2 * n3;
   a.MX0 = h->MX32.p;
   a.MX1 = h->MX32.p + n3;
+  a.MX2 = h->MX32.p + 2 * n3;
+  a.MX3 = h->MX32.p + 3 * n3;
   a.Y = h->Y32.p;
   a.S0 = h->S032.p;
   a.XB = h->XB32.p;
   a.Wv = h->Wv32.p;
   a.csum = h->csum.p;
   a.out = h->batch_out.p;
+  a.lin_momentum = lin_momentum(o);
   a.desaxce = o->static_problem ? 0 : 1;
   a.variant = o->variant;
   a.use_inf = o->use_infinity_norm ? 1 : 0;

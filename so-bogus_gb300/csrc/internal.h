@@ -55,6 +55,8 @@ struct PGArgsT {
   T* X2;
   T* MX0;
   T* MX1;
+  T* MX2;  // MX2, MX3: the kept W prev and the momentum product when lin_momentum (else unused, may be null)
+  T* MX3;
   T* Y;
   T* S0;
   T* XB;
@@ -68,6 +70,7 @@ struct PGArgsT {
   double* stripes;          // 8 stripe sums per reduced quantity (32 doubles)
   unsigned long long* mono; // 3 monotonic counters of the single-problem kernel's barriers (MonoBarrier); zero at launch
   int desaxce, variant, use_inf;
+  int lin_momentum;  // APGD's momentum product by linearity (needs MX2, MX3)
   double tol, opt, pess;
   unsigned max_iters, ls_iters;
   // test of the timeout path (single-problem kernel): the barriers count this many CTAs more than the launch

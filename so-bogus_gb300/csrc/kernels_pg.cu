@@ -45,13 +45,24 @@ template <class T>
 struct Bufs {
   const PGArgsT<T>& a;
   __device__ T* X(int k) const { return k == 0 ? a.X0 : (k == 1 ? a.X1 : (k == 2 ? a.X2 : a.Wv)); }
-  __device__ T* MX(int k) const { return k == 0 ? a.MX0 : a.MX1; }
+  __device__ T* MX(int k) const { return k == 0 ? a.MX0 : (k == 1 ? a.MX1 : (k == 2 ? a.MX2 : a.MX3)); }
 };
 
 __device__ __forceinline__ int third(int p, int q) {
   for (int k = 0; k < 3; ++k)
     if (k != p && k != q) return k;
   return 0;
+}
+
+// The first two of the product buffers {0, 1, 2, 3} other than p and q (p == q allowed).
+__device__ __forceinline__ void two_free_mx(int p, int q, int& f0, int& f1) {
+  f0 = -1;
+  f1 = -1;
+  for (int v = 0; v < 4; ++v) {
+    if (v == p || v == q) continue;
+    if (f0 < 0) f0 = v;
+    else if (f1 < 0) f1 = v;
+  }
 }
 
 // The first two of the position buffers {0, 1, 2, 4} other than p and q (p == q allowed).
@@ -243,6 +254,10 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     // need the residual and objective, so a warp reads them (iteration top: trace, best iterate, convergence)
     // after the product of its first chunk, or after the phase when it gets no chunk.
     int ispec = 4;
+    // momentum product by linearity: imp holds W prev (prev = x after the projection: MX(imx)); each trial
+    // product goes to ims and the momentum product fma(beta, W xs - W prev, W xs) to imn
+    const bool lin = apgd && a.lin_momentum != 0;
+    int imp = imx, ims = 1, imn = 2;
     double alpha_t = alpha * a.opt;
     if (!runA(alpha_t, true)) return -1;
     for (;;) {
@@ -268,8 +283,10 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
       double theta_spec = theta;
       const double beta_spec = apgd ? nesterov_inertia(theta_spec, 0.0) : 0.0;
       const T bt = T(beta_spec);
+      if (lin) two_free_mx(imx, imp, ims, imn);
+      const int ims_t = lin ? ims : 1 - imx;
       for (;;) {
-        // C: Mxs = W xs, the line-search terms and the speculative momentum point
+        // C: Mxs = W xs, the line-search terms and the speculative momentum point (and its product, lin)
         for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
@@ -278,7 +295,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
           if (!top()) return -1;
           if (converged) break;
           if (i < a.n) {
-            store3(B.MX(1 - imx), i, acc);
+            store3(B.MX(ims_t), i, acc);
             T x[3], xs[3], pv[3], y[3];
             load3cg(B.X(ix), i, x);
             load3cg(B.X(ixs), i, xs);
@@ -297,6 +314,13 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
             if (apgd) {
               const T xn[3] = {fma(bt, xs[0] - pv[0], xs[0]), fma(bt, xs[1] - pv[1], xs[1]), fma(bt, xs[2] - pv[2], xs[2])};
               store3(B.X(ispec), i, xn);
+              if (lin) {
+                T mp[3];
+                load3cg(B.MX(imp), i, mp);
+                const T mn[3] = {fma(bt, acc[0] - mp[0], acc[0]), fma(bt, acc[1] - mp[1], acc[1]),
+                                 fma(bt, acc[2] - mp[2], acc[2])};
+                store3(B.MX(imn), i, mn);
+              }
             }
           }
           put4(c, v0, v1, v2, v3);
@@ -338,6 +362,13 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
         two_free(ix, iprev, ixs, ispec);
         if (!more) break;
         alpha_t = alpha * a.opt;
+        if (lin) {
+          // W x formed in C: A alone
+          imx = imn;
+          imp = ims;
+          if (!runA(alpha_t, true)) return -1;
+          continue;
+        }
         // E + A: Mx = W x, then A of the next iteration on the same rows
         ph[6]++;
         for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
@@ -356,7 +387,12 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
         theta = 1.;
         ix = ixs;
         iprev = ixs;
-        imx = 1 - imx;
+        if (lin) {
+          imx = ims;
+          imp = ims;
+        } else {
+          imx = 1 - imx;
+        }
         two_free(ix, iprev, ixs, ispec);
         if (!more) break;
         alpha_t = alpha * a.opt;
@@ -555,6 +591,10 @@ __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgsT<T> ba) {
     a.X2 = ba.base.X2 + 3 * (size_t)c0;
     a.MX0 = ba.base.MX0 + 3 * (size_t)c0;
     a.MX1 = ba.base.MX1 + 3 * (size_t)c0;
+    if (ba.base.lin_momentum) {
+      a.MX2 = ba.base.MX2 + 3 * (size_t)c0;
+      a.MX3 = ba.base.MX3 + 3 * (size_t)c0;
+    }
     a.Y = ba.base.Y + 3 * (size_t)c0;
     a.S0 = ba.base.S0 + c0;
     a.XB = ba.base.XB + 3 * (size_t)c0;
@@ -650,6 +690,10 @@ __global__ void __launch_bounds__(256, 3) k_pg_team(PGBatchArgsT<T> ba, PGTeamAr
     a.X2 = ba.base.X2 + 3 * (size_t)c0;
     a.MX0 = ba.base.MX0 + 3 * (size_t)c0;
     a.MX1 = ba.base.MX1 + 3 * (size_t)c0;
+    if (ba.base.lin_momentum) {
+      a.MX2 = ba.base.MX2 + 3 * (size_t)c0;
+      a.MX3 = ba.base.MX3 + 3 * (size_t)c0;
+    }
     a.Y = ba.base.Y + 3 * (size_t)c0;
     a.S0 = ba.base.S0 + c0;
     a.XB = ba.base.XB + 3 * (size_t)c0;

@@ -124,6 +124,8 @@ extern "C" int bogus_gpu_solve_pg_noalloc(int device, int n, int nnzb, const int
   if (o->variant != BOGUS_GPU_PG_APGD && o->variant != BOGUS_GPU_PG_DESCENT && o->variant != BOGUS_GPU_PG_SPG)
     return fail(BOGUS_GPU_BAD_INPUT, "projected-gradient variant not available on the GPU (APGD, Descent, SPG)");
   if (o->ls_iters == 0 && o->variant != BOGUS_GPU_PG_SPG) return fail(BOGUS_GPU_BAD_INPUT, "ls_iters must be >= 1");
+  if (o->momentum_by_linearity && o->variant == BOGUS_GPU_PG_APGD)
+    return fail(BOGUS_GPU_BAD_INPUT, "momentum_by_linearity needs two more product buffers than the fixed array holds");
   if (o->mixed_precision) return fail(BOGUS_GPU_BAD_INPUT, "the allocation-free entry point solves in FP64 only");
   if (!(o->tol >= 0) || !(o->ls_optimistic_factor > 0) || !(o->ls_pessimistic_factor > 0))
     return fail(BOGUS_GPU_BAD_INPUT, "invalid projected-gradient factors");
