@@ -390,7 +390,7 @@ def measure_secondary(args, D, d, r_fp64, fp64_ms):
                       "its null space"}
     # options with no counterpart in the reference: APGD's momentum product formed by linearity (one pass over
     # W fewer per momentum step; the oracle restates the same variant, tests check it bit for bit), alone and
-    # with the FP32-refined form
+    # with the FP32-refined form (where it applies to the FP64 iterations)
     for key, mixed in (("apgd_momentum_by_linearity_to_1e-6", False),
                        ("fp32_refined_momentum_by_linearity_to_1e-6", True)):
         pgl = bogus_gpu.ProjectedGradient()
@@ -522,6 +522,14 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
     solve(pgm)
     mixed_ms, (res_m, its_m) = _sync_time(lambda: solve(pgm), world)
     st_m = D.solve_stats()
+    # the momentum product formed by linearity (an option, not the reference's arithmetic), same budget
+    pgl = bogus_gpu.ProjectedGradient()
+    pgl.setTol(TOL)
+    pgl.setMaxIters(BATCH_MAX_ITERS)
+    pgl.setMomentumByLinearity(True)
+    solve(pgl)
+    lin_ms, (res_l, its_l) = _sync_time(lambda: solve(pgl), world)
+    st_l = D.solve_stats()
     # the launch shape chosen by the tuner (measured on this batch) against the default rule, same results
     rule_shape = D.batchShape()
     D.setBatchTuning(True)
@@ -558,13 +566,15 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
                "capture_call_ms": graph[0], "identical_results": graph_same,
                "note": "host-buffer calls (pinned r), wall time per call including copies; the first graph call "
                        "captures"}
-    allres = shard.gather_results(mine, np.stack([res, its, res_m], 1), nprob, world)
+    allres = shard.gather_results(mine, np.stack([res, its, res_m, res_l], 1), nprob, world)
     out = {"problems": nprob, "contacts": int(d.n), "ranks": world, "max_iters": BATCH_MAX_ITERS,
            "batched_ms": statistics.median(times), "kernel_ms": statistics.median(kernel),
            "tuned": tuned, "cuda_graph": graphed,
            "algorithmic_gbs": st["algorithmic_bytes"] / (st["device_ms"] * 1e-3) / 1e9,
            "fp32_refined": {"split": "up to 200 FP32 + 300 FP64 iterations per problem", "batched_ms": mixed_ms,
                             "kernel_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"]},
+           "momentum_by_linearity": {"batched_ms": lin_ms, "kernel_ms": st_l["device_ms"],
+                                     "w_passes": st_l["w_passes"], "w_passes_reference_form": st["w_passes"]},
            "timing": f"median of {steps} solves after a warm-up, wall time between device synchronisations"}
     if world > 1:
         out["partition"] = {"rule": "greedy bin-pack on W blocks", "blocks_per_rank": [int(costs[q].sum()) for q in parts],
@@ -576,6 +586,8 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
     out["converged_fraction"] = float(np.mean(allres[:, 0] < TOL))
     out["fp32_refined"]["converged_fraction"] = float(np.mean(allres[:, 2] < TOL))
     out["fp32_refined"]["speedup_vs_fp64_batch"] = out["batched_ms"] / mixed_ms
+    out["momentum_by_linearity"]["converged_fraction"] = float(np.mean(allres[:, 3] < TOL))
+    out["momentum_by_linearity"]["speedup_vs_fp64_batch"] = out["batched_ms"] / lin_ms
     if world == 1 and sample_stride:
         # the single-problem path, problem by problem (inputs set beforehand, each solve timed with its r copies)
         sys.path.insert(0, os.path.join(REPO, "oracle"))

@@ -79,7 +79,9 @@ typedef struct bogus_gpu_pg_options {
                                      product and the kept product of prev: one pass over W fewer per momentum
                                      step, iterates that differ from the reference's by rounding (and a returned
                                      residual evaluated with that product, equal to the error function at the
-                                     returned iterate up to rounding). Single-problem and batched solves; the
+                                     returned iterate up to rounding). Single-problem and batched solves; with
+                                     mixed_precision it applies to the FP64 iterations only (in FP32 the
+                                     recombined product's rounding makes the line search retry more often); the
                                      allocation-free entry point rejects it */
 } bogus_gpu_pg_options;
 

@@ -655,6 +655,9 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   a.stripes = h->scal.p + 8;
   a.mono = reinterpret_cast<unsigned long long*>(h->barrier.p + 8);
   fill_args(a, o);
+  // momentum_by_linearity applies to the FP64 iterations only: in FP32 the recombined product's rounding makes
+  // the line search retry more often (measured slower, with a worse starting point for the FP64 part)
+  a.lin_momentum = 0;
   BG_CUDA(launch_convert(n3, h->X.p, h->X32.p, s));
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 16 * sizeof(unsigned), s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
@@ -3403,7 +3406,7 @@ int run_pg_batch_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, doub
   a.Wv = h->Wv32.p;
   a.csum = h->csum.p;
   a.out = h->batch_out.p;
-  a.lin_momentum = lin_momentum(o);
+  a.lin_momentum = 0;  // FP64 iterations only, as in run_pg_mixed
   a.desaxce = o->static_problem ? 0 : 1;
   a.variant = o->variant;
   a.use_inf = o->use_infinity_norm ? 1 : 0;

@@ -97,10 +97,10 @@ def test_lin_momentum_full_size(bg, oracle):
 
 
 def test_lin_momentum_mixed_precision(bg, oracle, c1):
-    """FP32-refined with the option: the FP32 part and the FP64 refinement both form the momentum product by
-    linearity; the returned residual meets the tolerance and equals the oracle's error function at the returned
-    iterate up to rounding (it is evaluated with the product formed by linearity), and the solve repeats bit
-    for bit."""
+    """FP32-refined with the option (applied to the FP64 iterations: the FP32 part is the plain FP32-refined
+    one): the returned residual meets the tolerance and equals the oracle's error function at the returned
+    iterate up to rounding (it is evaluated with the product formed by linearity), the FP32 part makes as many
+    passes over W as without the option, and the solve repeats bit for bit."""
     d, rp, cl, vl = c1
     D = bg.DualFrictionProblem()
     D.set(rp, cl, vl, d.b, d.mu)
@@ -113,8 +113,14 @@ def test_lin_momentum_mixed_precision(bg, oracle, c1):
     r = np.zeros(3 * d.n)
     res = D.solveWith(pg, r, staticProblem=True)
     assert res < 1e-10 and abs(res - O.eval(r, coulomb=False)) <= 1e-9 * res
+    st = D.solve_stats()
     r2 = np.zeros(3 * d.n)
     assert D.solveWith(pg, r2, staticProblem=True) == res and np.array_equal(r, r2)
+    pg.setMomentumByLinearity(False)
+    D.solveWith(pg, np.zeros(3 * d.n), staticProblem=True)
+    plain = D.solve_stats()
+    assert plain["fp32_device_ms"] > 0 and st["iterations"] - st["refine_iterations"] == \
+        plain["iterations"] - plain["refine_iterations"]
 
 
 def test_lin_momentum_batched(bg, oracle):
