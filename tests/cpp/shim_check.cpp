@@ -56,8 +56,11 @@ int defaults() {
   // options built from the setters
   pg.setMaxIters(17);
   pg.setDefaultVariant(bogus_gpu::projected_gradient::SPG);
+  expect(pg.options(true).momentum_by_linearity == 0, "ProjectedGradient: the reference's momentum product by default");
+  pg.setMomentumByLinearity(true);
   const bogus_gpu_pg_options o = pg.options(false);
-  expect(o.max_iters == 17 && o.variant == BOGUS_GPU_PG_SPG && o.static_problem == 0, "ProjectedGradient options");
+  expect(o.max_iters == 17 && o.variant == BOGUS_GPU_PG_SPG && o.static_problem == 0 && o.momentum_by_linearity == 1,
+         "ProjectedGradient options");
 
   // host-side BAD_INPUT paths (no GPU needed)
   bogus_gpu::DualFrictionProblem<3> dual;
