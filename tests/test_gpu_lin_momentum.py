@@ -149,6 +149,42 @@ def test_lin_momentum_batched(bg, oracle):
         assert np.array_equal(r[3 * c0:3 * c1_], r_o), p
 
 
+@pytest.mark.parametrize("mixed", [False, True])
+def test_lin_momentum_team_batch(bg, oracle, mixed):
+    """Few large problems (several CTAs per problem, the team schedule): each problem equals its own
+    single-problem solve with the option and, in FP64, the oracle's variant."""
+    from bogus_gpu import generator
+
+    d, cptr = generator.batch(nproblems=5, nmin=1500, nmax=3000, seed=13)
+    D = bg.DualFrictionProblem()
+    D.computeFrom(bg.PrimalFrictionProblem.from_generated(d))
+    D.setBatch(cptr)
+    pg = bg.ProjectedGradient()
+    pg.setTol(1e-8)
+    pg.setMaxIters(150)
+    pg.setMomentumByLinearity(True)
+    if mixed:
+        pg.setMixedPrecision(True, 40)
+    r = np.zeros(3 * d.n)
+    res, its = D.solveBatchWith(pg, r, staticProblem=True)
+    rp, cl, vl = D.W_lower()
+    vl = vl.reshape(-1, 9)
+    single = bg.DualFrictionProblem()
+    for p in range(len(cptr) - 1):
+        c0, c1_ = cptr[p], cptr[p + 1]
+        prp, pcl, pvl = rp[c0:c1_ + 1] - rp[c0], cl[rp[c0]:rp[c1_]] - c0, vl[rp[c0]:rp[c1_]].reshape(-1)
+        single.set(prp, pcl, pvl, d.b[c0:c1_], d.mu[c0:c1_])
+        rs = np.zeros(3 * (c1_ - c0))
+        res_s = single.solveWith(pg, rs)
+        assert res[p] == res_s and its[p] == single.last_iterations, p
+        assert np.array_equal(r[3 * c0:3 * c1_], rs), p
+        if not mixed:
+            O = oracle.DualProblem(prp, pcl, pvl, d.b[c0:c1_], d.mu[c0:c1_])
+            res_o, r_o, it_o = O.solve_pg(np.zeros(3 * (c1_ - c0)), variant=3, coulomb=False, tol=1e-8,
+                                          max_iters=150, lin_momentum=True)
+            assert res[p] == res_o and its[p] == it_o and np.array_equal(rs, r_o), p
+
+
 def test_noalloc_rejects_lin_momentum(bg):
     """The allocation-free entry point has no room for the two extra product buffers: BAD_INPUT before anything
     runs (an empty problem, so no device pointer is needed)."""
