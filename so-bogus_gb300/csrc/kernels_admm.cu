@@ -114,6 +114,7 @@ __device__ __forceinline__ void store3(double* p, int i, const double* v) {
 template <int D>
 __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
   constexpr int DM = D > 0 ? D : kMaxDof;
+  constexpr bool kPair = D > 0 && D % 2 == 0;
   const int d = dofs<D>(a);
   const int lane = threadIdx.x & 31;
   const int C = ctx.nchunks;
@@ -153,60 +154,165 @@ __device__ void admm_body(const ADMMArgs& a, AdmmCtx& ctx) {
   unsigned it = 0;
   for (it = 0; it < a.max_iters; ++it) {
     const double* rc = rb[cur];
-    // P1: x = prox(prox_arg) per body (lane order a.border: bodies of similar contact counts share a warp)
-    for (int c = ctx.next(); c < CB; c = ctx.next()) {
-      const int slot = 32 * c + lane;
-      if (slot < a.nbodies) {
-        const int b = a.border ? __ldg(a.border + slot) : slot;
-        double acc[DM];
-        const double* xb = a.x + (size_t)b * d;
+    // P1: x = prox(prox_arg) per body (lane order a.border: bodies of similar contact counts share a warp).
+    // Even compile-time d: a lane pair per body, each lane the FMA chains of half the dofs (16 bodies per warp,
+    // twice the chunks to spread over the warps), the halves exchanged exactly for the prox product.
+    if (kPair) {
+      constexpr int H2 = kPair ? D / 2 : 1;
+      const int half = lane & 1;
+      const int CB2 = (a.nbodies + 15) / 16;
+      for (int c = ctx.next(); c < CB2; c = ctx.next()) {
+        const int slot = 16 * c + (lane >> 1);
+        const bool on = slot < a.nbodies;
+        const int b = on ? (a.border ? __ldg(a.border + slot) : slot) : 0;
+        const int q0 = half * H2;
+        double acc[H2];
 #pragma unroll
-        for (int q = 0; q < DM; ++q)
-          if (q < d) acc[q] = with_lambda ? il * ldcg(xb + q) : 0.0;
-        const int e0 = __ldg(a.bptr + b), e1 = __ldg(a.bptr + b + 1);
+        for (int k = 0; k < H2; ++k) acc[k] = (on && with_lambda) ? il * ldcg(a.x + (size_t)b * D + q0 + k) : 0.0;
+        const int e0 = on ? __ldg(a.bptr + b) : 0, e1 = on ? __ldg(a.bptr + b + 1) : 0;
+        // the incidence indices two steps ahead, this lane's H columns and r one step ahead of the accumulation
+        int ent1 = e0 < e1 ? __ldg(a.bent + e0) : 0;
+        int ent2 = e0 + 1 < e1 ? __ldg(a.bent + e0 + 1) : 0;
+        double Hn[3 * H2], rn[3] = {0.0, 0.0, 0.0};
+        auto load_inc = [&](int ent, double* Hv, double* rv) {
+          const double* Hb = a.H + (size_t)ent * 3 * D + q0;
+#pragma unroll
+          for (int rr = 0; rr < 3; ++rr)
+#pragma unroll
+            for (int k = 0; k < H2; ++k) Hv[rr * H2 + k] = __ldg(Hb + rr * D + k);
+          load3(rc, ent >> 1, rv);
+        };
+        if (e0 < e1) load_inc(ent1, Hn, rn);
         for (int e = e0; e < e1; ++e) {
-          const int ent = __ldg(a.bent + e);
-          const int i = ent >> 1;
-          const double* Hb = a.H + (size_t)ent * 3 * d;
-          double rv[3];
-          load3(rc, i, rv);
+          const int ent = ent1;
+          ent1 = ent2;
+          ent2 = e + 2 < e1 ? __ldg(a.bent + e + 2) : 0;
+          double Hc[3 * H2], rv[3] = {rn[0], rn[1], rn[2]};
+#pragma unroll
+          for (int k = 0; k < 3 * H2; ++k) Hc[k] = Hn[k];
+          if (e + 1 < e1) load_inc(ent1, Hn, rn);
           if (with_lambda) {
+            const int i = ent >> 1;
             double za[3], ut[3];
             load3(plain ? a.z : a.zacc, i, za);
             load3(a.ut, i, ut);
             for (int k = 0; k < 3; ++k) rv[k] = fma(gamma, za[k] - ut[k], rv[k]);
           }
 #pragma unroll
-          for (int q = 0; q < DM; ++q) {
-            if (q < d) {
-              double s = acc[q];
-              for (int rr = 0; rr < 3; ++rr) s = fma(__ldg(Hb + rr * d + q), rv[rr], s);
-              acc[q] = s;
-            }
+          for (int k = 0; k < H2; ++k) {
+            double s = acc[k];
+#pragma unroll
+            for (int rr = 0; rr < 3; ++rr) s = fma(Hc[rr * H2 + k], rv[rr], s);
+            acc[k] = s;
           }
         }
         // QuadraticProxOp::eval: res = prox (rhs - f)
-        if (a.f) {
+        if (on && a.f) {
 #pragma unroll
-          for (int q = 0; q < DM; ++q)
-            if (q < d) acc[q] = acc[q] - __ldg(a.f + (size_t)b * d + q);
+          for (int k = 0; k < H2; ++k) acc[k] = acc[k] - __ldg(a.f + (size_t)b * D + q0 + k);
         }
-        const double* P = a.prox + (size_t)b * d * d;
-        double xn[DM];
+        double full[kPair ? D : 1];
 #pragma unroll
-        for (int m = 0; m < DM; ++m) {
-          if (m < d) {
-            double s = 0.0;
+        for (int k = 0; k < H2; ++k) {
+          const double other = __shfl_xor_sync(0xffffffffu, acc[k], 1);
+          full[k] = half ? other : acc[k];
+          full[H2 + k] = half ? acc[k] : other;
+        }
+        if (on) {
+          const double* P = a.prox + (size_t)b * D * D;
 #pragma unroll
-            for (int q = 0; q < DM; ++q)
-              if (q < d) s = fma(__ldg(P + m * d + q), acc[q], s);
-            xn[m] = s;
+          for (int k = 0; k < H2; ++k) {
+            const int m = q0 + k;
+            double sum = 0.0;
+#pragma unroll
+            for (int q = 0; q < D; ++q) sum = fma(__ldg(P + m * D + q), full[q], sum);
+            a.x[(size_t)b * D + m] = sum;
           }
         }
-        double* xw = a.x + (size_t)b * d;
-#pragma unroll
-        for (int m = 0; m < DM; ++m)
-          if (m < d) xw[m] = xn[m];
+      }
+    } else {
+      for (int c = ctx.next(); c < CB; c = ctx.next()) {
+        const int slot = 32 * c + lane;
+        if (slot < a.nbodies) {
+          const int b = a.border ? __ldg(a.border + slot) : slot;
+          double acc[DM];
+          const double* xb = a.x + (size_t)b * d;
+  #pragma unroll
+          for (int q = 0; q < DM; ++q)
+            if (q < d) acc[q] = with_lambda ? il * ldcg(xb + q) : 0.0;
+          const int e0 = __ldg(a.bptr + b), e1 = __ldg(a.bptr + b + 1);
+          // Loads run ahead of the accumulation (its order is unchanged): the incidence indices two steps
+          // ahead and, for a compile-time d, the H rows and r of the next incidence, so that no step waits on
+          // the dependent index -> H / r load chain.
+          constexpr bool kPre = D > 0;
+          int ent1 = e0 < e1 ? __ldg(a.bent + e0) : 0;
+          int ent2 = e0 + 1 < e1 ? __ldg(a.bent + e0 + 1) : 0;
+          double Hn[kPre ? 3 * DM : 1], rn[3] = {0.0, 0.0, 0.0};
+          if (kPre && e0 < e1) {
+            const double* Hb = a.H + (size_t)ent1 * 3 * DM;
+  #pragma unroll
+            for (int k = 0; k < (kPre ? 3 * DM : 1); ++k) Hn[k] = __ldg(Hb + k);
+            load3(rc, ent1 >> 1, rn);
+          }
+          for (int e = e0; e < e1; ++e) {
+            const int ent = ent1;
+            ent1 = ent2;
+            ent2 = e + 2 < e1 ? __ldg(a.bent + e + 2) : 0;
+            const int i = ent >> 1;
+            double Hc[kPre ? 3 * DM : 1];
+            double rv[3];
+            if (kPre) {
+  #pragma unroll
+              for (int k = 0; k < (kPre ? 3 * DM : 1); ++k) Hc[k] = Hn[k];
+              rv[0] = rn[0]; rv[1] = rn[1]; rv[2] = rn[2];
+              if (e + 1 < e1) {
+                const double* Hb = a.H + (size_t)ent1 * 3 * DM;
+  #pragma unroll
+                for (int k = 0; k < (kPre ? 3 * DM : 1); ++k) Hn[k] = __ldg(Hb + k);
+                load3(rc, ent1 >> 1, rn);
+              }
+            } else {
+              load3(rc, i, rv);
+            }
+            if (with_lambda) {
+              double za[3], ut[3];
+              load3(plain ? a.z : a.zacc, i, za);
+              load3(a.ut, i, ut);
+              for (int k = 0; k < 3; ++k) rv[k] = fma(gamma, za[k] - ut[k], rv[k]);
+            }
+            const double* Hb = a.H + (size_t)ent * 3 * d;
+  #pragma unroll
+            for (int q = 0; q < DM; ++q) {
+              if (q < d) {
+                double s = acc[q];
+                for (int rr = 0; rr < 3; ++rr) s = fma(kPre ? Hc[rr * DM + q] : __ldg(Hb + rr * d + q), rv[rr], s);
+                acc[q] = s;
+              }
+            }
+          }
+          // QuadraticProxOp::eval: res = prox (rhs - f)
+          if (a.f) {
+  #pragma unroll
+            for (int q = 0; q < DM; ++q)
+              if (q < d) acc[q] = acc[q] - __ldg(a.f + (size_t)b * d + q);
+          }
+          const double* P = a.prox + (size_t)b * d * d;
+          double xn[DM];
+  #pragma unroll
+          for (int m = 0; m < DM; ++m) {
+            if (m < d) {
+              double s = 0.0;
+  #pragma unroll
+              for (int q = 0; q < DM; ++q)
+                if (q < d) s = fma(__ldg(P + m * d + q), acc[q], s);
+              xn[m] = s;
+            }
+          }
+          double* xw = a.x + (size_t)b * d;
+  #pragma unroll
+          for (int m = 0; m < DM; ++m)
+            if (m < d) xw[m] = xn[m];
+        }
       }
     }
     if (!ctx.sync()) return;
