@@ -148,6 +148,10 @@ struct bogus_gpu_problem {
   bool il_valid = false;
   DevBuf<long long> slot0;
   DevBuf<int> chunk_order;  // chunks by decreasing segment length (ticket order of the persistent solvers)
+  std::vector<int> h_chunk_order;  // the same on the host
+  // per-CTA chunk lists of the single-problem kernel for a grid of cta_grid CTAs (0: none built)
+  DevBuf<int> cta_ptr, cta_list;
+  int cta_grid = 0;
   DevBuf<int> icol;
   DevBuf<double> ival;
   // FP32 copies of W (interleaved), b, mu, scalings and FP32 work (mixed precision), valid while W is unchanged
@@ -428,6 +432,7 @@ int ensure_pg_work(bogus_gpu_problem* h, unsigned max_iters) {
 }
 
 int ensure_interleaved(bogus_gpu_problem* h);
+int ensure_cta_lists(bogus_gpu_problem* h, int G);
 int ensure_incidence(bogus_gpu_problem* h);
 
 // Algorithmic bytes and W passes of one persistent solve from its phase counters. A W pass reads nnzb blocks
@@ -508,6 +513,9 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
   const int want = (a.nchunks + 7) / 8;
   if (want < grid) grid = want < 1 ? 1 : want;
+  if (int e = ensure_cta_lists(h, grid)) return e;
+  a.cta_ptr = h->cta_ptr.p;
+  a.cta_list = h->cta_list.p;
   BG_CUDA(cudaEventRecord(h->ev0, h->stream));
   BG_CUDA(launch_pg_persistent(a, grid, h->stream));
   BG_CUDA(cudaEventRecord(h->ev1, h->stream));
@@ -544,6 +552,33 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
 
 // The interleaved copy of W: chunk c (rows 32c .. 32c+31, blocks [B0, B1)) takes 32 S slots, S =
 // ceil((B1 - B0) / 32) (1 for an empty chunk), from slot0[c].
+// Per-CTA chunk lists for a grid of G CTAs: the chunks in ticket order (largest first) dealt to the CTAs
+// in serpentine rounds (0 .. G-1, then G-1 .. 0, ...), so every CTA's total and every SM's (its resident
+// CTAs') are equal to within about one chunk; each CTA's warps share its list dynamically. A phase then
+// ends with every SM at about the same time instead of each SM finishing the chunks it happened to hold when
+// a global ticket pool ran out. Which warp handles a chunk does not change any result.
+int ensure_cta_lists(bogus_gpu_problem* h, int G) {
+  if (h->cta_grid == G) return BOGUS_GPU_OK;
+  const int C = (int)h->h_chunk_order.size();
+  std::vector<int> cnt(G + 1, 0), owner(C);
+  for (int k = 0; k < C; ++k) {
+    const int round = k / G, pos = k % G;
+    owner[k] = (round & 1) ? G - 1 - pos : pos;
+    ++cnt[owner[k] + 1];
+  }
+  for (int b = 0; b < G; ++b) cnt[b + 1] += cnt[b];
+  std::vector<int> list(C > 0 ? C : 1), fill(cnt.begin(), cnt.end() - 1);
+  for (int k = 0; k < C; ++k) list[fill[owner[k]]++] = h->h_chunk_order[k];
+  BG_CUDA(h->cta_ptr.ensure(G + 1));
+  BG_CUDA(h->cta_list.ensure(C > 0 ? C : 1));
+  BG_CUDA(cudaMemcpyAsync(h->cta_ptr.p, cnt.data(), sizeof(int) * (G + 1), cudaMemcpyHostToDevice, h->stream));
+  BG_CUDA(cudaMemcpyAsync(h->cta_list.p, list.data(), sizeof(int) * (C > 0 ? C : 1), cudaMemcpyHostToDevice,
+                          h->stream));
+  BG_CUDA(cudaStreamSynchronize(h->stream));
+  h->cta_grid = G;
+  return BOGUS_GPU_OK;
+}
+
 int ensure_interleaved(bogus_gpu_problem* h) {
   if (h->il_valid) return BOGUS_GPU_OK;
   const int n = h->W.n;
@@ -561,6 +596,8 @@ int ensure_interleaved(bogus_gpu_problem* h) {
     order[c] = c;
   }
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return seg[x] > seg[y]; });
+  h->h_chunk_order = order;
+  h->cta_grid = 0;
   BG_CUDA(h->chunk_order.ensure(C > 0 ? C : 1));
   if (C) BG_CUDA(cudaMemcpyAsync(h->chunk_order.p, order.data(), sizeof(int) * C, cudaMemcpyHostToDevice, h->stream));
   const size_t slots = (size_t)s0[C];
@@ -665,6 +702,9 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   if (grid <= 0) return fail(BOGUS_GPU_CUDA_ERROR, "cooperative occupancy query failed");
   const int want = (a.nchunks + 7) / 8;
   if (want < grid) grid = want < 1 ? 1 : want;
+  if (int e = ensure_cta_lists(h, grid)) return e;
+  a.cta_ptr = h->cta_ptr.p;
+  a.cta_list = h->cta_list.p;
   BG_CUDA(cudaEventRecord(h->ev0, s));
   BG_CUDA(launch_pg_persistent(a, grid, s));
   BG_CUDA(cudaEventRecord(h->ev1, s));
@@ -957,6 +997,8 @@ int bogus_gpu_destroy(bogus_gpu_problem* h) {
     b->release();
   h->slot0.release();
   h->chunk_order.release();
+  h->cta_ptr.release();
+  h->cta_list.release();
   h->icol.release();
   h->ival.release();
   for (auto* b : {&h->a_prox, &h->a_f, &h->a_w, &h->a_mu, &h->a_invmu, &h->a_x, &h->a_r, &h->a_ut, &h->a_z, &h->a_zacc,

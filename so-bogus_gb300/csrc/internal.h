@@ -47,6 +47,10 @@ struct PGArgsT {
   const T* ival;
   const long long* slot0;
   const int* chunk_order;  // chunks in the order the tickets hand them out (largest first); null: natural
+  // per-CTA chunk lists of the single-problem kernel (CTA b takes cta_list[cta_ptr[b] .. cta_ptr[b+1]), its
+  // warps sharing them through a counter in shared memory); null: one global ticket counter
+  const int* cta_ptr;
+  const int* cta_list;
   const T* b;
   const T* mu;
   const T* scaling;

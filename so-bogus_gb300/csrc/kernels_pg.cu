@@ -478,24 +478,38 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
 // Single problem: the whole GPU, phases separated by bounded grid barriers on monotonic counters
 // (mono_barrier); at a reducing barrier the last CTAs to arrive combine the chunk sums, one stripe each, and
 // the last of them publishes the scalars in global memory. After a split reduction the CTAs go on once every
-// CTA has arrived, and each warp waits for the publication only where it reads the scalars. Warps take 32-contact chunks from a ticket counter (one
-// per phase parity, cleared by the last CTA of the barrier that ends the phase), so SMs that finish early
-// take more chunks; tickets map to chunks largest first (chunk_order), so the last chunks of a phase are
-// the short ones. Every cross-phase dependency goes through a barrier, and the reduction order does not
-// depend on which warp handles a chunk.
+// CTA has arrived, and each warp waits for the publication only where it reads the scalars. Each CTA takes
+// its 32-contact chunks from its own list (cta_ptr / cta_list: the chunks dealt largest first to the CTAs in
+// serpentine rounds, so every SM's total is the same to within about one chunk), its warps sharing the list
+// through a shared-memory counter per phase parity; without lists (the allocation-free entry point) warps
+// take chunks from a global ticket counter per phase parity, cleared by the last CTA of the barrier that ends
+// the phase, in largest-first order (chunk_order). Every cross-phase dependency goes through a barrier, and
+// the reduction order does not depend on which warp handles a chunk.
 template <class T>
 struct GridCtx {
   const PGArgsT<T>& a;
   double* smem8;
   ChunkScratchT<T>* cs;
+  unsigned* s_cnt;     // 2 shared-memory counters (phase parity) over the CTA's chunk list
   unsigned phase = 0;  // barriers passed (identical in every CTA)
   __device__ int ticket() {
     int c = 0;
     if ((threadIdx.x & 31) == 0) {
-      c = (int)atomicAdd(a.tickets + (phase & 1u), 1u);
-      if (a.chunk_order) c = c < a.nchunks ? __ldg(a.chunk_order + c) : a.nchunks;
+      if (a.cta_ptr) {
+        const int k = (int)atomicAdd(s_cnt + (phase & 1u), 1u);
+        const int b0 = __ldg(a.cta_ptr + blockIdx.x), b1 = __ldg(a.cta_ptr + blockIdx.x + 1);
+        c = b0 + k < b1 ? __ldg(a.cta_list + b0 + k) : a.nchunks;
+      } else {
+        c = (int)atomicAdd(a.tickets + (phase & 1u), 1u);
+        if (a.chunk_order) c = c < a.nchunks ? __ldg(a.chunk_order + c) : a.nchunks;
+      }
     }
     return __shfl_sync(0xffffffffu, c, 0);
+  }
+  // after a barrier (every warp of the CTA is past its draws of this phase): the counter of this phase's
+  // parity is free for the phase after next
+  __device__ void reset_cta_counter() {
+    if (a.cta_ptr && threadIdx.x == 0) s_cnt[phase & 1u] = 0u;
   }
   __device__ int first_chunk() { return ticket(); }
   __device__ int next_chunk(int) { return ticket(); }
@@ -508,12 +522,14 @@ struct GridCtx {
   __device__ MonoBarrier mb() const { return MonoBarrier{a.mono, a.gb.status, gridDim.x + a.phantom_ctas}; }
   __device__ bool sync() {
     const bool ok = mono_barrier(mb(), phase, [&] { clear_tickets(); });
+    reset_cta_counter();
     ++phase;
     return ok;
   }
   __device__ bool reduce(int K, unsigned maxmask, bool split) {
     const bool ok = mono_barrier_combine(mb(), phase, reductions, split, a.csum, (size_t)a.nchunks, a.nchunks,
                                          a.nchunks, K, maxmask, a.stripes, a.scal, [&] { clear_tickets(); });
+    reset_cta_counter();
     ++phase;
     ++reductions;
     pending = split;
@@ -534,7 +550,10 @@ template <class T, bool IL>
 __global__ void __launch_bounds__(256, 3) k_pg_persistent(PGArgsT<T> a) {
   __shared__ double smem8[32];
   __shared__ ChunkScratchT<T> cs[8];
-  GridCtx<T> ctx{a, smem8, cs};
+  __shared__ unsigned s_cnt[2];
+  if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0u;
+  __syncthreads();
+  GridCtx<T> ctx{a, smem8, cs, s_cnt};
   pg_body<T, IL>(a, ctx);
 }
 
