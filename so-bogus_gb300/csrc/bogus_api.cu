@@ -2353,6 +2353,7 @@ int run_adjoint(bogus_gpu_problem* h, const bogus_gpu_adjoint_options* o, double
   a.scal = h->scal.p;
   a.out = h->adj_out.p;
   a.gb = GridBarrier{h->barrier.p, h->barrier.p + 1, h->status.p};
+  a.tickets = h->barrier.p + 2;
   a.combine_count = h->barrier.p + 4;
   a.stripes = h->scal.p + 8;
   a.tol = o->tol;

@@ -385,6 +385,24 @@ __device__ __forceinline__ bool grid_barrier_combine(const GridBarrier& gb, unsi
   return ok;
 }
 
+// Dynamic work split: warps take 32-contact (or 32-body) chunks from a ticket counter, one per phase parity,
+// cleared by the last CTA of the barrier that ends the phase (every draw of the phase is done by then), so SMs
+// whose sub-partitions finish early take more chunks. Chunk sums are stored by chunk index, so the reduction
+// order does not depend on which warp handled a chunk.
+struct Tickets {
+  unsigned* t;         // 2 counters, zero at launch
+  unsigned phase = 0;  // barriers passed (identical in every CTA)
+  __device__ int next() {
+    int c = 0;
+    if ((threadIdx.x & 31) == 0) c = (int)atomicAdd(t + (phase & 1u), 1u);
+    return __shfl_sync(0xffffffffu, c, 0);
+  }
+  // run by every thread of the barrier's last CTA
+  __device__ void clear() {
+    if (threadIdx.x == 0) t[phase & 1u] = 0u;
+  }
+};
+
 // ---- grid barrier on monotonic counters (single-problem persistent solvers) ------------------------------
 // mono[0] counts CTA arrivals, mono[1] finished stripe combinations, mono[2] published reductions; all start
 // at zero at launch and only grow. Barrier k of a launch is complete when mono[0] reaches parties (k + 1),

@@ -307,6 +307,7 @@ struct AdjArgs {
   double* csum;
   double* scal;
   unsigned* combine_count;  // grid_barrier_combine's counter; zero at launch
+  unsigned* tickets;        // 2 chunk-ticket counters (one per phase parity); zero at launch
   double* stripes;          // 8 stripe sums per reduced quantity
   AdjOut* out;
   GridBarrier gb;

@@ -138,13 +138,22 @@ __device__ __forceinline__ void basis_apply_t(const double* V, const double* D, 
   }
 }
 
+// Warps take chunks from ticket counters (Tickets: dynamic balance; the chunk sums stay in chunk order).
 struct AdjCtx {
   const AdjArgs& a;
   double* smem8;
-  __device__ bool sync() { return grid_barrier(a.gb, [] {}); }
+  Tickets tk{a.tickets};
+  __device__ int next() { return tk.next(); }
+  __device__ bool sync() {
+    const bool ok = grid_barrier(a.gb, [&] { tk.clear(); });
+    ++tk.phase;
+    return ok;
+  }
   __device__ bool sync_reduce(int K) {
-    return grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)a.nchunks, a.nchunks, a.nchunks, K, 0u,
-                                a.stripes, a.scal, [] {});
+    const bool ok = grid_barrier_combine(a.gb, a.combine_count, a.csum, (size_t)a.nchunks, a.nchunks, a.nchunks, K,
+                                         0u, a.stripes, a.scal, [&] { tk.clear(); });
+    ++tk.phase;
+    return ok;
   }
 };
 
@@ -154,8 +163,6 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
   AdjCtx ctx{a, smem8};
   ChunkScratch& sh = cs[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
   const int C = a.nchunks;
   const bool writer = blockIdx.x == 0 && threadIdx.x == 0;
   auto put = [&](int q, int c, double v) {
@@ -169,7 +176,7 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
 
   // setup: x = r - alpha (W r + b), the basis, the preconditioner, rhs c = m o V^T g; p = 0, res = c,
   // z = Pinv c, dir = z, Y = V (m o dir)
-  for (int c = gwarp; c < C; c += nwarps) {
+  for (int c = ctx.next(); c < C; c = ctx.next()) {
     const int i = 32 * c + lane;
     double acc[3] = {0.0, 0.0, 0.0};
     product(c, a.r, acc);
@@ -213,7 +220,7 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
   for (; it < a.max_iters; ++it) {
     if (!(rr > stop)) break;
     // q = D o dir + m o V^T W Y, dir . q
-    for (int c = gwarp; c < C; c += nwarps) {
+    for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       double acc[3] = {0.0, 0.0, 0.0};
       product(c, a.Y, acc);
@@ -234,7 +241,7 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
     const double dq = ldcg(a.scal);
     if (!(dq > 0.0)) break;  // S is positive definite on the unmasked components; guards exact convergence
     const double step = rz / dq;
-    for (int c = gwarp; c < C; c += nwarps) {
+    for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       double v = 0.0, w = 0.0;
       if (i < a.n) {
@@ -263,7 +270,7 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
     const double rz_new = ldcg(a.scal + 1);
     const double beta = rz_new / rz;
     rz = rz_new;
-    for (int c = gwarp; c < C; c += nwarps) {
+    for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       if (i < a.n) {
         double V[9], D[3], z[3], d[3], y[3];
@@ -280,7 +287,7 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
     if (!ctx.sync()) return;
   }
   // s = dL/db = -V (m o p)
-  for (int c = gwarp; c < C; c += nwarps) {
+  for (int c = ctx.next(); c < C; c = ctx.next()) {
     const int i = 32 * c + lane;
     if (i < a.n) {
       double V[9], D[3], p[3], y[3];
@@ -294,7 +301,7 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
   }
   if (!ctx.sync()) return;
   // lam_hat and dL/dmu = K^T V lam_hat
-  for (int c = gwarp; c < C; c += nwarps) {
+  for (int c = ctx.next(); c < C; c = ctx.next()) {
     const int i = 32 * c + lane;
     double acc[3] = {0.0, 0.0, 0.0};
     product(c, a.S, acc);
@@ -399,8 +406,6 @@ __global__ void __launch_bounds__(256) k_adjoint_coulomb(AdjArgs a) {
   AdjCtx ctx{a, smem8};
   ChunkScratch& sh = cs[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  const int gwarp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
   const int C = a.nchunks;
   const bool writer = blockIdx.x == 0 && threadIdx.x == 0;
   auto put = [&](int q, int c, double v) {
@@ -425,7 +430,7 @@ __global__ void __launch_bounds__(256) k_adjoint_coulomb(AdjArgs a) {
   };
   // setup: u = W r + b, s(u), x = r - alpha (u + s(u)), the basis, tau, the preconditioner; rhs c = m o V^T g;
   // p = 0, residual = shadow = c, direction = v = 0
-  for (int c = gwarp; c < C; c += nwarps) {
+  for (int c = ctx.next(); c < C; c = ctx.next()) {
     const int i = 32 * c + lane;
     double acc[3] = {0.0, 0.0, 0.0};
     product(c, a.r, acc);
@@ -476,7 +481,7 @@ __global__ void __launch_bounds__(256) k_adjoint_coulomb(AdjArgs a) {
     if (!(rr > stop)) break;
     const double beta = (rho / rho_old) * (alpha / omega);
     // direction = r + beta (direction - omega v); ph = Pinv direction; Y = T^T V (m o ph)
-    for (int c = gwarp; c < C; c += nwarps) {
+    for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       if (i < a.n) {
         double res[3], d[3], v[3], Pinv[9], ph[3], V[9], D[3], tc[3], y[3];
@@ -495,7 +500,7 @@ __global__ void __launch_bounds__(256) k_adjoint_coulomb(AdjArgs a) {
     }
     if (!ctx.sync()) return;
     // v = A ph; shadow . v
-    for (int c = gwarp; c < C; c += nwarps) {
+    for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       double acc[3] = {0.0, 0.0, 0.0};
       product(c, a.Y, acc);
@@ -515,7 +520,7 @@ __global__ void __launch_bounds__(256) k_adjoint_coulomb(AdjArgs a) {
     if (!(hv != 0.0)) break;  // breakdown (or exact convergence)
     alpha = rho / hv;
     // s = r - alpha v; sh = Pinv s; Y = T^T V (m o sh)
-    for (int c = gwarp; c < C; c += nwarps) {
+    for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       if (i < a.n) {
         double res[3], v[3], sv[3], Pinv[9], shv[3], V[9], D[3], tc[3], y[3];
@@ -533,7 +538,7 @@ __global__ void __launch_bounds__(256) k_adjoint_coulomb(AdjArgs a) {
     }
     if (!ctx.sync()) return;
     // t = A sh; t . s, t . t
-    for (int c = gwarp; c < C; c += nwarps) {
+    for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       double acc[3] = {0.0, 0.0, 0.0};
       product(c, a.Y, acc);
@@ -554,7 +559,7 @@ __global__ void __launch_bounds__(256) k_adjoint_coulomb(AdjArgs a) {
     const double ts = ldcg(a.scal), tt = ldcg(a.scal + 1);
     omega = tt > 0.0 ? ts / tt : 0.0;
     // p += alpha ph + omega sh; r = s - omega t; shadow . r, r . r
-    for (int c = gwarp; c < C; c += nwarps) {
+    for (int c = ctx.next(); c < C; c = ctx.next()) {
       const int i = 32 * c + lane;
       double hr = 0.0, r2 = 0.0;
       if (i < a.n) {
@@ -587,7 +592,7 @@ __global__ void __launch_bounds__(256) k_adjoint_coulomb(AdjArgs a) {
     }
   }
   // s = dL/db = -T^T V (m o p)
-  for (int c = gwarp; c < C; c += nwarps) {
+  for (int c = ctx.next(); c < C; c = ctx.next()) {
     const int i = 32 * c + lane;
     if (i < a.n) {
       double V[9], D[3], tc[3], p[3], y[3];
@@ -600,7 +605,7 @@ __global__ void __launch_bounds__(256) k_adjoint_coulomb(AdjArgs a) {
   }
   if (!ctx.sync()) return;
   // lam_hat and dL/dmu = K^T V lam_hat - |u_T| (V m o p)_N
-  for (int c = gwarp; c < C; c += nwarps) {
+  for (int c = ctx.next(); c < C; c = ctx.next()) {
     const int i = 32 * c + lane;
     double acc[3] = {0.0, 0.0, 0.0};
     product(c, a.S, acc);
