@@ -52,10 +52,16 @@ int fail(int status, const std::string& msg) {
       return fail(BOGUS_GPU_CUDA_ERROR, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+// A device array owned by a handle: grown on demand, freed by release() or when the handle is deleted (on
+// the handle's device, which bogus_gpu_destroy makes current first). Not copyable: one owner per allocation.
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
   cudaError_t ensure(size_t count) {
     if (count <= n && p) return cudaSuccess;
     if (p) cudaFree(p);
@@ -189,7 +195,7 @@ struct bogus_gpu_problem {
   bool frames_valid = false;
   DevBuf<double> frames;
   // DualAMA: mass blocks, affine part and work
-  DevBuf<double> dm_M, dm_f, dm_v, dm_rs, dm_x, dm_hr, dm_g, dm_yp, dm_rb, dm_vb;
+  DevBuf<double> dm_M, dm_f, dm_v, dm_rs, dm_x, dm_hr, dm_g, dm_yp, dm_rb, dm_vb, dm_v2, dm_yp2;
   DevBuf<DamaOut> dama_out;
   // Cadoux fixed point: the original right-hand side while the inner solves use COV(u) + b
   DevBuf<double> cad_b;
@@ -2783,7 +2789,8 @@ int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_opti
   if (int e = ensure_incidence(h)) return e;
   const size_t nv = n3 > 0 ? n3 : 1;
   for (auto* b : {&h->a_w, &h->a_r, &h->a_ut, &h->dm_rs, &h->dm_g, &h->dm_rb}) BG_CUDA(b->ensure(nv));
-  for (auto* b : {&h->dm_f, &h->dm_v, &h->dm_x, &h->dm_hr, &h->dm_yp, &h->dm_vb}) BG_CUDA(b->ensure(m));
+  for (auto* b : {&h->dm_f, &h->dm_v, &h->dm_x, &h->dm_hr, &h->dm_yp, &h->dm_vb, &h->dm_v2, &h->dm_yp2})
+    BG_CUDA(b->ensure(m));
   BG_CUDA(h->dm_M.ensure(m * d));
   BG_CUDA(h->a_mu.ensure(n > 0 ? n : 1));
   const int C = (n + 31) / 32, CB = (nb + 31) / 32;
@@ -2828,6 +2835,8 @@ int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_opti
   a.ut = h->a_ut.p;
   a.g = h->dm_g.p;
   a.y_prev = h->dm_yp.p;
+  a.v_spare = h->dm_v2.p;
+  a.yp_spare = h->dm_yp2.p;
   a.r_best = h->dm_rb.p;
   a.v_best = h->dm_vb.p;
   a.csum = h->csum.p;
@@ -2872,13 +2881,15 @@ int bogus_gpu_solve_dual_ama(bogus_gpu_problem* h, const bogus_gpu_dual_ama_opti
     // per iteration: Q1 reads M, f, v, H^T r per body and writes x; reads w, H and v of the bodies, r, mu and
     // the scaling and writes u per contact; Q2 reads u, mu, H and (H^T r, x) of the bodies, writes g; per
     // line-search trial Q3 reads r, g, mu and writes r_s, Q4 reads the incidences, H rows and r_s per
-    // incidence, x, v, y_prev, f and M per body and writes H^T r_s; Q5 reads H^T r, x, v, y_prev and writes
-    // v, y_prev
+    // incidence, x, v, y_prev, f and M per body and writes H^T r_s and the candidate v, y_prev; without a line
+    // search Q5 reads the incidences, H rows and r per incidence, x, v, y_prev and writes H^T r, v, y_prev
     const double inc = (double)h->admm_ninc, dd = (double)d, nn = (double)n, bb = (double)nb;
+    const bool ls = o->ls_iters != 0;
     const double q1 = bb * (8.0 * dd * dd + 32.0 * dd) + inc * (24.0 * dd + 8.0 * dd) + nn * (24.0 * 3 + 16.0);
     const double q2 = inc * (24.0 * dd + 16.0 * dd) + nn * (24.0 + 8.0 + 24.0);
-    const double q34 = nn * (24.0 * 3 + 8.0) + inc * (4.0 + 24.0 * dd + 24.0) + bb * (8.0 * dd * dd + 48.0 * dd);
-    const double q5 = bb * 48.0 * dd;
+    const double q34 =
+        nn * (24.0 * 3 + 8.0) + inc * (4.0 + 24.0 * dd + 24.0) + bb * (8.0 * dd * dd + 48.0 * dd + 16.0 * dd);
+    const double q5 = ls ? 0.0 : inc * (4.0 + 24.0 * dd + 24.0) + bb * 48.0 * dd;
     h->last_stats.iterations = out.iters;
     h->last_stats.refine_iterations = 0;
     h->last_stats.fp32_device_ms = 0.0;

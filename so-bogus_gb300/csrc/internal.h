@@ -266,6 +266,7 @@ struct DamaArgs {
   const double* mu;       // n
   const double* scaling;  // n
   double *v, *r, *rs, *x, *HrBp, *ut, *g, *y_prev, *r_best, *v_best;
+  double *v_spare, *yp_spare;  // nbodies x d each: the line search's candidate v and y_prev
   double* csum;           // 3 x max(contact chunks, body chunks)
   double* scal;
   unsigned* combine_count;  // grid_barrier_combine's counter; zero at launch

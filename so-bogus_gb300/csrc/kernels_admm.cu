@@ -404,6 +404,8 @@ __global__ void __launch_bounds__(256) k_admm_persistent(ADMMArgs a) {
 //     Q4 bodies           H^T r_s, y = v + gamma (H^T r_s - x) over-relaxed, |(H^T r_s - f) - M y|^2 .. reduce
 //   (no line search: Q3 writes r = P(r - lambda g), Q5 forms H^T r)
 //   Q5 bodies             z = H^T r - x, y = v + gamma z, v = y + beta (y - y_prev) ..................... barrier
+//                         (with a line search Q4 already forms these for its trial: the last trial's become
+//                         the current v and y_prev by a pointer swap, and Q5 and its barrier are skipped)
 // Orders: M v chains over the dofs from 0 and is added to f (subtracted from H^T r - f); H^T r per dof over the
 // body's contacts in increasing order, rows inner; H z and H v as the ADMM kernel's products; dof norms each body's
 // dofs left to right, then the canonical sum over bodies.
@@ -488,6 +490,11 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
 
   double* r = a.r;
   double* rs = a.rs;
+  // v and y_prev, and the line search's candidates for them (swapped in when a trial ends the search)
+  double* vc = a.v;
+  double* ypc = a.y_prev;
+  double* vn = a.v_spare;
+  double* ypn = a.yp_spare;
   // H^T r once
   for (int c = next(); c < CB; c = next()) {
     const int b = 32 * c + lane;
@@ -512,7 +519,7 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
         double ev = 0.0;
         if (i < a.n) {
           double u[3];
-          contact_H(i, a.w, a.v, u);
+          contact_H(i, a.w, vc, u);
           a.ut[3 * i] = u[0];
           a.ut[3 * i + 1] = u[1];
           a.ut[3 * i + 2] = u[2];
@@ -530,7 +537,7 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
         double vb[DM];
 #pragma unroll
         for (int q = 0; q < DM; ++q)
-          if (q < d) vb[q] = ldcg(a.v + (size_t)b * d + q);
+          if (q < d) vb[q] = ldcg(vc + (size_t)b * d + q);
 #pragma unroll
         for (int q = 0; q < DM; ++q)
           if (q < d) {
@@ -572,7 +579,7 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
       if (t >= C) {
         const int b = 32 * (t - C) + lane;
         if (b < a.nbodies)
-          for (int q = 0; q < d; ++q) a.v_best[(size_t)b * d + q] = ldcg(a.v + (size_t)b * d + q);
+          for (int q = 0; q < d; ++q) a.v_best[(size_t)b * d + q] = ldcg(vc + (size_t)b * d + q);
         continue;
       }
       const int c = t;
@@ -651,8 +658,11 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
               if (q < d) {
                 a.HrBp[(size_t)b * d + q] = hr[q];
                 const double zq = hr[q] - ldcg(a.x + (size_t)b * d + q);
-                const double yk = ldcg(a.v + (size_t)b * d + q) + a.gamma * zq;
-                y[q] = yk + beta * (yk - ldcg(a.y_prev + (size_t)b * d + q));
+                const double yk = ldcg(vc + (size_t)b * d + q) + a.gamma * zq;
+                y[q] = yk + beta * (yk - ldcg(ypc + (size_t)b * d + q));
+                // the velocity update of this trial (Q5's values, should the trial be the last)
+                vn[(size_t)b * d + q] = y[q];
+                ypn[(size_t)b * d + q] = yk;
               }
 #pragma unroll
             for (int q = 0; q < DM; ++q)
@@ -671,33 +681,37 @@ __device__ void dama_body(const DamaArgs& a, double* smem8) {
       double* t = r;  // r = r_s
       r = rs;
       rs = t;
+      // Q5 with a line search: its v = yk + beta (yk - y_prev) and y_prev = yk are the last trial's, already
+      // formed by Q4 with the same operations; they become the current ones
+      t = vc;
+      vc = vn;
+      vn = t;
+      t = ypc;
+      ypc = ypn;
+      ypn = t;
     }
-    // Q5
-    for (int c = next(); c < CB; c = next()) {
-      const int b = 32 * c + lane;
-      if (b < a.nbodies) {
-        double hr[DM];
-        if (a.ls_iters == 0) {
+    // Q5 (no line search): z = H^T r - x, y = v + gamma z, v = y + beta (y - y_prev)
+    if (a.ls_iters == 0) {
+      for (int c = next(); c < CB; c = next()) {
+        const int b = 32 * c + lane;
+        if (b < a.nbodies) {
+          double hr[DM];
           body_HT(b, r, hr);
-        } else {
 #pragma unroll
           for (int q = 0; q < DM; ++q)
-            if (q < d) hr[q] = ldcg(a.HrBp + (size_t)b * d + q);
+            if (q < d) {
+              a.HrBp[(size_t)b * d + q] = hr[q];
+              const double zq = hr[q] - ldcg(a.x + (size_t)b * d + q);
+              const double yk = ldcg(vc + (size_t)b * d + q) + a.gamma * zq;
+              const double yp = ldcg(ypc + (size_t)b * d + q);
+              vc[(size_t)b * d + q] = yk + beta * (yk - yp);
+              ypc[(size_t)b * d + q] = yk;
+            }
         }
-#pragma unroll
-        for (int q = 0; q < DM; ++q)
-          if (q < d) {
-            a.HrBp[(size_t)b * d + q] = hr[q];
-            const double zq = hr[q] - ldcg(a.x + (size_t)b * d + q);
-            const double yk = ldcg(a.v + (size_t)b * d + q) + a.gamma * zq;
-            const double yp = ldcg(a.y_prev + (size_t)b * d + q);
-            a.v[(size_t)b * d + q] = yk + beta * (yk - yp);
-            a.y_prev[(size_t)b * d + q] = yk;
-          }
       }
     }
     res_prev = res;
-    if (!sync()) return;
+    if (a.ls_iters == 0 && !sync()) return;
   }
   if (writer) {
     a.out->min_res = min_res;

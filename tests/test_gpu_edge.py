@@ -142,3 +142,42 @@ def test_frames_rotate_w(bg, oracle):
             outs.append((res, v, rr_))
         assert outs[0][0] == outs[1][0] and np.array_equal(outs[0][2], outs[1][2])
         assert np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_destroyed_handles_return_their_device_memory(bg):
+    """Handles that ran every solver family (projected gradient, Gauss-Seidel, ADMM, DualAMA, the matrix-free
+    Gauss-Seidel, the adjoint) give all their device arrays back when destroyed: the free device memory after
+    a few create / solve / destroy rounds is what it was after the first round."""
+    import gc
+
+    import torch
+    from bogus_gpu import generator
+
+    d = generator.make("c1")
+    mass = np.linalg.inv(d.minv)
+
+    def one_round():
+        P = bg.PrimalFrictionProblem(d.minv, d.objA, d.objB, d.HA, d.HB, d.b, d.mu, M=mass,
+                                     f=np.zeros(6 * d.nbodies))
+        D = bg.DualFrictionProblem()
+        D.computeFrom(P)
+        r = np.zeros(3 * d.n)
+        pg = bg.ProjectedGradient()
+        pg.setTol(1e-10)
+        D.solveWith(pg, r, staticProblem=True)
+        D.solveWith(bg.GaussSeidel(), np.zeros(3 * d.n))
+        D.adjoint(r, np.ones(3 * d.n), tol=1e-8)
+        v = np.zeros(6 * d.nbodies)
+        P.solveWith(bg.ADMM(), 0.0, v, np.zeros(3 * d.n))
+        P.solveWith(bg.DualAMA(), np.zeros(6 * d.nbodies), np.zeros(3 * d.n))
+        P.solveWith(bg.ProductGaussSeidel(), np.zeros(3 * d.n))
+        del D, P
+        gc.collect()
+        torch.cuda.synchronize()
+
+    one_round()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        one_round()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 >= free0 - (2 << 20), (free0, free1)
