@@ -185,7 +185,9 @@ int bogus_gpu_eval(bogus_gpu_problem* h, const double* r, int static_problem, in
                    double* residual);
 
 /* DualFrictionProblem::solveWith(ProjectedGradient&, r, staticProblem) (Interfaces/FrictionProblem.cpp:49-54,
- * ProjectedGradient.impl.hpp:74-382). r: host array, in/out. iters may be NULL. Variants APGD, Descent, SPG. */
+ * ProjectedGradient.impl.hpp:74-382). r: host array, in/out. iters may be NULL. All five variants; Standard
+ * and Conjugated (Armijo line search) in FP64 single-problem solves only: the FP32-refined, batched and
+ * allocation-free forms return BAD_INPUT for them. */
 int bogus_gpu_solve_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* opts, double* r, double* residual,
                        unsigned* iters);
 

@@ -428,8 +428,8 @@ int ensure_pg_work(bogus_gpu_problem* h, unsigned max_iters) {
   BG_CUDA(h->S0.ensure(n));
   BG_CUDA(h->XB.ensure(n3));
   BG_CUDA(h->Wv.ensure(n3));
-  BG_CUDA(h->csum.ensure(4 * (size_t)C));
-  BG_CUDA(h->scal.ensure(8 + 32));  // scalars, then the stripe sums of grid_barrier_combine
+  BG_CUDA(h->csum.ensure(5 * (size_t)C));  // up to 5 reduced quantities (the Conjugated variant)
+  BG_CUDA(h->scal.ensure(8 + 40));         // scalars, then the stripe sums of grid_barrier_combine
   BG_CUDA(h->trace.ensure((size_t)max_iters + 1));
   BG_CUDA(h->pgout.ensure(1));
   BG_CUDA(h->barrier.ensure(16));  // [0..7] barrier words, [8..13] three 64-bit monotonic counters
@@ -512,6 +512,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.max_iters = o->max_iters;
   a.ls_iters = o->ls_iters;
   a.lin_momentum = lin_momentum(o);
+  a.armijo = o->ls_armijo_coefficient;
   a.phantom_ctas = h->test_wait_timeout ? 1u : 0u;
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 16 * sizeof(unsigned), h->stream));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
@@ -654,6 +655,7 @@ void fill_args(PGArgsT<T>& a, const bogus_gpu_pg_options* o) {
   a.max_iters = o->max_iters;
   a.ls_iters = o->ls_iters;
   a.lin_momentum = lin_momentum(o);
+  a.armijo = o->ls_armijo_coefficient;
 }
 
 // Mixed precision: FP32 solve from X[0] (double), its best iterate back into X[0], then the FP64 solve from
@@ -744,8 +746,11 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
 
 int check_pg_options(const bogus_gpu_pg_options* o) {
   if (!o) return fail(BOGUS_GPU_BAD_INPUT, "null options");
-  if (o->variant != BOGUS_GPU_PG_APGD && o->variant != BOGUS_GPU_PG_DESCENT && o->variant != BOGUS_GPU_PG_SPG)
-    return fail(BOGUS_GPU_BAD_INPUT, "projected-gradient variant not available on the GPU (APGD, Descent, SPG)");
+  if (o->variant < BOGUS_GPU_PG_STANDARD || o->variant > BOGUS_GPU_PG_SPG)
+    return fail(BOGUS_GPU_BAD_INPUT, "unknown projected-gradient variant");
+  const bool std_conj = o->variant == BOGUS_GPU_PG_STANDARD || o->variant == BOGUS_GPU_PG_CONJUGATED;
+  if (std_conj && o->mixed_precision)
+    return fail(BOGUS_GPU_BAD_INPUT, "the Standard and Conjugated variants run in FP64 only");
   if (o->ls_iters == 0 && o->variant != BOGUS_GPU_PG_SPG)
     return fail(BOGUS_GPU_BAD_INPUT, "ls_iters must be >= 1 (the reference reuses an undefined step otherwise)");
   if (!(o->tol >= 0) || !(o->ls_optimistic_factor > 0) || !(o->ls_pessimistic_factor > 0))
@@ -3390,6 +3395,8 @@ int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
 int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
   if (int e = check_handle(h)) return e;
   if (int e = check_pg_options(o)) return e;
+  if (o->variant == BOGUS_GPU_PG_STANDARD || o->variant == BOGUS_GPU_PG_CONJUGATED)
+    return fail(BOGUS_GPU_BAD_INPUT, "batched solves run APGD, Descent or SPG");
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
   if (h->nproblems == 0 && h->W.n > 0) return fail(BOGUS_GPU_NO_PROBLEM, "no batch partition set (bogus_gpu_set_batch)");
 

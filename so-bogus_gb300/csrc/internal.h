@@ -76,6 +76,7 @@ struct PGArgsT {
   int desaxce, variant, use_inf;
   int lin_momentum;  // APGD's momentum product by linearity (needs MX2, MX3)
   double tol, opt, pess;
+  double armijo;     // the Armijo coefficient of the Standard and Conjugated variants' line search
   unsigned max_iters, ls_iters;
   // test of the timeout path (single-problem kernel): the barriers count this many CTAs more than the launch
   // has, so the first one never completes and its bounded wait runs out; 0 in every solve

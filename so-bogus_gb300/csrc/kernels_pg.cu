@@ -95,7 +95,9 @@ struct BlocksOf<T, true> {
 
 // IL: read W through its interleaved copy (single-problem solves) or the plain BSR arrays (batched and
 // allocation-free solves). The arithmetic is the same.
-template <class T, bool IL, class Ctx>
+// SC: the Standard and Conjugated variants (their own kernel instantiation, so that their code does not change the
+// register allocation of the APGD / Descent / SPG kernels).
+template <class T, bool IL, bool SC = false, class Ctx>
 __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
   using Ops = SocOps<T>;
   const Bufs<T> B{a};
@@ -244,6 +246,196 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
   double min_res = -1.0, theta = 1.0;
   bool best_pending = false;
   unsigned it = 0;
+
+  if constexpr (SC) {
+    // ------------------------------------------------ Standard (:157-209) and Conjugated (:211-286)
+    // Single-problem solves only (the host rejects them elsewhere): the Conjugated variant's first reduction
+    // has 5 quantities. x = X(ix), the line search's trial point X(ixs) (the two swap when a search ends),
+    // Mx = MX(imx), its product MX(1 - imx). Standard: pg = X(2), W pg = MX(2). Conjugated: prev_pg = X(2),
+    // prev_dir = MX(2) (formed in A as (x - x_old) / alpha of the last search, x_old still in X(ixs)),
+    // dir = X(4).
+    const bool conj = a.variant == 2;
+    double alpha_s = 1.0, alpha_prev = 1.0, prev_n2 = 0.0;
+    bool have_prev = false;
+    for (;;) {
+      // A: y = Mx + b, the residual, s = COV(y), y += s, J; xs = P(x - y), pg = x - xs (:164-176, :218-231)
+      ph[2]++;
+      for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
+        const int i = 32 * c + lane;
+        double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        if (i < a.n) {
+          T x[3], Mx[3], bb[3];
+          load3cg(B.X(ix), i, x);
+          load3cg(B.MX(imx), i, Mx);
+          bb[0] = __ldg(a.b + 3 * i);
+          bb[1] = __ldg(a.b + 3 * i + 1);
+          bb[2] = __ldg(a.b + 3 * i + 2);
+          const T mu = __ldg(a.mu + i), sc = __ldg(a.scaling + i);
+          T y[3] = {Mx[0] + bb[0], Mx[1] + bb[1], Mx[2] + bb[2]};
+          const T lx[3] = {x[0] * sc, x[1] * sc, x[2] * sc};
+          v[0] = Ops::law_eval(desaxce, mu, lx, y);
+          const T s0 = Ops::cov(desaxce, mu, y);
+          y[0] = y[0] + s0;
+          y[1] = Ops::plus0(y[1]);
+          y[2] = Ops::plus0(y[2]);
+          const T t[3] = {(Ops::half(Mx[0]) + bb[0]) + s0, Ops::plus0(Ops::half(Mx[1]) + bb[1]),
+                          Ops::plus0(Ops::half(Mx[2]) + bb[2])};
+          v[1] = Ops::dot3(x, t);
+          T xs[3] = {x[0] - y[0], x[1] - y[1], x[2] - y[2]};
+          Ops::project(mu, xs);
+          const T pg[3] = {x[0] - xs[0], x[1] - xs[1], x[2] - xs[2]};
+          store3(a.Y, i, y);
+          a.S0[i] = s0;
+          if (!conj) {
+            v[2] = Ops::dot3(y, pg);
+          } else {
+            v[2] = Ops::sq3(pg);
+            if (have_prev) {
+              T xo[3], ppg[3];
+              load3cg(B.X(ixs), i, xo);
+              load3cg(B.X(2), i, ppg);
+              const T pd[3] = {(x[0] - xo[0]) / T(alpha_prev), (x[1] - xo[1]) / T(alpha_prev),
+                               (x[2] - xo[2]) / T(alpha_prev)};
+              store3(B.MX(2), i, pd);
+              const T dg[3] = {pg[0] - ppg[0], pg[1] - ppg[1], pg[2] - ppg[2]};
+              v[3] = Ops::dot3(pd, dg);
+              v[4] = Ops::dot3(pg, ppg);
+            }
+          }
+          store3(B.X(2), i, pg);
+        }
+        put(0, c, v[0], res_mask != 0);
+        put(1, c, v[1], false);
+        put(2, c, v[2], false);
+        if (conj) {
+          put(3, c, v[3], false);
+          put(4, c, v[4], false);
+        }
+      }
+      if (!sync_reduce(conj ? 5 : 3, res_mask)) return -1;
+      const double res = residual_of(scal(0)), J = scal(1), s2 = scal(2);
+      const double den_c = conj ? scal(3) : 0.0, xp = conj ? scal(4) : 0.0;
+      if (a.trace && ctx.writer()) a.trace[it] = res;
+      if (it == 0 || res < min_res) {
+        min_res = res;
+        best_pending = true;
+      }
+      if (res < a.tol) return finish(min_res, it, ix, 1);
+      // the step direction
+      double beta = 0.0;
+      bool neg_y = false;
+      if (!conj) {
+        // Mpg = W pg, pg.Mpg (:177-181); pg *= beta with beta = -y.pg / pg.Mpg
+        ph[3]++;
+        for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
+          const int i = 32 * c + lane;
+          double v0 = 0.0;
+          T acc[3] = {T(0), T(0), T(0)};
+          product(c, B.X(2), acc);
+          if (i < a.n) {
+            T pg[3];
+            load3cg(B.X(2), i, pg);
+            store3(B.MX(2), i, acc);
+            v0 = Ops::dot3(pg, acc);
+          }
+          put(0, c, v0, false);
+        }
+        if (!sync_reduce(1, 0u)) return -1;
+        beta = -s2 / scal(0);
+      } else if (prev_n2 == 0.) {
+        neg_y = true;  // dir = -y (:232-233)
+      } else {
+        // dir = beta prev_dir - y, with dir = -y when it is not a descent direction (:235-245)
+        beta = (den_c < 1.e-12) ? dmax(0., (s2 - xp)) / prev_n2 : dmax(0., (s2 - xp)) / den_c;
+        const T bc = T(beta);
+        ph[7]++;
+        for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
+          const int i = 32 * c + lane;
+          double v0 = 0.0;
+          if (i < a.n) {
+            T pd[3], y[3];
+            load3cg(B.MX(2), i, pd);
+            load3cg(a.Y, i, y);
+            const T dir[3] = {bc * pd[0] - y[0], bc * pd[1] - y[1], bc * pd[2] - y[2]};
+            store3(B.X(4), i, dir);
+            v0 = Ops::dot3(dir, y);
+          }
+          put(0, c, v0, false);
+        }
+        if (!sync_reduce(1, 0u)) return -1;
+        neg_y = scal(0) >= 0.;
+      }
+      if (conj) prev_n2 = s2;
+      // Armijo line search (:93-107 of the same file's line-search helper): xs = P(x + alpha dir), W xs,
+      // Js = xs.((W xs / 2 + (b + s)) + 0) against J + armijo (y.(xs - x))
+      alpha_s = conj ? alpha_s * a.opt : dmin(1., alpha_s * a.opt);
+      const T bt = T(beta);
+      for (unsigned ls = 0; ls < a.ls_iters; ++ls) {
+        const T al = T(alpha_s);
+        ph[4]++;
+        for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
+          const int i = 32 * c + lane;
+          if (i < a.n) {
+            T x[3], d[3];
+            load3cg(B.X(ix), i, x);
+            if (!conj) {
+              T pg[3];
+              load3cg(B.X(2), i, pg);
+              d[0] = pg[0] * bt; d[1] = pg[1] * bt; d[2] = pg[2] * bt;
+            } else if (neg_y) {
+              T y[3];
+              load3cg(a.Y, i, y);
+              d[0] = -y[0]; d[1] = -y[1]; d[2] = -y[2];
+            } else {
+              load3cg(B.X(4), i, d);
+            }
+            T xs[3] = {fma(al, d[0], x[0]), fma(al, d[1], x[1]), fma(al, d[2], x[2])};
+            Ops::project(__ldg(a.mu + i), xs);
+            store3(B.X(ixs), i, xs);
+            if (best_pending) store3(a.XB, i, x);
+          }
+        }
+        best_pending = false;
+        if (!sync()) return -1;
+        ph[3]++;
+        for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
+          const int i = 32 * c + lane;
+          double v0 = 0.0, v1 = 0.0;
+          T acc[3] = {T(0), T(0), T(0)};
+          product(c, B.X(ixs), acc);
+          if (i < a.n) {
+            store3(B.MX(1 - imx), i, acc);
+            T x[3], xs[3], y[3];
+            load3cg(B.X(ix), i, x);
+            load3cg(B.X(ixs), i, xs);
+            load3cg(a.Y, i, y);
+            const T s0 = ldcg(a.S0 + i);
+            const T bs[3] = {__ldg(a.b + 3 * i) + s0, Ops::plus0(__ldg(a.b + 3 * i + 1)),
+                             Ops::plus0(__ldg(a.b + 3 * i + 2))};
+            const T t[3] = {Ops::plus0(Ops::half(acc[0]) + bs[0]), Ops::plus0(Ops::half(acc[1]) + bs[1]),
+                            Ops::plus0(Ops::half(acc[2]) + bs[2])};
+            v0 = Ops::dot3(xs, t);
+            const T dd[3] = {xs[0] - x[0], xs[1] - x[1], xs[2] - x[2]};
+            v1 = Ops::dot3(y, dd);
+          }
+          put2(c, v0, v1, false);
+        }
+        if (!sync_reduce(2, 0u)) return -1;
+        if (scal(0) < J + a.armijo * scal(1)) break;
+        alpha_s *= a.pess;
+      }
+      // x = xs, Mx = W xs
+      const int t2 = ix;
+      ix = ixs;
+      ixs = t2;
+      imx = 1 - imx;
+      alpha_prev = alpha_s;
+      have_prev = true;
+      ++it;
+      if (it >= a.max_iters) break;
+    }
+    return finish(min_res, it, 3, 0);
+  }
 
   if (!spg) {
     // ---------------------------------------------------------------- APGD / Descent
@@ -546,7 +738,7 @@ struct GridCtx {
 };
 
 // Occupancy target: 3 resident CTAs per SM (see pg_max_grid).
-template <class T, bool IL>
+template <class T, bool IL, bool SC = false>
 __global__ void __launch_bounds__(256, 3) k_pg_persistent(PGArgsT<T> a) {
   __shared__ double smem8[32];
   __shared__ ChunkScratchT<T> cs[8];
@@ -554,7 +746,7 @@ __global__ void __launch_bounds__(256, 3) k_pg_persistent(PGArgsT<T> a) {
   if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0u;
   __syncthreads();
   GridCtx<T> ctx{a, smem8, cs, s_cnt};
-  pg_body<T, IL>(a, ctx);
+  pg_body<T, IL, SC>(a, ctx);
 }
 
 // One problem per CTA (batched solves): phases separated by __syncthreads, scalars reduced by the CTA's
@@ -796,7 +988,10 @@ int pg_batched_grid(int device, bool fp32) {
 cudaError_t launch_pg_persistent(const PGArgs& a, int grid, cudaStream_t s) {
   PGArgs copy = a;
   void* args[] = {&copy};
-  const void* fn = a.slot0 ? (const void*)k_pg_persistent<double, true> : (const void*)k_pg_persistent<double, false>;
+  const bool sc = a.variant == 0 || a.variant == 2;  // Standard, Conjugated
+  if (sc && !a.slot0) return cudaErrorInvalidValue;  // they run on the interleaved copy only
+  const void* fn = sc ? (const void*)k_pg_persistent<double, true, true>
+                      : (a.slot0 ? (const void*)k_pg_persistent<double, true> : (const void*)k_pg_persistent<double, false>);
   return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s);
 }
 

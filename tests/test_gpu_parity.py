@@ -81,7 +81,7 @@ def test_eval_bitwise(bg, oracle, c1, inf_norm):
         assert D.evalWith(pg, r, staticProblem=static) == O.eval(r, coulomb=not static, inf_norm=inf_norm)
 
 
-@pytest.mark.parametrize("variant", [3, 1, 4])  # APGD, Descent, SPG
+@pytest.mark.parametrize("variant", [3, 1, 4, 0, 2])  # APGD, Descent, SPG, Standard, Conjugated
 @pytest.mark.parametrize("static", [True, False])
 def test_projected_gradient_bitwise(bg, oracle, c1, variant, static):
     d, rp, cl, vl = c1
@@ -402,6 +402,49 @@ def test_full_size_apgd(bg, oracle, c2):
         assert trace == tr.items
         # the returned residual is the error function at the returned iterate
         assert res == O.eval(r, coulomb=not static)
+
+
+@pytest.mark.parametrize("variant", [0, 2])  # Standard, Conjugated
+def test_full_size_standard_and_conjugated(bg, oracle, c2, variant):
+    """The projected-gradient variants with an Armijo line search, 40 iterations on 200 000 contacts (Coulomb
+    law): iterate, residual, iteration count and trace bit-identical to the oracle's."""
+    d, D = c2
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    O = oracle.DualProblem(*P.assemble(), d.b, d.mu)
+    pg = bg.ProjectedGradient()
+    pg.setDefaultVariant(variant)
+    pg.setMaxIters(40)
+    trace = []
+    pg.callback().connect(lambda it, res: trace.append((it, res)))
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r, staticProblem=False)
+    tr = oracle.Trace()
+    res_o, r_o, it_o = O.solve_pg(np.zeros(3 * d.n), variant=variant, coulomb=True, max_iters=40, trace=tr)
+    assert res == res_o and D.last_iterations == it_o
+    assert np.array_equal(r, r_o)
+    assert trace == tr.items
+
+
+def test_standard_and_conjugated_rejected_where_not_built(bg, c1):
+    """Standard and Conjugated run in FP64 single-problem solves: the FP32-refined and batched forms refuse them."""
+    from bogus_gpu import generator
+
+    d, rp, cl, vl = c1
+    D = _gpu_dual(bg, rp, cl, vl, d.b, d.mu)
+    for variant in (0, 2):
+        pg = bg.ProjectedGradient()
+        pg.setDefaultVariant(variant)
+        pg.setMixedPrecision(True, 10)
+        with pytest.raises(bg.BogusGpuError):
+            D.solveWith(pg, np.zeros(3 * d.n))
+    db, cptr = generator.batch(nproblems=3, nmin=16, nmax=40, seed=3)
+    B = bg.DualFrictionProblem()
+    B.computeFrom(bg.PrimalFrictionProblem.from_generated(db))
+    B.setBatch(cptr)
+    pg = bg.ProjectedGradient()
+    pg.setDefaultVariant(2)
+    with pytest.raises(bg.BogusGpuError):
+        B.solveBatchWith(pg, np.zeros(3 * db.n))
 
 
 def test_full_size_mixed_precision(bg, oracle, c2):

@@ -1,8 +1,8 @@
 """Ragged sizes against the oracle, bit for bit: problems of 1, 2, 31, 32, 33 and 65 contacts (a partial chunk, a
 full one, one past it, two and one past), on few bodies so that W rows are long (up to every contact coupled:
 segments of many blocks per lane) and on many bodies (short rows). Every solver family that runs over 32-contact
-chunks: the product, the error function, APGD / SPG (with and without the momentum product by linearity),
-Gauss-Seidel (natural and colored), and primal ADMM.
+chunks: the product, the error function, APGD / SPG / Standard / Conjugated (APGD also with the momentum
+product by linearity), Gauss-Seidel (natural and colored), and primal ADMM.
 """
 import numpy as np
 import pytest
@@ -42,7 +42,7 @@ def test_ragged_product_eval_pg(bg, oracle, n, dense):
     for static in (True, False):
         pg = bg.ProjectedGradient()
         assert D.evalWith(pg, x, staticProblem=static) == O.eval(x, coulomb=not static)
-    for variant, lin in ((3, False), (3, True), (4, False)):
+    for variant, lin in ((3, False), (3, True), (4, False), (0, False), (2, False)):
         pg = bg.ProjectedGradient()
         pg.setDefaultVariant(variant)
         pg.setTol(1e-10)
