@@ -530,6 +530,14 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
     solve(pgl)
     lin_ms, (res_l, its_l) = _sync_time(lambda: solve(pgl), world)
     st_l = D.solve_stats()
+    # both: the FP32-refined batch with the momentum product by linearity on its FP64 iterations
+    pgml = bogus_gpu.ProjectedGradient()
+    pgml.setTol(TOL)
+    pgml.setMaxIters(200)
+    pgml.setMixedPrecision(True, BATCH_MAX_ITERS - 200)
+    pgml.setMomentumByLinearity(True)
+    solve(pgml)
+    ml_ms, (res_ml, its_ml) = _sync_time(lambda: solve(pgml), world)
     # the launch shape chosen by the tuner (measured on this batch) against the default rule, same results
     rule_shape = D.batchShape()
     D.setBatchTuning(True)
@@ -566,7 +574,7 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
                "capture_call_ms": graph[0], "identical_results": graph_same,
                "note": "host-buffer calls (pinned r), wall time per call including copies; the first graph call "
                        "captures"}
-    allres = shard.gather_results(mine, np.stack([res, its, res_m, res_l], 1), nprob, world)
+    allres = shard.gather_results(mine, np.stack([res, its, res_m, res_l, res_ml], 1), nprob, world)
     out = {"problems": nprob, "contacts": int(d.n), "ranks": world, "max_iters": BATCH_MAX_ITERS,
            "batched_ms": statistics.median(times), "kernel_ms": statistics.median(kernel),
            "tuned": tuned, "cuda_graph": graphed,
@@ -575,6 +583,9 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
                             "kernel_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"]},
            "momentum_by_linearity": {"batched_ms": lin_ms, "kernel_ms": st_l["device_ms"],
                                      "w_passes": st_l["w_passes"], "w_passes_reference_form": st["w_passes"]},
+           "fp32_refined_momentum_by_linearity": {"split": "up to 200 FP32 + 300 FP64 iterations per problem, the "
+                                                           "FP64 ones with the momentum product by linearity",
+                                                  "batched_ms": ml_ms},
            "timing": f"median of {steps} solves after a warm-up, wall time between device synchronisations"}
     if world > 1:
         out["partition"] = {"rule": "greedy bin-pack on W blocks", "blocks_per_rank": [int(costs[q].sum()) for q in parts],
@@ -588,6 +599,8 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
     out["fp32_refined"]["speedup_vs_fp64_batch"] = out["batched_ms"] / mixed_ms
     out["momentum_by_linearity"]["converged_fraction"] = float(np.mean(allres[:, 3] < TOL))
     out["momentum_by_linearity"]["speedup_vs_fp64_batch"] = out["batched_ms"] / lin_ms
+    out["fp32_refined_momentum_by_linearity"]["converged_fraction"] = float(np.mean(allres[:, 4] < TOL))
+    out["fp32_refined_momentum_by_linearity"]["speedup_vs_fp64_batch"] = out["batched_ms"] / ml_ms
     if world == 1 and sample_stride:
         # the single-problem path, problem by problem (inputs set beforehand, each solve timed with its r copies)
         sys.path.insert(0, os.path.join(REPO, "oracle"))
