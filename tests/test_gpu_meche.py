@@ -68,6 +68,8 @@ def assert_same(g, o):
 @pytest.mark.parametrize("algorithm, extra", [
     (0, {}),                                    # Gauss-Seidel, Coulomb
     (1, {"pg_variant": 3}),                     # projected gradient (APGD)
+    (1, {"pg_variant": 0}),                     # projected gradient (Standard)
+    (1, {"pg_variant": 2, "cadoux_iters": 5}),  # projected gradient (Conjugated) + Cadoux
     (1, {"cadoux_iters": 8}),                   # projected gradient (SPG, the facade's default) + Cadoux
     (0, {"cadoux_iters": 5}),                   # Gauss-Seidel + Cadoux
     (2, {}),                                    # matrix-free Gauss-Seidel
