@@ -40,7 +40,8 @@ TOL = 1e-6
 MAX_ITERS = 20_000        # budget of the time-to-residual solve; APGD reaches 1e-6 well before it here
 CAP_500 = 500             # the iteration budget of the configuration's wording, reported beside the headline
 CPU_SAMPLE_ITERS = 1000   # the oracle's bounded sample: the first 1000 iterations of the same solve
-FP32_ITERS = 2000         # FP32-refined: at most this many FP32 iterations, then FP64 ones to the tolerance
+FP32_ITERS = 20000        # FP32-refined: FP32 iterations until the stall test ends them (at most this many),
+                          # then FP64 ones to the tolerance
 MAX_ADJ_FWD_ITERS = 20000
 METRIC = "time-to-residual 1e-6 (ms), FP64 APGD, 200k contacts"
 WORKLOAD = "fp64_apgd_200k_contacts_to_1e-6"
@@ -373,7 +374,8 @@ def measure_secondary(args, D, d, r_fp64, fp64_ms):
     res, st, _ = best_of(pg)
     out["apgd_500_iterations"] = {"device_ms": st["device_ms"], "iterations": st["iterations"], "residual": res,
                                   "note": "the same solve stopped at 500 iterations (the configuration's budget)"}
-    # FP32-refined: up to FP32_ITERS FP32 iterations, then FP64 ones to the tolerance
+    # FP32-refined: FP32 iterations until FP32 rounding stops their progress (the library's stall test, default 4
+    # stagnant iterations in a row), then FP64 ones to the tolerance
     pgm = bogus_gpu.ProjectedGradient()
     pgm.setTol(TOL)
     pgm.setMaxIters(FP32_ITERS)
@@ -716,9 +718,9 @@ def run_gs(args) -> None:
 
 
 def run_mixed(args) -> None:
-    """FP32-refined APGD on the 200 000-contact problem, time to residual 1e-6 for several FP32 / FP64 splits (at
-    most m FP32 iterations, then FP64 ones to the tolerance), against the FP64 solve to 1e-6; with each result its
-    relative distance to the FP64 result."""
+    """FP32-refined APGD on the 200 000-contact problem, time to residual 1e-6 for several FP32 / FP64 splits (m
+    FP32 iterations, then FP64 ones to the tolerance) and with the stall test ending the FP32 part, against the
+    FP64 solve to 1e-6; with each result its relative distance to the FP64 result."""
     import bogus_gpu
 
     d = make_problem()
@@ -740,13 +742,15 @@ def run_mixed(args) -> None:
     pg64.setMaxIters(args.max_iters)
     res_p, st_p, r64 = timed(pg64)
     splits = {}
-    for m32 in (1000, 2000, 3000, 4000, 5000, 6000, 8000):
+    # fixed FP32 budgets (stall test off), then the stall test with a budget it does not reach
+    for m32, stall in ((1000, 0), (2000, 0), (3000, 0), (4000, 0), (6000, 0), (20000, 4)):
         pgm = bogus_gpu.ProjectedGradient()
         pgm.setTol(TOL)
         pgm.setMaxIters(m32)
         pgm.setMixedPrecision(True, args.max_iters)
+        pgm.setFp32StallIterations(stall)
         res_m, st_m, rm = timed(pgm)
-        splits[m32] = {"device_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"],
+        splits[f"{m32}" if stall == 0 else f"stall_test_{stall}"] = {"device_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"],
                        "fp32_iterations": st_m["iterations"] - st_m["refine_iterations"],
                        "fp64_iterations": st_m["refine_iterations"], "residual": res_m,
                        "reached_tol": bool(res_m < TOL), "speedup_vs_fp64": st_p["device_ms"] / st_m["device_ms"],

@@ -83,6 +83,12 @@ typedef struct bogus_gpu_pg_options {
                                      mixed_precision it applies to the FP64 iterations only (in FP32 the
                                      recombined product's rounding makes the line search retry more often); the
                                      allocation-free entry point rejects it */
+  unsigned fp32_stall_iters;      /* 4 (not in the reference; mixed_precision only): the FP32 part ends before
+                                     max_iters once FP32 rounding stops its progress, that is when its residual
+                                     has repeated bit for bit on this many consecutive iterations or (APGD,
+                                     Descent) its line search has run out of trials this many times in a row;
+                                     the FP64 iterations then start from the best FP32 iterate. 0: the FP32 part
+                                     runs to max_iters */
 } bogus_gpu_pg_options;
 
 /* GaussSeidel setters and defaults (Core/BlockSolvers/GaussSeidelBase.hpp:39-91) plus the coloring switch

@@ -269,6 +269,8 @@ class ProjectedGradient : public SolverBase {
   }
   // extension: APGD's momentum product by linearity (one pass over W fewer per momentum step)
   void setMomentumByLinearity(bool on) { lin_ = on; }
+  // extension: the FP32 part of the FP32-refined solve ends once FP32 rounding stops its progress (0: never)
+  void setFp32StallIterations(unsigned n) { stall_ = n; }
 
   bogus_gpu_pg_options options(bool static_problem) const {
     bogus_gpu_pg_options o;
@@ -285,11 +287,12 @@ class ProjectedGradient : public SolverBase {
     o.mixed_precision = mixed_ ? 1 : 0;
     o.refine_max_iters = refine_;
     o.momentum_by_linearity = lin_ ? 1 : 0;
+    o.fp32_stall_iters = stall_;
     return o;
   }
 
  private:
-  unsigned ls_iters_ = 8, refine_ = 50;
+  unsigned ls_iters_ = 8, refine_ = 50, stall_ = 4;
   double opt_ = 1.25, pess_ = 0.5, armijo_ = 0.5;
   int variant_ = BOGUS_GPU_PG_APGD;
   bool mixed_ = false, lin_ = false;

@@ -42,7 +42,7 @@ class PgOptions(C.Structure):
                 ("ls_optimistic_factor", C.c_double), ("ls_pessimistic_factor", C.c_double),
                 ("ls_armijo_coefficient", C.c_double), ("variant", C.c_int), ("use_infinity_norm", C.c_int),
                 ("static_problem", C.c_int), ("mixed_precision", C.c_int), ("refine_max_iters", C.c_uint),
-                ("momentum_by_linearity", C.c_int)]
+                ("momentum_by_linearity", C.c_int), ("fp32_stall_iters", C.c_uint)]
 
 
 class GsOptions(C.Structure):
@@ -261,6 +261,7 @@ class ProjectedGradient(_SolverBase):
         self._variant = APGD
         self._mixed, self._refine = False, 50
         self._lin = False
+        self._stall = 4
 
     def setMomentumByLinearity(self, on: bool = True) -> None:
         """APGD's momentum product formed by linearity, W x = W xs + beta (W xs - W prev), instead of the product
@@ -272,6 +273,12 @@ class ProjectedGradient(_SolverBase):
         """FP32-refined solve: FP32 W / iterates / per-contact law (FP64 reductions and decisions), then up to
         refine_max_iters FP64 iterations from the FP32 result. No counterpart in the reference."""
         self._mixed, self._refine = bool(on), int(refine_max_iters)
+
+    def setFp32StallIterations(self, n: int) -> None:
+        """FP32-refined solve: end the FP32 part once its residual has repeated bit for bit on n consecutive
+        iterations or its line search has run out of trials n times in a row (0: run it to max_iters). No
+        counterpart in the reference."""
+        self._stall = int(n)
 
     def setLineSearchIterations(self, n: int) -> None: self._ls = int(n)
     def setLineSearchOptimisticFactor(self, f: float) -> None: self._opt = float(f)
@@ -288,6 +295,7 @@ class ProjectedGradient(_SolverBase):
         o.variant, o.use_infinity_norm, o.static_problem = self._variant, int(self._inf), int(static_problem)
         o.mixed_precision, o.refine_max_iters = int(self._mixed), self._refine
         o.momentum_by_linearity = int(self._lin)
+        o.fp32_stall_iters = self._stall
         return o
 
 

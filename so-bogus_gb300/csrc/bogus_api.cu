@@ -703,6 +703,7 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   // momentum_by_linearity applies to the FP64 iterations only: in FP32 the recombined product's rounding makes
   // the line search retry more often (measured slower, with a worse starting point for the FP64 part)
   a.lin_momentum = 0;
+  a.stall_iters = o->fp32_stall_iters;
   BG_CUDA(launch_convert(n3, h->X.p, h->X32.p, s));
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 16 * sizeof(unsigned), s));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), s));
@@ -935,6 +936,7 @@ void bogus_gpu_pg_options_default(bogus_gpu_pg_options* o) {
   o->mixed_precision = 0;
   o->refine_max_iters = 50;
   o->momentum_by_linearity = 0;
+  o->fp32_stall_iters = 4;
 }
 
 void bogus_gpu_gs_options_default(bogus_gpu_gs_options* o) {
@@ -3476,6 +3478,7 @@ int run_pg_batch_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, doub
   a.pess = o->ls_pessimistic_factor;
   a.max_iters = o->max_iters;
   a.ls_iters = o->ls_iters;
+  a.stall_iters = o->fp32_stall_iters;
   ba.nproblems = np;
   ba.contact_ptr = h->contact_ptr.p;
   ba.chunk_ptr = h->chunk_ptr.p;

@@ -78,6 +78,9 @@ struct PGArgsT {
   double tol, opt, pess;
   double armijo;     // the Armijo coefficient of the Standard and Conjugated variants' line search
   unsigned max_iters, ls_iters;
+  // FP32 part of the FP32-refined solves (0 elsewhere): stop once the residual has repeated bit for bit on this
+  // many consecutive iterations, or the line search has run out of trials this many times in a row
+  unsigned stall_iters;
   // test of the timeout path (single-problem kernel): the barriers count this many CTAs more than the launch
   // has, so the first one never completes and its bounded wait runs out; 0 in every solve
   unsigned phantom_ctas;

@@ -451,10 +451,16 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     const bool lin = apgd && a.lin_momentum != 0;
     int imp = imx, ims = 1, imn = 2;
     double alpha_t = alpha * a.opt;
+    // stall test of the FP32 part (stall_iters > 0; compiled into the FP32 kernels only): consecutive iterations
+    // whose residual repeats the previous one bit for bit or whose line search ran out of trials
+    constexpr bool kStallTest = sizeof(T) == 4;
+    unsigned stall_run = 0;
+    bool exhausted = false;
+    double prev_res = 0.0;
     if (!runA(alpha_t, true)) return -1;
     for (;;) {
       double res = 0.0, J = 0.0;
-      bool top_done = false, converged = false;
+      bool top_done = false, converged = false, stalled = false;
       auto top = [&]() -> bool {
         if (top_done) return true;
         if (!ctx.await_scalars()) return false;
@@ -466,6 +472,11 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
           best_pending = true;
         }
         converged = res < a.tol;
+        if (kStallTest && a.stall_iters) {
+          stall_run = ((it > 0 && res == prev_res) || exhausted) ? stall_run + 1 : 0;
+          prev_res = res;
+          stalled = !converged && stall_run >= a.stall_iters;
+        }
         top_done = true;
         return true;
       };
@@ -485,7 +496,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
           T acc[3] = {T(0), T(0), T(0)};
           product(c, B.X(ixs), acc);
           if (!top()) return -1;
-          if (converged) break;
+          if (converged || (kStallTest && stalled)) break;
           if (i < a.n) {
             store3(B.MX(ims_t), i, acc);
             T x[3], xs[3], pv[3], y[3];
@@ -519,6 +530,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
         }
         if (!top()) return -1;
         if (converged) return finish(min_res, it, best_pending ? ix : 3, 1);
+        if (kStallTest && stalled) return finish(min_res, it, best_pending ? ix : 3, 0);
         ph[3]++;
         best_pending = false;
         if (!sync_reduce(4, 0u)) return -1;
@@ -544,6 +556,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
         }
         if (!sync()) return -1;
       }
+      if (kStallTest) exhausted = ls > 0 && ls >= a.ls_iters;
       ++it;
       const bool more = it < a.max_iters;
       if (apgd && decr2 < 0) {
@@ -596,6 +609,8 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
 
   // ------------------------------------------------------------------ SPG (:288-351)
   const double a_min = 1.e-6, a_max = 1.e6;
+  unsigned repeats = 0;  // stall test of the FP32 part (stall_iters > 0; FP32 kernels): the residual repeats in a row
+  double prev_res = 0.0;
   for (;;) {
     if (!runA(alpha, false)) return -1;  // y, residual, s, xs = P(x - alpha y), (xs - prev).y
     const double res = residual_of(scal(0)), decr = scal(1);
@@ -606,6 +621,11 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     }
     if (res < a.tol) {
       return finish(min_res, it, best_pending ? ix : 3, 1);
+    }
+    if (sizeof(T) == 4 && a.stall_iters) {
+      repeats = (it > 0 && res == prev_res) ? repeats + 1 : 0;
+      prev_res = res;
+      if (repeats >= a.stall_iters) return finish(min_res, it, best_pending ? ix : 3, 0);
     }
     const bool mom = decr < 0.;
     const double beta = mom ? nesterov_inertia(theta, 0.0) : 0.0;

@@ -61,6 +61,9 @@ int defaults() {
   const bogus_gpu_pg_options o = pg.options(false);
   expect(o.max_iters == 17 && o.variant == BOGUS_GPU_PG_SPG && o.static_problem == 0 && o.momentum_by_linearity == 1,
          "ProjectedGradient options");
+  expect(o.fp32_stall_iters == 4, "ProjectedGradient: FP32 stall test on by default");
+  pg.setFp32StallIterations(0);
+  expect(pg.options(true).fp32_stall_iters == 0, "ProjectedGradient: FP32 stall test off");
 
   // host-side BAD_INPUT paths (no GPU needed)
   bogus_gpu::DualFrictionProblem<3> dual;

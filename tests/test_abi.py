@@ -58,6 +58,7 @@ def test_defaults_match_reference(built_lib):
     assert (o.ls_optimistic_factor, o.ls_pessimistic_factor, o.ls_armijo_coefficient) == (1.25, 0.5, 0.5)
     assert o.variant == bogus_gpu.APGD and o.static_problem == 1
     assert o.mixed_precision == 0 and o.momentum_by_linearity == 0  # the drop-in: the reference's arithmetic
+    assert o.fp32_stall_iters == 4  # FP32-refined solves only
     g = bogus_gpu.GsOptions()
     L.bogus_gpu_gs_options_default(C.byref(g))
     assert (g.tol, g.max_iters, g.eval_every, g.skip_tol, g.skip_iters) == (1e-6, 250, 25, 1e-6, 10)
