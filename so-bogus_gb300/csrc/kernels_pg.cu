@@ -1031,9 +1031,10 @@ int pg_max_grid(int device, bool fp32, bool interleaved) {
   const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
   if (e != cudaSuccess) return 0;
   // Measured on the 200 000-contact problem: 3 resident CTAs per SM for FP64 (0.388 ms per APGD iteration
-  // against 0.411 with 2 and 0.502 with 1; later 0.215 ms against 0.249 with 4 CTAs at 64 registers). FP32: 3 CTAs at 80 registers with the block values and x loaded
-  // two blocks ahead, 0.120 ms per iteration, against 0.126 at 4 CTAs (64 registers, one block ahead), 0.137
-  // at 4 CTAs with only x ahead, 0.141 with 5 at 48 registers and 0.232 with 2.
+  // against 0.411 with 2 and 0.502 with 1; later 0.215 ms against 0.249 with 4 CTAs at 64 registers). FP32:
+  // 3 CTAs at 80 registers with the block values and x loaded two blocks ahead, 0.120 ms per iteration, against
+  // 0.126 at 4 CTAs (64 registers, one block ahead), 0.137 at 4 CTAs with only x ahead, 0.141 with 5 at 48
+  // registers and 0.232 with 2.
   const int cap = 3;
   if (per > cap) per = cap;
   return per * sms;
