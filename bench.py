@@ -42,6 +42,7 @@ CAP_500 = 500             # the iteration budget of the configuration's wording,
 CPU_SAMPLE_ITERS = 1000   # the oracle's bounded sample: the first 1000 iterations of the same solve
 FP32_ITERS = 20000        # FP32-refined: FP32 iterations until the stall test ends them (at most this many),
                           # then FP64 ones to the tolerance
+HY_REFRESH = 50           # FP32 correction products in those FP64 iterations: x_ref refreshed this often
 MAX_ADJ_FWD_ITERS = 20000
 METRIC = "time-to-residual 1e-6 (ms), FP64 APGD, 200k contacts"
 WORKLOAD = "fp64_apgd_200k_contacts_to_1e-6"
@@ -390,6 +391,22 @@ def measure_secondary(args, D, d, r_fp64, fp64_ms):
         "error_note": "||r_mixed - r_fp64|| / ||r_fp64||, r_fp64 the FP64 solve to 1e-6 (bit-identical to the "
                       "oracle's iterates); W is singular here, so two iterates at residual 1e-6 may differ along "
                       "its null space"}
+    # the FP32-refined form whose FP64 iterations take FP32 correction products (x_ref refreshed every 50
+    # iterations), then a plain FP64 check of the tolerance
+    pgh = bogus_gpu.ProjectedGradient()
+    pgh.setTol(TOL)
+    pgh.setMaxIters(FP32_ITERS)
+    pgh.setMixedPrecision(True, args.max_iters)
+    pgh.setFp32CorrectionProducts(HY_REFRESH)
+    res, st, rh = best_of(pgh)
+    out["fp32_refined_fp32_products_to_1e-6"] = {
+        "device_ms": st["device_ms"], "fp32_ms": st["fp32_device_ms"],
+        "fp32_iterations": st["iterations"] - st["refine_iterations"],
+        "fp32_product_iterations": st["fp32_product_iterations"],
+        "fp64_iterations": st["refine_iterations"] - st["fp32_product_iterations"],
+        "residual": res, "reached_tol": bool(res < TOL), "speedup_vs_fp64": fp64_ms / st["device_ms"],
+        "rel_error_vs_fp64": float(np.linalg.norm(rh - r_fp64) / np.linalg.norm(r_fp64)),
+        "refresh": HY_REFRESH}
     # options with no counterpart in the reference: APGD's momentum product formed by linearity (one pass over
     # W fewer per momentum step; the oracle restates the same variant, tests check it bit for bit), alone and
     # with the FP32-refined form (where it applies to the FP64 iterations)
@@ -742,17 +759,26 @@ def run_mixed(args) -> None:
     pg64.setMaxIters(args.max_iters)
     res_p, st_p, r64 = timed(pg64)
     splits = {}
-    # fixed FP32 budgets (stall test off), then the stall test with a budget it does not reach
-    for m32, stall in ((1000, 0), (2000, 0), (3000, 0), (4000, 0), (6000, 0), (20000, 4)):
+    # fixed FP32 budgets (stall test off), then the stall test with a budget it does not reach, then that with
+    # FP32 correction products in the FP64 iterations (x_ref refreshed every 25, 50, 100 iterations), and those
+    # products alone (no FP32 part)
+    for m32, stall, hy in ((1000, 0, 0), (2000, 0, 0), (3000, 0, 0), (4000, 0, 0), (6000, 0, 0), (20000, 4, 0),
+                           (20000, 4, 25), (20000, 4, 50), (20000, 4, 100), (0, 4, 50)):
         pgm = bogus_gpu.ProjectedGradient()
         pgm.setTol(TOL)
         pgm.setMaxIters(m32)
         pgm.setMixedPrecision(True, args.max_iters)
         pgm.setFp32StallIterations(stall)
+        pgm.setFp32CorrectionProducts(hy)
         res_m, st_m, rm = timed(pgm)
-        splits[f"{m32}" if stall == 0 else f"stall_test_{stall}"] = {"device_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"],
+        key = f"{m32}" if stall == 0 else f"stall_test_{stall}"
+        if hy:
+            key = f"fp32_products_refresh_{hy}" + ("_no_fp32_part" if m32 == 0 else "")
+        splits[key] = {"device_ms": st_m["device_ms"], "fp32_ms": st_m["fp32_device_ms"],
                        "fp32_iterations": st_m["iterations"] - st_m["refine_iterations"],
-                       "fp64_iterations": st_m["refine_iterations"], "residual": res_m,
+                       "fp32_product_iterations": st_m["fp32_product_iterations"],
+                       "fp64_iterations": st_m["refine_iterations"] - st_m["fp32_product_iterations"],
+                       "residual": res_m,
                        "reached_tol": bool(res_m < TOL), "speedup_vs_fp64": st_p["device_ms"] / st_m["device_ms"],
                        "rel_error_vs_fp64": float(np.linalg.norm(rm - r64) / np.linalg.norm(r64))}
     print(json.dumps({

@@ -89,6 +89,14 @@ typedef struct bogus_gpu_pg_options {
                                      Descent) its line search has run out of trials this many times in a row;
                                      the FP64 iterations then start from the best FP32 iterate. 0: the FP32 part
                                      runs to max_iters */
+  unsigned fp32_products_refresh; /* 0 (not in the reference; mixed_precision with APGD only). N > 0: the FP64
+                                     iterations after the FP32 part keep FP64 iterates, law and reductions but
+                                     form their products as W x_ref + W32 (v - x_ref), the correction v - x_ref
+                                     rounded to FP32 and multiplied by the FP32 copy of W, with x_ref and
+                                     W x_ref (FP64) refreshed at the first momentum step on or after every N
+                                     iterations; a plain FP64 solve from their best iterate then checks the
+                                     tolerance with the exact error function (it runs on while the budget
+                                     refine_max_iters lasts). max_iters = 0 skips the FP32 part */
 } bogus_gpu_pg_options;
 
 /* GaussSeidel setters and defaults (Core/BlockSolvers/GaussSeidelBase.hpp:39-91) plus the coloring switch
@@ -388,6 +396,7 @@ typedef struct bogus_gpu_solve_stats {
   double fp64_fma;           /* FP64 fused multiply-adds of the W passes */
   unsigned refine_iterations; /* FP64 iterations after the FP32 ones (mixed precision), else 0 */
   double fp32_device_ms;      /* device time of the FP32 part (mixed precision), else 0 */
+  unsigned fp32_product_iterations; /* of refine_iterations, those with FP32 correction products */
 } bogus_gpu_solve_stats;
 int bogus_gpu_get_solve_stats(const bogus_gpu_problem* h, bogus_gpu_solve_stats* out);
 

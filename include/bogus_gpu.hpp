@@ -271,6 +271,8 @@ class ProjectedGradient : public SolverBase {
   void setMomentumByLinearity(bool on) { lin_ = on; }
   // extension: the FP32 part of the FP32-refined solve ends once FP32 rounding stops its progress (0: never)
   void setFp32StallIterations(unsigned n) { stall_ = n; }
+  // extension: FP32 correction products in the FP64 iterations of the FP32-refined solve (0: off)
+  void setFp32CorrectionProducts(unsigned refresh = 100) { hy_ = refresh; }
 
   bogus_gpu_pg_options options(bool static_problem) const {
     bogus_gpu_pg_options o;
@@ -288,11 +290,12 @@ class ProjectedGradient : public SolverBase {
     o.refine_max_iters = refine_;
     o.momentum_by_linearity = lin_ ? 1 : 0;
     o.fp32_stall_iters = stall_;
+    o.fp32_products_refresh = hy_;
     return o;
   }
 
  private:
-  unsigned ls_iters_ = 8, refine_ = 50, stall_ = 4;
+  unsigned ls_iters_ = 8, refine_ = 50, stall_ = 4, hy_ = 0;
   double opt_ = 1.25, pess_ = 0.5, armijo_ = 0.5;
   int variant_ = BOGUS_GPU_PG_APGD;
   bool mixed_ = false, lin_ = false;

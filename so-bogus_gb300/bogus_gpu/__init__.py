@@ -42,7 +42,8 @@ class PgOptions(C.Structure):
                 ("ls_optimistic_factor", C.c_double), ("ls_pessimistic_factor", C.c_double),
                 ("ls_armijo_coefficient", C.c_double), ("variant", C.c_int), ("use_infinity_norm", C.c_int),
                 ("static_problem", C.c_int), ("mixed_precision", C.c_int), ("refine_max_iters", C.c_uint),
-                ("momentum_by_linearity", C.c_int), ("fp32_stall_iters", C.c_uint)]
+                ("momentum_by_linearity", C.c_int), ("fp32_stall_iters", C.c_uint),
+                ("fp32_products_refresh", C.c_uint)]
 
 
 class GsOptions(C.Structure):
@@ -86,7 +87,8 @@ class BatchShape(C.Structure):
 class SolveStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("kernel_launches", C.c_uint), ("iterations", C.c_uint),
                 ("w_passes", C.c_uint), ("algorithmic_bytes", C.c_double), ("fp64_fma", C.c_double),
-                ("refine_iterations", C.c_uint), ("fp32_device_ms", C.c_double)]
+                ("refine_iterations", C.c_uint), ("fp32_device_ms", C.c_double),
+                ("fp32_product_iterations", C.c_uint)]
 
 
 CALLBACK = C.CFUNCTYPE(None, C.c_uint, C.c_double, C.c_void_p)
@@ -262,6 +264,7 @@ class ProjectedGradient(_SolverBase):
         self._mixed, self._refine = False, 50
         self._lin = False
         self._stall = 4
+        self._hy = 0
 
     def setMomentumByLinearity(self, on: bool = True) -> None:
         """APGD's momentum product formed by linearity, W x = W xs + beta (W xs - W prev), instead of the product
@@ -280,6 +283,13 @@ class ProjectedGradient(_SolverBase):
         counterpart in the reference."""
         self._stall = int(n)
 
+    def setFp32CorrectionProducts(self, refresh: int = 100) -> None:
+        """FP32-refined solve: the FP64 iterations after the FP32 part form their products as
+        W x_ref + W32 (v - x_ref) (FP32 correction, FP64 iterates and law), x_ref refreshed every `refresh`
+        iterations, then a plain FP64 solve checks the tolerance (0: plain FP64 iterations). APGD only. No
+        counterpart in the reference."""
+        self._hy = int(refresh)
+
     def setLineSearchIterations(self, n: int) -> None: self._ls = int(n)
     def setLineSearchOptimisticFactor(self, f: float) -> None: self._opt = float(f)
     def setLineSearchPessimisticFactor(self, f: float) -> None: self._pess = float(f)
@@ -296,6 +306,7 @@ class ProjectedGradient(_SolverBase):
         o.mixed_precision, o.refine_max_iters = int(self._mixed), self._refine
         o.momentum_by_linearity = int(self._lin)
         o.fp32_stall_iters = self._stall
+        o.fp32_products_refresh = self._hy
         return o
 
 

@@ -164,6 +164,9 @@ struct bogus_gpu_problem {
   bool fp32_valid = false;
   DevBuf<float> val32, b32, mu32, sc32, X32, MX32, Y32, S032, XB32, Wv32;
   DevBuf<float> val32p;  // FP32 copy of W's plain BSR values (batched FP32 solves)
+  // FP32 correction products of the FP64 refinement: v - x_ref for 4 position buffers, x_ref, W x_ref
+  DevBuf<float> hy_d;
+  DevBuf<double> hy_xref, hy_wxref;
   bool fp32p_valid = false;
   DevBuf<PGOut> pgout;
   DevBuf<unsigned> barrier;
@@ -448,9 +451,10 @@ struct PGTraffic {
   double bytes = 0, fma = 0;
   unsigned passes = 0;
 };
-PGTraffic pg_traffic(const PGOut& out, int n, long long nnzb, int variant, double elem, bool lin = false) {
+PGTraffic pg_traffic(const PGOut& out, int n, long long nnzb, int variant, double elem, bool lin = false,
+                     double welem = 0.0) {
   const bool spg = variant == BOGUS_GPU_PG_SPG, apgd = variant == BOGUS_GPU_PG_APGD;
-  const double wpass = (double)nnzb * (9.0 * elem + 4.0) + 4.0 * (n + 1);
+  const double wpass = (double)nnzb * (9.0 * (welem > 0.0 ? welem : elem) + 4.0) + 4.0 * (n + 1);
   // values per contact; APGD's trial product also writes the momentum point (and, by linearity, reads the kept
   // product of prev and writes the momentum product)
   const double per_contact[9] = {7, 6, spg ? 21.0 : 18.0, apgd ? (lin ? 28.0 : 22.0) : 19.0, 10, 9, 18, 15, 12};
@@ -466,8 +470,19 @@ PGTraffic pg_traffic(const PGOut& out, int n, long long nnzb, int variant, doubl
   return t;
 }
 
-// Runs the persistent solver with r already in X[0]; returns the buffer holding the result.
-int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual, unsigned* iters, const double** best) {
+// FP32 correction products of an FP64 refinement (k_pg_persistent<double, true, false, true>).
+struct HyArgs {
+  const float* ival;
+  float* d;
+  double* xref;
+  double* wxref;
+  unsigned refresh;
+};
+
+// Runs the persistent solver with r already in X[0]; returns the buffer holding the result. hy: FP64 iterations
+// with FP32 correction products (APGD; no callback: their residuals are those of the corrected products).
+int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual, unsigned* iters, const double** best,
+           const HyArgs* hy = nullptr) {
   const int n = h->W.n;
   const size_t n3 = 3 * (size_t)n;
   if (int e = ensure_interleaved(h)) return e;
@@ -514,6 +529,14 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   a.lin_momentum = lin_momentum(o);
   a.armijo = o->ls_armijo_coefficient;
   a.phantom_ctas = h->test_wait_timeout ? 1u : 0u;
+  if (hy) {
+    a.hy_ival = hy->ival;
+    a.hy_d = hy->d;
+    a.hy_xref = hy->xref;
+    a.hy_wxref = hy->wxref;
+    a.hy_refresh = hy->refresh;
+    a.lin_momentum = 0;
+  }
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 16 * sizeof(unsigned), h->stream));
   BG_CUDA(cudaMemsetAsync(h->status.p, 0, sizeof(int), h->stream));
   int grid = pg_max_grid(h->device, false, true);
@@ -535,10 +558,12 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   h->last_launches = 1;
   if (st != 0) return fail(st, "device-side wait timed out in the projected-gradient kernel");
   {
-    const PGTraffic t = pg_traffic(out, n, h->W.nnzb, o->variant, 8.0, lin_momentum(o) != 0);
+    // hy: the trial and momentum products read FP32 values (the guess product and refreshes FP64, counted so too)
+    const PGTraffic t = pg_traffic(out, n, h->W.nnzb, o->variant, 8.0, lin_momentum(o) != 0 && !hy, hy ? 4.0 : 0.0);
     h->last_stats.iterations = out.iters;
     h->last_stats.refine_iterations = 0;
     h->last_stats.fp32_device_ms = 0.0;
+    h->last_stats.fp32_product_iterations = 0;
     h->last_stats.w_passes = t.passes;
     h->last_stats.algorithmic_bytes = t.bytes;
     h->last_stats.fp64_fma = t.fma;
@@ -546,7 +571,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   if (residual) *residual = out.min_res;
   if (iters) *iters = out.iters;
   *best = out.best_buf == 3 ? h->XB.p : (out.best_buf == 4 ? h->Wv.p : h->X.p + (size_t)out.best_buf * n3);
-  if (h->callback) {
+  if (h->callback && !hy) {
     const unsigned count = out.converged ? out.iters + 1 : out.iters;
     std::vector<double> tr(count);
     if (count) {
@@ -728,20 +753,40 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   const float* b32 =
       out.best_buf == 3 ? h->XB32.p : (out.best_buf == 4 ? h->Wv32.p : h->X32.p + (size_t)out.best_buf * n3);
   BG_CUDA(launch_convert(n3, b32, h->X.p, s));
+  const unsigned it32 = out.iters;
+  const PGTraffic t32 = pg_traffic(out, n, h->W.nnzb, o->variant, 4.0, lin_momentum(o) != 0);
   bogus_gpu_pg_options o64 = *o;
   o64.max_iters = o->refine_max_iters;
-  const unsigned it32 = out.iters;
+  // FP64 iterations with FP32 correction products, then the plain FP64 check from their best iterate
+  unsigned ith = 0;
+  float msh = 0.f;
+  bogus_gpu_solve_stats sth{};
+  if (o->fp32_products_refresh) {
+    BG_CUDA(h->hy_d.ensure(4 * n3));
+    BG_CUDA(h->hy_xref.ensure(n3));
+    BG_CUDA(h->hy_wxref.ensure(n3));
+    const HyArgs hy{h->val32.p, h->hy_d.p, h->hy_xref.p, h->hy_wxref.p, o->fp32_products_refresh};
+    double resh = 0.0;
+    const double* besth = nullptr;
+    const int hst = run_pg(h, &o64, &resh, &ith, &besth, &hy);
+    if (hst != BOGUS_GPU_OK && hst != BOGUS_GPU_NOT_CONVERGED) return hst;
+    if (besth != h->X.p) BG_CUDA(cudaMemcpyAsync(h->X.p, besth, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s));
+    sth = h->last_stats;
+    msh = h->last_ms;
+    o64.max_iters = o->refine_max_iters > ith ? o->refine_max_iters - ith : 1u;
+  }
   const int rst = run_pg(h, &o64, residual, iters, best);
   if (rst != BOGUS_GPU_OK && rst != BOGUS_GPU_NOT_CONVERGED) return rst;
-  const PGTraffic t32 = pg_traffic(out, n, h->W.nnzb, o->variant, 4.0, lin_momentum(o) != 0);
-  h->last_stats.refine_iterations = h->last_stats.iterations;
-  h->last_stats.iterations = it32 + h->last_stats.iterations;
-  h->last_stats.w_passes += t32.passes;
-  h->last_stats.algorithmic_bytes += t32.bytes;
+  h->last_stats.refine_iterations = h->last_stats.iterations + ith;
+  h->last_stats.fp32_product_iterations = ith;
+  h->last_stats.iterations = it32 + ith + h->last_stats.iterations;
+  h->last_stats.w_passes += t32.passes + sth.w_passes;
+  h->last_stats.algorithmic_bytes += t32.bytes + sth.algorithmic_bytes;
+  h->last_stats.fp64_fma += sth.fp64_fma;
   h->last_stats.fp32_device_ms = ms32;
-  h->last_ms += ms32;
-  h->last_launches += 1;
-  if (iters) *iters = it32 + *iters;
+  h->last_ms += ms32 + msh;
+  h->last_launches += o->fp32_products_refresh ? 2 : 1;
+  if (iters) *iters = it32 + ith + *iters;
   return rst;
 }
 
@@ -758,6 +803,9 @@ int check_pg_options(const bogus_gpu_pg_options* o) {
     return fail(BOGUS_GPU_BAD_INPUT, "invalid projected-gradient factors");
   if (o->mixed_precision && o->refine_max_iters == 0)
     return fail(BOGUS_GPU_BAD_INPUT, "mixed precision needs refine_max_iters >= 1 (the FP64 residual)");
+  if (o->fp32_products_refresh && (!o->mixed_precision || o->variant != BOGUS_GPU_PG_APGD || o->momentum_by_linearity))
+    return fail(BOGUS_GPU_BAD_INPUT,
+                "fp32_products_refresh needs mixed_precision and the APGD variant, without momentum_by_linearity");
   return BOGUS_GPU_OK;
 }
 
@@ -937,6 +985,7 @@ void bogus_gpu_pg_options_default(bogus_gpu_pg_options* o) {
   o->refine_max_iters = 50;
   o->momentum_by_linearity = 0;
   o->fp32_stall_iters = 4;
+  o->fp32_products_refresh = 0;
 }
 
 void bogus_gpu_gs_options_default(bogus_gpu_gs_options* o) {
@@ -3399,6 +3448,8 @@ int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
   if (int e = check_pg_options(o)) return e;
   if (o->variant == BOGUS_GPU_PG_STANDARD || o->variant == BOGUS_GPU_PG_CONJUGATED)
     return fail(BOGUS_GPU_BAD_INPUT, "batched solves run APGD, Descent or SPG");
+  if (o->fp32_products_refresh)
+    return fail(BOGUS_GPU_BAD_INPUT, "FP32 correction products (fp32_products_refresh) are single-problem only");
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
   if (h->nproblems == 0 && h->W.n > 0) return fail(BOGUS_GPU_NO_PROBLEM, "no batch partition set (bogus_gpu_set_batch)");
 

@@ -80,6 +80,31 @@ __device__ __forceinline__ void two_free(int p, int q, int& f0, int& f1) {
 
 }  // namespace
 
+// Per-warp scratch of the FP32 correction products, allocated only in the kernel that uses them (HY).
+template <bool HY>
+__device__ __forceinline__ ChunkScratchT<float>* hy_scratch() { return nullptr; }
+template <>
+__device__ __forceinline__ ChunkScratchT<float>* hy_scratch<true>() {
+  __shared__ ChunkScratchT<float> s[8];
+  return s;
+}
+
+// W v for row 32c + lane as W x_ref + W32 (v - x_ref)_32, d = (v - x_ref)_32: FP32 chains over the FP32
+// interleaved copy of W in the chunk-segmented order, then added to the FP64 W x_ref.
+template <class T>
+__device__ __forceinline__ void hy_product(const PGArgsT<T>& a, int c, const float* __restrict__ d,
+                                           ChunkScratchT<float>& sh32, T* acc) {
+  const InterleavedBlocks<float> b32{a.icol, a.hy_ival, a.slot0};
+  float acc32[3] = {0.f, 0.f, 0.f};
+  spmv_chunk<1, true>(a.rowptr, b32, a.n, c, sh32, [&](int j, float* x) { load3cg(d, j, x); }, acc32);
+  const int i = 32 * c + (threadIdx.x & 31);
+  if (i < a.n) {
+    acc[0] = ldcg(a.hy_wxref + 3 * i) + (double)acc32[0];
+    acc[1] = ldcg(a.hy_wxref + 3 * i + 1) + (double)acc32[1];
+    acc[2] = ldcg(a.hy_wxref + 3 * i + 2) + (double)acc32[2];
+  }
+}
+
 template <class T, bool IL>
 struct BlocksOf;
 template <class T>
@@ -97,8 +122,10 @@ struct BlocksOf<T, true> {
 // allocation-free solves). The arithmetic is the same.
 // SC: the Standard and Conjugated variants (their own kernel instantiation, so that their code does not change the
 // register allocation of the APGD / Descent / SPG kernels).
-template <class T, bool IL, bool SC = false, class Ctx>
-__device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
+// HY: APGD with FP32 correction products (FP64 iterates, law and reductions; its own instantiation as well):
+// W v = W x_ref + W32 (v - x_ref)_32, x_ref and W x_ref refreshed in FP64 every hy_refresh iterations.
+template <class T, bool IL, bool SC = false, bool HY = false, class Ctx>
+__device__ __forceinline__ int pg_body_inl(const PGArgsT<T>& a, Ctx& ctx) {
   using Ops = SocOps<T>;
   const Bufs<T> B{a};
   ChunkScratchT<T>& sh = ctx.cs[threadIdx.x >> 5];
@@ -108,6 +135,28 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     spmv_chunk<1, true>(a.rowptr, blocks, a.n, c, sh, [&](int j, T* x) { load3cg(xsrc, j, x); }, acc);
   };
   const int lane = threadIdx.x & 31;
+  // HY: the FP32 correction v - x_ref of position buffer k (0, 1, 2 or 4), written beside every position that a
+  // later product multiplies
+  auto hy_d = [&](int k) -> float* { return a.hy_d + (size_t)(k == 4 ? 3 : k) * 3 * (size_t)a.n; };
+  auto store_corr = [&](int k, int i, const T* v) {
+    if constexpr (HY) {
+      T xr[3];
+      load3cg(a.hy_xref, i, xr);
+      float* d = hy_d(k);
+      d[3 * i] = (float)(v[0] - xr[0]);
+      d[3 * i + 1] = (float)(v[1] - xr[1]);
+      d[3 * i + 2] = (float)(v[2] - xr[2]);
+    }
+  };
+  // W X(k) for row 32c + lane: the FP64 product or, HY, W x_ref + W32 (X(k) - x_ref)_32 (FP32 FMA chains in the
+  // chunk-segmented order over the FP32 interleaved copy of W)
+  auto product_k = [&](int c, int k, T* acc) {
+    if constexpr (HY) {
+      hy_product(a, c, hy_d(k), hy_scratch<HY>()[threadIdx.x >> 5], acc);
+    } else {
+      product(c, B.X(k), acc);
+    }
+  };
   const bool desaxce = a.desaxce != 0;
   const bool spg = a.variant == 4;
   const bool apgd = a.variant == 3;
@@ -181,6 +230,10 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
       load3cg(a.X0, i, x);
       const T d[3] = {x[0] - T(1), x[1] - T(1), x[2] - T(1)};
       v1 = Ops::sq3(d);
+      if constexpr (HY) {
+        store3(a.hy_wxref, i, acc);
+        store3(a.hy_xref, i, x);
+      }
     }
     put2(c, v0, v1, false);
   }
@@ -216,6 +269,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     store3(a.Y, i, y);
     a.S0[i] = s0;
     store3(B.X(ixs), i, xs);
+    store_corr(ixs, i, xs);
     if (spg) {
       T pv[3];
       load3cg(B.X(iprev), i, pv);
@@ -450,13 +504,18 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
     // product goes to ims and the momentum product fma(beta, W xs - W prev, W xs) to imn
     const bool lin = apgd && a.lin_momentum != 0;
     int imp = imx, ims = 1, imn = 2;
+    unsigned next_refresh = HY ? a.hy_refresh : 0u;  // HY: the first iteration whose momentum step refreshes x_ref
     double alpha_t = alpha * a.opt;
     // stall test of the FP32 part (stall_iters > 0; compiled into the FP32 kernels only): consecutive iterations
     // whose residual repeats the previous one bit for bit or whose line search ran out of trials
-    constexpr bool kStallTest = sizeof(T) == 4;
+    // HY: the part ends (for the plain FP64 solve to take over) when the best residual has not improved by 1 %
+    // in 10 refresh intervals, the noise of the FP32 corrections having become the limit
+    constexpr bool kStallTest = sizeof(T) == 4 || HY;
     unsigned stall_run = 0;
     bool exhausted = false;
     double prev_res = 0.0;
+    double hy_best = 0.0;
+    unsigned hy_best_it = 0;
     if (!runA(alpha_t, true)) return -1;
     for (;;) {
       double res = 0.0, J = 0.0;
@@ -472,10 +531,17 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
           best_pending = true;
         }
         converged = res < a.tol;
-        if (kStallTest && a.stall_iters) {
+        if (sizeof(T) == 4 && a.stall_iters) {
           stall_run = ((it > 0 && res == prev_res) || exhausted) ? stall_run + 1 : 0;
           prev_res = res;
           stalled = !converged && stall_run >= a.stall_iters;
+        }
+        if constexpr (HY) {
+          if (it == 0 || res < 0.99 * hy_best) {
+            hy_best = res;
+            hy_best_it = it;
+          }
+          stalled = !converged && it - hy_best_it >= 10u * a.hy_refresh;
         }
         top_done = true;
         return true;
@@ -494,7 +560,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
           const int i = 32 * c + lane;
           double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
           T acc[3] = {T(0), T(0), T(0)};
-          product(c, B.X(ixs), acc);
+          product_k(c, ixs, acc);
           if (!top()) return -1;
           if (converged || (kStallTest && stalled)) break;
           if (i < a.n) {
@@ -517,6 +583,7 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
             if (apgd) {
               const T xn[3] = {fma(bt, xs[0] - pv[0], xs[0]), fma(bt, xs[1] - pv[1], xs[1]), fma(bt, xs[2] - pv[2], xs[2])};
               store3(B.X(ispec), i, xn);
+              store_corr(ispec, i, xn);
               if (lin) {
                 T mp[3];
                 load3cg(B.MX(imp), i, mp);
@@ -552,11 +619,12 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
             T xs[3] = {fma(na, y[0], x[0]), fma(na, y[1], x[1]), fma(na, y[2], x[2])};
             Ops::project(__ldg(a.mu + i), xs);
             store3(B.X(ixs), i, xs);
+            store_corr(ixs, i, xs);
           }
         }
         if (!sync()) return -1;
       }
-      if (kStallTest) exhausted = ls > 0 && ls >= a.ls_iters;
+      if (sizeof(T) == 4) exhausted = ls > 0 && ls >= a.ls_iters;
       ++it;
       const bool more = it < a.max_iters;
       if (apgd && decr2 < 0) {
@@ -574,19 +642,36 @@ __device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
           if (!runA(alpha_t, true)) return -1;
           continue;
         }
-        // E + A: Mx = W x, then A of the next iteration on the same rows
+        // E + A: Mx = W x, then A of the next iteration on the same rows (HY: at a refresh the FP64 product,
+        // which becomes W x_ref, with x_ref = x)
+        const bool refresh = HY && it >= next_refresh;
         ph[6]++;
         for (int c = ctx.first_chunk(); c < C; c = ctx.next_chunk(c)) {
           const int i = 32 * c + lane;
           double r = 0.0, q = 0.0;
           T acc[3] = {T(0), T(0), T(0)};
-          product(c, B.X(ix), acc);
+          if constexpr (HY) {
+            if (refresh) {
+              product(c, B.X(ix), acc);
+              if (i < a.n) {
+                T xr[3];
+                load3cg(B.X(ix), i, xr);
+                store3(a.hy_xref, i, xr);
+                store3(a.hy_wxref, i, acc);
+              }
+            } else {
+              product_k(c, ix, acc);
+            }
+          } else {
+            product(c, B.X(ix), acc);
+          }
           if (i < a.n) {
             store3(B.MX(imx), i, acc);
             phaseA(i, acc, alpha_t, r, q);
           }
           put2(c, r, q, res_mask != 0);
         }
+        if (refresh) next_refresh = it + a.hy_refresh;
         if (!sync_reduce_split(2, res_mask)) return -1;
       } else {
         theta = 1.;
@@ -757,8 +842,15 @@ struct GridCtx {
   __device__ double scal(int q) const { return ldcg(a.scal + q); }
 };
 
+// The solver body; the hybrid instantiation is inlined by force (the compiler's own choice outlines it, with
+// 500-odd bytes of spills), the others as the compiler decides.
+template <class T, bool IL, bool SC = false, bool HY = false, class Ctx>
+__device__ int pg_body(const PGArgsT<T>& a, Ctx& ctx) {
+  return pg_body_inl<T, IL, SC, HY>(a, ctx);
+}
+
 // Occupancy target: 3 resident CTAs per SM (see pg_max_grid).
-template <class T, bool IL, bool SC = false>
+template <class T, bool IL, bool SC = false, bool HY = false>
 __global__ void __launch_bounds__(256, 3) k_pg_persistent(PGArgsT<T> a) {
   __shared__ double smem8[32];
   __shared__ ChunkScratchT<T> cs[8];
@@ -766,7 +858,11 @@ __global__ void __launch_bounds__(256, 3) k_pg_persistent(PGArgsT<T> a) {
   if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0u;
   __syncthreads();
   GridCtx<T> ctx{a, smem8, cs, s_cnt};
-  pg_body<T, IL, SC>(a, ctx);
+  if constexpr (HY) {
+    pg_body_inl<T, IL, SC, HY>(a, ctx);
+  } else {
+    pg_body<T, IL, SC, HY>(a, ctx);
+  }
 }
 
 // One problem per CTA (batched solves): phases separated by __syncthreads, scalars reduced by the CTA's
@@ -1009,9 +1105,14 @@ cudaError_t launch_pg_persistent(const PGArgs& a, int grid, cudaStream_t s) {
   PGArgs copy = a;
   void* args[] = {&copy};
   const bool sc = a.variant == 0 || a.variant == 2;  // Standard, Conjugated
-  if (sc && !a.slot0) return cudaErrorInvalidValue;  // they run on the interleaved copy only
+  const bool hy = a.hy_refresh != 0;                 // FP32 correction products (APGD)
+  if ((sc || hy) && !a.slot0) return cudaErrorInvalidValue;  // they run on the interleaved copy only
+  if (hy && (a.variant != 3 || a.lin_momentum || !a.hy_ival || !a.hy_d || !a.hy_xref || !a.hy_wxref))
+    return cudaErrorInvalidValue;
   const void* fn = sc ? (const void*)k_pg_persistent<double, true, true>
-                      : (a.slot0 ? (const void*)k_pg_persistent<double, true> : (const void*)k_pg_persistent<double, false>);
+                      : (hy ? (const void*)k_pg_persistent<double, true, false, true>
+                            : (a.slot0 ? (const void*)k_pg_persistent<double, true>
+                                       : (const void*)k_pg_persistent<double, false>));
   return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s);
 }
 

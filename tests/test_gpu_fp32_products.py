@@ -1,0 +1,120 @@
+"""FP32 correction products in the FP64 iterations of the FP32-refined solve (an addition with no counterpart in
+the reference): after the FP32 part, APGD keeps FP64 iterates, law and reductions but forms its products as
+W x_ref + W32 (v - x_ref), the correction rounded to FP32 and multiplied by the FP32 copy of W, with x_ref and
+W x_ref refreshed in FP64; a plain FP64 solve then checks the tolerance with the exact error function.
+
+The results are not the reference's iterates (the products are rounded differently), so the tests check what
+the form promises: the returned residual is the oracle's FP64 error function at the returned iterate, below the
+tolerance; the solve repeats bit for bit; a stalled correction part hands over to the plain FP64 iterations;
+the forms it does not cover refuse it.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def bg():
+    import bogus_gpu
+
+    bogus_gpu.lib()
+    return bogus_gpu
+
+
+@pytest.fixture(scope="module")
+def c1(oracle):
+    from bogus_gpu import generator
+
+    d = generator.make("c1")
+    P = oracle.PrimalProblem(d.minv, d.objA, d.objB, d.HA, d.HB)
+    rp, cl, vl = P.assemble()
+    return d, rp, cl, vl
+
+
+@pytest.mark.parametrize("fp32_iters", [400, 0])  # with and without the FP32 part
+@pytest.mark.parametrize("static", [True, False])
+def test_correction_products_reach_the_fp64_tolerance(bg, oracle, c1, fp32_iters, static):
+    d, rp, cl, vl = c1
+    D = bg.DualFrictionProblem()
+    D.set(rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    pg = bg.ProjectedGradient()
+    pg.setTol(1e-10)
+    pg.setMaxIters(fp32_iters)
+    pg.setMixedPrecision(True, 4000)
+    pg.setFp32CorrectionProducts(50)
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r, staticProblem=static)
+    st = D.solve_stats()
+    assert res == O.eval(r, coulomb=not static) and res < 1e-10
+    assert st["fp32_product_iterations"] > 0 and st["refine_iterations"] >= st["fp32_product_iterations"]
+    assert st["kernel_launches"] == 3
+    r2 = np.zeros(3 * d.n)
+    assert D.solveWith(pg, r2, staticProblem=static) == res and np.array_equal(r2, r)
+
+
+def test_stalled_corrections_hand_over_to_fp64(bg, oracle, c1):
+    """A refresh interval too long for the tolerance: the correction part stops once its best residual has not
+    improved by 1 % in 10 intervals, and the plain FP64 iterations go on from its best iterate."""
+    d, rp, cl, vl = c1
+    D = bg.DualFrictionProblem()
+    D.set(rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    pg = bg.ProjectedGradient()
+    pg.setTol(1e-14)
+    pg.setMaxIters(200)
+    pg.setMixedPrecision(True, 30000)
+    pg.setFp32CorrectionProducts(1000)
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r, staticProblem=True)
+    st = D.solve_stats()
+    assert 0 < st["fp32_product_iterations"] < 30000
+    assert st["refine_iterations"] > st["fp32_product_iterations"]  # plain FP64 iterations followed
+    assert res == O.eval(r, coulomb=False)
+
+
+def test_full_size_correction_products(bg, oracle):
+    """200 000 contacts to 1e-6: the FP64 error function of the returned iterate meets the tolerance."""
+    from bogus_gpu import generator
+
+    d = generator.make("c2")
+    D = bg.DualFrictionProblem()
+    D.computeFrom(bg.PrimalFrictionProblem.from_generated(d))
+    rp, cl, vl = D.W_lower()
+    O = oracle.DualProblem(rp, cl, vl.reshape(-1), d.b, d.mu)
+    pg = bg.ProjectedGradient()
+    pg.setTol(1e-6)
+    pg.setMaxIters(20000)
+    pg.setMixedPrecision(True, 20000)
+    pg.setFp32CorrectionProducts(50)
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r, staticProblem=True)
+    st = D.solve_stats()
+    assert res < 1e-6 and res == O.eval(r, coulomb=False)
+    assert st["fp32_product_iterations"] > 0
+
+
+def test_correction_products_refused_where_not_built(bg, c1):
+    d, rp, cl, vl = c1
+    D = bg.DualFrictionProblem()
+    D.set(rp, cl, vl, d.b, d.mu)
+    for setup in (lambda pg: None,                                                  # no FP32-refined solve
+                  lambda pg: (pg.setMixedPrecision(True, 50), pg.setDefaultVariant(4)),  # SPG
+                  lambda pg: (pg.setMixedPrecision(True, 50), pg.setMomentumByLinearity(True))):
+        pg = bg.ProjectedGradient()
+        setup(pg)
+        pg.setFp32CorrectionProducts(50)
+        with pytest.raises(bg.BogusGpuError):
+            D.solveWith(pg, np.zeros(3 * d.n))
+    from bogus_gpu import generator
+
+    db, cptr = generator.batch(nproblems=4, nmin=16, nmax=64, seed=3)
+    B = bg.DualFrictionProblem()
+    B.computeFrom(bg.PrimalFrictionProblem.from_generated(db))
+    B.setBatch(cptr)
+    pg = bg.ProjectedGradient()
+    pg.setMixedPrecision(True, 50)
+    pg.setFp32CorrectionProducts(50)
+    with pytest.raises(bg.BogusGpuError):
+        B.solveBatchWith(pg, np.zeros(3 * db.n))
