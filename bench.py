@@ -456,8 +456,9 @@ def measure_secondary(args, D, d, r_fp64, fp64_ms):
     return out
 
 
-def run_profile(iters: int, mixed: bool = False) -> None:
-    """One APGD solve of the benchmark problem capped at `iters` iterations (the solver kernel under ncu)."""
+def run_profile(iters: int, mixed: bool = False, products: bool = False) -> None:
+    """One APGD solve of the benchmark problem capped at `iters` iterations (the solver kernel under ncu);
+    products: the FP64 iterations with FP32 correction products (no FP32 part), then the plain FP64 check."""
     import bogus_gpu
 
     d = make_problem()
@@ -468,6 +469,10 @@ def run_profile(iters: int, mixed: bool = False) -> None:
     pg.setMaxIters(iters)
     if mixed:
         pg.setMixedPrecision(True, 1)
+    if products:
+        pg.setMaxIters(0)
+        pg.setMixedPrecision(True, iters)
+        pg.setFp32CorrectionProducts(HY_REFRESH)
     r = np.zeros(3 * d.n)
     res = D.solveWith(pg, r)
     st = D.solve_stats()
@@ -960,6 +965,8 @@ def main():
                     help="--workload adjoint: the laws to run")
     ap.add_argument("--profile-mixed", action="store_true",
                     help="with --profile: the FP32-refined solve (FP32 iterations, then 1 FP64 iteration)")
+    ap.add_argument("--profile-fp32-products", action="store_true",
+                    help="with --profile: FP64 iterations with FP32 correction products (no FP32 part)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -969,7 +976,7 @@ def main():
         single[args.workload](args)
         return
     if args.profile:
-        run_profile(args.profile, args.profile_mixed)
+        run_profile(args.profile, args.profile_mixed, args.profile_fp32_products)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)
