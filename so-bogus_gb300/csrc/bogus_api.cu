@@ -558,8 +558,13 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
   h->last_launches = 1;
   if (st != 0) return fail(st, "device-side wait timed out in the projected-gradient kernel");
   {
-    // hy: the trial and momentum products read FP32 values (the guess product and refreshes FP64, counted so too)
-    const PGTraffic t = pg_traffic(out, n, h->W.nnzb, o->variant, 8.0, lin_momentum(o) != 0 && !hy, hy ? 4.0 : 0.0);
+    // hy: the trial and momentum products read FP32 values; the guess product and the refreshes the FP64 ones
+    PGTraffic t = pg_traffic(out, n, h->W.nnzb, o->variant, 8.0, lin_momentum(o) != 0 && !hy, hy ? 4.0 : 0.0);
+    if (hy) {
+      const double fp64_passes = (double)out.phases[1] + (double)out.hy_refreshes;
+      t.bytes += fp64_passes * 36.0 * (double)h->W.nnzb;
+      t.fma = 9.0 * (double)h->W.nnzb * (2.0 * out.phases[1] + out.hy_refreshes);
+    }
     h->last_stats.iterations = out.iters;
     h->last_stats.refine_iterations = 0;
     h->last_stats.fp32_device_ms = 0.0;

@@ -32,6 +32,7 @@ struct PGOut {
   // 0 projection, 1 guess product, 2 A, 3 C (trial product), 4 B (retry), 5 D (momentum), 6 E+A,
   // 7 SPG D, 8 SPG E
   unsigned phases[9];
+  unsigned hy_refreshes;  // FP32 correction products: momentum steps that took the FP64 product (x_ref refreshed)
 };
 
 // T: storage and per-contact arithmetic type (double: the FP64 drop-in; float: the FP32 part of the

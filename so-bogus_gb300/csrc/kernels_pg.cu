@@ -189,6 +189,7 @@ __device__ __forceinline__ int pg_body_inl(const PGArgsT<T>& a, Ctx& ctx) {
   // ConstrainedSolverBase::eval: sum / (1 + n), or the maximum with the infinity norm
   auto residual_of = [&](double reduced) { return a.use_inf ? reduced : reduced / (double)(1 + a.n); };
   unsigned ph[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned n_refresh = 0;  // HY: refreshes of x_ref
   auto finish = [&](double min_res, unsigned iters, int best_buf, int converged) -> int {
     if (ctx.writer()) {
       a.out->min_res = min_res;
@@ -197,6 +198,7 @@ __device__ __forceinline__ int pg_body_inl(const PGArgsT<T>& a, Ctx& ctx) {
       a.out->converged = converged;
 #pragma unroll
       for (int k = 0; k < 9; ++k) a.out->phases[k] = ph[k];
+      a.out->hy_refreshes = n_refresh;
     }
     return best_buf;
   };
@@ -671,7 +673,10 @@ __device__ __forceinline__ int pg_body_inl(const PGArgsT<T>& a, Ctx& ctx) {
           }
           put2(c, r, q, res_mask != 0);
         }
-        if (refresh) next_refresh = it + a.hy_refresh;
+        if (refresh) {
+          next_refresh = it + a.hy_refresh;
+          ++n_refresh;
+        }
         if (!sync_reduce_split(2, res_mask)) return -1;
       } else {
         theta = 1.;
