@@ -96,7 +96,11 @@ typedef struct bogus_gpu_pg_options {
                                      W x_ref (FP64) refreshed at the first momentum step on or after every N
                                      iterations; a plain FP64 solve from their best iterate then checks the
                                      tolerance with the exact error function (it runs on while the budget
-                                     refine_max_iters lasts). max_iters = 0 skips the FP32 part */
+                                     refine_max_iters lasts). The corrections leave a floor in the error
+                                     function that grows with N (about 1e-8 N on a 200 000-contact problem):
+                                     choose N well below tol / 1e-8 there; a part whose best residual stops
+                                     improving (1 % in 10 N iterations) hands over early. max_iters = 0 skips
+                                     the FP32 part */
 } bogus_gpu_pg_options;
 
 /* GaussSeidel setters and defaults (Core/BlockSolvers/GaussSeidelBase.hpp:39-91) plus the coloring switch
