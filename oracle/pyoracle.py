@@ -52,7 +52,8 @@ def lib():
     L.oracle_dual_eval.argtypes = [vp, C.c_int, _dp, C.c_int]
     L.oracle_dual_solve_pg.restype = C.c_double
     L.oracle_dual_solve_pg.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_double,
-                                       C.c_double, C.c_int, C.c_int, _dp, C.POINTER(C.c_uint), CALLBACK, C.c_void_p]
+                                       C.c_double, C.c_int, C.c_int, C.c_uint, _dp, C.POINTER(C.c_uint), CALLBACK,
+                                       C.c_void_p]
     L.oracle_dual_coloring.restype = C.c_int
     L.oracle_dual_coloring.argtypes = [vp, _ip, _ip]
     L.oracle_dual_solve_cadoux_gs.restype = C.c_double
@@ -193,14 +194,16 @@ class DualProblem:
         return perm, colors[: nc + 1]
 
     def solve_pg(self, r, variant=3, coulomb=False, tol=1e-6, max_iters=300, ls_iters=8, optimistic=1.25,
-                 pessimistic=0.5, armijo=0.5, inf_norm=False, trace: Trace | None = None, lin_momentum=False):
-        """lin_momentum: APGD's momentum product by linearity (not in the reference; see ProjectedGradient)."""
+                 pessimistic=0.5, armijo=0.5, inf_norm=False, trace: Trace | None = None, lin_momentum=False,
+                 hy_refresh=0):
+        """lin_momentum: APGD's momentum product by linearity; hy_refresh: FP32 correction products refreshed
+        every hy_refresh iterations (neither is in the reference; see ProjectedGradient)."""
         r = _f64(r).copy()
         it = C.c_uint(0)
         cb = trace._cb if trace else _NO_CB
         res = lib().oracle_dual_solve_pg(self.h, variant, int(coulomb), tol, max_iters, ls_iters, optimistic,
-                                         pessimistic, armijo, int(inf_norm), int(lin_momentum), r, C.byref(it), cb,
-                                         None)
+                                         pessimistic, armijo, int(inf_norm), int(lin_momentum), int(hy_refresh), r,
+                                         C.byref(it), cb, None)
         return res, r, it.value
 
     def solve_cadoux_gs(self, r, cadoux_iters, strategy=3, tol=1e-6, max_iters=250, eval_every=25, skip_tol=1e-6,

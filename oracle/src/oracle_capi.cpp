@@ -115,12 +115,13 @@ double oracle_dual_eval(void* h, int desaxce, const double* r, int useInfinityNo
 
 double oracle_dual_solve_pg(void* h, int variant, int desaxce, double tol, unsigned maxIters, unsigned lsIters,
                             double optimistic, double pessimistic, double armijo, int useInfinityNorm, int linMomentum,
-                            double* r, unsigned* iters, oracle_callback cb, void* user) {
+                            unsigned hyRefresh, double* r, unsigned* iters, oracle_callback cb, void* user) {
   auto* p = static_cast<DualProblem*>(h);
   ProjectedGradient pg;
   pg.setMatrix(p->full);
   pg.variant = variant;
   pg.linMomentum = linMomentum != 0;
+  pg.hyRefresh = hyRefresh;
   pg.tol = tol;
   pg.maxIters = maxIters;
   pg.lsIters = lsIters;

@@ -298,12 +298,19 @@ struct ProjectedGradient : SolverBase {
   // product W x of ProjectedGradient.impl.hpp:141 (same fma form as x itself). One pass over W fewer per
   // momentum step; the iterates differ from the reference's by the rounding of the two forms.
   bool linMomentum = false;
+  // Not in the reference: FP32 correction products (APGD). Each trial and momentum product is
+  // W x_ref + W32 (v - x_ref)_32 (spmv32 on the correction rounded to float, added to the FP64 W x_ref); the
+  // first momentum step on or after every hyRefresh iterations takes the FP64 product instead, which becomes
+  // W x_ref with x_ref = x. The solve ends (not converged) when its best residual has not improved by 1 % in
+  // 10 hyRefresh iterations. 0: off.
+  unsigned hyRefresh = 0;
 
   ProjectedGradient() { tol = 1e-6; maxIters = 300; }
 
   bool testResidual(const Law& law, unsigned it, const double* x, const double* y, std::vector<double>& x_best,
-                    double& min_res) const {
+                    double& min_res, double* resOut = nullptr) const {
     const double res = eval(law, y, x);
+    if (resOut) *resOut = res;
     trigger(it, res);
     if (0 == it || res < min_res) {
       x_best.assign(x, x + 3 * (size_t)n());
@@ -351,13 +358,43 @@ struct ProjectedGradient : SolverBase {
     double theta = 1., q = 0;
     prev.assign(x, x + n3);
     if (linMomentum) Mprev = Mx;  // W prev
+    // FP32 correction products (hyRefresh > 0)
+    std::vector<float> W32, d32, p32;
+    std::vector<double> xref, wxref;
+    unsigned nextRefresh = hyRefresh, hyBestIt = 0;
+    double hyBest = 0.0;
+    if (hyRefresh) {
+      W32.resize(W->val.size());
+      for (size_t k = 0; k < W32.size(); ++k) W32[k] = (float)W->val[k];
+      d32.resize(n3);
+      p32.resize(n3);
+      xref.assign(x, x + n3);
+      wxref = Mx;
+    }
+    auto product = [&](const double* v, double* out) {
+      if (!hyRefresh) {
+        spmv(*W, v, out);
+        return;
+      }
+      for (size_t k = 0; k < n3; ++k) d32[k] = (float)(v[k] - xref[k]);
+      spmv32(*W, W32.data(), d32.data(), p32.data());
+      for (size_t k = 0; k < n3; ++k) out[k] = wxref[k] + (double)p32[k];
+    };
     double alpha = 1.;
     guessAlpha(x, alpha);
     double min_res = -1;
     unsigned it;
     for (it = 0; it < maxIters; ++it) {
       for (size_t k = 0; k < n3; ++k) y[k] = Mx[k] + b[k];
-      if (testResidual(law, it, x, y.data(), x_best, min_res)) break;
+      double res = 0.0;
+      if (testResidual(law, it, x, y.data(), x_best, min_res, &res)) break;
+      if (hyRefresh) {
+        if (it == 0 || res < 0.99 * hyBest) {
+          hyBest = res;
+          hyBestIt = it;
+        }
+        if (it - hyBestIt >= 10u * hyRefresh) break;
+      }
       dualityCOVAll(law, y.data(), s.data());
       for (size_t k = 0; k < n3; ++k) y[k] = y[k] + s[k];
       const double J = objective(x, Mx.data(), b, s.data());
@@ -366,7 +403,7 @@ struct ProjectedGradient : SolverBase {
       for (unsigned ls = 0; ls < lsIters; ++ls, alpha *= lsPessimisticFactor) {
         for (size_t k = 0; k < n3; ++k) xs[k] = std::fma(-alpha, y[k], x[k]);
         projectOnConstraints(law, xs.data());
-        spmv(*W, xs.data(), Mx.data());
+        product(xs.data(), Mx.data());
         Js = objective(xs.data(), Mx.data(), b, s.data());
         const double decr = reduceContacts(N, [&](int i) {
           const double d[3] = {xs[3 * i] - x[3 * i], xs[3 * i + 1] - x[3 * i + 1], xs[3 * i + 2] - x[3 * i + 2]};
@@ -392,8 +429,13 @@ struct ProjectedGradient : SolverBase {
             Mx[k] = std::fma(beta, mxs - Mprev[k], mxs);
             Mprev[k] = mxs;
           }
+        } else if (hyRefresh && it + 1 >= nextRefresh) {
+          spmv(*W, x, Mx.data());  // refresh: x_ref = x, W x_ref = W x
+          xref.assign(x, x + n3);
+          wxref = Mx;
+          nextRefresh = it + 1 + hyRefresh;
         } else {
-          spmv(*W, x, Mx.data());
+          product(x, Mx.data());
         }
       } else {
         std::copy(xs.begin(), xs.end(), x);

@@ -126,6 +126,47 @@ inline void spmv(const BSR& W, const double* x, double* y, const double* init = 
   }
 }
 
+// y = W32 x in single precision, W32 the float copy of W's values (9 per block, BSR order), in the same canonical
+// chunk-segmented order as spmv (pieces from 0 by fmaf chains, the first piece of a row placed as 0 + piece, the
+// next ones added). Not in the reference: the FP32 correction products of the FP32-refined solve.
+inline void spmv32(const BSR& W, const float* W32, const float* x, float* y) {
+  const int C = (W.n + 31) / 32;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < C; ++c) {
+    const int r0 = 32 * c, r1 = std::min(W.n, r0 + 32);
+    const int B0 = W.rowptr[r0], B1 = W.rowptr[r1];
+    const int T = B1 - B0;
+    const int S = T > 0 ? (T + 31) / 32 : 1;
+    for (int i = r0; i < r1; ++i) {
+      float acc[3] = {0.f, 0.f, 0.f};
+      int k = W.rowptr[i];
+      const int hi = W.rowptr[i + 1];
+      while (k < hi) {
+        const int l = (k - B0) / S;
+        const int e = std::min(hi, std::min(B0 + (l + 1) * S, B1));
+        float p[3] = {0.f, 0.f, 0.f};
+        for (; k < e; ++k) {
+          const float* B = W32 + 9 * (size_t)k;
+          const float* xv = x + 3 * (size_t)W.col[k];
+          for (int r = 0; r < 3; ++r) {
+            float a = p[r];
+            a = std::fma(B[3 * r + 0], xv[0], a);
+            a = std::fma(B[3 * r + 1], xv[1], a);
+            a = std::fma(B[3 * r + 2], xv[2], a);
+            p[r] = a;
+          }
+        }
+        acc[0] = acc[0] + p[0];
+        acc[1] = acc[1] + p[1];
+        acc[2] = acc[2] + p[2];
+      }
+      y[3 * i] = acc[0];
+      y[3 * i + 1] = acc[1];
+      y[3 * i + 2] = acc[2];
+    }
+  }
+}
+
 // res += sum_{j != row} W_row,j x_j (splitRowMultiply), full view
 inline void splitRowMultiply(const BSR& W, int row, const double* x, double* res) {
   for (int k = W.rowptr[row]; k < W.rowptr[row + 1]; ++k) {

@@ -3,10 +3,11 @@ the reference): after the FP32 part, APGD keeps FP64 iterates, law and reduction
 W x_ref + W32 (v - x_ref), the correction rounded to FP32 and multiplied by the FP32 copy of W, with x_ref and
 W x_ref refreshed in FP64; a plain FP64 solve then checks the tolerance with the exact error function.
 
-The results are not the reference's iterates (the products are rounded differently), so the tests check what
-the form promises: the returned residual is the oracle's FP64 error function at the returned iterate, below the
-tolerance; the solve repeats bit for bit; a stalled correction part hands over to the plain FP64 iterations;
-the forms it does not cover refuse it.
+The results are not the reference's iterates (the products are rounded differently). The oracle restates the
+form (ProjectedGradient::hyRefresh), and without an FP32 part the GPU iterations equal it bit for bit; beyond
+that the tests check what the form promises: the returned residual is the oracle's FP64 error function at the
+returned iterate, below the tolerance; the solve repeats bit for bit; a stalled correction part hands over to
+the plain FP64 iterations; the forms it does not cover refuse it.
 """
 import numpy as np
 import pytest
@@ -52,6 +53,33 @@ def test_correction_products_reach_the_fp64_tolerance(bg, oracle, c1, fp32_iters
     assert st["kernel_launches"] == 3
     r2 = np.zeros(3 * d.n)
     assert D.solveWith(pg, r2, staticProblem=static) == res and np.array_equal(r2, r)
+
+
+@pytest.mark.parametrize("refresh, tol, budget", [(7, 1e-10, 3000), (50, 1e-10, 3000), (1000, 1e-14, 30000)])
+@pytest.mark.parametrize("static", [True, False])
+def test_correction_products_bitwise_against_the_oracle(bg, oracle, c1, refresh, tol, budget, static):
+    """Without an FP32 part (max_iters = 0, r = 0) the correction iterations equal the oracle's restatement of
+    them bit for bit (iteration count, refreshes, stall rule), and so does the plain FP64 check that follows from
+    their best iterate (iterate, residual, iteration count)."""
+    d, rp, cl, vl = c1
+    D = bg.DualFrictionProblem()
+    D.set(rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    pg = bg.ProjectedGradient()
+    pg.setTol(tol)
+    pg.setMaxIters(0)
+    pg.setMixedPrecision(True, budget)
+    pg.setFp32CorrectionProducts(refresh)
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r, staticProblem=static)
+    st = D.solve_stats()
+    ith = st["fp32_product_iterations"]
+    _, r_h, it_h = O.solve_pg(np.zeros(3 * d.n), variant=3, coulomb=not static, tol=tol, max_iters=budget,
+                              hy_refresh=refresh)
+    assert ith == it_h
+    res_c, r_c, it_c = O.solve_pg(r_h, variant=3, coulomb=not static, tol=tol, max_iters=max(1, budget - it_h))
+    assert st["refine_iterations"] - ith == it_c
+    assert res == res_c and np.array_equal(r, r_c)
 
 
 def test_stalled_corrections_hand_over_to_fp64(bg, oracle, c1):
