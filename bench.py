@@ -562,6 +562,14 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
     pgml.setMomentumByLinearity(True)
     solve(pgml)
     ml_ms, (res_ml, its_ml) = _sync_time(lambda: solve(pgml), world)
+    # the FP32-refined batch whose FP64 iterations take FP32 correction products, same budget
+    pgmh = bogus_gpu.ProjectedGradient()
+    pgmh.setTol(TOL)
+    pgmh.setMaxIters(200)
+    pgmh.setMixedPrecision(True, BATCH_MAX_ITERS - 200)
+    pgmh.setFp32CorrectionProducts(HY_REFRESH)
+    solve(pgmh)
+    mh_ms, (res_mh, its_mh) = _sync_time(lambda: solve(pgmh), world)
     # the launch shape chosen by the tuner (measured on this batch) against the default rule, same results
     rule_shape = D.batchShape()
     D.setBatchTuning(True)
@@ -598,7 +606,7 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
                "capture_call_ms": graph[0], "identical_results": graph_same,
                "note": "host-buffer calls (pinned r), wall time per call including copies; the first graph call "
                        "captures"}
-    allres = shard.gather_results(mine, np.stack([res, its, res_m, res_l, res_ml], 1), nprob, world)
+    allres = shard.gather_results(mine, np.stack([res, its, res_m, res_l, res_ml, res_mh], 1), nprob, world)
     out = {"problems": nprob, "contacts": int(d.n), "ranks": world, "max_iters": BATCH_MAX_ITERS,
            "batched_ms": statistics.median(times), "kernel_ms": statistics.median(kernel),
            "tuned": tuned, "cuda_graph": graphed,
@@ -610,6 +618,9 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
            "fp32_refined_momentum_by_linearity": {"split": "up to 200 FP32 + 300 FP64 iterations per problem, the "
                                                            "FP64 ones with the momentum product by linearity",
                                                   "batched_ms": ml_ms},
+           "fp32_refined_fp32_products": {"split": "up to 200 FP32 + 300 FP64 iterations per problem, the FP64 ones "
+                                                   f"with FP32 correction products (x_ref refreshed every {HY_REFRESH})",
+                                          "batched_ms": mh_ms},
            "timing": f"median of {steps} solves after a warm-up, wall time between device synchronisations"}
     if world > 1:
         out["partition"] = {"rule": "greedy bin-pack on W blocks", "blocks_per_rank": [int(costs[q].sum()) for q in parts],
@@ -625,6 +636,8 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
     out["momentum_by_linearity"]["speedup_vs_fp64_batch"] = out["batched_ms"] / lin_ms
     out["fp32_refined_momentum_by_linearity"]["converged_fraction"] = float(np.mean(allres[:, 4] < TOL))
     out["fp32_refined_momentum_by_linearity"]["speedup_vs_fp64_batch"] = out["batched_ms"] / ml_ms
+    out["fp32_refined_fp32_products"]["converged_fraction"] = float(np.mean(allres[:, 5] < TOL))
+    out["fp32_refined_fp32_products"]["speedup_vs_fp64_batch"] = out["batched_ms"] / mh_ms
     if world == 1 and sample_stride:
         # the single-problem path, problem by problem (inputs set beforehand, each solve timed with its r copies)
         sys.path.insert(0, os.path.join(REPO, "oracle"))

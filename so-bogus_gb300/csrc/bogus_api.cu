@@ -477,6 +477,7 @@ struct HyArgs {
   double* xref;
   double* wxref;
   unsigned refresh;
+  size_t stride;  // floats between the position buffers' corrections in d
 };
 
 // Runs the persistent solver with r already in X[0]; returns the buffer holding the result. hy: FP64 iterations
@@ -535,6 +536,7 @@ int run_pg(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residual
     a.hy_xref = hy->xref;
     a.hy_wxref = hy->wxref;
     a.hy_refresh = hy->refresh;
+    a.hy_stride = hy->stride;
     a.lin_momentum = 0;
   }
   BG_CUDA(cudaMemsetAsync(h->barrier.p, 0, 16 * sizeof(unsigned), h->stream));
@@ -770,7 +772,7 @@ int run_pg_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
     BG_CUDA(h->hy_d.ensure(4 * n3));
     BG_CUDA(h->hy_xref.ensure(n3));
     BG_CUDA(h->hy_wxref.ensure(n3));
-    const HyArgs hy{h->val32.p, h->hy_d.p, h->hy_xref.p, h->hy_wxref.p, o->fp32_products_refresh};
+    const HyArgs hy{h->val32.p, h->hy_d.p, h->hy_xref.p, h->hy_wxref.p, o->fp32_products_refresh, n3};
     double resh = 0.0;
     const double* besth = nullptr;
     const int hst = run_pg(h, &o64, &resh, &ith, &besth, &hy);
@@ -3408,7 +3410,7 @@ PGBatchArgs batch_args64(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
 
 // Per-problem outputs and the solve statistics from the per-problem results.
 int finish_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, const PGOut* out, double* residuals,
-                 unsigned* iters) {
+                 unsigned* iters, bool hy = false) {
   const int np = h->nproblems;
   bool all = true;
   PGTraffic sum;
@@ -3418,7 +3420,13 @@ int finish_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, const PGOu
     if (iters) iters[p] = out[p].iters;
     all = all && (out[p].converged || h->h_contact_ptr[p + 1] == h->h_contact_ptr[p]);
     const int np_c = h->h_contact_ptr[p + 1] - h->h_contact_ptr[p];
-    const PGTraffic t = pg_traffic(out[p], np_c, h->h_problem_nnz[p], o->variant, 8.0, lin_momentum(o) != 0);
+    PGTraffic t = pg_traffic(out[p], np_c, h->h_problem_nnz[p], o->variant, 8.0, lin_momentum(o) != 0 && !hy,
+                             hy ? 4.0 : 0.0);
+    if (hy) {  // the guess product and the refreshes read the FP64 values
+      const double nnz = (double)h->h_problem_nnz[p];
+      t.bytes += ((double)out[p].phases[1] + (double)out[p].hy_refreshes) * 36.0 * nnz;
+      t.fma = 9.0 * nnz * (2.0 * out[p].phases[1] + out[p].hy_refreshes);
+    }
     sum.bytes += t.bytes;
     sum.fma += t.fma;
     sum.passes += t.passes;
@@ -3427,15 +3435,27 @@ int finish_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, const PGOu
   h->last_stats.iterations = maxit;
   h->last_stats.refine_iterations = 0;
   h->last_stats.fp32_device_ms = 0.0;
+  h->last_stats.fp32_product_iterations = 0;
   h->last_stats.w_passes = sum.passes;
   h->last_stats.algorithmic_bytes = sum.bytes;
   h->last_stats.fp64_fma = sum.fma;
   return all ? BOGUS_GPU_OK : BOGUS_GPU_NOT_CONVERGED;
 }
 
-int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residuals, unsigned* iters) {
+// hy: the FP64 iterations with FP32 correction products (the plain FP32 copy of W's values)
+int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* residuals, unsigned* iters,
+                 const HyArgs* hy = nullptr) {
   const int np = h->nproblems;
-  const PGBatchArgs ba = batch_args64(h, o);
+  PGBatchArgs ba = batch_args64(h, o);
+  if (hy) {
+    ba.base.hy_ival = hy->ival;
+    ba.base.hy_d = hy->d;
+    ba.base.hy_xref = hy->xref;
+    ba.base.hy_wxref = hy->wxref;
+    ba.base.hy_refresh = hy->refresh;
+    ba.base.hy_stride = hy->stride;
+    ba.base.lin_momentum = 0;
+  }
   BatchShape sh;
   if (int e = choose_shape(h, ba, false, sizeof(double) * 3 * (size_t)h->W.n, h->X.p, &sh)) return e;
   if (int e = launch_shape(h, sh, &ba, nullptr, true)) return e;
@@ -3445,7 +3465,7 @@ int run_pg_batch(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, double* re
   if (int e = read_status(h)) return e;
   BG_CUDA(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
   h->last_launches = 1;
-  return finish_batch(h, o, out.data(), residuals, iters);
+  return finish_batch(h, o, out.data(), residuals, iters, hy != nullptr);
 }
 
 int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
@@ -3453,8 +3473,6 @@ int batch_checks(bogus_gpu_problem* h, const bogus_gpu_pg_options* o) {
   if (int e = check_pg_options(o)) return e;
   if (o->variant == BOGUS_GPU_PG_STANDARD || o->variant == BOGUS_GPU_PG_CONJUGATED)
     return fail(BOGUS_GPU_BAD_INPUT, "batched solves run APGD, Descent or SPG");
-  if (o->fp32_products_refresh)
-    return fail(BOGUS_GPU_BAD_INPUT, "FP32 correction products (fp32_products_refresh) are single-problem only");
   if (!h->has_dual) return fail(BOGUS_GPU_NO_PROBLEM, "no dual problem set");
   if (h->nproblems == 0 && h->W.n > 0) return fail(BOGUS_GPU_NO_PROBLEM, "no batch partition set (bogus_gpu_set_batch)");
 
@@ -3555,18 +3573,44 @@ int run_pg_batch_mixed(bogus_gpu_problem* h, const bogus_gpu_pg_options* o, doub
   bogus_gpu_pg_options o64 = *o;
   o64.max_iters = o->refine_max_iters;
   o64.mixed_precision = 0;
+  o64.fp32_products_refresh = 0;
+  // FP64 iterations with FP32 correction products, then the plain FP64 check from each problem's best iterate
+  std::vector<unsigned> ith(np, 0u);
+  unsigned maxh = 0;
+  float msh = 0.f;
+  bogus_gpu_solve_stats sth{};
+  if (o->fp32_products_refresh) {
+    BG_CUDA(h->hy_d.ensure(4 * n3));
+    BG_CUDA(h->hy_xref.ensure(n3));
+    BG_CUDA(h->hy_wxref.ensure(n3));
+    const HyArgs hy{h->val32p.p, h->hy_d.p, h->hy_xref.p, h->hy_wxref.p, o->fp32_products_refresh, n3};
+    std::vector<double> resh(np);
+    bogus_gpu_pg_options oh = o64;
+    oh.fp32_products_refresh = o->fp32_products_refresh;
+    oh.mixed_precision = 1;
+    const int hst = run_pg_batch(h, &oh, resh.data(), ith.data(), &hy);
+    if (hst != BOGUS_GPU_OK && hst != BOGUS_GPU_NOT_CONVERGED) return hst;
+    for (int p = 0; p < np; ++p) maxh = std::max(maxh, ith[p]);
+    sth = h->last_stats;
+    msh = h->last_ms;
+    o64.max_iters = o->refine_max_iters > maxh ? o->refine_max_iters - maxh : 1u;
+  }
   const int st = run_pg_batch(h, &o64, residuals, iters);
   if (st != BOGUS_GPU_OK && st != BOGUS_GPU_NOT_CONVERGED) return st;
   unsigned maxit = 0;
   for (int p = 0; p < np; ++p) {
-    if (iters) iters[p] += out32[p].iters;
+    if (iters) iters[p] += out32[p].iters + ith[p];
     maxit = std::max(maxit, out32[p].iters);
   }
-  h->last_stats.refine_iterations = h->last_stats.iterations;
-  h->last_stats.iterations += maxit;
+  h->last_stats.refine_iterations = h->last_stats.iterations + maxh;
+  h->last_stats.fp32_product_iterations = maxh;
+  h->last_stats.iterations += maxit + maxh;
+  h->last_stats.w_passes += sth.w_passes;
+  h->last_stats.algorithmic_bytes += sth.algorithmic_bytes;
+  h->last_stats.fp64_fma += sth.fp64_fma;
   h->last_stats.fp32_device_ms = ms32;
-  h->last_ms += ms32;
-  h->last_launches += 1;
+  h->last_ms += ms32 + msh;
+  h->last_launches += o->fp32_products_refresh ? 2 : 1;
   return st;
 }
 

@@ -82,12 +82,14 @@ struct PGArgsT {
   // FP32 part of the FP32-refined solves (0 elsewhere): stop once the residual has repeated bit for bit on this
   // many consecutive iterations, or the line search has run out of trials this many times in a row
   unsigned stall_iters;
-  // FP64 iterations with FP32 correction products (the k_pg_persistent<double, true, false, true> instantiation
-  // only): W v = W x_ref + W32 (v - x_ref)_32, with x_ref and W x_ref (FP64) refreshed at the first momentum
-  // step on or after every hy_refresh iterations. hy_ival: FP32 values in the interleaved layout (icol, slot0
-  // shared); hy_d: v - x_ref in FP32 for the position buffers 0, 1, 2 and 4 (4 * 3n floats, buffer 4 last)
+  // FP64 iterations with FP32 correction products (the HY instantiations of the FP64 kernels): W v = W x_ref +
+  // W32 (v - x_ref)_32, with x_ref and W x_ref (FP64) refreshed at the first momentum step on or after every
+  // hy_refresh iterations. hy_ival: FP32 values of W in the layout the kernel reads (interleaved: icol and slot0
+  // shared; plain: col); hy_d: v - x_ref in FP32 for the position buffers 0, 1, 2 and 4 (buffer 4 last), the
+  // buffers hy_stride floats apart (3 n of the whole problem or batch)
   const float* hy_ival;
   float* hy_d;
+  size_t hy_stride;
   double* hy_xref;
   double* hy_wxref;
   unsigned hy_refresh;

@@ -89,14 +89,20 @@ __device__ __forceinline__ ChunkScratchT<float>* hy_scratch<true>() {
   return s;
 }
 
-// W v for row 32c + lane as W x_ref + W32 (v - x_ref)_32, d = (v - x_ref)_32: FP32 chains over the FP32
-// interleaved copy of W in the chunk-segmented order, then added to the FP64 W x_ref.
-template <class T>
+// W v for row 32c + lane as W x_ref + W32 (v - x_ref)_32, d = (v - x_ref)_32: FP32 chains over the FP32 copy of
+// W (interleaved, or the plain BSR values of the batched solves) in the chunk-segmented order, then added to the
+// FP64 W x_ref.
+template <class T, bool IL>
 __device__ __forceinline__ void hy_product(const PGArgsT<T>& a, int c, const float* __restrict__ d,
                                            ChunkScratchT<float>& sh32, T* acc) {
-  const InterleavedBlocks<float> b32{a.icol, a.hy_ival, a.slot0};
   float acc32[3] = {0.f, 0.f, 0.f};
-  spmv_chunk<1, true>(a.rowptr, b32, a.n, c, sh32, [&](int j, float* x) { load3cg(d, j, x); }, acc32);
+  if constexpr (IL) {
+    const InterleavedBlocks<float> b32{a.icol, a.hy_ival, a.slot0};
+    spmv_chunk<1, true>(a.rowptr, b32, a.n, c, sh32, [&](int j, float* x) { load3cg(d, j, x); }, acc32);
+  } else {
+    const PlainBlocks<float> b32{a.col, a.hy_ival};
+    spmv_chunk<1, true>(a.rowptr, b32, a.n, c, sh32, [&](int j, float* x) { load3cg(d, j, x); }, acc32);
+  }
   const int i = 32 * c + (threadIdx.x & 31);
   if (i < a.n) {
     acc[0] = ldcg(a.hy_wxref + 3 * i) + (double)acc32[0];
@@ -137,7 +143,7 @@ __device__ __forceinline__ int pg_body_inl(const PGArgsT<T>& a, Ctx& ctx) {
   const int lane = threadIdx.x & 31;
   // HY: the FP32 correction v - x_ref of position buffer k (0, 1, 2 or 4), written beside every position that a
   // later product multiplies
-  auto hy_d = [&](int k) -> float* { return a.hy_d + (size_t)(k == 4 ? 3 : k) * 3 * (size_t)a.n; };
+  auto hy_d = [&](int k) -> float* { return a.hy_d + (size_t)(k == 4 ? 3 : k) * a.hy_stride; };
   auto store_corr = [&](int k, int i, const T* v) {
     if constexpr (HY) {
       T xr[3];
@@ -152,7 +158,7 @@ __device__ __forceinline__ int pg_body_inl(const PGArgsT<T>& a, Ctx& ctx) {
   // chunk-segmented order over the FP32 interleaved copy of W)
   auto product_k = [&](int c, int k, T* acc) {
     if constexpr (HY) {
-      hy_product(a, c, hy_d(k), hy_scratch<HY>()[threadIdx.x >> 5], acc);
+      hy_product<T, IL>(a, c, hy_d(k), hy_scratch<HY>()[threadIdx.x >> 5], acc);
     } else {
       product(c, B.X(k), acc);
     }
@@ -897,7 +903,7 @@ struct BlockCtx {
 
 // Batched solves: CTAs take problems from a queue (largest first); each runs the complete solve of its
 // problem with the same arithmetic as the single-problem kernel, then writes the best iterate to r.
-template <class T>
+template <class T, bool HY = false>
 __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgsT<T> ba) {
   __shared__ double smem8[32], sscal[8];
   __shared__ ChunkScratchT<T> cs[8];
@@ -934,8 +940,18 @@ __global__ void __launch_bounds__(256) k_pg_batched(PGBatchArgsT<T> ba) {
     a.csum = ba.base.csum + 4 * (size_t)ba.chunk_ptr[p];
     a.trace = nullptr;
     a.out = ba.base.out + p;
+    if constexpr (HY) {
+      a.hy_d = ba.base.hy_d + 3 * (size_t)c0;
+      a.hy_xref = ba.base.hy_xref + 3 * (size_t)c0;
+      a.hy_wxref = ba.base.hy_wxref + 3 * (size_t)c0;
+    }
     BlockCtx<T> ctx{a, smem8, sscal, cs};
-    const int best = pg_body<T, false>(a, ctx);
+    int best;
+    if constexpr (HY) {
+      best = pg_body_inl<T, false, false, true>(a, ctx);
+    } else {
+      best = pg_body<T, false>(a, ctx);
+    }
     __syncthreads();
     if (n == 0) continue;
     const T* src = best == 3 ? a.XB : (best == 4 ? a.Wv : (best == 0 ? a.X0 : (best == 1 ? a.X1 : a.X2)));
@@ -986,7 +1002,7 @@ struct TeamCtx {
   __device__ double scal(int q) const { return ldcg(sc + q); }
 };
 
-template <class T>
+template <class T, bool HY = false>
 __global__ void __launch_bounds__(256, 3) k_pg_team(PGBatchArgsT<T> ba, PGTeamArgs ta) {
   __shared__ double smem8[32];
   __shared__ ChunkScratchT<T> cs[8];
@@ -1033,8 +1049,18 @@ __global__ void __launch_bounds__(256, 3) k_pg_team(PGBatchArgsT<T> ba, PGTeamAr
     a.csum = ba.base.csum + 4 * (size_t)ba.chunk_ptr[p];
     a.trace = nullptr;
     a.out = ba.base.out + p;
+    if constexpr (HY) {
+      a.hy_d = ba.base.hy_d + 3 * (size_t)c0;
+      a.hy_xref = ba.base.hy_xref + 3 * (size_t)c0;
+      a.hy_wxref = ba.base.hy_wxref + 3 * (size_t)c0;
+    }
     TeamCtx<T> ctx{a, smem8, cs, cnt + 2, cnt + 4, ta.scal + 40 * (size_t)team, gb, rank};
-    const int best = pg_body<T, false>(a, ctx);
+    int best;
+    if constexpr (HY) {
+      best = pg_body_inl<T, false, false, true>(a, ctx);
+    } else {
+      best = pg_body<T, false>(a, ctx);
+    }
     if (best < 0) return;  // a wait ran out (status recorded)
     if (n == 0) continue;
     const T* src = best == 3 ? a.XB : (best == 4 ? a.Wv : (best == 0 ? a.X0 : (best == 1 ? a.X1 : a.X2)));
@@ -1044,12 +1070,32 @@ __global__ void __launch_bounds__(256, 3) k_pg_team(PGBatchArgsT<T> ba, PGTeamAr
   }
 }
 
+// Resident 256-thread CTAs per SM that both kernels reach (the FP64 batched kernels and their instantiations with
+// FP32 correction products share launch shapes).
+template <class K1, class K2>
+cudaError_t occupancy_min(int* per, K1 k1, K2 k2) {
+  int a = 0, b = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k1, 256, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k2, 256, 0);
+  *per = a < b ? a : b;
+  return e;
+}
+
 template <class T>
 cudaError_t launch_team_t(const PGBatchArgsT<T>& b, const PGTeamArgs& t, int grid, cudaStream_t s) {
   PGBatchArgsT<T> bc = b;
   PGTeamArgs tc = t;
   void* args[] = {&bc, &tc};
-  return cudaLaunchCooperativeKernel((const void*)k_pg_team<T>, dim3(grid), dim3(256), args, 0, s);
+  const void* fn = (const void*)k_pg_team<T>;
+  if constexpr (sizeof(T) == 8) {
+    if (b.base.hy_refresh) {
+      if (b.base.variant != 3 || b.base.lin_momentum || !b.base.hy_ival || !b.base.hy_d || !b.base.hy_xref ||
+          !b.base.hy_wxref)
+        return cudaErrorInvalidValue;
+      fn = (const void*)k_pg_team<T, true>;
+    }
+  }
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s);
 }
 
 cudaError_t launch_pg_team(const PGBatchArgs& b, const PGTeamArgs& t, int grid, cudaStream_t s) {
@@ -1064,7 +1110,7 @@ int pg_team_per_sm(int device, bool fp32) {
   int per = 0;
   (void)device;
   const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_team<float>, 256, 0)
-                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_team<double>, 256, 0);
+                             : occupancy_min(&per, k_pg_team<double>, k_pg_team<double, true>);
   return e == cudaSuccess ? per : 0;
 }
 
@@ -1072,7 +1118,7 @@ int pg_batched_per_sm(int device, bool fp32) {
   int per = 0;
   (void)device;
   const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_batched<float>, 256, 0)
-                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_batched<double>, 256, 0);
+                             : occupancy_min(&per, k_pg_batched<double>, k_pg_batched<double, true>);
   return e == cudaSuccess ? per : 0;
 }
 
@@ -1080,7 +1126,7 @@ int pg_team_grid(int device, bool fp32) {
   int sms = 0, per = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
   const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_team<float>, 256, 0)
-                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_team<double>, 256, 0);
+                             : occupancy_min(&per, k_pg_team<double>, k_pg_team<double, true>);
   if (e != cudaSuccess) return 0;
   const int cap = 3;
   if (per > cap) per = cap;
@@ -1088,7 +1134,14 @@ int pg_team_grid(int device, bool fp32) {
 }
 
 cudaError_t launch_pg_batched(const PGBatchArgs& b, int grid, cudaStream_t s) {
-  k_pg_batched<double><<<grid, 256, 0, s>>>(b);
+  if (b.base.hy_refresh) {
+    if (b.base.variant != 3 || b.base.lin_momentum || !b.base.hy_ival || !b.base.hy_d || !b.base.hy_xref ||
+        !b.base.hy_wxref)
+      return cudaErrorInvalidValue;
+    k_pg_batched<double, true><<<grid, 256, 0, s>>>(b);
+  } else {
+    k_pg_batched<double><<<grid, 256, 0, s>>>(b);
+  }
   return cudaGetLastError();
 }
 
@@ -1101,7 +1154,7 @@ int pg_batched_grid(int device, bool fp32) {
   int sms = 0, per = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
   const cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_batched<float>, 256, 0)
-                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pg_batched<double>, 256, 0);
+                             : occupancy_min(&per, k_pg_batched<double>, k_pg_batched<double, true>);
   if (e != cudaSuccess) return 0;
   return per * sms;
 }

@@ -7,7 +7,8 @@ The results are not the reference's iterates (the products are rounded different
 form (ProjectedGradient::hyRefresh), and without an FP32 part the GPU iterations equal it bit for bit; beyond
 that the tests check what the form promises: the returned residual is the oracle's FP64 error function at the
 returned iterate, below the tolerance; the solve repeats bit for bit; a stalled correction part hands over to
-the plain FP64 iterations; the forms it does not cover refuse it.
+the plain FP64 iterations; the batched forms stop each problem where its own solve stops; the forms it does
+not cover refuse it.
 """
 import numpy as np
 import pytest
@@ -135,14 +136,36 @@ def test_correction_products_refused_where_not_built(bg, c1):
         pg.setFp32CorrectionProducts(50)
         with pytest.raises(bg.BogusGpuError):
             D.solveWith(pg, np.zeros(3 * d.n))
+
+
+@pytest.mark.parametrize("sizes", [(16, 16, 300), (5, 1500, 3000)])  # one CTA per problem; teams of CTAs
+def test_batched_correction_products_match_single_problem_solves(bg, sizes):
+    """The batched forms (plain FP32 copy of W, one CTA or a team per problem) stop, refresh and round each
+    problem's correction products as its single-problem solve does (interleaved copy): bit for bit."""
     from bogus_gpu import generator
 
-    db, cptr = generator.batch(nproblems=4, nmin=16, nmax=64, seed=3)
-    B = bg.DualFrictionProblem()
-    B.computeFrom(bg.PrimalFrictionProblem.from_generated(db))
-    B.setBatch(cptr)
+    nproblems, nmin, nmax = sizes
+    d, cptr = generator.batch(nproblems=nproblems, nmin=nmin, nmax=nmax, seed=23)
+    D = bg.DualFrictionProblem()
+    D.computeFrom(bg.PrimalFrictionProblem.from_generated(d))
+    D.setBatch(cptr)
     pg = bg.ProjectedGradient()
-    pg.setMixedPrecision(True, 50)
-    pg.setFp32CorrectionProducts(50)
-    with pytest.raises(bg.BogusGpuError):
-        B.solveBatchWith(pg, np.zeros(3 * db.n))
+    pg.setTol(1e-9)
+    pg.setMaxIters(100)
+    pg.setMixedPrecision(True, 1500)
+    pg.setFp32CorrectionProducts(20)
+    r = np.zeros(3 * d.n)
+    res, its = D.solveBatchWith(pg, r, staticProblem=True)
+    rp, cl, vl = D.W_lower()
+    vl = vl.reshape(-1, 9)
+    single = bg.DualFrictionProblem()
+    for p in range(len(cptr) - 1):
+        c0, c1_ = cptr[p], cptr[p + 1]
+        single.set(rp[c0:c1_ + 1] - rp[c0], cl[rp[c0]:rp[c1_]] - c0, vl[rp[c0]:rp[c1_]].reshape(-1), d.b[c0:c1_],
+                   d.mu[c0:c1_])
+        rs = np.zeros(3 * (c1_ - c0))
+        res_s = single.solveWith(pg, rs)
+        st = single.solve_stats()
+        assert res[p] == res_s, p
+        assert np.array_equal(r[3 * c0:3 * c1_], rs), p
+        assert st["fp32_product_iterations"] > 0, p
