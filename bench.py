@@ -43,6 +43,7 @@ CPU_SAMPLE_ITERS = 1000   # the oracle's bounded sample: the first 1000 iteratio
 FP32_ITERS = 20000        # FP32-refined: FP32 iterations until the stall test ends them (at most this many),
                           # then FP64 ones to the tolerance
 HY_REFRESH = 50           # FP32 correction products in those FP64 iterations: x_ref refreshed this often
+BATCH_HY_REFRESH = 5      # the same in the 4096-problem batch (its 300 FP64 iterations leave no room for a floor)
 MAX_ADJ_FWD_ITERS = 20000
 METRIC = "time-to-residual 1e-6 (ms), FP64 APGD, 200k contacts"
 WORKLOAD = "fp64_apgd_200k_contacts_to_1e-6"
@@ -567,7 +568,7 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
     pgmh.setTol(TOL)
     pgmh.setMaxIters(200)
     pgmh.setMixedPrecision(True, BATCH_MAX_ITERS - 200)
-    pgmh.setFp32CorrectionProducts(HY_REFRESH)
+    pgmh.setFp32CorrectionProducts(BATCH_HY_REFRESH)
     solve(pgmh)
     mh_ms, (res_mh, its_mh) = _sync_time(lambda: solve(pgmh), world)
     # the launch shape chosen by the tuner (measured on this batch) against the default rule, same results
@@ -619,7 +620,7 @@ def measure_batch(args, sample_stride=16, rank=0, world=1, dev=0, steps=None):
                                                            "FP64 ones with the momentum product by linearity",
                                                   "batched_ms": ml_ms},
            "fp32_refined_fp32_products": {"split": "up to 200 FP32 + 300 FP64 iterations per problem, the FP64 ones "
-                                                   f"with FP32 correction products (x_ref refreshed every {HY_REFRESH})",
+                                                   f"with FP32 correction products (x_ref refreshed every {BATCH_HY_REFRESH})",
                                           "batched_ms": mh_ms},
            "timing": f"median of {steps} solves after a warm-up, wall time between device synchronisations"}
     if world > 1:

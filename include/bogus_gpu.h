@@ -89,7 +89,8 @@ typedef struct bogus_gpu_pg_options {
                                      Descent) its line search has run out of trials this many times in a row;
                                      the FP64 iterations then start from the best FP32 iterate. 0: the FP32 part
                                      runs to max_iters */
-  unsigned fp32_products_refresh; /* 0 (not in the reference; mixed_precision with APGD only). N > 0: the FP64
+  unsigned fp32_products_refresh; /* 0 (not in the reference; mixed_precision with APGD only; single-problem and
+                                     batched solves). N > 0: the FP64
                                      iterations after the FP32 part keep FP64 iterates, law and reductions but
                                      form their products as W x_ref + W32 (v - x_ref), the correction v - x_ref
                                      rounded to FP32 and multiplied by the FP32 copy of W, with x_ref and
