@@ -54,6 +54,9 @@ def lib():
     L.oracle_dual_solve_pg.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double, C.c_double,
                                        C.c_double, C.c_int, C.c_int, C.c_uint, _dp, C.POINTER(C.c_uint), CALLBACK,
                                        C.c_void_p]
+    L.oracle_dual_solve_pg_fp32.restype = C.c_double
+    L.oracle_dual_solve_pg_fp32.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_uint, C.c_double,
+                                            C.c_double, C.c_int, C.c_uint, _dp, C.POINTER(C.c_uint)]
     L.oracle_dual_coloring.restype = C.c_int
     L.oracle_dual_coloring.argtypes = [vp, _ip, _ip]
     L.oracle_dual_solve_cadoux_gs.restype = C.c_double
@@ -204,6 +207,16 @@ class DualProblem:
         res = lib().oracle_dual_solve_pg(self.h, variant, int(coulomb), tol, max_iters, ls_iters, optimistic,
                                          pessimistic, armijo, int(inf_norm), int(lin_momentum), int(hy_refresh), r,
                                          C.byref(it), cb, None)
+        return res, r, it.value
+
+    def solve_pg_fp32(self, r, apgd=True, coulomb=False, tol=1e-6, max_iters=300, ls_iters=8, optimistic=1.25,
+                      pessimistic=0.5, inf_norm=False, stall_iters=4):
+        """The FP32 part of the FP32-refined solve (not in the reference): returns (residual, best iterate widened
+        to double, iterations)."""
+        r = _f64(r).copy()
+        it = C.c_uint(0)
+        res = lib().oracle_dual_solve_pg_fp32(self.h, int(apgd), int(coulomb), tol, max_iters, ls_iters, optimistic,
+                                              pessimistic, int(inf_norm), int(stall_iters), r, C.byref(it))
         return res, r, it.value
 
     def solve_cadoux_gs(self, r, cadoux_iters, strategy=3, tol=1e-6, max_iters=250, eval_every=25, skip_tol=1e-6,

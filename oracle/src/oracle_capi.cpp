@@ -6,6 +6,7 @@
 #include <memory>
 #include <vector>
 
+#include "oracle_fp32.hpp"
 #include "oracle_math.hpp"
 #include "oracle_meche.hpp"
 #include "oracle_solvers.hpp"
@@ -132,6 +133,29 @@ double oracle_dual_solve_pg(void* h, int variant, int desaxce, double tol, unsig
   pg.callback = wrap(cb, user);
   Law law{desaxce != 0, RevHybrid, p->mu.data()};
   return pg.solve(law, p->b.data(), r, iters);
+}
+
+// The FP32 part of the FP32-refined solve (APGD when apgd, else Descent): r is rounded to float, solved in
+// single precision with the stall test, and the best iterate is written back widened to double.
+double oracle_dual_solve_pg_fp32(void* h, int apgd, int desaxce, double tol, unsigned maxIters, unsigned lsIters,
+                                 double optimistic, double pessimistic, int useInfinityNorm, unsigned stallIters,
+                                 double* r, unsigned* iters) {
+  auto* p = static_cast<DualProblem*>(h);
+  ProjectedGradient pg;
+  pg.setMatrix(p->full);
+  pg.tol = tol;
+  pg.maxIters = maxIters;
+  pg.lsIters = lsIters;
+  pg.lsOptimisticFactor = optimistic;
+  pg.lsPessimisticFactor = pessimistic;
+  pg.useInfinityNorm = useInfinityNorm != 0;
+  const size_t n3 = 3 * (size_t)p->full.n;
+  std::vector<float> x(n3);
+  for (size_t k = 0; k < n3; ++k) x[k] = (float)r[k];
+  const double res = fp32::solveAPGD32(pg, p->full, desaxce != 0, p->mu.data(), p->b.data(), x.data(), apgd != 0,
+                                       stallIters, iters);
+  for (size_t k = 0; k < n3; ++k) r[k] = (double)x[k];
+  return res;
 }
 
 // Greedy coloring of the stored lower triangle; returns the number of colors (perm: n, colors: ncolors+1).

@@ -83,6 +83,32 @@ def test_correction_products_bitwise_against_the_oracle(bg, oracle, c1, refresh,
     assert res == res_c and np.array_equal(r, r_c)
 
 
+@pytest.mark.parametrize("static", [True, False])
+def test_fp32_refined_pipeline_bitwise_against_the_oracle(bg, oracle, c1, static):
+    """The whole FP32-refined solve with correction products (FP32 part with its stall test, correction
+    iterations, plain FP64 check) against the oracle's restatements of the three parts, bit for bit."""
+    d, rp, cl, vl = c1
+    D = bg.DualFrictionProblem()
+    D.set(rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    tol, budget = 1e-10, 3000
+    pg = bg.ProjectedGradient()
+    pg.setTol(tol)
+    pg.setMaxIters(2000)
+    pg.setMixedPrecision(True, budget)
+    pg.setFp32CorrectionProducts(20)
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r, staticProblem=static)
+    st = D.solve_stats()
+    _, r32, k = O.solve_pg_fp32(np.zeros(3 * d.n), coulomb=not static, tol=tol, max_iters=2000, stall_iters=4)
+    assert k == st["iterations"] - st["refine_iterations"]
+    _, r_h, it_h = O.solve_pg(r32, variant=3, coulomb=not static, tol=tol, max_iters=budget, hy_refresh=20)
+    assert it_h == st["fp32_product_iterations"]
+    res_c, r_c, it_c = O.solve_pg(r_h, variant=3, coulomb=not static, tol=tol, max_iters=max(1, budget - it_h))
+    assert st["refine_iterations"] - it_h == it_c
+    assert res == res_c and np.array_equal(r, r_c)
+
+
 def test_stalled_corrections_hand_over_to_fp64(bg, oracle, c1):
     """A refresh interval too long for the tolerance: the correction part stops once its best residual has not
     improved by 1 % in 10 intervals, and the plain FP64 iterations go on from its best iterate."""

@@ -37,6 +37,31 @@ def _fp32_iterations(st):
     return st["iterations"] - st["refine_iterations"]
 
 
+@pytest.mark.parametrize("variant", [3, 1])  # APGD, Descent
+@pytest.mark.parametrize("static", [True, False])
+def test_fp32_refined_bitwise_against_the_oracle(bg, oracle, c1, variant, static):
+    """The FP32 part against the oracle's restatement of it (float W, iterates and law; double reductions and
+    step decisions; the stall test), then the FP64 part from its best iterate: iterates, residual and iteration
+    counts bit for bit."""
+    d, rp, cl, vl = c1
+    D = bg.DualFrictionProblem()
+    D.set(rp, cl, vl, d.b, d.mu)
+    O = oracle.DualProblem(rp, cl, vl, d.b, d.mu)
+    pg = bg.ProjectedGradient()
+    pg.setDefaultVariant(variant)
+    pg.setTol(1e-10)
+    pg.setMaxIters(3000)
+    pg.setMixedPrecision(True, 400)
+    r = np.zeros(3 * d.n)
+    res = D.solveWith(pg, r, staticProblem=static)
+    st = D.solve_stats()
+    _, r32, k = O.solve_pg_fp32(np.zeros(3 * d.n), apgd=variant == 3, coulomb=not static, tol=1e-10, max_iters=3000,
+                                stall_iters=4)
+    assert k == _fp32_iterations(st)
+    res_o, r_o, it_o = O.solve_pg(r32, variant=variant, coulomb=not static, tol=1e-10, max_iters=400)
+    assert it_o == st["refine_iterations"] and res == res_o and np.array_equal(r, r_o)
+
+
 @pytest.mark.parametrize("static", [True, False])
 def test_stall_ends_the_fp32_part_like_a_budget(bg, oracle, c1, static):
     d, rp, cl, vl = c1
